@@ -1,0 +1,186 @@
+/*
+ * vacgpu.h - C ABI of the GB300 TVDLF/Hancock engine for VAC 4.52.
+ *
+ * The library replaces the explicit time step of VAC's `program vac`
+ * (src/vac.t:55-106): the dt selection (getdt_courant, src/vac.t:664-722),
+ * the split twostep advance (advance/advance_expl/advect/advect1,
+ * src/vac.t:223-572) with the Hancock predictor and TVDLF corrector
+ * (src/vactvdlf.t:5-367), the ghost-cell fill (getboundary,
+ * src/vacgrid.t:195-413) and the Powell/user source terms
+ * (addsource2, src/vac.t:575-605).
+ *
+ * All entry points are plain C: POD arguments, host pointers, an int status
+ * (0 = success, nonzero = error; the message is kept per thread and read with
+ * vacgpu_last_error).  A nonzero status is where the Fortran host calls
+ * die(message) (src/vacio.t:1108-1116).
+ *
+ * Arrays cross the boundary in VAC's own layout: column-major, ix1 fastest,
+ * one contiguous block per variable, mesh cells only (ixM, no ghost layers),
+ * exactly as readfileini_bin reads them (src/vacio.t:682-755) and
+ * savefileout_bin writes them (src/vacio.t:1008-1047).  The library owns its
+ * device copies; host arrays are never retained after a call returns.
+ *
+ * Threading: a handle is used by one host thread at a time (VAC itself is
+ * single threaded, COMMON-block state, src/vacdef.t:78-175).  Distinct
+ * handles are independent.
+ */
+#ifndef VACGPU_H
+#define VACGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VACGPU_MAXNW 8      /* 3-D ideal MHD: rho, m1..m3, e, b1..b3          */
+#define VACGPU_MAXB 6       /* 2*ndim default boundary regions (boundsetup)   */
+#define VACGPU_MAXEQPAR 4
+#define VACGPU_MAXSRCPAR 8
+
+/* physics module (setvac -p=..., src/setvac:5-17) */
+enum { VACGPU_PHYS_HD = 0, VACGPU_PHYS_MHD = 1 };
+
+/* typelimiter(iw) (dwlimiter2, src/vacgrid.t:938-996) */
+enum {
+  VACGPU_LIM_MINMOD = 0,
+  VACGPU_LIM_WOODWARD = 1,
+  VACGPU_LIM_SUPERBEE = 2,
+  VACGPU_LIM_VANLEER = 3,
+  VACGPU_LIM_ALBADA = 4
+};
+
+/* typeB(iw,iB) (getboundary, src/vacgrid.t:195-413) */
+enum {
+  VACGPU_BC_CONT = 0,
+  VACGPU_BC_PERIODIC = 1,
+  VACGPU_BC_SYMM = 2,
+  VACGPU_BC_ASYMM = 3
+};
+
+/* typefull1 (src/vactvdlf.t:92-299): second order 'tvdlf' or 'tvdlf1' */
+enum { VACGPU_TVDLF = 0, VACGPU_TVDLF1 = 1 };
+
+/* typelimited (src/vactvdlf.t:150-162) */
+enum {
+  VACGPU_LIMITED_ORIGINAL = 0,
+  VACGPU_LIMITED_PREVIOUS = 1,
+  VACGPU_LIMITED_PREDICTOR = 2
+};
+
+/* typedimsplit (src/vac.t:310-324) */
+enum { VACGPU_SPLIT_XYYX = 0, VACGPU_SPLIT_XY = 1 };
+
+/* Arithmetic of the device state.
+ * FP64: every operation in IEEE double, in the reference's operation order
+ *       (no FMA contraction), bit-compatible with the FP64 oracle.
+ * MIXED: state and fluxes in FP32; the thermal/total pressure recovery
+ *       p=(g-1)(e-m^2/2rho-B^2/2), the conservation sums and t+=dt in FP64. */
+enum { VACGPU_PREC_FP64 = 0, VACGPU_PREC_MIXED = 1 };
+
+/* device source hooks standing in for specialsource/getdt_special
+ * (src/vacnul.specialsource.t:9-71) */
+enum {
+  VACGPU_SRC_NONE = 0,
+  /* uniform gravity, vacusr.gravity.t:24-75: dm_i/dt += rho*g_i,
+   * de/dt += sum_i g_i*m_i; params = g_1..g_ndim */
+  VACGPU_SRC_GRAVITY = 1
+};
+
+/* Run parameters: the par/DEFAULT + par/PROBLEM namelist values the path
+ * reads (readparameters, src/vacio.t:5-531; par/DEFAULT:1-86) after VAC's
+ * derived defaults are applied (typepred1='hancock' for tvdlf, dimsplit and
+ * sourcesplit harmonisation, typelimited='previous' when unsplit). */
+typedef struct vacgpu_params {
+  int ndim;                     /* 1..3                                     */
+  int ndir;                     /* ndim..3 vector components                */
+  int physics;                  /* VACGPU_PHYS_*                            */
+  int nw;                       /* HD: 2+ndir, MHD: 2+2*ndir                */
+  int nx[3];                    /* mesh cells per dimension (ixM extent)    */
+  int dixB;                     /* ghost layers; must be 2 (src/vacdef.t:24)*/
+  double eqpar[VACGPU_MAXEQPAR];/* eqpar(gamma_)[, eqpar(eta_)]             */
+  int typefull;                 /* VACGPU_TVDLF / VACGPU_TVDLF1             */
+  int typelimiter[VACGPU_MAXNW];/* VACGPU_LIM_* per variable                */
+  int typelimited;              /* VACGPU_LIMITED_*                         */
+  int dimsplit;                 /* 1 = dimensional splitting                */
+  int typedimsplit;             /* VACGPU_SPLIT_*                           */
+  int divbfix;                  /* Powell source (MHD only)                 */
+  int sourceunsplit;            /* sources inside predictor/corrector       */
+  double courantpar;            /* CFL number                               */
+  double dtpar;                 /* >0: fixed dt                             */
+  double smallpcoeff;           /* smallp = min(p)*smallpcoeff at 1st call  */
+  double smallp;                /* <0: computed as in getpthermal           */
+  int slowsteps;
+  int dtcantgrow;
+  int tmaxexact;
+  int itmax;
+  double tmax;
+  double dtmin;
+  int typeB[VACGPU_MAXB][VACGPU_MAXNW]; /* [iB][iw]; iB = 2*(idim-1)+upper */
+  int precision;                /* VACGPU_PREC_*                            */
+} vacgpu_params;
+
+typedef struct vacgpu_handle vacgpu_handle;
+
+/* Fill *p with par/DEFAULT values for the given configuration
+ * (par/DEFAULT:1-86 plus the readparameters defaults src/vacio.t:55-118:
+ * typefull='tvdlf', typelimiter='minmod', typeB='cont'). */
+void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
+                           const int* nx);
+
+/* Validate parameters, allocate device state for one grid.
+ * Replaces readparameters + boundsetup + startup (src/vacio.t:5-531,
+ * src/vacgrid.t:9-160, src/vac.t:160-220). */
+int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out);
+
+/* Mesh coordinates x(ixM^S,1:ndim) as read from the .ini file.
+ * Replaces gridsetup1 (src/vacgrid.t:457-593): ghost coordinates are
+ * extrapolated linearly, dx=(x_{i+1}-x_{i-1})/2, dvolume, volume.
+ * The grid must be a Cartesian product grid (x_d depends on ix_d only). */
+int vacgpu_set_grid(vacgpu_handle* h, const double* x);
+
+/* Initial state w(ixM^S,1:nw) with its it and t (readfileini_bin,
+ * src/vacio.t:682-755); ghost cells are filled as by the getboundary call
+ * before the time loop (src/vac.t:54). */
+int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t);
+
+/* Current state w(ixM^S,1:nw) (what savefileout_bin writes,
+ * src/vacio.t:1008-1047). */
+int vacgpu_download(vacgpu_handle* h, double* w);
+
+/* Advance: repeat the body of the time loop (src/vac.t:59-106) at most
+ * maxsteps times.  Before each step the dt is chosen exactly as VAC does
+ * (dtpar / getdt_courant / getdt_special / dtcantgrow / slowsteps /
+ * tmaxexact) and the step is skipped and the call returns when
+ * timetofinish (src/vac.t:608-628) holds or t >= tstop (the next save time
+ * of the caller's timetosave).  dt, it and t stay on the device between
+ * steps; *t, *it, *dt receive their values at return, *finished is set to 1
+ * when timetofinish held. */
+int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
+                int* it, double* dt, int* finished);
+
+/* Volume-averaged variables wmean(iw) = sum(dvolume*w)/volume over the mesh
+ * in FP64 (savefilelog_default, src/vacio.t:1050-1105). */
+int vacgpu_sums(vacgpu_handle* h, double* wmean);
+
+/* Error counters nerror(1:4) (src/vacdef.t:54-55): toosmallp, toosmallr,
+ * couranterr, poissonerr. */
+int vacgpu_error_counts(vacgpu_handle* h, int* nerror);
+
+/* Install a device source hook (specialsource + getdt_special,
+ * src/vacnul.specialsource.t:9-71); VACGPU_SRC_NONE removes it. */
+int vacgpu_register_source(vacgpu_handle* h, int source_id,
+                           const double* params, int nparams);
+
+/* Release the handle and its device memory. */
+void vacgpu_destroy(vacgpu_handle* h);
+
+/* Copy the calling thread's last error message into buf (NUL terminated);
+ * returns its full length. */
+int vacgpu_last_error(char* buf, int len);
+
+/* Library version string. */
+const char* vacgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VACGPU_H */

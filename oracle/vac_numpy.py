@@ -1,0 +1,409 @@
+"""Second, independent restatement of VAC's explicit TVDLF/Hancock step in
+NumPy whole-array form.  TEST INFRASTRUCTURE ONLY.
+
+Each Fortran array statement of the reference becomes one NumPy slice
+expression over the same index range, evaluated in the same left-to-right
+order (IEEE double elementwise, no contraction), so it must agree bit for bit
+with the C restatement in ``vac_oracle.c``; ``tests/test_oracle.py`` checks
+that.  Only small grids are meant to run through it.
+
+Arrays carry ghost cells: shape (nw, nG1, nG2, nG3) with nG=nx+4 in a used
+dimension and 1 otherwise; the mesh is [2, nG-3].
+"""
+import numpy as np
+
+from vac_gb300 import abi
+
+HALF, ONE, TWO, ZERO = 0.5, 1.0, 2.0, 0.0
+SMALLDOUBLE, BIGDOUBLE = 1.0e-99, 1.0e99
+
+
+class Box:
+    def __init__(self, lo, hi):
+        self.lo, self.hi = list(lo), list(hi)
+
+    def sl(self, d=None, s=0):
+        out = []
+        for k in range(3):
+            a, b = self.lo[k], self.hi[k]
+            if k == d:
+                a, b = a + s, b + s
+            out.append(slice(a, b + 1))
+        return tuple(out)
+
+    def shifted(self, d, s):
+        b = Box(self.lo, self.hi)
+        b.lo[d] += s
+        b.hi[d] += s
+        return b
+
+
+class NumpyVac:
+    def __init__(self, p, x, w, it=0, t=0.0):
+        self.p = p
+        self.ndim, self.ndir, self.nw = p.ndim, p.ndir, p.nw
+        self.mhd = p.physics == abi.PHYS_MHD
+        self.gamma = p.eqpar[0]
+        self.e_ = 1 + self.ndir
+        self.b0 = self.e_
+        self.nG = [p.nx[d] + 4 if d < self.ndim else 1 for d in range(3)]
+        self.ixG = Box([0, 0, 0], [n - 1 for n in self.nG])
+        self.ixM = Box([2 if d < self.ndim else 0 for d in range(3)],
+                       [self.nG[d] - 3 if d < self.ndim else 0 for d in range(3)])
+        self.smallp = p.smallp
+        self.courantpar = p.courantpar
+        self.dtpar = p.dtpar
+        if self.dtpar > 0 and p.slowsteps != 1:
+            self.courantpar = -1.0
+        self.dtcourant = [BIGDOUBLE] * 3
+        self.nerror = [0] * 4
+        self.dt = 0.0
+        self.dtold = 0.0
+        self._grid(np.asarray(x, dtype=np.float64))
+        self.w = np.zeros([self.nw] + self.nG)
+        self.w[(slice(None),) + self.ixM.sl()] = np.asarray(w).reshape(
+            [self.nw] + [p.nx[d] if d < self.ndim else 1 for d in range(3)])
+        self.it, self.itmin, self.t = it, it, t
+        self.getboundary(self.w)
+
+    # ------------------------------------------------------------- grid
+    def _grid(self, xm):
+        """gridsetup1, src/vacgrid.t:457-593."""
+        nd = self.ndim
+        nQ = [self.nG[d] + 2 if d < nd else 1 for d in range(3)]
+        q0 = [1 if d < nd else 0 for d in range(3)]
+        qx = np.zeros([nd] + nQ)
+        msl = tuple(slice(self.ixM.lo[d] + q0[d], self.ixM.hi[d] + q0[d] + 1)
+                    for d in range(3))
+        qx[(slice(None),) + msl] = xm.reshape([nd] + [self.p.nx[d] if d < nd else 1
+                                                      for d in range(3)])
+        for idim in range(nd):
+            for upper in (True, False):
+                if upper:
+                    lo, hi = self.ixM.hi[idim] + 1 + q0[idim], nQ[idim] - 1
+                    ixe, ixf = lo - 1, lo - 2
+                else:
+                    lo, hi = 0, self.ixM.lo[idim] - 1 + q0[idim]
+                    ixe, ixf = hi + 1, hi + 2
+                for jd in range(nd):
+                    for ix in range(lo, hi + 1):
+                        c = abs(ixe - ix)
+                        a = [slice(None)] * 3
+                        e = [slice(None)] * 3
+                        f = [slice(None)] * 3
+                        a[idim], e[idim], f[idim] = ix, ixe, ixf
+                        qx[(jd,) + tuple(a)] = ((1 + c) * qx[(jd,) + tuple(e)]
+                                                - c * qx[(jd,) + tuple(f)])
+        gsl = tuple(slice(q0[d], q0[d] + self.nG[d]) for d in range(3))
+        self.dx = np.zeros([3] + self.nG)
+        for idim in range(nd):
+            j = list(gsl)
+            h = list(gsl)
+            j[idim] = slice(gsl[idim].start + 1, gsl[idim].stop + 1)
+            h[idim] = slice(gsl[idim].start - 1, gsl[idim].stop - 1)
+            self.dx[idim] = HALF * (qx[(idim,) + tuple(j)] - qx[(idim,) + tuple(h)])
+        dv = self.dx[0].copy()
+        for idim in range(1, nd):
+            dv = dv * self.dx[idim]
+        self.dvolume = dv
+        acc = 0.0
+        for v in self.dvolume[self.ixM.sl()].ravel(order="F"):
+            acc = acc + v
+        self.volume = acc
+
+    # ------------------------------------------------------------ physics
+    def sq_sum(self, w, i0, sl):
+        acc = w[(i0 + 1,) + sl] * w[(i0 + 1,) + sl]
+        for c in range(2, self.ndir + 1):
+            acc = acc + w[(i0 + c,) + sl] * w[(i0 + c,) + sl]
+        return acc
+
+    def getptotal(self, w, b):
+        sl = b.sl()
+        g = self.gamma
+        p = (ONE - HALF * g) * self.sq_sum(w, self.b0, sl)
+        p = p + (g - ONE) * w[(self.e_,) + sl]
+        p = p - HALF * (g - ONE) * self.sq_sum(w, 0, sl) / w[(0,) + sl]
+        return p
+
+    def getpthermal(self, w, b, clipping=True):
+        sl = b.sl()
+        g = self.gamma
+        if self.mhd:
+            p = self.sq_sum(w, 0, sl) / w[(0,) + sl]
+            for c in range(1, self.ndir + 1):
+                bc = w[(self.b0 + c,) + sl]
+                p = p + bc * bc
+            p = (g - 1) * (w[(self.e_,) + sl] - HALF * p)
+        else:
+            p = (g - 1) * (w[(self.e_,) + sl] - HALF * self.sq_sum(w, 0, sl) / w[(0,) + sl])
+        if self.smallp < ZERO:
+            self.smallp = p.min() * self.p.smallpcoeff
+            if self.mhd and self.smallp < ZERO:
+                self.smallp = p.max() * self.p.smallpcoeff
+        if clipping:
+            p = np.where(p >= self.smallp, p, self.smallp)
+        return p
+
+    def getcmax(self, w, b, idim, cache):
+        sl = b.sl()
+        rho = w[(0,) + sl]
+        m = w[(1 + idim,) + sl]
+        if self.mhd:
+            if "cs2" not in cache:
+                cs2 = self.gamma * self.getpthermal(w, b) / rho
+                cache["cs2"] = cs2
+                cache["cf2"] = self.sq_sum(w, self.b0, sl) / rho + cs2
+            cs2, cf2 = cache["cs2"], cache["cf2"]
+            bi = w[(self.b0 + 1 + idim,) + sl]
+            return (np.sqrt(HALF * (cf2 + np.sqrt(cf2 * cf2 - 4 * cs2 * (bi * bi) / rho)))
+                    + np.abs(m / rho))
+        if "cs" not in cache:
+            cache["cs"] = np.sqrt(self.gamma * self.getpthermal(w, b) / rho)
+        return cache["cs"] + np.abs(m / rho)
+
+    def getflux(self, w, b, iw, idim):
+        sl = b.sl()
+        rho = w[(0,) + sl]
+        nd = self.ndir
+        if self.mhd:
+            if iw == 0:
+                return np.zeros_like(rho), True
+            if 1 <= iw <= nd:
+                bk = w[(self.b0 + iw,) + sl]
+                bi = w[(self.b0 + 1 + idim,) + sl]
+                if iw == idim + 1:
+                    return self.getptotal(w, b) - bk * bi, True
+                return -bk * bi, True
+            if iw == self.e_:
+                pt = self.getptotal(w, b)
+                bm = w[(self.b0 + 1,) + sl] * w[(1,) + sl]
+                for c in range(2, nd + 1):
+                    bm = bm + w[(self.b0 + c,) + sl] * w[(c,) + sl]
+                return (w[(1 + idim,) + sl] * pt - w[(self.b0 + 1 + idim,) + sl] * bm) / rho, True
+            k = iw - self.b0
+            if k == idim + 1:
+                return np.zeros_like(rho), False
+            return -w[(k,) + sl] / rho * w[(self.b0 + 1 + idim,) + sl], True
+        if iw == 1 + idim:
+            return self.getpthermal(w, b), True
+        if iw == self.e_:
+            return w[(1 + idim,) + sl] / rho * self.getpthermal(w, b), True
+        return np.zeros_like(rho), True
+
+    # ------------------------------------------------------------ limiter
+    def dwlimiter2(self, dwC, ixC, iw, idim):
+        ixO = Box(ixC.lo, ixC.hi)
+        ixO.lo[idim] += 1
+        a = dwC[ixO.sl()]
+        bb = dwC[ixO.sl(idim, -1)]
+        s = np.copysign(ONE, a)
+        lim = self.p.typelimiter[iw]
+        if lim == abi.LIM_MINMOD:
+            r = s * np.maximum(ZERO, np.minimum(np.abs(a), s * bb))
+        elif lim == abi.LIM_WOODWARD:
+            r = 2 * s * np.maximum(ZERO, np.minimum(np.minimum(np.abs(a), s * bb),
+                                                    s * 0.25 * (bb + a)))
+        elif lim == abi.LIM_SUPERBEE:
+            r = s * np.maximum(np.maximum(ZERO, np.minimum(2 * np.abs(a), s * bb)),
+                               np.minimum(np.abs(a), 2 * s * bb))
+        elif lim == abi.LIM_VANLEER:
+            r = 2 * np.maximum(bb * a, 0.0) / (a + bb + 1.0e-12)
+        else:
+            r = (bb * (a * a + 1.0e-12) + a * (bb * bb + 1.0e-12)) / (a * a + bb * bb + 2.0e-12)
+        ldw = np.zeros(self.nG)
+        ldw[ixO.sl()] = r
+        return ldw
+
+    def upwindLR(self, ixL, ixR, idim, w, wLC, wRC):
+        ixC = Box(ixL.lo, ixR.shifted(idim, 1).hi)
+        ixC.lo[idim] = ixL.lo[idim] - 1
+        for iw in range(self.nw):
+            dwC = np.zeros(self.nG)
+            dwC[ixC.sl()] = w[(iw,) + ixC.sl(idim, 1)] - w[(iw,) + ixC.sl()]
+            ldw = self.dwlimiter2(dwC, ixC, iw, idim)
+            wRC[(iw,) + ixR.sl()] = wRC[(iw,) + ixR.sl()] - HALF * ldw[ixR.sl(idim, 1)]
+            wLC[(iw,) + ixL.sl()] = wLC[(iw,) + ixL.sl()] + HALF * ldw[ixL.sl()]
+
+    # ------------------------------------------------------- grid helpers
+    def addflux(self, qdt, ixO, iw, idim, fR, ixR, fL, ixL, wnew):
+        wnew[(iw,) + ixO.sl()] = (wnew[(iw,) + ixO.sl()]
+                                  - qdt / self.dx[(idim,) + ixO.sl()]
+                                  * (fR[ixR.sl()] - fL[ixL.sl()]))
+
+    def addsource2(self, qdt, ixO, wCT, wnew):
+        sl = ixO.sl()
+        if getattr(self, "src_id", 0) == abi.SRC_GRAVITY:
+            for iw in range(self.nw):
+                if 1 <= iw <= self.ndim:
+                    g = self.src_par[iw - 1]
+                    if abs(g) > SMALLDOUBLE:
+                        wnew[(iw,) + sl] = wnew[(iw,) + sl] + qdt * g * wCT[(0,) + sl]
+                elif iw == self.e_:
+                    for d in range(1, self.ndim + 1):
+                        g = self.src_par[d - 1]
+                        if abs(g) > SMALLDOUBLE:
+                            wnew[(iw,) + sl] = wnew[(iw,) + sl] + qdt * g * wCT[(d,) + sl]
+        if self.mhd and self.p.divbfix:
+            divb = np.zeros(self.nG)[sl]
+            for idim in range(self.ndim):
+                q = wCT[self.b0 + 1 + idim]
+                g = HALF * (q[ixO.sl(idim, 1)] - q[ixO.sl(idim, -1)]) / self.dx[(idim,) + sl]
+                divb = divb + g
+            divb = qdt * divb
+            rho = wCT[(0,) + sl]
+            for iw in range(self.nw):
+                if 1 <= iw <= self.ndir:
+                    wnew[(iw,) + sl] = wnew[(iw,) + sl] - wCT[(self.b0 + iw,) + sl] * divb
+                elif self.b0 < iw <= self.b0 + self.ndir:
+                    wnew[(iw,) + sl] = (wnew[(iw,) + sl]
+                                        - wCT[(iw - self.b0,) + sl] / rho * divb)
+                elif iw == self.e_:
+                    mb = wCT[(1,) + sl] * wCT[(self.b0 + 1,) + sl]
+                    for c in range(2, self.ndir + 1):
+                        mb = mb + wCT[(c,) + sl] * wCT[(self.b0 + c,) + sl]
+                    wnew[(iw,) + sl] = wnew[(iw,) + sl] - mb / rho * divb
+
+    def getboundary(self, w):
+        for iB in range(2 * self.ndim):
+            idim, upper = iB // 2, iB % 2
+            r = Box(self.ixG.lo, self.ixG.hi)
+            if upper:
+                r.lo[idim] = self.ixM.hi[idim] + 1
+            else:
+                r.hi[idim] = self.ixM.lo[idim] - 1
+            for iw in range(self.nw):
+                typ = self.p.typeB[iB][iw]
+                if typ == abi.BC_PERIODIC:
+                    n = self.nG[idim] - 4
+                    w[(iw,) + r.sl()] = w[(iw,) + r.sl(idim, -n if upper else n)]
+                    continue
+                for k in range(r.lo[idim], r.hi[idim] + 1):
+                    row = Box(r.lo, r.hi)
+                    row.lo[idim] = row.hi[idim] = k
+                    if typ == abi.BC_CONT:
+                        ixe = r.lo[idim] - 1 if upper else r.hi[idim] + 1
+                    else:
+                        ixe = (2 * r.lo[idim] - 1 if upper else 2 * r.hi[idim] + 1) - k
+                    w[(iw,) + row.sl()] = w[(iw,) + row.sl(idim, ixe - k)]
+                if typ == abi.BC_ASYMM:
+                    w[(iw,) + r.sl()] = -w[(iw,) + r.sl()]
+
+    # ------------------------------------------------------------ schemes
+    def hancock(self, qdt, ixO, d0, d1, wCT, wnew):
+        for idim in range(d0, d1 + 1):
+            hxO = ixO.shifted(idim, -1)
+            wLC = np.zeros_like(wCT)
+            wRC = np.zeros_like(wCT)
+            wRC[(slice(None),) + hxO.sl()] = wCT[(slice(None),) + ixO.sl()]
+            wLC[(slice(None),) + ixO.sl()] = wCT[(slice(None),) + ixO.sl()]
+            self.upwindLR(ixO, hxO, idim, wCT, wLC, wRC)
+            vR = np.zeros(self.nG)
+            vL = np.zeros(self.nG)
+            vR[hxO.sl()] = wRC[(1 + idim,) + hxO.sl()] / wRC[(0,) + hxO.sl()]
+            vL[ixO.sl()] = wLC[(1 + idim,) + ixO.sl()] / wLC[(0,) + ixO.sl()]
+            for iw in range(self.nw):
+                fR = np.zeros(self.nG)
+                fL = np.zeros(self.nG)
+                fR[hxO.sl()], tr = self.getflux(wRC, hxO, iw, idim)
+                fL[ixO.sl()], tr = self.getflux(wLC, ixO, iw, idim)
+                if tr:
+                    fR[hxO.sl()] = fR[hxO.sl()] + vR[hxO.sl()] * wRC[(iw,) + hxO.sl()]
+                    fL[ixO.sl()] = fL[ixO.sl()] + vL[ixO.sl()] * wLC[(iw,) + ixO.sl()]
+                self.addflux(qdt, ixO, iw, idim, fL, ixO, fR, hxO, wnew)
+        if self.p.sourceunsplit:
+            self.addsource2(qdt * (d1 - d0 + ONE) / self.ndim, ixO, wCT, wnew)
+
+    def tvdmusclf(self, qdt, ixO, d0, d1, wCT, wnew):
+        for idim in range(d0, d1 + 1):
+            hxO = ixO.shifted(idim, -1)
+            ixC = Box(ixO.lo, ixO.hi)
+            ixC.lo[idim] = hxO.lo[idim]
+            wLC = np.zeros_like(wCT)
+            wRC = np.zeros_like(wCT)
+            wRC[(slice(None),) + ixC.sl()] = wCT[(slice(None),) + ixC.sl(idim, 1)]
+            wLC[(slice(None),) + ixC.sl()] = wCT[(slice(None),) + ixC.sl()]
+            if self.p.typefull != abi.TVDLF1:
+                base = {abi.LIMITED_PREVIOUS: self.wold,
+                        abi.LIMITED_PREDICTOR: wCT}.get(self.p.typelimited, wnew)
+                self.upwindLR(ixC, ixC, idim, base, wLC, wRC)
+            A = (slice(None),) + ixC.sl()
+            wLC[A] = HALF * (wLC[A] + wRC[A])
+            cmax = np.zeros(self.nG)
+            cmax[ixC.sl()] = self.getcmax(wLC, ixC, idim, {})
+            if self.courantpar > ZERO and self.istep == 2:
+                q = cmax[ixC.sl()] * TWO / (self.dx[(idim,) + ixC.sl()]
+                                            + self.dx[(idim,) + ixC.sl(idim, 1)])
+                cm = q.max()
+                if qdt * cm > ONE:
+                    self.nerror[2] += 1
+                if cm > SMALLDOUBLE:
+                    self.dtcourant[idim] = min(self.dtcourant[idim], self.courantpar / cm)
+            wLC[A] = 2 * wLC[A] - wRC[A]
+            vL = wLC[(1 + idim,) + ixC.sl()] / wLC[(0,) + ixC.sl()]
+            vR = wRC[(1 + idim,) + ixC.sl()] / wRC[(0,) + ixC.sl()]
+            for iw in range(self.nw):
+                fL, tr = self.getflux(wLC, ixC, iw, idim)
+                fR, tr = self.getflux(wRC, ixC, iw, idim)
+                if tr:
+                    fL = fL + vL * wLC[(iw,) + ixC.sl()]
+                    fR = fR + vR * wRC[(iw,) + ixC.sl()]
+                fL = HALF * (fL + fR)
+                fR = -cmax[ixC.sl()] * HALF * (wRC[(iw,) + ixC.sl()] - wLC[(iw,) + ixC.sl()])
+                fL = fL + fR
+                F = np.zeros(self.nG)
+                F[ixC.sl()] = fL
+                self.addflux(qdt, ixO, iw, idim, F, ixO, F, hxO, wnew)
+        if self.p.sourceunsplit:
+            self.addsource2(qdt * (d1 - d0 + ONE) / self.ndim, ixO, wCT, wnew)
+
+    def advect(self, d0, d1):
+        w1 = self.w.copy()
+        self.istep = 1
+        self.hancock(self.dt / 2, self.ixM, d0, d1, self.w, w1)
+        self.getboundary(w1)
+        self.istep = 2
+        self.tvdmusclf(self.dt, self.ixM, d0, d1, w1, self.w)
+        self.getboundary(self.w)
+
+    def getdt_courant(self):
+        self.dt = BIGDOUBLE
+        cm = ZERO
+        cache = {}
+        for idim in range(self.ndim):
+            if self.dtcourant[idim] < BIGDOUBLE:
+                self.dt = min(self.dt, self.dtcourant[idim])
+            else:
+                c = self.getcmax(self.w, self.ixM, idim, cache)
+                cm = max(cm, (c / self.dx[(idim,) + self.ixM.sl()]).max())
+        self.dtcourant = [BIGDOUBLE] * 3
+        if cm > SMALLDOUBLE:
+            self.dt = min(self.dt, self.courantpar / cm)
+
+    def step(self, nsteps):
+        for _ in range(nsteps):
+            if self.dtpar > ZERO:
+                self.dt = self.dtpar
+            elif self.courantpar > ZERO:
+                self.getdt_courant()
+            p = self.p
+            if self.it >= p.itmax or self.t >= p.tmax or self.dt < p.dtmin:
+                return True
+            if p.tmaxexact:
+                self.dt = min(self.dt, p.tmax - self.t + SMALLDOUBLE)
+            self.wold = self.w.copy()
+            if p.dimsplit:
+                order = (range(self.ndim) if (self.it // 2) * 2 == self.it
+                         or p.typedimsplit == abi.SPLIT_XY
+                         else range(self.ndim - 1, -1, -1))
+                for d in order:
+                    self.advect(d, d)
+            else:
+                self.advect(0, self.ndim - 1)
+            self.it += 1
+            self.t = self.t + self.dt
+        return False
+
+    def state(self):
+        return self.w[(slice(None),) + self.ixM.sl()].reshape(
+            [self.nw] + [self.p.nx[d] for d in range(self.ndim)])

@@ -1,0 +1,946 @@
+/*
+ * vac_oracle.c - CPU FP64 restatement of VAC 4.52's explicit TVDLF/Hancock
+ * time step.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and
+ * the CPU-baseline leg of the benchmark use it as the checker.  Nothing in the
+ * product links it.
+ *
+ * PARITY STATUS: unpinned.  The reference is Fortran 90 and no Fortran
+ * compiler exists where this project builds or runs, and the reference ships
+ * no golden vectors or fixtures.  This file therefore restates the
+ * reference's algorithm statement by statement from its sources (file:line
+ * cited at every routine), keeping each Fortran array statement as one loop
+ * over the same index range with the same expression shape, so that each
+ * element sees the same IEEE operations in the same order.  It is
+ * cross-checked bit for bit against an independent NumPy whole-array
+ * restatement (oracle/vac_numpy.py) on committed fixtures.
+ *
+ * Build with -O2 -ffp-contract=off (no FMA contraction), no -ffast-math.
+ *
+ * Layout: like VAC, w(ixG1,ixG2,ixG3,nw) column-major with ix1 fastest and
+ * dixB=2 ghost layers in every used dimension; indices here are 0-based, the
+ * mesh is [2, nG-3] in a used dimension.  Unused dimensions have extent 1.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/vacgpu.h"
+
+#define ZERO 0.0
+#define ONE 1.0
+#define TWO 2.0
+#define HALF 0.5
+#define SMALLDOUBLE 1.0e-99
+#define BIGDOUBLE 1.0e+99
+
+typedef struct {
+  int lo[3], hi[3];
+} box;
+
+typedef struct vo_state {
+  vacgpu_params p;
+  int ndim, ndir, nw, mhd;
+  int nG[3];
+  long N;
+  long st[3];
+  box ixG, ixM;
+  /* variable indices (src/vacpar.t.mhd:9-26, src/vacpar.t.hd:9-26) */
+  int rho_, m0_, e_, b0_;
+  double *x, *dx, *dvolume;
+  double volume;
+  double *w, *w1, *wold;
+  double *wLC, *wRC, *fLC, *fRC, *vLC, *vRC, *cmaxC, *ldw, *dwC, *tmp,
+      *tmp2, *divb, *csound2, *cfast2, *pp;
+  double dtcourant[3];
+  double dt, t, dtold, dtpar, courantpar, dtgrav;
+  int it, itmin;
+  double smallp;
+  int nerror[4];
+  int istep, nstep;
+  int src_id;
+  double src_par[VACGPU_MAXSRCPAR];
+} vo_state;
+
+/* ------------------------------------------------------------------ boxes */
+
+static long IDX(const vo_state* s, int i1, int i2, int i3) {
+  return (long)i1 + s->st[1] * i2 + s->st[2] * i3;
+}
+
+#define FORBOX(b, ix)                                            \
+  for (int i3_ = (b).lo[2]; i3_ <= (b).hi[2]; i3_++)             \
+    for (int i2_ = (b).lo[1]; i2_ <= (b).hi[1]; i2_++)           \
+      for (long ix = IDX(s, (b).lo[0], i2_, i3_),                \
+                ixend_ = IDX(s, (b).hi[0], i2_, i3_);            \
+           ix <= ixend_; ix++)
+
+static box shift(box b, int idim, int d) {
+  b.lo[idim] += d;
+  b.hi[idim] += d;
+  return b;
+}
+
+#define W(a, iw) ((a) + (long)(iw)*s->N)
+
+/* ------------------------------------------------------------ physics MHD */
+
+/* getptotal, src/vacphys0.t.mhd:225-257 (ptot = (1-g/2)B^2+(g-1)e-(g-1)/2
+ * m^2/rho), unclipped */
+static void getptotal(vo_state* s, const double* w, box b, double* p) {
+  const double gamma = s->p.eqpar[0];
+  if (s->mhd) {
+    FORBOX(b, ix) {
+      double bb = 0.0;
+      for (int c = 1; c <= s->ndir; c++) {
+        double bc = W(w, s->b0_ + c)[ix];
+        bb = (c == 1) ? bc * bc : bb + bc * bc;
+      }
+      p[ix] = (ONE - HALF * gamma) * bb;
+    }
+    FORBOX(b, ix) { p[ix] = p[ix] + (gamma - ONE) * W(w, s->e_)[ix]; }
+    FORBOX(b, ix) {
+      double mm = 0.0;
+      for (int c = 1; c <= s->ndir; c++) {
+        double mc = W(w, s->m0_ + c)[ix];
+        mm = (c == 1) ? mc * mc : mm + mc * mc;
+      }
+      p[ix] = p[ix] - HALF * (gamma - ONE) * mm / W(w, s->rho_)[ix];
+    }
+  }
+}
+
+/* smallp initialisation inside getpthermal (src/vacphys0.t.mhd:202-217,
+ * src/vacphys0.t.hd:123-126) */
+static void init_smallp(vo_state* s, const double* p, box b) {
+  if (s->smallp < ZERO) {
+    double mn = BIGDOUBLE, mx = -BIGDOUBLE;
+    int first = 1;
+    FORBOX(b, ix) {
+      if (first) { mn = p[ix]; mx = p[ix]; first = 0; }
+      if (p[ix] < mn) mn = p[ix];
+      if (p[ix] > mx) mx = p[ix];
+    }
+    s->smallp = mn * s->p.smallpcoeff;
+    if (s->mhd && s->smallp < ZERO) s->smallp = mx * s->p.smallpcoeff;
+  }
+}
+
+/* getpthermal, src/vacphys0.t.mhd:165-222 and src/vacphys0.t.hd:103-134 */
+static void getpthermal(vo_state* s, int clipping, const double* w, box b,
+                        double* p) {
+  const double gamma = s->p.eqpar[0];
+  if (s->mhd) {
+    FORBOX(b, ix) {
+      double mm = 0.0;
+      for (int c = 1; c <= s->ndir; c++) {
+        double mc = W(w, s->m0_ + c)[ix];
+        mm = (c == 1) ? mc * mc : mm + mc * mc;
+      }
+      p[ix] = mm / W(w, s->rho_)[ix];
+    }
+    FORBOX(b, ix) {
+      double q = p[ix];
+      for (int c = 1; c <= s->ndir; c++) {
+        double bc = W(w, s->b0_ + c)[ix];
+        q = q + bc * bc;
+      }
+      p[ix] = q;
+    }
+    FORBOX(b, ix) {
+      p[ix] = (gamma - 1) * (W(w, s->e_)[ix] - HALF * p[ix]);
+    }
+  } else {
+    FORBOX(b, ix) {
+      double mm = 0.0;
+      for (int c = 1; c <= s->ndir; c++) {
+        double mc = W(w, s->m0_ + c)[ix];
+        mm = (c == 1) ? mc * mc : mm + mc * mc;
+      }
+      p[ix] = (gamma - 1) *
+              (W(w, s->e_)[ix] - HALF * mm / W(w, s->rho_)[ix]);
+    }
+  }
+  init_smallp(s, p, b);
+  if (clipping) {
+    FORBOX(b, ix) {
+      if (!(p[ix] >= s->smallp)) p[ix] = s->smallp;
+    }
+  }
+}
+
+/* getcsound2, src/vacphys0.t.mhd:140-162: csound2 = gamma*p/rho, p clipped */
+static void getcsound2(vo_state* s, const double* w, box b, double* cs2) {
+  getpthermal(s, 1, w, b, cs2);
+  const double gamma = s->p.eqpar[0];
+  FORBOX(b, ix) { cs2[ix] = gamma * cs2[ix] / W(w, s->rho_)[ix]; }
+}
+
+/* getcmax, src/vacphys0.t.mhd:79-116 (MHD fast speed) and
+ * src/vacphys0.t.hd:72-100 (HD sound speed).  new_cmax semantics: the
+ * direction independent part is recomputed when *new_cmax is set. */
+static void getcmax(vo_state* s, int* new_cmax, const double* w, box b,
+                    int idim, double* cmax) {
+  const double gamma = s->p.eqpar[0];
+  if (s->mhd) {
+    if (*new_cmax) {
+      *new_cmax = 0;
+      getcsound2(s, w, b, s->csound2);
+      FORBOX(b, ix) {
+        double bb = 0.0;
+        for (int c = 1; c <= s->ndir; c++) {
+          double bc = W(w, s->b0_ + c)[ix];
+          bb = (c == 1) ? bc * bc : bb + bc * bc;
+        }
+        s->cfast2[ix] = bb / W(w, s->rho_)[ix] + s->csound2[ix];
+      }
+    }
+    const double* bi = W(w, s->b0_ + idim + 1);
+    const double* mi = W(w, s->m0_ + idim + 1);
+    const double* rho = W(w, s->rho_);
+    FORBOX(b, ix) {
+      double cf2 = s->cfast2[ix];
+      cmax[ix] = sqrt(HALF * (cf2 + sqrt(cf2 * cf2 - 4 * s->csound2[ix] *
+                                                          (bi[ix] * bi[ix]) /
+                                                          rho[ix]))) +
+                 fabs(mi[ix] / rho[ix]);
+    }
+  } else {
+    if (*new_cmax) {
+      *new_cmax = 0;
+      getpthermal(s, 1, w, b, s->csound2);
+      FORBOX(b, ix) {
+        s->csound2[ix] = sqrt(gamma * s->csound2[ix] / W(w, s->rho_)[ix]);
+      }
+    }
+    const double* mi = W(w, s->m0_ + idim + 1);
+    const double* rho = W(w, s->rho_);
+    FORBOX(b, ix) { cmax[ix] = s->csound2[ix] + fabs(mi[ix] / rho[ix]); }
+  }
+}
+
+/* getv, src/vacphys0.t.mhd:57-75: v = m_idim/rho */
+static void getv(vo_state* s, const double* w, box b, int idim, double* v) {
+  FORBOX(b, ix) { v[ix] = W(w, s->m0_ + idim + 1)[ix] / W(w, s->rho_)[ix]; }
+}
+
+/* getflux, src/vacphys.mhd0.t:149-205 (MHD) and src/vacphys.t.hd:49-75 (HD)
+ * Returns the transport flag. */
+static int getflux(vo_state* s, const double* w, box b, int iw, int idim,
+                   double* f) {
+  const double* rho = W(w, s->rho_);
+  if (s->mhd) {
+    if (iw == s->rho_) {
+      FORBOX(b, ix) f[ix] = ZERO;
+      return 1;
+    }
+    if (iw > s->m0_ && iw <= s->m0_ + s->ndir) {
+      int k = iw - s->m0_;
+      const double* bk = W(w, s->b0_ + k);
+      const double* bi = W(w, s->b0_ + idim + 1);
+      if (k == idim + 1) {
+        getptotal(s, w, b, f);
+        FORBOX(b, ix) f[ix] = f[ix] - bk[ix] * bi[ix];
+      } else {
+        FORBOX(b, ix) f[ix] = -bk[ix] * bi[ix];
+      }
+      return 1;
+    }
+    if (iw == s->e_) {
+      getptotal(s, w, b, f);
+      const double* mi = W(w, s->m0_ + idim + 1);
+      const double* bi = W(w, s->b0_ + idim + 1);
+      FORBOX(b, ix) {
+        double bm = 0.0;
+        for (int c = 1; c <= s->ndir; c++) {
+          double t = W(w, s->b0_ + c)[ix] * W(w, s->m0_ + c)[ix];
+          bm = (c == 1) ? t : bm + t;
+        }
+        f[ix] = (mi[ix] * f[ix] - bi[ix] * bm) / rho[ix];
+      }
+      return 1;
+    }
+    /* b_k */
+    int k = iw - s->b0_;
+    if (k == idim + 1) {
+      FORBOX(b, ix) f[ix] = ZERO;
+      return 0;
+    }
+    const double* mk = W(w, s->m0_ + k);
+    const double* bi = W(w, s->b0_ + idim + 1);
+    FORBOX(b, ix) f[ix] = -mk[ix] / rho[ix] * bi[ix];
+    return 1;
+  } else {
+    if (iw == s->m0_ + idim + 1) {
+      getpthermal(s, 1, w, b, f);
+    } else if (iw == s->e_) {
+      getpthermal(s, 1, w, b, f);
+      const double* mi = W(w, s->m0_ + idim + 1);
+      FORBOX(b, ix) f[ix] = mi[ix] / rho[ix] * f[ix];
+    } else {
+      FORBOX(b, ix) f[ix] = ZERO;
+    }
+    return 1;
+  }
+}
+
+/* ---------------------------------------------------------------- limiter */
+
+static double sgn(double a) { return copysign(ONE, a); }
+static double fmax2(double a, double b) { return a > b ? a : b; }
+static double fmin2(double a, double b) { return a < b ? a : b; }
+
+/* dwlimiter2, src/vacgrid.t:938-996: ldw(ixO) from dwC(ixO), dwC(hxO) with
+ * ixO = ixC contracted by one at the low end in idim. */
+static void dwlimiter2(vo_state* s, const double* dwC, box ixC, int iw,
+                       int idim, double* ldw) {
+  box ixO = ixC;
+  ixO.lo[idim] += 1;
+  long sh = s->st[idim];
+  double* tmp = s->tmp;
+  FORBOX(ixO, ix) tmp[ix] = sgn(dwC[ix]);
+  const double qsmall = 1.0e-12, qsmall2 = 2.0e-12;
+  switch (s->p.typelimiter[iw]) {
+    case VACGPU_LIM_MINMOD:
+      FORBOX(ixO, ix) {
+        ldw[ix] = tmp[ix] * fmax2(ZERO, fmin2(fabs(dwC[ix]), tmp[ix] * dwC[ix - sh]));
+      }
+      break;
+    case VACGPU_LIM_WOODWARD:
+      FORBOX(ixO, ix) {
+        double m = fmin2(fmin2(fabs(dwC[ix]), tmp[ix] * dwC[ix - sh]),
+                         tmp[ix] * 0.25 * (dwC[ix - sh] + dwC[ix]));
+        ldw[ix] = 2 * tmp[ix] * fmax2(ZERO, m);
+      }
+      break;
+    case VACGPU_LIM_SUPERBEE:
+      FORBOX(ixO, ix) {
+        double a = fmin2(2 * fabs(dwC[ix]), tmp[ix] * dwC[ix - sh]);
+        double c = fmin2(fabs(dwC[ix]), 2 * tmp[ix] * dwC[ix - sh]);
+        ldw[ix] = tmp[ix] * fmax2(fmax2(ZERO, a), c);
+      }
+      break;
+    case VACGPU_LIM_VANLEER:
+      FORBOX(ixO, ix) {
+        ldw[ix] = 2 * fmax2(dwC[ix - sh] * dwC[ix], 0.0) /
+                  (dwC[ix] + dwC[ix - sh] + qsmall);
+      }
+      break;
+    case VACGPU_LIM_ALBADA:
+      FORBOX(ixO, ix) {
+        double a = dwC[ix], b = dwC[ix - sh];
+        ldw[ix] = (b * (a * a + qsmall) + a * (b * b + qsmall)) /
+                  (a * a + b * b + qsmall2);
+      }
+      break;
+  }
+}
+
+/* upwindLR, src/vactvdlf.t:302-367 (musclomega<=1, useprimitive=F):
+ * wRC(ixR) -= ldw(jxR)/2, wLC(ixL) += ldw(ixL)/2 */
+static void upwindLR(vo_state* s, box ixL, box ixR, int idim,
+                     const double* w, double* wLC, double* wRC) {
+  box jxR = shift(ixR, idim, 1);
+  box ixC = jxR;
+  ixC.lo[idim] = ixL.lo[idim] - 1;
+  for (int d = 0; d < 3; d++)
+    if (d != idim) {
+      ixC.lo[d] = ixL.lo[d];
+      ixC.hi[d] = jxR.hi[d];
+    }
+  long sh = s->st[idim];
+  for (int iw = 0; iw < s->nw; iw++) {
+    const double* wi = W(w, iw);
+    FORBOX(ixC, ix) s->dwC[ix] = wi[ix + sh] - wi[ix];
+    dwlimiter2(s, s->dwC, ixC, iw, idim, s->ldw);
+    double* r = W(wRC, iw);
+    double* l = W(wLC, iw);
+    FORBOX(ixR, ix) r[ix] = r[ix] - HALF * s->ldw[ix + sh];
+    FORBOX(ixL, ix) l[ix] = l[ix] + HALF * s->ldw[ix];
+  }
+}
+
+/* -------------------------------------------------------------- grid/flux */
+
+/* addflux, src/vacgrid.t:596-741, Cartesian slab branch (:669-678):
+ * wnew(ix) -= qdt/dx(ix,idim)*(fRC(ixR)-fLC(ixL)) */
+static void addflux(vo_state* s, double qdt, box ixO, int iw, int idim,
+                    const double* fR, box ixR, const double* fL, box ixL,
+                    double* wnew) {
+  long oR = IDX(s, ixR.lo[0], ixR.lo[1], ixR.lo[2]) -
+            IDX(s, ixO.lo[0], ixO.lo[1], ixO.lo[2]);
+  long oL = IDX(s, ixL.lo[0], ixL.lo[1], ixL.lo[2]) -
+            IDX(s, ixO.lo[0], ixO.lo[1], ixO.lo[2]);
+  double* wn = W(wnew, iw);
+  const double* dx = W(s->dx, idim);
+  FORBOX(ixO, ix) { wn[ix] = wn[ix] - qdt / dx[ix] * (fR[ix + oR] - fL[ix + oL]); }
+}
+
+/* gradient, src/vacgrid.t:775-837, slab branch (:816-823) */
+static void gradient(vo_state* s, const double* q, box ixO, int idir,
+                     double* gradq) {
+  long sh = s->st[idir];
+  const double* dx = W(s->dx, idir);
+  FORBOX(ixO, ix) gradq[ix] = HALF * (q[ix + sh] - q[ix - sh]) / dx[ix];
+}
+
+/* getdivb, src/vacphys.mhd0.t:106-146 (second order) */
+static void getdivb(vo_state* s, const double* w, box ixO, double* divb) {
+  FORBOX(ixO, ix) divb[ix] = ZERO;
+  for (int idim = 0; idim < s->ndim; idim++) {
+    gradient(s, W(w, s->b0_ + idim + 1), ixO, idim, s->tmp2);
+    FORBOX(ixO, ix) divb[ix] = divb[ix] + s->tmp2[ix];
+  }
+}
+
+/* addsource_divb, src/vacphys.mhd0.t:246-280 (Powell source) */
+static void addsource_divb(vo_state* s, double qdt, box ixO, const double* w,
+                           double* wnew) {
+  double* divb = s->divb;
+  getdivb(s, w, ixO, divb);
+  FORBOX(ixO, ix) divb[ix] = qdt * divb[ix];
+  const double* rho = W(w, s->rho_);
+  for (int iw = 0; iw < s->nw; iw++) {
+    double* wn = W(wnew, iw);
+    if (iw > s->m0_ && iw <= s->m0_ + s->ndir) {
+      const double* bk = W(w, s->b0_ + (iw - s->m0_));
+      FORBOX(ixO, ix) wn[ix] = wn[ix] - bk[ix] * divb[ix];
+    } else if (iw > s->b0_ && iw <= s->b0_ + s->ndir) {
+      const double* mk = W(w, s->m0_ + (iw - s->b0_));
+      FORBOX(ixO, ix) wn[ix] = wn[ix] - mk[ix] / rho[ix] * divb[ix];
+    } else if (iw == s->e_) {
+      FORBOX(ixO, ix) {
+        double mb = 0.0;
+        for (int c = 1; c <= s->ndir; c++) {
+          double t = W(w, s->m0_ + c)[ix] * W(w, s->b0_ + c)[ix];
+          mb = (c == 1) ? t : mb + t;
+        }
+        wn[ix] = wn[ix] - mb / rho[ix] * divb[ix];
+      }
+    }
+  }
+}
+
+/* addsource_grav, vacusr.gravity.t:24-75 (uniform gravity as specialsource) */
+static void addsource_grav(vo_state* s, double qdt, box ixO, const double* w,
+                           double* wnew) {
+  for (int iw = 0; iw < s->nw; iw++) {
+    if (iw > s->m0_ && iw <= s->m0_ + s->ndim) {
+      int idim = iw - s->m0_;
+      double g = s->src_par[idim - 1];
+      if (fabs(g) > SMALLDOUBLE) {
+        double* wn = W(wnew, iw);
+        const double* rho = W(w, s->rho_);
+        FORBOX(ixO, ix) wn[ix] = wn[ix] + qdt * g * rho[ix];
+      }
+    } else if (iw == s->e_) {
+      for (int idim = 1; idim <= s->ndim; idim++) {
+        double g = s->src_par[idim - 1];
+        if (fabs(g) > SMALLDOUBLE) {
+          double* wn = W(wnew, iw);
+          const double* m = W(w, s->m0_ + idim);
+          FORBOX(ixO, ix) wn[ix] = wn[ix] + qdt * g * m[ix];
+        }
+      }
+    }
+  }
+}
+
+/* addsource2, src/vac.t:575-605: specialsource then addsource */
+static void addsource2(vo_state* s, double qdt, box ixO, const double* wCT,
+                       double* w) {
+  if (s->src_id == VACGPU_SRC_GRAVITY) addsource_grav(s, qdt, ixO, wCT, w);
+  if (s->mhd && s->p.divbfix) addsource_divb(s, qdt, ixO, wCT, w);
+}
+
+/* getboundary, src/vacgrid.t:195-413 with the default regions of boundsetup
+ * (src/vacgrid.t:53-69) and periodic pairing (:121-135). */
+static void getboundary(vo_state* s, double* w) {
+  for (int iB = 0; iB < 2 * s->ndim; iB++) {
+    int idim = iB / 2, upper = iB % 2;
+    box r = s->ixG;
+    if (upper) {
+      r.lo[idim] = s->ixM.hi[idim] + 1;
+      r.hi[idim] = s->ixG.hi[idim];
+    } else {
+      r.lo[idim] = s->ixG.lo[idim];
+      r.hi[idim] = s->ixM.lo[idim] - 1;
+    }
+    long sh = s->st[idim];
+    for (int iw = 0; iw < s->nw; iw++) {
+      double* a = W(w, iw);
+      int type = s->p.typeB[iB][iw];
+      if (type == VACGPU_BC_CONT) {
+        int ixe = upper ? r.lo[idim] - 1 : r.hi[idim] + 1;
+        for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
+          box row = r;
+          row.lo[idim] = row.hi[idim] = k;
+          long off = (long)(ixe - k) * sh;
+          FORBOX(row, ix) a[ix] = a[ix + off];
+        }
+      } else if (type == VACGPU_BC_PERIODIC) {
+        long off = (long)(upper ? -(s->nG[idim] - 4) : (s->nG[idim] - 4)) * sh;
+        FORBOX(r, ix) a[ix] = a[ix + off];
+      } else {
+        int ixe = upper ? 2 * r.lo[idim] - 1 : 2 * r.hi[idim] + 1;
+        for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
+          box row = r;
+          row.lo[idim] = row.hi[idim] = k;
+          long off = (long)((ixe - k) - k) * sh;
+          FORBOX(row, ix) a[ix] = a[ix + off];
+        }
+        if (type == VACGPU_BC_ASYMM) FORBOX(r, ix) a[ix] = -a[ix];
+      }
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- schemes */
+
+/* hancock, src/vactvdlf.t:5-89 */
+static void hancock(vo_state* s, double qdt, box ixO, int idimmin,
+                    int idimmax, const double* wCT, double* wnew) {
+  for (int idim = idimmin; idim <= idimmax; idim++) {
+    box hxO = shift(ixO, idim, -1);
+    long sh = s->st[idim];
+    for (int iw = 0; iw < s->nw; iw++) {
+      double* r = W(s->wRC, iw);
+      double* l = W(s->wLC, iw);
+      const double* c = W(wCT, iw);
+      FORBOX(hxO, ix) r[ix] = c[ix + sh];
+      FORBOX(ixO, ix) l[ix] = c[ix];
+    }
+    upwindLR(s, ixO, hxO, idim, wCT, s->wLC, s->wRC);
+    getv(s, s->wRC, hxO, idim, s->vRC);
+    getv(s, s->wLC, ixO, idim, s->vLC);
+    for (int iw = 0; iw < s->nw; iw++) {
+      int tr = getflux(s, s->wRC, hxO, iw, idim, s->fRC);
+      getflux(s, s->wLC, ixO, iw, idim, s->fLC);
+      if (tr) {
+        const double* r = W(s->wRC, iw);
+        const double* l = W(s->wLC, iw);
+        FORBOX(hxO, ix) s->fRC[ix] = s->fRC[ix] + s->vRC[ix] * r[ix];
+        FORBOX(ixO, ix) s->fLC[ix] = s->fLC[ix] + s->vLC[ix] * l[ix];
+      }
+      addflux(s, qdt, ixO, iw, idim, s->fLC, ixO, s->fRC, hxO, wnew);
+    }
+  }
+  if (s->p.sourceunsplit)
+    addsource2(s, qdt * (idimmax - idimmin + ONE) / s->ndim, ixO, wCT, wnew);
+}
+
+/* tvdmusclf with method='tvdlf'/'tvdlf1', addfluxok=.true.,
+ * src/vactvdlf.t:92-299 */
+static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
+                      int idimmax, const double* wCT, double* wnew) {
+  for (int idim = idimmin; idim <= idimmax; idim++) {
+    box hxO = shift(ixO, idim, -1);
+    box ixC = ixO;
+    ixC.lo[idim] = hxO.lo[idim];
+    long sh = s->st[idim];
+    for (int iw = 0; iw < s->nw; iw++) {
+      double* r = W(s->wRC, iw);
+      double* l = W(s->wLC, iw);
+      const double* c = W(wCT, iw);
+      FORBOX(ixC, ix) r[ix] = c[ix + sh];
+      FORBOX(ixC, ix) l[ix] = c[ix];
+    }
+    if (s->p.typefull != VACGPU_TVDLF1) {
+      const double* base;
+      switch (s->p.typelimited) {
+        case VACGPU_LIMITED_PREVIOUS: base = s->wold; break;
+        case VACGPU_LIMITED_PREDICTOR: base = wCT; break;
+        default: base = wnew; break;
+      }
+      upwindLR(s, ixC, ixC, idim, base, s->wLC, s->wRC);
+    }
+    /* mean state in wLC, cmax, CFL, wLC regained (src/vactvdlf.t:168-206) */
+    for (int iw = 0; iw < s->nw; iw++) {
+      double* l = W(s->wLC, iw);
+      const double* r = W(s->wRC, iw);
+      FORBOX(ixC, ix) l[ix] = HALF * (l[ix] + r[ix]);
+    }
+    int new_cmax = 1;
+    getcmax(s, &new_cmax, s->wLC, ixC, idim, s->cmaxC);
+    if (s->courantpar > ZERO && s->istep == s->nstep) {
+      const double* dx = W(s->dx, idim);
+      double courantmax = 0.0;
+      int first = 1;
+      FORBOX(ixC, ix) {
+        double q = s->cmaxC[ix] * TWO / (dx[ix] + dx[ix + sh]);
+        if (first || q > courantmax) courantmax = q;
+        first = 0;
+      }
+      if (qdt * courantmax > ONE) s->nerror[2]++;
+      if (courantmax > SMALLDOUBLE) {
+        double c = s->courantpar / courantmax;
+        if (c < s->dtcourant[idim]) s->dtcourant[idim] = c;
+      }
+    }
+    for (int iw = 0; iw < s->nw; iw++) {
+      double* l = W(s->wLC, iw);
+      const double* r = W(s->wRC, iw);
+      FORBOX(ixC, ix) l[ix] = 2 * l[ix] - r[ix];
+    }
+    getv(s, s->wLC, ixC, idim, s->vLC);
+    getv(s, s->wRC, ixC, idim, s->vRC);
+    for (int iw = 0; iw < s->nw; iw++) {
+      const double* l = W(s->wLC, iw);
+      const double* r = W(s->wRC, iw);
+      int tr = getflux(s, s->wLC, ixC, iw, idim, s->fLC);
+      getflux(s, s->wRC, ixC, iw, idim, s->fRC);
+      if (tr) {
+        FORBOX(ixC, ix) s->fLC[ix] = s->fLC[ix] + s->vLC[ix] * l[ix];
+        FORBOX(ixC, ix) s->fRC[ix] = s->fRC[ix] + s->vRC[ix] * r[ix];
+      }
+      FORBOX(ixC, ix) s->fLC[ix] = HALF * (s->fLC[ix] + s->fRC[ix]);
+      FORBOX(ixC, ix) s->fRC[ix] = -s->cmaxC[ix] * HALF * (r[ix] - l[ix]);
+      FORBOX(ixC, ix) s->fLC[ix] = s->fLC[ix] + s->fRC[ix];
+      addflux(s, qdt, ixO, iw, idim, s->fLC, ixO, s->fLC, hxO, wnew);
+    }
+  }
+  if (s->p.sourceunsplit)
+    addsource2(s, qdt * (idimmax - idimmin + ONE) / s->ndim, ixO, wCT, wnew);
+}
+
+/* advect1, src/vac.t:489-572 (method hancock/tvdlf; ixO = ixI shrunk by 2) */
+static void advect1(vo_state* s, int pred, double qdt, int idimmin,
+                    int idimmax, const double* wCT, double* w) {
+  s->istep++;
+  if (pred)
+    hancock(s, qdt, s->ixM, idimmin, idimmax, wCT, w);
+  else
+    tvdmusclf(s, qdt, s->ixM, idimmin, idimmax, wCT, w);
+  getboundary(s, w);
+}
+
+/* advect, src/vac.t:363-486 with typeadvance='twostep' */
+static void advect(vo_state* s, int idimmin, int idimmax) {
+  memcpy(s->w1, s->w, sizeof(double) * s->N * s->nw);
+  s->istep = 0;
+  advect1(s, 1, s->dt / 2, idimmin, idimmax, s->w, s->w1);
+  advect1(s, 0, s->dt, idimmin, idimmax, s->w1, s->w);
+}
+
+/* advance_expl, src/vac.t:283-360 */
+static void advance_expl(vo_state* s) {
+  if (s->p.dimsplit) {
+    if ((s->it / 2) * 2 == s->it || s->p.typedimsplit == VACGPU_SPLIT_XY) {
+      for (int d = 0; d < s->ndim; d++) advect(s, d, d);
+    } else {
+      for (int d = s->ndim - 1; d >= 0; d--) advect(s, d, d);
+    }
+  } else {
+    advect(s, 0, s->ndim - 1);
+  }
+}
+
+/* getdt_courant, src/vac.t:664-722 */
+static void getdt_courant(vo_state* s) {
+  s->dt = BIGDOUBLE;
+  double courantmax = ZERO;
+  int new_cmax = 1;
+  for (int idim = 0; idim < s->ndim; idim++) {
+    if (s->dtcourant[idim] < BIGDOUBLE) {
+      if (s->dtcourant[idim] < s->dt) s->dt = s->dtcourant[idim];
+    } else {
+      getcmax(s, &new_cmax, s->w, s->ixM, idim, s->cmaxC);
+      const double* dx = W(s->dx, idim);
+      double m = 0.0;
+      int first = 1;
+      FORBOX(s->ixM, ix) {
+        double q = s->cmaxC[ix] / dx[ix];
+        if (first || q > m) m = q;
+        first = 0;
+      }
+      if (m > courantmax) courantmax = m;
+    }
+  }
+  for (int idim = 0; idim < s->ndim; idim++) s->dtcourant[idim] = BIGDOUBLE;
+  if (courantmax > SMALLDOUBLE) {
+    double c = s->courantpar / courantmax;
+    if (c < s->dt) s->dt = c;
+  }
+}
+
+/* getdt_grav, vacusr.gravity.t (dt limit of the gravity hook) */
+static void getdt_special(vo_state* s) {
+  if (s->src_id != VACGPU_SRC_GRAVITY) return;
+  if (s->it == s->itmin) {
+    s->dtgrav = BIGDOUBLE;
+    for (int idim = 0; idim < s->ndim; idim++) {
+      double g = fabs(s->src_par[idim]);
+      if (g > ZERO) {
+        double m = 0.0;
+        int first = 1;
+        for (int jdim = 0; jdim < s->ndim; jdim++) {
+          const double* dx = W(s->dx, jdim);
+          FORBOX(s->ixM, ix) {
+            double q = g / dx[ix];
+            if (first || q > m) m = q;
+            first = 0;
+          }
+        }
+        double c = ONE / sqrt(m);
+        if (c < s->dtgrav) s->dtgrav = c;
+      }
+    }
+  }
+  if (s->dtgrav < s->dt) s->dt = s->dtgrav;
+}
+
+/* -------------------------------------------------------------- public API */
+
+#define ERR(msg)                                   \
+  do {                                             \
+    snprintf(errbuf, sizeof(errbuf), "%s", msg);   \
+    return NULL;                                   \
+  } while (0)
+
+static char errbuf[256];
+
+const char* vo_last_error(void) { return errbuf; }
+
+vo_state* vo_create(const vacgpu_params* p) {
+  if (p->ndim < 1 || p->ndim > 3) ERR("ndim out of range");
+  if (p->ndir < p->ndim || p->ndir > 3) ERR("ndir out of range");
+  if (p->dixB != 2) ERR("dixB must be 2");
+  int nw = p->physics == VACGPU_PHYS_MHD ? 2 + 2 * p->ndir : 2 + p->ndir;
+  if (p->nw != nw) ERR("nw does not match physics and ndir");
+  vo_state* s = (vo_state*)calloc(1, sizeof(vo_state));
+  s->p = *p;
+  s->ndim = p->ndim;
+  s->ndir = p->ndir;
+  s->nw = nw;
+  s->mhd = p->physics == VACGPU_PHYS_MHD;
+  s->rho_ = 0;
+  s->m0_ = 0;
+  s->e_ = 1 + p->ndir;
+  s->b0_ = s->e_;
+  for (int d = 0; d < 3; d++) {
+    s->nG[d] = d < p->ndim ? p->nx[d] + 4 : 1;
+    s->ixG.lo[d] = 0;
+    s->ixG.hi[d] = s->nG[d] - 1;
+    s->ixM.lo[d] = d < p->ndim ? 2 : 0;
+    s->ixM.hi[d] = d < p->ndim ? s->nG[d] - 3 : 0;
+  }
+  s->st[0] = 1;
+  s->st[1] = s->nG[0];
+  s->st[2] = (long)s->nG[0] * s->nG[1];
+  s->N = s->st[2] * s->nG[2];
+  long N = s->N;
+  s->x = calloc(N * 3, sizeof(double));
+  s->dx = calloc(N * 3, sizeof(double));
+  s->dvolume = calloc(N, sizeof(double));
+  s->w = calloc(N * nw, sizeof(double));
+  s->w1 = calloc(N * nw, sizeof(double));
+  s->wold = calloc(N * nw, sizeof(double));
+  s->wLC = calloc(N * nw, sizeof(double));
+  s->wRC = calloc(N * nw, sizeof(double));
+  double** t1[] = {&s->fLC, &s->fRC, &s->vLC, &s->vRC, &s->cmaxC,
+                   &s->ldw, &s->dwC, &s->tmp, &s->tmp2, &s->divb,
+                   &s->csound2, &s->cfast2, &s->pp};
+  for (unsigned i = 0; i < sizeof(t1) / sizeof(t1[0]); i++)
+    *t1[i] = calloc(N, sizeof(double));
+  s->smallp = p->smallp;
+  s->courantpar = p->courantpar;
+  s->dtpar = p->dtpar;
+  s->nstep = 2;
+  /* startup, src/vac.t:160-220 */
+  for (int d = 0; d < 3; d++) s->dtcourant[d] = BIGDOUBLE;
+  if (s->dtpar > ZERO && p->slowsteps != 1) s->courantpar = -ONE;
+  return s;
+}
+
+void vo_destroy(vo_state* s) {
+  if (!s) return;
+  double* a[] = {s->x, s->dx, s->dvolume, s->w, s->w1, s->wold, s->wLC,
+                 s->wRC, s->fLC, s->fRC, s->vLC, s->vRC, s->cmaxC, s->ldw,
+                 s->dwC, s->tmp, s->tmp2, s->divb, s->csound2, s->cfast2,
+                 s->pp};
+  for (unsigned i = 0; i < sizeof(a) / sizeof(a[0]); i++) free(a[i]);
+  free(s);
+}
+
+/* gridsetup1, src/vacgrid.t:457-593 (Cartesian slab, fullgridini=F).
+ * xmesh: x(ixM^S,1:ndim) column-major. */
+int vo_set_grid(vo_state* s, const double* xmesh) {
+  int nd = s->ndim;
+  int nQ[3], q0[3];
+  for (int d = 0; d < 3; d++) {
+    nQ[d] = d < nd ? s->nG[d] + 2 : 1;
+    q0[d] = d < nd ? 1 : 0; /* qx index of G index 0 */
+  }
+  long qs1 = nQ[0], qs2 = (long)nQ[0] * nQ[1];
+  long NQ = qs2 * nQ[2];
+  double* qx = calloc(NQ * nd, sizeof(double));
+#define QX(i1, i2, i3, jd) \
+  qx[(long)(jd)*NQ + (i1) + qs1 * (i2) + qs2 * (i3)]
+  /* qx(ixG)=x(ixG); x in the ghost cells is zero, as in VAC */
+  long k = 0;
+  for (int jd = 0; jd < nd; jd++)
+    for (int i3 = s->ixM.lo[2]; i3 <= s->ixM.hi[2]; i3++)
+      for (int i2 = s->ixM.lo[1]; i2 <= s->ixM.hi[1]; i2++)
+        for (int i1 = s->ixM.lo[0]; i1 <= s->ixM.hi[0]; i1++)
+          QX(i1 + q0[0], i2 + q0[1], i3 + q0[2], jd) = xmesh[k++];
+  for (int idim = 0; idim < nd; idim++) {
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+      lo[d] = 0;
+      hi[d] = nQ[d] - 1;
+    }
+    for (int pass = 0; pass < 2; pass++) {
+      int ixe, ixf;
+      if (pass == 0) { /* upper layers */
+        lo[idim] = s->ixM.hi[idim] + 1 + q0[idim];
+        hi[idim] = nQ[idim] - 1;
+        ixe = lo[idim] - 1;
+        ixf = ixe - 1;
+      } else {
+        lo[idim] = 0;
+        hi[idim] = s->ixM.lo[idim] - 1 + q0[idim];
+        ixe = hi[idim] + 1;
+        ixf = ixe + 1;
+      }
+      for (int jd = 0; jd < nd; jd++)
+        for (int ix = lo[idim]; ix <= hi[idim]; ix++) {
+          int c = abs(ixe - ix);
+          int a[3];
+          for (a[2] = lo[2]; a[2] <= hi[2]; a[2]++)
+            for (a[1] = lo[1]; a[1] <= hi[1]; a[1]++)
+              for (a[0] = lo[0]; a[0] <= hi[0]; a[0]++) {
+                if (a[idim] != lo[idim]) continue;
+                int b[3] = {a[0], a[1], a[2]}, e[3] = {a[0], a[1], a[2]},
+                    f[3] = {a[0], a[1], a[2]};
+                b[idim] = ix;
+                e[idim] = ixe;
+                f[idim] = ixf;
+                QX(b[0], b[1], b[2], jd) =
+                    (1 + c) * QX(e[0], e[1], e[2], jd) -
+                    c * QX(f[0], f[1], f[2], jd);
+              }
+        }
+    }
+  }
+  for (int i3 = 0; i3 < s->nG[2]; i3++)
+    for (int i2 = 0; i2 < s->nG[1]; i2++)
+      for (int i1 = 0; i1 < s->nG[0]; i1++) {
+        long ix = IDX(s, i1, i2, i3);
+        int q[3] = {i1 + q0[0], i2 + q0[1], i3 + q0[2]};
+        for (int jd = 0; jd < nd; jd++)
+          W(s->x, jd)[ix] = QX(q[0], q[1], q[2], jd);
+        for (int idim = 0; idim < nd; idim++) {
+          int j[3] = {q[0], q[1], q[2]}, h[3] = {q[0], q[1], q[2]};
+          j[idim]++;
+          h[idim]--;
+          W(s->dx, idim)[ix] = HALF * (QX(j[0], j[1], j[2], idim) -
+                                       QX(h[0], h[1], h[2], idim));
+        }
+        double dv = W(s->dx, 0)[ix];
+        for (int idim = 1; idim < nd; idim++) dv = dv * W(s->dx, idim)[ix];
+        s->dvolume[ix] = dv;
+      }
+#undef QX
+  free(qx);
+  s->volume = 0.0;
+  FORBOX(s->ixM, ix) s->volume = s->volume + s->dvolume[ix];
+  return 0;
+}
+
+/* w(ixM^S,1:nw) from the .ini; ghosts by getboundary (src/vac.t:54) */
+void vo_set_state(vo_state* s, const double* wmesh, int it, double t) {
+  long k = 0;
+  for (int iw = 0; iw < s->nw; iw++) FORBOX(s->ixM, ix) W(s->w, iw)[ix] = wmesh[k++];
+  s->it = it;
+  s->itmin = it;
+  s->t = t;
+  getboundary(s, s->w);
+}
+
+void vo_get_state(vo_state* s, double* wmesh) {
+  long k = 0;
+  for (int iw = 0; iw < s->nw; iw++) FORBOX(s->ixM, ix) wmesh[k++] = W(s->w, iw)[ix];
+}
+
+/* full ixG state (test access to ghosts) */
+void vo_get_state_full(vo_state* s, double* wfull) {
+  memcpy(wfull, s->w, sizeof(double) * s->N * s->nw);
+}
+
+void vo_register_source(vo_state* s, int id, const double* par, int npar) {
+  s->src_id = id;
+  memset(s->src_par, 0, sizeof(s->src_par));
+  for (int i = 0; i < npar && i < VACGPU_MAXSRCPAR; i++) s->src_par[i] = par[i];
+}
+
+/* The time loop body, src/vac.t:55-106.  Returns the number of steps done;
+ * *finished=1 when timetofinish held. */
+int vo_step(vo_state* s, int maxsteps, double tstop, int* finished) {
+  int n = 0;
+  *finished = 0;
+  const vacgpu_params* p = &s->p;
+  while (n < maxsteps) {
+    double dtsave_dt = s->dt, dtold_save = s->dtold;
+    double dtc[3] = {s->dtcourant[0], s->dtcourant[1], s->dtcourant[2]};
+    if (s->dtpar > ZERO) {
+      s->dt = s->dtpar;
+    } else {
+      if (s->courantpar > ZERO) getdt_courant(s);
+      getdt_special(s);
+      if (p->dtcantgrow && s->it > s->itmin && s->dtold < s->dt) s->dt = s->dtold;
+      s->dtold = s->dt;
+    }
+    /* timetofinish, src/vac.t:608-628 (residual checks off) */
+    if (s->it >= p->itmax || s->t >= p->tmax || s->dt < p->dtmin) {
+      *finished = 1;
+      break;
+    }
+    if (s->t >= tstop) {
+      /* caller saves before this step: the dt evaluation is repeated then */
+      s->dt = dtsave_dt;
+      s->dtold = dtold_save;
+      for (int d = 0; d < 3; d++) s->dtcourant[d] = dtc[d];
+      break;
+    }
+    if (p->slowsteps == 1 && s->it == s->itmin) s->dtpar = -ONE;
+    if (p->slowsteps > s->it - s->itmin + 1) {
+      double r = ONE - (s->it - s->itmin + ONE) / p->slowsteps;
+      s->dt = s->dt * (ONE - r * r);
+    }
+    if (p->tmaxexact) {
+      double c = p->tmax - s->t + SMALLDOUBLE;
+      if (c < s->dt) s->dt = c;
+    }
+    memcpy(s->wold, s->w, sizeof(double) * s->N * s->nw);
+    advance_expl(s);
+    s->it = s->it + 1;
+    s->t = s->t + s->dt;
+    n++;
+  }
+  return n;
+}
+
+double vo_t(vo_state* s) { return s->t; }
+int vo_it(vo_state* s) { return s->it; }
+double vo_dt(vo_state* s) { return s->dt; }
+double vo_smallp(vo_state* s) { return s->smallp; }
+double vo_volume(vo_state* s) { return s->volume; }
+void vo_nerror(vo_state* s, int* n) { memcpy(n, s->nerror, sizeof(s->nerror)); }
+long vo_ncells_full(vo_state* s) { return s->N; }
+
+/* dx(ixG^S,idim) and x(ixG^S,idim), full grid */
+void vo_get_dx(vo_state* s, int idim, double* out) {
+  memcpy(out, W(s->dx, idim), sizeof(double) * s->N);
+}
+void vo_get_x(vo_state* s, int idim, double* out) {
+  memcpy(out, W(s->x, idim), sizeof(double) * s->N);
+}
+
+/* savefilelog_default, src/vacio.t:1050-1105 */
+void vo_sums(vo_state* s, double* wmean) {
+  for (int iw = 0; iw < s->nw; iw++) {
+    double acc = 0.0;
+    FORBOX(s->ixM, ix) acc = acc + s->dvolume[ix] * W(s->w, iw)[ix];
+    wmean[iw] = acc / s->volume;
+  }
+}
