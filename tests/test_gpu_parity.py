@@ -1,0 +1,123 @@
+"""GPU parity: the FP64 path through the C ABI against the FP64 CPU oracle,
+bit for bit (every variable of every mesh cell, t and it), and the mixed path
+against the oracle within its stated tolerance."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from vac_gb300 import abi, inistate
+from vac_gb300.engine import Engine
+
+pytestmark = pytest.mark.gpu
+
+# Relative L1 error per variable allowed for the mixed-precision path
+# (FP32 state; double-precision pressure recovery) against the FP64 oracle.
+MIXED_REL_L1 = 1e-5
+
+
+def bits(a):
+    return np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+
+
+def run_both(s, lim, bc, nsteps, tweak=None, precision=abi.PREC_FP64, src=None):
+    p = inistate.params_for(s, limiter=lim, bc=bc, precision=precision)
+    if tweak:
+        tweak(p)
+    o = Oracle(p, s.x, s.w)
+    e = Engine(p, s.x, s.w)
+    if src:
+        o.register_source(*src)
+        e.register_source(*src)
+    o.step(nsteps)
+    e.step(nsteps)
+    return o, e
+
+
+FP64_CASES = [
+    ("ot200-config1", lambda: inistate.orszag_tang(200), "minmod", "periodic", 200, None, None),
+    ("ot-woodward", lambda: inistate.orszag_tang(40), "woodward", "periodic", 30, None, None),
+    ("rm3-woodward", lambda: inistate.random_modes(20, seed=1), "woodward", "periodic", 8, None, None),
+    ("rm3-minmod-xy", lambda: inistate.random_modes(12, seed=2), "minmod", "periodic", 5,
+     lambda p: setattr(p, "typedimsplit", abi.SPLIT_XY), None),
+    ("hd-riemann-cont", lambda: inistate.riemann_2d(48, 3), "minmod", "cont", 30, None, None),
+    ("ot-superbee-cont", lambda: inistate.orszag_tang(24), "superbee", "cont", 10, None, None),
+    ("ot-vanleer-symm", lambda: inistate.orszag_tang(24), "vanleer", "symm", 10, None, None),
+    ("ot-albada", lambda: inistate.orszag_tang(24), "albada", "periodic", 10, None, None),
+    ("ot-unsplit", lambda: inistate.orszag_tang(24), "minmod", "periodic", 10,
+     lambda p: (setattr(p, "dimsplit", 0), setattr(p, "typelimited", abi.LIMITED_PREVIOUS)), None),
+    ("ot-tvdlf1", lambda: inistate.orszag_tang(24), "minmod", "periodic", 10,
+     lambda p: setattr(p, "typefull", abi.TVDLF1), None),
+    ("hd-gravity", lambda: inistate.riemann_2d(32, 5), "woodward", "cont", 10, None,
+     (abi.SRC_GRAVITY, [0.0, -0.5])),
+    ("ot-ragged", lambda: _ragged(), "minmod", "periodic", 10, None, None),
+]
+
+
+def _ragged():
+    """Non-square, odd-sized grid: 37 x 23 cells."""
+    s = inistate.orszag_tang(8)
+    x = inistate.domain_grid((37, 23), (0.0, 0.0), (2 * np.pi, 2 * np.pi))
+    g = 5.0 / 3.0
+    X, Y = x
+    w = inistate.conserve_mhd(np.full_like(X, g * g), [-np.sin(Y), np.sin(X)],
+                              np.full_like(X, g), [-np.sin(Y), np.sin(2 * X)], g)
+    s.x, s.w, s.nx = x, w, (37, 23)
+    return s
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", FP64_CASES,
+                         ids=[c[0] for c in FP64_CASES])
+def test_fp64_bit_exact(gpu_lib, name, mk, lim, bc, n, tweak, src):
+    o, e = run_both(mk(), lim, bc, n, tweak, src=src)
+    assert e.it == o.it and e.t == o.t, (e.it, o.it, e.t, o.t)
+    a, b = e.state(), o.state()
+    bad = np.count_nonzero(bits(a) != bits(b))
+    assert bad == 0, "%d of %d values differ, max |diff| %g" % (
+        bad, a.size, np.abs(a - b).max())
+    assert e.nerror() == o.nerror()
+
+
+def test_fp64_tstop_resume_and_itmax(gpu_lib):
+    s = inistate.orszag_tang(32)
+    p = inistate.params_for(s)
+    p.itmax = 12
+    o = Oracle(p, s.x, s.w)
+    e = Engine(p, s.x, s.w)
+    fin = e.step(1000, tstop=0.25)
+    assert not fin and e.t >= 0.25
+    fin = e.step(1000)
+    assert fin and e.it == 12
+    o.step(1000)
+    assert np.array_equal(bits(e.state()), bits(o.state()))
+
+
+def test_sums_match_log_definition(gpu_lib):
+    s = inistate.orszag_tang(64)
+    o, e = run_both(s, "minmod", "periodic", 5)
+    np.testing.assert_allclose(e.sums(), o.sums(), rtol=1e-13, atol=1e-15)
+
+
+MIXED_CASES = [
+    ("ot", lambda: inistate.orszag_tang(64), "minmod", "periodic", 50),
+    ("rm3", lambda: inistate.random_modes(32, seed=3), "woodward", "periodic", 20),
+    ("hd", lambda: inistate.riemann_2d(64, 7), "minmod", "cont", 30),
+]
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n", MIXED_CASES, ids=[c[0] for c in MIXED_CASES])
+def test_mixed_rel_l1(gpu_lib, name, mk, lim, bc, n):
+    s = mk()
+    p64 = inistate.params_for(s, limiter=lim, bc=bc)
+    pm = inistate.params_for(s, limiter=lim, bc=bc, precision=abi.PREC_MIXED)
+    o = Oracle(p64, s.x, s.w)
+    e = Engine(pm, s.x, s.w)
+    # same number of steps; dt is chosen by each run's own CFL
+    o.step(n)
+    e.step(n)
+    a, b = e.state(), o.state()
+    for iw in range(a.shape[0]):
+        den = np.abs(b[iw]).sum()
+        if den == 0:
+            continue
+        rel = np.abs(a[iw] - b[iw]).sum() / den
+        assert rel <= MIXED_REL_L1, (iw, rel)

@@ -1,0 +1,499 @@
+// sweep.cuh - kernels of one dimensional sweep of VAC's twostep
+// Hancock-predictor / TVDLF-corrector scheme (src/vac.t:363-572,
+// src/vactvdlf.t:5-299), the ghost-cell fill (src/vacgrid.t:195-413) and the
+// cell-centred CFL pass of getdt_courant (src/vac.t:664-722).
+//
+// Templated on a physics policy PH (storage type T, arithmetic type R and
+// the pointwise physics), the dimensionality and the physics module.
+#pragma once
+#include "vacgpu_internal.h"
+
+namespace vacgpu {
+
+__device__ __forceinline__ void atomic_max_key(unsigned long long* a,
+                                               unsigned long long k) {
+  atomicMax(a, k);
+}
+__device__ __forceinline__ void atomic_min_key(unsigned long long* a,
+                                               unsigned long long k) {
+  atomicMin(a, k);
+}
+
+// Block-wide max of an ordered key; thread 0 returns the result.
+template <int NT>
+__device__ __forceinline__ unsigned long long block_max_key(
+    unsigned long long k, unsigned long long* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o);
+    k = v > k ? v : k;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = k;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < NT / 32; i++) k = sh[i] > k ? sh[i] : k;
+  }
+  __syncthreads();
+  return k;
+}
+
+// Decompose a mesh-cell counter into ghost-box coordinates.
+__device__ __forceinline__ void cell_coords(const DevGrid& g, long long n,
+                                            int* c) {
+  int ix = (int)(n % g.nx[0]);
+  long long r = n / g.nx[0];
+  int iy = (int)(r % g.nx[1]);
+  int iz = (int)(r / g.nx[1]);
+  c[0] = ix + g.gh[0];
+  c[1] = iy + g.gh[1];
+  c[2] = iz + g.gh[2];
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+struct Sweep {
+  typedef typename PH::T T;
+  typedef typename PH::R R;
+  typedef Lay<NDIR, MHD> L;
+  static constexpr int NW = L::NW;
+
+  // addsource2 (src/vac.t:575-605): specialsource (uniform gravity,
+  // vacusr.gravity.t:24-75) then addsource (Powell divB source,
+  // src/vacphys.mhd0.t:246-280).  wc = wCT at the cell, wct points at the
+  // cell in the wCT array (for the divB central differences).
+  static __device__ __forceinline__ void add_sources(
+      const SweepArgs& a, double qdt, const R* wc, const T* __restrict__ wct,
+      const long long* st, const int* c, R* acc) {
+    if (a.ph.src_id == VACGPU_SRC_GRAVITY) {
+#pragma unroll
+      for (int d = 1; d <= NDIM; d++) {
+        double gr = a.ph.src_par[d - 1];
+        if (fabs(gr) > 1.0e-99) acc[d] = acc[d] + PH::mul_qg(qdt, gr) * wc[0];
+      }
+#pragma unroll
+      for (int d = 1; d <= NDIM; d++) {
+        double gr = a.ph.src_par[d - 1];
+        if (fabs(gr) > 1.0e-99)
+          acc[L::E] = acc[L::E] + PH::mul_qg(qdt, gr) * wc[d];
+      }
+    }
+    if (MHD && a.ph.divbfix) {
+      R divb = R(0);
+#pragma unroll
+      for (int d = 0; d < NDIM; d++) {
+        const T* q = wct + (long long)(L::B0 + 1 + d) * a.g.vs;
+        R gq = R(0.5) * (R(q[st[d]]) - R(q[-st[d]])) / PH::dx(a.a, d, c[d]);
+        divb = divb + gq;
+      }
+      divb = PH::qdiv(qdt) * divb;
+      R mb = wc[1] * wc[L::B0 + 1];
+#pragma unroll
+      for (int k = 2; k <= NDIR; k++) mb = mb + wc[k] * wc[L::B0 + k];
+#pragma unroll
+      for (int k = 1; k <= NDIR; k++) {
+        acc[k] = acc[k] - wc[L::B0 + k] * divb;
+        acc[L::B0 + k] = acc[L::B0 + k] - wc[k] / wc[0] * divb;
+      }
+      acc[L::E] = acc[L::E] - mb / wc[0] * divb;
+    }
+  }
+
+  // Hancock predictor (src/vactvdlf.t:5-89): w1 = w - dt/2/dx*(F(w+ldw/2)
+  // - F(w-ldw/2)) + dt/2*(nsweepdims/ndim)*S(w), on the mesh.
+  static __device__ void predict(const SweepArgs& a, const T* __restrict__ w,
+                                 T* __restrict__ w1) {
+    const Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    const long long st[3] = {1, a.g.P, a.g.plane};
+    const long long vs = a.g.vs;
+    const double qdt = ctrl->dt / 2;
+    const R smallp = R(ctrl->smallp);
+    R u[NW], acc[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      u[iw] = R(w[off + iw * vs]);
+      acc[iw] = u[iw];
+    }
+    for (int d = a.d0; d <= a.d1; d++) {
+      R uL[NW], uR[NW];
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) {
+        R wm = R(w[off + iw * vs - st[d]]);
+        R wp = R(w[off + iw * vs + st[d]]);
+        R l = PH::limiter(a.ph.lim[iw], wp - u[iw], u[iw] - wm);
+        uR[iw] = u[iw] - R(0.5) * l;
+        uL[iw] = u[iw] + R(0.5) * l;
+      }
+      R fL[NW], fR[NW];
+      PH::template flux<NDIR, MHD>(uR, d, a.ph, smallp, fR);
+      PH::template flux<NDIR, MHD>(uL, d, a.ph, smallp, fL);
+      const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) acc[iw] = acc[iw] - cq * (fL[iw] - fR[iw]);
+    }
+    if (a.ph.sourceunsplit)
+      add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, u, w + off, st, c,
+                  acc);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) w1[off + iw * vs] = T(acc[iw]);
+  }
+
+  // TVDLF numerical flux at the face between cell `o` and `o+st` in
+  // direction d (src/vactvdlf.t:140-259); returns the face cmax.
+  static __device__ __forceinline__ R face_flux(const SweepArgs& a,
+                                                const T* __restrict__ w1,
+                                                const T* __restrict__ base,
+                                                long long o, long long s,
+                                                int d, R smallp, R* F) {
+    const long long vs = a.g.vs;
+    R wL[NW], wR[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      wL[iw] = R(w1[o + iw * vs]);
+      wR[iw] = R(w1[o + iw * vs + s]);
+    }
+    if (a.ph.typefull != VACGPU_TVDLF1) {
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) {
+        const T* b = base + o + iw * vs;
+        R bm = R(b[-s]), b0 = R(b[0]), b1 = R(b[s]), b2 = R(b[2 * s]);
+        R ldL = PH::limiter(a.ph.lim[iw], b1 - b0, b0 - bm);
+        R ldR = PH::limiter(a.ph.lim[iw], b2 - b1, b1 - b0);
+        wR[iw] = wR[iw] - R(0.5) * ldR;
+        wL[iw] = wL[iw] + R(0.5) * ldL;
+      }
+    }
+    R mean[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) mean[iw] = R(0.5) * (wL[iw] + wR[iw]);
+    const R cmax = PH::template cmax<NDIR, MHD>(mean, d, a.ph, smallp);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) wL[iw] = R(2) * mean[iw] - wR[iw];
+    R fL[NW], fR[NW];
+    PH::template flux<NDIR, MHD>(wL, d, a.ph, smallp, fL);
+    PH::template flux<NDIR, MHD>(wR, d, a.ph, smallp, fR);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      R f = R(0.5) * (fL[iw] + fR[iw]);
+      R diss = -cmax * R(0.5) * (wR[iw] - wL[iw]);
+      F[iw] = f + diss;
+    }
+    return cmax;
+  }
+
+  // TVDLF corrector (src/vactvdlf.t:92-299) plus the CFL maximum of the last
+  // substep (src/vactvdlf.t:184-201).
+  template <int NT>
+  static __device__ void correct(const SweepArgs& a, const T* __restrict__ w,
+                                 const T* __restrict__ w1,
+                                 const T* __restrict__ base,
+                                 T* __restrict__ wout) {
+    __shared__ unsigned long long shk[NT / 32];
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = n < a.g.ncell;
+    unsigned long long key[3] = {0ULL, 0ULL, 0ULL};
+    if (active) {
+      int c[3];
+      cell_coords(a.g, n, c);
+      const long long off = gidx(a.g, c[0], c[1], c[2]);
+      const long long st[3] = {1, a.g.P, a.g.plane};
+      const long long vs = a.g.vs;
+      const double qdt = ctrl->dt;
+      const R smallp = R(ctrl->smallp);
+      R acc[NW];
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
+      for (int d = a.d0; d <= a.d1; d++) {
+        R Fm[NW], Fp[NW];
+        R cm = face_flux(a, w1, base, off - st[d], st[d], d, smallp, Fm);
+        R cp = face_flux(a, w1, base, off, st[d], d, smallp, Fp);
+        if (a.ph.courantpar > 0.0) {
+          double qm = PH::cfl(cm, a.a, d, c[d] - 1);
+          double qp = PH::cfl(cp, a.a, d, c[d]);
+          unsigned long long km = dkey(qm), kp = dkey(qp);
+          key[d] = km > kp ? km : kp;
+        }
+        const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++)
+          acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
+      }
+      if (a.ph.sourceunsplit) {
+        R wc[NW];
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
+        add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off, st,
+                    c, acc);
+      }
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
+    }
+    if (a.ph.courantpar > 0.0) {
+      for (int d = a.d0; d <= a.d1; d++) {
+        unsigned long long k = block_max_key<NT>(key[d], shk);
+        if (threadIdx.x == 0 && k)
+          atomic_max_key(&ctrl->face_cmax[d][blockIdx.x % NSLOT], k);
+      }
+    }
+  }
+
+  // getpthermal's one-time smallp: min/max of the unclipped pressure on the
+  // mesh (src/vacphys0.t.mhd:202-217).
+  template <int NT>
+  static __device__ void pminmax(const SweepArgs& a, const T* __restrict__ w) {
+    __shared__ unsigned long long shk[NT / 32];
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->done || !ctrl->need_smallp) return;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long kmin = ~0ULL, kmax = 0ULL;
+    if (n < a.g.ncell) {
+      int c[3];
+      cell_coords(a.g, n, c);
+      const long long off = gidx(a.g, c[0], c[1], c[2]);
+      R u[NW];
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+      double p = PH::template pthermal_raw<NDIR, MHD>(u, a.ph);
+      kmin = dkey(p);
+      kmax = kmin;
+    }
+    unsigned long long k = block_max_key<NT>(kmax, shk);
+    if (threadIdx.x == 0) atomic_max_key(&ctrl->pmax[blockIdx.x % NSLOT], k);
+    k = ~block_max_key<NT>(~kmin, shk);
+    if (threadIdx.x == 0) atomic_min_key(&ctrl->pmin[blockIdx.x % NSLOT], k);
+  }
+
+  // Cell-centred max(cmax/dx) of getdt_courant for the dimensions whose
+  // dtcourant is unset (src/vac.t:690-711).
+  template <int NT>
+  static __device__ void cell_cmax(const SweepArgs& a, const T* __restrict__ w) {
+    __shared__ unsigned long long shk[NT / 32];
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    if (!(ctrl->need_cell[0] | ctrl->need_cell[1] | ctrl->need_cell[2]))
+      return;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const R smallp = R(ctrl->smallp);
+    int c[3] = {0, 0, 0};
+    R u[NW];
+    const bool active = n < a.g.ncell;
+    if (active) {
+      cell_coords(a.g, n, c);
+      const long long off = gidx(a.g, c[0], c[1], c[2]);
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+    }
+    for (int d = 0; d < NDIM; d++) {
+      if (!ctrl->need_cell[d]) continue;
+      unsigned long long k = 0ULL;
+      if (active) {
+        R cm = PH::template cmax<NDIR, MHD>(u, d, a.ph, smallp);
+        k = dkey(PH::cell_ratio(cm, a.a, d, c[d]));
+      }
+      k = block_max_key<NT>(k, shk);
+      if (threadIdx.x == 0)
+        atomic_max_key(&ctrl->cell_cmax[d][blockIdx.x % NSLOT], k);
+    }
+  }
+};
+
+// Ghost-cell fill: ghost(i,j,k) = sign * w(map_x(i), map_y(j), map_z(k)),
+// the composition of getboundary's per-region copies (src/vacgrid.t:195-413:
+// regions are filled x first, then y, then z, each over the full extent of
+// the other dimensions, from mesh cells), for 'periodic', 'cont', 'symm' and
+// 'asymm'.
+__device__ __forceinline__ int bc_map(int gi, int n, int tlo, int thi,
+                                      int* sgn) {
+  if (gi < 2) {
+    switch (tlo) {
+      case VACGPU_BC_PERIODIC: return gi + n;
+      case VACGPU_BC_CONT: return 2;
+      case VACGPU_BC_ASYMM: *sgn = -*sgn; return 3 - gi;
+      default: return 3 - gi;
+    }
+  }
+  if (gi >= n + 2) {
+    switch (thi) {
+      case VACGPU_BC_PERIODIC: return gi - n;
+      case VACGPU_BC_CONT: return n + 1;
+      case VACGPU_BC_ASYMM: *sgn = -*sgn; return 2 * n + 3 - gi;
+      default: return 2 * n + 3 - gi;
+    }
+  }
+  return gi;
+}
+
+template <typename T, int NW>
+__global__ void k_ghost(T* __restrict__ w, DevGrid g, DevPhys ph,
+                        const Ctrl* ctrl) {
+  if (ctrl && ctrl->done) return;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ndim = g.ndim;
+  const long long nzs = ndim == 3 ? 4LL * g.nG[1] * g.nG[0] : 0;
+  const long long nys = ndim >= 2 ? 4LL * g.nx[2] * g.nG[0] : 0;
+  const long long nxs = 4LL * g.nx[1] * g.nx[2];
+  int c[3];
+  if (t < nzs) {
+    int l = (int)(t / ((long long)g.nG[1] * g.nG[0]));
+    long long r = t % ((long long)g.nG[1] * g.nG[0]);
+    c[2] = l < 2 ? l : g.nG[2] - 4 + l;
+    c[1] = (int)(r / g.nG[0]);
+    c[0] = (int)(r % g.nG[0]);
+  } else if (t < nzs + nys) {
+    long long u = t - nzs;
+    int l = (int)(u / ((long long)g.nx[2] * g.nG[0]));
+    long long r = u % ((long long)g.nx[2] * g.nG[0]);
+    c[1] = l < 2 ? l : g.nG[1] - 4 + l;
+    c[2] = (int)(r / g.nG[0]) + g.gh[2];
+    c[0] = (int)(r % g.nG[0]);
+  } else if (t < nzs + nys + nxs) {
+    long long u = t - nzs - nys;
+    int l = (int)(u % 4);
+    long long r = u / 4;
+    c[0] = l < 2 ? l : g.nG[0] - 4 + l;
+    c[1] = (int)(r % g.nx[1]) + g.gh[1];
+    c[2] = (int)(r / g.nx[1]) + g.gh[2];
+  } else {
+    return;
+  }
+  const long long dst = gidx(g, c[0], c[1], c[2]);
+#pragma unroll
+  for (int iw = 0; iw < NW; iw++) {
+    int sgn = 1, s[3] = {c[0], c[1], c[2]};
+    for (int d = 0; d < ndim; d++)
+      s[d] = bc_map(c[d], g.nx[d], ph.typeB[2 * d][iw], ph.typeB[2 * d + 1][iw],
+                    &sgn);
+    T v = w[gidx(g, s[0], s[1], s[2]) + iw * g.vs];
+    w[dst + iw * g.vs] = sgn < 0 ? -v : v;
+  }
+}
+
+inline long long ghost_count(const DevGrid& g) {
+  long long nzs = g.ndim == 3 ? 4LL * g.nG[1] * g.nG[0] : 0;
+  long long nys = g.ndim >= 2 ? 4LL * g.nx[2] * g.nG[0] : 0;
+  return nzs + nys + 4LL * g.nx[1] * g.nx[2];
+}
+
+// ---------------------------------------------------------------- wrappers
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_predict(SweepArgs a, const typename PH::T* __restrict__ w,
+              typename PH::T* __restrict__ w1) {
+  Sweep<PH, NDIM, NDIR, MHD>::predict(a, w, w1);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_correct(SweepArgs a, const typename PH::T* __restrict__ w,
+              const typename PH::T* __restrict__ w1,
+              const typename PH::T* __restrict__ base,
+              typename PH::T* __restrict__ wout) {
+  Sweep<PH, NDIM, NDIR, MHD>::template correct<128>(a, w, w1, base, wout);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_pminmax(SweepArgs a, const typename PH::T* __restrict__ w) {
+  Sweep<PH, NDIM, NDIR, MHD>::template pminmax<128>(a, w);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_cell_cmax(SweepArgs a, const typename PH::T* __restrict__ w) {
+  Sweep<PH, NDIM, NDIR, MHD>::template cell_cmax<128>(a, w);
+}
+
+// Dispatch on (ndim, ndir, physics) to a template instance.
+#define VACGPU_DISPATCH(a, KCALL)                                        \
+  do {                                                                   \
+    if ((a).mhd) {                                                       \
+      if ((a).g.ndim == 1 && (a).ndir == 1) { KCALL(1, 1, true); }       \
+      else if ((a).g.ndim == 2 && (a).ndir == 2) { KCALL(2, 2, true); }  \
+      else if ((a).g.ndim == 2 && (a).ndir == 3) { KCALL(2, 3, true); }  \
+      else if ((a).g.ndim == 3 && (a).ndir == 3) { KCALL(3, 3, true); }  \
+    } else {                                                             \
+      if ((a).g.ndim == 1 && (a).ndir == 1) { KCALL(1, 1, false); }      \
+      else if ((a).g.ndim == 2 && (a).ndir == 2) { KCALL(2, 2, false); } \
+      else if ((a).g.ndim == 2 && (a).ndir == 3) { KCALL(2, 3, false); } \
+      else if ((a).g.ndim == 3 && (a).ndir == 3) { KCALL(3, 3, false); } \
+    }                                                                    \
+  } while (0)
+
+inline unsigned grid_for(long long n, int nt) {
+  return (unsigned)((n + nt - 1) / nt);
+}
+
+template <class PH>
+struct Launch {
+  typedef typename PH::T T;
+  static void predict(const SweepArgs& a, const T* w, T* w1, cudaStream_t st) {
+    unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) k_predict<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
+  static void correct(const SweepArgs& a, const T* w, const T* w1,
+                      const T* base, T* wout, cudaStream_t st) {
+    unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) \
+  k_correct<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1, base, wout)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
+  static void ghost(const SweepArgs& a, T* w, cudaStream_t st) {
+    long long n = ghost_count(a.g);
+    unsigned nb = grid_for(n, 128);
+    int nw = a.mhd ? 2 + 2 * a.ndir : 2 + a.ndir;
+    switch (nw) {
+      case 3: k_ghost<T, 3><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl); break;
+      case 4: k_ghost<T, 4><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl); break;
+      case 5: k_ghost<T, 5><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl); break;
+      case 6: k_ghost<T, 6><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl); break;
+      case 8: k_ghost<T, 8><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl); break;
+    }
+  }
+  static void pminmax(const SweepArgs& a, const T* w, cudaStream_t st) {
+    unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) k_pminmax<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
+  static void cell_cmax(const SweepArgs& a, const T* w, cudaStream_t st) {
+    unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) k_cell_cmax<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
+};
+
+#define VACGPU_DEFINE_LAUNCHERS(SUF, PH)                                      \
+  void launch_predict_##SUF(const SweepArgs& s, const PH::T* w, PH::T* w1,   \
+                            cudaStream_t st) {                               \
+    Launch<PH>::predict(s, w, w1, st);                                       \
+  }                                                                          \
+  void launch_correct_##SUF(const SweepArgs& s, const PH::T* w,              \
+                            const PH::T* w1, const PH::T* base, PH::T* wout, \
+                            cudaStream_t st) {                               \
+    Launch<PH>::correct(s, w, w1, base, wout, st);                           \
+  }                                                                          \
+  void launch_ghost_##SUF(const SweepArgs& s, PH::T* w, cudaStream_t st) {   \
+    Launch<PH>::ghost(s, w, st);                                             \
+  }                                                                          \
+  void launch_pminmax_##SUF(const SweepArgs& s, const PH::T* w,              \
+                            cudaStream_t st) {                               \
+    Launch<PH>::pminmax(s, w, st);                                           \
+  }                                                                          \
+  void launch_cell_cmax_##SUF(const SweepArgs& s, const PH::T* w,            \
+                              cudaStream_t st) {                             \
+    Launch<PH>::cell_cmax(s, w, st);                                         \
+  }
+
+}  // namespace vacgpu

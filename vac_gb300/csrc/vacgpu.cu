@@ -1,0 +1,648 @@
+// vacgpu.cu - the C ABI of include/vacgpu.h: handle life cycle, grid set-up
+// (gridsetup1), state transfer, the device-resident time loop and the
+// conservation sums.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vacgpu_internal.h"
+
+using namespace vacgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(const std::string& m) {
+  g_err = m;
+  return 1;
+}
+
+#define CK(call)                                                        \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess)                                              \
+      return fail(std::string("CUDA error: ") + cudaGetErrorString(e_) + \
+                  " at " #call);                                        \
+  } while (0)
+
+const double BIGD = 1.0e99;
+
+// mesh <-> padded state transfer (VAC column-major mesh blocks per variable)
+template <typename T>
+__global__ void k_scatter(const double* __restrict__ src, T* __restrict__ w,
+                          DevGrid g, int nw) {
+  long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.ncell * nw) return;
+  int iw = (int)(n / g.ncell);
+  long long m = n % g.ncell;
+  int ix = (int)(m % g.nx[0]);
+  long long r = m / g.nx[0];
+  int iy = (int)(r % g.nx[1]);
+  int iz = (int)(r / g.nx[1]);
+  w[gidx(g, ix + g.gh[0], iy + g.gh[1], iz + g.gh[2]) + iw * g.vs] = (T)src[n];
+}
+
+template <typename T>
+__global__ void k_gather(const T* __restrict__ w, double* __restrict__ dst,
+                         DevGrid g, int nw) {
+  long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= g.ncell * nw) return;
+  int iw = (int)(n / g.ncell);
+  long long m = n % g.ncell;
+  int ix = (int)(m % g.nx[0]);
+  long long r = m / g.nx[0];
+  int iy = (int)(r % g.nx[1]);
+  int iz = (int)(r / g.nx[1]);
+  dst[n] = (double)w[gidx(g, ix + g.gh[0], iy + g.gh[1], iz + g.gh[2]) +
+                     iw * g.vs];
+}
+
+// Volume sums: per block partial sums of dvolume*w in FP64, folded in a
+// fixed order by a second kernel (deterministic).
+template <typename T>
+__global__ void k_sums_partial(const T* __restrict__ w, DevGrid g, int nw,
+                               const double* dx0, const double* dx1,
+                               const double* dx2, double* part) {
+  __shared__ double sh[8][256 / 32];
+  long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc[8];
+  for (int iw = 0; iw < 8; iw++) acc[iw] = 0.0;
+  if (n < g.ncell) {
+    int ix = (int)(n % g.nx[0]);
+    long long r = n / g.nx[0];
+    int iy = (int)(r % g.nx[1]);
+    int iz = (int)(r / g.nx[1]);
+    int gx = ix + g.gh[0], gy = iy + g.gh[1], gz = iz + g.gh[2];
+    double dv = dx0[gx];
+    if (g.ndim > 1) dv = dv * dx1[gy];
+    if (g.ndim > 2) dv = dv * dx2[gz];
+    long long off = gidx(g, gx, gy, gz);
+    for (int iw = 0; iw < nw; iw++) acc[iw] = dv * (double)w[off + iw * g.vs];
+  }
+  for (int iw = 0; iw < nw; iw++) {
+    double v = acc[iw];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[iw][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nw) {
+    double s = 0.0;
+    for (int i = 0; i < 256 / 32; i++) s += sh[threadIdx.x][i];
+    part[(long long)blockIdx.x * nw + threadIdx.x] = s;
+  }
+}
+
+__global__ void k_sums_final(const double* part, long long nblk, int nw,
+                             double* out) {
+  int iw = threadIdx.x;
+  if (iw >= nw) return;
+  double s = 0.0;
+  for (long long b = 0; b < nblk; b++) s += part[b * nw + iw];
+  out[iw] = s;
+}
+
+__global__ void k_call_begin(Ctrl* c, int maxsteps, double tstop) {
+  c->done = 0;
+  c->steps = 0;
+  c->maxsteps = maxsteps;
+  c->tstop = tstop;
+}
+
+}  // namespace
+
+struct vacgpu_handle {
+  vacgpu_params p;
+  DevGrid g;
+  DevPhys ph;
+  int nw;
+  size_t elem;
+  void* buf[3];      // two state buffers (ping-pong) + predictor output
+  void* wold;        // step-start copy for typelimited='previous' when split
+  int cur;           // which of buf[0], buf[1] holds the state
+  double* dx[3];
+  float* dxf[3];
+  std::vector<double> hdx[3];
+  double volume;
+  double* stage;     // mesh-ordered FP64 transfer buffer
+  double* part;      // sums partials
+  double* sums;
+  Ctrl* ctrl;
+  cudaStream_t st;
+  int it_host;
+  double dtgrav;
+  bool have_grid, have_state;
+  int pmode;         // mixed pressure variant (0 ff, 1 native f64, 2 f32)
+};
+
+namespace {
+
+SweepArgs make_args(vacgpu_handle* h, int d0, int d1) {
+  SweepArgs a;
+  a.g = h->g;
+  a.ph = h->ph;
+  for (int d = 0; d < 3; d++) {
+    a.a.dx[d] = h->dx[d];
+    a.a.dxf[d] = h->dxf[d];
+  }
+  a.ctrl = h->ctrl;
+  a.ndir = h->p.ndir;
+  a.mhd = h->p.physics == VACGPU_PHYS_MHD;
+  a.d0 = d0;
+  a.d1 = d1;
+  a.typelimited = h->p.typelimited;
+  return a;
+}
+
+template <typename T>
+void run_sweep(vacgpu_handle* h, int d0, int d1) {
+  SweepArgs a = make_args(h, d0, d1);
+  T* w = (T*)h->buf[h->cur];
+  T* wout = (T*)h->buf[h->cur ^ 1];
+  T* w1 = (T*)h->buf[2];
+  const T* base = w;
+  if (h->p.typelimited == VACGPU_LIMITED_PREDICTOR) base = w1;
+  if (h->p.typelimited == VACGPU_LIMITED_PREVIOUS && h->p.dimsplit)
+    base = (const T*)h->wold;
+  if (sizeof(T) == 8) {
+    launch_predict_fp64(a, (const double*)w, (double*)w1, h->st);
+    launch_ghost_fp64(a, (double*)w1, h->st);
+    launch_correct_fp64(a, (const double*)w, (const double*)w1,
+                        (const double*)base, (double*)wout, h->st);
+    launch_ghost_fp64(a, (double*)wout, h->st);
+  } else {
+    const float* fw = (const float*)w;
+    float* fw1 = (float*)w1;
+    float* fo = (float*)wout;
+    const float* fb = (const float*)base;
+    switch (h->pmode) {
+      case 1:
+        launch_predict_mixedf64(a, fw, fw1, h->st);
+        launch_ghost_mixedf64(a, fw1, h->st);
+        launch_correct_mixedf64(a, fw, fw1, fb, fo, h->st);
+        launch_ghost_mixedf64(a, fo, h->st);
+        break;
+      case 2:
+        launch_predict_mixedf32(a, fw, fw1, h->st);
+        launch_ghost_mixedf32(a, fw1, h->st);
+        launch_correct_mixedf32(a, fw, fw1, fb, fo, h->st);
+        launch_ghost_mixedf32(a, fo, h->st);
+        break;
+      default:
+        launch_predict_mixed(a, fw, fw1, h->st);
+        launch_ghost_mixed(a, fw1, h->st);
+        launch_correct_mixed(a, fw, fw1, fb, fo, h->st);
+        launch_ghost_mixed(a, fo, h->st);
+    }
+  }
+  h->cur ^= 1;
+}
+
+template <typename T>
+void run_step(vacgpu_handle* h, int parity_odd) {
+  const vacgpu_params& p = h->p;
+  SweepArgs a = make_args(h, 0, p.ndim - 1);
+  launch_dt_begin(h->ctrl, p.ndim, h->st);
+  const T* w = (const T*)h->buf[h->cur];
+  if (sizeof(T) == 8) {
+    launch_pminmax_fp64(a, (const double*)w, h->st);
+    launch_smallp(h->ctrl, a.mhd, p.smallpcoeff, h->st);
+    launch_cell_cmax_fp64(a, (const double*)w, h->st);
+  } else {
+    launch_pminmax_mixed(a, (const float*)w, h->st);
+    launch_smallp(h->ctrl, a.mhd, p.smallpcoeff, h->st);
+    launch_cell_cmax_mixed(a, (const float*)w, h->st);
+  }
+  launch_dt_end(h->ctrl, p, h->st);
+  if (p.typelimited == VACGPU_LIMITED_PREVIOUS && p.dimsplit)
+    cudaMemcpyAsync(h->wold, h->buf[h->cur], h->elem * h->g.vs * h->nw,
+                    cudaMemcpyDeviceToDevice, h->st);
+  if (p.dimsplit) {
+    if (!parity_odd || p.typedimsplit == VACGPU_SPLIT_XY) {
+      for (int d = 0; d < p.ndim; d++) run_sweep<T>(h, d, d);
+    } else {
+      for (int d = p.ndim - 1; d >= 0; d--) run_sweep<T>(h, d, d);
+    }
+  } else {
+    run_sweep<T>(h, 0, p.ndim - 1);
+  }
+  launch_step_end(h->ctrl, p.ndim, h->st);
+}
+
+int check_params(const vacgpu_params* p) {
+  if (p->ndim < 1 || p->ndim > 3) return fail("ndim must be 1..3");
+  if (p->ndir < p->ndim || p->ndir > 3) return fail("ndir must be ndim..3");
+  bool ok = (p->ndim == p->ndir) || (p->ndim == 2 && p->ndir == 3);
+  if (!ok) return fail("supported (ndim,ndir): (1,1) (2,2) (2,3) (3,3)");
+  if (p->physics != VACGPU_PHYS_HD && p->physics != VACGPU_PHYS_MHD)
+    return fail("physics must be VACGPU_PHYS_HD or VACGPU_PHYS_MHD");
+  int nw = p->physics == VACGPU_PHYS_MHD ? 2 + 2 * p->ndir : 2 + p->ndir;
+  if (p->nw != nw) return fail("nw does not match physics and ndir");
+  if (p->dixB != 2) return fail("dixB must be 2 (VAC's dixBlo=dixBhi=2)");
+  for (int d = 0; d < p->ndim; d++)
+    if (p->nx[d] < 2) return fail("nx must be >= 2 in every dimension");
+  if (!(p->eqpar[0] > 0.0)) return fail("eqpar(gamma_) must be positive");
+  if (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] != 0.0)
+    return fail("resistive MHD (eqpar(eta_)/=0) is not on this path");
+  if (p->typefull != VACGPU_TVDLF && p->typefull != VACGPU_TVDLF1)
+    return fail("typefull must be tvdlf or tvdlf1");
+  for (int iw = 0; iw < nw; iw++)
+    if (p->typelimiter[iw] < 0 || p->typelimiter[iw] > VACGPU_LIM_ALBADA)
+      return fail("unknown typelimiter");
+  if (p->typelimited < 0 || p->typelimited > VACGPU_LIMITED_PREDICTOR)
+    return fail("unknown typelimited");
+  if (!p->dimsplit && p->typelimited == VACGPU_LIMITED_ORIGINAL &&
+      p->typefull != VACGPU_TVDLF1)
+    return fail("Error in TVDMUSCLF: Unsplit dim. and original is limited");
+  if (p->physics == VACGPU_PHYS_MHD && p->divbfix && !p->sourceunsplit)
+    return fail("divbfix=T requires unsplitsource=T or splitsource=T !");
+  for (int d = 0; d < p->ndim; d++)
+    for (int iw = 0; iw < nw; iw++) {
+      int lo = p->typeB[2 * d][iw], hi = p->typeB[2 * d + 1][iw];
+      if (lo < 0 || lo > VACGPU_BC_ASYMM || hi < 0 || hi > VACGPU_BC_ASYMM)
+        return fail("unsupported boundary type (cont/periodic/symm/asymm)");
+      if ((lo == VACGPU_BC_PERIODIC) != (hi == VACGPU_BC_PERIODIC))
+        return fail("Error in BoundSetup: No periodic pair");
+    }
+  if (p->smallp < 0.0 && (p->dtpar > 0.0 || !(p->courantpar > 0.0)))
+    return fail("smallp<0 with a fixed dt: give smallp explicitly");
+  if (p->precision != VACGPU_PREC_FP64 && p->precision != VACGPU_PREC_MIXED)
+    return fail("precision must be VACGPU_PREC_FP64 or VACGPU_PREC_MIXED");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
+                           const int* nx) {
+  memset(p, 0, sizeof(*p));
+  p->ndim = ndim;
+  p->ndir = ndir;
+  p->physics = physics;
+  p->nw = physics == VACGPU_PHYS_MHD ? 2 + 2 * ndir : 2 + ndir;
+  for (int d = 0; d < 3; d++) p->nx[d] = d < ndim ? nx[d] : 1;
+  p->dixB = 2;
+  p->eqpar[0] = 5.0 / 3.0;
+  p->typefull = VACGPU_TVDLF;
+  for (int iw = 0; iw < VACGPU_MAXNW; iw++) p->typelimiter[iw] = VACGPU_LIM_MINMOD;
+  p->typelimited = VACGPU_LIMITED_ORIGINAL;
+  p->dimsplit = 1;
+  p->typedimsplit = VACGPU_SPLIT_XYYX;
+  p->divbfix = 1;
+  p->sourceunsplit = 1;
+  p->courantpar = 0.8;
+  p->dtpar = -1.0;
+  p->smallpcoeff = 1.0e-6;
+  p->smallp = -1.0;
+  p->itmax = 1000000;
+  p->tmax = 1.0e99;
+  p->dtmin = 1.0e-99;
+  for (int b = 0; b < VACGPU_MAXB; b++)
+    for (int iw = 0; iw < VACGPU_MAXNW; iw++) p->typeB[b][iw] = VACGPU_BC_CONT;
+  p->precision = VACGPU_PREC_FP64;
+}
+
+int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
+  *out = nullptr;
+  if (check_params(p)) return 1;
+  vacgpu_handle* h = new vacgpu_handle();  // value-initialised: zeroed
+  h->p = *p;
+  h->nw = p->nw;
+  h->elem = p->precision == VACGPU_PREC_FP64 ? 8 : 4;
+  const char* pm = getenv("VACGPU_MIXED_PRESSURE");
+  h->pmode = 0;
+  if (pm && !strcmp(pm, "f64")) h->pmode = 1;
+  if (pm && !strcmp(pm, "f32")) h->pmode = 2;
+  DevGrid& g = h->g;
+  g.ndim = p->ndim;
+  g.ncell = 1;
+  for (int d = 0; d < 3; d++) {
+    g.nx[d] = d < p->ndim ? p->nx[d] : 1;
+    g.gh[d] = d < p->ndim ? 2 : 0;
+    g.nG[d] = g.nx[d] + 2 * g.gh[d];
+    g.ncell *= g.nx[d];
+  }
+  const int align = (int)(128 / h->elem);
+  g.xpad = align - 2;
+  g.P = ((g.xpad + g.nG[0] + align - 1) / align) * align;
+  g.plane = g.P * g.nG[1];
+  g.vs = g.plane * g.nG[2];
+  DevPhys& ph = h->ph;
+  ph.gamma = p->eqpar[0];
+  ph.pt1 = 1.0 - 0.5 * p->eqpar[0];
+  ph.gm1 = p->eqpar[0] - 1.0;
+  ph.pt3 = 0.5 * (p->eqpar[0] - 1.0);
+  ph.smallpcoeff = p->smallpcoeff;
+  double courantpar = p->courantpar;
+  if (p->dtpar > 0.0 && p->slowsteps != 1) courantpar = -1.0;  // startup
+  ph.courantpar = courantpar;
+  for (int iw = 0; iw < VACGPU_MAXNW; iw++) ph.lim[iw] = p->typelimiter[iw];
+  memcpy(ph.typeB, p->typeB, sizeof(ph.typeB));
+  ph.typefull = p->typefull;
+  ph.divbfix = p->divbfix;
+  ph.sourceunsplit = p->sourceunsplit;
+  ph.src_id = VACGPU_SRC_NONE;
+  size_t bytes = h->elem * (size_t)g.vs * h->nw;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; i++) {
+    e = cudaMalloc(&h->buf[i], bytes);
+    if (e == cudaSuccess) e = cudaMemset(h->buf[i], 0, bytes);
+  }
+  if (e == cudaSuccess && p->typelimited == VACGPU_LIMITED_PREVIOUS &&
+      p->dimsplit)
+    e = cudaMalloc(&h->wold, bytes);
+  for (int d = 0; d < 3 && e == cudaSuccess; d++) {
+    e = cudaMalloc(&h->dx[d], sizeof(double) * g.nG[d]);
+    if (e == cudaSuccess) e = cudaMalloc(&h->dxf[d], sizeof(float) * g.nG[d]);
+  }
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->stage, sizeof(double) * g.ncell * h->nw);
+  long long nblk = (g.ncell + 255) / 256;
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->part, sizeof(double) * nblk * h->nw);
+  if (e == cudaSuccess) e = cudaMalloc(&h->sums, sizeof(double) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&h->ctrl, sizeof(Ctrl));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    vacgpu_destroy(h);
+    return fail(std::string("device allocation failed: ") + cudaGetErrorString(e));
+  }
+  Ctrl c;
+  memset(&c, 0, sizeof(c));
+  c.dtpar = p->dtpar;
+  c.courantpar = courantpar;
+  c.smallp = p->smallp;
+  c.dtgrav = BIGD;
+  for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
+  c.tstop = 1e300;
+  e = cudaMemcpy(h->ctrl, &c, sizeof(c), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    vacgpu_destroy(h);
+    return fail(std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  }
+  *out = h;
+  return 0;
+}
+
+// gridsetup1 (src/vacgrid.t:457-593) for a Cartesian product grid: the
+// ghost coordinates of each line are extrapolated linearly from the two
+// edge cells, dx = (x(i+1)-x(i-1))/2, dvolume = dx1*dx2*dx3 and volume is
+// summed in column-major order.
+int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
+  if (!h) return fail("null handle");
+  const DevGrid& g = h->g;
+  const int nd = h->p.ndim;
+  const long long n = g.ncell;
+  const long long st[3] = {1, g.nx[0], (long long)g.nx[0] * g.nx[1]};
+  for (int d = 0; d < nd; d++) {
+    // product-grid check: x_d must depend on ix_d only
+    const double* xd = x + d * n;
+    for (long long m = 0; m < n; m++) {
+      long long i = (m / st[d]) % g.nx[d];
+      if (xd[m] != xd[i * st[d]])
+        return fail("x is not a Cartesian product grid");
+    }
+    int N = g.nx[d];
+    std::vector<double> q(N + 6);  // qx over [ixGmin-1, ixGmax+1]
+    for (int i = 0; i < N; i++) q[i + 3] = xd[(long long)i * st[d]];
+    int ixe = N + 2, ixf = ixe - 1;  // upper layers
+    for (int ix = N + 3; ix <= N + 5; ix++) {
+      int c = std::abs(ixe - ix);
+      q[ix] = (1 + c) * q[ixe] - c * q[ixf];
+    }
+    ixe = 3;
+    ixf = 4;  // lower layers
+    for (int ix = 0; ix <= 2; ix++) {
+      int c = std::abs(ixe - ix);
+      q[ix] = (1 + c) * q[ixe] - c * q[ixf];
+    }
+    h->hdx[d].assign(N + 4, 0.0);
+    std::vector<float> f(N + 4);
+    for (int i = 0; i < N + 4; i++) {
+      h->hdx[d][i] = 0.5 * (q[i + 2] - q[i]);
+      f[i] = (float)h->hdx[d][i];
+      if (!(h->hdx[d][i] > 0.0)) return fail("grid spacing must be positive");
+    }
+    CK(cudaMemcpy(h->dx[d], h->hdx[d].data(), sizeof(double) * (N + 4),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->dxf[d], f.data(), sizeof(float) * (N + 4),
+                  cudaMemcpyHostToDevice));
+  }
+  for (int d = nd; d < 3; d++) {
+    double one = 1.0;
+    float onef = 1.0f;
+    CK(cudaMemcpy(h->dx[d], &one, sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->dxf[d], &onef, sizeof(float), cudaMemcpyHostToDevice));
+  }
+  double vol = 0.0;
+  for (int iz = 0; iz < g.nx[2]; iz++)
+    for (int iy = 0; iy < g.nx[1]; iy++)
+      for (int ix = 0; ix < g.nx[0]; ix++) {
+        double dv = h->hdx[0][ix + 2];
+        if (nd > 1) dv = dv * h->hdx[1][iy + 2];
+        if (nd > 2) dv = dv * h->hdx[2][iz + 2];
+        vol = vol + dv;
+      }
+  h->volume = vol;
+  h->have_grid = true;
+  return 0;
+}
+
+int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
+  if (!h) return fail("null handle");
+  const DevGrid& g = h->g;
+  long long n = g.ncell * h->nw;
+  CK(cudaMemcpyAsync(h->stage, w, sizeof(double) * n, cudaMemcpyHostToDevice,
+                     h->st));
+  unsigned nb = (unsigned)((n + 255) / 256);
+  SweepArgs a = make_args(h, 0, 0);
+  a.ctrl = nullptr;
+  if (h->elem == 8) {
+    k_scatter<double><<<nb, 256, 0, h->st>>>(h->stage, (double*)h->buf[0], g, h->nw);
+    launch_ghost_fp64(a, (double*)h->buf[0], h->st);
+  } else {
+    k_scatter<float><<<nb, 256, 0, h->st>>>(h->stage, (float*)h->buf[0], g, h->nw);
+    launch_ghost_mixed(a, (float*)h->buf[0], h->st);
+  }
+  CK(cudaGetLastError());
+  h->cur = 0;
+  // it, t, itmin (startup, src/vac.t:176) and the dt state of a fresh run
+  Ctrl c;
+  CK(cudaMemcpyAsync(&c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  c.it = it;
+  c.itmin = it;
+  c.t = t;
+  c.dt = 0.0;
+  c.dtold = 0.0;
+  c.done = 0;
+  c.dtpar = h->p.dtpar;
+  c.courantpar = h->ph.courantpar;
+  c.smallp = h->p.smallp;
+  for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
+  for (int i = 0; i < 4; i++) c.nerror[i] = 0;
+  c.dtgrav = h->dtgrav > 0 ? h->dtgrav : BIGD;
+  CK(cudaMemcpyAsync(h->ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->it_host = it;
+  h->have_state = true;
+  return 0;
+}
+
+int vacgpu_download(vacgpu_handle* h, double* w) {
+  if (!h) return fail("null handle");
+  const DevGrid& g = h->g;
+  long long n = g.ncell * h->nw;
+  unsigned nb = (unsigned)((n + 255) / 256);
+  if (h->elem == 8)
+    k_gather<double><<<nb, 256, 0, h->st>>>((const double*)h->buf[h->cur], h->stage, g, h->nw);
+  else
+    k_gather<float><<<nb, 256, 0, h->st>>>((const float*)h->buf[h->cur], h->stage, g, h->nw);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(w, h->stage, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                     h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
+                int* it, double* dt, int* finished) {
+  if (!h) return fail("null handle");
+  if (!h->have_grid || !h->have_state)
+    return fail("vacgpu_step before vacgpu_set_grid/vacgpu_upload");
+  if (maxsteps < 0) return fail("maxsteps must be >= 0");
+  const int nsw = h->p.dimsplit ? h->p.ndim : 1;
+  const int start_cur = h->cur;
+  k_call_begin<<<1, 1, 0, h->st>>>(h->ctrl, maxsteps, tstop);
+  CK(cudaGetLastError());
+  int issued = 0, chunk = 4;
+  Ctrl c;
+  while (issued < maxsteps) {
+    int k = maxsteps - issued < chunk ? maxsteps - issued : chunk;
+    for (int s = 0; s < k; s++) {
+      int par = (h->it_host + issued + s) & 1;
+      if (h->elem == 8)
+        run_step<double>(h, par);
+      else
+        run_step<float>(h, par);
+    }
+    issued += k;
+    CK(cudaGetLastError());
+    int done = 0;
+    CK(cudaMemcpyAsync(&done, &h->ctrl->done, sizeof(int),
+                       cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (done) break;
+    if (chunk < 64) chunk *= 2;
+  }
+  CK(cudaMemcpyAsync(&c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  // every executed step swapped the buffers nsw times; skipped ones none
+  h->cur = start_cur ^ ((c.steps * nsw) & 1);
+  h->it_host = c.it;
+  if (t) *t = c.t;
+  if (it) *it = c.it;
+  if (dt) *dt = c.dt;
+  if (finished) *finished = c.done == 1;
+  return 0;
+}
+
+int vacgpu_sums(vacgpu_handle* h, double* wmean) {
+  if (!h) return fail("null handle");
+  const DevGrid& g = h->g;
+  long long nblk = (g.ncell + 255) / 256;
+  if (h->elem == 8)
+    k_sums_partial<double><<<(unsigned)nblk, 256, 0, h->st>>>(
+        (const double*)h->buf[h->cur], g, h->nw, h->dx[0], h->dx[1], h->dx[2], h->part);
+  else
+    k_sums_partial<float><<<(unsigned)nblk, 256, 0, h->st>>>(
+        (const float*)h->buf[h->cur], g, h->nw, h->dx[0], h->dx[1], h->dx[2], h->part);
+  k_sums_final<<<1, 32, 0, h->st>>>(h->part, nblk, h->nw, h->sums);
+  CK(cudaGetLastError());
+  double s[8];
+  CK(cudaMemcpyAsync(s, h->sums, sizeof(double) * h->nw, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int iw = 0; iw < h->nw; iw++) wmean[iw] = s[iw] / h->volume;
+  return 0;
+}
+
+int vacgpu_error_counts(vacgpu_handle* h, int* nerror) {
+  if (!h) return fail("null handle");
+  Ctrl c;
+  CK(cudaMemcpyAsync(&c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int i = 0; i < 4; i++) nerror[i] = c.nerror[i];
+  return 0;
+}
+
+int vacgpu_register_source(vacgpu_handle* h, int source_id,
+                           const double* params, int nparams) {
+  if (!h) return fail("null handle");
+  if (source_id != VACGPU_SRC_NONE && source_id != VACGPU_SRC_GRAVITY)
+    return fail("unknown source id");
+  if (nparams < 0 || nparams > VACGPU_MAXSRCPAR) return fail("bad nparams");
+  if (!h->have_grid) return fail("register the source after vacgpu_set_grid");
+  h->ph.src_id = source_id;
+  for (int i = 0; i < VACGPU_MAXSRCPAR; i++)
+    h->ph.src_par[i] = i < nparams ? params[i] : 0.0;
+  // getdt_grav (vacusr.gravity.t): dtgrav = min_idim 1/sqrt(max(|g|/dx))
+  h->dtgrav = BIGD;
+  if (source_id == VACGPU_SRC_GRAVITY) {
+    for (int d = 0; d < h->p.ndim; d++) {
+      double gg = std::fabs(h->ph.src_par[d]);
+      if (gg > 0.0) {
+        double m = 0.0;
+        bool first = true;
+        for (int j = 0; j < h->p.ndim; j++)
+          for (int i = 2; i < h->g.nx[j] + 2; i++) {
+            double q = gg / h->hdx[j][i];
+            if (first || q > m) m = q;
+            first = false;
+          }
+        double c = 1.0 / std::sqrt(m);
+        if (c < h->dtgrav) h->dtgrav = c;
+      }
+    }
+  }
+  double v = h->dtgrav;
+  CK(cudaMemcpy(&h->ctrl->dtgrav, &v, sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+void vacgpu_destroy(vacgpu_handle* h) {
+  if (!h) return;
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (int i = 0; i < 3; i++) cudaFree(h->buf[i]);
+  cudaFree(h->wold);
+  for (int d = 0; d < 3; d++) {
+    cudaFree(h->dx[d]);
+    cudaFree(h->dxf[d]);
+  }
+  cudaFree(h->stage);
+  cudaFree(h->part);
+  cudaFree(h->sums);
+  cudaFree(h->ctrl);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+int vacgpu_last_error(char* buf, int len) {
+  int n = (int)g_err.size();
+  if (buf && len > 0) {
+    int m = n < len - 1 ? n : len - 1;
+    memcpy(buf, g_err.data(), m);
+    buf[m] = 0;
+  }
+  return n;
+}
+
+const char* vacgpu_version(void) { return "vacgpu 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// vacgpu_internal.h - device data layout, the device-resident control block
+// and the kernel launchers shared by the FP64 and mixed translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/vacgpu.h"
+
+namespace vacgpu {
+
+enum {
+  LIM_MINMOD = VACGPU_LIM_MINMOD,
+  LIM_WOODWARD = VACGPU_LIM_WOODWARD,
+  LIM_SUPERBEE = VACGPU_LIM_SUPERBEE,
+  LIM_VANLEER = VACGPU_LIM_VANLEER,
+  LIM_ALBADA = VACGPU_LIM_ALBADA
+};
+
+// Number of slots the grid-level max/min reductions spread their atomics
+// over (a block writes slot blockIdx % NSLOT); the step kernel folds them.
+constexpr int NSLOT = 128;
+
+// State layout in HBM: one padded box per variable (structure of arrays,
+// like VAC's w(ixG^T,nw)), x fastest.  A row holds the nG[0] cells of
+// ghost+mesh+ghost starting at column xpad, chosen so the first mesh cell
+// (gx=2) sits on a 128-byte boundary; rows have pitch P elements.
+struct DevGrid {
+  int ndim;
+  int nx[3];         // mesh cells (1 in unused dimensions)
+  int nG[3];         // with ghost layers (nx+4, or 1)
+  int gh[3];         // ghost width: 2 in used dimensions, 0 otherwise
+  int xpad;          // column of gx=0
+  long long P;       // row pitch (elements)
+  long long plane;   // P*nG[1]
+  long long vs;      // variable stride (elements)
+  long long ncell;   // mesh cells
+};
+
+__host__ __device__ inline long long gidx(const DevGrid& g, int gx, int gy,
+                                          int gz) {
+  return ((long long)gz * g.nG[1] + gy) * g.P + gx + g.xpad;
+}
+
+struct DevPhys {
+  double gamma, pt1, gm1, pt3;
+  double smallpcoeff;
+  double courantpar;  // <=0: no CFL evaluation (dtpar set)
+  int lim[VACGPU_MAXNW];
+  int typeB[VACGPU_MAXB][VACGPU_MAXNW];
+  int typefull;       // VACGPU_TVDLF / VACGPU_TVDLF1
+  int divbfix;
+  int sourceunsplit;
+  int src_id;
+  double src_par[VACGPU_MAXSRCPAR];
+};
+
+// Device-resident time-loop state: dt, it and t never leave the device
+// between steps, so a sequence of steps runs without host round trips (and
+// can be captured as one CUDA graph).
+struct Ctrl {
+  double t, dt, dtold, dtpar, courantpar;
+  double smallp;
+  double dtgrav;
+  double tstop;
+  double dtcourant[3];
+  int it, itmin;
+  int done;           // 0 running, 1 timetofinish, 2 tstop, 3 maxsteps
+  int steps;          // steps done in the current vacgpu_step call
+  int maxsteps;
+  int need_cell[3];   // this step's dt needs the cell-centred cmax pass
+  int need_smallp;    // smallp<0 at this step's first pressure evaluation
+  int nerror[4];
+  int pad;
+  // grid-level reductions (ordered-integer keys, atomicMax/atomicMin)
+  unsigned long long face_cmax[3][NSLOT];  // corrector max cmax*2/(dx+dx)
+  unsigned long long cell_cmax[3][NSLOT];  // getdt_courant max cmax/dx
+  unsigned long long pmin[NSLOT], pmax[NSLOT];
+};
+
+// Order-preserving map of a double onto unsigned 64-bit integers.
+__host__ __device__ inline unsigned long long dkey(double v) {
+  long long b;
+#ifdef __CUDA_ARCH__
+  b = __double_as_longlong(v);
+#else
+  memcpy(&b, &v, 8);
+#endif
+  return b < 0 ? ~(unsigned long long)b
+               : ((unsigned long long)b | 0x8000000000000000ULL);
+}
+__host__ __device__ inline double dkey_inv(unsigned long long k) {
+  long long b = (k & 0x8000000000000000ULL)
+                    ? (long long)(k & 0x7fffffffffffffffULL)
+                    : (long long)~k;
+  double v;
+#ifdef __CUDA_ARCH__
+  v = __longlong_as_double(b);
+#else
+  memcpy(&v, &b, 8);
+#endif
+  return v;
+}
+
+// Pointers of one grid's device arrays.
+struct DevArrays {
+  const double* dx[3];  // dx over the ghost-extended range, per dimension
+  const float* dxf[3];  // FP32 copies for the mixed path
+};
+
+// Launchers (sweep_fp64.cu, sweep_mixed.cu).  `w` is the state at the start
+// of the sweep, `w1` the predictor output, `wout` the corrected state.
+struct SweepArgs {
+  DevGrid g;
+  DevPhys ph;
+  DevArrays a;
+  Ctrl* ctrl;
+  int ndir, mhd;
+  int d0, d1;           // sweep dimensions (d0==d1 when split)
+  int typelimited;
+};
+
+// Precision-specific launchers (sweep_fp64.cu, sweep_mixed.cu).
+#define VACGPU_DECLARE_LAUNCHERS(SUF, T)                                      \
+  void launch_predict_##SUF(const SweepArgs& s, const T* w, T* w1,           \
+                            cudaStream_t st);                                \
+  void launch_correct_##SUF(const SweepArgs& s, const T* w, const T* w1,     \
+                            const T* base, T* wout, cudaStream_t st);        \
+  void launch_ghost_##SUF(const SweepArgs& s, T* w, cudaStream_t st);        \
+  void launch_pminmax_##SUF(const SweepArgs& s, const T* w, cudaStream_t st); \
+  void launch_cell_cmax_##SUF(const SweepArgs& s, const T* w,                \
+                              cudaStream_t st);
+VACGPU_DECLARE_LAUNCHERS(fp64, double)
+VACGPU_DECLARE_LAUNCHERS(mixed, float)
+VACGPU_DECLARE_LAUNCHERS(mixedf64, float)
+VACGPU_DECLARE_LAUNCHERS(mixedf32, float)
+
+// Precision-independent time-loop kernels (control.cu).
+void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st);
+void launch_smallp(Ctrl* c, int mhd, double smallpcoeff, cudaStream_t st);
+void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st);
+void launch_step_end(Ctrl* c, int ndim, cudaStream_t st);
+
+}  // namespace vacgpu

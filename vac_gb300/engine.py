@@ -1,0 +1,149 @@
+"""Python binding of the C ABI (``include/vacgpu.h``) through ctypes.
+
+This is how the tests, the benchmark and Python hosts drive the engine; it
+mirrors the sequence VAC's driver performs (readfileini -> gridsetup1 ->
+time loop -> savefile).  The shared library must have been built
+(``vac_gb300.build.build()``); there is no fallback path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "libvacgpu.so")
+
+SYMBOLS = [
+    "vacgpu_default_params", "vacgpu_create", "vacgpu_set_grid",
+    "vacgpu_upload", "vacgpu_download", "vacgpu_step", "vacgpu_sums",
+    "vacgpu_error_counts", "vacgpu_register_source", "vacgpu_destroy",
+    "vacgpu_last_error", "vacgpu_version",
+]
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(
+                "libvacgpu.so is not built (%s); run "
+                "python -c 'import __graft_entry__ as g; g.build()'" % LIB)
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int)
+        L.vacgpu_default_params.argtypes = [C.POINTER(abi.VacParams), C.c_int,
+                                            C.c_int, C.c_int, ip]
+        L.vacgpu_create.argtypes = [C.POINTER(abi.VacParams), C.POINTER(vp)]
+        L.vacgpu_set_grid.argtypes = [vp, dp]
+        L.vacgpu_upload.argtypes = [vp, dp, C.c_int, C.c_double]
+        L.vacgpu_download.argtypes = [vp, dp]
+        L.vacgpu_step.argtypes = [vp, C.c_int, C.c_double, dp, ip, dp, ip]
+        L.vacgpu_sums.argtypes = [vp, dp]
+        L.vacgpu_error_counts.argtypes = [vp, ip]
+        L.vacgpu_register_source.argtypes = [vp, C.c_int, dp, C.c_int]
+        L.vacgpu_destroy.argtypes = [vp]
+        L.vacgpu_destroy.restype = None
+        L.vacgpu_last_error.argtypes = [C.c_char_p, C.c_int]
+        L.vacgpu_version.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    lib().vacgpu_last_error(buf, 1024)
+    return buf.value.decode()
+
+
+def _ck(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s: %s" % (what, last_error()))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def pack_mesh(a):
+    a = np.asarray(a)
+    return np.concatenate([np.asarray(a[i]).ravel(order="F")
+                           for i in range(a.shape[0])])
+
+
+class Engine:
+    """One grid advanced on the GPU.  ``x``: (ndim, n1, ...) mesh
+    coordinates, ``w``: (nw, n1, ...) conservative state, both indexed like
+    VAC's x(ix^D,idim) and w(ix^D,iw)."""
+
+    def __init__(self, params, x, w, it=0, t=0.0):
+        L = lib()
+        self.p = params
+        h = C.c_void_p()
+        _ck(L.vacgpu_create(C.byref(params), C.byref(h)), "vacgpu_create")
+        self.h = h
+        self.nw = params.nw
+        self.nx = tuple(params.nx[d] for d in range(params.ndim))
+        xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)
+        _ck(L.vacgpu_set_grid(self.h, _dp(xf)), "vacgpu_set_grid")
+        self.upload(w, it, t)
+
+    def upload(self, w, it=0, t=0.0):
+        wf = np.ascontiguousarray(pack_mesh(w), dtype=np.float64)
+        _ck(lib().vacgpu_upload(self.h, _dp(wf), it, t), "vacgpu_upload")
+
+    def upload_flat(self, wflat, it=0, t=0.0):
+        """Upload a VAC-ordered flat FP64 host buffer (e.g. pinned memory)."""
+        _ck(lib().vacgpu_upload(self.h, C.cast(wflat, C.POINTER(C.c_double)),
+                                it, t), "vacgpu_upload")
+
+    def download_flat(self, out_ptr):
+        _ck(lib().vacgpu_download(self.h, C.cast(out_ptr, C.POINTER(C.c_double))),
+            "vacgpu_download")
+
+    def register_source(self, sid, par):
+        a = np.ascontiguousarray(par, dtype=np.float64)
+        _ck(lib().vacgpu_register_source(self.h, sid, _dp(a), len(a)),
+            "vacgpu_register_source")
+
+    def step(self, maxsteps, tstop=1e300):
+        t = C.c_double()
+        it = C.c_int()
+        dt = C.c_double()
+        fin = C.c_int()
+        _ck(lib().vacgpu_step(self.h, maxsteps, tstop, C.byref(t), C.byref(it),
+                              C.byref(dt), C.byref(fin)), "vacgpu_step")
+        self.t, self.it, self.dt = t.value, it.value, dt.value
+        return bool(fin.value)
+
+    def state(self):
+        n = int(np.prod(self.nx))
+        out = np.empty(self.nw * n, dtype=np.float64)
+        _ck(lib().vacgpu_download(self.h, _dp(out)), "vacgpu_download")
+        return np.stack([out[i * n:(i + 1) * n].reshape(self.nx, order="F")
+                         for i in range(self.nw)])
+
+    def sums(self):
+        out = np.empty(self.nw, dtype=np.float64)
+        _ck(lib().vacgpu_sums(self.h, _dp(out)), "vacgpu_sums")
+        return out
+
+    def nerror(self):
+        a = (C.c_int * 4)()
+        _ck(lib().vacgpu_error_counts(self.h, a), "vacgpu_error_counts")
+        return list(a)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vacgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
