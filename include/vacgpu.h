@@ -170,6 +170,36 @@ int vacgpu_error_counts(vacgpu_handle* h, int* nerror);
 int vacgpu_register_source(vacgpu_handle* h, int source_id,
                            const double* params, int nparams);
 
+/* Run the handle's work on the caller's CUDA stream (a cudaStream_t passed
+ * as void*; NULL returns to the handle's own stream).  No counterpart in the
+ * reference (VAC has no device); it lets a host order the engine's kernels
+ * with its own device work. */
+int vacgpu_set_stream(vacgpu_handle* h, void* stream);
+
+/* Kernel classes for vacgpu_kernel_stats. */
+enum {
+  VACGPU_K_PREDICT = 0, /* Hancock predictor (split kernels)              */
+  VACGPU_K_CORRECT = 1, /* TVDLF corrector (split kernels)                */
+  VACGPU_K_SWEEP = 2,   /* fused predictor+corrector sweep                */
+  VACGPU_K_GHOST = 3,   /* ghost-cell fill                                */
+  VACGPU_K_DT = 4,      /* cell-centred CFL / smallp passes               */
+  VACGPU_K_CONTROL = 5, /* single-block time-loop kernels                 */
+  VACGPU_K_NCLASS = 6
+};
+
+/* Device timing of the engine's kernels (no counterpart in the reference,
+ * which times its advance loop with the host clock, src/vac.t:52,115).
+ * enable=1 clears the statistics and brackets every following launch with
+ * CUDA events on the handle's stream; enable=0 stops bracketing.  Launch
+ * counts are kept whether or not timing is enabled. */
+int vacgpu_timing(vacgpu_handle* h, int enable);
+
+/* Launches of kernel class kclass since the last vacgpu_timing(h,1) (or
+ * since creation) and, when timing was enabled, their summed device time in
+ * milliseconds.  Synchronises the handle's stream. */
+int vacgpu_kernel_stats(vacgpu_handle* h, int kclass, long long* launches,
+                        double* ms);
+
 /* Release the handle and its device memory. */
 void vacgpu_destroy(vacgpu_handle* h);
 

@@ -68,7 +68,19 @@ static long IDX(const vo_state* s, int i1, int i2, int i3) {
   return (long)i1 + s->st[1] * i2 + s->st[2] * i3;
 }
 
+/* Elementwise array statement over a box.  Every use is a pure elementwise
+ * update (no element reads a value another element of the same statement
+ * writes), so the rows may run on several threads without changing a bit. */
 #define FORBOX(b, ix)                                            \
+  _Pragma("omp parallel for collapse(2) schedule(static)")       \
+  for (int i3_ = (b).lo[2]; i3_ <= (b).hi[2]; i3_++)             \
+    for (int i2_ = (b).lo[1]; i2_ <= (b).hi[1]; i2_++)           \
+      for (long ix = IDX(s, (b).lo[0], i2_, i3_),                \
+                ixend_ = IDX(s, (b).hi[0], i2_, i3_);            \
+           ix <= ixend_; ix++)
+
+/* Sequential loop over a box (reductions: min/max/sum in column order). */
+#define FORBOX_SEQ(b, ix)                                        \
   for (int i3_ = (b).lo[2]; i3_ <= (b).hi[2]; i3_++)             \
     for (int i2_ = (b).lo[1]; i2_ <= (b).hi[1]; i2_++)           \
       for (long ix = IDX(s, (b).lo[0], i2_, i3_),                \
@@ -116,7 +128,7 @@ static void init_smallp(vo_state* s, const double* p, box b) {
   if (s->smallp < ZERO) {
     double mn = BIGDOUBLE, mx = -BIGDOUBLE;
     int first = 1;
-    FORBOX(b, ix) {
+    FORBOX_SEQ(b, ix) {
       if (first) { mn = p[ix]; mx = p[ix]; first = 0; }
       if (p[ix] < mn) mn = p[ix];
       if (p[ix] > mx) mx = p[ix];
@@ -566,7 +578,7 @@ static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
       const double* dx = W(s->dx, idim);
       double courantmax = 0.0;
       int first = 1;
-      FORBOX(ixC, ix) {
+      FORBOX_SEQ(ixC, ix) {
         double q = s->cmaxC[ix] * TWO / (dx[ix] + dx[ix + sh]);
         if (first || q > courantmax) courantmax = q;
         first = 0;
@@ -648,7 +660,7 @@ static void getdt_courant(vo_state* s) {
       const double* dx = W(s->dx, idim);
       double m = 0.0;
       int first = 1;
-      FORBOX(s->ixM, ix) {
+      FORBOX_SEQ(s->ixM, ix) {
         double q = s->cmaxC[ix] / dx[ix];
         if (first || q > m) m = q;
         first = 0;
@@ -675,7 +687,7 @@ static void getdt_special(vo_state* s) {
         int first = 1;
         for (int jdim = 0; jdim < s->ndim; jdim++) {
           const double* dx = W(s->dx, jdim);
-          FORBOX(s->ixM, ix) {
+          FORBOX_SEQ(s->ixM, ix) {
             double q = g / dx[ix];
             if (first || q > m) m = q;
             first = 0;
@@ -843,14 +855,14 @@ int vo_set_grid(vo_state* s, const double* xmesh) {
 #undef QX
   free(qx);
   s->volume = 0.0;
-  FORBOX(s->ixM, ix) s->volume = s->volume + s->dvolume[ix];
+  FORBOX_SEQ(s->ixM, ix) s->volume = s->volume + s->dvolume[ix];
   return 0;
 }
 
 /* w(ixM^S,1:nw) from the .ini; ghosts by getboundary (src/vac.t:54) */
 void vo_set_state(vo_state* s, const double* wmesh, int it, double t) {
   long k = 0;
-  for (int iw = 0; iw < s->nw; iw++) FORBOX(s->ixM, ix) W(s->w, iw)[ix] = wmesh[k++];
+  for (int iw = 0; iw < s->nw; iw++) FORBOX_SEQ(s->ixM, ix) W(s->w, iw)[ix] = wmesh[k++];
   s->it = it;
   s->itmin = it;
   s->t = t;
@@ -859,7 +871,7 @@ void vo_set_state(vo_state* s, const double* wmesh, int it, double t) {
 
 void vo_get_state(vo_state* s, double* wmesh) {
   long k = 0;
-  for (int iw = 0; iw < s->nw; iw++) FORBOX(s->ixM, ix) wmesh[k++] = W(s->w, iw)[ix];
+  for (int iw = 0; iw < s->nw; iw++) FORBOX_SEQ(s->ixM, ix) wmesh[k++] = W(s->w, iw)[ix];
 }
 
 /* full ixG state (test access to ghosts) */
@@ -940,7 +952,7 @@ void vo_get_x(vo_state* s, int idim, double* out) {
 void vo_sums(vo_state* s, double* wmean) {
   for (int iw = 0; iw < s->nw; iw++) {
     double acc = 0.0;
-    FORBOX(s->ixM, ix) acc = acc + s->dvolume[ix] * W(s->w, iw)[ix];
+    FORBOX_SEQ(s->ixM, ix) acc = acc + s->dvolume[ix] * W(s->w, iw)[ix];
     wmean[iw] = acc / s->volume;
   }
 }

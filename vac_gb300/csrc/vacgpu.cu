@@ -138,9 +138,60 @@ struct vacgpu_handle {
   double dtgrav;
   bool have_grid, have_state;
   int pmode;         // mixed pressure variant (0 ff, 1 native f64, 2 f32)
+  cudaStream_t own_st;
+  // kernel statistics
+  long long nlaunch[VACGPU_K_NCLASS];
+  double kms[VACGPU_K_NCLASS];
+  bool timing;
+  struct Ev {
+    int k;
+    cudaEvent_t a, b;
+  };
+  std::vector<Ev> pending;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t open_ev;
+  int open_k;
 };
 
 namespace {
+
+cudaEvent_t get_event(vacgpu_handle* h) {
+  if (!h->pool.empty()) {
+    cudaEvent_t e = h->pool.back();
+    h->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Bracket the next launch of class k (events only while timing is on).
+void kbegin(vacgpu_handle* h, int k) {
+  h->nlaunch[k]++;
+  if (!h->timing) return;
+  h->open_ev = get_event(h);
+  h->open_k = k;
+  cudaEventRecord(h->open_ev, h->st);
+}
+void kend(vacgpu_handle* h) {
+  if (!h->timing) return;
+  cudaEvent_t b = get_event(h);
+  cudaEventRecord(b, h->st);
+  h->pending.push_back({h->open_k, h->open_ev, b});
+}
+
+void drain_events(vacgpu_handle* h) {
+  for (auto& e : h->pending) {
+    cudaEventSynchronize(e.b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    h->kms[e.k] += ms;
+    h->pool.push_back(e.a);
+    h->pool.push_back(e.b);
+  }
+  h->pending.clear();
+}
 
 SweepArgs make_args(vacgpu_handle* h, int d0, int d1) {
   SweepArgs a;
@@ -170,35 +221,43 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   if (h->p.typelimited == VACGPU_LIMITED_PREVIOUS && h->p.dimsplit)
     base = (const T*)h->wold;
   if (sizeof(T) == 8) {
+    kbegin(h, VACGPU_K_PREDICT);
     launch_predict_fp64(a, (const double*)w, (double*)w1, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_GHOST);
     launch_ghost_fp64(a, (double*)w1, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_CORRECT);
     launch_correct_fp64(a, (const double*)w, (const double*)w1,
                         (const double*)base, (double*)wout, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_GHOST);
     launch_ghost_fp64(a, (double*)wout, h->st);
+    kend(h);
   } else {
     const float* fw = (const float*)w;
     float* fw1 = (float*)w1;
     float* fo = (float*)wout;
     const float* fb = (const float*)base;
+#define MIXED_SWEEP(SUF)                                \
+  kbegin(h, VACGPU_K_PREDICT);                          \
+  launch_predict_##SUF(a, fw, fw1, h->st);              \
+  kend(h);                                              \
+  kbegin(h, VACGPU_K_GHOST);                            \
+  launch_ghost_##SUF(a, fw1, h->st);                    \
+  kend(h);                                              \
+  kbegin(h, VACGPU_K_CORRECT);                          \
+  launch_correct_##SUF(a, fw, fw1, fb, fo, h->st);      \
+  kend(h);                                              \
+  kbegin(h, VACGPU_K_GHOST);                            \
+  launch_ghost_##SUF(a, fo, h->st);                     \
+  kend(h);
     switch (h->pmode) {
-      case 1:
-        launch_predict_mixedf64(a, fw, fw1, h->st);
-        launch_ghost_mixedf64(a, fw1, h->st);
-        launch_correct_mixedf64(a, fw, fw1, fb, fo, h->st);
-        launch_ghost_mixedf64(a, fo, h->st);
-        break;
-      case 2:
-        launch_predict_mixedf32(a, fw, fw1, h->st);
-        launch_ghost_mixedf32(a, fw1, h->st);
-        launch_correct_mixedf32(a, fw, fw1, fb, fo, h->st);
-        launch_ghost_mixedf32(a, fo, h->st);
-        break;
-      default:
-        launch_predict_mixed(a, fw, fw1, h->st);
-        launch_ghost_mixed(a, fw1, h->st);
-        launch_correct_mixed(a, fw, fw1, fb, fo, h->st);
-        launch_ghost_mixed(a, fo, h->st);
+      case 1: MIXED_SWEEP(mixedf64) break;
+      case 2: MIXED_SWEEP(mixedf32) break;
+      default: MIXED_SWEEP(mixed)
     }
+#undef MIXED_SWEEP
   }
   h->cur ^= 1;
 }
@@ -207,18 +266,34 @@ template <typename T>
 void run_step(vacgpu_handle* h, int parity_odd) {
   const vacgpu_params& p = h->p;
   SweepArgs a = make_args(h, 0, p.ndim - 1);
+  kbegin(h, VACGPU_K_CONTROL);
   launch_dt_begin(h->ctrl, p.ndim, h->st);
+  kend(h);
   const T* w = (const T*)h->buf[h->cur];
   if (sizeof(T) == 8) {
+    kbegin(h, VACGPU_K_DT);
     launch_pminmax_fp64(a, (const double*)w, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_CONTROL);
     launch_smallp(h->ctrl, a.mhd, p.smallpcoeff, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_DT);
     launch_cell_cmax_fp64(a, (const double*)w, h->st);
+    kend(h);
   } else {
+    kbegin(h, VACGPU_K_DT);
     launch_pminmax_mixed(a, (const float*)w, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_CONTROL);
     launch_smallp(h->ctrl, a.mhd, p.smallpcoeff, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_DT);
     launch_cell_cmax_mixed(a, (const float*)w, h->st);
+    kend(h);
   }
+  kbegin(h, VACGPU_K_CONTROL);
   launch_dt_end(h->ctrl, p, h->st);
+  kend(h);
   if (p.typelimited == VACGPU_LIMITED_PREVIOUS && p.dimsplit)
     cudaMemcpyAsync(h->wold, h->buf[h->cur], h->elem * h->g.vs * h->nw,
                     cudaMemcpyDeviceToDevice, h->st);
@@ -231,7 +306,9 @@ void run_step(vacgpu_handle* h, int parity_odd) {
   } else {
     run_sweep<T>(h, 0, p.ndim - 1);
   }
+  kbegin(h, VACGPU_K_CONTROL);
   launch_step_end(h->ctrl, p.ndim, h->st);
+  kend(h);
 }
 
 int check_params(const vacgpu_params* p) {
@@ -370,6 +447,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   if (e == cudaSuccess) e = cudaMalloc(&h->sums, sizeof(double) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&h->ctrl, sizeof(Ctrl));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  h->own_st = h->st;
   if (e != cudaSuccess) {
     vacgpu_destroy(h);
     return fail(std::string("device allocation failed: ") + cudaGetErrorString(e));
@@ -520,7 +598,9 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   if (maxsteps < 0) return fail("maxsteps must be >= 0");
   const int nsw = h->p.dimsplit ? h->p.ndim : 1;
   const int start_cur = h->cur;
+  kbegin(h, VACGPU_K_CONTROL);
   k_call_begin<<<1, 1, 0, h->st>>>(h->ctrl, maxsteps, tstop);
+  kend(h);
   CK(cudaGetLastError());
   int issued = 0, chunk = 4;
   Ctrl c;
@@ -619,6 +699,7 @@ int vacgpu_register_source(vacgpu_handle* h, int source_id,
 void vacgpu_destroy(vacgpu_handle* h) {
   if (!h) return;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->own_st) cudaStreamSynchronize(h->own_st);
   for (int i = 0; i < 3; i++) cudaFree(h->buf[i]);
   cudaFree(h->wold);
   for (int d = 0; d < 3; d++) {
@@ -629,8 +710,42 @@ void vacgpu_destroy(vacgpu_handle* h) {
   cudaFree(h->part);
   cudaFree(h->sums);
   cudaFree(h->ctrl);
-  if (h->st) cudaStreamDestroy(h->st);
+  drain_events(h);
+  for (auto e : h->pool) cudaEventDestroy(e);
+  if (h->own_st) cudaStreamDestroy(h->own_st);
   delete h;
+}
+
+int vacgpu_set_stream(vacgpu_handle* h, void* stream) {
+  if (!h) return fail("null handle");
+  CK(cudaStreamSynchronize(h->st));
+  h->st = stream ? (cudaStream_t)stream : h->own_st;
+  return 0;
+}
+
+int vacgpu_timing(vacgpu_handle* h, int enable) {
+  if (!h) return fail("null handle");
+  CK(cudaStreamSynchronize(h->st));
+  drain_events(h);
+  if (enable) {
+    for (int k = 0; k < VACGPU_K_NCLASS; k++) {
+      h->nlaunch[k] = 0;
+      h->kms[k] = 0.0;
+    }
+  }
+  h->timing = enable != 0;
+  return 0;
+}
+
+int vacgpu_kernel_stats(vacgpu_handle* h, int kclass, long long* launches,
+                        double* ms) {
+  if (!h) return fail("null handle");
+  if (kclass < 0 || kclass >= VACGPU_K_NCLASS) return fail("bad kernel class");
+  CK(cudaStreamSynchronize(h->st));
+  drain_events(h);
+  if (launches) *launches = h->nlaunch[kclass];
+  if (ms) *ms = h->kms[kclass];
+  return 0;
 }
 
 int vacgpu_last_error(char* buf, int len) {

@@ -19,8 +19,12 @@ SYMBOLS = [
     "vacgpu_default_params", "vacgpu_create", "vacgpu_set_grid",
     "vacgpu_upload", "vacgpu_download", "vacgpu_step", "vacgpu_sums",
     "vacgpu_error_counts", "vacgpu_register_source", "vacgpu_destroy",
-    "vacgpu_last_error", "vacgpu_version",
+    "vacgpu_last_error", "vacgpu_version", "vacgpu_set_stream",
+    "vacgpu_timing", "vacgpu_kernel_stats",
 ]
+
+K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
+K_NAMES = ["predict", "correct", "sweep", "ghost", "dt", "control"]
 
 _lib = None
 
@@ -50,6 +54,9 @@ def lib():
         L.vacgpu_destroy.restype = None
         L.vacgpu_last_error.argtypes = [C.c_char_p, C.c_int]
         L.vacgpu_version.restype = C.c_char_p
+        L.vacgpu_set_stream.argtypes = [vp, vp]
+        L.vacgpu_timing.argtypes = [vp, C.c_int]
+        L.vacgpu_kernel_stats.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong), dp]
         _lib = L
     return _lib
 
@@ -136,6 +143,26 @@ class Engine:
         a = (C.c_int * 4)()
         _ck(lib().vacgpu_error_counts(self.h, a), "vacgpu_error_counts")
         return list(a)
+
+    def set_stream(self, stream_ptr):
+        """Run on a caller-owned cudaStream_t (int handle, e.g.
+        torch.cuda.Stream().cuda_stream); None returns to the own stream."""
+        _ck(lib().vacgpu_set_stream(self.h, C.c_void_p(stream_ptr or 0)),
+            "vacgpu_set_stream")
+
+    def timing(self, enable):
+        _ck(lib().vacgpu_timing(self.h, 1 if enable else 0), "vacgpu_timing")
+
+    def kernel_stats(self):
+        """{class name: (launches, device ms)}"""
+        out = {}
+        for k, name in enumerate(K_NAMES):
+            n = C.c_longlong()
+            ms = C.c_double()
+            _ck(lib().vacgpu_kernel_stats(self.h, k, C.byref(n), C.byref(ms)),
+                "vacgpu_kernel_stats")
+            out[name] = (n.value, ms.value)
+        return out
 
     def close(self):
         if getattr(self, "h", None):
