@@ -200,6 +200,54 @@ int vacgpu_timing(vacgpu_handle* h, int enable);
 int vacgpu_kernel_stats(vacgpu_handle* h, int kclass, long long* launches,
                         double* ms);
 
+/* Largest grid vacgpu_sweep_noalloc accepts, in cells including the ghost
+ * layers (prod over the used dimensions of nx+4): 262144 cells, e.g. 508^2
+ * in 2-D or 60^3 in 3-D.  Its scratch is a fixed 16 MiB FP64 device array
+ * (8 variables) that every GPU which loads the library holds until exit. */
+#define VACGPU_NOALLOC_MAX_GCELLS 262144
+
+/* One dimensional sweep of the split twostep scheme in FP64 -- the Hancock
+ * predictor over dt/2, the TVDLF corrector over dt, the unsplit sources of
+ * both substeps and the ghost-cell fill of both results, exactly as one
+ * advect(idim,idim) of vacgpu_step -- on device arrays the caller owns, and
+ * without allocating device memory.  No counterpart in the reference (VAC
+ * has no device and allocates nothing on one).
+ *
+ * It exists for callers that cannot call cudaMalloc: hosts that record the
+ * call into their own CUDA graph or stream capture (where an allocation is
+ * not allowed), hosts that own all device memory through their own pool,
+ * and latency-bound loops where cudaMalloc/cudaFree would synchronise the
+ * device.  The predictor's intermediate state and the CFL reduction slots
+ * live in a static device array of the library instead; the caller passes
+ * inputs and outputs.
+ *
+ *  p           run parameters (dimsplit, typelimited original or predictor,
+ *              precision FP64; smallp >= 0 must be given, dtpar unused)
+ *  w, wout     device FP64 arrays in VAC's full-grid layout w(ixG^T,nw),
+ *              column-major, nx+4 cells per used dimension; w must hold
+ *              valid ghost cells; wout receives mesh and ghost cells
+ *              (w and wout must not overlap)
+ *  dx0,dx1,dx2 device FP64 arrays of dx along each used dimension over the
+ *              ghost-extended range (nx+4 values; what vacgpu_set_grid
+ *              derives with gridsetup1); unused dimensions may be NULL
+ *  dt          the time step (qdt of the corrector)
+ *  idim        sweep direction, 0-based
+ *  courantmax  device pointer (or NULL) receiving the corrector's
+ *              max cmax*2/(dx_i+dx_i+1) over the faces of this sweep, the
+ *              value VAC folds into dtcourant(idim) (src/vactvdlf.t:184-201)
+ *  stream      cudaStream_t as void* (NULL = legacy default stream)
+ *
+ * The first call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress) for that device, with that device current; make
+ * that first call before any stream capture.  Every call shares the one
+ * scratch array, so calls that overlap on the GPU (different streams or
+ * host threads) race: serialise them.  Grids larger than
+ * VACGPU_NOALLOC_MAX_GCELLS are rejected with an error. */
+int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
+                         double* wout, const double* dx0, const double* dx1,
+                         const double* dx2, double dt, int idim,
+                         double* courantmax, void* stream);
+
 /* Release the handle and its device memory. */
 void vacgpu_destroy(vacgpu_handle* h);
 

@@ -25,6 +25,7 @@ UNITS = [
     ("control.cu", ["-fmad=false"]),
     ("sweep_mixed.cu", []),
     ("vacgpu.cu", []),
+    ("noalloc.cu", []),
 ]
 
 

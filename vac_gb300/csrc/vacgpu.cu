@@ -116,6 +116,8 @@ __global__ void k_call_begin(Ctrl* c, int maxsteps, double tstop) {
 
 }  // namespace
 
+int vacgpu_internal_fail(const char* msg) { return fail(msg); }
+
 struct vacgpu_handle {
   vacgpu_params p;
   DevGrid g;

@@ -20,7 +20,7 @@ SYMBOLS = [
     "vacgpu_upload", "vacgpu_download", "vacgpu_step", "vacgpu_sums",
     "vacgpu_error_counts", "vacgpu_register_source", "vacgpu_destroy",
     "vacgpu_last_error", "vacgpu_version", "vacgpu_set_stream",
-    "vacgpu_timing", "vacgpu_kernel_stats",
+    "vacgpu_timing", "vacgpu_kernel_stats", "vacgpu_sweep_noalloc",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
@@ -57,6 +57,8 @@ def lib():
         L.vacgpu_set_stream.argtypes = [vp, vp]
         L.vacgpu_timing.argtypes = [vp, C.c_int]
         L.vacgpu_kernel_stats.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong), dp]
+        L.vacgpu_sweep_noalloc.argtypes = [C.POINTER(abi.VacParams), vp, vp, vp,
+                                           vp, vp, C.c_double, C.c_int, vp, vp]
         _lib = L
     return _lib
 
