@@ -1,0 +1,89 @@
+"""The fused single-kernel sweep of the mixed path (TMA-fed z-marching
+tiles): against the FP64 oracle within the mixed tolerance, and against the
+split predictor/corrector kernels of the same precision, on periodic,
+outflow ('cont') and reflecting ('symm'/'asymm') boundaries and on grids that
+are not multiples of the 32x8 tile."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from vac_gb300 import abi, inistate
+from vac_gb300.engine import Engine
+
+pytestmark = pytest.mark.gpu
+
+MIXED_REL_L1 = 1e-5     # mixed path vs FP64 oracle, per variable
+FUSED_VS_SPLIT = 1e-6   # fused vs split FP32 kernels (different rounding only)
+
+
+def rel_l1(a, b):
+    return [float(np.abs(a[i] - b[i]).sum() / max(np.abs(b[i]).sum(), 1e-300))
+            for i in range(a.shape[0])]
+
+
+def reflecting(p, ndim):
+    """symm walls, asymm for the normal momentum (and normal B)."""
+    for d in range(ndim):
+        for side in (0, 1):
+            for iw in range(p.nw):
+                p.typeB[2 * d + side][iw] = abi.BC_SYMM
+            p.typeB[2 * d + side][1 + d] = abi.BC_ASYMM
+            if p.physics == abi.PHYS_MHD:
+                p.typeB[2 * d + side][p.ndir + 2 + d] = abi.BC_ASYMM
+
+
+def _blast(n):
+    s = inistate.blast_3d(n)
+    return s
+
+
+CASES = [
+    ("rm3-periodic-40", lambda: inistate.random_modes(40, seed=4), "woodward", "periodic", 12, None),
+    ("blast3-cont-36", lambda: _blast(36), "woodward", "cont", 10, None),
+    ("rm3-reflect-33", lambda: inistate.random_modes(33, seed=5), "minmod", "symm", 8,
+     lambda p: reflecting(p, 3)),
+    ("hd2-cont-70x50", lambda: _hd(70, 50), "minmod", "cont", 20, None),
+    ("ot2-periodic-64", lambda: inistate.orszag_tang(64), "minmod", "periodic", 30, None),
+    ("ot2-reflect-45", lambda: inistate.orszag_tang(45), "woodward", "symm", 15,
+     lambda p: reflecting(p, 2)),
+]
+
+
+def _hd(nx, ny):
+    s = inistate.riemann_2d(8, 11)
+    x = inistate.domain_grid((nx, ny), (0.0, 0.0), (1.0, 1.0))
+    X, Y = x
+    left = X + 0.3 * Y < 0.6
+    rho = np.where(left, 1.0, 0.125)
+    p = np.where(left, 1.0, 0.1)
+    w = inistate.conserve_hd(rho, [np.where(left, 0.2, -0.1), np.zeros_like(X)], p, 1.4)
+    s.x, s.w, s.nx = x, w, (nx, ny)
+    return s
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak", CASES, ids=[c[0] for c in CASES])
+def test_fused_against_oracle_and_split(gpu_lib, monkeypatch, name, mk, lim, bc, n, tweak):
+    s = mk()
+    p64 = inistate.params_for(s, limiter=lim, bc=bc)
+    pm = inistate.params_for(s, limiter=lim, bc=bc, precision=abi.PREC_MIXED)
+    if tweak:
+        tweak(p64)
+        tweak(pm)
+    o = Oracle(p64, s.x, s.w)
+    o.step(n)
+    ref = o.state()
+    monkeypatch.setenv("VACGPU_FUSED", "1")
+    ef = Engine(pm, s.x, s.w)
+    ef.step(n)
+    wf = ef.state()
+    st = ef.kernel_stats()
+    assert st["sweep"][0] > 0, "fused kernel did not run"
+    monkeypatch.setenv("VACGPU_FUSED", "0")
+    es = Engine(pm, s.x, s.w)
+    es.step(n)
+    ws = es.state()
+    assert es.kernel_stats()["sweep"][0] == 0
+    assert max(rel_l1(wf, ref)) <= MIXED_REL_L1, rel_l1(wf, ref)
+    assert max(rel_l1(wf, ws)) <= FUSED_VS_SPLIT, rel_l1(wf, ws)

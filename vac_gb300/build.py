@@ -26,6 +26,7 @@ UNITS = [
     ("sweep_mixed.cu", []),
     ("vacgpu.cu", []),
     ("noalloc.cu", []),
+    ("sweep_fused.cu", []),
 ]
 
 

@@ -1,0 +1,62 @@
+// sweep_fused.cu - instances and launcher of the fused mixed-precision sweep.
+#include "sweep_fused.cuh"
+
+namespace vacgpu {
+
+int fused_smem_bytes(int nw) { return fused_smem_floats(nw) * 4; }
+
+template <int NDIM, int D, bool MHD>
+static void launch_one(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
+                       cudaStream_t st) {
+  constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
+  const int smem = fused_smem_floats(NW) * 4;
+  auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  k<<<grid, FT_NT, smem, st>>>(*map, a);
+}
+
+bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
+                        const float* const* idxf, int nzc, cudaStream_t st) {
+  const int nd = s.g.ndim;
+  if (s.d0 != s.d1 || s.ndir != nd || (nd != 2 && nd != 3)) return false;
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.g = s.g;
+  a.ph = s.ph;
+  for (int d = 0; d < 3; d++) {
+    a.dxf[d] = s.a.dxf[d];
+    a.idxf[d] = idxf[d];
+  }
+  a.ctrl = s.ctrl;
+  a.wout = wout;
+  a.nzc = nzc;
+  const int nw = s.mhd ? 2 + 2 * s.ndir : 2 + s.ndir;
+  for (int d = 0; d < 3; d++)
+    for (int v = 0; v < nw; v++) {
+      if (s.ph.typeB[2 * d][v] == VACGPU_BC_PERIODIC) a.periodic_mask[d] |= 1 << v;
+      if (s.ph.typeB[2 * d][v] == VACGPU_BC_ASYMM) a.asymm_lo[d] |= 1 << v;
+      if (s.ph.typeB[2 * d + 1][v] == VACGPU_BC_ASYMM) a.asymm_hi[d] |= 1 << v;
+    }
+  dim3 grid((s.g.nx[0] + FT_X - 1) / FT_X, (s.g.nx[1] + FT_Y - 1) / FT_Y,
+            nd == 3 ? (s.g.nx[2] + nzc - 1) / nzc : 1);
+  a.zchunks = grid.z;
+  const CUtensorMap* map = (const CUtensorMap*)tmap;
+  const int D = s.d0;
+#define L1(ND, DD)                                              \
+  if (nd == ND && D == DD) {                                    \
+    if (s.mhd)                                                  \
+      launch_one<ND, DD, true>(map, a, grid, st);               \
+    else                                                        \
+      launch_one<ND, DD, false>(map, a, grid, st);              \
+    return true;                                                \
+  }
+  L1(2, 0) L1(2, 1) L1(3, 0) L1(3, 1) L1(3, 2)
+#undef L1
+  return false;
+}
+
+}  // namespace vacgpu

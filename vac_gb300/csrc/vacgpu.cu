@@ -1,6 +1,8 @@
 // vacgpu.cu - the C ABI of include/vacgpu.h: handle life cycle, grid set-up
 // (gridsetup1), state transfer, the device-resident time loop and the
 // conservation sums.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -153,6 +155,11 @@ struct vacgpu_handle {
   std::vector<cudaEvent_t> pool;
   cudaEvent_t open_ev;
   int open_k;
+  // fused mixed sweep: TMA descriptors of the two state buffers, 1/dx
+  bool fused;
+  CUtensorMap tmap[2];
+  float* idxf[3];
+  int nzc;
 };
 
 namespace {
@@ -195,6 +202,40 @@ void drain_events(vacgpu_handle* h) {
   h->pending.clear();
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library links the CUDA runtime statically and not libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 4-D map over one FP32 state buffer: (column, gy, gz, variable), box
+// {40, 12, 1, nw} = one plane of a 32x8 tile with its 2-cell halo.
+bool make_tmap(vacgpu_handle* h, void* base, CUtensorMap* m) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const DevGrid& g = h->g;
+  cuuint64_t dims[4] = {(cuuint64_t)g.P, (cuuint64_t)g.nG[1],
+                        (cuuint64_t)g.nG[2], (cuuint64_t)h->nw};
+  cuuint64_t strides[3] = {(cuuint64_t)g.P * 4, (cuuint64_t)g.plane * 4,
+                           (cuuint64_t)g.vs * 4};
+  cuuint32_t box[4] = {40, 12, 1, (cuuint32_t)h->nw};
+  cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides,
+                  box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 SweepArgs make_args(vacgpu_handle* h, int d0, int d1) {
   SweepArgs a;
   a.g = h->g;
@@ -235,6 +276,14 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
     launch_ghost_fp64(a, (double*)wout, h->st);
+    kend(h);
+  } else if (h->fused && h->pmode == 0 && d0 == d1) {
+    kbegin(h, VACGPU_K_SWEEP);
+    launch_sweep_fused(a, &h->tmap[h->cur], (float*)wout, h->idxf, h->nzc,
+                       h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_GHOST);
+    launch_ghost_mixed(a, (float*)wout, h->st);
     kend(h);
   } else {
     const float* fw = (const float*)w;
@@ -454,6 +503,22 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     vacgpu_destroy(h);
     return fail(std::string("device allocation failed: ") + cudaGetErrorString(e));
   }
+  h->nzc = 32;
+  if (const char* nz = getenv("VACGPU_NZC")) h->nzc = atoi(nz) > 0 ? atoi(nz) : 32;
+  h->fused = p->precision == VACGPU_PREC_MIXED && p->dimsplit &&
+             (p->ndim == 2 || p->ndim == 3) && p->ndir == p->ndim &&
+             p->typelimited == VACGPU_LIMITED_ORIGINAL;
+  if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
+  if (h->fused) {
+    bool ok = true;
+    for (int i = 0; i < 2 && ok; i++) ok = make_tmap(h, h->buf[i], &h->tmap[i]);
+    for (int d = 0; d < 3 && ok; d++)
+      ok = cudaMalloc(&h->idxf[d], sizeof(float) * g.nG[d]) == cudaSuccess;
+    if (!ok) {
+      vacgpu_destroy(h);
+      return fail("TMA descriptor set-up failed");
+    }
+  }
   Ctrl c;
   memset(&c, 0, sizeof(c));
   c.dtpar = p->dtpar;
@@ -514,12 +579,20 @@ int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
                   cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->dxf[d], f.data(), sizeof(float) * (N + 4),
                   cudaMemcpyHostToDevice));
+    if (h->idxf[d]) {
+      std::vector<float> fi(N + 4);
+      for (int i = 0; i < N + 4; i++) fi[i] = (float)(1.0 / h->hdx[d][i]);
+      CK(cudaMemcpy(h->idxf[d], fi.data(), sizeof(float) * (N + 4),
+                    cudaMemcpyHostToDevice));
+    }
   }
   for (int d = nd; d < 3; d++) {
     double one = 1.0;
     float onef = 1.0f;
     CK(cudaMemcpy(h->dx[d], &one, sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->dxf[d], &onef, sizeof(float), cudaMemcpyHostToDevice));
+    if (h->idxf[d])
+      CK(cudaMemcpy(h->idxf[d], &onef, sizeof(float), cudaMemcpyHostToDevice));
   }
   double vol = 0.0;
   for (int iz = 0; iz < g.nx[2]; iz++)
@@ -628,6 +701,7 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   CK(cudaStreamSynchronize(h->st));
   // every executed step swapped the buffers nsw times; skipped ones none
   h->cur = start_cur ^ ((c.steps * nsw) & 1);
+  if (c.fault) return fail("a device wait timed out (TMA copy never completed)");
   h->it_host = c.it;
   if (t) *t = c.t;
   if (it) *it = c.it;
@@ -707,6 +781,7 @@ void vacgpu_destroy(vacgpu_handle* h) {
   for (int d = 0; d < 3; d++) {
     cudaFree(h->dx[d]);
     cudaFree(h->dxf[d]);
+    cudaFree(h->idxf[d]);
   }
   cudaFree(h->stage);
   cudaFree(h->part);

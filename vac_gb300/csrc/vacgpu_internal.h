@@ -71,7 +71,7 @@ struct Ctrl {
   int need_cell[3];   // this step's dt needs the cell-centred cmax pass
   int need_smallp;    // smallp<0 at this step's first pressure evaluation
   int nerror[4];
-  int pad;
+  int fault;          // a bounded device wait gave up (TMA never completed)
   // grid-level reductions (ordered-integer keys, atomicMax/atomicMin)
   unsigned long long face_cmax[3][NSLOT];  // corrector max cmax*2/(dx+dx)
   unsigned long long cell_cmax[3][NSLOT];  // getdt_courant max cmax/dx
@@ -134,6 +134,13 @@ VACGPU_DECLARE_LAUNCHERS(fp64, double)
 VACGPU_DECLARE_LAUNCHERS(mixed, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf64, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf32, float)
+
+// Fused single-kernel sweep of the mixed path (sweep_fused.cu): returns
+// false when no fused instance exists for the configuration.  `tmap` is the
+// CUtensorMap (as bytes) of the input state buffer.
+bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
+                        const float* const* idxf, int nzc, cudaStream_t st);
+int fused_smem_bytes(int nw);
 
 // Precision-independent time-loop kernels (control.cu).
 void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st);
