@@ -23,10 +23,10 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = [
     ("sweep_fp64.cu", ["-fmad=false"]),
     ("control.cu", ["-fmad=false"]),
-    ("sweep_mixed.cu", []),
+    ("sweep_mixed.cu", ["--use_fast_math"]),
     ("vacgpu.cu", []),
     ("noalloc.cu", []),
-    ("sweep_fused.cu", []),
+    ("sweep_fused.cu", ["--use_fast_math"]),
 ]
 
 

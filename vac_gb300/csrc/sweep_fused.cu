@@ -5,18 +5,33 @@ namespace vacgpu {
 
 int fused_smem_bytes(int nw) { return fused_smem_floats(nw) * 4; }
 
-template <int NDIM, int D, bool MHD>
-static void launch_one(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
+template <int NDIM, int D, bool MHD, int LIMC>
+static void launch_lim(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
                        cudaStream_t st) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
   const int smem = fused_smem_floats(NW) * 4;
-  auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF>;
+  auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF, LIMC>;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
   k<<<grid, FT_NT, smem, st>>>(*map, a);
+}
+
+template <int NDIM, int D, bool MHD>
+static void launch_one(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
+                       cudaStream_t st) {
+  constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
+  int l0 = a.ph.lim[0];
+  bool uniform = a.ph.typefull != VACGPU_TVDLF1;
+  for (int v = 1; v < NW; v++) uniform = uniform && a.ph.lim[v] == l0;
+  if (uniform && l0 == VACGPU_LIM_WOODWARD)
+    launch_lim<NDIM, D, MHD, LIMC_WOODWARD>(map, a, grid, st);
+  else if (uniform && l0 == VACGPU_LIM_MINMOD)
+    launch_lim<NDIM, D, MHD, LIMC_MINMOD>(map, a, grid, st);
+  else
+    launch_lim<NDIM, D, MHD, LIMC_RUNTIME>(map, a, grid, st);
 }
 
 bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,

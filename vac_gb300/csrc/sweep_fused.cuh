@@ -112,7 +112,11 @@ __device__ __forceinline__ void fence_proxy_async() {
 
 // ---------------------------------------------------------------- kernel
 
-template <int NDIM, int D, bool MHD, int PM>
+// Limiter of all variables, fixed at compile time when uniform
+// (LIMC_RUNTIME: per variable from DevPhys).
+enum { LIMC_RUNTIME = 0, LIMC_MINMOD = 1, LIMC_WOODWARD = 2 };
+
+template <int NDIM, int D, bool MHD, int PM, int LIMC>
 struct Fused {
   static constexpr int NDIR = NDIM;
   static constexpr int NW = MHD ? 2 + 2 * NDIR : 2 + NDIR;
@@ -123,6 +127,67 @@ struct Fused {
   static __device__ __forceinline__ float W(const float* s, int v, int sy,
                                             int sx) {
     return s[v * FB_PLANE + sy * FB_X + sx];
+  }
+
+  static __device__ __forceinline__ float lim(const FusedArgs& a, int v,
+                                              float x, float y) {
+    if (LIMC == LIMC_MINMOD) {
+      const float sg = copysignf(1.0f, x);
+      return sg * fmaxf(0.0f, fminf(fabsf(x), sg * y));
+    }
+    if (LIMC == LIMC_WOODWARD) {
+      const float sg = copysignf(1.0f, x);
+      const float m = fminf(fminf(fabsf(x), sg * y), sg * 0.25f * (y + x));
+      return 2.0f * sg * fmaxf(0.0f, m);
+    }
+    return PH::limiter(a.ph.lim[v], x, y);
+  }
+
+  // Predictor of one magnetic component b_k only (k != D): the value the
+  // corrector's div B reads in the transverse halo.  Same arithmetic as
+  // predict_cell restricted to F_D[b_k] = v_D b_k - m_k/rho b_D and the
+  // Powell term of b_k.
+  static __device__ __forceinline__ float predict_b(
+      const FusedArgs& a, const float* pm, const float* p0, const float* pp,
+      int sy, int sx, int gd, const int* gc, float qdt, float qs, int k) {
+    const int iv[5] = {0, 1 + D, 1 + k, E + 1 + D, E + 1 + k};
+    float u[5], uL[5], uR[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      const int v = iv[i];
+      float c = W(p0, v, sy, sx), m, p;
+      if (D == 0) {
+        m = W(p0, v, sy, sx - 1);
+        p = W(p0, v, sy, sx + 1);
+      } else if (D == 1) {
+        m = W(p0, v, sy - 1, sx);
+        p = W(p0, v, sy + 1, sx);
+      } else {
+        m = W(pm, v, sy, sx);
+        p = W(pp, v, sy, sx);
+      }
+      const float l = lim(a, v, p - c, c - m);
+      u[i] = c;
+      uR[i] = c - 0.5f * l;
+      uL[i] = c + 0.5f * l;
+    }
+    const float riR = 1.0f / uR[0], riL = 1.0f / uL[0];
+    const float fR = uR[1] * riR * uR[4] - uR[2] * riR * uR[3];
+    const float fL = uL[1] * riL * uL[4] - uL[2] * riL * uL[3];
+    float out = u[4] - qdt * a.idxf[D][gd] * (fL - fR);
+    if (a.ph.sourceunsplit && a.ph.divbfix) {
+      const int o = sy * FB_X + sx;
+      const int bx = (E + 1) * FB_PLANE, by = (E + 2) * FB_PLANE;
+      float divb = 0.5f * (p0[bx + o + 1] - p0[bx + o - 1]) * a.idxf[0][gc[0]];
+      if (NDIM > 1)
+        divb += 0.5f * (p0[by + o + FB_X] - p0[by + o - FB_X]) * a.idxf[1][gc[1]];
+      if (NDIM > 2) {
+        const int bz = (E + 3) * FB_PLANE;
+        divb += 0.5f * (pp[bz + o] - pm[bz + o]) * a.idxf[2][gc[2]];
+      }
+      out = out - u[2] / u[0] * (qs * divb);
+    }
+    return out;
   }
 
   // Hancock predictor at one cell; u = center, m/p = neighbours along D,
@@ -149,7 +214,7 @@ struct Fused {
     float uL[NW], uR[NW];
 #pragma unroll
     for (int v = 0; v < NW; v++) {
-      float l = PH::limiter(a.ph.lim[v], up[v] - u[v], u[v] - um[v]);
+      float l = lim(a, v, up[v] - u[v], u[v] - um[v]);
       uR[v] = u[v] - 0.5f * l;
       uL[v] = u[v] + 0.5f * l;
     }
@@ -242,7 +307,7 @@ struct Fused {
     for (int v = 0; v < NW; v++)
       ld[v] = a.ph.typefull == VACGPU_TVDLF1
                   ? 0.0f
-                  : PH::limiter(a.ph.lim[v], bp[v] - b0[v], b0[v] - bm[v]);
+                  : lim(a, v, bp[v] - b0[v], b0[v] - bm[v]);
   }
 
   static __device__ void run(const CUtensorMap* map, const FusedArgs& a,
@@ -332,24 +397,46 @@ struct Fused {
       const float* pp = NDIM == 3 ? slot(j + 1) : nullptr;
       float* w1j = w1slot(j);
 
-      // (1) predictor on the tile + 1 halo of plane j
-      const bool zghost = NDIM == 3 && (j < 0 || j >= g.nx[2]);
-      for (int c = tid; c < FR_N; c += FT_NT) {
-        const int rx = c % FR_X, ry = c / FR_X;
+      // (1) predictor of plane j: the 32x8 tile cells (one per thread),
+      // then the 80 halo cells -- in full where a face flux reads them, only
+      // the transverse b component where only div B reads them (MHD), not at
+      // all where nothing reads them (HD).
+      for (int c = tid; c < FT_NT + 80; c += FT_NT) {
+        int rx, ry, hdir;  // hdir: -1 tile, 0 x-halo column, 1 y-halo row
+        if (c < FT_NT) {
+          rx = c % FT_X + 1;
+          ry = c / FT_X + 1;
+          hdir = -1;
+        } else {
+          const int h = c - FT_NT;
+          if (h < 64) {
+            rx = h % 32 + 1;
+            ry = h < 32 ? 0 : FR_Y - 1;
+            hdir = 1;
+          } else {
+            rx = h < 72 ? 0 : FR_X - 1;
+            ry = (h - 64) % 8 + 1;
+            hdir = 0;
+          }
+        }
         const int ix = x0 + rx - 1, iy = y0 + ry - 1;
-        const bool xin = ix >= 0 && ix < g.nx[0];
-        const bool yin = NDIM < 2 || (iy >= 0 && iy < g.nx[1]);
-        if (ix < -1 || ix > g.nx[0] || (NDIM >= 2 && (iy < -1 || iy > g.nx[1])))
-          continue;
-        if (!xin && !yin) continue;  // corner: never read
+        if (ix > g.nx[0] || (NDIM >= 2 && iy > g.nx[1])) continue;
+        if (NDIM < 2 && hdir == 1) continue;
+        const bool full = hdir < 0 || hdir == D;
+        if (!full && !MHD) continue;
         const int gc[3] = {ix + 2, iy + g.gh[1], j + g.gh[2]};
-        float out[NW];
-        predict_cell(a, pm, p0, pp, ry + 1, rx + 3, gc[D], gc, qdt2, qs1,
-                     smallp, out);
+        const int rc = ry * FR_X + rx;
+        if (full) {
+          float out[NW];
+          predict_cell(a, pm, p0, pp, ry + 1, rx + 3, gc[D], gc, qdt2, qs1,
+                       smallp, out);
 #pragma unroll
-        for (int v = 0; v < NW; v++) w1j[v * FR_N + c] = out[v];
+          for (int v = 0; v < NW; v++) w1j[v * FR_N + rc] = out[v];
+        } else if (MHD) {
+          w1j[(E + 1 + hdir) * FR_N + rc] =
+              predict_b(a, pm, p0, pp, ry + 1, rx + 3, gc[D], gc, qdt2, qs1, hdir);
+        }
       }
-      (void)zghost;
       // D==2: limited slope of the base state at (tile cell, plane j)
       float Lcur[NW];
       if (D == 2) {
@@ -567,11 +654,11 @@ struct Fused {
   }
 };
 
-template <int NDIM, int D, bool MHD, int PM>
+template <int NDIM, int D, bool MHD, int PM, int LIMC>
 __global__ void __launch_bounds__(FT_NT, 2)
     k_sweep_fused(const __grid_constant__ CUtensorMap map, FusedArgs a) {
   extern __shared__ __align__(128) float dsm[];
-  Fused<NDIM, D, MHD, PM>::run(&map, a, dsm);
+  Fused<NDIM, D, MHD, PM, LIMC>::run(&map, a, dsm);
 }
 
 }  // namespace vacgpu
