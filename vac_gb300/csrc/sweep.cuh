@@ -251,18 +251,18 @@ struct Sweep {
     __shared__ unsigned long long shk[NT / 32];
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done || !ctrl->need_smallp) return;
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long kmin = ~0ULL, kmax = 0ULL;
-    if (n < a.g.ncell) {
+    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+         n < a.g.ncell; n += (long long)gridDim.x * blockDim.x) {
       int c[3];
       cell_coords(a.g, n, c);
       const long long off = gidx(a.g, c[0], c[1], c[2]);
       R u[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
-      double p = PH::template pthermal_raw<NDIR, MHD>(u, a.ph);
-      kmin = dkey(p);
-      kmax = kmin;
+      const unsigned long long k = dkey(PH::template pthermal_raw<NDIR, MHD>(u, a.ph));
+      kmin = k < kmin ? k : kmin;
+      kmax = k > kmax ? k : kmax;
     }
     unsigned long long k = block_max_key<NT>(kmax, shk);
     if (threadIdx.x == 0) atomic_max_key(&ctrl->pmax[blockIdx.x % NSLOT], k);
@@ -279,25 +279,26 @@ struct Sweep {
     if (ctrl->done) return;
     if (!(ctrl->need_cell[0] | ctrl->need_cell[1] | ctrl->need_cell[2]))
       return;
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const R smallp = R(ctrl->smallp);
-    int c[3] = {0, 0, 0};
-    R u[NW];
-    const bool active = n < a.g.ncell;
-    if (active) {
+    unsigned long long key[3] = {0ULL, 0ULL, 0ULL};
+    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+         n < a.g.ncell; n += (long long)gridDim.x * blockDim.x) {
+      int c[3];
       cell_coords(a.g, n, c);
       const long long off = gidx(a.g, c[0], c[1], c[2]);
+      R u[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+      for (int d = 0; d < NDIM; d++) {
+        if (!ctrl->need_cell[d]) continue;
+        R cm = PH::template cmax<NDIR, MHD>(u, d, a.ph, smallp);
+        unsigned long long k = dkey(PH::cell_ratio(cm, a.a, d, c[d]));
+        key[d] = k > key[d] ? k : key[d];
+      }
     }
     for (int d = 0; d < NDIM; d++) {
       if (!ctrl->need_cell[d]) continue;
-      unsigned long long k = 0ULL;
-      if (active) {
-        R cm = PH::template cmax<NDIR, MHD>(u, d, a.ph, smallp);
-        k = dkey(PH::cell_ratio(cm, a.a, d, c[d]));
-      }
-      k = block_max_key<NT>(k, shk);
+      unsigned long long k = block_max_key<NT>(key[d], shk);
       if (threadIdx.x == 0)
         atomic_max_key(&ctrl->cell_cmax[d][blockIdx.x % NSLOT], k);
     }
@@ -462,12 +463,14 @@ struct Launch {
   }
   static void pminmax(const SweepArgs& a, const T* w, cudaStream_t st) {
     unsigned nb = grid_for(a.g.ncell, 128);
+    if (nb > 1216) nb = 1216;  // grid-stride: a no-op step costs one wave
 #define KC(D, C, M) k_pminmax<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }
   static void cell_cmax(const SweepArgs& a, const T* w, cudaStream_t st) {
     unsigned nb = grid_for(a.g.ncell, 128);
+    if (nb > 1216) nb = 1216;
 #define KC(D, C, M) k_cell_cmax<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
     VACGPU_DISPATCH(a, KC);
 #undef KC

@@ -21,6 +21,7 @@
 #include <cuda.h>
 
 #include "physics_mixed.cuh"
+#include "sweep.cuh"
 #include "vacgpu_internal.h"
 
 namespace vacgpu {
@@ -651,6 +652,55 @@ struct Fused {
     const long long off = gidx(g, gc[0], gc[1], gc[2]);
 #pragma unroll
     for (int v = 0; v < NW; v++) a.wout[off + v * g.vs] = acc[v];
+    write_ghosts(a, gc, acc);
+  }
+
+  // getboundary of the corrected state, fused into the sweep: a mesh cell
+  // within two cells of a face also writes every ghost cell whose boundary
+  // map (periodic shift, cont clamp, symm/asymm mirror; composed over the
+  // dimensions, src/vacgrid.t:195-413) lands on it.  Each ghost cell has
+  // exactly one source cell, so the writes never collide.
+  static __device__ __forceinline__ void write_ghosts(const FusedArgs& a,
+                                                      const int* gc,
+                                                      const float* acc) {
+    const DevGrid& g = a.g;
+    bool near = false;
+#pragma unroll
+    for (int d = 0; d < NDIM; d++) near |= gc[d] < 4 || gc[d] >= g.nx[d];
+    if (!near) return;
+#pragma unroll 1
+    for (int v = 0; v < NW; v++) {
+      int pos[3][3], sg[3][3], cnt[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        pos[d][0] = gc[d];
+        sg[d][0] = 1;
+        cnt[d] = 1;
+      }
+#pragma unroll
+      for (int d = 0; d < NDIM; d++) {
+        const int n = g.nx[d];
+        const int tlo = a.ph.typeB[2 * d][v], thi = a.ph.typeB[2 * d + 1][v];
+        const int cand[4] = {0, 1, n + 2, n + 3};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          int sgn = 1;
+          if (bc_map(cand[i], n, tlo, thi, &sgn) == gc[d] && cnt[d] < 3) {
+            pos[d][cnt[d]] = cand[i];
+            sg[d][cnt[d]] = sgn;
+            cnt[d]++;
+          }
+        }
+      }
+      for (int i0 = 0; i0 < cnt[0]; i0++)
+        for (int i1 = 0; i1 < cnt[1]; i1++)
+          for (int i2 = 0; i2 < cnt[2]; i2++) {
+            if ((i0 | i1 | i2) == 0) continue;
+            const int sgn = sg[0][i0] * sg[1][i1] * sg[2][i2];
+            a.wout[gidx(g, pos[0][i0], pos[1][i1], pos[2][i2]) + v * g.vs] =
+                sgn < 0 ? -acc[v] : acc[v];
+          }
+    }
   }
 };
 

@@ -280,10 +280,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
     kbegin(h, VACGPU_K_SWEEP);
     launch_sweep_fused(a, &h->tmap[h->cur], (float*)wout, h->idxf, h->nzc,
-                       h->st);
-    kend(h);
-    kbegin(h, VACGPU_K_GHOST);
-    launch_ghost_mixed(a, (float*)wout, h->st);
+                       h->st);  // also writes the ghost cells of wout
     kend(h);
   } else {
     const float* fw = (const float*)w;
