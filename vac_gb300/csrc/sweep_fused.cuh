@@ -668,7 +668,7 @@ struct Fused {
 #pragma unroll
     for (int d = 0; d < NDIM; d++) near |= gc[d] < 4 || gc[d] >= g.nx[d];
     if (!near) return;
-#pragma unroll 1
+#pragma unroll
     for (int v = 0; v < NW; v++) {
       int pos[3][3], sg[3][3], cnt[3];
 #pragma unroll
