@@ -141,6 +141,7 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
   ph.divbfix = p->divbfix;
   ph.sourceunsplit = p->sourceunsplit;
   ph.src_id = VACGPU_SRC_NONE;
+  set_gmaps(ph, p->ndim, p->nw);
   for (int d = 0; d < 3; d++) s.a.dx[d] = dxs[d];
   s.ctrl = a.ctrl;
   s.ndir = p->ndir;

@@ -365,6 +365,27 @@ __global__ void k_ghost(T* __restrict__ w, DevGrid g, DevPhys ph,
     return;
   }
   const long long dst = gidx(g, c[0], c[1], c[2]);
+  bool uni = true;
+  for (int d = 0; d < ndim; d++)
+    uni = uni && ph.gmap[d][0] != GMAP_MIXED && ph.gmap[d][1] != GMAP_MIXED;
+  if (uni) {
+    // one source cell for every variable; asymm flips per variable
+    int s[3] = {c[0], c[1], c[2]};
+    int flip = 0;
+    for (int d = 0; d < ndim; d++) {
+      const int side = c[d] < 2 ? 0 : (c[d] >= g.nx[d] + 2 ? 1 : -1);
+      if (side < 0) continue;
+      s[d] = gmap_src(c[d], g.nx[d], ph.gmap[d][side]);
+      flip ^= ph.asym[d][side];
+    }
+    const long long src = gidx(g, s[0], s[1], s[2]);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      T v = w[src + iw * g.vs];
+      w[dst + iw * g.vs] = ((flip >> iw) & 1) ? -v : v;
+    }
+    return;
+  }
 #pragma unroll
   for (int iw = 0; iw < NW; iw++) {
     int sgn = 1, s[3] = {c[0], c[1], c[2]};

@@ -38,6 +38,9 @@ bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
                         const float* const* idxf, int nzc, cudaStream_t st) {
   const int nd = s.g.ndim;
   if (s.d0 != s.d1 || s.ndir != nd || (nd != 2 && nd != 3)) return false;
+  for (int d = 0; d < nd; d++)
+    if (s.ph.gmap[d][0] == GMAP_MIXED || s.ph.gmap[d][1] == GMAP_MIXED)
+      return false;
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.g = s.g;

@@ -668,39 +668,41 @@ struct Fused {
 #pragma unroll
     for (int d = 0; d < NDIM; d++) near |= gc[d] < 4 || gc[d] >= g.nx[d];
     if (!near) return;
+    // ghost targets per dimension (the uniform index map of each face)
+    int t[3][3], f[3][3], cnt[3];
 #pragma unroll
-    for (int v = 0; v < NW; v++) {
-      int pos[3][3], sg[3][3], cnt[3];
+    for (int d = 0; d < 3; d++) {
+      t[d][0] = gc[d];
+      f[d][0] = 0;
+      cnt[d] = 1;
+    }
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        pos[d][0] = gc[d];
-        sg[d][0] = 1;
-        cnt[d] = 1;
-      }
+    for (int d = 0; d < NDIM; d++) {
+      const int n = g.nx[d];
 #pragma unroll
-      for (int d = 0; d < NDIM; d++) {
-        const int n = g.nx[d];
-        const int tlo = a.ph.typeB[2 * d][v], thi = a.ph.typeB[2 * d + 1][v];
-        const int cand[4] = {0, 1, n + 2, n + 3};
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          int sgn = 1;
-          if (bc_map(cand[i], n, tlo, thi, &sgn) == gc[d] && cnt[d] < 3) {
-            pos[d][cnt[d]] = cand[i];
-            sg[d][cnt[d]] = sgn;
-            cnt[d]++;
-          }
+      for (int i = 0; i < 4; i++) {
+        const int gi = i < 2 ? i : n + i;
+        const int side = i < 2 ? 0 : 1;
+        if (gmap_src(gi, n, a.ph.gmap[d][side]) == gc[d] && cnt[d] < 3) {
+          t[d][cnt[d]] = gi;
+          f[d][cnt[d]] = a.ph.asym[d][side];
+          cnt[d]++;
         }
       }
-      for (int i0 = 0; i0 < cnt[0]; i0++)
-        for (int i1 = 0; i1 < cnt[1]; i1++)
-          for (int i2 = 0; i2 < cnt[2]; i2++) {
-            if ((i0 | i1 | i2) == 0) continue;
-            const int sgn = sg[0][i0] * sg[1][i1] * sg[2][i2];
-            a.wout[gidx(g, pos[0][i0], pos[1][i1], pos[2][i2]) + v * g.vs] =
-                sgn < 0 ? -acc[v] : acc[v];
-          }
     }
+#pragma unroll 1
+    for (int i0 = 0; i0 < cnt[0]; i0++)
+#pragma unroll 1
+      for (int i1 = 0; i1 < cnt[1]; i1++)
+#pragma unroll 1
+        for (int i2 = 0; i2 < cnt[2]; i2++) {
+          if ((i0 | i1 | i2) == 0) continue;
+          const int flip = f[0][i0] ^ f[1][i1] ^ f[2][i2];
+          const long long o = gidx(g, t[0][i0], t[1][i1], t[2][i2]);
+#pragma unroll
+          for (int v = 0; v < NW; v++)
+            a.wout[o + v * g.vs] = ((flip >> v) & 1) ? -acc[v] : acc[v];
+        }
   }
 };
 

@@ -474,6 +474,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.divbfix = p->divbfix;
   ph.sourceunsplit = p->sourceunsplit;
   ph.src_id = VACGPU_SRC_NONE;
+  set_gmaps(ph, p->ndim, p->nw);
   size_t bytes = h->elem * (size_t)g.vs * h->nw;
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 3 && e == cudaSuccess; i++) {
@@ -506,6 +507,8 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
              (p->ndim == 2 || p->ndim == 3) && p->ndir == p->ndim &&
              p->typelimited == VACGPU_LIMITED_ORIGINAL;
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
+  for (int d = 0; d < p->ndim; d++)  // the fused epilogue needs uniform maps
+    if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED) h->fused = false;
   if (h->fused) {
     bool ok = true;
     for (int i = 0; i < 2 && ok; i++) ok = make_tmap(h, h->buf[i], &h->tmap[i]);

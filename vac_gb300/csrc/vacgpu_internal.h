@@ -53,7 +53,44 @@ struct DevPhys {
   int sourceunsplit;
   int src_id;
   double src_par[VACGPU_MAXSRCPAR];
+  // Boundary index map per face [dim][lo/hi] when every variable shares it:
+  // GMAP_PERIODIC, GMAP_CONT or GMAP_MIRROR ('symm' and 'asymm'); GMAP_MIXED
+  // when variables differ.  asym: bit iw set where variable iw is 'asymm'.
+  int gmap[3][2];
+  int asym[3][2];
 };
+
+enum { GMAP_MIXED = -1, GMAP_PERIODIC = 0, GMAP_CONT = 1, GMAP_MIRROR = 2 };
+
+// Fill gmap/asym of ph from its typeB table.
+inline void set_gmaps(DevPhys& ph, int ndim, int nw) {
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      int m = GMAP_PERIODIC;
+      int asy = 0;
+      for (int v = 0; v < nw && d < ndim; v++) {
+        int t = ph.typeB[2 * d + s][v];
+        int mv = t == VACGPU_BC_PERIODIC ? GMAP_PERIODIC
+                 : t == VACGPU_BC_CONT   ? GMAP_CONT
+                                         : GMAP_MIRROR;
+        if (t == VACGPU_BC_ASYMM) asy |= 1 << v;
+        if (v == 0)
+          m = mv;
+        else if (mv != m)
+          m = GMAP_MIXED;
+      }
+      ph.gmap[d][s] = m;
+      ph.asym[d][s] = asy;
+    }
+}
+
+// Ghost position gi (G coordinate, n mesh cells) -> source mesh position
+// under index map m of its face.
+__host__ __device__ inline int gmap_src(int gi, int n, int m) {
+  if (gi < 2)
+    return m == GMAP_PERIODIC ? gi + n : m == GMAP_CONT ? 2 : 3 - gi;
+  return m == GMAP_PERIODIC ? gi - n : m == GMAP_CONT ? n + 1 : 2 * n + 3 - gi;
+}
 
 // Device-resident time-loop state: dt, it and t never leave the device
 // between steps, so a sequence of steps runs without host round trips (and
