@@ -121,3 +121,16 @@ def test_mixed_rel_l1(gpu_lib, name, mk, lim, bc, n):
             continue
         rel = np.abs(a[iw] - b[iw]).sum() / den
         assert rel <= MIXED_REL_L1, (iw, rel)
+
+
+def test_graph_replay_matches_plain_launches(gpu_lib, monkeypatch):
+    """Two-step CUDA-graph replay (default) against plain launches."""
+    s = inistate.random_modes(24, seed=9)
+    out = []
+    for g in ("1", "0"):
+        monkeypatch.setenv("VACGPU_GRAPH", g)
+        e = Engine(inistate.params_for(s, limiter="woodward"), s.x, s.w)
+        e.step(7)
+        out.append((e.state(), e.t, e.it))
+    assert out[0][1:] == out[1][1:]
+    assert np.array_equal(bits(out[0][0]), bits(out[1][0]))

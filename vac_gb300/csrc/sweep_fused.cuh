@@ -21,7 +21,6 @@
 #include <cuda.h>
 
 #include "physics_mixed.cuh"
-#include "sweep.cuh"
 #include "vacgpu_internal.h"
 
 namespace vacgpu {
@@ -652,57 +651,6 @@ struct Fused {
     const long long off = gidx(g, gc[0], gc[1], gc[2]);
 #pragma unroll
     for (int v = 0; v < NW; v++) a.wout[off + v * g.vs] = acc[v];
-    write_ghosts(a, gc, acc);
-  }
-
-  // getboundary of the corrected state, fused into the sweep: a mesh cell
-  // within two cells of a face also writes every ghost cell whose boundary
-  // map (periodic shift, cont clamp, symm/asymm mirror; composed over the
-  // dimensions, src/vacgrid.t:195-413) lands on it.  Each ghost cell has
-  // exactly one source cell, so the writes never collide.
-  static __device__ __forceinline__ void write_ghosts(const FusedArgs& a,
-                                                      const int* gc,
-                                                      const float* acc) {
-    const DevGrid& g = a.g;
-    bool near = false;
-#pragma unroll
-    for (int d = 0; d < NDIM; d++) near |= gc[d] < 4 || gc[d] >= g.nx[d];
-    if (!near) return;
-    // ghost targets per dimension (the uniform index map of each face)
-    int t[3][3], f[3][3], cnt[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      t[d][0] = gc[d];
-      f[d][0] = 0;
-      cnt[d] = 1;
-    }
-#pragma unroll
-    for (int d = 0; d < NDIM; d++) {
-      const int n = g.nx[d];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const int gi = i < 2 ? i : n + i;
-        const int side = i < 2 ? 0 : 1;
-        if (gmap_src(gi, n, a.ph.gmap[d][side]) == gc[d] && cnt[d] < 3) {
-          t[d][cnt[d]] = gi;
-          f[d][cnt[d]] = a.ph.asym[d][side];
-          cnt[d]++;
-        }
-      }
-    }
-#pragma unroll 1
-    for (int i0 = 0; i0 < cnt[0]; i0++)
-#pragma unroll 1
-      for (int i1 = 0; i1 < cnt[1]; i1++)
-#pragma unroll 1
-        for (int i2 = 0; i2 < cnt[2]; i2++) {
-          if ((i0 | i1 | i2) == 0) continue;
-          const int flip = f[0][i0] ^ f[1][i1] ^ f[2][i2];
-          const long long o = gidx(g, t[0][i0], t[1][i1], t[2][i2]);
-#pragma unroll
-          for (int v = 0; v < NW; v++)
-            a.wout[o + v * g.vs] = ((flip >> v) & 1) ? -acc[v] : acc[v];
-        }
   }
 };
 

@@ -156,6 +156,10 @@ struct vacgpu_handle {
   cudaEvent_t open_ev;
   int open_k;
   // fused mixed sweep: TMA descriptors of the two state buffers, 1/dx
+  // CUDA graphs of two consecutive steps, keyed by (state buffer, parity
+  // of it): replayed instead of re-issuing ~20 launches per step.
+  cudaGraphExec_t gexec[2][2];
+  bool warmed;
   bool fused;
   CUtensorMap tmap[2];
   float* idxf[3];
@@ -280,7 +284,10 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
     kbegin(h, VACGPU_K_SWEEP);
     launch_sweep_fused(a, &h->tmap[h->cur], (float*)wout, h->idxf, h->nzc,
-                       h->st);  // also writes the ghost cells of wout
+                       h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_GHOST);
+    launch_ghost_mixed(a, (float*)wout, h->st);
     kend(h);
   } else {
     const float* fw = (const float*)w;
@@ -679,15 +686,45 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   CK(cudaGetLastError());
   int issued = 0, chunk = 4;
   Ctrl c;
+  const bool graphs = !h->timing && h->st != nullptr &&
+                      !(getenv("VACGPU_GRAPH") && atoi(getenv("VACGPU_GRAPH")) == 0);
+  auto issue_steps = [&](int k) -> int {
+    for (int s = 0; s < k;) {
+      const int par = (h->it_host + issued + s) & 1;
+      if (graphs && h->warmed && k - s >= 2) {
+        cudaGraphExec_t& ex = h->gexec[h->cur][par];
+        const int cur0 = h->cur;
+        if (!ex) {
+          cudaGraph_t gr;
+          CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+          for (int q = 0; q < 2; q++) {
+            if (h->elem == 8)
+              run_step<double>(h, (par + q) & 1);
+            else
+              run_step<float>(h, (par + q) & 1);
+          }
+          CK(cudaStreamEndCapture(h->st, &gr));
+          CK(cudaGraphInstantiate(&ex, gr, 0));
+          cudaGraphDestroy(gr);
+          h->cur = cur0;
+        }
+        CK(cudaGraphLaunch(ex, h->st));
+        h->cur = cur0 ^ ((2 * nsw) & 1);
+        s += 2;
+      } else {
+        if (h->elem == 8)
+          run_step<double>(h, par);
+        else
+          run_step<float>(h, par);
+        h->warmed = true;
+        s += 1;
+      }
+    }
+    return 0;
+  };
   while (issued < maxsteps) {
     int k = maxsteps - issued < chunk ? maxsteps - issued : chunk;
-    for (int s = 0; s < k; s++) {
-      int par = (h->it_host + issued + s) & 1;
-      if (h->elem == 8)
-        run_step<double>(h, par);
-      else
-        run_step<float>(h, par);
-    }
+    if (issue_steps(k)) return 1;
     issued += k;
     CK(cudaGetLastError());
     int done = 0;
@@ -789,6 +826,9 @@ void vacgpu_destroy(vacgpu_handle* h) {
   cudaFree(h->ctrl);
   drain_events(h);
   for (auto e : h->pool) cudaEventDestroy(e);
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      if (h->gexec[i][j]) cudaGraphExecDestroy(h->gexec[i][j]);
   if (h->own_st) cudaStreamDestroy(h->own_st);
   delete h;
 }
@@ -797,7 +837,7 @@ int vacgpu_set_stream(vacgpu_handle* h, void* stream) {
   if (!h) return fail("null handle");
   CK(cudaStreamSynchronize(h->st));
   h->st = stream ? (cudaStream_t)stream : h->own_st;
-  return 0;
+  return 0;  // graphs launch on whichever stream is current
 }
 
 int vacgpu_timing(vacgpu_handle* h, int enable) {
