@@ -200,6 +200,39 @@ int vacgpu_timing(vacgpu_handle* h, int enable);
 int vacgpu_kernel_stats(vacgpu_handle* h, int kclass, long long* launches,
                         double* ms);
 
+/* ------------------------------------------------------------ batches --
+ * Many independent grids of uneven sizes advanced together (each its own
+ * VAC run: own state, dt, it, t).  No counterpart in the reference, which
+ * advances one grid per process; the per-grid semantics are those of
+ * vacgpu_step.  A batch runs the mixed-precision fused sweep: every grid
+ * must have precision VACGPU_PREC_MIXED, dimsplit, ndir=ndim (2 or 3) and
+ * share physics, method, limiters and itmax with the others; all grids
+ * start from the same it. */
+typedef struct vacgpu_batch vacgpu_batch;
+
+/* n grids, params[i] for grid i (nx may differ). */
+int vacgpu_batch_create(const vacgpu_params* params, int n,
+                        vacgpu_batch** out);
+/* vacgpu_set_grid / vacgpu_upload / vacgpu_download of grid i. */
+int vacgpu_batch_set_grid(vacgpu_batch* b, int i, const double* x);
+int vacgpu_batch_upload(vacgpu_batch* b, int i, const double* w, int it,
+                        double t);
+int vacgpu_batch_download(vacgpu_batch* b, int i, double* w);
+/* Advance every grid by up to nsteps steps (vacgpu_step semantics per
+ * grid).  The steps are captured once into a CUDA graph of batched launches
+ * (persistent sweep kernels over the work list of all grids' tiles) and
+ * replayed on later calls with the same nsteps.  The first call tunes the
+ * launch shape (VACGPU_TUNE=0 skips tuning). */
+int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop);
+/* t, it, dt and the finished flag of grid i. */
+int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
+                        double* dt, int* finished);
+/* Run (or report) the launch-shape autotuner: persistent CTAs, work-list
+ * order (0 round-robin over grids, 1 grid-major) and the six trial times
+ * in ms (ctas 152/304/one per tile x order 0/1). */
+int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, double* ms);
+void vacgpu_batch_destroy(vacgpu_batch* b);
+
 /* Largest grid vacgpu_sweep_noalloc accepts, in cells including the ghost
  * layers (prod over the used dimensions of nx+4): 262144 cells, e.g. 508^2
  * in 2-D or 60^3 in 3-D.  Its scratch is a fixed 16 MiB FP64 device array

@@ -27,6 +27,7 @@ UNITS = [
     ("vacgpu.cu", []),
     ("noalloc.cu", []),
     ("sweep_fused.cu", ["--use_fast_math"]),
+    ("batch.cu", ["--use_fast_math"]),
 ]
 
 

@@ -1,0 +1,548 @@
+// batch.cu - many independent grids of uneven sizes advanced together.
+//
+// Every grid keeps its own state, dt, it and t (its own CFL condition, as
+// separate VAC runs would).  One step of the whole batch is a fixed sequence
+// of batched launches -- dt choice for all grids, one persistent sweep
+// kernel per direction over the (grid, tile) work list of all grids, one
+// ghost fill over all grids, the step epilogue for all grids -- and a call
+// of vacgpu_batch_step captures its steps into one CUDA graph that is
+// launched once.  The state buffer parity of each grid lives on the device
+// (Ctrl::cur), so a grid that finishes early simply stops swapping.
+//
+// The persistent-kernel shape (CTAs and work-list order) is chosen by a
+// small autotuner that times the candidates on the batch itself.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "physics_mixed.cuh"
+#include "sweep.cuh"
+#include "sweep_fused.cuh"
+#include "vacgpu_internal.h"
+
+using namespace vacgpu;
+
+int vacgpu_internal_fail(const char* msg);
+
+// internal accessors of vacgpu.cu
+struct HandleView {
+  DevGrid g;
+  DevPhys ph;
+  SweepArgs sa;
+  float* buf[2];
+  const float* dxf[3];
+  const float* idxf[3];
+  Ctrl* ctrl;
+  const void* tmap[2];
+  int nzc;
+  bool fused;
+};
+int vacgpu_internal_view(vacgpu_handle* h, HandleView* v);
+
+namespace {
+
+struct BItem {
+  int inst, bx, by, bz;
+};
+
+struct BInst {
+  FusedArgs fa;        // wout chosen per sweep from buf[] and Ctrl::cur
+  SweepArgs sa;        // ghost fill and first-step passes
+  float* buf[2];
+  long long ghost0;    // offset in the batched ghost index space
+  long long pad;
+};
+
+typedef PHMixed<PREC_FF> PHB;
+
+template <int NDIM, int D, bool MHD, int LIMC>
+__global__ void __launch_bounds__(FT_NT, 2)
+    kb_sweep(const BItem* __restrict__ items, int nitems,
+             const BInst* __restrict__ insts, const CUtensorMap* maps,
+             int sweep) {
+  extern __shared__ __align__(128) float dsm[];
+  __shared__ __align__(8) unsigned long long bars[FWRING];
+  __shared__ __align__(16) FusedArgs fa;
+  __shared__ int mapidx;
+  init_bars(bars);
+  int uses[FWRING] = {0, 0, 0, 0};
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const BItem item = items[it];
+    const BInst* in = insts + item.inst;
+    {  // the grid's arguments into shared memory (word copy)
+      const int* src = (const int*)&in->fa;
+      int* dst = (int*)&fa;
+      for (int k = threadIdx.x; k < (int)(sizeof(FusedArgs) / 4); k += blockDim.x)
+        dst[k] = src[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int src = in->fa.ctrl->cur ^ (sweep & 1);
+      fa.wout = in->buf[src ^ 1];
+      mapidx = item.inst * 2 + src;
+    }
+    __syncthreads();
+    bool ok = Fused<NDIM, D, MHD, PREC_FF, LIMC>::run(
+        &maps[mapidx], fa, dsm, item.bx, item.by, item.bz, bars, uses,
+        (unsigned)it);
+    __syncthreads();
+    if (!ok) return;
+  }
+}
+
+template <int NW>
+__global__ void kb_ghost(const BInst* __restrict__ insts, int n,
+                         long long total, int sweep) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+       t < total; t += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) / 2;
+      if (insts[mid].ghost0 <= t)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const BInst* in = insts + lo;
+    const Ctrl* c = in->sa.ctrl;
+    if (c->done) continue;
+    const int dst = c->cur ^ (sweep & 1) ^ 1;
+    ghost_cell<float, NW>(in->buf[dst], in->sa.g, in->sa.ph, t - in->ghost0);
+  }
+}
+
+template <int NDIM, bool MHD>
+__global__ void __launch_bounds__(128) kb_pminmax(const BInst* insts) {
+  const BInst* in = insts + blockIdx.y;
+  Sweep<PHB, NDIM, NDIM, MHD>::template pminmax<128>(in->sa, in->buf[in->sa.ctrl->cur]);
+}
+
+template <int NDIM, bool MHD>
+__global__ void __launch_bounds__(128) kb_cell_cmax(const BInst* insts) {
+  const BInst* in = insts + blockIdx.y;
+  Sweep<PHB, NDIM, NDIM, MHD>::template cell_cmax<128>(in->sa, in->buf[in->sa.ctrl->cur]);
+}
+
+}  // namespace
+
+struct vacgpu_batch {
+  int n;
+  vacgpu_params p0;
+  std::vector<vacgpu_handle*> h;
+  BInst* d_insts;
+  CUtensorMap* d_maps;
+  Ctrl** d_ctrls;
+  BItem* d_items[2];  // work list: 0 interleaved over grids, 1 grid-major
+  int nitems;
+  long long ghost_total;
+  cudaStream_t st;
+  int nw;
+  bool ready;
+  // launch shape (autotuned): persistent CTAs and work-list order
+  int ctas, order;
+  bool tuned;
+  double tune_ms[8];
+  int it0;
+  struct G {
+    int nsteps, par;
+    cudaGraphExec_t ex;
+  };
+  std::vector<G> graphs;
+};
+
+namespace {
+
+int bfail(const std::string& m) { return vacgpu_internal_fail(m.c_str()); }
+
+#define BCK(call)                                                         \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess)                                                \
+      return bfail(std::string("CUDA error: ") + cudaGetErrorString(e_) + \
+                   " at " #call);                                         \
+  } while (0)
+
+template <int NDIM, bool MHD>
+void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
+                    const BItem* items) {
+  constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
+  const int smem = fused_smem_floats(NW) * 4;
+#define KB(DD, LL)                                                          \
+  {                                                                         \
+    auto k = kb_sweep<NDIM, DD, MHD, LL>;                                   \
+    static bool attr = false;                                               \
+    if (!attr) {                                                            \
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                           smem);                                           \
+      attr = true;                                                          \
+    }                                                                       \
+    k<<<ctas, FT_NT, smem, b->st>>>(items, b->nitems, b->d_insts, b->d_maps, \
+                                    sweep);                                 \
+  }
+#define KBL(DD)                                 \
+  if (LIMC == LIMC_WOODWARD) KB(DD, LIMC_WOODWARD) \
+  else if (LIMC == LIMC_MINMOD) KB(DD, LIMC_MINMOD) \
+  else KB(DD, LIMC_RUNTIME)
+  if (D == 0) { KBL(0) }
+  else if (D == 1) { KBL(1) }
+  else if (NDIM == 3) { KBL(2 % NDIM) }
+#undef KBL
+#undef KB
+}
+
+void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas,
+                      const BItem* items) {
+  const vacgpu_params& p = b->p0;
+  int l0 = p.typelimiter[0];
+  bool uni = p.typefull != VACGPU_TVDLF1;
+  for (int v = 1; v < b->nw; v++) uni = uni && p.typelimiter[v] == l0;
+  const int LIMC = !uni ? LIMC_RUNTIME
+                   : l0 == VACGPU_LIM_WOODWARD ? LIMC_WOODWARD
+                   : l0 == VACGPU_LIM_MINMOD ? LIMC_MINMOD
+                                             : LIMC_RUNTIME;
+  const bool mhd = p.physics == VACGPU_PHYS_MHD;
+  if (p.ndim == 2) {
+    if (mhd) launch_sweep_b<2, true>(b, D, LIMC, sweep, ctas, items);
+    else launch_sweep_b<2, false>(b, D, LIMC, sweep, ctas, items);
+  } else {
+    if (mhd) launch_sweep_b<3, true>(b, D, LIMC, sweep, ctas, items);
+    else launch_sweep_b<3, false>(b, D, LIMC, sweep, ctas, items);
+  }
+}
+
+// One step of every grid (the body of VAC's time loop, batched).
+void issue_step(vacgpu_batch* b, int parity, int ctas, const BItem* items) {
+  const vacgpu_params& p = b->p0;
+  const int n = b->n;
+  const bool mhd = p.physics == VACGPU_PHYS_MHD;
+  launchb_control(0, b->d_ctrls, n, p, 0, 0, 0.0, b->st);
+  dim3 pg(8, n);
+#define PASS(K)                                                             \
+  if (p.ndim == 2) {                                                        \
+    if (mhd) K<2, true><<<pg, 128, 0, b->st>>>(b->d_insts);                 \
+    else K<2, false><<<pg, 128, 0, b->st>>>(b->d_insts);                    \
+  } else {                                                                  \
+    if (mhd) K<3, true><<<pg, 128, 0, b->st>>>(b->d_insts);                 \
+    else K<3, false><<<pg, 128, 0, b->st>>>(b->d_insts);                    \
+  }
+  PASS(kb_pminmax)
+  launchb_control(1, b->d_ctrls, n, p, 0, 0, 0.0, b->st);
+  PASS(kb_cell_cmax)
+#undef PASS
+  launchb_control(2, b->d_ctrls, n, p, 0, 0, 0.0, b->st);
+  const int nsw = p.ndim;
+  const unsigned gb = 152 * 4;
+  for (int s = 0; s < nsw; s++) {
+    const int D = (!parity || p.typedimsplit == VACGPU_SPLIT_XY) ? s : nsw - 1 - s;
+    launch_sweep_any(b, D, s, ctas, items);
+    switch (b->nw) {
+      case 4: kb_ghost<4><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
+      case 5: kb_ghost<5><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
+      case 6: kb_ghost<6><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
+      case 8: kb_ghost<8><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
+    }
+  }
+  launchb_control(3, b->d_ctrls, n, p, nsw & 1, 0, 0.0, b->st);
+}
+
+int prepare(vacgpu_batch* b) {
+  if (b->ready) return 0;
+  const int n = b->n;
+  std::vector<BInst> ins(n);
+  std::vector<CUtensorMap> maps(2 * n);
+  std::vector<Ctrl*> ctrls(n);
+  std::vector<BItem> items;
+  long long g0 = 0;
+  for (int i = 0; i < n; i++) {
+    HandleView v;
+    if (vacgpu_internal_view(b->h[i], &v)) return 1;
+    if (!v.fused)
+      return bfail("batched grids need the fused mixed-precision sweep "
+                   "(dimsplit, ndir=ndim, uniform boundary maps)");
+    BInst& bi = ins[i];
+    memset(&bi, 0, sizeof(bi));
+    FusedArgs& a = bi.fa;
+    a.g = v.g;
+    a.ph = v.ph;
+    for (int d = 0; d < 3; d++) {
+      a.dxf[d] = v.dxf[d];
+      a.idxf[d] = v.idxf[d];
+    }
+    a.ctrl = v.ctrl;
+    a.nzc = v.nzc;
+    for (int d = 0; d < 3; d++)
+      for (int w = 0; w < b->nw; w++) {
+        if (v.ph.typeB[2 * d][w] == VACGPU_BC_PERIODIC) a.periodic_mask[d] |= 1 << w;
+        if (v.ph.typeB[2 * d][w] == VACGPU_BC_ASYMM) a.asymm_lo[d] |= 1 << w;
+        if (v.ph.typeB[2 * d + 1][w] == VACGPU_BC_ASYMM) a.asymm_hi[d] |= 1 << w;
+      }
+    bi.sa = v.sa;
+    bi.buf[0] = v.buf[0];
+    bi.buf[1] = v.buf[1];
+    bi.ghost0 = g0;
+    g0 += ghost_count(v.g);
+    memcpy(&maps[2 * i], v.tmap[0], sizeof(CUtensorMap));
+    memcpy(&maps[2 * i + 1], v.tmap[1], sizeof(CUtensorMap));
+    ctrls[i] = v.ctrl;
+  }
+  b->ghost_total = g0;
+  // work list: every (grid, tile, z chunk); order 0 round-robin over grids
+  // (neighbouring CTAs work on different grids), order 1 grid-major
+  std::vector<std::vector<BItem>> per(n);
+  for (int i = 0; i < n; i++) {
+    const DevGrid& g = ins[i].fa.g;
+    int nbx = (g.nx[0] + FT_X - 1) / FT_X, nby = (g.nx[1] + FT_Y - 1) / FT_Y;
+    int nbz = g.ndim == 3 ? (g.nx[2] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
+    for (int z = 0; z < nbz; z++)
+      for (int y = 0; y < nby; y++)
+        for (int x = 0; x < nbx; x++) per[i].push_back({i, x, y, z});
+  }
+  std::vector<BItem> rr, gm;
+  size_t maxk = 0;
+  for (auto& v : per) maxk = std::max(maxk, v.size());
+  for (size_t k = 0; k < maxk; k++)
+    for (int i = 0; i < n; i++)
+      if (k < per[i].size()) rr.push_back(per[i][k]);
+  // grid-major, largest grid first
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int a, int c) { return per[a].size() > per[c].size(); });
+  for (int i : idx) gm.insert(gm.end(), per[i].begin(), per[i].end());
+  b->nitems = (int)rr.size();
+  BCK(cudaMalloc(&b->d_insts, sizeof(BInst) * n));
+  BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 2 * n));
+  BCK(cudaMalloc(&b->d_ctrls, sizeof(Ctrl*) * n));
+  for (int o = 0; o < 2; o++) BCK(cudaMalloc(&b->d_items[o], sizeof(BItem) * b->nitems));
+  BCK(cudaMemcpy(b->d_insts, ins.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 2 * n, cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_ctrls, ctrls.data(), sizeof(Ctrl*) * n, cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_items[0], rr.data(), sizeof(BItem) * b->nitems, cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_items[1], gm.data(), sizeof(BItem) * b->nitems, cudaMemcpyHostToDevice));
+  b->ready = true;
+  return 0;
+}
+
+// Autotuner: time one step of every candidate launch shape on the batch
+// itself (state and control blocks restored after each trial) and keep the
+// fastest.  Candidates: persistent CTAs = 1, 2 per SM (the resident limit of
+// the 103 KB kernel) or one CTA per work item, times two work-list orders.
+int autotune(vacgpu_batch* b) {
+  if (b->tuned) return 0;
+  const int n = b->n;
+  std::vector<HandleView> v(n);
+  size_t tot = 0;
+  for (int i = 0; i < n; i++) {
+    vacgpu_internal_view(b->h[i], &v[i]);
+    tot += 2 * (size_t)v[i].g.vs * b->nw * sizeof(float) + sizeof(Ctrl);
+  }
+  char* snap = nullptr;
+  BCK(cudaMalloc(&snap, tot));
+  auto copy = [&](bool save) -> int {
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+      size_t bytes = (size_t)v[i].g.vs * b->nw * sizeof(float);
+      for (int k = 0; k < 2; k++) {
+        void* a = snap + off;
+        if (save)
+          BCK(cudaMemcpyAsync(a, v[i].buf[k], bytes, cudaMemcpyDeviceToDevice, b->st));
+        else
+          BCK(cudaMemcpyAsync(v[i].buf[k], a, bytes, cudaMemcpyDeviceToDevice, b->st));
+        off += bytes;
+      }
+      if (save)
+        BCK(cudaMemcpyAsync(snap + off, v[i].ctrl, sizeof(Ctrl), cudaMemcpyDeviceToDevice, b->st));
+      else
+        BCK(cudaMemcpyAsync(v[i].ctrl, snap + off, sizeof(Ctrl), cudaMemcpyDeviceToDevice, b->st));
+      off += sizeof(Ctrl);
+    }
+    return 0;
+  };
+  if (copy(true)) return 1;
+  const int cand_ctas[3] = {152, 304, b->nitems};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bc = 304, bo = 0, k = 0;
+  for (int c = 0; c < 3; c++)
+    for (int o = 0; o < 2; o++, k++) {
+      launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
+      issue_step(b, b->it0 & 1, cand_ctas[c], b->d_items[o]);  // warm
+      if (copy(false)) return 1;
+      launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
+      cudaEventRecord(e0, b->st);
+      issue_step(b, b->it0 & 1, cand_ctas[c], b->d_items[o]);
+      cudaEventRecord(e1, b->st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      b->tune_ms[k] = ms;
+      if (ms < best) {
+        best = ms;
+        bc = cand_ctas[c];
+        bo = o;
+      }
+      if (copy(false)) return 1;
+    }
+  BCK(cudaStreamSynchronize(b->st));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(snap);
+  BCK(cudaGetLastError());
+  b->ctas = bc;
+  b->order = bo;
+  b->tuned = true;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vacgpu_batch_create(const vacgpu_params* params, int n,
+                        vacgpu_batch** out) {
+  *out = nullptr;
+  if (n < 1) return bfail("a batch needs at least one grid");
+  for (int i = 0; i < n; i++) {
+    const vacgpu_params& p = params[i];
+    const vacgpu_params& q = params[0];
+    if (p.precision != VACGPU_PREC_MIXED)
+      return bfail("batched grids run the mixed-precision path");
+    if (p.ndim != q.ndim || p.ndir != q.ndir || p.physics != q.physics ||
+        p.typedimsplit != q.typedimsplit || p.itmax != q.itmax ||
+        p.typefull != q.typefull ||
+        memcmp(p.typelimiter, q.typelimiter, sizeof(p.typelimiter)) != 0)
+      return bfail("grids of a batch share physics, dimensionality, method, "
+                   "limiters and itmax");
+  }
+  vacgpu_batch* b = new vacgpu_batch();
+  b->n = n;
+  b->p0 = params[0];
+  b->nw = params[0].nw;
+  b->ctas = 304;
+  for (int i = 0; i < n; i++) {
+    vacgpu_handle* h = nullptr;
+    if (vacgpu_create(&params[i], &h)) {
+      vacgpu_batch_destroy(b);
+      return 1;
+    }
+    b->h.push_back(h);
+  }
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) {
+    vacgpu_batch_destroy(b);
+    return bfail("stream creation failed");
+  }
+  *out = b;
+  return 0;
+}
+
+int vacgpu_batch_set_grid(vacgpu_batch* b, int i, const double* x) {
+  if (!b || i < 0 || i >= b->n) return bfail("bad batch index");
+  return vacgpu_set_grid(b->h[i], x);
+}
+
+int vacgpu_batch_upload(vacgpu_batch* b, int i, const double* w, int it,
+                        double t) {
+  if (!b || i < 0 || i >= b->n) return bfail("bad batch index");
+  if (vacgpu_upload(b->h[i], w, it, t)) return 1;
+  if (i == 0) b->it0 = it;
+  if (it != b->it0) return bfail("grids of a batch start at the same it");
+  b->graphs.clear();
+  return 0;
+}
+
+int vacgpu_batch_download(vacgpu_batch* b, int i, double* w) {
+  if (!b || i < 0 || i >= b->n) return bfail("bad batch index");
+  BCK(cudaStreamSynchronize(b->st));
+  HandleView v;
+  vacgpu_internal_view(b->h[i], &v);
+  int cur = 0;
+  BCK(cudaMemcpy(&cur, &v.ctrl->cur, sizeof(int), cudaMemcpyDeviceToHost));
+  extern int vacgpu_internal_set_cur(vacgpu_handle*, int);
+  vacgpu_internal_set_cur(b->h[i], cur);
+  return vacgpu_download(b->h[i], w);
+}
+
+int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop) {
+  if (!b) return bfail("null batch");
+  if (prepare(b)) return 1;
+  const char* tz = getenv("VACGPU_TUNE");
+  if (!b->tuned && !(tz && atoi(tz) == 0))
+    if (autotune(b)) return 1;
+  const int par = b->it0 & 1;
+  cudaGraphExec_t ex = nullptr;
+  for (auto& g : b->graphs)
+    if (g.nsteps == nsteps && g.par == par) ex = g.ex;
+  if (!ex) {
+    cudaGraph_t gr;
+    BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    launchb_control(4, b->d_ctrls, b->n, b->p0, 0, nsteps, tstop, b->st);
+    for (int s = 0; s < nsteps; s++)
+      issue_step(b, (par + s) & 1, b->ctas, b->d_items[b->order]);
+    BCK(cudaStreamEndCapture(b->st, &gr));
+    BCK(cudaGraphInstantiate(&ex, gr, 0));
+    cudaGraphDestroy(gr);
+    b->graphs.push_back({nsteps, par, ex});
+  }
+  BCK(cudaGraphLaunch(ex, b->st));
+  BCK(cudaStreamSynchronize(b->st));
+  // every grid advanced the same number of steps unless it finished early
+  int steps0 = -1;
+  for (int i = 0; i < b->n; i++) {
+    HandleView v;
+    vacgpu_internal_view(b->h[i], &v);
+    Ctrl c;
+    BCK(cudaMemcpy(&c, v.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+    if (c.fault) return bfail("a device wait timed out (TMA copy never completed)");
+    if (i == 0) steps0 = c.steps;
+  }
+  b->it0 += steps0;
+  return 0;
+}
+
+int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
+                        double* dt, int* finished) {
+  if (!b || i < 0 || i >= b->n) return bfail("bad batch index");
+  HandleView v;
+  vacgpu_internal_view(b->h[i], &v);
+  Ctrl c;
+  BCK(cudaStreamSynchronize(b->st));
+  BCK(cudaMemcpy(&c, v.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+  if (t) *t = c.t;
+  if (it) *it = c.it;
+  if (dt) *dt = c.dt;
+  if (finished) *finished = c.done == 1;
+  return 0;
+}
+
+int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, double* ms) {
+  if (!b) return bfail("null batch");
+  if (prepare(b) || autotune(b)) return 1;
+  if (ctas) *ctas = b->ctas;
+  if (order) *order = b->order;
+  if (ms)
+    for (int k = 0; k < 6; k++) ms[k] = b->tune_ms[k];
+  return 0;
+}
+
+void vacgpu_batch_destroy(vacgpu_batch* b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.ex);
+  for (auto* h : b->h) vacgpu_destroy(h);
+  cudaFree(b->d_insts);
+  cudaFree(b->d_maps);
+  cudaFree(b->d_ctrls);
+  cudaFree(b->d_items[0]);
+  cudaFree(b->d_items[1]);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+}  // extern "C"

@@ -28,7 +28,7 @@ __device__ unsigned long long fold_max(const unsigned long long* s) {
   return r;
 }
 
-__global__ void k_dt_begin(Ctrl* c, int ndim) {
+__device__ void dt_begin_dev(Ctrl* c, int ndim) {
   __shared__ int stop;
   if (threadIdx.x == 0) {
     stop = c->done;
@@ -60,7 +60,7 @@ __global__ void k_dt_begin(Ctrl* c, int ndim) {
 // smallp = minval(p)*smallpcoeff at the first getpthermal call; MHD falls
 // back to maxval(p)*smallpcoeff for a negative minimum
 // (src/vacphys0.t.mhd:202-217, src/vacphys0.t.hd:123-126).
-__global__ void k_smallp(Ctrl* c, int mhd, double coeff) {
+__device__ void smallp_dev(Ctrl* c, int mhd, double coeff) {
   if (c->done || !c->need_smallp) return;
   unsigned long long kmax = fold_max(c->pmax);
   __shared__ unsigned long long sh[NSLOT];
@@ -86,7 +86,7 @@ struct DtEndArgs {
   double tmax, dtmin;
 };
 
-__global__ void k_dt_end(Ctrl* c, DtEndArgs p) {
+__device__ void dt_end_dev(Ctrl* c, const DtEndArgs& p) {
   if (c->done) return;
   unsigned long long km[3] = {0, 0, 0};
   for (int d = 0; d < p.ndim; d++)
@@ -150,7 +150,8 @@ __global__ void k_dt_end(Ctrl* c, DtEndArgs p) {
 
 // After the last sweep: fold the correctors' CFL maxima into dtcourant
 // (src/vactvdlf.t:184-201), count Courant violations, it+1, t+dt.
-__global__ void k_step_end(Ctrl* c, int ndim) {
+// toggle: the number of buffer swaps of one step (batched grids).
+__device__ void step_end_dev(Ctrl* c, int ndim, int toggle) {
   if (c->done) return;
   unsigned long long km[3] = {0, 0, 0};
   if (c->courantpar > 0.0)
@@ -168,6 +169,37 @@ __global__ void k_step_end(Ctrl* c, int ndim) {
   c->it = c->it + 1;
   c->t = c->t + c->dt;
   c->steps = c->steps + 1;
+  c->cur ^= toggle;
+}
+
+__global__ void k_dt_begin(Ctrl* c, int ndim) { dt_begin_dev(c, ndim); }
+__global__ void k_smallp(Ctrl* c, int mhd, double coeff) {
+  smallp_dev(c, mhd, coeff);
+}
+__global__ void k_dt_end(Ctrl* c, DtEndArgs p) { dt_end_dev(c, p); }
+__global__ void k_step_end(Ctrl* c, int ndim) { step_end_dev(c, ndim, 0); }
+
+// batched: block b serves grid b
+__global__ void kb_dt_begin(Ctrl* const* cs, int ndim) {
+  dt_begin_dev(cs[blockIdx.x], ndim);
+}
+__global__ void kb_smallp(Ctrl* const* cs, int mhd, double coeff) {
+  smallp_dev(cs[blockIdx.x], mhd, coeff);
+}
+__global__ void kb_dt_end(Ctrl* const* cs, DtEndArgs p) {
+  dt_end_dev(cs[blockIdx.x], p);
+}
+__global__ void kb_step_end(Ctrl* const* cs, int ndim, int toggle) {
+  step_end_dev(cs[blockIdx.x], ndim, toggle);
+}
+__global__ void kb_call_begin(Ctrl* const* cs, int maxsteps, double tstop) {
+  Ctrl* c = cs[blockIdx.x];
+  if (threadIdx.x == 0) {
+    c->done = 0;
+    c->steps = 0;
+    c->maxsteps = maxsteps;
+    c->tstop = tstop;
+  }
 }
 
 void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st) {
@@ -189,6 +221,32 @@ void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st) {
 }
 void launch_step_end(Ctrl* c, int ndim, cudaStream_t st) {
   k_step_end<<<1, NSLOT, 0, st>>>(c, ndim);
+}
+
+static DtEndArgs dt_end_args(const vacgpu_params& p) {
+  DtEndArgs a;
+  a.ndim = p.ndim;
+  a.itmax = p.itmax;
+  a.slowsteps = p.slowsteps;
+  a.dtcantgrow = p.dtcantgrow;
+  a.tmaxexact = p.tmaxexact;
+  a.tmax = p.tmax;
+  a.dtmin = p.dtmin;
+  return a;
+}
+
+void launchb_control(int which, Ctrl* const* cs, int n, const vacgpu_params& p,
+                     int toggle, int maxsteps, double tstop, cudaStream_t st) {
+  switch (which) {
+    case 0: kb_dt_begin<<<n, NSLOT, 0, st>>>(cs, p.ndim); break;
+    case 1:
+      kb_smallp<<<n, NSLOT, 0, st>>>(cs, p.physics == VACGPU_PHYS_MHD,
+                                     p.smallpcoeff);
+      break;
+    case 2: kb_dt_end<<<n, NSLOT, 0, st>>>(cs, dt_end_args(p)); break;
+    case 3: kb_step_end<<<n, NSLOT, 0, st>>>(cs, p.ndim, toggle); break;
+    case 4: kb_call_begin<<<n, 32, 0, st>>>(cs, maxsteps, tstop); break;
+  }
 }
 
 }  // namespace vacgpu

@@ -332,10 +332,8 @@ __device__ __forceinline__ int bc_map(int gi, int n, int tlo, int thi,
 }
 
 template <typename T, int NW>
-__global__ void k_ghost(T* __restrict__ w, DevGrid g, DevPhys ph,
-                        const Ctrl* ctrl) {
-  if (ctrl && ctrl->done) return;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void ghost_cell(T* __restrict__ w, const DevGrid& g,
+                                           const DevPhys& ph, long long t) {
   const int ndim = g.ndim;
   const long long nzs = ndim == 3 ? 4LL * g.nG[1] * g.nG[0] : 0;
   const long long nys = ndim >= 2 ? 4LL * g.nx[2] * g.nG[0] : 0;
@@ -395,6 +393,13 @@ __global__ void k_ghost(T* __restrict__ w, DevGrid g, DevPhys ph,
     T v = w[gidx(g, s[0], s[1], s[2]) + iw * g.vs];
     w[dst + iw * g.vs] = sgn < 0 ? -v : v;
   }
+}
+
+template <typename T, int NW>
+__global__ void k_ghost(T* __restrict__ w, DevGrid g, DevPhys ph,
+                        const Ctrl* ctrl) {
+  if (ctrl && ctrl->done) return;
+  ghost_cell<T, NW>(w, g, ph, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 inline long long ghost_count(const DevGrid& g) {

@@ -310,11 +310,16 @@ struct Fused {
                   : lim(a, v, bp[v] - b0[v], b0[v] - bm[v]);
   }
 
-  static __device__ void run(const CUtensorMap* map, const FusedArgs& a,
-                             float* sm) {
+  // One tile (bx, by) and z chunk bz of one grid.  bars: the CTA's
+  // FWRING mbarriers (initialised once); uses[s]: loads completed on slot s
+  // before this tile (kept identically by every thread, gives the phase
+  // parity).  Returns false when a TMA wait timed out.
+  static __device__ bool run(const CUtensorMap* map, const FusedArgs& a,
+                             float* sm, int bx, int by, int bz,
+                             unsigned long long* bars, int* uses,
+                             unsigned slotid) {
     Ctrl* ctrl = a.ctrl;
-    if (ctrl->done) return;
-    __shared__ __align__(8) unsigned long long bars[FWRING];
+    if (ctrl->done) return true;
     __shared__ unsigned long long shkey[FT_NT / 32];
     float* wring = sm;
     float* w1ring = wring + FWRING * NW * FB_PLANE;
@@ -322,8 +327,8 @@ struct Fused {
     const int tid = threadIdx.x;
     const int lx = tid % FT_X, ly = tid / FT_X;
     const DevGrid& g = a.g;
-    const int x0 = blockIdx.x * FT_X, y0 = blockIdx.y * FT_Y;
-    const int zc = NDIM == 3 ? (int)blockIdx.z : 0;
+    const int x0 = bx * FT_X, y0 = by * FT_Y;
+    const int zc = NDIM == 3 ? bz : 0;
     const int z0 = NDIM == 3 ? zc * a.nzc : 0;
     const int z1 = NDIM == 3 ? min(z0 + a.nzc, g.nx[2]) : 1;  // exclusive
     const double dtd = ctrl->dt;
@@ -334,12 +339,6 @@ struct Fused {
     const float smallp = (float)ctrl->smallp;
     const int colx = x0 + g.xpad - 4 + 2;  // TMA x start (multiple of 4)
     const unsigned plane_bytes = NW * FB_PLANE * 4;
-
-    if (tid == 0) {
-      for (int i = 0; i < FWRING; i++) mbar_init(&bars[i], 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
 
     // plane p of the mesh lives in slot (p - pbase) % FWRING
     const int pbase = NDIM == 3 ? z0 - 2 : 0;
@@ -358,7 +357,7 @@ struct Fused {
     };
     auto wait_plane = [&](int p) -> bool {
       int q = p - pbase;
-      return mbar_wait(&bars[q % FWRING], (q / FWRING) & 1);
+      return mbar_wait(&bars[q % FWRING], (uses[q % FWRING] + q / FWRING) & 1);
     };
 
     unsigned long long key = 0ULL;
@@ -390,7 +389,7 @@ struct Fused {
       }
       if (__syncthreads_or(!ok)) {
         if (tid == 0) atomicExch(&ctrl->fault, 1);
-        return;
+        return false;
       }
       const float* pm = NDIM == 3 ? slot(j - 1) : nullptr;
       const float* p0 = slot(j);
@@ -477,7 +476,8 @@ struct Fused {
             key = k > key ? k : key;
           }
         }
-        if (out_plane) corrector_out(a, jo, x0, y0, lx, ly, qdt, qs2, Fprev, Fnew);
+        if (out_plane)
+          corrector_out(a, jo, x0, y0, lx, ly, qdt, qs2, Fprev, Fnew, pbase);
 #pragma unroll
         for (int v = 0; v < NW; v++) {
           Lprev[v] = Lcur[v];
@@ -537,9 +537,14 @@ struct Fused {
           Fm[v] = fbuf[v * FFACE + fm];
           Fp[v] = fbuf[v * FFACE + fp];
         }
-        corrector_out(a, jo, x0, y0, lx, ly, qdt, qs2, Fm, Fp);
+        corrector_out(a, jo, x0, y0, lx, ly, qdt, qs2, Fm, Fp, pbase);
       }
       __syncthreads();  // ring slots of planes j-1 (state) and j-2 reusable
+    }
+    {  // phase bookkeeping: planes pbase .. (NDIM==3 ? z1+1 : 0) were loaded
+      const int np = NDIM == 3 ? z1 + 2 - pbase : 1;
+#pragma unroll
+      for (int s2 = 0; s2 < FWRING; s2++) uses[s2] += (np - s2 + FWRING - 1) / FWRING;
     }
     // CFL maximum of this CTA's faces
     if (a.ph.courantpar > 0.0) {
@@ -552,10 +557,11 @@ struct Fused {
       __syncthreads();
       if (tid == 0) {
         for (int i = 1; i < FT_NT / 32; i++) key = shkey[i] > key ? shkey[i] : key;
-        const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        if (key) atomicMax(&ctrl->face_cmax[D][b % NSLOT], key);
+        if (key) atomicMax(&ctrl->face_cmax[D][slotid % NSLOT], key);
       }
+      __syncthreads();
     }
+    return true;
   }
 
   // getboundary on w1: cells of the predictor region in the first ghost
@@ -621,13 +627,11 @@ struct Fused {
   // + sources(w1), written to HBM.
   static __device__ __forceinline__ void corrector_out(
       const FusedArgs& a, int jo, int x0, int y0, int lx, int ly, float qdt,
-      float qs, const float* Fm, const float* Fp) {
+      float qs, const float* Fm, const float* Fp, int pbase) {
     const DevGrid& g = a.g;
     const int ix = x0 + lx, iy = y0 + ly;
     if (ix >= g.nx[0] || (NDIM >= 2 && iy >= g.nx[1])) return;
     extern __shared__ __align__(128) float dsm[];
-    const int z0 = NDIM == 3 ? (int)blockIdx.z * a.nzc : 0;
-    const int pbase = NDIM == 3 ? z0 - 2 : 0;
     const float* bpl = dsm + ((jo - pbase) % FWRING) * NW * FB_PLANE;
     float* w1ring = dsm + FWRING * NW * FB_PLANE;
     auto w1s = [&](int p) -> const float* {
@@ -654,11 +658,24 @@ struct Fused {
   }
 };
 
+__device__ __forceinline__ void init_bars(unsigned long long* bars) {
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < FWRING; i++) mbar_init(&bars[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
 template <int NDIM, int D, bool MHD, int PM, int LIMC>
 __global__ void __launch_bounds__(FT_NT, 2)
     k_sweep_fused(const __grid_constant__ CUtensorMap map, FusedArgs a) {
   extern __shared__ __align__(128) float dsm[];
-  Fused<NDIM, D, MHD, PM, LIMC>::run(&map, a, dsm);
+  __shared__ __align__(8) unsigned long long bars[FWRING];
+  init_bars(bars);
+  int uses[FWRING] = {0, 0, 0, 0};
+  const unsigned slotid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  Fused<NDIM, D, MHD, PM, LIMC>::run(&map, a, dsm, blockIdx.x, blockIdx.y,
+                                     blockIdx.z, bars, uses, slotid);
 }
 
 }  // namespace vacgpu

@@ -120,6 +120,19 @@ __global__ void k_call_begin(Ctrl* c, int maxsteps, double tstop) {
 
 int vacgpu_internal_fail(const char* msg) { return fail(msg); }
 
+struct HandleView {
+  DevGrid g;
+  DevPhys ph;
+  SweepArgs sa;
+  float* buf[2];
+  const float* dxf[3];
+  const float* idxf[3];
+  Ctrl* ctrl;
+  const void* tmap[2];
+  int nzc;
+  bool fused;
+};
+
 struct vacgpu_handle {
   vacgpu_params p;
   DevGrid g;
@@ -410,6 +423,29 @@ int check_params(const vacgpu_params* p) {
 
 }  // namespace
 
+// Internal views used by batch.cu.
+int vacgpu_internal_view(vacgpu_handle* h, HandleView* v) {
+  v->g = h->g;
+  v->ph = h->ph;
+  v->sa = make_args(h, 0, h->p.ndim - 1);
+  v->buf[0] = (float*)h->buf[0];
+  v->buf[1] = (float*)h->buf[1];
+  for (int d = 0; d < 3; d++) {
+    v->dxf[d] = h->dxf[d];
+    v->idxf[d] = h->idxf[d];
+  }
+  v->ctrl = h->ctrl;
+  v->tmap[0] = &h->tmap[0];
+  v->tmap[1] = &h->tmap[1];
+  v->nzc = h->nzc;
+  v->fused = h->fused;
+  return 0;
+}
+int vacgpu_internal_set_cur(vacgpu_handle* h, int cur) {
+  h->cur = cur;
+  return 0;
+}
+
 extern "C" {
 
 void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
@@ -649,6 +685,8 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
   for (int i = 0; i < 4; i++) c.nerror[i] = 0;
   c.dtgrav = h->dtgrav > 0 ? h->dtgrav : BIGD;
+  c.cur = 0;
+  c.fault = 0;
   CK(cudaMemcpyAsync(h->ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
   h->it_host = it;

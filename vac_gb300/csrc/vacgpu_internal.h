@@ -109,6 +109,7 @@ struct Ctrl {
   int need_smallp;    // smallp<0 at this step's first pressure evaluation
   int nerror[4];
   int fault;          // a bounded device wait gave up (TMA never completed)
+  int cur;            // batched grids: which state buffer holds the state
   // grid-level reductions (ordered-integer keys, atomicMax/atomicMin)
   unsigned long long face_cmax[3][NSLOT];  // corrector max cmax*2/(dx+dx)
   unsigned long long cell_cmax[3][NSLOT];  // getdt_courant max cmax/dx
@@ -184,5 +185,9 @@ void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st);
 void launch_smallp(Ctrl* c, int mhd, double smallpcoeff, cudaStream_t st);
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st);
 void launch_step_end(Ctrl* c, int ndim, cudaStream_t st);
+// Batched control: which = 0 dt_begin, 1 smallp, 2 dt_end, 3 step_end
+// (toggle = buffer swaps per step), 4 call_begin; one block per grid.
+void launchb_control(int which, Ctrl* const* cs, int n, const vacgpu_params& p,
+                     int toggle, int maxsteps, double tstop, cudaStream_t st);
 
 }  // namespace vacgpu

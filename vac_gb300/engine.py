@@ -21,6 +21,9 @@ SYMBOLS = [
     "vacgpu_error_counts", "vacgpu_register_source", "vacgpu_destroy",
     "vacgpu_last_error", "vacgpu_version", "vacgpu_set_stream",
     "vacgpu_timing", "vacgpu_kernel_stats", "vacgpu_sweep_noalloc",
+    "vacgpu_batch_create", "vacgpu_batch_set_grid", "vacgpu_batch_upload",
+    "vacgpu_batch_download", "vacgpu_batch_step", "vacgpu_batch_status",
+    "vacgpu_batch_tune", "vacgpu_batch_destroy",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
@@ -59,6 +62,15 @@ def lib():
         L.vacgpu_kernel_stats.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong), dp]
         L.vacgpu_sweep_noalloc.argtypes = [C.POINTER(abi.VacParams), vp, vp, vp,
                                            vp, vp, C.c_double, C.c_int, vp, vp]
+        L.vacgpu_batch_create.argtypes = [C.POINTER(abi.VacParams), C.c_int, C.POINTER(vp)]
+        L.vacgpu_batch_set_grid.argtypes = [vp, C.c_int, dp]
+        L.vacgpu_batch_upload.argtypes = [vp, C.c_int, dp, C.c_int, C.c_double]
+        L.vacgpu_batch_download.argtypes = [vp, C.c_int, dp]
+        L.vacgpu_batch_step.argtypes = [vp, C.c_int, C.c_double]
+        L.vacgpu_batch_status.argtypes = [vp, C.c_int, dp, ip, dp, ip]
+        L.vacgpu_batch_tune.argtypes = [vp, ip, ip, dp]
+        L.vacgpu_batch_destroy.argtypes = [vp]
+        L.vacgpu_batch_destroy.restype = None
         _lib = L
     return _lib
 
@@ -169,6 +181,59 @@ class Engine:
     def close(self):
         if getattr(self, "h", None):
             lib().vacgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many grids advanced together (vacgpu_batch_*): ``snaps`` is a list of
+    (params, x, w) for each grid."""
+
+    def __init__(self, grids):
+        L = lib()
+        n = len(grids)
+        arr = (abi.VacParams * n)(*[g[0] for g in grids])
+        h = C.c_void_p()
+        _ck(L.vacgpu_batch_create(arr, n, C.byref(h)), "vacgpu_batch_create")
+        self.h = h
+        self.n = n
+        self.meta = [(g[0].nw, tuple(g[0].nx[d] for d in range(g[0].ndim))) for g in grids]
+        for i, (p, x, w) in enumerate(grids):
+            xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)
+            _ck(L.vacgpu_batch_set_grid(self.h, i, _dp(xf)), "vacgpu_batch_set_grid")
+            wf = np.ascontiguousarray(pack_mesh(w), dtype=np.float64)
+            _ck(L.vacgpu_batch_upload(self.h, i, _dp(wf), 0, 0.0), "vacgpu_batch_upload")
+
+    def step(self, nsteps, tstop=1e300):
+        _ck(lib().vacgpu_batch_step(self.h, nsteps, tstop), "vacgpu_batch_step")
+
+    def tune(self):
+        c, o = C.c_int(), C.c_int()
+        ms = (C.c_double * 6)()
+        _ck(lib().vacgpu_batch_tune(self.h, C.byref(c), C.byref(o), ms), "vacgpu_batch_tune")
+        return c.value, o.value, list(ms)
+
+    def status(self, i):
+        t, it, dt, fin = C.c_double(), C.c_int(), C.c_double(), C.c_int()
+        _ck(lib().vacgpu_batch_status(self.h, i, C.byref(t), C.byref(it), C.byref(dt),
+                                      C.byref(fin)), "vacgpu_batch_status")
+        return t.value, it.value, dt.value, bool(fin.value)
+
+    def state(self, i):
+        nw, nx = self.meta[i]
+        n = int(np.prod(nx))
+        out = np.empty(nw * n, dtype=np.float64)
+        _ck(lib().vacgpu_batch_download(self.h, i, _dp(out)), "vacgpu_batch_download")
+        return np.stack([out[k * n:(k + 1) * n].reshape(nx, order="F") for k in range(nw)])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vacgpu_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

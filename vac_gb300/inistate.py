@@ -196,3 +196,20 @@ def params_for(snap, limiter="minmod", bc="periodic", precision=abi.PREC_FP64):
     abi.set_all_bc(p, abi.BC_NAMES[bc])
     p.precision = precision
     return p
+
+
+def batch_sides(n=64, seed=0, lo=64, hi=1024):
+    """Grid sides drawn log-uniformly in [lo, hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [int(round(np.exp(v))) for v in rng.uniform(np.log(lo), np.log(hi), n)]
+
+
+def riemann_batch(n=64, seed=0, lo=64, hi=1024, precision=abi.PREC_MIXED):
+    """The batched workload: n two-state gamma=1.4 problems on square grids
+    with log-uniform sides, outflow ('cont') boundaries, minmod."""
+    grids = []
+    for i, side in enumerate(batch_sides(n, seed, lo, hi)):
+        s = riemann_2d(side, seed * 1000 + i)
+        p = params_for(s, limiter="minmod", bc="cont", precision=precision)
+        grids.append((p, s.x, s.w))
+    return grids
