@@ -30,10 +30,9 @@ def test_batch_matches_single_grid_runs(gpu_lib):
 
 
 def test_batch_mhd3d_and_tuner(gpu_lib):
-    grids = []
-    for i, n in enumerate([12, 20, 33]):
-        s = inistate.random_modes(n, seed=i)
-        grids.append((inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED), s.x, s.w))
+    snaps = [inistate.random_modes(n, seed=i) for i, n in enumerate([12, 20, 33])]
+    grids = [(inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED), s.x, s.w)
+             for s in snaps]
     b = Batch(grids)
     ctas, order, ms = b.tune()
     assert ctas > 0 and order in (0, 1) and all(m > 0 for m in ms)
@@ -42,12 +41,9 @@ def test_batch_mhd3d_and_tuner(gpu_lib):
         e = Engine(p, x, w)
         e.step(5)
         assert np.array_equal(bits(b.state(i)), bits(e.state())), i
-        p64 = inistate.params_for(inistate.random_modes(8), limiter="woodward")
-        p64.nx[0] = p64.nx[1] = p64.nx[2] = p.nx[0]
-        o = Oracle(p64, x, w)
+        o = Oracle(inistate.params_for(snaps[i], limiter="woodward"), x, w)
         o.step(5)
-        ref = o.state()
-        got = b.state(i)
+        ref, got = o.state(), b.state(i)
         for iw in range(p.nw):
             rel = np.abs(got[iw] - ref[iw]).sum() / np.abs(ref[iw]).sum()
             assert rel <= 1e-5, (i, iw, rel)

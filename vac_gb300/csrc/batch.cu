@@ -44,6 +44,7 @@ struct HandleView {
   bool fused;
 };
 int vacgpu_internal_view(vacgpu_handle* h, HandleView* v);
+int vacgpu_internal_set_cur(vacgpu_handle* h, int cur);
 
 namespace {
 
@@ -464,7 +465,6 @@ int vacgpu_batch_download(vacgpu_batch* b, int i, double* w) {
   vacgpu_internal_view(b->h[i], &v);
   int cur = 0;
   BCK(cudaMemcpy(&cur, &v.ctrl->cur, sizeof(int), cudaMemcpyDeviceToHost));
-  extern int vacgpu_internal_set_cur(vacgpu_handle*, int);
   vacgpu_internal_set_cur(b->h[i], cur);
   return vacgpu_download(b->h[i], w);
 }
