@@ -233,6 +233,37 @@ int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
 int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, double* ms);
 void vacgpu_batch_destroy(vacgpu_batch* b);
 
+/* ------------------------------------------------------------- server --
+ * Continuous-batching request server (no counterpart in the reference).
+ * A worker thread admits submitted solves in arrival order while their
+ * device memory fits the HBM budget and fewer than max_active are running,
+ * keeps each admitted solve's state on the device, and issues its steps in
+ * chunks of steps_per_chunk (replayed CUDA graphs) on its own stream as
+ * soon as its previous chunk finished, so the admitted solves overlap on
+ * the GPU; a finished solve is copied back and its memory released for the
+ * next one.  Each solve runs exactly as vacgpu_step would run it alone. */
+typedef struct vacgpu_server vacgpu_server;
+
+int vacgpu_server_create(double hbm_budget_bytes, int max_active,
+                         int steps_per_chunk, vacgpu_server** out);
+/* Queue a solve: grid x(ixM^S,1:ndim), state w(ixM^S,1:nw) at it=0, t=0,
+ * advanced nsteps steps.  Thread safe; the inputs are copied. */
+int vacgpu_server_submit(vacgpu_server* s, const vacgpu_params* p,
+                         const double* x, const double* w, int nsteps,
+                         long long* id);
+/* 0: finished (state copied into w when w is not NULL, with its t, it and
+ * the time from submission to result in seconds); 1: not finished after
+ * waiting up to wait_s seconds; other nonzero: the solve failed. */
+int vacgpu_server_result(vacgpu_server* s, long long id, double wait_s,
+                         double* w, double* t, int* it, double* tts);
+/* Queue length, running solves, finished solves, the largest number of
+ * solves that ran at once, cell updates of finished solves and the time
+ * from the first submission to the last completion. */
+int vacgpu_server_stats(vacgpu_server* s, int* nqueued, int* nactive,
+                        int* ndone, int* peak_active, double* cell_updates,
+                        double* span_s);
+void vacgpu_server_destroy(vacgpu_server* s);
+
 /* Largest grid vacgpu_sweep_noalloc accepts, in cells including the ghost
  * layers (prod over the used dimensions of nx+4): 262144 cells, e.g. 508^2
  * in 2-D or 60^3 in 3-D.  Its scratch is a fixed 16 MiB FP64 device array

@@ -28,6 +28,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("sweep_fused.cu", ["--use_fast_math"]),
     ("batch.cu", ["--use_fast_math"]),
+    ("server.cu", []),
 ]
 
 

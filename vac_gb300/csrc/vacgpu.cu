@@ -379,6 +379,47 @@ void run_step(vacgpu_handle* h, int parity_odd) {
   kend(h);
 }
 
+// Issue k steps on the handle's stream without waiting: two-step units
+// are replayed from captured CUDA graphs keyed by (state buffer, parity of
+// it); h->cur follows the swaps of steps that execute.
+int issue_steps(vacgpu_handle* h, int k, int it_base) {
+  const int nsw = h->p.dimsplit ? h->p.ndim : 1;
+  const bool graphs = !h->timing && h->st != nullptr &&
+                      !(getenv("VACGPU_GRAPH") && atoi(getenv("VACGPU_GRAPH")) == 0);
+  for (int s = 0; s < k;) {
+    const int par = (it_base + s) & 1;
+    if (graphs && h->warmed && k - s >= 2) {
+      cudaGraphExec_t& ex = h->gexec[h->cur][par];
+      const int cur0 = h->cur;
+      if (!ex) {
+        cudaGraph_t gr;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < 2; q++) {
+          if (h->elem == 8)
+            run_step<double>(h, (par + q) & 1);
+          else
+            run_step<float>(h, (par + q) & 1);
+        }
+        CK(cudaStreamEndCapture(h->st, &gr));
+        CK(cudaGraphInstantiate(&ex, gr, 0));
+        cudaGraphDestroy(gr);
+        h->cur = cur0;
+      }
+      CK(cudaGraphLaunch(ex, h->st));
+      h->cur = cur0 ^ ((2 * nsw) & 1);
+      s += 2;
+    } else {
+      if (h->elem == 8)
+        run_step<double>(h, par);
+      else
+        run_step<float>(h, par);
+      h->warmed = true;
+      s += 1;
+    }
+  }
+  return 0;
+}
+
 int check_params(const vacgpu_params* p) {
   if (p->ndim < 1 || p->ndim > 3) return fail("ndim must be 1..3");
   if (p->ndir < p->ndim || p->ndir > 3) return fail("ndir must be ndim..3");
@@ -444,6 +485,33 @@ int vacgpu_internal_view(vacgpu_handle* h, HandleView* v) {
 int vacgpu_internal_set_cur(vacgpu_handle* h, int cur) {
   h->cur = cur;
   return 0;
+}
+
+// Server support: issue k steps that all execute (no stop condition in
+// between) without any host synchronisation.
+int vacgpu_internal_step_async(vacgpu_handle* h, int k) {
+  k_call_begin<<<1, 1, 0, h->st>>>(h->ctrl, k, 1e300);
+  if (issue_steps(h, k, h->it_host)) return 1;
+  h->it_host += k;
+  CK(cudaGetLastError());
+  return 0;
+}
+void* vacgpu_internal_stream(vacgpu_handle* h) { return (void*)h->st; }
+
+// Device bytes vacgpu_create allocates for p (admission control).
+size_t vacgpu_internal_device_bytes(const vacgpu_params* p) {
+  size_t elem = p->precision == VACGPU_PREC_FP64 ? 8 : 4;
+  long long nG[3], ncell = 1;
+  for (int d = 0; d < 3; d++) {
+    nG[d] = d < p->ndim ? p->nx[d] + 4 : 1;
+    ncell *= d < p->ndim ? p->nx[d] : 1;
+  }
+  const long long align = 128 / elem;
+  const long long P = ((align - 2 + nG[0] + align - 1) / align) * align;
+  const size_t vs = (size_t)P * nG[1] * nG[2];
+  size_t b = 3 * elem * vs * p->nw + 8 * (size_t)ncell * p->nw;
+  b += 8 * ((ncell + 255) / 256) * p->nw + sizeof(Ctrl) + 64 * 1024;
+  return b;
 }
 
 extern "C" {
@@ -724,45 +792,9 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   CK(cudaGetLastError());
   int issued = 0, chunk = 4;
   Ctrl c;
-  const bool graphs = !h->timing && h->st != nullptr &&
-                      !(getenv("VACGPU_GRAPH") && atoi(getenv("VACGPU_GRAPH")) == 0);
-  auto issue_steps = [&](int k) -> int {
-    for (int s = 0; s < k;) {
-      const int par = (h->it_host + issued + s) & 1;
-      if (graphs && h->warmed && k - s >= 2) {
-        cudaGraphExec_t& ex = h->gexec[h->cur][par];
-        const int cur0 = h->cur;
-        if (!ex) {
-          cudaGraph_t gr;
-          CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-          for (int q = 0; q < 2; q++) {
-            if (h->elem == 8)
-              run_step<double>(h, (par + q) & 1);
-            else
-              run_step<float>(h, (par + q) & 1);
-          }
-          CK(cudaStreamEndCapture(h->st, &gr));
-          CK(cudaGraphInstantiate(&ex, gr, 0));
-          cudaGraphDestroy(gr);
-          h->cur = cur0;
-        }
-        CK(cudaGraphLaunch(ex, h->st));
-        h->cur = cur0 ^ ((2 * nsw) & 1);
-        s += 2;
-      } else {
-        if (h->elem == 8)
-          run_step<double>(h, par);
-        else
-          run_step<float>(h, par);
-        h->warmed = true;
-        s += 1;
-      }
-    }
-    return 0;
-  };
   while (issued < maxsteps) {
     int k = maxsteps - issued < chunk ? maxsteps - issued : chunk;
-    if (issue_steps(k)) return 1;
+    if (issue_steps(h, k, h->it_host + issued)) return 1;
     issued += k;
     CK(cudaGetLastError());
     int done = 0;

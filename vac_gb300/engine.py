@@ -23,7 +23,9 @@ SYMBOLS = [
     "vacgpu_timing", "vacgpu_kernel_stats", "vacgpu_sweep_noalloc",
     "vacgpu_batch_create", "vacgpu_batch_set_grid", "vacgpu_batch_upload",
     "vacgpu_batch_download", "vacgpu_batch_step", "vacgpu_batch_status",
-    "vacgpu_batch_tune", "vacgpu_batch_destroy",
+    "vacgpu_batch_tune", "vacgpu_batch_destroy", "vacgpu_server_create",
+    "vacgpu_server_submit", "vacgpu_server_result", "vacgpu_server_stats",
+    "vacgpu_server_destroy",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
@@ -71,6 +73,13 @@ def lib():
         L.vacgpu_batch_tune.argtypes = [vp, ip, ip, dp]
         L.vacgpu_batch_destroy.argtypes = [vp]
         L.vacgpu_batch_destroy.restype = None
+        L.vacgpu_server_create.argtypes = [C.c_double, C.c_int, C.c_int, C.POINTER(vp)]
+        L.vacgpu_server_submit.argtypes = [vp, C.POINTER(abi.VacParams), dp, dp, C.c_int,
+                                           C.POINTER(C.c_longlong)]
+        L.vacgpu_server_result.argtypes = [vp, C.c_longlong, C.c_double, dp, dp, ip, dp]
+        L.vacgpu_server_stats.argtypes = [vp, ip, ip, ip, ip, dp, dp]
+        L.vacgpu_server_destroy.argtypes = [vp]
+        L.vacgpu_server_destroy.restype = None
         _lib = L
     return _lib
 
@@ -234,6 +243,62 @@ class Batch:
     def close(self):
         if getattr(self, "h", None):
             lib().vacgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching solve server (vacgpu_server_*)."""
+
+    def __init__(self, hbm_budget_bytes=150e9, max_active=16, steps_per_chunk=16):
+        h = C.c_void_p()
+        _ck(lib().vacgpu_server_create(float(hbm_budget_bytes), max_active,
+                                       steps_per_chunk, C.byref(h)), "vacgpu_server_create")
+        self.h = h
+        self.meta = {}
+
+    def submit(self, params, x, w, nsteps):
+        xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)
+        wf = np.ascontiguousarray(pack_mesh(w), dtype=np.float64)
+        rid = C.c_longlong()
+        _ck(lib().vacgpu_server_submit(self.h, C.byref(params), _dp(xf), _dp(wf),
+                                       nsteps, C.byref(rid)), "vacgpu_server_submit")
+        self.meta[rid.value] = (params.nw, tuple(params.nx[d] for d in range(params.ndim)))
+        return rid.value
+
+    def result(self, rid, wait=0.0, fetch=True):
+        """None if not finished, else (state or None, t, it, seconds to solution)."""
+        nw, nx = self.meta[rid]
+        n = int(np.prod(nx))
+        out = np.empty(nw * n, dtype=np.float64) if fetch else None
+        t, it, tts = C.c_double(), C.c_int(), C.c_double()
+        rc = lib().vacgpu_server_result(self.h, rid, wait, _dp(out) if fetch else None,
+                                        C.byref(t), C.byref(it), C.byref(tts))
+        if rc == 1:
+            return None
+        _ck(rc, "vacgpu_server_result")
+        st = None
+        if fetch:
+            st = np.stack([out[k * n:(k + 1) * n].reshape(nx, order="F") for k in range(nw)])
+        return st, t.value, it.value, tts.value
+
+    def stats(self):
+        q, a, d, pk = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        cu, span = C.c_double(), C.c_double()
+        _ck(lib().vacgpu_server_stats(self.h, C.byref(q), C.byref(a), C.byref(d),
+                                      C.byref(pk), C.byref(cu), C.byref(span)),
+            "vacgpu_server_stats")
+        return {"queued": q.value, "active": a.value, "done": d.value,
+                "peak_active": pk.value, "cell_updates": cu.value, "span_s": span.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vacgpu_server_destroy(self.h)
             self.h = None
 
     def __del__(self):
