@@ -139,6 +139,82 @@ def cpu_sample(snap, steps, threads):
     return N ** 3 * steps / dt, dt
 
 
+def run_batched(args):
+    """Config 3: 64 2-D gamma=1.4 Riemann problems, sides log-uniform in
+    [64, 1024], outflow, minmod, mixed precision; all grids advance 50 steps
+    in one replay of a CUDA graph of batched persistent-kernel launches."""
+    import torch
+    from vac_gb300 import inistate
+    from vac_gb300.engine import Batch
+    grids = inistate.riemann_batch(n=64, seed=0)
+    cells = sum(int(np.prod([g[0].nx[d] for d in range(2)])) for g in grids)
+    b = Batch(grids)
+    ctas, order, ms = b.tune()
+    b.step(50)  # capture + first replay
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(50)
+    el = time.perf_counter() - t0
+    b.close()
+    return {"workload": "64 grids 2D HD Riemann, sides log-uniform [64,1024] (seeded), "
+                        "cont, minmod, mixed, 50 steps per grid in one graph launch",
+            "grids": 64, "cells": cells, "steps": 50, "seconds": el,
+            "value": cells * 50 / el, "unit": UNIT,
+            "tuned": {"persistent_ctas": ctas, "order": ["round-robin", "grid-major"][order],
+                      "trial_ms": ms}}
+
+
+def run_served(args, capacity):
+    """Config 4: a Poisson stream of 2-D (128^2..2048^2) and 3-D (64^3..256^3)
+    random-mode MHD solves, 20..500 steps each, mixed precision, admitted
+    against a 150 GB HBM budget; p50/p99 time to solution."""
+    import threading
+    from vac_gb300 import abi, inistate
+    from vac_gb300.engine import Server
+    rng = np.random.default_rng(7)
+    reqs = []
+    for i in range(args.served):
+        if rng.uniform() < 0.5:
+            n = int(round(np.exp(rng.uniform(np.log(128), np.log(2048)))))
+            s = inistate.random_modes(n, seed=100 + i, ndim=2)
+        else:
+            n = int(round(np.exp(rng.uniform(np.log(64), np.log(256)))))
+            s = inistate.random_modes(n, seed=100 + i, ndim=3)
+        steps = int(rng.integers(20, 501))
+        p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
+        reqs.append((p, s.x, s.w, steps, int(np.prod(s.w.shape[1:]))))
+    work = [r[4] * r[3] for r in reqs]
+    rate = 0.9 * capacity / np.mean(work)  # offered load ~0.9 of capacity
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    srv = Server(hbm_budget_bytes=150e9, max_active=8, steps_per_chunk=16)
+    ids = [None] * len(reqs)
+    t0 = time.perf_counter()
+
+    def feed():
+        for i, r in enumerate(reqs):
+            dt = arrivals[i] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids[i] = srv.submit(r[0], r[1], r[2], r[3])
+
+    th = threading.Thread(target=feed)
+    th.start()
+    th.join()
+    tts = []
+    for rid in ids:
+        res = srv.result(rid, wait=600.0, fetch=False)
+        tts.append(res[3])
+    st = srv.stats()
+    srv.close()
+    return {"workload": "Poisson stream of %d MHD solves: 2D 128^2-2048^2 / 3D 64^3-256^3, "
+                        "20-500 steps, random modes, mixed, 150 GB budget" % len(reqs),
+            "requests": len(reqs), "offered_rate_per_s": rate,
+            "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+            "value": st["cell_updates"] / st["span_s"] if st["span_s"] > 0 else None,
+            "unit": UNIT, "peak_concurrent": st["peak_active"],
+            "cell_updates": st["cell_updates"], "span_s": st["span_s"]}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -175,6 +251,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--served", type=int, default=12, help="requests in the served stream (0: skip)")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     ws, rank, lrank = dist_setup()
     if args.impl == "reference":
@@ -279,6 +357,12 @@ def main():
                 "rel_l1_mixed_vs_fp64": rel_l1, "rel_linf_mixed_vs_fp64": linf}
         e64.close()
 
+    batched = served = None
+    if rank == 0 and not args.no_batched:
+        batched = run_batched(args)
+    if rank == 0 and args.served > 0:
+        served = run_served(args, value / ws)
+
     cpu = None
     if rank == 0 and ws == 1 and args.cpu_steps > 0:
         threads = os.cpu_count() or 1
@@ -306,7 +390,8 @@ def main():
                              "traffic": traffic, "avg_launch_ms": avg_s * 1e3,
                              "alg_bytes_per_launch": alg_bytes,
                              "kernel_share": shares},
-                "fp64": fp64, "cpu_baseline": cpu, "clocks": clk.summary()}
+                "fp64": fp64, "batched": batched, "served": served,
+                "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:
