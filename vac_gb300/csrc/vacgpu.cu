@@ -172,6 +172,7 @@ struct vacgpu_handle {
   // CUDA graphs of two consecutive steps, keyed by (state buffer, parity
   // of it): replayed instead of re-issuing ~20 launches per step.
   cudaGraphExec_t gexec[2][2];
+  long long glaunch[2][2][VACGPU_K_NCLASS];  // kernels per replay, by class
   bool warmed;
   bool fused;
   CUtensorMap tmap[2];
@@ -393,6 +394,8 @@ int issue_steps(vacgpu_handle* h, int k, int it_base) {
       const int cur0 = h->cur;
       if (!ex) {
         cudaGraph_t gr;
+        long long before[VACGPU_K_NCLASS];
+        memcpy(before, h->nlaunch, sizeof(before));
         CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
         for (int q = 0; q < 2; q++) {
           if (h->elem == 8)
@@ -403,9 +406,14 @@ int issue_steps(vacgpu_handle* h, int k, int it_base) {
         CK(cudaStreamEndCapture(h->st, &gr));
         CK(cudaGraphInstantiate(&ex, gr, 0));
         cudaGraphDestroy(gr);
+        for (int k = 0; k < VACGPU_K_NCLASS; k++) {
+          h->glaunch[cur0][par][k] = h->nlaunch[k] - before[k];
+          h->nlaunch[k] = before[k];  // counted when the graph runs
+        }
         h->cur = cur0;
       }
       CK(cudaGraphLaunch(ex, h->st));
+      for (int k = 0; k < VACGPU_K_NCLASS; k++) h->nlaunch[k] += h->glaunch[cur0][par][k];
       h->cur = cur0 ^ ((2 * nsw) & 1);
       s += 2;
     } else {
