@@ -1,0 +1,87 @@
+"""vacgb, the drop-in host program: VAC par files (namelists with repeat
+counts, subscripts, comments, &end) and .ini files in, .out snapshots and
+.log rows out, exactly where VAC's timetosave puts them."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from vac_gb300 import abi, inistate, vacfile
+
+PAR = """ &testlist /
+ &filelist
+        filenameini='ot.ini'                ! initial file
+        filename='ot.log','ot.out'
+ /
+ &savelist
+        ditsave=5,10
+ /
+ &stoplist
+        itmax=20
+ /
+ &methodlist
+        typefull=   6*'tvdlf'
+        typelimiter=6*'woodward'
+        typelimiter(2)='minmod'
+        dimsplit=T
+        smallpcoeff=1.D-6
+ &end
+ &boundlist
+        typeB=6*'periodic',6*'periodic',
+              12*'periodic'
+        typeB(1,3)='periodic'
+ /
+ &paramlist
+        courantpar=0.8D0
+ /
+"""
+
+
+@pytest.fixture(scope="module")
+def vacgb():
+    from vac_gb300 import build
+    build.build()
+    return build.VACGB
+
+
+def _setup(tmp_path, n=32):
+    s = inistate.orszag_tang(n)
+    vacfile.write(str(tmp_path / "ot.ini"), s)
+    (tmp_path / "ot.par").write_text(PAR)
+    return s
+
+
+def test_par_parsing(vacgb, tmp_path):
+    _setup(tmp_path)
+    out = subprocess.run([vacgb, "--dump-params"], cwd=tmp_path, capture_output=True,
+                         text=True, input=PAR, check=True).stdout
+    d = json.loads(out)
+    assert (d["ndim"], d["ndir"], d["physics"], d["nw"]) == (2, 2, abi.PHYS_MHD, 6)
+    assert d["typelimiter"] == [1, 0, 1, 1, 1, 1]
+    assert d["typeB"] == [[1] * 6] * 4
+    assert d["ditsave"] == [5, 10] and d["itmax"] == 20
+    assert d["filenames"] == ["ot.log", "ot.out"]
+    assert abs(d["gamma"] - 5.0 / 3.0) < 1e-15
+
+
+@pytest.mark.gpu
+def test_run_writes_vac_outputs(vacgb, tmp_path):
+    s = _setup(tmp_path)
+    r = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True,
+                       input=PAR)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Finish Advance" in r.stdout
+    p = inistate.params_for(s, limiter="woodward")
+    p.typelimiter[1] = abi.LIM_MINMOD
+    o = Oracle(p, s.x, s.w)
+    for snap, it in ((1, 10), (2, 20)):
+        got = vacfile.read(str(tmp_path / "ot.out"), snapshot=snap)
+        o.step(it - o.it)
+        assert got.it == it and got.t == o.t
+        assert np.array_equal(got.w.view(np.uint64), o.state().view(np.uint64))
+    rows = [ln.split() for ln in open(tmp_path / "ot.log").read().splitlines()[2:]]
+    assert [int(r[0]) for r in rows] == [5, 10, 15, 20]
+    np.testing.assert_allclose([float(v) for v in rows[-1][3:]], o.sums(), rtol=1e-5)

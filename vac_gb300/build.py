@@ -17,6 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 LIB = os.path.join(LIBDIR, "libvacgpu.so")
+BINDIR = os.path.join(HERE, "bin")
+VACGB = os.path.join(BINDIR, "vacgb")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # (source, extra flags)
@@ -68,6 +70,16 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
+    # the host program (a drop-in for VAC's `vac` on this path)
+    src = os.path.join(HERE, "host", "vacgb.cpp")
+    os.makedirs(BINDIR, exist_ok=True)
+    if not os.path.exists(VACGB) or os.path.getmtime(VACGB) < max(
+            os.path.getmtime(src), os.path.getmtime(LIB)):
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", src, "-o", VACGB,
+               "-L" + LIBDIR, "-lvacgpu", "-Wl,-rpath,$ORIGIN/../lib"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host program build failed:\n" + r.stderr)
     return LIB
 
 
