@@ -84,4 +84,5 @@ def test_run_writes_vac_outputs(vacgb, tmp_path):
         assert np.array_equal(got.w.view(np.uint64), o.state().view(np.uint64))
     rows = [ln.split() for ln in open(tmp_path / "ot.log").read().splitlines()[2:]]
     assert [int(r[0]) for r in rows] == [5, 10, 15, 20]
-    np.testing.assert_allclose([float(v) for v in rows[-1][3:]], o.sums(), rtol=1e-5)
+    np.testing.assert_allclose([float(v) for v in rows[-1][3:]], o.sums(), rtol=1e-5,
+                               atol=1e-12)  # momentum means are round-off sized
