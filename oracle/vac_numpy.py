@@ -331,7 +331,8 @@ class NumpyVac:
             wLC[A] = HALF * (wLC[A] + wRC[A])
             cmax = np.zeros(self.nG)
             cmax[ixC.sl()] = self.getcmax(wLC, ixC, idim, {})
-            if self.courantpar > ZERO and self.istep == 2:
+            nstep = 1 if self.p.typefull == abi.TVDLF1 else 2
+            if self.courantpar > ZERO and self.istep == nstep:
                 q = cmax[ixC.sl()] * TWO / (self.dx[(idim,) + ixC.sl()]
                                             + self.dx[(idim,) + ixC.sl(idim, 1)])
                 cm = q.max()
@@ -359,6 +360,11 @@ class NumpyVac:
 
     def advect(self, d0, d1):
         w1 = self.w.copy()
+        if self.p.typefull == abi.TVDLF1:  # typepred1='nul': onestep
+            self.istep = 1
+            self.tvdmusclf(self.dt, self.ixM, d0, d1, w1, self.w)
+            self.getboundary(self.w)
+            return
         self.istep = 1
         self.hancock(self.dt / 2, self.ixM, d0, d1, self.w, w1)
         self.getboundary(w1)

@@ -626,10 +626,16 @@ static void advect1(vo_state* s, int pred, double qdt, int idimmin,
   getboundary(s, w);
 }
 
-/* advect, src/vac.t:363-486 with typeadvance='twostep' */
+/* advect, src/vac.t:363-486.  'tvdlf' has the default predictor 'hancock'
+ * (twostep); 'tvdlf1' has typepred1='nul', which turns twostep into onestep
+ * (src/vacio.t:286-299,511): one tvdlf1 substep with wCT = a copy of w. */
 static void advect(vo_state* s, int idimmin, int idimmax) {
   memcpy(s->w1, s->w, sizeof(double) * s->N * s->nw);
   s->istep = 0;
+  if (s->p.typefull == VACGPU_TVDLF1) {
+    advect1(s, 0, s->dt, idimmin, idimmax, s->w1, s->w);
+    return;
+  }
   advect1(s, 1, s->dt / 2, idimmin, idimmax, s->w, s->w1);
   advect1(s, 0, s->dt, idimmin, idimmax, s->w1, s->w);
 }
@@ -757,7 +763,7 @@ vo_state* vo_create(const vacgpu_params* p) {
   s->smallp = p->smallp;
   s->courantpar = p->courantpar;
   s->dtpar = p->dtpar;
-  s->nstep = 2;
+  s->nstep = p->typefull == VACGPU_TVDLF1 ? 1 : 2;  /* onestep / twostep */
   /* startup, src/vac.t:160-220 */
   for (int d = 0; d < 3; d++) s->dtcourant[d] = BIGDOUBLE;
   if (s->dtpar > ZERO && p->slowsteps != 1) s->courantpar = -ONE;

@@ -281,7 +281,24 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   if (h->p.typelimited == VACGPU_LIMITED_PREDICTOR) base = w1;
   if (h->p.typelimited == VACGPU_LIMITED_PREVIOUS && h->p.dimsplit)
     base = (const T*)h->wold;
-  if (sizeof(T) == 8) {
+  if (h->p.typefull == VACGPU_TVDLF1) {
+    // typepred1='nul': onestep, the corrector alone with wCT = w
+    // (src/vacio.t:286-299,511); no limiter, so the base is unused
+    kbegin(h, VACGPU_K_CORRECT);
+    if (sizeof(T) == 8)
+      launch_correct_fp64(a, (const double*)w, (const double*)w,
+                          (const double*)w, (double*)wout, h->st);
+    else
+      launch_correct_mixed(a, (const float*)w, (const float*)w,
+                           (const float*)w, (float*)wout, h->st);
+    kend(h);
+    kbegin(h, VACGPU_K_GHOST);
+    if (sizeof(T) == 8)
+      launch_ghost_fp64(a, (double*)wout, h->st);
+    else
+      launch_ghost_mixed(a, (float*)wout, h->st);
+    kend(h);
+  } else if (sizeof(T) == 8) {
     kbegin(h, VACGPU_K_PREDICT);
     launch_predict_fp64(a, (const double*)w, (double*)w1, h->st);
     kend(h);
@@ -624,7 +641,8 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   if (const char* nz = getenv("VACGPU_NZC")) h->nzc = atoi(nz) > 0 ? atoi(nz) : 32;
   h->fused = p->precision == VACGPU_PREC_MIXED && p->dimsplit &&
              (p->ndim == 2 || p->ndim == 3) && p->ndir == p->ndim &&
-             p->typelimited == VACGPU_LIMITED_ORIGINAL;
+             p->typelimited == VACGPU_LIMITED_ORIGINAL &&
+             p->typefull == VACGPU_TVDLF;
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
   for (int d = 0; d < p->ndim; d++)  // the fused epilogue needs uniform maps
     if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED) h->fused = false;
