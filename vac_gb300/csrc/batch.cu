@@ -39,7 +39,7 @@ struct HandleView {
   const float* dxf[3];
   const float* idxf[3];
   Ctrl* ctrl;
-  const void* tmap[2];
+  const void* tmap[2][2];  // [state buffer][box: x/z sweeps, y sweep]
   int nzc;
   bool fused;
 };
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(FT_NT, 2)
     if (threadIdx.x == 0) {
       const int src = in->fa.ctrl->cur ^ (sweep & 1);
       fa.wout = in->buf[src ^ 1];
-      mapidx = item.inst * 2 + src;
+      mapidx = item.inst * 4 + src * 2 + (D == 1);
     }
     __syncthreads();
     bool ok = Fused<NDIM, D, MHD, PREC_FF, LIMC>::run(
@@ -137,15 +137,18 @@ struct vacgpu_batch {
   vacgpu_params p0;
   std::vector<vacgpu_handle*> h;
   BInst* d_insts;
-  CUtensorMap* d_maps;
+  CUtensorMap* d_maps;  // per grid: [state buffer][box: x/z, y]
   Ctrl** d_ctrls;
-  BItem* d_items[2];  // work list: 0 interleaved over grids, 1 grid-major
-  int nitems;
+  // work lists per sweep direction (tile shapes differ): order 0
+  // interleaved over grids, 1 grid-major
+  BItem* d_items[3][2];
+  int nitems[3];
   long long ghost_total;
   cudaStream_t st;
   int nw;
   bool ready;
-  // launch shape (autotuned): persistent CTAs and work-list order
+  // launch shape (autotuned): persistent CTAs (0: one per work item) and
+  // work-list order
   int ctas, order;
   bool tuned;
   double tune_ms[8];
@@ -171,9 +174,12 @@ int bfail(const std::string& m) { return vacgpu_internal_fail(m.c_str()); }
 
 template <int NDIM, bool MHD>
 void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
-                    const BItem* items) {
+                    int order) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
-  const int smem = fused_smem_floats(NW) * 4;
+  const int smem = fused_smem_floats(NW, D) * 4;
+  const int n = b->nitems[D];
+  const BItem* items = b->d_items[D][order];
+  if (ctas <= 0 || ctas > n) ctas = n;
 #define KB(DD, LL)                                                          \
   {                                                                         \
     auto k = kb_sweep<NDIM, DD, MHD, LL>;                                   \
@@ -183,8 +189,7 @@ void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
                            smem);                                           \
       attr = true;                                                          \
     }                                                                       \
-    k<<<ctas, FT_NT, smem, b->st>>>(items, b->nitems, b->d_insts, b->d_maps, \
-                                    sweep);                                 \
+    k<<<ctas, FT_NT, smem, b->st>>>(items, n, b->d_insts, b->d_maps, sweep); \
   }
 #define KBL(DD)                                 \
   if (LIMC == LIMC_WOODWARD) KB(DD, LIMC_WOODWARD) \
@@ -197,8 +202,7 @@ void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
 #undef KB
 }
 
-void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas,
-                      const BItem* items) {
+void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas, int order) {
   const vacgpu_params& p = b->p0;
   int l0 = p.typelimiter[0];
   bool uni = p.typefull != VACGPU_TVDLF1;
@@ -209,16 +213,16 @@ void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas,
                                              : LIMC_RUNTIME;
   const bool mhd = p.physics == VACGPU_PHYS_MHD;
   if (p.ndim == 2) {
-    if (mhd) launch_sweep_b<2, true>(b, D, LIMC, sweep, ctas, items);
-    else launch_sweep_b<2, false>(b, D, LIMC, sweep, ctas, items);
+    if (mhd) launch_sweep_b<2, true>(b, D, LIMC, sweep, ctas, order);
+    else launch_sweep_b<2, false>(b, D, LIMC, sweep, ctas, order);
   } else {
-    if (mhd) launch_sweep_b<3, true>(b, D, LIMC, sweep, ctas, items);
-    else launch_sweep_b<3, false>(b, D, LIMC, sweep, ctas, items);
+    if (mhd) launch_sweep_b<3, true>(b, D, LIMC, sweep, ctas, order);
+    else launch_sweep_b<3, false>(b, D, LIMC, sweep, ctas, order);
   }
 }
 
 // One step of every grid (the body of VAC's time loop, batched).
-void issue_step(vacgpu_batch* b, int parity, int ctas, const BItem* items) {
+void issue_step(vacgpu_batch* b, int parity, int ctas, int order) {
   const vacgpu_params& p = b->p0;
   const int n = b->n;
   const bool mhd = p.physics == VACGPU_PHYS_MHD;
@@ -241,7 +245,7 @@ void issue_step(vacgpu_batch* b, int parity, int ctas, const BItem* items) {
   const unsigned gb = 152 * 4;
   for (int s = 0; s < nsw; s++) {
     const int D = (!parity || p.typedimsplit == VACGPU_SPLIT_XY) ? s : nsw - 1 - s;
-    launch_sweep_any(b, D, s, ctas, items);
+    launch_sweep_any(b, D, s, ctas, order);
     switch (b->nw) {
       case 4: kb_ghost<4><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
       case 5: kb_ghost<5><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
@@ -256,9 +260,8 @@ int prepare(vacgpu_batch* b) {
   if (b->ready) return 0;
   const int n = b->n;
   std::vector<BInst> ins(n);
-  std::vector<CUtensorMap> maps(2 * n);
+  std::vector<CUtensorMap> maps(4 * n);
   std::vector<Ctrl*> ctrls(n);
-  std::vector<BItem> items;
   long long g0 = 0;
   for (int i = 0; i < n; i++) {
     HandleView v;
@@ -288,43 +291,51 @@ int prepare(vacgpu_batch* b) {
     bi.buf[1] = v.buf[1];
     bi.ghost0 = g0;
     g0 += ghost_count(v.g);
-    memcpy(&maps[2 * i], v.tmap[0], sizeof(CUtensorMap));
-    memcpy(&maps[2 * i + 1], v.tmap[1], sizeof(CUtensorMap));
+    for (int k = 0; k < 4; k++)
+      memcpy(&maps[4 * i + k], v.tmap[k / 2][k % 2], sizeof(CUtensorMap));
     ctrls[i] = v.ctrl;
   }
   b->ghost_total = g0;
-  // work list: every (grid, tile, z chunk); order 0 round-robin over grids
-  // (neighbouring CTAs work on different grids), order 1 grid-major
-  std::vector<std::vector<BItem>> per(n);
-  for (int i = 0; i < n; i++) {
-    const DevGrid& g = ins[i].fa.g;
-    int nbx = (g.nx[0] + FT_X - 1) / FT_X, nby = (g.nx[1] + FT_Y - 1) / FT_Y;
-    int nbz = g.ndim == 3 ? (g.nx[2] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
-    for (int z = 0; z < nbz; z++)
-      for (int y = 0; y < nby; y++)
-        for (int x = 0; x < nbx; x++) per[i].push_back({i, x, y, z});
-  }
-  std::vector<BItem> rr, gm;
-  size_t maxk = 0;
-  for (auto& v : per) maxk = std::max(maxk, v.size());
-  for (size_t k = 0; k < maxk; k++)
-    for (int i = 0; i < n; i++)
-      if (k < per[i].size()) rr.push_back(per[i][k]);
-  // grid-major, largest grid first
-  std::vector<int> idx(n);
-  for (int i = 0; i < n; i++) idx[i] = i;
-  std::sort(idx.begin(), idx.end(), [&](int a, int c) { return per[a].size() > per[c].size(); });
-  for (int i : idx) gm.insert(gm.end(), per[i].begin(), per[i].end());
-  b->nitems = (int)rr.size();
   BCK(cudaMalloc(&b->d_insts, sizeof(BInst) * n));
-  BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 2 * n));
+  BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 4 * n));
   BCK(cudaMalloc(&b->d_ctrls, sizeof(Ctrl*) * n));
-  for (int o = 0; o < 2; o++) BCK(cudaMalloc(&b->d_items[o], sizeof(BItem) * b->nitems));
   BCK(cudaMemcpy(b->d_insts, ins.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice));
-  BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 2 * n, cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 4 * n, cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_ctrls, ctrls.data(), sizeof(Ctrl*) * n, cudaMemcpyHostToDevice));
-  BCK(cudaMemcpy(b->d_items[0], rr.data(), sizeof(BItem) * b->nitems, cudaMemcpyHostToDevice));
-  BCK(cudaMemcpy(b->d_items[1], gm.data(), sizeof(BItem) * b->nitems, cudaMemcpyHostToDevice));
+  // work lists: every (grid, tile, z chunk) of the tile shape of each sweep
+  // direction; order 0 round-robin over grids (neighbouring CTAs work on
+  // different grids), order 1 grid-major, largest grid first
+  for (int D = 0; D < b->p0.ndim; D++) {
+    const int tx = D == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
+    const int ty = D == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
+    std::vector<std::vector<BItem>> per(n);
+    for (int i = 0; i < n; i++) {
+      const DevGrid& g = ins[i].fa.g;
+      const int nbx = (g.nx[0] + tx - 1) / tx, nby = (g.nx[1] + ty - 1) / ty;
+      const int nbz = g.ndim == 3 ? (g.nx[2] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
+      for (int z = 0; z < nbz; z++)
+        for (int y = 0; y < nby; y++)
+          for (int x = 0; x < nbx; x++) per[i].push_back({i, x, y, z});
+    }
+    std::vector<BItem> rr, gm;
+    size_t maxk = 0;
+    for (auto& v : per) maxk = std::max(maxk, v.size());
+    for (size_t k = 0; k < maxk; k++)
+      for (int i = 0; i < n; i++)
+        if (k < per[i].size()) rr.push_back(per[i][k]);
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++) idx[i] = i;
+    std::sort(idx.begin(), idx.end(),
+              [&](int a, int c) { return per[a].size() > per[c].size(); });
+    for (int i : idx) gm.insert(gm.end(), per[i].begin(), per[i].end());
+    b->nitems[D] = (int)rr.size();
+    for (int o = 0; o < 2; o++) {
+      const std::vector<BItem>& l = o ? gm : rr;
+      BCK(cudaMalloc(&b->d_items[D][o], sizeof(BItem) * l.size()));
+      BCK(cudaMemcpy(b->d_items[D][o], l.data(), sizeof(BItem) * l.size(),
+                     cudaMemcpyHostToDevice));
+    }
+  }
   b->ready = true;
   return 0;
 }
@@ -365,7 +376,7 @@ int autotune(vacgpu_batch* b) {
     return 0;
   };
   if (copy(true)) return 1;
-  const int cand_ctas[3] = {152, 304, b->nitems};
+  const int cand_ctas[3] = {152, 304, 0};  // 0: one CTA per work item
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -374,11 +385,11 @@ int autotune(vacgpu_batch* b) {
   for (int c = 0; c < 3; c++)
     for (int o = 0; o < 2; o++, k++) {
       launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
-      issue_step(b, b->it0 & 1, cand_ctas[c], b->d_items[o]);  // warm
+      issue_step(b, b->it0 & 1, cand_ctas[c], o);  // warm
       if (copy(false)) return 1;
       launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
       cudaEventRecord(e0, b->st);
-      issue_step(b, b->it0 & 1, cand_ctas[c], b->d_items[o]);
+      issue_step(b, b->it0 & 1, cand_ctas[c], o);
       cudaEventRecord(e1, b->st);
       cudaEventSynchronize(e1);
       float ms = 0.f;
@@ -484,7 +495,7 @@ int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop) {
     BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     launchb_control(4, b->d_ctrls, b->n, b->p0, 0, nsteps, tstop, b->st);
     for (int s = 0; s < nsteps; s++)
-      issue_step(b, (par + s) & 1, b->ctas, b->d_items[b->order]);
+      issue_step(b, (par + s) & 1, b->ctas, b->order);
     BCK(cudaStreamEndCapture(b->st, &gr));
     BCK(cudaGraphInstantiate(&ex, gr, 0));
     cudaGraphDestroy(gr);
@@ -524,7 +535,7 @@ int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
 int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, double* ms) {
   if (!b) return bfail("null batch");
   if (prepare(b) || autotune(b)) return 1;
-  if (ctas) *ctas = b->ctas;
+  if (ctas) *ctas = b->ctas > 0 ? b->ctas : b->nitems[0];
   if (order) *order = b->order;
   if (ms)
     for (int k = 0; k < 6; k++) ms[k] = b->tune_ms[k];
@@ -539,8 +550,8 @@ void vacgpu_batch_destroy(vacgpu_batch* b) {
   cudaFree(b->d_insts);
   cudaFree(b->d_maps);
   cudaFree(b->d_ctrls);
-  cudaFree(b->d_items[0]);
-  cudaFree(b->d_items[1]);
+  for (int D = 0; D < 3; D++)
+    for (int o = 0; o < 2; o++) cudaFree(b->d_items[D][o]);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }

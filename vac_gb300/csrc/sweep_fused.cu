@@ -3,13 +3,13 @@
 
 namespace vacgpu {
 
-int fused_smem_bytes(int nw) { return fused_smem_floats(nw) * 4; }
+int fused_smem_bytes(int nw, int d) { return fused_smem_floats(nw, d) * 4; }
 
 template <int NDIM, int D, bool MHD, int LIMC>
 static void launch_lim(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
                        cudaStream_t st) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
-  const int smem = fused_smem_floats(NW) * 4;
+  const int smem = fused_smem_floats(NW, D) * 4;
   auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF, LIMC>;
   static bool attr = false;
   if (!attr) {
@@ -59,7 +59,9 @@ bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
       if (s.ph.typeB[2 * d][v] == VACGPU_BC_ASYMM) a.asymm_lo[d] |= 1 << v;
       if (s.ph.typeB[2 * d + 1][v] == VACGPU_BC_ASYMM) a.asymm_hi[d] |= 1 << v;
     }
-  dim3 grid((s.g.nx[0] + FT_X - 1) / FT_X, (s.g.nx[1] + FT_Y - 1) / FT_Y,
+  const int tx = s.d0 == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
+  const int ty = s.d0 == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
+  dim3 grid((s.g.nx[0] + tx - 1) / tx, (s.g.nx[1] + ty - 1) / ty,
             nd == 3 ? (s.g.nx[2] + nzc - 1) / nzc : 1);
   a.zchunks = grid.z;
   const CUtensorMap* map = (const CUtensorMap*)tmap;

@@ -128,7 +128,7 @@ struct HandleView {
   const float* dxf[3];
   const float* idxf[3];
   Ctrl* ctrl;
-  const void* tmap[2];
+  const void* tmap[2][2];  // [state buffer][box: x/z sweeps, y sweep]
   int nzc;
   bool fused;
 };
@@ -175,7 +175,7 @@ struct vacgpu_handle {
   long long glaunch[2][2][VACGPU_K_NCLASS];  // kernels per replay, by class
   bool warmed;
   bool fused;
-  CUtensorMap tmap[2];
+  CUtensorMap tmap[2][2];  // [state buffer][box: x/z sweeps, y sweep]
   float* idxf[3];
   int nzc;
 };
@@ -236,8 +236,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 4-D map over one FP32 state buffer: (column, gy, gz, variable), box
-// {40, 12, 1, nw} = one plane of a 32x8 tile with its 2-cell halo.
-bool make_tmap(vacgpu_handle* h, void* base, CUtensorMap* m) {
+// {40, rows, 1, nw} = one plane of a tile with its 2-cell halo.
+bool make_tmap(vacgpu_handle* h, void* base, int rows, CUtensorMap* m) {
   auto fn = encode_fn();
   if (!fn) return false;
   const DevGrid& g = h->g;
@@ -245,7 +245,7 @@ bool make_tmap(vacgpu_handle* h, void* base, CUtensorMap* m) {
                         (cuuint64_t)g.nG[2], (cuuint64_t)h->nw};
   cuuint64_t strides[3] = {(cuuint64_t)g.P * 4, (cuuint64_t)g.plane * 4,
                            (cuuint64_t)g.vs * 4};
-  cuuint32_t box[4] = {40, 12, 1, (cuuint32_t)h->nw};
+  cuuint32_t box[4] = {40, (cuuint32_t)rows, 1, (cuuint32_t)h->nw};
   cuuint32_t es[4] = {1, 1, 1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides,
                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -314,7 +314,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
     kbegin(h, VACGPU_K_SWEEP);
-    launch_sweep_fused(a, &h->tmap[h->cur], (float*)wout, h->idxf, h->nzc,
+    launch_sweep_fused(a, &h->tmap[h->cur][d0 == 1], (float*)wout, h->idxf, h->nzc,
                        h->st);
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
@@ -501,8 +501,8 @@ int vacgpu_internal_view(vacgpu_handle* h, HandleView* v) {
     v->idxf[d] = h->idxf[d];
   }
   v->ctrl = h->ctrl;
-  v->tmap[0] = &h->tmap[0];
-  v->tmap[1] = &h->tmap[1];
+  for (int i = 0; i < 2; i++)
+    for (int k = 0; k < 2; k++) v->tmap[i][k] = &h->tmap[i][k];
   v->nzc = h->nzc;
   v->fused = h->fused;
   return 0;
@@ -648,7 +648,9 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED) h->fused = false;
   if (h->fused) {
     bool ok = true;
-    for (int i = 0; i < 2 && ok; i++) ok = make_tmap(h, h->buf[i], &h->tmap[i]);
+    for (int i = 0; i < 2 && ok; i++)
+      for (int k = 0; k < 2 && ok; k++)
+        ok = make_tmap(h, h->buf[i], FUSED_BOX_ROWS[k], &h->tmap[i][k]);
     for (int d = 0; d < 3 && ok; d++)
       ok = cudaMalloc(&h->idxf[d], sizeof(float) * g.nG[d]) == cudaSuccess;
     if (!ok) {

@@ -175,10 +175,13 @@ VACGPU_DECLARE_LAUNCHERS(mixedf32, float)
 
 // Fused single-kernel sweep of the mixed path (sweep_fused.cu): returns
 // false when no fused instance exists for the configuration.  `tmap` is the
-// CUtensorMap (as bytes) of the input state buffer.
+// CUtensorMap (as bytes) of the input state buffer with the box of the sweep
+// direction (fused_box_rows).
 bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
                         const float* const* idxf, int nzc, cudaStream_t st);
-int fused_smem_bytes(int nw);
+// rows of the fused sweep's TMA box: x and z sweeps (k=0), y sweep (k=1)
+constexpr int FUSED_BOX_ROWS[2] = {12, 10};
+int fused_smem_bytes(int nw, int d);
 
 // Precision-independent time-loop kernels (control.cu).
 void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st);
