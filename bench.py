@@ -39,10 +39,13 @@ NW = 8
 
 
 def workload_config(prec_name):
-    return {"workload": "3D ideal MHD TVDLF+woodward 256^3 periodic, random modes "
-                        "(seeded), 100-step config timed per step",
+    mb = NW * 4 * N ** 3 / 1e6
+    return {"workload": "3D ideal MHD TVDLF+woodward %d^3 periodic, random modes "
+                        "(seeded), 100-step config timed per step" % N,
             "grid": [N, N, N], "nw": NW, "limiter": "woodward",
-            "precision": prec_name, "l2": "state > L2 (537 MB FP32), no flush needed"}
+            "precision": prec_name,
+            "l2": "state > L2 (%.0f MB FP32), no flush needed" % mb if mb > 129
+                  else "state fits L2 (%.0f MB FP32)" % mb}
 
 
 class ClockSampler:
@@ -244,6 +247,7 @@ def run_reference(args, ws, rank):
 
 
 def main():
+    global N
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -253,7 +257,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--served", type=int, default=12, help="requests in the served stream (0: skip)")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--side", type=int, default=N,
+                    help="cells per side of the cube (smaller cases for profiling)")
     args = ap.parse_args()
+    N = args.side
     ws, rank, lrank = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -368,8 +375,8 @@ def main():
         threads = os.cpu_count() or 1
         v, t = cpu_sample(snap, args.cpu_steps, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d full 256^3 steps of the FP64 oracle port (OpenMP, %d threads), "
-                         "%.1f s" % (args.cpu_steps, threads, t)}
+               "sample": "%d full %d^3 steps of the FP64 oracle port (OpenMP, %d threads), "
+                         "%.1f s" % (args.cpu_steps, N, threads, t)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,

@@ -280,6 +280,8 @@ int prepare(vacgpu_batch* b) {
     }
     a.ctrl = v.ctrl;
     a.nzc = v.nzc;
+    for (int d = 0; d < 3; d++) a.gravf[d] = (float)v.ph.src_par[d];
+    a.cfl = v.ph.courantpar > 0.0;
     for (int d = 0; d < 3; d++)
       for (int w = 0; w < b->nw; w++) {
         if (v.ph.typeB[2 * d][w] == VACGPU_BC_PERIODIC) a.periodic_mask[d] |= 1 << w;

@@ -132,6 +132,8 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
   ph.gamma = p->eqpar[0];
   ph.pt1 = 1.0 - 0.5 * p->eqpar[0];
   ph.gm1 = p->eqpar[0] - 1.0;
+  ph.gammaf = (float)ph.gamma;
+  ph.gm1f = (float)ph.gm1;
   ph.pt3 = 0.5 * (p->eqpar[0] - 1.0);
   ph.smallpcoeff = p->smallpcoeff;
   ph.courantpar = courantmax ? 1.0 : -1.0;

@@ -138,7 +138,7 @@ struct PHMixed {
     const float rinv = 1.0f / u[0];
     const float v = u[1 + d] * rinv;
     float hbb;
-    float p = pressure_mixed<NDIR, MHD ? NDIR : 0, PM>(u, rinv, (float)k.gm1,
+    float p = pressure_mixed<NDIR, MHD ? NDIR : 0, PM>(u, rinv, k.gm1f,
                                                        &hbb);
     if (MHD) {
       const float pt = p + hbb;
@@ -183,10 +183,10 @@ struct PHMixed {
     const int E = NDIR + 1;
     const float rinv = 1.0f / u[0];
     float hbb;
-    float p = pressure_mixed<NDIR, MHD ? NDIR : 0, PM>(u, rinv, (float)k.gm1,
+    float p = pressure_mixed<NDIR, MHD ? NDIR : 0, PM>(u, rinv, k.gm1f,
                                                        &hbb);
     p = p >= smallp ? p : smallp;
-    const float cs2 = (float)k.gamma * p * rinv;
+    const float cs2 = k.gammaf * p * rinv;
     if (MHD) {
       const float cf2 = 2.0f * hbb * rinv + cs2;
       const float bi = u[E + 1 + d];

@@ -52,6 +52,8 @@ bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
   a.ctrl = s.ctrl;
   a.wout = wout;
   a.nzc = nzc;
+  for (int d = 0; d < 3; d++) a.gravf[d] = (float)s.ph.src_par[d];
+  a.cfl = s.ph.courantpar > 0.0;
   const int nw = s.mhd ? 2 + 2 * s.ndir : 2 + s.ndir;
   for (int d = 0; d < 3; d++)
     for (int v = 0; v < nw; v++) {

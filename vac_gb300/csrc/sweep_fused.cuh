@@ -59,11 +59,11 @@ __host__ __device__ constexpr int fused_slot_floats(int nw, int D) {
 }
 
 // shared-memory floats of the sweep in direction D for nw variables:
-// state ring, two predictor planes, face fluxes, slopes
+// state ring, two predictor planes, two face-flux planes, slopes
 __host__ __device__ constexpr int fused_smem_floats(int nw, int D) {
   return FWRING * fused_slot_floats(nw, D) +
          2 * nw * (D == 0 ? TileCfg<0>::RN : D == 1 ? TileCfg<1>::RN : TileCfg<2>::RN) +
-         (D == 2 ? 0 : nw * (D == 0 ? TileCfg<0>::NF : TileCfg<1>::NF) + nw * 256);
+         (D == 2 ? 0 : 2 * nw * (D == 0 ? TileCfg<0>::NF : TileCfg<1>::NF) + nw * 256);
 }
 
 // rows of the TMA box of direction D (one tensor map per box shape)
@@ -87,6 +87,8 @@ struct FusedArgs {
   int zchunks;
   int periodic_mask[3];  // bit iw set: variable iw periodic in dimension d
   int asymm_lo[3], asymm_hi[3];  // bit iw set: 'asymm' at that face
+  float gravf[3];        // gravity source parameters (FP32)
+  int cfl;               // evaluate the CFL maximum (courantpar > 0)
 };
 
 // ------------------------------------------------------------ TMA/mbarrier
@@ -167,16 +169,17 @@ struct Fused {
   static constexpr int SLOT = fused_slot_floats(NW, D);
   typedef PHMixed<PM> PH;
 
-  // shared memory: state ring | w1 slot 0 | w1 slot 1 | faces | slopes
-  // (predictor plane p in slot p & 1)
+  // shared memory: state ring | w1 slot 0 | w1 slot 1 | faces 0 | faces 1
+  // | slopes (predictor plane p in w1 slot p & 1; the faces of plane p in
+  // face slot (p + 1) & 1)
   static __device__ __forceinline__ float* w1slot(float* sm, int p) {
     return sm + FWRING * SLOT + (p & 1) * NW * C::RN;
   }
-  static __device__ __forceinline__ float* fbuf(float* sm) {
-    return sm + FWRING * SLOT + 2 * NW * C::RN;
+  static __device__ __forceinline__ float* fbuf(float* sm, int p) {
+    return sm + FWRING * SLOT + 2 * NW * C::RN + ((p + 1) & 1) * NW * C::NF;
   }
   static __device__ __forceinline__ float* ldbuf(float* sm) {
-    return fbuf(sm) + NW * C::NF;
+    return sm + FWRING * SLOT + 2 * NW * C::RN + 2 * NW * C::NF;
   }
   // state plane slot: [v][sy][sx]
   static __device__ __forceinline__ float W(const float* s, int v, int sy,
@@ -224,12 +227,12 @@ struct Fused {
     if (a.ph.src_id == VACGPU_SRC_GRAVITY) {
 #pragma unroll
       for (int d = 1; d <= NDIM; d++) {
-        const float gr = (float)a.ph.src_par[d - 1];
+        const float gr = a.gravf[d - 1];
         if (gr != 0.0f) acc[d] = acc[d] + (qs * gr) * wc[0];
       }
 #pragma unroll
       for (int d = 1; d <= NDIM; d++) {
-        const float gr = (float)a.ph.src_par[d - 1];
+        const float gr = a.gravf[d - 1];
         if (gr != 0.0f) acc[E] = acc[E] + (qs * gr) * wc[d];
       }
     }
@@ -351,38 +354,40 @@ struct Fused {
   }
 
   // getboundary on w1: region cells in the first ghost layer of a
-  // non-periodic x/y face take the adjacent mesh value; at a z face the
-  // whole plane does (-1 from 0, nz from nz-1).
+  // non-periodic x/y face take the adjacent mesh value (when xy is set);
+  // at a z face the whole plane does (-1 from 0, nz from nz-1).
   static __device__ void fix_w1_ghosts(const FusedArgs& a, float* sm, int j,
-                                       int x0, int y0) {
+                                       int x0, int y0, bool xy, bool z) {
     const DevGrid& g = a.g;
     float* w1j = w1slot(sm, j);
-    for (int c = threadIdx.x; c < C::RN; c += FT_NT) {
-      const int rx = c % C::RX, ry = c / C::RX;
-      const int ix = x0 + rx - 1, iy = y0 + ry - 1;
-      int d = -1, src = c, lo = 0;
-      if ((ix == -1 || ix == g.nx[0]) && (NDIM < 2 || (iy >= 0 && iy < g.nx[1]))) {
-        d = 0;
-        lo = ix == -1;
-        src = c + (lo ? 1 : -1);
-      } else if (NDIM >= 2 && (iy == -1 || iy == g.nx[1]) && ix >= 0 && ix < g.nx[0]) {
-        d = 1;
-        lo = iy == -1;
-        src = c + (lo ? C::RX : -C::RX);
-      }
-      if (d < 0) continue;
-      const int asy = lo ? a.asymm_lo[d] : a.asymm_hi[d];
+    if (xy) {
+      for (int c = threadIdx.x; c < C::RN; c += FT_NT) {
+        const int rx = c % C::RX, ry = c / C::RX;
+        const int ix = x0 + rx - 1, iy = y0 + ry - 1;
+        int d = -1, src = c, lo = 0;
+        if ((ix == -1 || ix == g.nx[0]) && (NDIM < 2 || (iy >= 0 && iy < g.nx[1]))) {
+          d = 0;
+          lo = ix == -1;
+          src = c + (lo ? 1 : -1);
+        } else if (NDIM >= 2 && (iy == -1 || iy == g.nx[1]) && ix >= 0 && ix < g.nx[0]) {
+          d = 1;
+          lo = iy == -1;
+          src = c + (lo ? C::RX : -C::RX);
+        }
+        if (d < 0) continue;
+        const int asy = lo ? a.asymm_lo[d] : a.asymm_hi[d];
 #pragma unroll
-      for (int v = 0; v < NW; v++) {
-        if ((a.periodic_mask[d] >> v) & 1) continue;
-        const float s = w1j[v * C::RN + src];
-        w1j[v * C::RN + c] = ((asy >> v) & 1) ? -s : s;
+        for (int v = 0; v < NW; v++) {
+          if ((a.periodic_mask[d] >> v) & 1) continue;
+          const float s = w1j[v * C::RN + src];
+          w1j[v * C::RN + c] = ((asy >> v) & 1) ? -s : s;
+        }
       }
     }
-    if (NDIM == 3 && (j == 0 || j == g.nx[2])) {
+    if (NDIM == 3 && z) {
       const int dst = j == 0 ? -1 : j, srcp = j == 0 ? 0 : j - 1;
       const int asy = j == 0 ? a.asymm_lo[2] : a.asymm_hi[2];
-      __syncthreads();  // the x/y fix of the source plane is complete
+      if (xy) __syncthreads();  // the x/y fix of the source plane is complete
       float* dp = w1slot(sm, dst);
       const float* sp = w1slot(sm, srcp);
       for (int c = threadIdx.x; c < C::RN; c += FT_NT) {
@@ -396,21 +401,26 @@ struct Fused {
     }
   }
 
-  // The TVDLF faces along D (0 or 1) of plane jo, one per thread, into the
-  // face buffer; slopes from the predictor's slope buffer of plane jo.
+  // The TVDLF faces along D (0 or 1) of plane jo into its face slot: one
+  // face per thread, each warp one row of faces (x: 31 faces, lane 31
+  // idle; y: 32).  The slopes are the predictor's: the thread that predicted
+  // the left/lower cell of the face had this thread's index.
   static __device__ __forceinline__ void in_plane_faces(
       const FusedArgs& a, float* sm, int jo, int x0, int y0, float smallp,
-      unsigned long long& key) {
-    const int f = threadIdx.x;
-    if (f >= C::NF) return;
+      float& qmax) {
+    const int tid = threadIdx.x;
     const DevGrid& g = a.g;
-    int rx, ry;  // left / lower cell of the face, region coordinates
+    int rx, ry, f;  // left / lower cell of the face (region), face index
     if (D == 0) {
-      rx = f % (C::TX + 1);
-      ry = f / (C::TX + 1) + 1;
+      rx = tid % 32;
+      ry = tid / 32 + 1;
+      if (rx > C::TX) return;
+      f = (ry - 1) * (C::TX + 1) + rx;
     } else {
-      rx = f % C::TX + 1;
-      ry = f / C::TX;
+      if (tid >= C::NF) return;
+      rx = tid % 32 + 1;
+      ry = tid / 32;
+      f = tid;
     }
     const int ix = x0 + rx - 1, iy = y0 + ry - 1;
     const bool valid = D == 0 ? (ix >= -1 && ix < g.nx[0] && (NDIM < 2 || iy < g.nx[1]))
@@ -418,10 +428,7 @@ struct Fused {
     if (!valid) return;
     const float* w1o = w1slot(sm, jo);
     const float* lb = ldbuf(sm);
-    // slope-buffer index of the region cell (rx, ry): the predictor
-    // thread that owned it
-    const int fl = D == 0 ? (ry - 1) * 32 + rx : ry * 32 + rx - 1;
-    const int fr = D == 0 ? fl + 1 : fl + 32;
+    const int fr = D == 0 ? tid + 1 : tid + 32;
     const int rl = ry * C::RX + rx;
     const int rr = D == 0 ? rl + 1 : rl + C::RX;
     float wl[NW], wr[NW], ldl[NW], ldr[NW], F[NW];
@@ -429,18 +436,17 @@ struct Fused {
     for (int v = 0; v < NW; v++) {
       wl[v] = w1o[v * C::RN + rl];
       wr[v] = w1o[v * C::RN + rr];
-      ldl[v] = lb[v * 256 + fl];
+      ldl[v] = lb[v * 256 + tid];
       ldr[v] = lb[v * 256 + fr];
     }
     const float cm = face(a, wl, wr, ldl, ldr, smallp, F);
-    float* fb = fbuf(sm);
+    float* fb = fbuf(sm, jo);
 #pragma unroll
     for (int v = 0; v < NW; v++) fb[v * C::NF + f] = F[v];
-    if (a.ph.courantpar > 0.0) {
+    if (a.cfl) {
       const int gi = (D == 0 ? ix : iy) + 2;
       const float q = cm * 2.0f / (a.dxf[D][gi] + a.dxf[D][gi + 1]);
-      const unsigned long long k = dkey((double)q);
-      key = k > key ? k : key;
+      qmax = (q > qmax || q != q) ? q : qmax;  // a NaN sticks
     }
   }
 
@@ -490,14 +496,23 @@ struct Fused {
   // One tile (bx, by) and z chunk bz of one grid.  bars: the CTA's FWRING
   // mbarriers (initialised once); uses[s]: loads completed on slot s before
   // this tile (kept identically by every thread: the phase parity).
-  // Returns false when a TMA wait timed out.
+  // Returns false when a TMA wait timed out.  The caller synchronises the
+  // CTA before reusing the shared memory.
+  //
+  // 3-D plane loop, iteration j (predictor plane j, corrected plane j-1):
+  //   faces of j-1 (x/y sweeps)            reads w1(j-1), slopes(j-1)
+  //   wait for state plane j+1; barrier A  (also: nobody is still in j-1)
+  //   TMA of state plane j+2 into the slot of j-2
+  //   predictor of plane j                 writes w1(j), slopes(j)
+  //   barrier B [ghost fix of w1(j); barrier]
+  //   corrector of plane j-1               reads faces(j-1), w1(j-1), w1(j)
   static __device__ bool run(const CUtensorMap* map, const FusedArgs& a,
                              float* sm, int bx, int by, int bz,
                              unsigned long long* bars, int* uses,
                              unsigned slotid) {
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) return true;
-    __shared__ unsigned long long shkey[FT_NT / 32];
+    __shared__ float shq[FT_NT / 32];
     const int tid = threadIdx.x;
     const DevGrid& g = a.g;
     const int x0 = bx * C::TX, y0 = by * C::TY;
@@ -516,8 +531,14 @@ struct Fused {
     const int colx = cstart & ~3;
     const int sh = cstart - colx;
     const unsigned plane_bytes = NW * C::BPL * 4;
-    const bool bz_edge_only = NDIM == 3 && D < 2;  // planes z0-1, z1: b_z only
     const bool need_bz = MHD && a.ph.divbfix && a.ph.sourceunsplit;
+    // ghost fix of w1 needed: a non-periodic x/y face inside the region,
+    // or (per plane) a non-periodic z face
+    const int all = (1 << NW) - 1;
+    const bool fix_xy =
+        (a.periodic_mask[0] != all && (x0 == 0 || x0 + C::TX >= g.nx[0])) ||
+        (NDIM >= 2 && a.periodic_mask[1] != all && (y0 == 0 || y0 + C::TY >= g.nx[1]));
+    const bool fix_zb = NDIM == 3 && a.periodic_mask[2] != all;
 
     const int pbase = NDIM == 3 ? z0 - 2 : 0;
     auto slot = [&](int p) -> float* { return sm + ((p - pbase) % FWRING) * SLOT; };
@@ -535,13 +556,13 @@ struct Fused {
     // this thread's full-predictor cell (region coordinates)
     const int frx = D == 0 ? tid % 32 : tid % 32 + 1;
     const int fry = D == 1 ? tid / 32 : tid / 32 + 1;
-    // this thread's output cell
-    const bool has_out = tid < C::NOUT;
-    const int lx = tid % C::TX, ly = tid / C::TX;
+    // this thread's output cell: warp ly, lane lx
+    const int lx = tid % 32, ly = tid / 32;
+    const bool has_out = lx < C::TX && ly < C::TY;
     const int oix = x0 + lx, oiy = y0 + ly;
     const bool out_ok = has_out && oix < g.nx[0] && (NDIM < 2 || oiy < g.nx[1]);
 
-    unsigned long long key = 0ULL;
+    float qmax = 0.0f;  // CFL: max cmax*2/(dx_i+dx_i+1) over this thread's faces
     const int pfirst = NDIM == 3 ? z0 - 1 : 0;
     const int plast = NDIM == 3 ? z1 : 0;
     if (tid == 0) {
@@ -553,12 +574,23 @@ struct Fused {
         issue(0);
       }
     }
-    float Lprev[NW], Fprev[NW];  // D == 2: carried along z
+    float Lprev[NW], Fprev[NW];  // z sweep: carried along z
 #pragma unroll
     for (int v = 0; v < NW; v++) Lprev[v] = Fprev[v] = 0.0f;
 
     for (int j = pfirst; j <= plast; j++) {
-      if (NDIM == 3 && tid == 0 && j + 2 <= z1 + 1) issue(j + 2);
+      const int jo = NDIM == 3 ? j - 1 : 0;  // plane corrected this iteration
+      const bool out_plane = NDIM == 3 ? (jo >= z0 && jo < z1) : true;
+      // x/y sweeps: planes outside the chunk feed only b_z of div B
+      const bool edge = NDIM == 3 && D < 2 && (j == z0 - 1 || j == z1);
+
+      // b_z of w1(j-2): its slot takes the predictor of plane j
+      float bzm = 0.0f;
+      if (NDIM == 3 && need_bz && out_plane && has_out)
+        bzm = w1slot(sm, j - 2)[(E + 3) * C::RN + (ly + 1) * C::RX + lx + 1];
+      if (NDIM == 3 && D < 2 && out_plane)
+        in_plane_faces(a, sm, jo, x0, y0, smallp, qmax);
+
       bool ok = true;
       if (NDIM == 3) {
         if (j == pfirst) ok = wait_plane(j - 1) && wait_plane(j);
@@ -566,33 +598,20 @@ struct Fused {
       } else {
         ok = wait_plane(0);
       }
-      if (__syncthreads_or(!ok)) {
+      if (__syncthreads_or(!ok)) {  // barrier A
         if (tid == 0) atomicExch(&ctrl->fault, 1);
         return false;
       }
+      if (NDIM == 3 && tid == 0 && j + 2 <= z1 + 1) issue(j + 2);
       const float* pm = NDIM == 3 ? slot(j - 1) : nullptr;
       const float* p0 = slot(j);
       const float* pp = NDIM == 3 ? slot(j + 1) : nullptr;
-      const int jo = NDIM == 3 ? j - 1 : 0;  // plane corrected this iteration
-      const bool out_plane = NDIM == 3 ? (jo >= z0 && jo < z1) : true;
-      const bool edge = bz_edge_only && (j == z0 - 1 || j == z1);
-
-      // b_z of w1(j-2): its slot is overwritten by the predictor of plane j
-      float bzm = 0.0f;
-      if (NDIM == 3 && need_bz && out_plane && has_out)
-        bzm = w1slot(sm, j - 2)[(E + 3) * C::RN + (ly + 1) * C::RX + lx + 1];
-      // in-plane faces of plane jo while its slopes are still in the slope
-      // buffer (3-D, D < 2)
-      if (NDIM == 3 && D < 2 && out_plane)
-        in_plane_faces(a, sm, jo, x0, y0, smallp, key);
-      __syncthreads();
 
       // predictor of plane j
       float Lcur[NW];
 #pragma unroll
       for (int v = 0; v < NW; v++) Lcur[v] = 0.0f;
       if (edge) {
-        // only b_z at the output cells feeds the corrector (div B)
         if (need_bz && has_out && oix <= g.nx[0] && oiy <= g.nx[1]) {
           const int gc[3] = {oix + 2, oiy + g.gh[1], j + g.gh[2]};
           w1slot(sm, j)[(E + 3) * C::RN + (ly + 1) * C::RX + lx + 1] =
@@ -619,32 +638,37 @@ struct Fused {
             for (int v = 0; v < NW; v++) lb[v * 256 + tid] = Lcur[v];
           }
         }
-        if (MHD && tid < C::NB) {
-          // transverse B of the halo cells that only div B reads
-          const int h = tid;
+        if (need_bz && tid < C::NB + (D == 1 ? 0 : 64 - 2 * C::TX)) {
+          // transverse B of the halo cells that only div B reads: b_y on
+          // the rows above and below (one warp each), b_x on the columns
+          // left and right
           int rx, ry, k;
-          if (D == 0 || (D == 2 && h < 2 * C::TX)) {
-            rx = h % C::TX + 1;
-            ry = h < C::TX ? 0 : C::RY - 1;
+          bool on = true;
+          if (D != 1 && tid < 64) {
+            rx = tid % 32 + 1;
+            ry = tid < 32 ? 0 : C::RY - 1;
             k = 1;
+            on = rx <= C::TX;
           } else {
-            const int hh = D == 2 ? h - 2 * C::TX : h;
+            const int hh = D == 1 ? tid : tid - 64;
             rx = hh < C::TY ? 0 : C::RX - 1;
             ry = hh % C::TY + 1;
             k = 0;
           }
           const int bix = x0 + rx - 1, biy = y0 + ry - 1;
-          if (need_bz && (NDIM >= 2 || k == 0) && bix <= g.nx[0] &&
-              (NDIM < 2 || biy <= g.nx[1])) {
+          if (on && bix <= g.nx[0] && (NDIM < 2 || biy <= g.nx[1])) {
             const int gc[3] = {bix + 2, biy + g.gh[1], j + g.gh[2]};
             w1slot(sm, j)[(E + 1 + k) * C::RN + ry * C::RX + rx] =
                 predict_b(a, pm, p0, pp, ry + 1, rx + 3 + sh, gc, qdt2, qs1, k);
           }
         }
       }
-      __syncthreads();
-      fix_w1_ghosts(a, sm, j, x0, y0);
-      __syncthreads();
+      __syncthreads();  // barrier B
+      const bool fz = fix_zb && (j == 0 || j == g.nx[2]);
+      if (fix_xy || fz) {
+        fix_w1_ghosts(a, sm, j, x0, y0, fix_xy, fz);
+        __syncthreads();
+      }
 
       if (D == 2) {
         // the z face between planes j-1 and j of this column
@@ -662,11 +686,10 @@ struct Fused {
             wr[v] = a2[v * C::RN + r];
           }
           const float cm = face(a, wl, wr, Lprev, Lcur, smallp, Fnew);
-          if (a.ph.courantpar > 0.0 && out_ok) {
+          if (a.cfl && out_ok) {
             const int gz = j + 1;  // ghost-range index of plane j-1
             const float q = cm * 2.0f / (a.dxf[2][gz] + a.dxf[2][gz + 1]);
-            const unsigned long long k = dkey((double)q);
-            key = k > key ? k : key;
+            qmax = (q > qmax || q != q) ? q : qmax;
           }
         }
         if (out_plane && out_ok)
@@ -678,11 +701,11 @@ struct Fused {
         }
       } else {
         if (NDIM == 2) {
-          in_plane_faces(a, sm, 0, x0, y0, smallp, key);
+          in_plane_faces(a, sm, 0, x0, y0, smallp, qmax);
           __syncthreads();
         }
         if (out_plane && out_ok) {
-          const float* fb = fbuf(sm);
+          const float* fb = fbuf(sm, jo);
           float Fm[NW], Fp[NW];
           const int fm = D == 0 ? ly * (C::TX + 1) + lx : ly * C::TX + lx;
           const int fp = D == 0 ? fm + 1 : fm + C::TX;
@@ -695,26 +718,26 @@ struct Fused {
                  Fm, Fp, bzm);
         }
       }
-      __syncthreads();  // ring slots and buffers reusable
     }
     {  // phase bookkeeping: planes pbase .. (NDIM==3 ? z1+1 : 0) were loaded
       const int np = NDIM == 3 ? z1 + 2 - pbase : 1;
 #pragma unroll
       for (int s2 = 0; s2 < FWRING; s2++) uses[s2] += (np - s2 + FWRING - 1) / FWRING;
     }
-    if (a.ph.courantpar > 0.0) {
+    if (a.cfl) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long v = __shfl_xor_sync(0xffffffffu, key, o);
-        key = v > key ? v : key;
+        const float v = __shfl_xor_sync(0xffffffffu, qmax, o);
+        qmax = (v > qmax || v != v) ? v : qmax;
       }
-      if ((tid & 31) == 0) shkey[tid >> 5] = key;
+      if ((tid & 31) == 0) shq[tid >> 5] = qmax;
       __syncthreads();
       if (tid == 0) {
-        for (int i = 1; i < FT_NT / 32; i++) key = shkey[i] > key ? shkey[i] : key;
-        if (key) atomicMax(&ctrl->face_cmax[D][slotid % NSLOT], key);
+        for (int i = 1; i < FT_NT / 32; i++)
+          qmax = (shq[i] > qmax || shq[i] != shq[i]) ? shq[i] : qmax;
+        const unsigned long long key = dkey((double)qmax);
+        if (qmax != 0.0f) atomicMax(&ctrl->face_cmax[D][slotid % NSLOT], key);
       }
-      __syncthreads();
     }
     return true;
   }

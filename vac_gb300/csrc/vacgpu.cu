@@ -599,6 +599,8 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.gamma = p->eqpar[0];
   ph.pt1 = 1.0 - 0.5 * p->eqpar[0];
   ph.gm1 = p->eqpar[0] - 1.0;
+  ph.gammaf = (float)ph.gamma;
+  ph.gm1f = (float)ph.gm1;
   ph.pt3 = 0.5 * (p->eqpar[0] - 1.0);
   ph.smallpcoeff = p->smallpcoeff;
   double courantpar = p->courantpar;

@@ -44,6 +44,7 @@ __host__ __device__ inline long long gidx(const DevGrid& g, int gx, int gy,
 
 struct DevPhys {
   double gamma, pt1, gm1, pt3;
+  float gammaf, gm1f;  // the same, rounded once for the FP32 physics
   double smallpcoeff;
   double courantpar;  // <=0: no CFL evaluation (dtpar set)
   int lim[VACGPU_MAXNW];
