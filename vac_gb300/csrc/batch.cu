@@ -3,8 +3,8 @@
 // Every grid keeps its own state, dt, it and t (its own CFL condition, as
 // separate VAC runs would).  One step of the whole batch is a fixed sequence
 // of batched launches -- dt choice for all grids, one persistent sweep
-// kernel per direction over the (grid, tile) work list of all grids, one
-// ghost fill over all grids, the step epilogue for all grids -- and a call
+// kernel per direction over the (grid, tile) work list of all grids (it also
+// fills the ghost cells), the step epilogue for all grids -- and a call
 // of vacgpu_batch_step captures its steps into one CUDA graph that is
 // launched once.  The state buffer parity of each grid lives on the device
 // (Ctrl::cur), so a grid that finishes early simply stops swapping.
@@ -54,10 +54,8 @@ struct BItem {
 
 struct BInst {
   FusedArgs fa;        // wout chosen per sweep from buf[] and Ctrl::cur
-  SweepArgs sa;        // ghost fill and first-step passes
+  SweepArgs sa;        // first-step passes
   float* buf[2];
-  long long ghost0;    // offset in the batched ghost index space
-  long long pad;
 };
 
 typedef PHMixed<PREC_FF> PHB;
@@ -97,27 +95,6 @@ __global__ void __launch_bounds__(FT_NT, 2)
   }
 }
 
-template <int NW>
-__global__ void kb_ghost(const BInst* __restrict__ insts, int n,
-                         long long total, int sweep) {
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-       t < total; t += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) / 2;
-      if (insts[mid].ghost0 <= t)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const BInst* in = insts + lo;
-    const Ctrl* c = in->sa.ctrl;
-    if (c->done) continue;
-    const int dst = c->cur ^ (sweep & 1) ^ 1;
-    ghost_cell<float, NW>(in->buf[dst], in->sa.g, in->sa.ph, t - in->ghost0);
-  }
-}
-
 template <int NDIM, bool MHD>
 __global__ void __launch_bounds__(128) kb_pminmax(const BInst* insts) {
   const BInst* in = insts + blockIdx.y;
@@ -143,7 +120,6 @@ struct vacgpu_batch {
   // interleaved over grids, 1 grid-major
   BItem* d_items[3][2];
   int nitems[3];
-  long long ghost_total;
   cudaStream_t st;
   int nw;
   bool ready;
@@ -242,16 +218,9 @@ void issue_step(vacgpu_batch* b, int parity, int ctas, int order) {
 #undef PASS
   launchb_control(2, b->d_ctrls, n, p, 0, 0, 0.0, b->st);
   const int nsw = p.ndim;
-  const unsigned gb = 152 * 4;
   for (int s = 0; s < nsw; s++) {
     const int D = (!parity || p.typedimsplit == VACGPU_SPLIT_XY) ? s : nsw - 1 - s;
-    launch_sweep_any(b, D, s, ctas, order);
-    switch (b->nw) {
-      case 4: kb_ghost<4><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
-      case 5: kb_ghost<5><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
-      case 6: kb_ghost<6><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
-      case 8: kb_ghost<8><<<gb, 256, 0, b->st>>>(b->d_insts, n, b->ghost_total, s); break;
-    }
+    launch_sweep_any(b, D, s, ctas, order);  // also fills the ghost cells
   }
   launchb_control(3, b->d_ctrls, n, p, nsw & 1, 0, 0.0, b->st);
 }
@@ -262,7 +231,6 @@ int prepare(vacgpu_batch* b) {
   std::vector<BInst> ins(n);
   std::vector<CUtensorMap> maps(4 * n);
   std::vector<Ctrl*> ctrls(n);
-  long long g0 = 0;
   for (int i = 0; i < n; i++) {
     HandleView v;
     if (vacgpu_internal_view(b->h[i], &v)) return 1;
@@ -291,13 +259,10 @@ int prepare(vacgpu_batch* b) {
     bi.sa = v.sa;
     bi.buf[0] = v.buf[0];
     bi.buf[1] = v.buf[1];
-    bi.ghost0 = g0;
-    g0 += ghost_count(v.g);
     for (int k = 0; k < 4; k++)
       memcpy(&maps[4 * i + k], v.tmap[k / 2][k % 2], sizeof(CUtensorMap));
     ctrls[i] = v.ctrl;
   }
-  b->ghost_total = g0;
   BCK(cudaMalloc(&b->d_insts, sizeof(BInst) * n));
   BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 4 * n));
   BCK(cudaMalloc(&b->d_ctrls, sizeof(Ctrl*) * n));

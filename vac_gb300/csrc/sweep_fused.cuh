@@ -491,6 +491,99 @@ struct Fused {
     const long long off = gidx(g, gc[0], gc[1], gc[2]);
 #pragma unroll
     for (int v = 0; v < NW; v++) a.wout[off + v * g.vs] = acc[v];
+    if (near_bnd(g, gc)) ghost_images(a, gc, acc);
+  }
+
+  // Within two cells of a mesh face: the cell is the source of ghost cells.
+  static __device__ __forceinline__ bool near_bnd(const DevGrid& g,
+                                                  const int* gc) {
+    bool b = false;
+#pragma unroll
+    for (int d = 0; d < NDIM; d++) b = b || gc[d] < 4 || gc[d] >= g.nx[d];
+    return b;
+  }
+
+  // Ghost-cell preimages of the mesh index gi along one dimension (n cells,
+  // ghost-range indices 0..n+3, n >= 4): up to two ghost positions p1, p2
+  // whose boundary map lands on gi, and the 'asymm' sign mask of each.
+  // periodic: gi-n for gi >= n, gi+n for gi < 4; cont: 0 and 1 for gi = 2,
+  // n+2 and n+3 for gi = n+1; symm/asymm: 3-gi for gi < 4, 2n+3-gi for
+  // gi >= n (negated for 'asymm' variables).
+  static __device__ __forceinline__ int preimages(const FusedArgs& a, int d,
+                                                  int gi, int& p1, int& f1,
+                                                  int& p2) {
+    const int n = a.g.nx[d];
+    const int mlo = a.ph.gmap[d][0], mhi = a.ph.gmap[d][1];
+    p1 = p2 = gi;
+    f1 = 0;
+    if (gi < 4) {
+      if (mlo == GMAP_CONT && gi == 2) {
+        p1 = 0;
+        p2 = 1;
+        return 2;
+      }
+      if (mlo == GMAP_MIRROR) {
+        p1 = 3 - gi;
+        f1 = a.ph.asym[d][0];
+        return 1;
+      }
+      if (mhi == GMAP_PERIODIC) {
+        p1 = gi + n;
+        return 1;
+      }
+    }
+    if (gi >= n) {
+      if (mhi == GMAP_CONT && gi == n + 1) {
+        p1 = n + 2;
+        p2 = n + 3;
+        return 2;
+      }
+      if (mhi == GMAP_MIRROR) {
+        p1 = 2 * n + 3 - gi;
+        f1 = a.ph.asym[d][1];
+        return 1;
+      }
+      if (mlo == GMAP_PERIODIC) {
+        p1 = gi - n;
+        return 1;
+      }
+    }
+    return 0;
+  }
+
+  // getboundary of the new state, done by its sources: every ghost cell
+  // (gx, gy, gz) holds sign * w(map_x(gx), map_y(gy), map_z(gz)) (the
+  // region-by-region copies of src/vacgrid.t:195-413 composed), so the cell
+  // gc writes its value to each position whose coordinates are gc's own or
+  // preimages in every dimension, at least one of them a preimage.
+  static __device__ __forceinline__ void ghost_images(const FusedArgs& a,
+                                                      const int* gc,
+                                                      const float (&acc)[NW]) {
+    const DevGrid& g = a.g;
+    int x1, x2, fx, y1 = 0, y2 = 0, fy = 0, z1 = 0, z2 = 0, fz = 0;
+    const int nx_ = 1 + preimages(a, 0, gc[0], x1, fx, x2);
+    const int ny_ = NDIM > 1 ? 1 + preimages(a, 1, gc[1], y1, fy, y2) : 1;
+    const int nz_ = NDIM > 2 ? 1 + preimages(a, 2, gc[2], z1, fz, z2) : 1;
+#pragma unroll 1
+    for (int k = 0; k < nz_; k++) {
+      const int pz = k == 0 ? gc[2] : (k == 1 ? z1 : z2);
+      const int sz = k == 1 ? fz : 0;
+#pragma unroll 1
+      for (int jj = 0; jj < ny_; jj++) {
+        const int py = jj == 0 ? gc[1] : (jj == 1 ? y1 : y2);
+        const int sy = jj == 1 ? fy : 0;
+#pragma unroll 1
+        for (int i = 0; i < nx_; i++) {
+          if ((i | jj | k) == 0) continue;
+          const int px = i == 0 ? gc[0] : (i == 1 ? x1 : x2);
+          const int fl = (i == 1 ? fx : 0) ^ sy ^ sz;
+          const long long o = gidx(g, px, py, pz);
+#pragma unroll
+          for (int v = 0; v < NW; v++)
+            a.wout[o + v * g.vs] = ((fl >> v) & 1) ? -acc[v] : acc[v];
+        }
+      }
+    }
   }
 
   // One tile (bx, by) and z chunk bz of one grid.  bars: the CTA's FWRING

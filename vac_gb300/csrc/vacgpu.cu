@@ -314,11 +314,9 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
     kbegin(h, VACGPU_K_SWEEP);
+    // the fused sweep also writes the ghost cells of its output
     launch_sweep_fused(a, &h->tmap[h->cur][d0 == 1], (float*)wout, h->idxf, h->nzc,
                        h->st);
-    kend(h);
-    kbegin(h, VACGPU_K_GHOST);
-    launch_ghost_mixed(a, (float*)wout, h->st);
     kend(h);
   } else {
     const float* fw = (const float*)w;
@@ -646,8 +644,11 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
              p->typelimited == VACGPU_LIMITED_ORIGINAL &&
              p->typefull == VACGPU_TVDLF;
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
-  for (int d = 0; d < p->ndim; d++)  // the fused epilogue needs uniform maps
-    if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED) h->fused = false;
+  // its ghost writes need uniform maps, periodic faces in pairs and n >= 4
+  for (int d = 0; d < p->ndim; d++)
+    if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED || g.nx[d] < 4 ||
+        (ph.gmap[d][0] == GMAP_PERIODIC) != (ph.gmap[d][1] == GMAP_PERIODIC))
+      h->fused = false;
   if (h->fused) {
     bool ok = true;
     for (int i = 0; i < 2 && ok; i++)
