@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(FT_NT, 2)
       mapidx = item.inst * 4 + src * 2 + (D == 1);
     }
     __syncthreads();
-    bool ok = Fused<NDIM, D, MHD, PREC_FF, LIMC>::run(
+    bool ok = Fused<NDIM, D, MHD, PREC_FF, LIMC, PREC_FF>::run(
         &maps[mapidx], fa, dsm, item.bx, item.by, item.bz, bars, uses,
         (unsigned)it);
     __syncthreads();

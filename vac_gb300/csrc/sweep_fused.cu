@@ -1,22 +1,44 @@
 // sweep_fused.cu - instances and launcher of the fused mixed-precision sweep.
+#include <cstdlib>
+#include <cstring>
+
 #include "sweep_fused.cuh"
 
 namespace vacgpu {
 
 int fused_smem_bytes(int nw, int d) { return fused_smem_floats(nw, d) * 4; }
 
-template <int NDIM, int D, bool MHD, int LIMC>
-static void launch_lim(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
+template <int NDIM, int D, bool MHD, int LIMC, int PMF>
+static void launch_pmf(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
                        cudaStream_t st) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
   const int smem = fused_smem_floats(NW, D) * 4;
-  auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF, LIMC>;
+  auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF, LIMC, PMF>;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
   k<<<grid, FT_NT, smem, st>>>(*map, a);
+}
+
+// VACGPU_FLUX_PRESSURE=f32: FP32 pressure recovery in the fluxes (the wave
+// speeds keep the double-float recovery).  Read once per process.
+static bool flux_pressure_f32() {
+  static const bool f = [] {
+    const char* e = getenv("VACGPU_FLUX_PRESSURE");
+    return e && !strcmp(e, "f32");
+  }();
+  return f;
+}
+
+template <int NDIM, int D, bool MHD, int LIMC>
+static void launch_lim(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
+                       cudaStream_t st) {
+  if (flux_pressure_f32())
+    launch_pmf<NDIM, D, MHD, LIMC, PREC_F32>(map, a, grid, st);
+  else
+    launch_pmf<NDIM, D, MHD, LIMC, PREC_FF>(map, a, grid, st);
 }
 
 template <int NDIM, int D, bool MHD>

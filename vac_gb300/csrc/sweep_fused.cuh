@@ -160,14 +160,20 @@ __device__ __forceinline__ void init_bars(unsigned long long* bars) {
 // (LIMC_RUNTIME: per variable from DevPhys).
 enum { LIMC_RUNTIME = 0, LIMC_MINMOD = 1, LIMC_WOODWARD = 2 };
 
-template <int NDIM, int D, bool MHD, int PM, int LIMC>
+// PM: pressure recovery of the wave speeds; PMF: of the fluxes.
+template <int NDIM, int D, bool MHD, int PM, int LIMC, int PMF = PM>
 struct Fused {
   typedef TileCfg<D> C;
   static constexpr int NDIR = NDIM;
   static constexpr int NW = MHD ? 2 + 2 * NDIR : 2 + NDIR;
   static constexpr int E = NDIR + 1;
   static constexpr int SLOT = fused_slot_floats(NW, D);
+  // Pressure recovery: PM in the wave speeds, PMF in the four flux
+  // evaluations per cell (the same double-float recovery by default; FP32
+  // in the fluxes is the opt-in variant -- p enters a flux only through
+  // p + B^2/2 and v(e + p), whose FP32 error is set by the energy scale).
   typedef PHMixed<PM> PH;
+  typedef PHMixed<PMF> PHF;
 
   // shared memory: state ring | w1 slot 0 | w1 slot 1 | faces 0 | faces 1
   // | slopes (predictor plane p in w1 slot p & 1; the faces of plane p in
@@ -277,8 +283,8 @@ struct Fused {
       uL[v] = u[v] + 0.5f * l;
     }
     float fL[NW], fR[NW];
-    PH::template flux<NDIR, MHD>(uR, D, a.ph, smallp, fR);
-    PH::template flux<NDIR, MHD>(uL, D, a.ph, smallp, fL);
+    PHF::template flux<NDIR, MHD>(uR, D, a.ph, smallp, fR);
+    PHF::template flux<NDIR, MHD>(uL, D, a.ph, smallp, fL);
     const float cq = qdt * a.idxf[D][gc[D]];
 #pragma unroll
     for (int v = 0; v < NW; v++) out[v] = u[v] - cq * (fL[v] - fR[v]);
@@ -345,8 +351,8 @@ struct Fused {
 #pragma unroll
     for (int v = 0; v < NW; v++) L[v] = 2.0f * M[v] - R[v];
     float fL[NW], fR[NW];
-    PH::template flux<NDIR, MHD>(L, D, a.ph, smallp, fL);
-    PH::template flux<NDIR, MHD>(R, D, a.ph, smallp, fR);
+    PHF::template flux<NDIR, MHD>(L, D, a.ph, smallp, fL);
+    PHF::template flux<NDIR, MHD>(R, D, a.ph, smallp, fR);
 #pragma unroll
     for (int v = 0; v < NW; v++)
       F[v] = 0.5f * (fL[v] + fR[v]) - cmax * 0.5f * (R[v] - L[v]);
@@ -836,7 +842,7 @@ struct Fused {
   }
 };
 
-template <int NDIM, int D, bool MHD, int PM, int LIMC>
+template <int NDIM, int D, bool MHD, int PM, int LIMC, int PMF>
 __global__ void __launch_bounds__(FT_NT, 2)
     k_sweep_fused(const __grid_constant__ CUtensorMap map, FusedArgs a) {
   extern __shared__ __align__(128) float dsm[];
@@ -844,8 +850,8 @@ __global__ void __launch_bounds__(FT_NT, 2)
   init_bars(bars);
   int uses[FWRING] = {0, 0, 0, 0};
   const unsigned slotid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  Fused<NDIM, D, MHD, PM, LIMC>::run(&map, a, dsm, blockIdx.x, blockIdx.y,
-                                     blockIdx.z, bars, uses, slotid);
+  Fused<NDIM, D, MHD, PM, LIMC, PMF>::run(&map, a, dsm, blockIdx.x, blockIdx.y,
+                                          blockIdx.z, bars, uses, slotid);
 }
 
 }  // namespace vacgpu
