@@ -7,10 +7,11 @@
 // its result must be accurate relative to p, not to e.  Three evaluations
 // are provided:
 //   PREC_FF   double-float arithmetic: each square is split exactly with the
-//             FMA-based TwoProduct, sums use Knuth's TwoSum and m^2/rho is a
-//             FP32 quotient plus an FMA-computed remainder correction
-//             (Dekker 1971; Ogita, Rump & Oishi 2005).  ~48-bit accurate,
-//             runs entirely on the FP32 pipes.
+//             FMA-based TwoProduct, the (non-negative) sums use Dekker's
+//             Fast2Sum on the ordered pair, m^2/rho is a FP32 quotient plus
+//             an FMA-computed remainder correction (Dekker 1971; Ogita, Rump
+//             & Oishi 2005), and e - S/2 is one FMA, exact where it cancels.
+//             Accurate to a few ulps of p itself; runs on the FP32 pipes.
 //   PREC_F64  the same expression in native IEEE double on the FP64 pipe.
 //   PREC_F32  plain FP32 (reference for the error study only).
 // Total pressure uses ptot = p + B^2/2, which equals the reference's
@@ -24,16 +25,18 @@ namespace vacgpu {
 
 enum { PREC_F32 = 0, PREC_FF = 1, PREC_F64 = 2 };
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s,
-                                        float& e) {
-  s = a + b;
-  float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
 __device__ __forceinline__ void two_prod(float a, float b, float& p,
                                          float& e) {
   p = a * b;
   e = fmaf(a, b, -p);
+}
+// s + e = a + b exactly for a, b >= 0 (Dekker's Fast2Sum on the ordered
+// pair: the larger operand first).
+__device__ __forceinline__ void two_sum_pos(float a, float b, float& s,
+                                            float& e) {
+  const float hi = fmaxf(a, b), lo = fminf(a, b);
+  s = hi + lo;
+  e = lo - (s - hi);
 }
 
 // Thermal pressure (unclipped) and the magnetic energy density B^2/2 of a
@@ -56,13 +59,14 @@ __device__ __forceinline__ float pressure_mixed(const float* u, float rinv,
     *half_bb = (float)(0.5 * bb);
     return (float)((double)gm1 * ((double)u[E] - 0.5 * (q + bb)));
   } else if (PM == PREC_FF) {
+    // sums of squares as unevaluated pairs (hi + lo), all terms >= 0
     float mh, ml;
     two_prod(u[1], u[1], mh, ml);
 #pragma unroll
     for (int c = 2; c <= NDIR; c++) {
       float ph, pl, t;
       two_prod(u[c], u[c], ph, pl);
-      two_sum(mh, ph, mh, t);
+      two_sum_pos(mh, ph, mh, t);
       ml = ml + (pl + t);
     }
     // q = mm/rho: FP32 quotient, exact FMA remainder, corrected low part
@@ -77,20 +81,22 @@ __device__ __forceinline__ float pressure_mixed(const float* u, float rinv,
       for (int c = 2; c <= NB; c++) {
         float ph, pl, t;
         two_prod(u[E + c], u[E + c], ph, pl);
-        two_sum(bh, ph, bh, t);
+        two_sum_pos(bh, ph, bh, t);
         bl = bl + (pl + t);
       }
       *half_bb = 0.5f * (bh + bl);
       float t;
-      two_sum(qh, bh, sh, t);
+      two_sum_pos(qh, bh, sh, t);
       sl = ql + bl + t;
     } else {
       *half_bb = 0.0f;
     }
-    float dh, dl;
-    two_sum(u[E], -0.5f * sh, dh, dl);
-    dl = dl - 0.5f * sl;
-    return gm1 * (dh + dl);
+    // e - (sh + sl)/2: the FMA is exact where the subtraction cancels
+    // (e and sh/2 within a factor 2, Sterbenz) and rounds to the nearest
+    // float of a result no smaller than sh/2 otherwise
+    float d = fmaf(-0.5f, sh, u[E]);
+    d = fmaf(-0.5f, sl, d);
+    return gm1 * d;
   } else {
     float mm = u[1] * u[1], bb = 0.0f;
 #pragma unroll
