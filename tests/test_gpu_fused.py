@@ -87,3 +87,18 @@ def test_fused_against_oracle_and_split(gpu_lib, monkeypatch, name, mk, lim, bc,
     assert es.kernel_stats()["sweep"][0] == 0
     assert max(rel_l1(wf, ref)) <= MIXED_REL_L1, rel_l1(wf, ref)
     assert max(rel_l1(wf, ws)) <= FUSED_VS_SPLIT, rel_l1(wf, ws)
+
+
+def test_z_chunk_tuning_is_invisible(monkeypatch):
+    """At 128^3 the first step call tunes the fused sweep's z chunk from a
+    snapshot of the state; the run must be bit-identical to one with the
+    chunk pinned (VACGPU_NZC), in state, t and it."""
+    s = inistate.random_modes(128, seed=5)
+    p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
+    tuned = Engine(p, s.x, s.w)
+    tuned.step(4)
+    monkeypatch.setenv("VACGPU_NZC", "32")
+    pinned = Engine(p, s.x, s.w)
+    pinned.step(4)
+    assert (tuned.it, tuned.t) == (pinned.it, pinned.t)
+    assert np.array_equal(tuned.state().view(np.uint64), pinned.state().view(np.uint64))

@@ -178,6 +178,12 @@ struct vacgpu_handle {
   CUtensorMap tmap[2][2];  // [state buffer][box: x/z sweeps, y sweep]
   float* idxf[3];
   int nzc;
+  // z-chunk tuning of the fused 3-D sweep (results do not depend on the
+  // chunk): pending until the first vacgpu_step call, which times one step
+  // per candidate from a snapshot of the state and keeps the fastest
+  bool tuning;
+  int tncand;
+  int tcand[6];
 };
 
 namespace {
@@ -398,6 +404,51 @@ void run_step(vacgpu_handle* h, int parity_odd) {
 // Issue k steps on the handle's stream without waiting: two-step units
 // are replayed from captured CUDA graphs keyed by (state buffer, parity of
 // it); h->cur follows the swaps of steps that execute.
+// z-chunk tuning of the fused 3-D sweep: one step per candidate from a
+// snapshot of the state (kept in the predictor buffer, which the fused
+// sweep does not use) and of the control block, restored after each trial,
+// so the run itself is untouched; the fastest candidate is kept.
+int tune_nzc(vacgpu_handle* h) {
+  h->tuning = false;
+  const size_t bytes = (size_t)h->g.vs * h->nw * h->elem;
+  const int cur0 = h->cur;
+  long long nl[VACGPU_K_NCLASS];
+  memcpy(nl, h->nlaunch, sizeof(nl));
+  Ctrl saved;
+  CK(cudaMemcpyAsync(&saved, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->buf[2], h->buf[cur0], bytes, cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int nbest = h->nzc;
+  for (int i = 0; i < h->tncand; i++) {
+    h->nzc = h->tcand[i];
+    k_call_begin<<<1, 1, 0, h->st>>>(h->ctrl, 1, 1e300);
+    cudaEventRecord(e0, h->st);
+    run_step<float>(h, h->it_host & 1);
+    cudaEventRecord(e1, h->st);
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      nbest = h->tcand[i];
+    }
+    CK(cudaMemcpyAsync(h->buf[cur0], h->buf[2], bytes, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->cur = cur0;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  memcpy(h->nlaunch, nl, sizeof(nl));
+  h->nzc = nbest;
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int issue_steps(vacgpu_handle* h, int k, int it_base) {
   const int nsw = h->p.dimsplit ? h->p.ndim : 1;
   const bool graphs = !h->timing && h->st != nullptr &&
@@ -513,6 +564,7 @@ int vacgpu_internal_set_cur(vacgpu_handle* h, int cur) {
 // Server support: issue k steps that all execute (no stop condition in
 // between) without any host synchronisation.
 int vacgpu_internal_step_async(vacgpu_handle* h, int k) {
+  h->tuning = false;  // served solves keep the default z chunk
   k_call_begin<<<1, 1, 0, h->st>>>(h->ctrl, k, 1e300);
   if (issue_steps(h, k, h->it_host)) return 1;
   h->it_host += k;
@@ -649,6 +701,12 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED || g.nx[d] < 4 ||
         (ph.gmap[d][0] == GMAP_PERIODIC) != (ph.gmap[d][1] == GMAP_PERIODIC))
       h->fused = false;
+  if (h->fused && p->ndim == 3 && !getenv("VACGPU_NZC") && g.ncell >= (1LL << 21)) {
+    static const int cands[5] = {16, 24, 32, 48, 64};
+    for (int i = 0; i < 5; i++)
+      if (cands[i] < g.nx[2]) h->tcand[h->tncand++] = cands[i];
+    h->tuning = h->tncand > 1;
+  }
   if (h->fused) {
     bool ok = true;
     for (int i = 0; i < 2 && ok; i++)
@@ -815,6 +873,7 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   if (!h->have_grid || !h->have_state)
     return fail("vacgpu_step before vacgpu_set_grid/vacgpu_upload");
   if (maxsteps < 0) return fail("maxsteps must be >= 0");
+  if (h->tuning && maxsteps > 0 && !h->timing && tune_nzc(h)) return 1;
   const int nsw = h->p.dimsplit ? h->p.ndim : 1;
   const int start_cur = h->cur;
   kbegin(h, VACGPU_K_CONTROL);
