@@ -116,6 +116,12 @@ typedef struct vacgpu_params {
   double dtmin;
   int typeB[VACGPU_MAXB][VACGPU_MAXNW]; /* [iB][iw]; iB = 2*(idim-1)+upper */
   int precision;                /* VACGPU_PREC_*                            */
+  /* positivity repair in getboundary (keeppositive, src/vacphys.t.mhd:9-53,
+   * src/vacphys.t.hd:176-219, src/vacproc.positive.t:2-34)               */
+  int smallfix;                 /* 1 = keeppositive before each ghost fill  */
+  double smallrho;              /* -1: min(rho)*smallrhocoeff at 1st use    */
+  double smallrhocoeff;
+  double vacuumrho;             /* >=0: rho<smallrho becomes vacuum         */
 } vacgpu_params;
 
 typedef struct vacgpu_handle vacgpu_handle;

@@ -48,6 +48,8 @@ def lib():
         L.vo_dt.argtypes = [vp]
         L.vo_smallp.restype = C.c_double
         L.vo_smallp.argtypes = [vp]
+        L.vo_smallrho.restype = C.c_double
+        L.vo_smallrho.argtypes = [vp]
         L.vo_volume.restype = C.c_double
         L.vo_volume.argtypes = [vp]
         L.vo_nerror.argtypes = [vp, C.POINTER(C.c_int)]
@@ -135,6 +137,10 @@ class Oracle:
     @property
     def smallp(self):
         return lib().vo_smallp(self.h)
+
+    @property
+    def smallrho(self):
+        return lib().vo_smallrho(self.h)
 
     @property
     def volume(self):

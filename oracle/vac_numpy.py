@@ -51,6 +51,7 @@ class NumpyVac:
         self.ixM = Box([2 if d < self.ndim else 0 for d in range(3)],
                        [self.nG[d] - 3 if d < self.ndim else 0 for d in range(3)])
         self.smallp = p.smallp
+        self.smallrho = p.smallrho
         self.courantpar = p.courantpar
         self.dtpar = p.dtpar
         if self.dtpar > 0 and p.slowsteps != 1:
@@ -264,7 +265,45 @@ class NumpyVac:
                         mb = mb + wCT[(c,) + sl] * wCT[(self.b0 + c,) + sl]
                     wnew[(iw,) + sl] = wnew[(iw,) + sl] - mb / rho * divb
 
+    def keeppositive(self, w):
+        """smallfix: src/vacphys.t.mhd:9-53, src/vacphys.t.hd:176-219,
+        src/vacproc.positive.t:2-34 (density floor or vacuum state, then e
+        from max(p, smallp) in every mesh cell when any p < max(0, smallp))."""
+        sl = self.ixM.sl()
+        g = self.gamma
+        rho = w[(0,) + sl]
+        if self.p.vacuumrho < ZERO:
+            if self.smallrho == -ONE:
+                self.smallrho = rho.min() * self.p.smallrhocoeff
+            if (rho < max(ZERO, self.smallrho)).any():
+                self.nerror[1] += 1
+                if self.smallrho > ZERO:
+                    w[(0,) + sl] = np.where(rho > self.smallrho, rho, self.smallrho)
+        else:
+            vac = rho < self.smallrho
+            for c in range(1, self.ndir + 1):
+                w[(c,) + sl][vac] = ZERO
+            w[(0,) + sl][vac] = self.p.vacuumrho
+            if self.mhd:
+                e = self.smallp / (g - ONE) + HALF * self.sq_sum(w, self.b0, sl)
+            else:
+                e = np.full(rho.shape, self.smallp / (g - ONE))
+            w[(self.e_,) + sl][vac] = e[vac]
+        p = self.getpthermal(w, self.ixM, clipping=False)
+        if (p < max(ZERO, self.smallp)).any():
+            self.nerror[0] += 1
+            if self.smallp > ZERO:
+                a = np.where(p > self.smallp, p, self.smallp) / (g - 1)
+                mm = self.sq_sum(w, 0, sl)
+                rho = w[(0,) + sl]
+                if self.mhd:
+                    w[(self.e_,) + sl] = a + HALF * (mm / rho + self.sq_sum(w, self.b0, sl))
+                else:
+                    w[(self.e_,) + sl] = a + HALF / rho * mm
+
     def getboundary(self, w):
+        if self.p.smallfix:
+            self.keeppositive(w)
         for iB in range(2 * self.ndim):
             idim, upper = iB // 2, iB % 2
             r = Box(self.ixG.lo, self.ixG.hi)

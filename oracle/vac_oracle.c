@@ -56,6 +56,7 @@ typedef struct vo_state {
   double dt, t, dtold, dtpar, courantpar, dtgrav;
   int it, itmin;
   double smallp;
+  double smallrho;   /* keeppositive_rho: -1 until set from min(rho) */
   int nerror[4];
   int istep, nstep;
   int src_id;
@@ -465,9 +466,89 @@ static void addsource2(vo_state* s, double qdt, box ixO, const double* wCT,
   if (s->mhd && s->p.divbfix) addsource_divb(s, qdt, ixO, wCT, w);
 }
 
+/* keeppositive (smallfix=T), src/vacphys.t.mhd:9-53 and src/vacphys.t.hd:
+ * 176-219, with keeppositive_rho, src/vacproc.positive.t:2-34: on the mesh,
+ * density floor (or vacuum state), then, if any unclipped pressure is below
+ * max(0,smallp), e recomputed from max(p,smallp) in every mesh cell.
+ * nerror(toosmallp_=1), nerror(toosmallr_=2) count calls that found any. */
+static void keeppositive(vo_state* s, double* w) {
+  const box b = s->ixM;
+  const double gamma = s->p.eqpar[0];
+  double* rho = W(w, s->rho_);
+  double* e = W(w, s->e_);
+  if (s->p.vacuumrho < ZERO) {
+    if (s->smallrho == -ONE) {
+      double mn = ZERO;
+      int first = 1;
+      FORBOX_SEQ(b, ix) {
+        if (first || rho[ix] < mn) mn = rho[ix];
+        first = 0;
+      }
+      s->smallrho = mn * s->p.smallrhocoeff;
+    }
+    const double lim = fmax2(ZERO, s->smallrho);
+    int toosmallr = 0;
+    FORBOX_SEQ(b, ix) {
+      if (rho[ix] < lim) toosmallr = 1;
+    }
+    if (toosmallr) {
+      s->nerror[1]++;
+      if (s->smallrho > ZERO) FORBOX(b, ix) { rho[ix] = fmax2(rho[ix], s->smallrho); }
+    }
+  } else {
+    FORBOX(b, ix) {
+      if (rho[ix] < s->smallrho) {
+        for (int c = 1; c <= s->ndir; c++) W(w, s->m0_ + c)[ix] = ZERO;
+        rho[ix] = s->p.vacuumrho;
+        if (s->mhd) {
+          double bb = 0.0;
+          for (int c = 1; c <= s->ndir; c++) {
+            double bc = W(w, s->b0_ + c)[ix];
+            bb = (c == 1) ? bc * bc : bb + bc * bc;
+          }
+          e[ix] = s->smallp / (gamma - ONE) + HALF * bb;
+        } else {
+          e[ix] = s->smallp / (gamma - ONE);
+        }
+      }
+    }
+  }
+  getpthermal(s, 0, w, b, s->tmp);
+  const double plim = fmax2(ZERO, s->smallp);
+  int toosmallp = 0;
+  FORBOX_SEQ(b, ix) {
+    if (s->tmp[ix] < plim) toosmallp = 1;
+  }
+  if (toosmallp) {
+    s->nerror[0]++;
+    if (s->smallp > ZERO) {
+      FORBOX(b, ix) {
+        double mm = 0.0;
+        for (int c = 1; c <= s->ndir; c++) {
+          double mc = W(w, s->m0_ + c)[ix];
+          mm = (c == 1) ? mc * mc : mm + mc * mc;
+        }
+        const double a = fmax2(s->tmp[ix], s->smallp) / (gamma - 1);
+        if (s->mhd) {
+          double bb = 0.0;
+          for (int c = 1; c <= s->ndir; c++) {
+            double bc = W(w, s->b0_ + c)[ix];
+            bb = (c == 1) ? bc * bc : bb + bc * bc;
+          }
+          e[ix] = a + HALF * (mm / rho[ix] + bb);
+        } else {
+          e[ix] = a + HALF / rho[ix] * mm;
+        }
+      }
+    }
+  }
+}
+
 /* getboundary, src/vacgrid.t:195-413 with the default regions of boundsetup
- * (src/vacgrid.t:53-69) and periodic pairing (:121-135). */
+ * (src/vacgrid.t:53-69) and periodic pairing (:121-135); keeppositive first
+ * when smallfix (:213). */
 static void getboundary(vo_state* s, double* w) {
+  if (s->p.smallfix) keeppositive(s, w);
   for (int iB = 0; iB < 2 * s->ndim; iB++) {
     int idim = iB / 2, upper = iB % 2;
     box r = s->ixG;
@@ -761,6 +842,7 @@ vo_state* vo_create(const vacgpu_params* p) {
   for (unsigned i = 0; i < sizeof(t1) / sizeof(t1[0]); i++)
     *t1[i] = calloc(N, sizeof(double));
   s->smallp = p->smallp;
+  s->smallrho = p->smallrho;
   s->courantpar = p->courantpar;
   s->dtpar = p->dtpar;
   s->nstep = p->typefull == VACGPU_TVDLF1 ? 1 : 2;  /* onestep / twostep */
@@ -942,6 +1024,7 @@ double vo_t(vo_state* s) { return s->t; }
 int vo_it(vo_state* s) { return s->it; }
 double vo_dt(vo_state* s) { return s->dt; }
 double vo_smallp(vo_state* s) { return s->smallp; }
+double vo_smallrho(vo_state* s) { return s->smallrho; }
 double vo_volume(vo_state* s) { return s->volume; }
 void vo_nerror(vo_state* s, int* n) { memcpy(n, s->nerror, sizeof(s->nerror)); }
 long vo_ncells_full(vo_state* s) { return s->N; }

@@ -53,6 +53,31 @@ FP64_CASES = [
 ]
 
 
+def _smallfix(**kw):
+    def tweak(p):
+        p.smallfix = 1
+        for k, v in kw.items():
+            setattr(p, k, v)
+    return tweak
+
+
+# keeppositive (smallfix=T): density floor, vacuum state, pressure repair,
+# automatic smallrho/smallp; the error counts must agree too
+SMALLFIX_CASES = [
+    ("hd-smallfix-floor", lambda: inistate.riemann_2d(40, 3), "minmod", "cont", 12,
+     _smallfix(smallp=0.3, smallrho=0.3), None),
+    ("hd-smallfix-vacuum", lambda: inistate.riemann_2d(40, 5), "minmod", "cont", 12,
+     _smallfix(smallp=0.2, smallrho=0.3, vacuumrho=0.05), None),
+    ("ot-smallfix", lambda: inistate.orszag_tang(32), "woodward", "periodic", 10,
+     _smallfix(smallp=1.6), None),
+    ("rm3-smallfix-vacuum", lambda: inistate.random_modes(12, seed=3), "minmod", "periodic", 4,
+     _smallfix(smallp=0.049, smallrho=0.9, vacuumrho=0.1), None),
+    ("hd-smallfix-auto", lambda: inistate.riemann_2d(32, 7), "minmod", "cont", 10,
+     _smallfix(), None),
+]
+FP64_CASES = FP64_CASES + SMALLFIX_CASES
+
+
 def _ragged():
     """Non-square, odd-sized grid: 37 x 23 cells."""
     s = inistate.orszag_tang(8)
@@ -134,3 +159,15 @@ def test_graph_replay_matches_plain_launches(gpu_lib, monkeypatch):
         out.append((e.state(), e.t, e.it))
     assert out[0][1:] == out[1][1:]
     assert np.array_equal(bits(out[0][0]), bits(out[1][0]))
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", SMALLFIX_CASES[:3],
+                         ids=[c[0] for c in SMALLFIX_CASES[:3]])
+def test_mixed_smallfix_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
+    """The split mixed kernels with keeppositive (the fused sweep has no
+    global pass between its substeps, so smallfix selects the split path)."""
+    o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
+    a, b = e.state(), o.state()
+    for iw in range(a.shape[0]):
+        rel = np.abs(a[iw] - b[iw]).sum() / np.abs(b[iw]).sum()
+        assert rel <= MIXED_REL_L1, (iw, rel)

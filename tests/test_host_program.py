@@ -86,3 +86,20 @@ def test_run_writes_vac_outputs(vacgb, tmp_path):
     assert [int(r[0]) for r in rows] == [5, 10, 15, 20]
     np.testing.assert_allclose([float(v) for v in rows[-1][3:]], o.sums(), rtol=1e-5,
                                atol=1e-12)  # momentum means are round-off sized
+
+
+def test_par_parsing_smallfix(vacgb, tmp_path):
+    """keeppositive settings of &methodlist reach the parameter block."""
+    _setup(tmp_path)
+    par = PAR.replace("smallpcoeff=1.D-6", "smallpcoeff=1.D-6\n        smallfix=T\n"
+                      "        smallp=0.25\n        smallrho=0.5D0\n"
+                      "        smallrhocoeff=1.D-4\n        vacuumrho=1.D-3")
+    out = subprocess.run([vacgb, "--dump-params"], cwd=tmp_path, capture_output=True,
+                         text=True, input=par, check=True).stdout
+    d = json.loads(out)
+    assert d["smallfix"] == 1 and d["smallp"] == 0.25 and d["smallrho"] == 0.5
+    assert d["smallrhocoeff"] == 1e-4 and d["vacuumrho"] == 1e-3
+    d0 = json.loads(subprocess.run([vacgb, "--dump-params"], cwd=tmp_path,
+                                   capture_output=True, text=True, input=PAR,
+                                   check=True).stdout)
+    assert (d0["smallfix"], d0["smallrho"], d0["vacuumrho"]) == (0, -1.0, -1.0)

@@ -31,6 +31,32 @@ CASES = [
 ]
 
 
+def smallfix(**kw):
+    """Tweak: smallfix=T with the given smallp/smallrho/vacuumrho."""
+    def tweak(p):
+        p.smallfix = 1
+        for k, v in kw.items():
+            setattr(p, k, v)
+    return tweak
+
+
+# keeppositive branches: density floor and pressure repair (HD, MHD),
+# vacuum state (HD, MHD 3-D), automatic smallp/smallrho
+SMALLFIX_CASES = [
+    ("hd-smallfix-floor", lambda: inistate.riemann_2d(24, 3), "minmod", "cont", 6,
+     smallfix(smallp=0.3, smallrho=0.3)),
+    ("hd-smallfix-vacuum", lambda: inistate.riemann_2d(24, 5), "minmod", "cont", 6,
+     smallfix(smallp=0.2, smallrho=0.3, vacuumrho=0.05)),
+    ("ot-smallfix", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5,
+     smallfix(smallp=1.6)),
+    ("rm3-smallfix-vacuum", lambda: inistate.random_modes(8, seed=3), "minmod", "periodic", 3,
+     smallfix(smallp=0.049, smallrho=0.9, vacuumrho=0.1)),
+    ("hd-smallfix-auto", lambda: inistate.riemann_2d(20, 7), "minmod", "cont", 6,
+     smallfix()),
+]
+CASES = CASES + SMALLFIX_CASES
+
+
 @pytest.mark.parametrize("name,mk,lim,bc,nsteps,tweak", CASES, ids=[c[0] for c in CASES])
 def test_c_oracle_matches_numpy_restatement(name, mk, lim, bc, nsteps, tweak):
     s = mk()
@@ -85,3 +111,21 @@ def test_itmax_and_tstop_semantics():
     assert not fin and o2.t >= 0.3
     o2.step(6 - n)
     assert np.array_equal(bits(o1.state()), bits(o2.state()))
+
+
+def test_smallfix_counts_and_floors():
+    """keeppositive fires: nerror(toosmallp_) and nerror(toosmallr_) count
+    the getboundary calls that found small values; afterwards the mesh
+    holds no density below smallrho and no pressure below smallp."""
+    s = inistate.riemann_2d(24, 3)
+    p = inistate.params_for(s, bc="cont")
+    smallfix(smallp=0.3, smallrho=0.3)(p)
+    o = Oracle(p, s.x, s.w)
+    o.step(3)
+    ne = o.nerror()
+    assert ne[0] >= 1 and ne[1] >= 1
+    w = o.state()
+    assert w[0].min() >= 0.3
+    gm1 = p.eqpar[0] - 1
+    pth = gm1 * (w[3] - 0.5 * (w[1] ** 2 + w[2] ** 2) / w[0])
+    assert pth.min() >= 0.3 * (1 - 1e-12)

@@ -55,6 +55,10 @@ class VacParams(C.Structure):
         ("dtmin", C.c_double),
         ("typeB", (C.c_int * MAXNW) * MAXB),
         ("precision", C.c_int),
+        ("smallfix", C.c_int),
+        ("smallrho", C.c_double),
+        ("smallrhocoeff", C.c_double),
+        ("vacuumrho", C.c_double),
     ]
 
 
@@ -94,6 +98,10 @@ def default_params(ndim, ndir, physics, nx, gamma=5.0 / 3.0):
         for iw in range(MAXNW):
             p.typeB[ib][iw] = BC_CONT
     p.precision = PREC_FP64
+    p.smallfix = 0
+    p.smallrho = -1.0
+    p.smallrhocoeff = 1.0e-6
+    p.vacuumrho = -1.0
     return p
 
 

@@ -208,6 +208,59 @@ void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st) {
 void launch_smallp(Ctrl* c, int mhd, double coeff, cudaStream_t st) {
   k_smallp<<<1, NSLOT, 0, st>>>(c, mhd, coeff);
 }
+
+// keeppositive (src/vacphys.t.mhd:9-53, src/vacproc.positive.t:2-34):
+// the one-time smallrho (min(rho)*smallrhocoeff, when the density floor is
+// in use and smallrho is still -1) and smallp (getpthermal's first call)
+// minima are due when their value is unset.
+__global__ void k_kp_begin(Ctrl* c, int rho_floor) {
+  __shared__ int need_r, need_p;
+  if (threadIdx.x == 0) {
+    need_r = need_p = 0;
+    if (!c->done) {
+      need_r = rho_floor && c->smallrho == -1.0;
+      need_p = c->smallp < 0.0;
+      c->need_smallrho = need_r;
+      c->need_smallp = need_p;
+    }
+  }
+  __syncthreads();
+  const int i = threadIdx.x;
+  if (need_r) c->rmin[i] = ~0ULL;
+  if (need_p) {
+    c->pmin[i] = ~0ULL;
+    c->pmax[i] = 0ULL;
+  }
+}
+__global__ void k_kp_smallrho(Ctrl* c, double coeff) {
+  if (c->done || !c->need_smallrho) return;
+  __shared__ unsigned long long sh[NSLOT];
+  sh[threadIdx.x] = ~c->rmin[threadIdx.x];
+  __syncthreads();
+  for (int o = NSLOT / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o && sh[threadIdx.x + o] > sh[threadIdx.x])
+      sh[threadIdx.x] = sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    c->smallrho = dkey_inv(~sh[0]) * coeff;
+    c->need_smallrho = 0;
+  }
+}
+__global__ void k_kp_end(Ctrl* c) {
+  if (c->done) return;
+  c->nerror[0] += c->kp_p;  // toosmallp_
+  c->nerror[1] += c->kp_r;  // toosmallr_
+  c->kp_p = 0;
+  c->kp_r = 0;
+}
+void launch_kp_begin(Ctrl* c, int rho_floor, cudaStream_t st) {
+  k_kp_begin<<<1, NSLOT, 0, st>>>(c, rho_floor);
+}
+void launch_kp_smallrho(Ctrl* c, double coeff, cudaStream_t st) {
+  k_kp_smallrho<<<1, NSLOT, 0, st>>>(c, coeff);
+}
+void launch_kp_end(Ctrl* c, cudaStream_t st) { k_kp_end<<<1, 1, 0, st>>>(c); }
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st) {
   DtEndArgs a;
   a.ndim = p.ndim;

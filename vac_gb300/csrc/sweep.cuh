@@ -270,6 +270,104 @@ struct Sweep {
     if (threadIdx.x == 0) atomic_min_key(&ctrl->pmin[blockIdx.x % NSLOT], k);
   }
 
+  // keeppositive (smallfix), src/vacphys.t.mhd:9-53, src/vacphys.t.hd:
+  // 176-219, src/vacproc.positive.t:2-34, in the reference's expression
+  // order.  min(rho) for the one-time smallrho:
+  template <int NT>
+  static __device__ void kp_rhomin(const SweepArgs& a, const T* __restrict__ w) {
+    __shared__ unsigned long long shk[NT / 32];
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->done || !ctrl->need_smallrho) return;
+    unsigned long long kmin = ~0ULL;
+    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+         n < a.g.ncell; n += (long long)gridDim.x * blockDim.x) {
+      int c[3];
+      cell_coords(a.g, n, c);
+      const unsigned long long k = dkey((double)w[gidx(a.g, c[0], c[1], c[2])]);
+      kmin = k < kmin ? k : kmin;
+    }
+    const unsigned long long k = ~block_max_key<NT>(~kmin, shk);
+    if (threadIdx.x == 0) atomic_min_key(&ctrl->rmin[blockIdx.x % NSLOT], k);
+  }
+
+  // density floor rho = max(rho, smallrho) (keeppositive_rho), or the
+  // vacuum state where rho < smallrho (vacuumrho >= 0)
+  static __device__ void kp_rho(const SweepArgs& a, T* __restrict__ w) {
+    const Ctrl* ctrl = a.ctrl;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ctrl->done || n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    const double smallrho = ctrl->smallrho;
+    const double rho = (double)w[off];
+    if (a.ph.vacuumrho < 0.0) {
+      if (rho < fmax2(0.0, smallrho)) atomicOr((int*)&a.ctrl->kp_r, 1);
+      if (smallrho > 0.0) w[off] = T(fmax2(rho, smallrho));
+    } else if (rho < smallrho) {
+#pragma unroll
+      for (int k = 1; k <= NDIR; k++) w[off + k * a.g.vs] = T(0.0);
+      w[off] = T(a.ph.vacuumrho);
+      double e = ctrl->smallp / a.ph.gm1;
+      if (MHD) {
+        double b1 = (double)w[off + (L::B0 + 1) * a.g.vs];
+        double bb = b1 * b1;
+#pragma unroll
+        for (int k = 2; k <= NDIR; k++) {
+          const double bk = (double)w[off + (L::B0 + k) * a.g.vs];
+          bb = bb + bk * bk;
+        }
+        e = e + 0.5 * bb;
+      }
+      w[off + L::E * a.g.vs] = T(e);
+    }
+  }
+
+  // any unclipped pressure below max(0, smallp)?
+  static __device__ void kp_pcheck(const SweepArgs& a, const T* __restrict__ w) {
+    const Ctrl* ctrl = a.ctrl;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ctrl->done || n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    R u[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+    const double p = PH::template pthermal_raw<NDIR, MHD>(u, a.ph);
+    if (p < fmax2(0.0, ctrl->smallp)) atomicOr((int*)&a.ctrl->kp_p, 1);
+  }
+
+  // if so (and smallp > 0): e from max(p, smallp) in every mesh cell
+  static __device__ void kp_pfix(const SweepArgs& a, T* __restrict__ w) {
+    const Ctrl* ctrl = a.ctrl;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ctrl->done || !ctrl->kp_p || !(ctrl->smallp > 0.0) || n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    R u[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+    const double smallp = ctrl->smallp;
+    const double p = PH::template pthermal_raw<NDIR, MHD>(u, a.ph);
+    double mm = (double)u[1] * (double)u[1];
+#pragma unroll
+    for (int k = 2; k <= NDIR; k++) mm = mm + (double)u[k] * (double)u[k];
+    const double x = fmax2(p, smallp) / a.ph.gm1;
+    double e;
+    if (MHD) {
+      double bb = (double)u[L::B0 + 1] * (double)u[L::B0 + 1];
+#pragma unroll
+      for (int k = 2; k <= NDIR; k++)
+        bb = bb + (double)u[L::B0 + k] * (double)u[L::B0 + k];
+      e = x + 0.5 * (mm / (double)u[0] + bb);
+    } else {
+      e = x + 0.5 / (double)u[0] * mm;
+    }
+    w[off + L::E * a.g.vs] = T(e);
+  }
+
   // Cell-centred max(cmax/dx) of getdt_courant for the dimensions whose
   // dtcourant is unset (src/vac.t:690-711).
   template <int NT>
@@ -438,6 +536,27 @@ __global__ void __launch_bounds__(128)
   Sweep<PH, NDIM, NDIR, MHD>::template cell_cmax<128>(a, w);
 }
 
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_kp_rhomin(SweepArgs a, const typename PH::T* __restrict__ w) {
+  Sweep<PH, NDIM, NDIR, MHD>::template kp_rhomin<128>(a, w);
+}
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_kp_rho(SweepArgs a, typename PH::T* __restrict__ w) {
+  Sweep<PH, NDIM, NDIR, MHD>::kp_rho(a, w);
+}
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_kp_pcheck(SweepArgs a, const typename PH::T* __restrict__ w) {
+  Sweep<PH, NDIM, NDIR, MHD>::kp_pcheck(a, w);
+}
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_kp_pfix(SweepArgs a, typename PH::T* __restrict__ w) {
+  Sweep<PH, NDIM, NDIR, MHD>::kp_pfix(a, w);
+}
+
 // Dispatch on (ndim, ndir, physics) to a template instance.
 #define VACGPU_DISPATCH(a, KCALL)                                        \
   do {                                                                   \
@@ -501,6 +620,32 @@ struct Launch {
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }
+  // keeppositive on the mesh of w (getboundary with smallfix=T,
+  // src/vacgrid.t:213); decisions stay on the device.
+  static void keeppositive(const SweepArgs& a, T* w, cudaStream_t st) {
+    const unsigned nb = grid_for(a.g.ncell, 128);
+    const unsigned nr = nb > 1216 ? 1216 : nb;
+    const bool floor = a.ph.vacuumrho < 0.0;
+    launch_kp_begin(a.ctrl, floor, st);
+    if (floor) {
+#define KC(D, C, M) k_kp_rhomin<PH, D, C, M><<<nr, 128, 0, st>>>(a, w)
+      VACGPU_DISPATCH(a, KC);
+#undef KC
+      launch_kp_smallrho(a.ctrl, a.ph.smallrhocoeff, st);
+    }
+#define KC(D, C, M) k_kp_rho<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+    pminmax(a, w, st);  // getpthermal's one-time smallp, if still unset
+    launch_smallp(a.ctrl, a.mhd, a.ph.smallpcoeff, st);
+#define KC(D, C, M) k_kp_pcheck<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+#define KC(D, C, M) k_kp_pfix<PH, D, C, M><<<nb, 128, 0, st>>>(a, w)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+    launch_kp_end(a.ctrl, st);
+  }
 };
 
 #define VACGPU_DEFINE_LAUNCHERS(SUF, PH)                                      \
@@ -523,6 +668,10 @@ struct Launch {
   void launch_cell_cmax_##SUF(const SweepArgs& s, const PH::T* w,            \
                               cudaStream_t st) {                             \
     Launch<PH>::cell_cmax(s, w, st);                                         \
+  }                                                                          \
+  void launch_keeppositive_##SUF(const SweepArgs& s, PH::T* w,               \
+                                 cudaStream_t st) {                          \
+    Launch<PH>::keeppositive(s, w, st);                                      \
   }
 
 }  // namespace vacgpu

@@ -298,6 +298,14 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
       launch_correct_mixed(a, (const float*)w, (const float*)w,
                            (const float*)w, (float*)wout, h->st);
     kend(h);
+    if (h->p.smallfix) {
+      kbegin(h, VACGPU_K_GHOST);
+      if (sizeof(T) == 8)
+        launch_keeppositive_fp64(a, (double*)wout, h->st);
+      else
+        launch_keeppositive_mixed(a, (float*)wout, h->st);
+      kend(h);
+    }
     kbegin(h, VACGPU_K_GHOST);
     if (sizeof(T) == 8)
       launch_ghost_fp64(a, (double*)wout, h->st);
@@ -309,6 +317,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     launch_predict_fp64(a, (const double*)w, (double*)w1, h->st);
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
+    if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)w1, h->st);
     launch_ghost_fp64(a, (double*)w1, h->st);
     kend(h);
     kbegin(h, VACGPU_K_CORRECT);
@@ -316,6 +325,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
                         (const double*)base, (double*)wout, h->st);
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
+    if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)wout, h->st);
     launch_ghost_fp64(a, (double*)wout, h->st);
     kend(h);
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
@@ -334,12 +344,14 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   launch_predict_##SUF(a, fw, fw1, h->st);              \
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
+  if (h->p.smallfix) launch_keeppositive_##SUF(a, fw1, h->st); \
   launch_ghost_##SUF(a, fw1, h->st);                    \
   kend(h);                                              \
   kbegin(h, VACGPU_K_CORRECT);                          \
   launch_correct_##SUF(a, fw, fw1, fb, fo, h->st);      \
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
+  if (h->p.smallfix) launch_keeppositive_##SUF(a, fo, h->st); \
   launch_ghost_##SUF(a, fo, h->st);                     \
   kend(h);
     switch (h->pmode) {
@@ -618,6 +630,10 @@ void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
   for (int b = 0; b < VACGPU_MAXB; b++)
     for (int iw = 0; iw < VACGPU_MAXNW; iw++) p->typeB[b][iw] = VACGPU_BC_CONT;
   p->precision = VACGPU_PREC_FP64;
+  p->smallfix = 0;
+  p->smallrho = -1.0;
+  p->smallrhocoeff = 1.0e-6;
+  p->vacuumrho = -1.0;
 }
 
 int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
@@ -661,6 +677,9 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.typefull = p->typefull;
   ph.divbfix = p->divbfix;
   ph.sourceunsplit = p->sourceunsplit;
+  ph.smallfix = p->smallfix;
+  ph.vacuumrho = p->vacuumrho;
+  ph.smallrhocoeff = p->smallrhocoeff;
   ph.src_id = VACGPU_SRC_NONE;
   set_gmaps(ph, p->ndim, p->nw);
   size_t bytes = h->elem * (size_t)g.vs * h->nw;
@@ -694,7 +713,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   h->fused = p->precision == VACGPU_PREC_MIXED && p->dimsplit &&
              (p->ndim == 2 || p->ndim == 3) && p->ndir == p->ndim &&
              p->typelimited == VACGPU_LIMITED_ORIGINAL &&
-             p->typefull == VACGPU_TVDLF;
+             p->typefull == VACGPU_TVDLF && !p->smallfix;
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
   // its ghost writes need uniform maps, periodic faces in pairs and n >= 4
   for (int d = 0; d < p->ndim; d++)
@@ -812,20 +831,6 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   if (!h) return fail("null handle");
   const DevGrid& g = h->g;
   long long n = g.ncell * h->nw;
-  CK(cudaMemcpyAsync(h->stage, w, sizeof(double) * n, cudaMemcpyHostToDevice,
-                     h->st));
-  unsigned nb = (unsigned)((n + 255) / 256);
-  SweepArgs a = make_args(h, 0, 0);
-  a.ctrl = nullptr;
-  if (h->elem == 8) {
-    k_scatter<double><<<nb, 256, 0, h->st>>>(h->stage, (double*)h->buf[0], g, h->nw);
-    launch_ghost_fp64(a, (double*)h->buf[0], h->st);
-  } else {
-    k_scatter<float><<<nb, 256, 0, h->st>>>(h->stage, (float*)h->buf[0], g, h->nw);
-    launch_ghost_mixed(a, (float*)h->buf[0], h->st);
-  }
-  CK(cudaGetLastError());
-  h->cur = 0;
   // it, t, itmin (startup, src/vac.t:176) and the dt state of a fresh run
   Ctrl c;
   CK(cudaMemcpyAsync(&c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
@@ -839,13 +844,32 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   c.dtpar = h->p.dtpar;
   c.courantpar = h->ph.courantpar;
   c.smallp = h->p.smallp;
+  c.smallrho = h->p.smallrho;
+  c.kp_r = c.kp_p = 0;
   for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
   for (int i = 0; i < 4; i++) c.nerror[i] = 0;
   c.dtgrav = h->dtgrav > 0 ? h->dtgrav : BIGD;
   c.cur = 0;
   c.fault = 0;
   CK(cudaMemcpyAsync(h->ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->stage, w, sizeof(double) * n, cudaMemcpyHostToDevice,
+                     h->st));
+  unsigned nb = (unsigned)((n + 255) / 256);
+  // the getboundary before the time loop (src/vac.t:54), keeppositive first
+  // when smallfix
+  SweepArgs a = make_args(h, 0, 0);
+  if (h->elem == 8) {
+    k_scatter<double><<<nb, 256, 0, h->st>>>(h->stage, (double*)h->buf[0], g, h->nw);
+    if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)h->buf[0], h->st);
+    launch_ghost_fp64(a, (double*)h->buf[0], h->st);
+  } else {
+    k_scatter<float><<<nb, 256, 0, h->st>>>(h->stage, (float*)h->buf[0], g, h->nw);
+    if (h->p.smallfix) launch_keeppositive_mixed(a, (float*)h->buf[0], h->st);
+    launch_ghost_mixed(a, (float*)h->buf[0], h->st);
+  }
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->st));
+  h->cur = 0;
   h->it_host = it;
   h->have_state = true;
   return 0;

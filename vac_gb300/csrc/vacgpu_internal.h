@@ -52,6 +52,8 @@ struct DevPhys {
   int typefull;       // VACGPU_TVDLF / VACGPU_TVDLF1
   int divbfix;
   int sourceunsplit;
+  int smallfix;          // keeppositive before each ghost fill
+  double vacuumrho, smallrhocoeff;
   int src_id;
   double src_par[VACGPU_MAXSRCPAR];
   // Boundary index map per face [dim][lo/hi] when every variable shares it:
@@ -111,10 +113,14 @@ struct Ctrl {
   int nerror[4];
   int fault;          // a bounded device wait gave up (TMA never completed)
   int cur;            // batched grids: which state buffer holds the state
+  double smallrho;    // keeppositive_rho: -1 until set from min(rho)
+  int need_smallrho;  // this keeppositive call sets smallrho
+  int kp_r, kp_p;     // this keeppositive call found small rho / p
   // grid-level reductions (ordered-integer keys, atomicMax/atomicMin)
   unsigned long long face_cmax[3][NSLOT];  // corrector max cmax*2/(dx+dx)
   unsigned long long cell_cmax[3][NSLOT];  // getdt_courant max cmax/dx
   unsigned long long pmin[NSLOT], pmax[NSLOT];
+  unsigned long long rmin[NSLOT];          // keeppositive_rho min(rho)
 };
 
 // Order-preserving map of a double onto unsigned 64-bit integers.
@@ -168,7 +174,8 @@ struct SweepArgs {
   void launch_ghost_##SUF(const SweepArgs& s, T* w, cudaStream_t st);        \
   void launch_pminmax_##SUF(const SweepArgs& s, const T* w, cudaStream_t st); \
   void launch_cell_cmax_##SUF(const SweepArgs& s, const T* w,                \
-                              cudaStream_t st);
+                              cudaStream_t st);                              \
+  void launch_keeppositive_##SUF(const SweepArgs& s, T* w, cudaStream_t st);
 VACGPU_DECLARE_LAUNCHERS(fp64, double)
 VACGPU_DECLARE_LAUNCHERS(mixed, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf64, float)
@@ -187,6 +194,11 @@ int fused_smem_bytes(int nw, int d);
 // Precision-independent time-loop kernels (control.cu).
 void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st);
 void launch_smallp(Ctrl* c, int mhd, double smallpcoeff, cudaStream_t st);
+// keeppositive bookkeeping: start (which one-time minima are due), the
+// smallrho fold, and the end (nerror counts of the call).
+void launch_kp_begin(Ctrl* c, int rho_floor, cudaStream_t st);
+void launch_kp_smallrho(Ctrl* c, double coeff, cudaStream_t st);
+void launch_kp_end(Ctrl* c, cudaStream_t st);
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st);
 void launch_step_end(Ctrl* c, int ndim, cudaStream_t st);
 // Batched control: which = 0 dt_begin, 1 smallp, 2 dt_end, 3 step_end

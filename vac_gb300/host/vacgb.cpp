@@ -428,6 +428,10 @@ int main(int argc, char** argv) {
   p.sourceunsplit = getb("sourceunsplit", true);
   p.smallp = getd("smallp", -1.0);
   p.smallpcoeff = getd("smallpcoeff", 1.0e-6);
+  p.smallfix = getb("smallfix", false);
+  p.smallrho = getd("smallrho", -1.0);
+  p.smallrhocoeff = getd("smallrhocoeff", 1.0e-6);
+  p.vacuumrho = getd("vacuumrho", -1.0);
   // paramlist, stoplist
   p.courantpar = getd("courantpar", 0.8);
   p.dtpar = getd("dtpar", -1.0);
@@ -492,9 +496,11 @@ int main(int argc, char** argv) {
     for (int iw = 0; iw < nw; iw++) std::printf("%s%d", iw ? ", " : "", p.typelimiter[iw]);
     std::printf("], \"typelimited\": %d, \"dimsplit\": %d, \"typedimsplit\": %d, \"divbfix\": %d,"
                 " \"courantpar\": %.17g, \"dtpar\": %.17g, \"itmax\": %d, \"tmax\": %.17g,"
-                " \"typeB\": [",
+                " \"smallfix\": %d, \"smallp\": %.17g, \"smallrho\": %.17g,"
+                " \"smallrhocoeff\": %.17g, \"vacuumrho\": %.17g, \"typeB\": [",
                 p.typelimited, p.dimsplit, p.typedimsplit, p.divbfix, p.courantpar, p.dtpar,
-                p.itmax, p.tmax);
+                p.itmax, p.tmax, p.smallfix, p.smallp, p.smallrho, p.smallrhocoeff,
+                p.vacuumrho);
     for (int ib = 0; ib < 2 * p.ndim; ib++) {
       std::printf("%s[", ib ? ", " : "");
       for (int iw = 0; iw < nw; iw++) std::printf("%s%d", iw ? ", " : "", p.typeB[ib][iw]);
