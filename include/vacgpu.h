@@ -122,6 +122,8 @@ typedef struct vacgpu_params {
   double smallrho;              /* -1: min(rho)*smallrhocoeff at 1st use    */
   double smallrhocoeff;
   double vacuumrho;             /* >=0: rho<smallrho becomes vacuum         */
+  int useprimitive;             /* limit primitive variables (upwindLR,     */
+                                /* src/vactvdlf.t:325-362)                  */
 } vacgpu_params;
 
 typedef struct vacgpu_handle vacgpu_handle;

@@ -216,7 +216,35 @@ class NumpyVac:
         ldw[ixO.sl()] = r
         return ldw
 
+    def primitive(self, b, w):
+        """src/vacphys0.t.mhd:31-52, src/vacphys0.t.hd:30-51 (in place)."""
+        sl = b.sl()
+        w[(self.e_,) + sl] = self.getpthermal(w, b, clipping=True)
+        for c in range(1, self.ndir + 1):
+            w[(c,) + sl] = w[(c,) + sl] / w[(0,) + sl]
+
+    def conserve(self, b, w):
+        """src/vacphys0.t.mhd:5-27, src/vacphys0.t.hd:5-26 (in place)."""
+        sl = b.sl()
+        g = self.gamma
+        rho = w[(0,) + sl]
+        vv = self.sq_sum(w, 0, sl)
+        if self.mhd:
+            w[(self.e_,) + sl] = (w[(self.e_,) + sl] / (g - 1)
+                                  + HALF * (rho * vv + self.sq_sum(w, self.b0, sl)))
+        else:
+            w[(self.e_,) + sl] = w[(self.e_,) + sl] / (g - 1) + HALF * rho * vv
+        for c in range(1, self.ndir + 1):
+            w[(c,) + sl] = rho * w[(c,) + sl]
+
     def upwindLR(self, ixL, ixR, idim, w, wLC, wRC):
+        """src/vactvdlf.t:302-367; with useprimitive the base w (over
+        ixG) and the face states are limited in primitive variables and
+        converted back in place."""
+        if self.p.useprimitive:
+            self.primitive(self.ixG, w)
+            self.primitive(ixL, wLC)
+            self.primitive(ixR, wRC)
         ixC = Box(ixL.lo, ixR.shifted(idim, 1).hi)
         ixC.lo[idim] = ixL.lo[idim] - 1
         for iw in range(self.nw):
@@ -225,6 +253,10 @@ class NumpyVac:
             ldw = self.dwlimiter2(dwC, ixC, iw, idim)
             wRC[(iw,) + ixR.sl()] = wRC[(iw,) + ixR.sl()] - HALF * ldw[ixR.sl(idim, 1)]
             wLC[(iw,) + ixL.sl()] = wLC[(iw,) + ixL.sl()] + HALF * ldw[ixL.sl()]
+        if self.p.useprimitive:
+            self.conserve(self.ixG, w)
+            self.conserve(ixL, wLC)
+            self.conserve(ixR, wRC)
 
     # ------------------------------------------------------- grid helpers
     def addflux(self, qdt, ixO, iw, idim, fR, ixR, fL, ixL, wnew):

@@ -349,10 +349,57 @@ static void dwlimiter2(vo_state* s, const double* dwC, box ixC, int iw,
   }
 }
 
-/* upwindLR, src/vactvdlf.t:302-367 (musclomega<=1, useprimitive=F):
- * wRC(ixR) -= ldw(jxR)/2, wLC(ixL) += ldw(ixL)/2 */
-static void upwindLR(vo_state* s, box ixL, box ixR, int idim,
-                     const double* w, double* wLC, double* wRC) {
+/* primitive, src/vacphys0.t.mhd:31-52 and src/vacphys0.t.hd:30-51: the
+ * clipped thermal pressure into e_, v = m/rho */
+static void primitive(vo_state* s, box b, double* w) {
+  getpthermal(s, 1, w, b, s->pp);
+  FORBOX(b, ix) W(w, s->e_)[ix] = s->pp[ix];
+  for (int c = 1; c <= s->ndir; c++) {
+    double* m = W(w, s->m0_ + c);
+    FORBOX(b, ix) m[ix] = m[ix] / W(w, s->rho_)[ix];
+  }
+}
+
+/* conserve, src/vacphys0.t.mhd:5-27 and src/vacphys0.t.hd:5-26 */
+static void conserve(vo_state* s, box b, double* w) {
+  const double gamma = s->p.eqpar[0];
+  FORBOX(b, ix) {
+    double vv = 0.0;
+    for (int c = 1; c <= s->ndir; c++) {
+      double vc = W(w, s->m0_ + c)[ix];
+      vv = (c == 1) ? vc * vc : vv + vc * vc;
+    }
+    const double rho = W(w, s->rho_)[ix];
+    double* e = W(w, s->e_);
+    if (s->mhd) {
+      double bb = 0.0;
+      for (int c = 1; c <= s->ndir; c++) {
+        double bc = W(w, s->b0_ + c)[ix];
+        bb = (c == 1) ? bc * bc : bb + bc * bc;
+      }
+      e[ix] = e[ix] / (gamma - 1) + HALF * (rho * vv + bb);
+    } else {
+      e[ix] = e[ix] / (gamma - 1) + HALF * rho * vv;
+    }
+  }
+  for (int c = 1; c <= s->ndir; c++) {
+    double* m = W(w, s->m0_ + c);
+    FORBOX(b, ix) m[ix] = W(w, s->rho_)[ix] * m[ix];
+  }
+}
+
+/* upwindLR, src/vactvdlf.t:302-367 (musclomega<=1):
+ * wRC(ixR) -= ldw(jxR)/2, wLC(ixL) += ldw(ixL)/2.  With useprimitive the
+ * base w (over ixG) and the face states are limited in primitive
+ * variables and converted back in place (:325-330,357-362), so w leaves
+ * round-tripped. */
+static void upwindLR(vo_state* s, box ixL, box ixR, int idim, double* w,
+                     double* wLC, double* wRC) {
+  if (s->p.useprimitive) {
+    primitive(s, s->ixG, w);
+    primitive(s, ixL, wLC);
+    primitive(s, ixR, wRC);
+  }
   box jxR = shift(ixR, idim, 1);
   box ixC = jxR;
   ixC.lo[idim] = ixL.lo[idim] - 1;
@@ -370,6 +417,11 @@ static void upwindLR(vo_state* s, box ixL, box ixR, int idim,
     double* l = W(wLC, iw);
     FORBOX(ixR, ix) r[ix] = r[ix] - HALF * s->ldw[ix + sh];
     FORBOX(ixL, ix) l[ix] = l[ix] + HALF * s->ldw[ix];
+  }
+  if (s->p.useprimitive) {
+    conserve(s, s->ixG, w);
+    conserve(s, ixL, wLC);
+    conserve(s, ixR, wRC);
   }
 }
 
@@ -592,7 +644,7 @@ static void getboundary(vo_state* s, double* w) {
 
 /* hancock, src/vactvdlf.t:5-89 */
 static void hancock(vo_state* s, double qdt, box ixO, int idimmin,
-                    int idimmax, const double* wCT, double* wnew) {
+                    int idimmax, double* wCT, double* wnew) {
   for (int idim = idimmin; idim <= idimmax; idim++) {
     box hxO = shift(ixO, idim, -1);
     long sh = s->st[idim];
@@ -625,7 +677,7 @@ static void hancock(vo_state* s, double qdt, box ixO, int idimmin,
 /* tvdmusclf with method='tvdlf'/'tvdlf1', addfluxok=.true.,
  * src/vactvdlf.t:92-299 */
 static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
-                      int idimmax, const double* wCT, double* wnew) {
+                      int idimmax, double* wCT, double* wnew) {
   for (int idim = idimmin; idim <= idimmax; idim++) {
     box hxO = shift(ixO, idim, -1);
     box ixC = ixO;
@@ -639,7 +691,7 @@ static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
       FORBOX(ixC, ix) l[ix] = c[ix];
     }
     if (s->p.typefull != VACGPU_TVDLF1) {
-      const double* base;
+      double* base;
       switch (s->p.typelimited) {
         case VACGPU_LIMITED_PREVIOUS: base = s->wold; break;
         case VACGPU_LIMITED_PREDICTOR: base = wCT; break;
@@ -698,7 +750,7 @@ static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
 
 /* advect1, src/vac.t:489-572 (method hancock/tvdlf; ixO = ixI shrunk by 2) */
 static void advect1(vo_state* s, int pred, double qdt, int idimmin,
-                    int idimmax, const double* wCT, double* w) {
+                    int idimmax, double* wCT, double* w) {
   s->istep++;
   if (pred)
     hancock(s, qdt, s->ixM, idimmin, idimmax, wCT, w);

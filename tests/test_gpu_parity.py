@@ -75,7 +75,17 @@ SMALLFIX_CASES = [
     ("hd-smallfix-auto", lambda: inistate.riemann_2d(32, 7), "minmod", "cont", 10,
      _smallfix(), None),
 ]
-FP64_CASES = FP64_CASES + SMALLFIX_CASES
+# reconstruction in primitive variables (upwindLR with useprimitive=T)
+PRIMITIVE_CASES = [
+    ("ot-useprimitive", lambda: inistate.orszag_tang(32), "woodward", "periodic", 12,
+     lambda p: setattr(p, "useprimitive", 1), None),
+    ("hd-useprimitive-cont", lambda: inistate.riemann_2d(40, 4), "minmod", "cont", 12,
+     lambda p: setattr(p, "useprimitive", 1), None),
+    ("rm3-useprimitive-smallfix", lambda: inistate.random_modes(12, seed=4), "minmod",
+     "periodic", 4, lambda p: (setattr(p, "useprimitive", 1), _smallfix(smallp=0.049)(p)),
+     None),
+]
+FP64_CASES = FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES
 
 
 def _ragged():
@@ -166,6 +176,16 @@ def test_graph_replay_matches_plain_launches(gpu_lib, monkeypatch):
 def test_mixed_smallfix_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
     """The split mixed kernels with keeppositive (the fused sweep has no
     global pass between its substeps, so smallfix selects the split path)."""
+    o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
+    a, b = e.state(), o.state()
+    for iw in range(a.shape[0]):
+        rel = np.abs(a[iw] - b[iw]).sum() / np.abs(b[iw]).sum()
+        assert rel <= MIXED_REL_L1, (iw, rel)
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", PRIMITIVE_CASES[:2],
+                         ids=[c[0] for c in PRIMITIVE_CASES[:2]])
+def test_mixed_useprimitive_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
     o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
     a, b = e.state(), o.state()
     for iw in range(a.shape[0]):

@@ -92,6 +92,7 @@ def test_par_parsing_smallfix(vacgb, tmp_path):
     """keeppositive settings of &methodlist reach the parameter block."""
     _setup(tmp_path)
     par = PAR.replace("smallpcoeff=1.D-6", "smallpcoeff=1.D-6\n        smallfix=T\n"
+                      "        useprimitive=T\n"
                       "        smallp=0.25\n        smallrho=0.5D0\n"
                       "        smallrhocoeff=1.D-4\n        vacuumrho=1.D-3")
     out = subprocess.run([vacgb, "--dump-params"], cwd=tmp_path, capture_output=True,
@@ -99,6 +100,7 @@ def test_par_parsing_smallfix(vacgb, tmp_path):
     d = json.loads(out)
     assert d["smallfix"] == 1 and d["smallp"] == 0.25 and d["smallrho"] == 0.5
     assert d["smallrhocoeff"] == 1e-4 and d["vacuumrho"] == 1e-3
+    assert d["useprimitive"] == 1
     d0 = json.loads(subprocess.run([vacgb, "--dump-params"], cwd=tmp_path,
                                    capture_output=True, text=True, input=PAR,
                                    check=True).stdout)

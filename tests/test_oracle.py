@@ -54,7 +54,15 @@ SMALLFIX_CASES = [
     ("hd-smallfix-auto", lambda: inistate.riemann_2d(20, 7), "minmod", "cont", 6,
      smallfix()),
 ]
-CASES = CASES + SMALLFIX_CASES
+CASES = CASES + SMALLFIX_CASES + [
+    # reconstruction in primitive variables (useprimitive=T)
+    ("ot-useprimitive", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5,
+     lambda p: setattr(p, "useprimitive", 1)),
+    ("hd-useprimitive-cont", lambda: inistate.riemann_2d(20, 4), "minmod", "cont", 6,
+     lambda p: setattr(p, "useprimitive", 1)),
+    ("rm3-useprimitive-smallfix", lambda: inistate.random_modes(8, seed=4), "minmod",
+     "periodic", 3, lambda p: (setattr(p, "useprimitive", 1), smallfix(smallp=0.049)(p))),
+]
 
 
 @pytest.mark.parametrize("name,mk,lim,bc,nsteps,tweak", CASES, ids=[c[0] for c in CASES])

@@ -59,6 +59,7 @@ class VacParams(C.Structure):
         ("smallrho", C.c_double),
         ("smallrhocoeff", C.c_double),
         ("vacuumrho", C.c_double),
+        ("useprimitive", C.c_int),
     ]
 
 
@@ -102,6 +103,7 @@ def default_params(ndim, ndir, physics, nx, gamma=5.0 / 3.0):
     p.smallrho = -1.0
     p.smallrhocoeff = 1.0e-6
     p.vacuumrho = -1.0
+    p.useprimitive = 0
     return p
 
 

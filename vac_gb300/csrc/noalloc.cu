@@ -76,9 +76,9 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
         "predictor");
   if (!(p->smallp >= 0.0))
     return vacgpu_internal_fail("vacgpu_sweep_noalloc needs smallp >= 0");
-  if (p->smallfix)
+  if (p->smallfix || p->useprimitive)
     return vacgpu_internal_fail(
-        "vacgpu_sweep_noalloc has no keeppositive (smallfix must be 0)");
+        "vacgpu_sweep_noalloc supports neither smallfix nor useprimitive");
   const double* dxs[3] = {dx0, dx1, dx2};
   long long gcells = 1;
   for (int d = 0; d < p->ndim; d++) {

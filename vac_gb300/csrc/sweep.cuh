@@ -98,8 +98,63 @@ struct Sweep {
     }
   }
 
+  // primitive (src/vacphys0.t.mhd:31-52, src/vacphys0.t.hd:30-51): the
+  // clipped thermal pressure into e, v = m/rho
+  static __device__ __forceinline__ void to_prim(const SweepArgs& a, R smallp,
+                                                 R* u) {
+    R p = R(PH::template pthermal_raw<NDIR, MHD>(u, a.ph));
+    p = (p >= smallp) ? p : smallp;
+    u[L::E] = p;
+#pragma unroll
+    for (int k = 1; k <= NDIR; k++) u[k] = u[k] / u[0];
+  }
+  // conserve (src/vacphys0.t.mhd:5-27, src/vacphys0.t.hd:5-26)
+  static __device__ __forceinline__ void to_cons(const SweepArgs& a, R* u) {
+    R vv = u[1] * u[1];
+#pragma unroll
+    for (int k = 2; k <= NDIR; k++) vv = vv + u[k] * u[k];
+    const R gm1 = R(a.ph.gm1);
+    if (MHD) {
+      R bb = u[L::B0 + 1] * u[L::B0 + 1];
+#pragma unroll
+      for (int k = 2; k <= NDIR; k++) bb = bb + u[L::B0 + k] * u[L::B0 + k];
+      u[L::E] = u[L::E] / gm1 + R(0.5) * (u[0] * vv + bb);
+    } else {
+      u[L::E] = u[L::E] / gm1 + R(0.5) * u[0] * vv;
+    }
+#pragma unroll
+    for (int k = 1; k <= NDIR; k++) u[k] = u[0] * u[k];
+  }
+  static __device__ __forceinline__ void load(const T* __restrict__ w,
+                                              long long o, long long vs, R* u) {
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) u[iw] = R(w[o + iw * vs]);
+  }
+
+  // useprimitive's in-place round trip of the limiter base over the ghost
+  // box: out = conserve(primitive(w)) (src/vactvdlf.t:325-330,357-362).
+  static __device__ void roundtrip(const SweepArgs& a, const T* __restrict__ w,
+                                   T* __restrict__ out) {
+    const Ctrl* ctrl = a.ctrl;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nG = (long long)a.g.nG[0] * a.g.nG[1] * a.g.nG[2];
+    if (ctrl->done || n >= nG) return;
+    const int gx = (int)(n % a.g.nG[0]);
+    const long long r = n / a.g.nG[0];
+    const int gy = (int)(r % a.g.nG[1]), gz = (int)(r / a.g.nG[1]);
+    const long long off = gidx(a.g, gx, gy, gz);
+    R u[NW];
+    load(w, off, a.g.vs, u);
+    to_prim(a, R(ctrl->smallp), u);
+    to_cons(a, u);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) out[off + iw * a.g.vs] = T(u[iw]);
+  }
+
   // Hancock predictor (src/vactvdlf.t:5-89): w1 = w - dt/2/dx*(F(w+ldw/2)
-  // - F(w-ldw/2)) + dt/2*(nsweepdims/ndim)*S(w), on the mesh.
+  // - F(w-ldw/2)) + dt/2*(nsweepdims/ndim)*S(w), on the mesh.  With
+  // useprimitive the slopes and face states are formed in primitive
+  // variables and the sources see the round-tripped state.
   static __device__ void predict(const SweepArgs& a, const T* __restrict__ w,
                                  T* __restrict__ w1) {
     const Ctrl* ctrl = a.ctrl;
@@ -119,15 +174,37 @@ struct Sweep {
       u[iw] = R(w[off + iw * vs]);
       acc[iw] = u[iw];
     }
+    R pc[NW];  // useprimitive: primitive state of the cell
+    if (a.ph.useprim) {
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) pc[iw] = u[iw];
+      to_prim(a, smallp, pc);
+    }
     for (int d = a.d0; d <= a.d1; d++) {
       R uL[NW], uR[NW];
+      if (a.ph.useprim) {
+        R pm[NW], pp[NW];
+        load(w, off - st[d], vs, pm);
+        load(w, off + st[d], vs, pp);
+        to_prim(a, smallp, pm);
+        to_prim(a, smallp, pp);
 #pragma unroll
-      for (int iw = 0; iw < NW; iw++) {
-        R wm = R(w[off + iw * vs - st[d]]);
-        R wp = R(w[off + iw * vs + st[d]]);
-        R l = PH::limiter(a.ph.lim[iw], wp - u[iw], u[iw] - wm);
-        uR[iw] = u[iw] - R(0.5) * l;
-        uL[iw] = u[iw] + R(0.5) * l;
+        for (int iw = 0; iw < NW; iw++) {
+          R l = PH::limiter(a.ph.lim[iw], pp[iw] - pc[iw], pc[iw] - pm[iw]);
+          uR[iw] = pc[iw] - R(0.5) * l;
+          uL[iw] = pc[iw] + R(0.5) * l;
+        }
+        to_cons(a, uR);
+        to_cons(a, uL);
+      } else {
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++) {
+          R wm = R(w[off + iw * vs - st[d]]);
+          R wp = R(w[off + iw * vs + st[d]]);
+          R l = PH::limiter(a.ph.lim[iw], wp - u[iw], u[iw] - wm);
+          uR[iw] = u[iw] - R(0.5) * l;
+          uL[iw] = u[iw] + R(0.5) * l;
+        }
       }
       R fL[NW], fR[NW];
       PH::template flux<NDIR, MHD>(uR, d, a.ph, smallp, fR);
@@ -136,9 +213,16 @@ struct Sweep {
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) acc[iw] = acc[iw] - cq * (fL[iw] - fR[iw]);
     }
-    if (a.ph.sourceunsplit)
+    if (a.ph.sourceunsplit) {
+      // the round-tripped state (useprimitive) leaves rho and B unchanged
+      if (a.ph.useprim) {
+        to_cons(a, pc);
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++) u[iw] = pc[iw];
+      }
       add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, u, w + off, st, c,
                   acc);
+    }
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) w1[off + iw * vs] = T(acc[iw]);
   }
@@ -157,7 +241,29 @@ struct Sweep {
       wL[iw] = R(w1[o + iw * vs]);
       wR[iw] = R(w1[o + iw * vs + s]);
     }
-    if (a.ph.typefull != VACGPU_TVDLF1) {
+    if (a.ph.typefull != VACGPU_TVDLF1 && a.ph.useprim) {
+      // useprimitive: primitive face states and base (src/vactvdlf.t:325-362)
+      R bm[NW], b0[NW], b1[NW], b2[NW];
+      load(base, o - s, vs, bm);
+      load(base, o, vs, b0);
+      load(base, o + s, vs, b1);
+      load(base, o + 2 * s, vs, b2);
+      to_prim(a, smallp, bm);
+      to_prim(a, smallp, b0);
+      to_prim(a, smallp, b1);
+      to_prim(a, smallp, b2);
+      to_prim(a, smallp, wL);
+      to_prim(a, smallp, wR);
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) {
+        R ldL = PH::limiter(a.ph.lim[iw], b1[iw] - b0[iw], b0[iw] - bm[iw]);
+        R ldR = PH::limiter(a.ph.lim[iw], b2[iw] - b1[iw], b1[iw] - b0[iw]);
+        wR[iw] = wR[iw] - R(0.5) * ldR;
+        wL[iw] = wL[iw] + R(0.5) * ldL;
+      }
+      to_cons(a, wL);
+      to_cons(a, wR);
+    } else if (a.ph.typefull != VACGPU_TVDLF1) {
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) {
         const T* b = base + o + iw * vs;
@@ -210,6 +316,11 @@ struct Sweep {
       R acc[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
+      if (a.ph.useprim && a.ph.typefull != VACGPU_TVDLF1) {
+        // the limiter base (the state) leaves upwindLR round-tripped
+        to_prim(a, smallp, acc);
+        to_cons(a, acc);
+      }
       for (int d = a.d0; d <= a.d1; d++) {
         R Fm[NW], Fp[NW];
         R cm = face_flux(a, w1, base, off - st[d], st[d], d, smallp, Fm);
@@ -538,6 +649,13 @@ __global__ void __launch_bounds__(128)
 
 template <class PH, int NDIM, int NDIR, bool MHD>
 __global__ void __launch_bounds__(128)
+    k_roundtrip(SweepArgs a, const typename PH::T* __restrict__ w,
+                typename PH::T* __restrict__ out) {
+  Sweep<PH, NDIM, NDIR, MHD>::roundtrip(a, w, out);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
     k_kp_rhomin(SweepArgs a, const typename PH::T* __restrict__ w) {
   Sweep<PH, NDIM, NDIR, MHD>::template kp_rhomin<128>(a, w);
 }
@@ -620,6 +738,12 @@ struct Launch {
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }
+  static void roundtrip(const SweepArgs& a, const T* w, T* out, cudaStream_t st) {
+    const long long n = (long long)a.g.nG[0] * a.g.nG[1] * a.g.nG[2];
+#define KC(D, C, M) k_roundtrip<PH, D, C, M><<<grid_for(n, 128), 128, 0, st>>>(a, w, out)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
   // keeppositive on the mesh of w (getboundary with smallfix=T,
   // src/vacgrid.t:213); decisions stay on the device.
   static void keeppositive(const SweepArgs& a, T* w, cudaStream_t st) {
@@ -672,6 +796,10 @@ struct Launch {
   void launch_keeppositive_##SUF(const SweepArgs& s, PH::T* w,               \
                                  cudaStream_t st) {                          \
     Launch<PH>::keeppositive(s, w, st);                                      \
+  }                                                                          \
+  void launch_roundtrip_##SUF(const SweepArgs& s, const PH::T* w,            \
+                              PH::T* out, cudaStream_t st) {                 \
+    Launch<PH>::roundtrip(s, w, out, st);                                    \
   }
 
 }  // namespace vacgpu

@@ -287,6 +287,23 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   if (h->p.typelimited == VACGPU_LIMITED_PREDICTOR) base = w1;
   if (h->p.typelimited == VACGPU_LIMITED_PREVIOUS && h->p.dimsplit)
     base = (const T*)h->wold;
+  // useprimitive: the predictor's upwindLR leaves the state round-tripped
+  // through primitive variables (src/vactvdlf.t:325-362); the corrector
+  // limits and updates that copy
+  const T* wc = w;
+  if (h->ph.useprim) {
+    kbegin(h, VACGPU_K_PREDICT);
+    if (sizeof(T) == 8)
+      launch_roundtrip_fp64(a, (const double*)w, (double*)h->wold, h->st);
+    else if (h->pmode == 1)
+      launch_roundtrip_mixedf64(a, (const float*)w, (float*)h->wold, h->st);
+    else if (h->pmode == 2)
+      launch_roundtrip_mixedf32(a, (const float*)w, (float*)h->wold, h->st);
+    else
+      launch_roundtrip_mixed(a, (const float*)w, (float*)h->wold, h->st);
+    kend(h);
+    wc = base = (const T*)h->wold;
+  }
   if (h->p.typefull == VACGPU_TVDLF1) {
     // typepred1='nul': onestep, the corrector alone with wCT = w
     // (src/vacio.t:286-299,511); no limiter, so the base is unused
@@ -321,7 +338,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     launch_ghost_fp64(a, (double*)w1, h->st);
     kend(h);
     kbegin(h, VACGPU_K_CORRECT);
-    launch_correct_fp64(a, (const double*)w, (const double*)w1,
+    launch_correct_fp64(a, (const double*)wc, (const double*)w1,
                         (const double*)base, (double*)wout, h->st);
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
@@ -336,6 +353,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
   } else {
     const float* fw = (const float*)w;
+    const float* fwc = (const float*)wc;
     float* fw1 = (float*)w1;
     float* fo = (float*)wout;
     const float* fb = (const float*)base;
@@ -348,7 +366,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   launch_ghost_##SUF(a, fw1, h->st);                    \
   kend(h);                                              \
   kbegin(h, VACGPU_K_CORRECT);                          \
-  launch_correct_##SUF(a, fw, fw1, fb, fo, h->st);      \
+  launch_correct_##SUF(a, fwc, fw1, fb, fo, h->st);     \
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fo, h->st); \
@@ -531,6 +549,13 @@ int check_params(const vacgpu_params* p) {
   if (!p->dimsplit && p->typelimited == VACGPU_LIMITED_ORIGINAL &&
       p->typefull != VACGPU_TVDLF1)
     return fail("Error in TVDMUSCLF: Unsplit dim. and original is limited");
+  if (p->useprimitive && p->typefull == VACGPU_TVDLF) {
+    if (!p->dimsplit || p->typelimited != VACGPU_LIMITED_ORIGINAL)
+      return fail("useprimitive=T is supported with dimsplit and typelimited='original'");
+    if (p->smallp < 0.0 && !(p->dtpar <= 0.0 && p->courantpar > 0.0))
+      return fail("useprimitive=T with a fixed dt needs smallp given (its first "
+                  "getpthermal call would set smallp over the ghost box)");
+  }
   if (p->physics == VACGPU_PHYS_MHD && p->divbfix && !p->sourceunsplit)
     return fail("divbfix=T requires unsplitsource=T or splitsource=T !");
   for (int d = 0; d < p->ndim; d++)
@@ -680,6 +705,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.smallfix = p->smallfix;
   ph.vacuumrho = p->vacuumrho;
   ph.smallrhocoeff = p->smallrhocoeff;
+  ph.useprim = p->useprimitive && p->typefull == VACGPU_TVDLF;
   ph.src_id = VACGPU_SRC_NONE;
   set_gmaps(ph, p->ndim, p->nw);
   size_t bytes = h->elem * (size_t)g.vs * h->nw;
@@ -688,8 +714,10 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     e = cudaMalloc(&h->buf[i], bytes);
     if (e == cudaSuccess) e = cudaMemset(h->buf[i], 0, bytes);
   }
-  if (e == cudaSuccess && p->typelimited == VACGPU_LIMITED_PREVIOUS &&
-      p->dimsplit)
+  // wold: the step-start copy ('previous') or useprimitive's round-tripped
+  // limiter base
+  if (e == cudaSuccess && ((p->typelimited == VACGPU_LIMITED_PREVIOUS && p->dimsplit) ||
+                           (p->useprimitive && p->typefull == VACGPU_TVDLF)))
     e = cudaMalloc(&h->wold, bytes);
   for (int d = 0; d < 3 && e == cudaSuccess; d++) {
     e = cudaMalloc(&h->dx[d], sizeof(double) * g.nG[d]);
@@ -713,7 +741,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   h->fused = p->precision == VACGPU_PREC_MIXED && p->dimsplit &&
              (p->ndim == 2 || p->ndim == 3) && p->ndir == p->ndim &&
              p->typelimited == VACGPU_LIMITED_ORIGINAL &&
-             p->typefull == VACGPU_TVDLF && !p->smallfix;
+             p->typefull == VACGPU_TVDLF && !p->smallfix && !p->useprimitive;
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
   // its ghost writes need uniform maps, periodic faces in pairs and n >= 4
   for (int d = 0; d < p->ndim; d++)

@@ -54,6 +54,7 @@ struct DevPhys {
   int sourceunsplit;
   int smallfix;          // keeppositive before each ghost fill
   double vacuumrho, smallrhocoeff;
+  int useprim;           // limit primitive variables (useprimitive)
   int src_id;
   double src_par[VACGPU_MAXSRCPAR];
   // Boundary index map per face [dim][lo/hi] when every variable shares it:
@@ -175,7 +176,9 @@ struct SweepArgs {
   void launch_pminmax_##SUF(const SweepArgs& s, const T* w, cudaStream_t st); \
   void launch_cell_cmax_##SUF(const SweepArgs& s, const T* w,                \
                               cudaStream_t st);                              \
-  void launch_keeppositive_##SUF(const SweepArgs& s, T* w, cudaStream_t st);
+  void launch_keeppositive_##SUF(const SweepArgs& s, T* w, cudaStream_t st); \
+  void launch_roundtrip_##SUF(const SweepArgs& s, const T* w, T* out,       \
+                              cudaStream_t st);
 VACGPU_DECLARE_LAUNCHERS(fp64, double)
 VACGPU_DECLARE_LAUNCHERS(mixed, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf64, float)

@@ -412,7 +412,7 @@ int main(int argc, char** argv) {
   }
   if (gets("typeadvance", "twostep") != "twostep")
     die("typeadvance=" + gets("typeadvance", "") + " is not on this path");
-  if (getb("useprimitive", false)) die("useprimitive=T is not on this path");
+  p.useprimitive = getb("useprimitive", false);
   if (getb("sourcesplit", false)) die("sourcesplit=T is not on this path");
   std::string tds = lower(gets("typedimsplit", "default"));
   bool dimsplit = getb("dimsplit", true);
@@ -496,10 +496,10 @@ int main(int argc, char** argv) {
     for (int iw = 0; iw < nw; iw++) std::printf("%s%d", iw ? ", " : "", p.typelimiter[iw]);
     std::printf("], \"typelimited\": %d, \"dimsplit\": %d, \"typedimsplit\": %d, \"divbfix\": %d,"
                 " \"courantpar\": %.17g, \"dtpar\": %.17g, \"itmax\": %d, \"tmax\": %.17g,"
-                " \"smallfix\": %d, \"smallp\": %.17g, \"smallrho\": %.17g,"
+                " \"useprimitive\": %d, \"smallfix\": %d, \"smallp\": %.17g, \"smallrho\": %.17g,"
                 " \"smallrhocoeff\": %.17g, \"vacuumrho\": %.17g, \"typeB\": [",
                 p.typelimited, p.dimsplit, p.typedimsplit, p.divbfix, p.courantpar, p.dtpar,
-                p.itmax, p.tmax, p.smallfix, p.smallp, p.smallrho, p.smallrhocoeff,
+                p.itmax, p.tmax, p.useprimitive, p.smallfix, p.smallp, p.smallrho, p.smallrhocoeff,
                 p.vacuumrho);
     for (int ib = 0; ib < 2 * p.ndim; ib++) {
       std::printf("%s[", ib ? ", " : "");
