@@ -48,12 +48,21 @@ enum {
   VACGPU_LIM_ALBADA = 4
 };
 
-/* typeB(iw,iB) (getboundary, src/vacgrid.t:195-413) */
+/* typeB(iw,iB) (getboundary, src/vacgrid.t:195-413).  'fixed', 'fixed1'
+ * and 'grad1' store their ghost values (grad1: ghost minus edge) at the
+ * first ghost fill after vacgpu_upload and reuse them; 'cont1' extrapolates
+ * linearly every time; 'symm0' is 'symm' with zero flux of the variable
+ * through the boundary face (setnoflux, src/vacgrid.t:416-454). */
 enum {
   VACGPU_BC_CONT = 0,
   VACGPU_BC_PERIODIC = 1,
   VACGPU_BC_SYMM = 2,
-  VACGPU_BC_ASYMM = 3
+  VACGPU_BC_ASYMM = 3,
+  VACGPU_BC_FIXED = 4,
+  VACGPU_BC_FIXED1 = 5,
+  VACGPU_BC_CONT1 = 6,
+  VACGPU_BC_GRAD1 = 7,
+  VACGPU_BC_SYMM0 = 8
 };
 
 /* typefull1 (src/vactvdlf.t:92-299): second order 'tvdlf' or 'tvdlf1' */

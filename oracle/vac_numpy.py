@@ -52,6 +52,8 @@ class NumpyVac:
                        [self.nG[d] - 3 if d < self.ndim else 0 for d in range(3)])
         self.smallp = p.smallp
         self.smallrho = p.smallrho
+        self.fixB = {}
+        self.initialized = False
         self.courantpar = p.courantpar
         self.dtpar = p.dtpar
         if self.dtpar > 0 and p.slowsteps != 1:
@@ -260,6 +262,7 @@ class NumpyVac:
 
     # ------------------------------------------------------- grid helpers
     def addflux(self, qdt, ixO, iw, idim, fR, ixR, fL, ixL, wnew):
+        self.setnoflux(iw, idim, ixO, fR, ixR, fL, ixL)
         wnew[(iw,) + ixO.sl()] = (wnew[(iw,) + ixO.sl()]
                                   - qdt / self.dx[(idim,) + ixO.sl()]
                                   * (fR[ixR.sl()] - fL[ixL.sl()]))
@@ -333,16 +336,27 @@ class NumpyVac:
                 else:
                     w[(self.e_,) + sl] = a + HALF / rho * mm
 
+    def region(self, iB):
+        idim, upper = iB // 2, iB % 2
+        r = Box(self.ixG.lo, self.ixG.hi)
+        if upper:
+            r.lo[idim] = self.ixM.hi[idim] + 1
+        else:
+            r.hi[idim] = self.ixM.lo[idim] - 1
+        return r
+
     def getboundary(self, w):
+        """src/vacgrid.t:195-413: regions in iB order over the full extent
+        of the other dimensions; fixed/fixed1/grad1 store their ghost
+        values (grad1: minus the edge) at the first call."""
         if self.p.smallfix:
             self.keeppositive(w)
+        fixed_types = (abi.BC_FIXED, abi.BC_FIXED1, abi.BC_GRAD1)
         for iB in range(2 * self.ndim):
             idim, upper = iB // 2, iB % 2
-            r = Box(self.ixG.lo, self.ixG.hi)
-            if upper:
-                r.lo[idim] = self.ixM.hi[idim] + 1
-            else:
-                r.hi[idim] = self.ixM.lo[idim] - 1
+            r = self.region(iB)
+            ixe = r.lo[idim] - 1 if upper else r.hi[idim] + 1
+            ixf = ixe - 1 if upper else ixe + 1
             for iw in range(self.nw):
                 typ = self.p.typeB[iB][iw]
                 if typ == abi.BC_PERIODIC:
@@ -352,13 +366,58 @@ class NumpyVac:
                 for k in range(r.lo[idim], r.hi[idim] + 1):
                     row = Box(r.lo, r.hi)
                     row.lo[idim] = row.hi[idim] = k
-                    if typ == abi.BC_CONT:
-                        ixe = r.lo[idim] - 1 if upper else r.hi[idim] + 1
+                    if typ in fixed_types and self.initialized:
+                        fb = self.fixB[(iB, iw)][row.sl()]
+                        if typ == abi.BC_GRAD1:
+                            w[(iw,) + row.sl()] = fb + w[(iw,) + row.sl(idim, ixe - k)]
+                        else:
+                            w[(iw,) + row.sl()] = fb
+                    elif typ in (abi.BC_CONT, abi.BC_FIXED):
+                        w[(iw,) + row.sl()] = w[(iw,) + row.sl(idim, ixe - k)]
+                    elif typ in (abi.BC_CONT1, abi.BC_FIXED1, abi.BC_GRAD1):
+                        dk = abs(k - ixe)
+                        w[(iw,) + row.sl()] = ((dk + 1) * w[(iw,) + row.sl(idim, ixe - k)]
+                                               - dk * w[(iw,) + row.sl(idim, ixf - k)])
                     else:
-                        ixe = (2 * r.lo[idim] - 1 if upper else 2 * r.hi[idim] + 1) - k
-                    w[(iw,) + row.sl()] = w[(iw,) + row.sl(idim, ixe - k)]
+                        ixm = (2 * r.lo[idim] - 1 if upper else 2 * r.hi[idim] + 1) - k
+                        w[(iw,) + row.sl()] = w[(iw,) + row.sl(idim, ixm - k)]
                 if typ == abi.BC_ASYMM:
                     w[(iw,) + r.sl()] = -w[(iw,) + r.sl()]
+        if not self.initialized:
+            self.initialized = True
+            for iB in range(2 * self.ndim):
+                idim, upper = iB // 2, iB % 2
+                r = self.region(iB)
+                ixe = r.lo[idim] - 1 if upper else r.hi[idim] + 1
+                for iw in range(self.nw):
+                    typ = self.p.typeB[iB][iw]
+                    if typ not in fixed_types:
+                        continue
+                    fb = np.zeros(self.nG)
+                    for k in range(r.lo[idim], r.hi[idim] + 1):
+                        row = Box(r.lo, r.hi)
+                        row.lo[idim] = row.hi[idim] = k
+                        if typ == abi.BC_GRAD1:
+                            fb[row.sl()] = w[(iw,) + row.sl()] - w[(iw,) + row.sl(idim, ixe - k)]
+                        else:
+                            fb[row.sl()] = w[(iw,) + row.sl()]
+                    self.fixB[(iB, iw)] = fb
+
+    def setnoflux(self, iw, idim, ixO, fR, ixR, fL, ixL):
+        """src/vacgrid.t:416-454: zero flux through a 'symm0' face."""
+        for upper in (0, 1):
+            iB = 2 * idim + upper
+            if self.p.typeB[iB][iw] != abi.BC_SYMM0:
+                continue
+            face = self.region(iB)
+            if upper:
+                ixe = face.lo[idim] - 1 + ixR.lo[idim] - ixO.lo[idim]
+                face.lo[idim] = face.hi[idim] = ixe
+                fR[face.sl()] = ZERO
+            else:
+                ixe = face.hi[idim] + 1 + ixL.lo[idim] - ixO.lo[idim]
+                face.lo[idim] = face.hi[idim] = ixe
+                fL[face.sl()] = ZERO
 
     # ------------------------------------------------------------ schemes
     def hancock(self, qdt, ixO, d0, d1, wCT, wnew):

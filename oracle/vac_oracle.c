@@ -57,6 +57,11 @@ typedef struct vo_state {
   int it, itmin;
   double smallp;
   double smallrho;   /* keeppositive_rho: -1 until set from min(rho) */
+  /* fixed/fixed1/grad1 ghost values (grad1: minus the edge), stored by the
+   * first getboundary call (src/vacgrid.t:373-409); full-size arrays per
+   * boundary region, only the region's cells used */
+  double* fixB[VACGPU_MAXB];
+  int initialized;
   int nerror[4];
   int istep, nstep;
   int src_id;
@@ -427,11 +432,37 @@ static void upwindLR(vo_state* s, box ixL, box ixR, int idim, double* w,
 
 /* -------------------------------------------------------------- grid/flux */
 
-/* addflux, src/vacgrid.t:596-741, Cartesian slab branch (:669-678):
+static box region(vo_state* s, int iB);
+/* setnoflux, src/vacgrid.t:416-454 (called from addflux, :639-640): a
+ * variable with 'symm0' at a face of idim has zero flux through that face:
+ * fR at the last mesh layer (upper face), fL at the layer before the first
+ * (lower face); fR/fL are indexed as addflux's fRC(ixR)/fLC(ixL). */
+static void setnoflux(vo_state* s, int iw, int idim, box ixO, double* fR,
+                      box ixR, double* fL, box ixL) {
+  for (int upper = 0; upper < 2; upper++) {
+    const int iB = 2 * idim + upper;
+    if (s->p.typeB[iB][iw] != VACGPU_BC_SYMM0) continue;
+    box r = region(s, iB);
+    box face = r;
+    if (upper) {
+      /* fRC(ixe) with ixe = ixBmin-1+ixRmin-ixmin */
+      const int ixe = r.lo[idim] - 1 + ixR.lo[idim] - ixO.lo[idim];
+      face.lo[idim] = face.hi[idim] = ixe;
+      FORBOX(face, ix) fR[ix] = ZERO;
+    } else {
+      const int ixe = r.hi[idim] + 1 + ixL.lo[idim] - ixO.lo[idim];
+      face.lo[idim] = face.hi[idim] = ixe;
+      FORBOX(face, ix) fL[ix] = ZERO;
+    }
+  }
+}
+
+/* addflux, src/vacgrid.t:596-741, Cartesian slab branch (:669-678), after
+ * setnoflux (:639-640):
  * wnew(ix) -= qdt/dx(ix,idim)*(fRC(ixR)-fLC(ixL)) */
 static void addflux(vo_state* s, double qdt, box ixO, int iw, int idim,
-                    const double* fR, box ixR, const double* fL, box ixL,
-                    double* wnew) {
+                    double* fR, box ixR, double* fL, box ixL, double* wnew) {
+  setnoflux(s, iw, idim, ixO, fR, ixR, fL, ixL);
   long oR = IDX(s, ixR.lo[0], ixR.lo[1], ixR.lo[2]) -
             IDX(s, ixO.lo[0], ixO.lo[1], ixO.lo[2]);
   long oL = IDX(s, ixL.lo[0], ixL.lo[1], ixL.lo[2]) -
@@ -596,45 +627,108 @@ static void keeppositive(vo_state* s, double* w) {
   }
 }
 
+/* ghost region iB (boundsetup defaults, src/vacgrid.t:53-69): the two
+ * ghost layers of idim over the full ghost box in the other dimensions */
+static box region(vo_state* s, int iB) {
+  const int idim = iB / 2, upper = iB % 2;
+  box r = s->ixG;
+  if (upper) {
+    r.lo[idim] = s->ixM.hi[idim] + 1;
+    r.hi[idim] = s->ixG.hi[idim];
+  } else {
+    r.lo[idim] = s->ixG.lo[idim];
+    r.hi[idim] = s->ixM.lo[idim] - 1;
+  }
+  return r;
+}
+
 /* getboundary, src/vacgrid.t:195-413 with the default regions of boundsetup
  * (src/vacgrid.t:53-69) and periodic pairing (:121-135); keeppositive first
- * when smallfix (:213). */
+ * when smallfix (:213).  Regions are filled in iB order, each over the full
+ * extent of the other dimensions. */
 static void getboundary(vo_state* s, double* w) {
   if (s->p.smallfix) keeppositive(s, w);
   for (int iB = 0; iB < 2 * s->ndim; iB++) {
-    int idim = iB / 2, upper = iB % 2;
-    box r = s->ixG;
-    if (upper) {
-      r.lo[idim] = s->ixM.hi[idim] + 1;
-      r.hi[idim] = s->ixG.hi[idim];
-    } else {
-      r.lo[idim] = s->ixG.lo[idim];
-      r.hi[idim] = s->ixM.lo[idim] - 1;
-    }
+    const int idim = iB / 2, upper = iB % 2;
+    const box r = region(s, iB);
     long sh = s->st[idim];
+    /* edge (ixe) and inner edge (ixf) mesh layers */
+    const int ixe = upper ? r.lo[idim] - 1 : r.hi[idim] + 1;
+    const int ixf = upper ? ixe - 1 : ixe + 1;
     for (int iw = 0; iw < s->nw; iw++) {
       double* a = W(w, iw);
       int type = s->p.typeB[iB][iw];
-      if (type == VACGPU_BC_CONT) {
-        int ixe = upper ? r.lo[idim] - 1 : r.hi[idim] + 1;
+      const int fixedtype = type == VACGPU_BC_FIXED || type == VACGPU_BC_FIXED1 ||
+                            type == VACGPU_BC_GRAD1;
+      if (fixedtype && s->initialized) {
+        /* restore the stored values, grad1 on top of the current edge */
+        const double* fb = W(s->fixB[iB], iw);
+        for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
+          box row = r;
+          row.lo[idim] = row.hi[idim] = k;
+          long off = (long)(ixe - k) * sh;
+          if (type == VACGPU_BC_GRAD1)
+            FORBOX(row, ix) a[ix] = fb[ix] + a[ix + off];
+          else
+            FORBOX(row, ix) a[ix] = fb[ix];
+        }
+      } else if (type == VACGPU_BC_CONT || type == VACGPU_BC_FIXED) {
         for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
           box row = r;
           row.lo[idim] = row.hi[idim] = k;
           long off = (long)(ixe - k) * sh;
           FORBOX(row, ix) a[ix] = a[ix + off];
         }
+      } else if (type == VACGPU_BC_CONT1 || type == VACGPU_BC_FIXED1 ||
+                 type == VACGPU_BC_GRAD1) {
+        /* first order extrapolation, (|ix-ixe|+1)*w(ixe)-|ix-ixe|*w(ixf) */
+        for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
+          box row = r;
+          row.lo[idim] = row.hi[idim] = k;
+          const int dk = abs(k - ixe);
+          long oe = (long)(ixe - k) * sh, of = (long)(ixf - k) * sh;
+          FORBOX(row, ix) a[ix] = (dk + 1) * a[ix + oe] - dk * a[ix + of];
+        }
       } else if (type == VACGPU_BC_PERIODIC) {
         long off = (long)(upper ? -(s->nG[idim] - 4) : (s->nG[idim] - 4)) * sh;
         FORBOX(r, ix) a[ix] = a[ix + off];
       } else {
-        int ixe = upper ? 2 * r.lo[idim] - 1 : 2 * r.hi[idim] + 1;
+        /* symm, symm0, asymm */
+        int ixm = upper ? 2 * r.lo[idim] - 1 : 2 * r.hi[idim] + 1;
         for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
           box row = r;
           row.lo[idim] = row.hi[idim] = k;
-          long off = (long)((ixe - k) - k) * sh;
+          long off = (long)((ixm - k) - k) * sh;
           FORBOX(row, ix) a[ix] = a[ix + off];
         }
         if (type == VACGPU_BC_ASYMM) FORBOX(r, ix) a[ix] = -a[ix];
+      }
+    }
+  }
+  if (!s->initialized) {
+    /* fixed boundaries store their values, grad1 its differences */
+    s->initialized = 1;
+    for (int iB = 0; iB < 2 * s->ndim; iB++) {
+      const int idim = iB / 2, upper = iB % 2;
+      const box r = region(s, iB);
+      long sh = s->st[idim];
+      const int ixe = upper ? r.lo[idim] - 1 : r.hi[idim] + 1;
+      for (int iw = 0; iw < s->nw; iw++) {
+        int type = s->p.typeB[iB][iw];
+        if (type != VACGPU_BC_FIXED && type != VACGPU_BC_FIXED1 && type != VACGPU_BC_GRAD1)
+          continue;
+        if (!s->fixB[iB]) s->fixB[iB] = calloc(s->N * s->nw, sizeof(double));
+        double* fb = W(s->fixB[iB], iw);
+        const double* a = W(w, iw);
+        for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
+          box row = r;
+          row.lo[idim] = row.hi[idim] = k;
+          long off = (long)(ixe - k) * sh;
+          if (type == VACGPU_BC_GRAD1)
+            FORBOX(row, ix) fb[ix] = a[ix] - a[ix + off];
+          else
+            FORBOX(row, ix) fb[ix] = a[ix];
+        }
       }
     }
   }
@@ -911,6 +1005,7 @@ void vo_destroy(vo_state* s) {
                  s->dwC, s->tmp, s->tmp2, s->divb, s->csound2, s->cfast2,
                  s->pp};
   for (unsigned i = 0; i < sizeof(a) / sizeof(a[0]); i++) free(a[i]);
+  for (int iB = 0; iB < VACGPU_MAXB; iB++) free(s->fixB[iB]);
   free(s);
 }
 
@@ -1006,6 +1101,7 @@ void vo_set_state(vo_state* s, const double* wmesh, int it, double t) {
   s->it = it;
   s->itmin = it;
   s->t = t;
+  s->initialized = 0;  /* a new run: fixed boundaries store again */
   getboundary(s, s->w);
 }
 

@@ -85,7 +85,34 @@ PRIMITIVE_CASES = [
      "periodic", 4, lambda p: (setattr(p, "useprimitive", 1), _smallfix(smallp=0.049)(p)),
      None),
 ]
-FP64_CASES = FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES
+def _bcs(*per_face):
+    """typeB per face (x-lo, x-hi, y-lo, y-hi[, z-lo, z-hi]); an entry may
+    be a dict {iw: type} over a default "*"."""
+    def tweak(p):
+        for iB, spec in enumerate(per_face):
+            for iw in range(p.nw):
+                p.typeB[iB][iw] = (spec.get(iw, spec.get("*", abi.BC_CONT))
+                                   if isinstance(spec, dict) else spec)
+    return tweak
+
+
+B = abi
+# fixed, fixed1, cont1, grad1 (ordered face fill, stored values) and
+# symm0 (zero flux through the face)
+BC_CASES = [
+    ("hd-fixed-cont1", lambda: inistate.riemann_2d(40, 8), "minmod", "cont", 12,
+     _bcs(B.BC_FIXED, B.BC_CONT1, B.BC_CONT1, B.BC_FIXED), None),
+    ("hd-fixed1-grad1", lambda: inistate.riemann_2d(40, 9), "minmod", "cont", 12,
+     _bcs(B.BC_FIXED1, B.BC_GRAD1, B.BC_GRAD1, B.BC_FIXED1), None),
+    ("ot-symm0-walls", lambda: inistate.orszag_tang(32), "woodward", "cont", 10,
+     _bcs({"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM},
+          {"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM}, B.BC_PERIODIC, B.BC_PERIODIC),
+     None),
+    ("rm3-mixed-bcs", lambda: inistate.random_modes(12, seed=6), "minmod", "cont", 4,
+     _bcs(B.BC_GRAD1, B.BC_FIXED, B.BC_SYMM0, B.BC_CONT1, B.BC_PERIODIC, B.BC_PERIODIC),
+     None),
+]
+FP64_CASES = FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES
 
 
 def _ragged():
@@ -186,6 +213,16 @@ def test_mixed_smallfix_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, s
 @pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", PRIMITIVE_CASES[:2],
                          ids=[c[0] for c in PRIMITIVE_CASES[:2]])
 def test_mixed_useprimitive_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
+    o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
+    a, b = e.state(), o.state()
+    for iw in range(a.shape[0]):
+        rel = np.abs(a[iw] - b[iw]).sum() / np.abs(b[iw]).sum()
+        assert rel <= MIXED_REL_L1, (iw, rel)
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", BC_CASES,
+                         ids=[c[0] for c in BC_CASES])
+def test_mixed_boundary_types_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
     o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
     a, b = e.state(), o.state()
     for iw in range(a.shape[0]):

@@ -54,7 +54,35 @@ SMALLFIX_CASES = [
     ("hd-smallfix-auto", lambda: inistate.riemann_2d(20, 7), "minmod", "cont", 6,
      smallfix()),
 ]
-CASES = CASES + SMALLFIX_CASES + [
+def bcs(*per_face):
+    """Tweak: typeB per face (x-lo, x-hi, y-lo, y-hi[, z-lo, z-hi]) for all
+    variables; a face entry may be a dict {iw: type} over a default."""
+    def tweak(p):
+        for iB, spec in enumerate(per_face):
+            if isinstance(spec, dict):
+                dflt = spec.get("*", abi.BC_CONT)
+                for iw in range(p.nw):
+                    p.typeB[iB][iw] = spec.get(iw, dflt)
+            else:
+                for iw in range(p.nw):
+                    p.typeB[iB][iw] = spec
+    return tweak
+
+
+B = abi
+BC_CASES = [
+    ("hd-fixed-cont1", lambda: inistate.riemann_2d(20, 8), "minmod", "cont", 6,
+     bcs(B.BC_FIXED, B.BC_CONT1, B.BC_CONT1, B.BC_FIXED)),
+    ("hd-fixed1-grad1", lambda: inistate.riemann_2d(20, 9), "minmod", "cont", 6,
+     bcs(B.BC_FIXED1, B.BC_GRAD1, B.BC_GRAD1, B.BC_FIXED1)),
+    ("ot-symm0-walls", lambda: inistate.orszag_tang(16), "woodward", "cont", 5,
+     bcs({"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM}, {"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM},
+         B.BC_PERIODIC, B.BC_PERIODIC)),
+    ("rm3-mixed-bcs", lambda: inistate.random_modes(8, seed=6), "minmod", "cont", 3,
+     bcs(B.BC_GRAD1, B.BC_FIXED, B.BC_SYMM0, B.BC_CONT1, B.BC_PERIODIC, B.BC_PERIODIC)),
+]
+
+CASES = CASES + SMALLFIX_CASES + BC_CASES + [
     # reconstruction in primitive variables (useprimitive=T)
     ("ot-useprimitive", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5,
      lambda p: setattr(p, "useprimitive", 1)),

@@ -13,7 +13,7 @@ MAXSRCPAR = 8
 
 PHYS_HD, PHYS_MHD = 0, 1
 LIM_MINMOD, LIM_WOODWARD, LIM_SUPERBEE, LIM_VANLEER, LIM_ALBADA = range(5)
-BC_CONT, BC_PERIODIC, BC_SYMM, BC_ASYMM = range(4)
+BC_CONT, BC_PERIODIC, BC_SYMM, BC_ASYMM, BC_FIXED, BC_FIXED1, BC_CONT1, BC_GRAD1, BC_SYMM0 = range(9)
 TVDLF, TVDLF1 = 0, 1
 LIMITED_ORIGINAL, LIMITED_PREVIOUS, LIMITED_PREDICTOR = range(3)
 SPLIT_XYYX, SPLIT_XY = 0, 1
@@ -24,7 +24,8 @@ LIMITER_NAMES = {"minmod": LIM_MINMOD, "woodward": LIM_WOODWARD,
                  "superbee": LIM_SUPERBEE, "vanleer": LIM_VANLEER,
                  "albada": LIM_ALBADA}
 BC_NAMES = {"cont": BC_CONT, "periodic": BC_PERIODIC, "symm": BC_SYMM,
-            "asymm": BC_ASYMM}
+            "asymm": BC_ASYMM, "fixed": BC_FIXED, "fixed1": BC_FIXED1,
+            "cont1": BC_CONT1, "grad1": BC_GRAD1, "symm0": BC_SYMM0}
 
 
 class VacParams(C.Structure):

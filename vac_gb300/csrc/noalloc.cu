@@ -147,6 +147,10 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
   ph.sourceunsplit = p->sourceunsplit;
   ph.src_id = VACGPU_SRC_NONE;
   set_gmaps(ph, p->ndim, p->nw);
+  for (int d = 0; d < p->ndim; d++)
+    if (ph.genbc || ph.noflux[d][0] || ph.noflux[d][1])
+      return vacgpu_internal_fail(
+          "vacgpu_sweep_noalloc supports cont, periodic, symm and asymm faces");
   for (int d = 0; d < 3; d++) s.a.dx[d] = dxs[d];
   s.ctrl = a.ctrl;
   s.ndir = p->ndir;

@@ -209,6 +209,18 @@ struct Sweep {
       R fL[NW], fR[NW];
       PH::template flux<NDIR, MHD>(uR, d, a.ph, smallp, fR);
       PH::template flux<NDIR, MHD>(uL, d, a.ph, smallp, fL);
+      // 'symm0' faces (setnoflux, src/vacgrid.t:416-454): no flux through
+      // the mesh edge
+      if (c[d] == a.g.nx[d] + 1 && a.ph.noflux[d][1]) {
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++)
+          if ((a.ph.noflux[d][1] >> iw) & 1) fL[iw] = R(0);
+      }
+      if (c[d] == 2 && a.ph.noflux[d][0]) {
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++)
+          if ((a.ph.noflux[d][0] >> iw) & 1) fR[iw] = R(0);
+      }
       const R cq = PH::qdx(qdt, a.a, d, c[d]);
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) acc[iw] = acc[iw] - cq * (fL[iw] - fR[iw]);
@@ -330,6 +342,16 @@ struct Sweep {
           double qp = PH::cfl(cp, a.a, d, c[d]);
           unsigned long long km = dkey(qm), kp = dkey(qp);
           key[d] = km > kp ? km : kp;
+        }
+        if (c[d] == a.g.nx[d] + 1 && a.ph.noflux[d][1]) {  // 'symm0'
+#pragma unroll
+          for (int iw = 0; iw < NW; iw++)
+            if ((a.ph.noflux[d][1] >> iw) & 1) Fp[iw] = R(0);
+        }
+        if (c[d] == 2 && a.ph.noflux[d][0]) {
+#pragma unroll
+          for (int iw = 0; iw < NW; iw++)
+            if ((a.ph.noflux[d][0] >> iw) & 1) Fm[iw] = R(0);
         }
         const R cq = PH::qdx(qdt, a.a, d, c[d]);
 #pragma unroll
@@ -611,6 +633,116 @@ __global__ void k_ghost(T* __restrict__ w, DevGrid g, DevPhys ph,
   ghost_cell<T, NW>(w, g, ph, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// Ordered ghost fill for grids with 'fixed', 'fixed1', 'cont1' or 'grad1'
+// faces: the body of getboundary's region loop (src/vacgrid.t:230-366) for
+// region iB -- the two ghost layers of dimension iB/2 over the full ghost
+// box of the other dimensions -- launched in iB order so corners see the
+// earlier regions' values as in the reference.  restore: the stored values
+// of the fixed types (src/vacgrid.t:253-305) are used; otherwise they are
+// computed ('fixed' as 'cont', 'fixed1'/'grad1' as 'cont1').
+__device__ __forceinline__ long long face_cells(const DevGrid& g, int iB,
+                                                int* lo, int* ext) {
+  const int idim = iB / 2, upper = iB % 2;
+  for (int d = 0; d < 3; d++) {
+    lo[d] = 0;
+    ext[d] = g.nG[d];
+  }
+  ext[idim] = 2;
+  lo[idim] = upper ? g.nx[idim] + 2 : 0;
+  return (long long)ext[0] * ext[1] * ext[2];
+}
+
+template <typename T, int NW>
+__global__ void k_ghost_face(T* __restrict__ w, DevGrid g, DevPhys ph,
+                             const Ctrl* ctrl, int iB,
+                             const T* __restrict__ fixb, int restore) {
+  if (ctrl && ctrl->done) return;
+  int lo[3], ext[3];
+  const long long tot = face_cells(g, iB, lo, ext);
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= tot) return;
+  const int idim = iB / 2, upper = iB % 2;
+  int c[3];
+  c[0] = lo[0] + (int)(n % ext[0]);
+  const long long r = n / ext[0];
+  c[1] = lo[1] + (int)(r % ext[1]);
+  c[2] = lo[2] + (int)(r / ext[1]);
+  const int k = c[idim], nx = g.nx[idim];
+  const int ixe = upper ? nx + 1 : 2;  // edge mesh layer
+  const int ixf = upper ? ixe - 1 : ixe + 1;
+  auto at = [&](int kk) {
+    int cc[3] = {c[0], c[1], c[2]};
+    cc[idim] = kk;
+    return gidx(g, cc[0], cc[1], cc[2]);
+  };
+  const long long dst = gidx(g, c[0], c[1], c[2]);
+  const long long oe = at(ixe), of = at(ixf);
+  const int dk = k > ixe ? k - ixe : ixe - k;
+#pragma unroll
+  for (int iw = 0; iw < NW; iw++) {
+    const int t = ph.typeB[iB][iw];
+    const long long vo = (long long)iw * g.vs;
+    const bool fixedtype = t == VACGPU_BC_FIXED || t == VACGPU_BC_FIXED1 ||
+                           t == VACGPU_BC_GRAD1;
+    T v;
+    if (fixedtype && restore) {
+      v = fixb[iw * tot + n];
+      if (t == VACGPU_BC_GRAD1) v = v + w[oe + vo];
+    } else if (t == VACGPU_BC_CONT || t == VACGPU_BC_FIXED) {
+      v = w[oe + vo];
+    } else if (fixedtype || t == VACGPU_BC_CONT1) {
+      v = T(dk + 1) * w[oe + vo] - T(dk) * w[of + vo];
+    } else if (t == VACGPU_BC_PERIODIC) {
+      v = w[at(upper ? k - nx : k + nx) + vo];
+    } else {  // symm, symm0, asymm
+      const int ixm = upper ? 2 * nx + 3 : 3;
+      v = w[at(ixm - k) + vo];
+      if (t == VACGPU_BC_ASYMM) v = -v;
+    }
+    w[dst + vo] = v;
+  }
+}
+
+// The first fill's values of the fixed types (grad1: minus the edge),
+// src/vacgrid.t:373-409.
+template <typename T, int NW>
+__global__ void k_fix_store(const T* __restrict__ w, DevGrid g, DevPhys ph,
+                            int iB, T* __restrict__ fixb) {
+  int lo[3], ext[3];
+  const long long tot = face_cells(g, iB, lo, ext);
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= tot) return;
+  const int idim = iB / 2, upper = iB % 2;
+  int c[3];
+  c[0] = lo[0] + (int)(n % ext[0]);
+  const long long r = n / ext[0];
+  c[1] = lo[1] + (int)(r % ext[1]);
+  c[2] = lo[2] + (int)(r / ext[1]);
+  int ce[3] = {c[0], c[1], c[2]};
+  ce[idim] = upper ? g.nx[idim] + 1 : 2;
+  const long long dst = gidx(g, c[0], c[1], c[2]);
+  const long long oe = gidx(g, ce[0], ce[1], ce[2]);
+#pragma unroll
+  for (int iw = 0; iw < NW; iw++) {
+    const int t = ph.typeB[iB][iw];
+    const long long vo = (long long)iw * g.vs;
+    if (t == VACGPU_BC_GRAD1)
+      fixb[iw * tot + n] = w[dst + vo] - w[oe + vo];
+    else if (t == VACGPU_BC_FIXED || t == VACGPU_BC_FIXED1)
+      fixb[iw * tot + n] = w[dst + vo];
+  }
+}
+
+// Elements of the fixed-boundary store of face iB (offset of face iB: the
+// sum over the earlier faces).
+inline long long fix_face_elems(const DevGrid& g, int iB, int nw) {
+  const int idim = iB / 2;
+  long long n = 2;
+  for (int d = 0; d < 3; d++)
+    if (d != idim) n *= g.nG[d];
+  return n * nw;
+}
+
 inline long long ghost_count(const DevGrid& g) {
   long long nzs = g.ndim == 3 ? 4LL * g.nG[1] * g.nG[0] : 0;
   long long nys = g.ndim >= 2 ? 4LL * g.nx[2] * g.nG[0] : 0;
@@ -738,6 +870,41 @@ struct Launch {
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }
+  // getboundary face by face (grids with fixed/extrapolating faces)
+  static void ghost_faces(const SweepArgs& a, T* w, T* fixb, int restore,
+                          cudaStream_t st) {
+    const int nw = a.mhd ? 2 + 2 * a.ndir : 2 + a.ndir;
+    long long off = 0;
+    for (int iB = 0; iB < 2 * a.g.ndim; iB++) {
+      const long long tot = fix_face_elems(a.g, iB, 1);
+      const unsigned nb = grid_for(tot, 128);
+      T* fb = fixb + off;
+      switch (nw) {
+        case 3: k_ghost_face<T, 3><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+        case 4: k_ghost_face<T, 4><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+        case 5: k_ghost_face<T, 5><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+        case 6: k_ghost_face<T, 6><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+        case 8: k_ghost_face<T, 8><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+      }
+      off += fix_face_elems(a.g, iB, nw);
+    }
+  }
+  static void fix_store(const SweepArgs& a, const T* w, T* fixb, cudaStream_t st) {
+    const int nw = a.mhd ? 2 + 2 * a.ndir : 2 + a.ndir;
+    long long off = 0;
+    for (int iB = 0; iB < 2 * a.g.ndim; iB++) {
+      const unsigned nb = grid_for(fix_face_elems(a.g, iB, 1), 128);
+      T* fb = fixb + off;
+      switch (nw) {
+        case 3: k_fix_store<T, 3><<<nb, 128, 0, st>>>(w, a.g, a.ph, iB, fb); break;
+        case 4: k_fix_store<T, 4><<<nb, 128, 0, st>>>(w, a.g, a.ph, iB, fb); break;
+        case 5: k_fix_store<T, 5><<<nb, 128, 0, st>>>(w, a.g, a.ph, iB, fb); break;
+        case 6: k_fix_store<T, 6><<<nb, 128, 0, st>>>(w, a.g, a.ph, iB, fb); break;
+        case 8: k_fix_store<T, 8><<<nb, 128, 0, st>>>(w, a.g, a.ph, iB, fb); break;
+      }
+      off += fix_face_elems(a.g, iB, nw);
+    }
+  }
   static void roundtrip(const SweepArgs& a, const T* w, T* out, cudaStream_t st) {
     const long long n = (long long)a.g.nG[0] * a.g.nG[1] * a.g.nG[2];
 #define KC(D, C, M) k_roundtrip<PH, D, C, M><<<grid_for(n, 128), 128, 0, st>>>(a, w, out)
@@ -800,6 +967,14 @@ struct Launch {
   void launch_roundtrip_##SUF(const SweepArgs& s, const PH::T* w,            \
                               PH::T* out, cudaStream_t st) {                 \
     Launch<PH>::roundtrip(s, w, out, st);                                    \
+  }                                                                          \
+  void launch_ghost_faces_##SUF(const SweepArgs& s, PH::T* w, PH::T* fixb,    \
+                                int restore, cudaStream_t st) {              \
+    Launch<PH>::ghost_faces(s, w, fixb, restore, st);                        \
+  }                                                                          \
+  void launch_fix_store_##SUF(const SweepArgs& s, const PH::T* w,            \
+                              PH::T* fixb, cudaStream_t st) {                \
+    Launch<PH>::fix_store(s, w, fixb, st);                                   \
   }
 
 }  // namespace vacgpu

@@ -141,6 +141,7 @@ struct vacgpu_handle {
   size_t elem;
   void* buf[3];      // two state buffers (ping-pong) + predictor output
   void* wold;        // step-start copy for typelimited='previous' when split
+  void* fixb;        // stored ghost values of fixed/fixed1/grad1 faces
   int cur;           // which of buf[0], buf[1] holds the state
   double* dx[3];
   float* dxf[3];
@@ -260,6 +261,22 @@ bool make_tmap(vacgpu_handle* h, void* base, int rows, CUtensorMap* m) {
   return r == CUDA_SUCCESS;
 }
 
+// getboundary's ghost fill of w: composed index maps, or face by face
+// (restore: reuse the stored values of fixed/fixed1/grad1 faces) when the
+// grid has fixed or extrapolating faces.
+void fill_ghosts(vacgpu_handle* h, const SweepArgs& a, void* w, int restore) {
+  if (h->ph.genbc) {
+    if (h->elem == 8)
+      launch_ghost_faces_fp64(a, (double*)w, (double*)h->fixb, restore, h->st);
+    else
+      launch_ghost_faces_mixed(a, (float*)w, (float*)h->fixb, restore, h->st);
+  } else if (h->elem == 8) {
+    launch_ghost_fp64(a, (double*)w, h->st);
+  } else {
+    launch_ghost_mixed(a, (float*)w, h->st);
+  }
+}
+
 SweepArgs make_args(vacgpu_handle* h, int d0, int d1) {
   SweepArgs a;
   a.g = h->g;
@@ -324,10 +341,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
       kend(h);
     }
     kbegin(h, VACGPU_K_GHOST);
-    if (sizeof(T) == 8)
-      launch_ghost_fp64(a, (double*)wout, h->st);
-    else
-      launch_ghost_mixed(a, (float*)wout, h->st);
+    fill_ghosts(h, a, wout, 1);
     kend(h);
   } else if (sizeof(T) == 8) {
     kbegin(h, VACGPU_K_PREDICT);
@@ -335,7 +349,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)w1, h->st);
-    launch_ghost_fp64(a, (double*)w1, h->st);
+    fill_ghosts(h, a, w1, 1);
     kend(h);
     kbegin(h, VACGPU_K_CORRECT);
     launch_correct_fp64(a, (const double*)wc, (const double*)w1,
@@ -343,7 +357,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)wout, h->st);
-    launch_ghost_fp64(a, (double*)wout, h->st);
+    fill_ghosts(h, a, wout, 1);
     kend(h);
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
     kbegin(h, VACGPU_K_SWEEP);
@@ -363,14 +377,14 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fw1, h->st); \
-  launch_ghost_##SUF(a, fw1, h->st);                    \
+  fill_ghosts(h, a, fw1, 1);                            \
   kend(h);                                              \
   kbegin(h, VACGPU_K_CORRECT);                          \
   launch_correct_##SUF(a, fwc, fw1, fb, fo, h->st);     \
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fo, h->st); \
-  launch_ghost_##SUF(a, fo, h->st);                     \
+  fill_ghosts(h, a, fo, 1);                             \
   kend(h);
     switch (h->pmode) {
       case 1: MIXED_SWEEP(mixedf64) break;
@@ -561,8 +575,8 @@ int check_params(const vacgpu_params* p) {
   for (int d = 0; d < p->ndim; d++)
     for (int iw = 0; iw < nw; iw++) {
       int lo = p->typeB[2 * d][iw], hi = p->typeB[2 * d + 1][iw];
-      if (lo < 0 || lo > VACGPU_BC_ASYMM || hi < 0 || hi > VACGPU_BC_ASYMM)
-        return fail("unsupported boundary type (cont/periodic/symm/asymm)");
+      if (lo < 0 || lo > VACGPU_BC_SYMM0 || hi < 0 || hi > VACGPU_BC_SYMM0)
+        return fail("unsupported boundary type");
       if ((lo == VACGPU_BC_PERIODIC) != (hi == VACGPU_BC_PERIODIC))
         return fail("Error in BoundSetup: No periodic pair");
     }
@@ -725,6 +739,18 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   }
   if (e == cudaSuccess)
     e = cudaMalloc(&h->stage, sizeof(double) * g.ncell * h->nw);
+  if (e == cudaSuccess && ph.genbc) {
+    // stored ghost values: per face its two layers over the other
+    // dimensions' ghost box, all variables
+    size_t n = 0;
+    for (int iB = 0; iB < 2 * g.ndim; iB++) {
+      size_t f = 2;
+      for (int d = 0; d < 3; d++)
+        if (d != iB / 2) f *= g.nG[d];
+      n += f * h->nw;
+    }
+    e = cudaMalloc(&h->fixb, n * h->elem);
+  }
   long long nblk = (g.ncell + 255) / 256;
   if (e == cudaSuccess)
     e = cudaMalloc(&h->part, sizeof(double) * nblk * h->nw);
@@ -743,10 +769,12 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
              p->typelimited == VACGPU_LIMITED_ORIGINAL &&
              p->typefull == VACGPU_TVDLF && !p->smallfix && !p->useprimitive;
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
-  // its ghost writes need uniform maps, periodic faces in pairs and n >= 4
+  // its ghost writes need uniform copy maps, periodic faces in pairs and
+  // n >= 4; 'symm0' needs the split kernels' zero face fluxes
   for (int d = 0; d < p->ndim; d++)
     if (ph.gmap[d][0] == GMAP_MIXED || ph.gmap[d][1] == GMAP_MIXED || g.nx[d] < 4 ||
-        (ph.gmap[d][0] == GMAP_PERIODIC) != (ph.gmap[d][1] == GMAP_PERIODIC))
+        (ph.gmap[d][0] == GMAP_PERIODIC) != (ph.gmap[d][1] == GMAP_PERIODIC) ||
+        ph.noflux[d][0] || ph.noflux[d][1])
       h->fused = false;
   if (h->fused && p->ndim == 3 && !getenv("VACGPU_NZC") && g.ncell >= (1LL << 21)) {
     static const int cands[5] = {16, 24, 32, 48, 64};
@@ -889,11 +917,15 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   if (h->elem == 8) {
     k_scatter<double><<<nb, 256, 0, h->st>>>(h->stage, (double*)h->buf[0], g, h->nw);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)h->buf[0], h->st);
-    launch_ghost_fp64(a, (double*)h->buf[0], h->st);
+    fill_ghosts(h, a, h->buf[0], 0);
+    if (h->ph.genbc)
+      launch_fix_store_fp64(a, (const double*)h->buf[0], (double*)h->fixb, h->st);
   } else {
     k_scatter<float><<<nb, 256, 0, h->st>>>(h->stage, (float*)h->buf[0], g, h->nw);
     if (h->p.smallfix) launch_keeppositive_mixed(a, (float*)h->buf[0], h->st);
-    launch_ghost_mixed(a, (float*)h->buf[0], h->st);
+    fill_ghosts(h, a, h->buf[0], 0);
+    if (h->ph.genbc)
+      launch_fix_store_mixed(a, (const float*)h->buf[0], (float*)h->fixb, h->st);
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->st));
@@ -1027,6 +1059,7 @@ void vacgpu_destroy(vacgpu_handle* h) {
   if (h->own_st) cudaStreamSynchronize(h->own_st);
   for (int i = 0; i < 3; i++) cudaFree(h->buf[i]);
   cudaFree(h->wold);
+  cudaFree(h->fixb);
   for (int d = 0; d < 3; d++) {
     cudaFree(h->dx[d]);
     cudaFree(h->dxf[d]);

@@ -62,22 +62,33 @@ struct DevPhys {
   // when variables differ.  asym: bit iw set where variable iw is 'asymm'.
   int gmap[3][2];
   int asym[3][2];
+  // bit iw set: 'symm0' face, zero flux of iw through it (setnoflux)
+  int noflux[3][2];
+  // some face is 'fixed', 'fixed1', 'cont1' or 'grad1': ghost cells are
+  // filled face by face in getboundary's order (k_ghost_face)
+  int genbc;
 };
 
 enum { GMAP_MIXED = -1, GMAP_PERIODIC = 0, GMAP_CONT = 1, GMAP_MIRROR = 2 };
 
-// Fill gmap/asym of ph from its typeB table.
+// Fill gmap/asym/noflux/genbc of ph from its typeB table.
 inline void set_gmaps(DevPhys& ph, int ndim, int nw) {
+  ph.genbc = 0;
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {
       int m = GMAP_PERIODIC;
-      int asy = 0;
+      int asy = 0, nof = 0;
       for (int v = 0; v < nw && d < ndim; v++) {
         int t = ph.typeB[2 * d + s][v];
-        int mv = t == VACGPU_BC_PERIODIC ? GMAP_PERIODIC
-                 : t == VACGPU_BC_CONT   ? GMAP_CONT
-                                         : GMAP_MIRROR;
+        const bool gen = t == VACGPU_BC_FIXED || t == VACGPU_BC_FIXED1 ||
+                         t == VACGPU_BC_CONT1 || t == VACGPU_BC_GRAD1;
+        int mv = gen ? GMAP_MIXED
+                 : t == VACGPU_BC_PERIODIC ? GMAP_PERIODIC
+                 : t == VACGPU_BC_CONT     ? GMAP_CONT
+                                           : GMAP_MIRROR;
+        if (gen) ph.genbc = 1;
         if (t == VACGPU_BC_ASYMM) asy |= 1 << v;
+        if (t == VACGPU_BC_SYMM0) nof |= 1 << v;
         if (v == 0)
           m = mv;
         else if (mv != m)
@@ -85,6 +96,7 @@ inline void set_gmaps(DevPhys& ph, int ndim, int nw) {
       }
       ph.gmap[d][s] = m;
       ph.asym[d][s] = asy;
+      ph.noflux[d][s] = nof;
     }
 }
 
@@ -178,6 +190,10 @@ struct SweepArgs {
                               cudaStream_t st);                              \
   void launch_keeppositive_##SUF(const SweepArgs& s, T* w, cudaStream_t st); \
   void launch_roundtrip_##SUF(const SweepArgs& s, const T* w, T* out,       \
+                              cudaStream_t st);                              \
+  void launch_ghost_faces_##SUF(const SweepArgs& s, T* w, T* fixb,            \
+                                int restore, cudaStream_t st);               \
+  void launch_fix_store_##SUF(const SweepArgs& s, const T* w, T* fixb,        \
                               cudaStream_t st);
 VACGPU_DECLARE_LAUNCHERS(fp64, double)
 VACGPU_DECLARE_LAUNCHERS(mixed, float)

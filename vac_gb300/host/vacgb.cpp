@@ -442,7 +442,8 @@ int main(int argc, char** argv) {
   p.tmaxexact = getb("tmaxexact", false);
   p.dtmin = getd("dtmin", 1e-99);
   // boundlist: typeB(iw,iB) in column order (iw fastest), default 'cont'
-  const char* bcnames[] = {"cont", "periodic", "symm", "asymm"};
+  const char* bcnames[] = {"cont", "periodic", "symm", "asymm", "fixed",
+                           "fixed1", "cont1", "grad1", "symm0"};
   for (auto* a : find_all("typeb")) {
     size_t o = 0;
     if (a->idx.size() == 2) o = (a->idx[1] - 1) * nw + (a->idx[0] - 1);
@@ -453,7 +454,7 @@ int main(int argc, char** argv) {
       if (ib >= 2 * ini.ndim) break;
       std::string t = lower(to_str(a->vals[k]));
       int b = -1;
-      for (int m = 0; m < 4; m++)
+      for (int m = 0; m < 9; m++)
         if (t == bcnames[m]) b = m;
       if (b < 0) die("Error in GetBoundary: boundary type " + t + " is not on this path");
       p.typeB[ib][iw] = b;
