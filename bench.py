@@ -167,6 +167,91 @@ def run_batched(args):
                       "trial_ms": ms}}
 
 
+def _timed_steps(eng, k, stream):
+    """k steps on the engine's stream between CUDA events; seconds."""
+    import torch
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    eng.step(k)
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def run_plain(args):
+    """Config 1: the plain FP64 method, 2-D ideal MHD Orszag-Tang on
+    200^2 periodic cells, minmod, 200 steps (state resident, 2 MB: an L2
+    resident latency case, not a roofline case), with the FP64 oracle port
+    on the host cores timed on the same run."""
+    import torch
+    from vac_gb300 import abi, inistate
+    from vac_gb300.engine import Engine
+    snap = inistate.orszag_tang(200)
+    p = inistate.params_for(snap, limiter="minmod", bc="periodic", precision=abi.PREC_FP64)
+    stream = torch.cuda.Stream()
+    e = Engine(p, snap.x, snap.w)
+    e.set_stream(stream.cuda_stream)
+    e.step(3)
+    e.upload(snap.w)
+    el = _timed_steps(e, 200, stream)
+    e.close()
+    out = {"workload": "2D ideal MHD Orszag-Tang 200^2 periodic, minmod, FP64, 200 steps",
+           "steps": 200, "seconds": el, "ms_per_step": el / 200 * 1e3,
+           "value": 200 * 200 * 200 / el, "unit": UNIT}
+    if args.cpu_steps > 0:
+        os.environ["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
+        from oracle.oracle import Oracle
+        o = Oracle(p, snap.x, snap.w)
+        t0 = time.perf_counter()
+        o.step(200)
+        ct = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 200 * 200 * 200 / ct, "unit": UNIT,
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": "the same 200 steps, FP64 oracle port (OpenMP)"}
+    return out
+
+
+def run_blast(args):
+    """Config 5: 3-D ideal MHD blast on 512^3 cells, outflow ('cont'),
+    woodward, B=(1,1,0)/sqrt2, p from 10 to 0.1 across r=0.1: mixed
+    precision timed over --blast-steps steps (the fused sweep), FP64 over 2
+    steps, and the mixed-vs-FP64 relative L1 after those 2 steps from the
+    same initial state."""
+    import torch
+    from vac_gb300 import abi, inistate
+    from vac_gb300.engine import Engine
+    n = args.blast_side
+    snap = inistate.blast_3d(n)
+    ncell = n ** 3
+    stream = torch.cuda.Stream()
+    out = {"workload": "3D ideal MHD blast %d^3, cont, woodward, mixed %d steps timed, "
+                       "FP64 2 steps timed" % (n, args.blast_steps)}
+    pm = inistate.params_for(snap, limiter="woodward", bc="cont", precision=abi.PREC_MIXED)
+    em = Engine(pm, snap.x, snap.w)
+    em.set_stream(stream.cuda_stream)
+    em.step(2)
+    wm2 = em.state()
+    em.step(3)
+    el = _timed_steps(em, args.blast_steps, stream)
+    em.close()
+    out["mixed"] = {"steps": args.blast_steps, "ms_per_step": el / args.blast_steps * 1e3,
+                    "value": ncell * args.blast_steps / el, "unit": UNIT}
+    p64 = inistate.params_for(snap, limiter="woodward", bc="cont", precision=abi.PREC_FP64)
+    e64 = Engine(p64, snap.x, snap.w)
+    e64.set_stream(stream.cuda_stream)
+    el64 = _timed_steps(e64, 2, stream)
+    w64 = e64.state()
+    e64.close()
+    out["fp64"] = {"steps": 2, "ms_per_step": el64 / 2 * 1e3, "value": ncell * 2 / el64,
+                   "unit": UNIT}
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["rel_l1_mixed_vs_fp64_after_2_steps"] = [
+        float(np.abs(wm2[i] - w64[i]).sum() / max(np.abs(w64[i]).sum(), 1e-300))
+        for i in range(w64.shape[0])]
+    return out
+
+
 def run_served(args, capacity):
     """Config 4: a Poisson stream of 2-D (128^2..2048^2) and 3-D (64^3..256^3)
     random-mode MHD solves, 20..500 steps each, mixed precision, admitted
@@ -257,6 +342,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--served", type=int, default=12, help="requests in the served stream (0: skip)")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip config 1")
+    ap.add_argument("--blast-side", type=int, default=512,
+                    help="config 5 cells per side (0: skip)")
+    ap.add_argument("--blast-steps", type=int, default=20)
     ap.add_argument("--side", type=int, default=N,
                     help="cells per side of the cube (smaller cases for profiling)")
     args = ap.parse_args()
@@ -370,7 +459,11 @@ def main():
                 "rel_l1_mixed_vs_fp64": rel_l1, "rel_linf_mixed_vs_fp64": linf}
         e64.close()
 
-    batched = served = None
+    batched = served = plain = blast = None
+    if rank == 0 and not args.no_plain:
+        plain = run_plain(args)
+    if rank == 0 and args.blast_side > 0:
+        blast = run_blast(args)
     if rank == 0 and not args.no_batched:
         batched = run_batched(args)
     if rank == 0 and args.served > 0:
@@ -403,7 +496,8 @@ def main():
                              "traffic": traffic, "avg_launch_ms": avg_s * 1e3,
                              "alg_bytes_per_launch": alg_bytes,
                              "kernel_share": shares},
-                "fp64": fp64, "batched": batched, "served": served,
+                "fp64": fp64, "plain_fp64_config1": plain, "blast_config5": blast,
+                "batched": batched, "served": served,
                 "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     eng.close()
