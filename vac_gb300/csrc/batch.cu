@@ -152,7 +152,7 @@ template <int NDIM, bool MHD>
 void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
                     int order) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
-  const int smem = fused_smem_floats(NW, D) * 4;
+  const int smem = fused_smem_floats(NW, fused_kind(NDIM, D)) * 4;
   const int n = b->nitems[D];
   const BItem* items = b->d_items[D][order];
   if (ctas <= 0 || ctas > n) ctas = n;
@@ -273,13 +273,16 @@ int prepare(vacgpu_batch* b) {
   // direction; order 0 round-robin over grids (neighbouring CTAs work on
   // different grids), order 1 grid-major, largest grid first
   for (int D = 0; D < b->p0.ndim; D++) {
-    const int tx = D == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
-    const int ty = D == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
+    // tiles over x and the row axis, z chunks along the marching axis
+    const int kind = fused_kind(b->p0.ndim, D);
+    const int tx = kind == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
+    const int ty = kind == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
+    const int ar = kind == 2 && D == 1 ? 2 : 1, am = kind == 2 ? D : 2;
     std::vector<std::vector<BItem>> per(n);
     for (int i = 0; i < n; i++) {
       const DevGrid& g = ins[i].fa.g;
-      const int nbx = (g.nx[0] + tx - 1) / tx, nby = (g.nx[1] + ty - 1) / ty;
-      const int nbz = g.ndim == 3 ? (g.nx[2] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
+      const int nbx = (g.nx[0] + tx - 1) / tx, nby = (g.nx[ar] + ty - 1) / ty;
+      const int nbz = g.ndim == 3 ? (g.nx[am] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
       for (int z = 0; z < nbz; z++)
         for (int y = 0; y < nby; y++)
           for (int x = 0; x < nbx; x++) per[i].push_back({i, x, y, z});

@@ -6,13 +6,13 @@
 
 namespace vacgpu {
 
-int fused_smem_bytes(int nw, int d) { return fused_smem_floats(nw, d) * 4; }
+int fused_smem_bytes(int nw, int k) { return fused_smem_floats(nw, k) * 4; }
 
 template <int NDIM, int D, bool MHD, int LIMC, int PMF>
 static void launch_pmf(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
                        cudaStream_t st) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
-  const int smem = fused_smem_floats(NW, D) * 4;
+  const int smem = fused_smem_floats(NW, fused_kind(NDIM, D)) * 4;
   auto k = k_sweep_fused<NDIM, D, MHD, PREC_FF, LIMC, PMF>;
   static bool attr = false;
   if (!attr) {
@@ -83,10 +83,14 @@ bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
       if (s.ph.typeB[2 * d][v] == VACGPU_BC_ASYMM) a.asymm_lo[d] |= 1 << v;
       if (s.ph.typeB[2 * d + 1][v] == VACGPU_BC_ASYMM) a.asymm_hi[d] |= 1 << v;
     }
-  const int tx = s.d0 == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
-  const int ty = s.d0 == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
-  dim3 grid((s.g.nx[0] + tx - 1) / tx, (s.g.nx[1] + ty - 1) / ty,
-            nd == 3 ? (s.g.nx[2] + nzc - 1) / nzc : 1);
+  // tiles over x and the row axis, z chunks along the marching axis
+  const int kind = fused_kind(nd, s.d0);
+  const int tx = kind == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
+  const int ty = kind == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
+  const int ar = kind == 2 && s.d0 == 1 ? 2 : 1;
+  const int am = kind == 2 ? s.d0 : 2;
+  dim3 grid((s.g.nx[0] + tx - 1) / tx, (s.g.nx[ar] + ty - 1) / ty,
+            nd == 3 ? (s.g.nx[am] + nzc - 1) / nzc : 1);
   a.zchunks = grid.z;
   const CUtensorMap* map = (const CUtensorMap*)tmap;
   const int D = s.d0;

@@ -12,11 +12,14 @@
 // per sweep is one read and one write of the state plus halo re-reads that
 // mostly hit L2.
 //
-// The tile shape depends on the sweep direction D so that each phase is one
-// work item per thread: the predictor is needed in full on (TX+2) x TY cells
-// for D=0, TX x (TY+2) for D=1 and TX x TY for D=2 -- 256 cells each with
-// 30x8, 32x6 and 32x8 tiles -- and the face fluxes along D number at most
-// 256.  The remaining halo cells feed only the div B of the Powell source,
+// Geometry kinds: K=0 (x sweep) and K=1 (y sweep of 2-D grids) keep the
+// sweep direction inside the tile plane and march along z; K=2 marches along
+// the sweep direction itself (z sweep, and y sweep of 3-D grids with tile
+// rows along z), so its faces are evaluated in registers plane by plane.
+// The tile shape depends on the kind so that each phase is one work item
+// per thread: the predictor is needed in full on (TX+2) x TY cells for K=0,
+// TX x (TY+2) for K=1 and TX x TY for K=2 -- 256 cells each with 30x8, 32x6
+// and 32x8 tiles -- and the in-plane faces number at most 256.  The remaining halo cells feed only the div B of the Powell source,
 // so there only the transverse B component is predicted.  With
 // typelimited='original' the corrector limits the same state w that the
 // predictor limits (src/vactvdlf.t:150-157), so the predictor's limited
@@ -39,36 +42,41 @@ constexpr int FT_NT = 256;  // threads per CTA
 constexpr int FB_X = 40;    // TMA box width
 constexpr int FWRING = 4;   // state planes resident (j-1, j, j+1, j+2)
 
-template <int D>
+// geometry kind of the sweep in direction d of an ndim-D grid
+__host__ __device__ constexpr int fused_kind(int ndim, int d) {
+  return ndim == 3 && d >= 1 ? 2 : d;
+}
+
+template <int K>
 struct TileCfg {
-  static constexpr int TX = D == 0 ? 30 : 32;   // output tile
-  static constexpr int TY = D == 1 ? 6 : 8;
+  static constexpr int TX = K == 0 ? 30 : 32;   // output tile
+  static constexpr int TY = K == 1 ? 6 : 8;
   static constexpr int RX = TX + 2, RY = TY + 2;  // predictor region
   static constexpr int RN = RX * RY;
   static constexpr int BY = TY + 4;              // TMA box rows
   static constexpr int BPL = FB_X * BY;          // floats / variable / plane
-  static constexpr int NF = D == 0 ? (TX + 1) * TY : D == 1 ? TX * (TY + 1) : 0;
+  static constexpr int NF = K == 0 ? (TX + 1) * TY : K == 1 ? TX * (TY + 1) : 0;
   static constexpr int NOUT = TX * TY;
   // halo cells where only a transverse B component is predicted
-  static constexpr int NB = D == 0 ? 2 * TX : D == 1 ? 2 * TY : 2 * TX + 2 * TY;
+  static constexpr int NB = K == 0 ? 2 * TX : K == 1 ? 2 * TY : 2 * TX + 2 * TY;
 };
 
 // floats of one state-plane slot (multiple of 32: 128-byte aligned slots)
-__host__ __device__ constexpr int fused_slot_floats(int nw, int D) {
-  return (nw * FB_X * (D == 1 ? TileCfg<1>::BY : TileCfg<0>::BY) + 31) / 32 * 32;
+__host__ __device__ constexpr int fused_slot_floats(int nw, int K) {
+  return (nw * FB_X * (K == 1 ? TileCfg<1>::BY : TileCfg<0>::BY) + 31) / 32 * 32;
 }
 
-// shared-memory floats of the sweep in direction D for nw variables:
-// state ring, two predictor planes, two face-flux planes, slopes
-__host__ __device__ constexpr int fused_smem_floats(int nw, int D) {
-  return FWRING * fused_slot_floats(nw, D) +
-         2 * nw * (D == 0 ? TileCfg<0>::RN : D == 1 ? TileCfg<1>::RN : TileCfg<2>::RN) +
-         (D == 2 ? 0 : 2 * nw * (D == 0 ? TileCfg<0>::NF : TileCfg<1>::NF) + nw * 256);
+// shared-memory floats of a sweep of kind K for nw variables: state ring,
+// two predictor planes, two face-flux planes, slopes
+__host__ __device__ constexpr int fused_smem_floats(int nw, int K) {
+  return FWRING * fused_slot_floats(nw, K) +
+         2 * nw * (K == 0 ? TileCfg<0>::RN : K == 1 ? TileCfg<1>::RN : TileCfg<2>::RN) +
+         (K == 2 ? 0 : 2 * nw * (K == 0 ? TileCfg<0>::NF : TileCfg<1>::NF) + nw * 256);
 }
 
-// rows of the TMA box of direction D (one tensor map per box shape)
-__host__ __device__ constexpr int fused_box_rows(int D) {
-  return D == 1 ? TileCfg<1>::BY : TileCfg<0>::BY;
+// rows of the TMA box of kind K (one tensor map per box shape)
+__host__ __device__ constexpr int fused_box_rows(int K) {
+  return K == 1 ? TileCfg<1>::BY : TileCfg<0>::BY;
 }
 
 static_assert(fused_box_rows(0) == FUSED_BOX_ROWS[0] &&
@@ -163,11 +171,14 @@ enum { LIMC_RUNTIME = 0, LIMC_MINMOD = 1, LIMC_WOODWARD = 2 };
 // PM: pressure recovery of the wave speeds; PMF: of the fluxes.
 template <int NDIM, int D, bool MHD, int PM, int LIMC, int PMF = PM>
 struct Fused {
-  typedef TileCfg<D> C;
+  static constexpr int K = fused_kind(NDIM, D);  // geometry kind
+  static constexpr int AM = K == 2 ? D : 2;       // marching axis (3-D)
+  static constexpr int AR = K == 2 && D == 1 ? 2 : 1;  // tile-row axis
+  typedef TileCfg<K> C;
   static constexpr int NDIR = NDIM;
   static constexpr int NW = MHD ? 2 + 2 * NDIR : 2 + NDIR;
   static constexpr int E = NDIR + 1;
-  static constexpr int SLOT = fused_slot_floats(NW, D);
+  static constexpr int SLOT = fused_slot_floats(NW, K);
   // Pressure recovery: PM in the wave speeds, PMF in the four flux
   // evaluations per cell (the same double-float recovery by default; FP32
   // in the fluxes is the opt-in variant -- p enters a flux only through
@@ -214,13 +225,13 @@ struct Fused {
                                                  const float* pp, int sy,
                                                  int sx, const int* gc) {
     const int o = sy * FB_X + sx;
-    const int bx = (E + 1) * C::BPL, by = (E + 2) * C::BPL;
+    const int bx = (E + 1) * C::BPL, by = (E + 1 + AR) * C::BPL;
     float divb = 0.5f * (p0[bx + o + 1] - p0[bx + o - 1]) * a.idxf[0][gc[0]];
     if (NDIM > 1)
-      divb += 0.5f * (p0[by + o + FB_X] - p0[by + o - FB_X]) * a.idxf[1][gc[1]];
+      divb += 0.5f * (p0[by + o + FB_X] - p0[by + o - FB_X]) * a.idxf[AR][gc[AR]];
     if (NDIM > 2) {
-      const int bz = (E + 3) * C::BPL;
-      divb += 0.5f * (pp[bz + o] - pm[bz + o]) * a.idxf[2][gc[2]];
+      const int bz = (E + 1 + AM) * C::BPL;
+      divb += 0.5f * (pp[bz + o] - pm[bz + o]) * a.idxf[AM][gc[AM]];
     }
     return divb;
   }
@@ -267,10 +278,10 @@ struct Fused {
     for (int v = 0; v < NW; v++) {
       float um, up;
       u[v] = W(p0, v, sy, sx);
-      if (D == 0) {
+      if (K == 0) {
         um = W(p0, v, sy, sx - 1);
         up = W(p0, v, sy, sx + 1);
-      } else if (D == 1) {
+      } else if (K == 1) {
         um = W(p0, v, sy - 1, sx);
         up = W(p0, v, sy + 1, sx);
       } else {
@@ -308,10 +319,10 @@ struct Fused {
       const int v = iv[i];
       const float c = W(p0, v, sy, sx);
       float m, p;
-      if (D == 0) {
+      if (K == 0) {
         m = W(p0, v, sy, sx - 1);
         p = W(p0, v, sy, sx + 1);
-      } else if (D == 1) {
+      } else if (K == 1) {
         m = W(p0, v, sy - 1, sx);
         p = W(p0, v, sy + 1, sx);
       } else {
@@ -360,8 +371,9 @@ struct Fused {
   }
 
   // getboundary on w1: region cells in the first ghost layer of a
-  // non-periodic x/y face take the adjacent mesh value (when xy is set);
-  // at a z face the whole plane does (-1 from 0, nz from nz-1).
+  // non-periodic x or tile-row face take the adjacent mesh value (when xy
+  // is set); at a face of the marching axis the whole plane does (-1 from
+  // 0, n from n-1).
   static __device__ void fix_w1_ghosts(const FusedArgs& a, float* sm, int j,
                                        int x0, int y0, bool xy, bool z) {
     const DevGrid& g = a.g;
@@ -371,12 +383,12 @@ struct Fused {
         const int rx = c % C::RX, ry = c / C::RX;
         const int ix = x0 + rx - 1, iy = y0 + ry - 1;
         int d = -1, src = c, lo = 0;
-        if ((ix == -1 || ix == g.nx[0]) && (NDIM < 2 || (iy >= 0 && iy < g.nx[1]))) {
+        if ((ix == -1 || ix == g.nx[0]) && (NDIM < 2 || (iy >= 0 && iy < g.nx[AR]))) {
           d = 0;
           lo = ix == -1;
           src = c + (lo ? 1 : -1);
-        } else if (NDIM >= 2 && (iy == -1 || iy == g.nx[1]) && ix >= 0 && ix < g.nx[0]) {
-          d = 1;
+        } else if (NDIM >= 2 && (iy == -1 || iy == g.nx[AR]) && ix >= 0 && ix < g.nx[0]) {
+          d = AR;
           lo = iy == -1;
           src = c + (lo ? C::RX : -C::RX);
         }
@@ -392,14 +404,14 @@ struct Fused {
     }
     if (NDIM == 3 && z) {
       const int dst = j == 0 ? -1 : j, srcp = j == 0 ? 0 : j - 1;
-      const int asy = j == 0 ? a.asymm_lo[2] : a.asymm_hi[2];
-      if (xy) __syncthreads();  // the x/y fix of the source plane is complete
+      const int asy = j == 0 ? a.asymm_lo[AM] : a.asymm_hi[AM];
+      if (xy) __syncthreads();  // the in-plane fix of the source plane is complete
       float* dp = w1slot(sm, dst);
       const float* sp = w1slot(sm, srcp);
       for (int c = threadIdx.x; c < C::RN; c += FT_NT) {
 #pragma unroll
         for (int v = 0; v < NW; v++) {
-          if ((a.periodic_mask[2] >> v) & 1) continue;
+          if ((a.periodic_mask[AM] >> v) & 1) continue;
           const float s = sp[v * C::RN + c];
           dp[v * C::RN + c] = ((asy >> v) & 1) ? -s : s;
         }
@@ -417,7 +429,7 @@ struct Fused {
     const int tid = threadIdx.x;
     const DevGrid& g = a.g;
     int rx, ry, f;  // left / lower cell of the face (region), face index
-    if (D == 0) {
+    if (K == 0) {
       rx = tid % 32;
       ry = tid / 32 + 1;
       if (rx > C::TX) return;
@@ -429,14 +441,14 @@ struct Fused {
       f = tid;
     }
     const int ix = x0 + rx - 1, iy = y0 + ry - 1;
-    const bool valid = D == 0 ? (ix >= -1 && ix < g.nx[0] && (NDIM < 2 || iy < g.nx[1]))
-                              : (iy >= -1 && iy < g.nx[1] && ix < g.nx[0]);
+    const bool valid = K == 0 ? (ix >= -1 && ix < g.nx[0] && (NDIM < 2 || iy < g.nx[AR]))
+                              : (iy >= -1 && iy < g.nx[AR] && ix < g.nx[0]);
     if (!valid) return;
     const float* w1o = w1slot(sm, jo);
     const float* lb = ldbuf(sm);
-    const int fr = D == 0 ? tid + 1 : tid + 32;
+    const int fr = K == 0 ? tid + 1 : tid + 32;
     const int rl = ry * C::RX + rx;
-    const int rr = D == 0 ? rl + 1 : rl + C::RX;
+    const int rr = K == 0 ? rl + 1 : rl + C::RX;
     float wl[NW], wr[NW], ldl[NW], ldr[NW], F[NW];
 #pragma unroll
     for (int v = 0; v < NW; v++) {
@@ -450,15 +462,24 @@ struct Fused {
 #pragma unroll
     for (int v = 0; v < NW; v++) fb[v * C::NF + f] = F[v];
     if (a.cfl) {
-      const int gi = (D == 0 ? ix : iy) + 2;
+      const int gi = (K == 0 ? ix : iy) + 2;
       const float q = cm * 2.0f / (a.dxf[D][gi] + a.dxf[D][gi + 1]);
       qmax = (q > qmax || q != q) ? q : qmax;  // a NaN sticks
     }
   }
 
+  // mesh coordinates (x, tile row, plane) -> ghost-range indices (x, y, z)
+  static __device__ __forceinline__ void gcoords(const DevGrid& g, int ix,
+                                                 int iy, int jp, int* gc) {
+    gc[0] = ix + 2;
+    gc[AR] = iy + g.gh[AR];
+    if (NDIM == 3) gc[AM] = jp + g.gh[AM];
+    else gc[2] = 0;
+  }
+
   // Corrected state of the output cell (lx, ly) of plane jo:
   // w - qdt/dx (F+ - F-) + sources(w1), written to HBM.  bpl: the state
-  // plane jo; bzm: b_z of w1 at plane jo-1 (3-D).
+  // plane jo; bzm: the marching-axis B component of w1 at plane jo-1 (3-D).
   static __device__ __forceinline__ void update(const FusedArgs& a,
                                                 float* sm, const float* bpl,
                                                 int jo, int ix, int iy,
@@ -469,7 +490,8 @@ struct Fused {
     const DevGrid& g = a.g;
     const float* c0 = w1slot(sm, jo);
     const int r = (ly + 1) * C::RX + lx + 1;
-    const int gc[3] = {ix + 2, iy + g.gh[1], jo + g.gh[2]};
+    int gc[3];
+    gcoords(g, ix, iy, jo, gc);
     float acc[NW], wc[NW];
 #pragma unroll
     for (int v = 0; v < NW; v++) {
@@ -482,13 +504,13 @@ struct Fused {
     if (a.ph.sourceunsplit) {
       float qdivb = 0.0f;
       if (MHD && a.ph.divbfix) {
-        const int bxo = (E + 1) * C::RN + r, byo = (E + 2) * C::RN + r;
+        const int bxo = (E + 1) * C::RN + r, byo = (E + 1 + AR) * C::RN + r;
         float divb = 0.5f * (c0[bxo + 1] - c0[bxo - 1]) * a.idxf[0][gc[0]];
         if (NDIM > 1)
-          divb += 0.5f * (c0[byo + C::RX] - c0[byo - C::RX]) * a.idxf[1][gc[1]];
+          divb += 0.5f * (c0[byo + C::RX] - c0[byo - C::RX]) * a.idxf[AR][gc[AR]];
         if (NDIM > 2) {
-          const float bzp = w1slot(sm, jo + 1)[(E + 3) * C::RN + r];
-          divb += 0.5f * (bzp - bzm) * a.idxf[2][gc[2]];
+          const float bzp = w1slot(sm, jo + 1)[(E + 1 + AM) * C::RN + r];
+          divb += 0.5f * (bzp - bzm) * a.idxf[AM][gc[AM]];
         }
         qdivb = qs * divb;
       }
@@ -614,9 +636,10 @@ struct Fused {
     __shared__ float shq[FT_NT / 32];
     const int tid = threadIdx.x;
     const DevGrid& g = a.g;
+    // x0: first column; y0: first tile row (axis AR); planes along AM
     const int x0 = bx * C::TX, y0 = by * C::TY;
     const int z0 = NDIM == 3 ? bz * a.nzc : 0;
-    const int z1 = NDIM == 3 ? min(z0 + a.nzc, g.nx[2]) : 1;  // exclusive
+    const int z1 = NDIM == 3 ? min(z0 + a.nzc, g.nx[AM]) : 1;  // exclusive
     const double dtd = ctrl->dt;
     const float qdt = (float)dtd;               // corrector
     const float qdt2 = (float)(dtd / 2);        // predictor
@@ -631,13 +654,13 @@ struct Fused {
     const int sh = cstart - colx;
     const unsigned plane_bytes = NW * C::BPL * 4;
     const bool need_bz = MHD && a.ph.divbfix && a.ph.sourceunsplit;
-    // ghost fix of w1 needed: a non-periodic x/y face inside the region,
-    // or (per plane) a non-periodic z face
+    // ghost fix of w1 needed: a non-periodic x or row face inside the
+    // region, or (per plane) a non-periodic face of the marching axis
     const int all = (1 << NW) - 1;
     const bool fix_xy =
         (a.periodic_mask[0] != all && (x0 == 0 || x0 + C::TX >= g.nx[0])) ||
-        (NDIM >= 2 && a.periodic_mask[1] != all && (y0 == 0 || y0 + C::TY >= g.nx[1]));
-    const bool fix_zb = NDIM == 3 && a.periodic_mask[2] != all;
+        (NDIM >= 2 && a.periodic_mask[AR] != all && (y0 == 0 || y0 + C::TY >= g.nx[AR]));
+    const bool fix_zb = NDIM == 3 && a.periodic_mask[AM] != all;
 
     const int pbase = NDIM == 3 ? z0 - 2 : 0;
     auto slot = [&](int p) -> float* { return sm + ((p - pbase) % FWRING) * SLOT; };
@@ -645,7 +668,7 @@ struct Fused {
       const int q = p - pbase;
       fence_proxy_async();
       mbar_expect_tx(&bars[q % FWRING], plane_bytes);
-      tma_load_plane(map, slot(p), &bars[q % FWRING], colx, y0, p + g.gh[2]);
+      tma_load_plane(map, slot(p), &bars[q % FWRING], colx, y0, p + g.gh[AM]);
     };
     auto wait_plane = [&](int p) -> bool {
       const int q = p - pbase;
@@ -653,13 +676,13 @@ struct Fused {
     };
 
     // this thread's full-predictor cell (region coordinates)
-    const int frx = D == 0 ? tid % 32 : tid % 32 + 1;
-    const int fry = D == 1 ? tid / 32 : tid / 32 + 1;
+    const int frx = K == 0 ? tid % 32 : tid % 32 + 1;
+    const int fry = K == 1 ? tid / 32 : tid / 32 + 1;
     // this thread's output cell: warp ly, lane lx
     const int lx = tid % 32, ly = tid / 32;
     const bool has_out = lx < C::TX && ly < C::TY;
     const int oix = x0 + lx, oiy = y0 + ly;
-    const bool out_ok = has_out && oix < g.nx[0] && (NDIM < 2 || oiy < g.nx[1]);
+    const bool out_ok = has_out && oix < g.nx[0] && (NDIM < 2 || oiy < g.nx[AR]);
 
     float qmax = 0.0f;  // CFL: max cmax*2/(dx_i+dx_i+1) over this thread's faces
     const int pfirst = NDIM == 3 ? z0 - 1 : 0;
@@ -673,21 +696,21 @@ struct Fused {
         issue(0);
       }
     }
-    float Lprev[NW], Fprev[NW];  // z sweep: carried along z
+    float Lprev[NW], Fprev[NW];  // marching sweeps: carried along the march
 #pragma unroll
     for (int v = 0; v < NW; v++) Lprev[v] = Fprev[v] = 0.0f;
 
     for (int j = pfirst; j <= plast; j++) {
       const int jo = NDIM == 3 ? j - 1 : 0;  // plane corrected this iteration
       const bool out_plane = NDIM == 3 ? (jo >= z0 && jo < z1) : true;
-      // x/y sweeps: planes outside the chunk feed only b_z of div B
-      const bool edge = NDIM == 3 && D < 2 && (j == z0 - 1 || j == z1);
+      // in-plane sweeps: planes outside the chunk feed only b_z of div B
+      const bool edge = NDIM == 3 && K < 2 && (j == z0 - 1 || j == z1);
 
-      // b_z of w1(j-2): its slot takes the predictor of plane j
+      // marching-axis B of w1(j-2): its slot takes the predictor of plane j
       float bzm = 0.0f;
       if (NDIM == 3 && need_bz && out_plane && has_out)
-        bzm = w1slot(sm, j - 2)[(E + 3) * C::RN + (ly + 1) * C::RX + lx + 1];
-      if (NDIM == 3 && D < 2 && out_plane)
+        bzm = w1slot(sm, j - 2)[(E + 1 + AM) * C::RN + (ly + 1) * C::RX + lx + 1];
+      if (NDIM == 3 && K < 2 && out_plane)
         in_plane_faces(a, sm, jo, x0, y0, smallp, qmax);
 
       bool ok = true;
@@ -711,19 +734,21 @@ struct Fused {
 #pragma unroll
       for (int v = 0; v < NW; v++) Lcur[v] = 0.0f;
       if (edge) {
-        if (need_bz && has_out && oix <= g.nx[0] && oiy <= g.nx[1]) {
-          const int gc[3] = {oix + 2, oiy + g.gh[1], j + g.gh[2]};
-          w1slot(sm, j)[(E + 3) * C::RN + (ly + 1) * C::RX + lx + 1] =
-              predict_b(a, pm, p0, pp, ly + 2, lx + 4 + sh, gc, qdt2, qs1, 2);
+        if (need_bz && has_out && oix <= g.nx[0] && oiy <= g.nx[AR]) {
+          int gc[3];
+          gcoords(g, oix, oiy, j, gc);
+          w1slot(sm, j)[(E + 1 + AM) * C::RN + (ly + 1) * C::RX + lx + 1] =
+              predict_b(a, pm, p0, pp, ly + 2, lx + 4 + sh, gc, qdt2, qs1, AM);
         }
       } else {
         const int ix = x0 + frx - 1, iy = y0 + fry - 1;
         const bool need = ix >= -1 && ix <= g.nx[0] &&
-                          (NDIM < 2 || (iy >= -1 && iy <= g.nx[1] &&
+                          (NDIM < 2 || (iy >= -1 && iy <= g.nx[AR] &&
                                         !((ix == -1 || ix == g.nx[0]) &&
-                                          (iy == -1 || iy == g.nx[1]))));
+                                          (iy == -1 || iy == g.nx[AR]))));
         if (need) {
-          const int gc[3] = {ix + 2, iy + g.gh[1], j + g.gh[2]};
+          int gc[3];
+          gcoords(g, ix, iy, j, gc);
           float out[NW];
           predict_cell(a, pm, p0, pp, fry + 1, frx + 3 + sh, gc, qdt2, qs1,
                        smallp, out, Lcur);
@@ -731,46 +756,47 @@ struct Fused {
           const int rc = fry * C::RX + frx;
 #pragma unroll
           for (int v = 0; v < NW; v++) w1j[v * C::RN + rc] = out[v];
-          if (D < 2) {
+          if (K < 2) {
             float* lb = ldbuf(sm);
 #pragma unroll
             for (int v = 0; v < NW; v++) lb[v * 256 + tid] = Lcur[v];
           }
         }
-        if (need_bz && tid < C::NB + (D == 1 ? 0 : 64 - 2 * C::TX)) {
-          // transverse B of the halo cells that only div B reads: b_y on
-          // the rows above and below (one warp each), b_x on the columns
-          // left and right
+        if (need_bz && tid < C::NB + (K == 1 ? 0 : 64 - 2 * C::TX)) {
+          // transverse B of the halo cells that only div B reads: the
+          // row-axis component on the rows above and below (one warp each),
+          // b_x on the columns left and right
           int rx, ry, k;
           bool on = true;
-          if (D != 1 && tid < 64) {
+          if (K != 1 && tid < 64) {
             rx = tid % 32 + 1;
             ry = tid < 32 ? 0 : C::RY - 1;
-            k = 1;
+            k = AR;
             on = rx <= C::TX;
           } else {
-            const int hh = D == 1 ? tid : tid - 64;
+            const int hh = K == 1 ? tid : tid - 64;
             rx = hh < C::TY ? 0 : C::RX - 1;
             ry = hh % C::TY + 1;
             k = 0;
           }
           const int bix = x0 + rx - 1, biy = y0 + ry - 1;
-          if (on && bix <= g.nx[0] && (NDIM < 2 || biy <= g.nx[1])) {
-            const int gc[3] = {bix + 2, biy + g.gh[1], j + g.gh[2]};
+          if (on && bix <= g.nx[0] && (NDIM < 2 || biy <= g.nx[AR])) {
+            int gc[3];
+            gcoords(g, bix, biy, j, gc);
             w1slot(sm, j)[(E + 1 + k) * C::RN + ry * C::RX + rx] =
                 predict_b(a, pm, p0, pp, ry + 1, rx + 3 + sh, gc, qdt2, qs1, k);
           }
         }
       }
       __syncthreads();  // barrier B
-      const bool fz = fix_zb && (j == 0 || j == g.nx[2]);
+      const bool fz = fix_zb && (j == 0 || j == g.nx[AM]);
       if (fix_xy || fz) {
         fix_w1_ghosts(a, sm, j, x0, y0, fix_xy, fz);
         __syncthreads();
       }
 
-      if (D == 2) {
-        // the z face between planes j-1 and j of this column
+      if (K == 2) {
+        // the face between planes j-1 and j of this column
         float Fnew[NW];
 #pragma unroll
         for (int v = 0; v < NW; v++) Fnew[v] = 0.0f;
@@ -787,7 +813,7 @@ struct Fused {
           const float cm = face(a, wl, wr, Lprev, Lcur, smallp, Fnew);
           if (a.cfl && out_ok) {
             const int gz = j + 1;  // ghost-range index of plane j-1
-            const float q = cm * 2.0f / (a.dxf[2][gz] + a.dxf[2][gz + 1]);
+            const float q = cm * 2.0f / (a.dxf[D][gz] + a.dxf[D][gz + 1]);
             qmax = (q > qmax || q != q) ? q : qmax;
           }
         }
@@ -806,8 +832,8 @@ struct Fused {
         if (out_plane && out_ok) {
           const float* fb = fbuf(sm, jo);
           float Fm[NW], Fp[NW];
-          const int fm = D == 0 ? ly * (C::TX + 1) + lx : ly * C::TX + lx;
-          const int fp = D == 0 ? fm + 1 : fm + C::TX;
+          const int fm = K == 0 ? ly * (C::TX + 1) + lx : ly * C::TX + lx;
+          const int fp = K == 0 ? fm + 1 : fm + C::TX;
 #pragma unroll
           for (int v = 0; v < NW; v++) {
             Fm[v] = fb[v * C::NF + fm];

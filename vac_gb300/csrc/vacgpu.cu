@@ -176,7 +176,7 @@ struct vacgpu_handle {
   long long glaunch[2][2][VACGPU_K_NCLASS];  // kernels per replay, by class
   bool warmed;
   bool fused;
-  CUtensorMap tmap[2][2];  // [state buffer][box: x/z sweeps, y sweep]
+  CUtensorMap tmap[2][2];  // [state buffer][x/z sweeps, y sweep]
   float* idxf[3];
   int nzc;
   // z-chunk tuning of the fused 3-D sweep (results do not depend on the
@@ -243,8 +243,10 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 4-D map over one FP32 state buffer: (column, gy, gz, variable), box
-// {40, rows, 1, nw} = one plane of a tile with its 2-cell halo.
-bool make_tmap(vacgpu_handle* h, void* base, int rows, CUtensorMap* m) {
+// {40, rows, 1, nw} = one plane of a tile with its 2-cell halo.  With yz
+// the two middle axes swap, (column, gz, gy, variable): the 3-D y sweep's
+// planes are x-z slabs at fixed gy.
+bool make_tmap(vacgpu_handle* h, void* base, int rows, bool yz, CUtensorMap* m) {
   auto fn = encode_fn();
   if (!fn) return false;
   const DevGrid& g = h->g;
@@ -252,6 +254,12 @@ bool make_tmap(vacgpu_handle* h, void* base, int rows, CUtensorMap* m) {
                         (cuuint64_t)g.nG[2], (cuuint64_t)h->nw};
   cuuint64_t strides[3] = {(cuuint64_t)g.P * 4, (cuuint64_t)g.plane * 4,
                            (cuuint64_t)g.vs * 4};
+  if (yz) {
+    dims[1] = (cuuint64_t)g.nG[2];
+    dims[2] = (cuuint64_t)g.nG[1];
+    strides[0] = (cuuint64_t)g.plane * 4;
+    strides[1] = (cuuint64_t)g.P * 4;
+  }
   cuuint32_t box[4] = {40, (cuuint32_t)rows, 1, (cuuint32_t)h->nw};
   cuuint32_t es[4] = {1, 1, 1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides,
@@ -786,7 +794,8 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     bool ok = true;
     for (int i = 0; i < 2 && ok; i++)
       for (int k = 0; k < 2 && ok; k++)
-        ok = make_tmap(h, h->buf[i], FUSED_BOX_ROWS[k], &h->tmap[i][k]);
+        ok = make_tmap(h, h->buf[i], FUSED_BOX_ROWS[p->ndim == 3 ? 0 : k],
+                       p->ndim == 3 && k == 1, &h->tmap[i][k]);
     for (int d = 0; d < 3 && ok; d++)
       ok = cudaMalloc(&h->idxf[d], sizeof(float) * g.nG[d]) == cudaSuccess;
     if (!ok) {

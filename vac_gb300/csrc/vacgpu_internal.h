@@ -206,9 +206,10 @@ VACGPU_DECLARE_LAUNCHERS(mixedf32, float)
 // direction (fused_box_rows).
 bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
                         const float* const* idxf, int nzc, cudaStream_t st);
-// rows of the fused sweep's TMA box: x and z sweeps (k=0), y sweep (k=1)
+// rows of the fused sweep's TMA box: x and z sweeps and the 3-D y sweep
+// (k=0), the 2-D y sweep (k=1)
 constexpr int FUSED_BOX_ROWS[2] = {12, 10};
-int fused_smem_bytes(int nw, int d);
+int fused_smem_bytes(int nw, int kind);
 
 // Precision-independent time-loop kernels (control.cu).
 void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st);
