@@ -519,7 +519,7 @@ struct Fused {
     const long long off = gidx(g, gc[0], gc[1], gc[2]);
 #pragma unroll
     for (int v = 0; v < NW; v++) a.wout[off + v * g.vs] = acc[v];
-    if (near_bnd(g, gc)) ghost_images(a, gc, acc);
+    if (near_bnd(g, gc)) ghost_images(a, gc, off, acc);
   }
 
   // Within two cells of a mesh face: the cell is the source of ghost cells.
@@ -584,12 +584,30 @@ struct Fused {
   // region-by-region copies of src/vacgrid.t:195-413 composed), so the cell
   // gc writes its value to each position whose coordinates are gc's own or
   // preimages in every dimension, at least one of them a preimage.
+  // off: the cell's own index in the state buffer (images are offsets
+  // from it).  The common case -- an x-boundary cell with interior y and z
+  // -- writes its one or two images in its own row without the general
+  // loop.
   static __device__ __forceinline__ void ghost_images(const FusedArgs& a,
                                                       const int* gc,
+                                                      long long off,
                                                       const float (&acc)[NW]) {
     const DevGrid& g = a.g;
-    int x1, x2, fx, y1 = 0, y2 = 0, fy = 0, z1 = 0, z2 = 0, fz = 0;
+    int x1, x2, fx;
     const int nx_ = 1 + preimages(a, 0, gc[0], x1, fx, x2);
+    const bool yin = NDIM < 2 || (gc[1] >= 4 && gc[1] < g.nx[1]);
+    const bool zin = NDIM < 3 || (gc[2] >= 4 && gc[2] < g.nx[2]);
+    if (yin && zin) {
+      for (int i = 1; i < nx_; i++) {
+        const long long o = off + ((i == 1 ? x1 : x2) - gc[0]);
+        const int fl = i == 1 ? fx : 0;
+#pragma unroll
+        for (int v = 0; v < NW; v++)
+          a.wout[o + v * g.vs] = ((fl >> v) & 1) ? -acc[v] : acc[v];
+      }
+      return;
+    }
+    int y1 = 0, y2 = 0, fy = 0, z1 = 0, z2 = 0, fz = 0;
     const int ny_ = NDIM > 1 ? 1 + preimages(a, 1, gc[1], y1, fy, y2) : 1;
     const int nz_ = NDIM > 2 ? 1 + preimages(a, 2, gc[2], z1, fz, z2) : 1;
 #pragma unroll 1
@@ -600,12 +618,14 @@ struct Fused {
       for (int jj = 0; jj < ny_; jj++) {
         const int py = jj == 0 ? gc[1] : (jj == 1 ? y1 : y2);
         const int sy = jj == 1 ? fy : 0;
+        const long long orow = off + (long long)(pz - gc[2]) * g.plane +
+                               (long long)(py - gc[1]) * g.P;
 #pragma unroll 1
         for (int i = 0; i < nx_; i++) {
           if ((i | jj | k) == 0) continue;
           const int px = i == 0 ? gc[0] : (i == 1 ? x1 : x2);
           const int fl = (i == 1 ? fx : 0) ^ sy ^ sz;
-          const long long o = gidx(g, px, py, pz);
+          const long long o = orow + (px - gc[0]);
 #pragma unroll
           for (int v = 0; v < NW; v++)
             a.wout[o + v * g.vs] = ((fl >> v) & 1) ? -acc[v] : acc[v];
