@@ -119,9 +119,17 @@ def max_over_ranks(ws, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job(ws, units_per_rank, seconds):
+    """Replicas: every rank advanced units_per_rank cell-updates in its own
+    seconds; the job's rate is all ranks' units over the slowest rank."""
+    el = max_over_ranks(ws, seconds)
+    return units_per_rank * ws / el, el
 
 
 def make_params(snap, prec):
@@ -381,10 +389,9 @@ def main():
         torch.cuda.synchronize()
     el = ev0.elapsed_time(ev1) / 1e3
     barrier(ws)
-    el = max_over_ranks(ws, el)
+    value, el = whole_job(ws, ncell * K, el)
     stats = eng.kernel_stats()
     launches = sum(v[0] for v in stats.values())
-    value = ncell * K * ws / el
 
     # ---- roofline of the dominant kernel: a second pass with per-launch events
     eng.timing(True)
@@ -429,8 +436,7 @@ def main():
     eng2.step(K)
     eng2.download_flat(hout.data_ptr())
     torch.cuda.synchronize()
-    e2e_el = max_over_ranks(ws, time.perf_counter() - t0)
-    e2e_value = ncell * K * ws / e2e_el
+    e2e_value, e2e_el = whole_job(ws, ncell * K, time.perf_counter() - t0)
     eng2.close()
 
     # ---- plain FP64 run of the same steps and the mixed-vs-FP64 error
