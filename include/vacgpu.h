@@ -133,6 +133,9 @@ typedef struct vacgpu_params {
   double vacuumrho;             /* >=0: rho<smallrho becomes vacuum         */
   int useprimitive;             /* limit primitive variables (upwindLR,     */
                                 /* src/vactvdlf.t:325-362)                  */
+  /* resistive MHD, eqpar[1] = eqpar(eta_) > 0 (src/vacphys.mhdres.t)     */
+  int compactres;               /* 1: Laplacian form, 0: curl form          */
+  double dtdiffpar;             /* diffusion dt limit dtdiffpar*dx^2/eta    */
 } vacgpu_params;
 
 typedef struct vacgpu_handle vacgpu_handle;

@@ -280,6 +280,11 @@ class NumpyVac:
                         g = self.src_par[d - 1]
                         if abs(g) > SMALLDOUBLE:
                             wnew[(iw,) + sl] = wnew[(iw,) + sl] + qdt * g * wCT[(d,) + sl]
+        if self.mhd and abs(self.p.eqpar[1]) > SMALLDOUBLE:
+            if self.p.compactres:
+                self.addsource_res1(qdt, ixO, wCT, wnew)
+            else:
+                self.addsource_res2(qdt, ixO, wCT, wnew)
         if self.mhd and self.p.divbfix:
             divb = np.zeros(self.nG)[sl]
             for idim in range(self.ndim):
@@ -299,6 +304,92 @@ class NumpyVac:
                     for c in range(2, self.ndir + 1):
                         mb = mb + wCT[(c,) + sl] * wCT[(self.b0 + c,) + sl]
                     wnew[(iw,) + sl] = wnew[(iw,) + sl] - mb / rho * divb
+
+    @staticmethod
+    def lvc(i, j, k):
+        if i == j or j == k or i == k:
+            return 0
+        return 1 if (i, j, k) in ((1, 2, 3), (2, 3, 1), (3, 1, 2)) else -1
+
+    def grad(self, q, b, idim):
+        """slab gradient, src/vacgrid.t:816-823, on box b (full arrays)"""
+        out = np.zeros(self.nG)
+        out[b.sl()] = HALF * (q[b.sl(idim, 1)] - q[b.sl(idim, -1)]) / self.dx[(idim,) + b.sl()]
+        return out
+
+    def getcurrent(self, w, b):
+        """src/vacphys.mhdres.t:48-93: J = curl B on b; (idirmin, J)."""
+        idirmin0 = 7 - 2 * self.ndir
+        idirmin = 4
+        cur = {i: np.zeros(self.nG) for i in range(idirmin0, 4)}
+        for idir in range(idirmin0, 4):
+            for jdir in range(1, self.ndim + 1):
+                for kdir in range(1, self.ndir + 1):
+                    l = self.lvc(idir, jdir, kdir)
+                    if not l:
+                        continue
+                    g = self.grad(w[self.b0 + kdir], b, jdir - 1)
+                    c = cur[idir]
+                    c[b.sl()] = c[b.sl()] + g[b.sl()] if l == 1 else c[b.sl()] - g[b.sl()]
+                    idirmin = min(idirmin, idir)
+        return idirmin, cur
+
+    def addsource_res2(self, qdt, ixO, w, wnew):
+        """src/vacphys.mhdres.t:236-315, constant eta"""
+        ix = Box(ixO.lo, ixO.hi)
+        for d in range(self.ndim):
+            ix.lo[d] -= 1
+            ix.hi[d] += 1
+        idirmin, cur = self.getcurrent(w, ix)
+        eta = self.p.eqpar[1]
+        sl = ixO.sl()
+        for iw in range(self.nw):
+            if self.b0 < iw <= self.b0 + self.ndir:
+                idir = iw - self.b0
+                for jdir in range(1, self.ndim + 1):
+                    for kdir in range(idirmin, 4):
+                        l = self.lvc(idir, jdir, kdir)
+                        if not l:
+                            continue
+                        tmp = np.zeros(self.nG)
+                        tmp[ix.sl()] = cur[kdir][ix.sl()] * eta * qdt
+                        g = self.grad(tmp, ixO, jdir - 1)[sl]
+                        wnew[(iw,) + sl] = wnew[(iw,) + sl] - g if l == 1 else wnew[(iw,) + sl] + g
+            elif iw == self.e_:
+                for idir in range(1, self.ndim + 1):
+                    for jdir in range(1, self.ndir + 1):
+                        for kdir in range(idirmin, 4):
+                            l = self.lvc(idir, jdir, kdir)
+                            if not l:
+                                continue
+                            tmp = np.zeros(self.nG)
+                            tmp[ix.sl()] = (w[(self.b0 + jdir,) + ix.sl()] * cur[kdir][ix.sl()]
+                                            * eta * qdt)
+                            g = self.grad(tmp, ixO, idir - 1)[sl]
+                            wnew[(iw,) + sl] = (wnew[(iw,) + sl] + g if l == 1
+                                                else wnew[(iw,) + sl] - g)
+
+    def addsource_res1(self, qdt, ixO, w, wnew):
+        """src/vacphys.mhdres.t:96-233, constant eta"""
+        idirmin, cur = self.getcurrent(w, ixO)
+        eta = self.p.eqpar[1]
+        sl = ixO.sl()
+        for idir in range(1, self.ndir + 1):
+            q = w[self.b0 + idir]
+            tmp = np.zeros(self.nG)[sl]
+            for idim in range(self.ndim):
+                dx = self.dx[(idim,) + sl]
+                tmp = tmp + (q[ixO.sl(idim, 1)] - 2 * q[sl] + q[ixO.sl(idim, -1)]) / (dx * dx)
+            tmp = tmp * eta
+            for iw in range(self.nw):
+                if iw == self.b0 + idir:
+                    wnew[(iw,) + sl] = wnew[(iw,) + sl] + qdt * tmp
+                elif iw == self.e_:
+                    wnew[(iw,) + sl] = wnew[(iw,) + sl] + qdt * tmp * q[sl]
+        jj = np.zeros(self.nG)[sl]
+        for idir in range(idirmin, 4):
+            jj = jj + cur[idir][sl] * cur[idir][sl]
+        wnew[(self.e_,) + sl] = wnew[(self.e_,) + sl] + qdt * eta * jj
 
     def keeppositive(self, w):
         """smallfix: src/vacphys.t.mhd:9-53, src/vacphys.t.hd:176-219,
@@ -520,8 +611,13 @@ class NumpyVac:
         for _ in range(nsteps):
             if self.dtpar > ZERO:
                 self.dt = self.dtpar
-            elif self.courantpar > ZERO:
-                self.getdt_courant()
+            else:
+                if self.courantpar > ZERO:
+                    self.getdt_courant()
+                if self.mhd and self.p.eqpar[1] != ZERO:
+                    # getdt_res, src/vacphys.mhdres.t:5-45
+                    m = min(self.dx[(d,) + self.ixM.sl()].min() for d in range(self.ndim))
+                    self.dt = min(self.dt, self.p.dtdiffpar * (m * m) / self.p.eqpar[1])
             p = self.p
             if self.it >= p.itmax or self.t >= p.tmax or self.dt < p.dtmin:
                 return True

@@ -52,6 +52,7 @@ typedef struct vo_state {
   double *w, *w1, *wold;
   double *wLC, *wRC, *fLC, *fRC, *vLC, *vRC, *cmaxC, *ldw, *dwC, *tmp,
       *tmp2, *divb, *csound2, *cfast2, *pp;
+  double* cur[3];    /* current density components (resistive MHD) */
   double dtcourant[3];
   double dt, t, dtold, dtpar, courantpar, dtgrav;
   int it, itmin;
@@ -542,10 +543,125 @@ static void addsource_grav(vo_state* s, double qdt, box ixO, const double* w,
   }
 }
 
-/* addsource2, src/vac.t:575-605: specialsource then addsource */
+/* Levi-Civita symbol lvc(i,j,k), 1-based indices */
+static int lvc(int i, int j, int k) {
+  if (i == j || j == k || i == k) return 0;
+  return ((i == 1 && j == 2) || (i == 2 && j == 3) || (i == 3 && j == 1)) ? 1 : -1;
+}
+
+/* getcurrent, src/vacphys.mhdres.t:48-93: J_i = eps_ijk d_j B_k on ix with
+ * the slab gradient; components idirmin0=7-2*ndir..3; returns idirmin */
+static int getcurrent(vo_state* s, const double* w, box ix) {
+  const int idirmin0 = 7 - 2 * s->ndir;
+  int idirmin = 4;
+  for (int idir = idirmin0; idir <= 3; idir++) FORBOX(ix, i) s->cur[idir - 1][i] = ZERO;
+  for (int idir = idirmin0; idir <= 3; idir++)
+    for (int jdir = 1; jdir <= s->ndim; jdir++)
+      for (int kdir = 1; kdir <= s->ndir; kdir++) {
+        const int l = lvc(idir, jdir, kdir);
+        if (!l) continue;
+        gradient(s, W(w, s->b0_ + kdir), ix, jdir - 1, s->tmp2);
+        double* c = s->cur[idir - 1];
+        if (l == 1)
+          FORBOX(ix, i) c[i] = c[i] + s->tmp2[i];
+        else
+          FORBOX(ix, i) c[i] = c[i] - s->tmp2[i];
+        if (idir < idirmin) idirmin = idir;
+      }
+  return idirmin;
+}
+
+/* addsource_res2, src/vacphys.mhdres.t:236-315 (curl form, compactres=F),
+ * constant eta = eqpar(eta_) > 0:  B_i -= eps_ijk d_j (eta J_k) qdt,
+ * e += eps_ijk d_i (B_j eta J_k qdt) */
+static void addsource_res2(vo_state* s, double qdt, box ixO, const double* w,
+                           double* wnew) {
+  box ix = ixO;
+  for (int d = 0; d < s->ndim; d++) {
+    ix.lo[d]--;
+    ix.hi[d]++;
+  }
+  const int idirmin = getcurrent(s, w, ix);
+  const double eta = s->p.eqpar[1];
+  for (int iw = 0; iw < s->nw; iw++) {
+    double* wn = W(wnew, iw);
+    if (iw > s->b0_ && iw <= s->b0_ + s->ndir) {
+      const int idir = iw - s->b0_;
+      for (int jdir = 1; jdir <= s->ndim; jdir++)
+        for (int kdir = idirmin; kdir <= 3; kdir++) {
+          const int l = lvc(idir, jdir, kdir);
+          if (!l) continue;
+          const double* c = s->cur[kdir - 1];
+          FORBOX(ix, i) s->tmp[i] = c[i] * eta * qdt;
+          gradient(s, s->tmp, ixO, jdir - 1, s->tmp2);
+          if (l == 1)
+            FORBOX(ixO, i) wn[i] = wn[i] - s->tmp2[i];
+          else
+            FORBOX(ixO, i) wn[i] = wn[i] + s->tmp2[i];
+        }
+    } else if (iw == s->e_) {
+      for (int idir = 1; idir <= s->ndim; idir++)
+        for (int jdir = 1; jdir <= s->ndir; jdir++)
+          for (int kdir = idirmin; kdir <= 3; kdir++) {
+            const int l = lvc(idir, jdir, kdir);
+            if (!l) continue;
+            const double* c = s->cur[kdir - 1];
+            const double* bj = W(w, s->b0_ + jdir);
+            FORBOX(ix, i) s->tmp[i] = bj[i] * c[i] * eta * qdt;
+            gradient(s, s->tmp, ixO, idir - 1, s->tmp2);
+            if (l == 1)
+              FORBOX(ixO, i) wn[i] = wn[i] + s->tmp2[i];
+            else
+              FORBOX(ixO, i) wn[i] = wn[i] - s->tmp2[i];
+          }
+    }
+  }
+}
+
+/* addsource_res1, src/vacphys.mhdres.t:96-233 (compact form, compactres=T),
+ * constant eta > 0: B_i += qdt eta lap(B_i), e += qdt eta lap(B_i) B_i for
+ * each i, then e += qdt eta J^2 */
+static void addsource_res1(vo_state* s, double qdt, box ixO, const double* w,
+                           double* wnew) {
+  const int idirmin = getcurrent(s, w, ixO);
+  const double eta = s->p.eqpar[1];
+  double* tmp = s->tmp;
+  for (int idir = 1; idir <= s->ndir; idir++) {
+    FORBOX(ixO, i) tmp[i] = ZERO;
+    const double* q = W(w, s->b0_ + idir);
+    for (int idim = 0; idim < s->ndim; idim++) {
+      const long sh = s->st[idim];
+      const double* dx = W(s->dx, idim);
+      FORBOX(ixO, i) tmp[i] = tmp[i] + (q[i + sh] - 2 * q[i] + q[i - sh]) / (dx[i] * dx[i]);
+    }
+    FORBOX(ixO, i) tmp[i] = tmp[i] * eta;
+    for (int iw = 0; iw < s->nw; iw++) {
+      double* wn = W(wnew, iw);
+      if (iw == s->b0_ + idir)
+        FORBOX(ixO, i) wn[i] = wn[i] + qdt * tmp[i];
+      else if (iw == s->e_)
+        FORBOX(ixO, i) wn[i] = wn[i] + qdt * tmp[i] * q[i];
+    }
+  }
+  double* e = W(wnew, s->e_);
+  FORBOX(ixO, i) {
+    double jj = ZERO;
+    for (int idir = idirmin; idir <= 3; idir++) jj = jj + s->cur[idir - 1][i] * s->cur[idir - 1][i];
+    e[i] = e[i] + qdt * eta * jj;
+  }
+}
+
+/* addsource2, src/vac.t:575-605: specialsource then addsource (resistive
+ * terms, src/vacphys.mhd0.t:223-230, then Powell) */
 static void addsource2(vo_state* s, double qdt, box ixO, const double* wCT,
                        double* w) {
   if (s->src_id == VACGPU_SRC_GRAVITY) addsource_grav(s, qdt, ixO, wCT, w);
+  if (s->mhd && fabs(s->p.eqpar[1]) > SMALLDOUBLE) {
+    if (s->p.compactres)
+      addsource_res1(s, qdt, ixO, wCT, w);
+    else
+      addsource_res2(s, qdt, ixO, wCT, w);
+  }
   if (s->mhd && s->p.divbfix) addsource_divb(s, qdt, ixO, wCT, w);
 }
 
@@ -908,6 +1024,22 @@ static void getdt_courant(vo_state* s) {
   }
 }
 
+/* getdt_res, src/vacphys.mhdres.t:5-45 (eqpar(eta_) > 0): the diffusion
+ * limit dtdiffpar*min(dx)^2/eta, called from getdt (src/vacphys.mhd0.t:83-103) */
+static void getdt_res(vo_state* s) {
+  double m = ZERO;
+  int first = 1;
+  for (int d = 0; d < s->ndim; d++) {
+    const double* dx = W(s->dx, d);
+    FORBOX_SEQ(s->ixM, i) {
+      if (first || dx[i] < m) m = dx[i];
+      first = 0;
+    }
+  }
+  const double dtdiff = s->p.dtdiffpar * (m * m) / s->p.eqpar[1];
+  if (dtdiff < s->dt) s->dt = dtdiff;
+}
+
 /* getdt_grav, vacusr.gravity.t (dt limit of the gravity hook) */
 static void getdt_special(vo_state* s) {
   if (s->src_id != VACGPU_SRC_GRAVITY) return;
@@ -987,6 +1119,7 @@ vo_state* vo_create(const vacgpu_params* p) {
                    &s->csound2, &s->cfast2, &s->pp};
   for (unsigned i = 0; i < sizeof(t1) / sizeof(t1[0]); i++)
     *t1[i] = calloc(N, sizeof(double));
+  for (int c = 0; c < 3; c++) s->cur[c] = calloc(N, sizeof(double));
   s->smallp = p->smallp;
   s->smallrho = p->smallrho;
   s->courantpar = p->courantpar;
@@ -1006,6 +1139,7 @@ void vo_destroy(vo_state* s) {
                  s->pp};
   for (unsigned i = 0; i < sizeof(a) / sizeof(a[0]); i++) free(a[i]);
   for (int iB = 0; iB < VACGPU_MAXB; iB++) free(s->fixB[iB]);
+  for (int c = 0; c < 3; c++) free(s->cur[c]);
   free(s);
 }
 
@@ -1134,6 +1268,7 @@ int vo_step(vo_state* s, int maxsteps, double tstop, int* finished) {
       s->dt = s->dtpar;
     } else {
       if (s->courantpar > ZERO) getdt_courant(s);
+      if (s->mhd && s->p.eqpar[1] != ZERO) getdt_res(s);
       getdt_special(s);
       if (p->dtcantgrow && s->it > s->itmin && s->dtold < s->dt) s->dt = s->dtold;
       s->dtold = s->dt;

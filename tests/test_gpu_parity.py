@@ -112,7 +112,26 @@ BC_CASES = [
      _bcs(B.BC_GRAD1, B.BC_FIXED, B.BC_SYMM0, B.BC_CONT1, B.BC_PERIODIC, B.BC_PERIODIC),
      None),
 ]
-FP64_CASES = FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES
+def _resistive(eta, compact=0):
+    def tweak(p):
+        p.eqpar[1] = eta
+        p.compactres = compact
+    return tweak
+
+
+# resistive MHD (constant eta): curl and compact forms, 2-D and 3-D, and a
+# run whose dt is the diffusion limit
+RES_CASES = [
+    ("ot-resistive", lambda: inistate.orszag_tang(32), "woodward", "periodic", 10,
+     _resistive(0.01), None),
+    ("ot-resistive-compact", lambda: inistate.orszag_tang(32), "minmod", "periodic", 10,
+     _resistive(0.01, 1), None),
+    ("rm3-resistive", lambda: inistate.random_modes(12, seed=7), "minmod", "periodic", 4,
+     _resistive(0.002), None),
+    ("ot-resistive-dtdiff", lambda: inistate.orszag_tang(24), "minmod", "periodic", 6,
+     _resistive(1.0), None),
+]
+FP64_CASES = FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES + RES_CASES
 
 
 def _ragged():
@@ -223,6 +242,16 @@ def test_mixed_useprimitive_within_tolerance(gpu_lib, name, mk, lim, bc, n, twea
 @pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", BC_CASES,
                          ids=[c[0] for c in BC_CASES])
 def test_mixed_boundary_types_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
+    o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
+    a, b = e.state(), o.state()
+    for iw in range(a.shape[0]):
+        rel = np.abs(a[iw] - b[iw]).sum() / np.abs(b[iw]).sum()
+        assert rel <= MIXED_REL_L1, (iw, rel)
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", RES_CASES[:3],
+                         ids=[c[0] for c in RES_CASES[:3]])
+def test_mixed_resistive_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
     o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
     a, b = e.state(), o.state()
     for iw in range(a.shape[0]):

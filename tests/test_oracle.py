@@ -82,7 +82,25 @@ BC_CASES = [
      bcs(B.BC_GRAD1, B.BC_FIXED, B.BC_SYMM0, B.BC_CONT1, B.BC_PERIODIC, B.BC_PERIODIC)),
 ]
 
-CASES = CASES + SMALLFIX_CASES + BC_CASES + [
+def resistive(eta, compact=0):
+    def tweak(p):
+        p.eqpar[1] = eta
+        p.compactres = compact
+    return tweak
+
+
+RES_CASES = [
+    ("ot-resistive", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5,
+     resistive(0.01)),
+    ("ot-resistive-compact", lambda: inistate.orszag_tang(16), "minmod", "periodic", 5,
+     resistive(0.01, 1)),
+    ("rm3-resistive", lambda: inistate.random_modes(8, seed=7), "minmod", "periodic", 3,
+     resistive(0.002)),
+    ("ot-resistive-dtdiff", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     resistive(1.0)),
+]
+
+CASES = CASES + SMALLFIX_CASES + BC_CASES + RES_CASES + [
     # reconstruction in primitive variables (useprimitive=T)
     ("ot-useprimitive", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5,
      lambda p: setattr(p, "useprimitive", 1)),

@@ -61,6 +61,8 @@ class VacParams(C.Structure):
         ("smallrhocoeff", C.c_double),
         ("vacuumrho", C.c_double),
         ("useprimitive", C.c_int),
+        ("compactres", C.c_int),
+        ("dtdiffpar", C.c_double),
     ]
 
 
@@ -105,6 +107,8 @@ def default_params(ndim, ndir, physics, nx, gamma=5.0 / 3.0):
     p.smallrhocoeff = 1.0e-6
     p.vacuumrho = -1.0
     p.useprimitive = 0
+    p.compactres = 0
+    p.dtdiffpar = 0.5
     return p
 
 

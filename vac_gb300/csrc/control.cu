@@ -118,6 +118,9 @@ __device__ void dt_end_dev(Ctrl* c, const DtEndArgs& p) {
         if (q < dt) dt = q;
       }
     }
+    // getdt: the resistive diffusion limit (getdt_res,
+    // src/vacphys.mhdres.t:5-45), fixed by the grid
+    if (c->dtdiff < dt) dt = c->dtdiff;
     // getdt_special (uniform gravity: dtgrav fixed at the first step)
     if (c->dtgrav < dt) dt = c->dtgrav;
     if (p.dtcantgrow && c->it > c->itmin && c->dtold < dt) dt = c->dtold;

@@ -76,9 +76,11 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
         "predictor");
   if (!(p->smallp >= 0.0))
     return vacgpu_internal_fail("vacgpu_sweep_noalloc needs smallp >= 0");
-  if (p->smallfix || p->useprimitive)
+  if (p->smallfix || p->useprimitive ||
+      (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] != 0.0))
     return vacgpu_internal_fail(
-        "vacgpu_sweep_noalloc supports neither smallfix nor useprimitive");
+        "vacgpu_sweep_noalloc supports neither smallfix, useprimitive nor "
+        "resistivity");
   const double* dxs[3] = {dx0, dx1, dx2};
   long long gcells = 1;
   for (int d = 0; d < p->ndim; d++) {

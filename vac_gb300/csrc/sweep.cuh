@@ -57,10 +57,111 @@ struct Sweep {
   typedef Lay<NDIR, MHD> L;
   static constexpr int NW = L::NW;
 
+  // Levi-Civita symbol, 1-based indices
+  static __host__ __device__ constexpr int lvc(int i, int j, int k) {
+    return (i == j || j == k || i == k)
+               ? 0
+               : (((i == 1 && j == 2) || (i == 2 && j == 3) || (i == 3 && j == 1)) ? 1 : -1);
+  }
+  // first current component getcurrent fills (src/vacphys.mhdres.t:48-93)
+  static constexpr int IDM0 = 7 - 2 * NDIR;
+
+  // J_k = eps_kjl d_j B_l at the cell o (offset from the cell of wct) with
+  // ghost-range coordinates cc, slab gradients (src/vacgrid.t:816-823)
+  static __device__ __forceinline__ R current(const SweepArgs& a,
+                                              const T* __restrict__ wct,
+                                              long long o, const long long* st,
+                                              const int* cc, int k) {
+    R j = R(0);
+#pragma unroll
+    for (int jd = 1; jd <= NDIM; jd++)
+#pragma unroll
+      for (int kd = 1; kd <= NDIR; kd++) {
+        const int l = lvc(k, jd, kd);
+        if (!l) continue;
+        const T* q = wct + o + (long long)(L::B0 + kd) * a.g.vs;
+        const R g = R(0.5) * (R(q[st[jd - 1]]) - R(q[-st[jd - 1]])) /
+                    PH::dx(a.a, jd - 1, cc[jd - 1]);
+        j = l == 1 ? j + g : j - g;
+      }
+    return j;
+  }
+
+  // resistive terms of addsource for constant eta = eqpar(eta_) > 0:
+  // addsource_res2 (curl form, src/vacphys.mhdres.t:236-315) or
+  // addsource_res1 (compactres, :96-233), in the reference's term order
+  static __device__ __forceinline__ void add_resistive(
+      const SweepArgs& a, double qdt, const R* wc, const T* __restrict__ wct,
+      const long long* st, const int* c, R* acc) {
+    const R eta = R(a.ph.eta), q = PH::qdiv(qdt);
+    const long long vs = a.g.vs;
+    if (!a.ph.compactres) {
+      // B_i -= eps_ijk d_j (eta J_k qdt)
+#pragma unroll
+      for (int idir = 1; idir <= NDIR; idir++)
+#pragma unroll
+        for (int jd = 1; jd <= NDIM; jd++)
+#pragma unroll
+          for (int kd = IDM0; kd <= 3; kd++) {
+            const int l = lvc(idir, jd, kd);
+            if (!l) continue;
+            int cp[3] = {c[0], c[1], c[2]}, cm[3] = {c[0], c[1], c[2]};
+            cp[jd - 1]++;
+            cm[jd - 1]--;
+            const long long s = st[jd - 1];
+            const R tp = current(a, wct, s, st, cp, kd) * eta * q;
+            const R tm = current(a, wct, -s, st, cm, kd) * eta * q;
+            const R g = R(0.5) * (tp - tm) / PH::dx(a.a, jd - 1, c[jd - 1]);
+            acc[L::B0 + idir] = l == 1 ? acc[L::B0 + idir] - g : acc[L::B0 + idir] + g;
+          }
+      // e += eps_ijk d_i (B_j eta J_k qdt)
+#pragma unroll
+      for (int idir = 1; idir <= NDIM; idir++)
+#pragma unroll
+        for (int jd = 1; jd <= NDIR; jd++)
+#pragma unroll
+          for (int kd = IDM0; kd <= 3; kd++) {
+            const int l = lvc(idir, jd, kd);
+            if (!l) continue;
+            int cp[3] = {c[0], c[1], c[2]}, cm[3] = {c[0], c[1], c[2]};
+            cp[idir - 1]++;
+            cm[idir - 1]--;
+            const long long s = st[idir - 1];
+            const T* bj = wct + (long long)(L::B0 + jd) * vs;
+            const R tp = R(bj[s]) * current(a, wct, s, st, cp, kd) * eta * q;
+            const R tm = R(bj[-s]) * current(a, wct, -s, st, cm, kd) * eta * q;
+            const R g = R(0.5) * (tp - tm) / PH::dx(a.a, idir - 1, c[idir - 1]);
+            acc[L::E] = l == 1 ? acc[L::E] + g : acc[L::E] - g;
+          }
+    } else {
+      // B_i += qdt eta lap(B_i), e += qdt eta lap(B_i) B_i, then e += qdt eta J^2
+#pragma unroll
+      for (int idir = 1; idir <= NDIR; idir++) {
+        const T* qb = wct + (long long)(L::B0 + idir) * vs;
+        R t = R(0);
+#pragma unroll
+        for (int d = 0; d < NDIM; d++) {
+          const R dx = PH::dx(a.a, d, c[d]);
+          t = t + (R(qb[st[d]]) - R(2) * R(qb[0]) + R(qb[-st[d]])) / (dx * dx);
+        }
+        t = t * eta;
+        acc[L::B0 + idir] = acc[L::B0 + idir] + q * t;
+        acc[L::E] = acc[L::E] + q * t * wc[L::B0 + idir];
+      }
+      R jj = R(0);
+#pragma unroll
+      for (int k = IDM0; k <= 3; k++) {
+        const R jk = current(a, wct, 0, st, c, k);
+        jj = jj + jk * jk;
+      }
+      acc[L::E] = acc[L::E] + q * eta * jj;
+    }
+  }
+
   // addsource2 (src/vac.t:575-605): specialsource (uniform gravity,
-  // vacusr.gravity.t:24-75) then addsource (Powell divB source,
-  // src/vacphys.mhd0.t:246-280).  wc = wCT at the cell, wct points at the
-  // cell in the wCT array (for the divB central differences).
+  // vacusr.gravity.t:24-75) then addsource (resistive terms, then the
+  // Powell divB source, src/vacphys.mhd0.t:208-280).  wc = wCT at the
+  // cell, wct points at the cell in the wCT array (for the differences).
   static __device__ __forceinline__ void add_sources(
       const SweepArgs& a, double qdt, const R* wc, const T* __restrict__ wct,
       const long long* st, const int* c, R* acc) {
@@ -77,6 +178,7 @@ struct Sweep {
           acc[L::E] = acc[L::E] + PH::mul_qg(qdt, gr) * wc[d];
       }
     }
+    if (MHD && fabs(a.ph.eta) > 1.0e-99) add_resistive(a, qdt, wc, wct, st, c, acc);
     if (MHD && a.ph.divbfix) {
       R divb = R(0);
 #pragma unroll

@@ -154,6 +154,7 @@ struct vacgpu_handle {
   cudaStream_t st;
   int it_host;
   double dtgrav;
+  double dtdiff;     // resistive diffusion dt limit (getdt_res), BIG if ideal
   bool have_grid, have_state;
   int pmode;         // mixed pressure variant (0 ff, 1 native f64, 2 f32)
   cudaStream_t own_st;
@@ -559,8 +560,8 @@ int check_params(const vacgpu_params* p) {
   for (int d = 0; d < p->ndim; d++)
     if (p->nx[d] < 2) return fail("nx must be >= 2 in every dimension");
   if (!(p->eqpar[0] > 0.0)) return fail("eqpar(gamma_) must be positive");
-  if (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] != 0.0)
-    return fail("resistive MHD (eqpar(eta_)/=0) is not on this path");
+  if (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] < 0.0)
+    return fail("eqpar(eta_)<0 needs the user's specialeta, not on this path");
   if (p->typefull != VACGPU_TVDLF && p->typefull != VACGPU_TVDLF1)
     return fail("typefull must be tvdlf or tvdlf1");
   for (int iw = 0; iw < nw; iw++)
@@ -681,6 +682,8 @@ void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
   p->smallrho = -1.0;
   p->smallrhocoeff = 1.0e-6;
   p->vacuumrho = -1.0;
+  p->compactres = 0;
+  p->dtdiffpar = 0.5;
 }
 
 int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
@@ -728,6 +731,8 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.vacuumrho = p->vacuumrho;
   ph.smallrhocoeff = p->smallrhocoeff;
   ph.useprim = p->useprimitive && p->typefull == VACGPU_TVDLF;
+  ph.eta = p->physics == VACGPU_PHYS_MHD ? p->eqpar[1] : 0.0;
+  ph.compactres = p->compactres;
   ph.src_id = VACGPU_SRC_NONE;
   set_gmaps(ph, p->ndim, p->nw);
   size_t bytes = h->elem * (size_t)g.vs * h->nw;
@@ -775,7 +780,8 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   h->fused = p->precision == VACGPU_PREC_MIXED && p->dimsplit &&
              (p->ndim == 2 || p->ndim == 3) && p->ndir == p->ndim &&
              p->typelimited == VACGPU_LIMITED_ORIGINAL &&
-             p->typefull == VACGPU_TVDLF && !p->smallfix && !p->useprimitive;
+             p->typefull == VACGPU_TVDLF && !p->smallfix && !p->useprimitive &&
+             !(p->physics == VACGPU_PHYS_MHD && p->eqpar[1] != 0.0);
   if (const char* fz = getenv("VACGPU_FUSED")) h->fused = h->fused && atoi(fz) != 0;
   // its ghost writes need uniform copy maps, periodic faces in pairs and
   // n >= 4; 'symm0' needs the split kernels' zero face fluxes
@@ -809,6 +815,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   c.courantpar = courantpar;
   c.smallp = p->smallp;
   c.dtgrav = BIGD;
+  c.dtdiff = BIGD;
   for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
   c.tstop = 1e300;
   e = cudaMemcpy(h->ctrl, &c, sizeof(c), cudaMemcpyHostToDevice);
@@ -888,6 +895,17 @@ int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
         vol = vol + dv;
       }
   h->volume = vol;
+  // getdt_res (src/vacphys.mhdres.t:5-45): dtdiffpar*min(dx)^2/eta, a
+  // constant of the grid
+  h->dtdiff = BIGD;
+  if (h->ph.eta != 0.0) {
+    double m = h->hdx[0][2];
+    for (int d = 0; d < nd; d++)
+      for (int i = 0; i < g.nx[d]; i++)
+        if (h->hdx[d][i + 2] < m) m = h->hdx[d][i + 2];
+    h->dtdiff = h->p.dtdiffpar * (m * m) / h->ph.eta;
+  }
+  CK(cudaMemcpy(&h->ctrl->dtdiff, &h->dtdiff, sizeof(double), cudaMemcpyHostToDevice));
   h->have_grid = true;
   return 0;
 }
@@ -914,6 +932,7 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
   for (int i = 0; i < 4; i++) c.nerror[i] = 0;
   c.dtgrav = h->dtgrav > 0 ? h->dtgrav : BIGD;
+  c.dtdiff = h->have_grid ? h->dtdiff : BIGD;
   c.cur = 0;
   c.fault = 0;
   CK(cudaMemcpyAsync(h->ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));

@@ -55,6 +55,8 @@ struct DevPhys {
   int smallfix;          // keeppositive before each ghost fill
   double vacuumrho, smallrhocoeff;
   int useprim;           // limit primitive variables (useprimitive)
+  double eta;            // resistivity eqpar(eta_) (0: ideal MHD)
+  int compactres;        // resistive source in the Laplacian form
   int src_id;
   double src_par[VACGPU_MAXSRCPAR];
   // Boundary index map per face [dim][lo/hi] when every variable shares it:
@@ -115,6 +117,7 @@ struct Ctrl {
   double t, dt, dtold, dtpar, courantpar;
   double smallp;
   double dtgrav;
+  double dtdiff;      // resistive diffusion dt limit (BIG without resistivity)
   double tstop;
   double dtcourant[3];
   int it, itmin;

@@ -413,6 +413,7 @@ int main(int argc, char** argv) {
   if (gets("typeadvance", "twostep") != "twostep")
     die("typeadvance=" + gets("typeadvance", "") + " is not on this path");
   p.useprimitive = getb("useprimitive", false);
+  p.compactres = getb("compactres", false);
   if (getb("sourcesplit", false)) die("sourcesplit=T is not on this path");
   std::string tds = lower(gets("typedimsplit", "default"));
   bool dimsplit = getb("dimsplit", true);
@@ -435,6 +436,7 @@ int main(int argc, char** argv) {
   // paramlist, stoplist
   p.courantpar = getd("courantpar", 0.8);
   p.dtpar = getd("dtpar", -1.0);
+  p.dtdiffpar = getd("dtdiffpar", 0.5);
   p.slowsteps = geti("slowsteps", 0);
   p.dtcantgrow = getb("dtcantgrow", false);
   p.itmax = geti("itmax", 1000000);
