@@ -65,8 +65,25 @@ enum {
   VACGPU_BC_SYMM0 = 8
 };
 
-/* typefull1 (src/vactvdlf.t:92-299): second order 'tvdlf' or 'tvdlf1' */
-enum { VACGPU_TVDLF = 0, VACGPU_TVDLF1 = 1 };
+/* typefull1 (src/vactvdlf.t:92-299): second order 'tvdlf' or 'tvdlf1'
+ * (Lax-Friedrichs dissipation), 'tvdmu' or 'tvdmu1' (TVD-MUSCL: Roe
+ * characteristic dissipation, src/vactvd.t:86-206, src/vacphys.mhdroe.t,
+ * src/vacphys.hdroe.t).  The first order forms run as one substep. */
+enum {
+  VACGPU_TVDLF = 0,
+  VACGPU_TVDLF1 = 1,
+  VACGPU_TVDMU = 2,
+  VACGPU_TVDMU1 = 3
+};
+
+/* typeentropy per characteristic wave (entropyfix, src/vactvd.t:422-451) */
+enum {
+  VACGPU_ENTROPY_NUL = 0,
+  VACGPU_ENTROPY_HARTEN = 1,
+  VACGPU_ENTROPY_POWELL = 2,
+  VACGPU_ENTROPY_RATIO = 3,
+  VACGPU_ENTROPY_YEE = 4
+};
 
 /* typelimited (src/vactvdlf.t:150-162) */
 enum {
@@ -106,7 +123,7 @@ typedef struct vacgpu_params {
   int nx[3];                    /* mesh cells per dimension (ixM extent)    */
   int dixB;                     /* ghost layers; must be 2 (src/vacdef.t:24)*/
   double eqpar[VACGPU_MAXEQPAR];/* eqpar(gamma_)[, eqpar(eta_)]             */
-  int typefull;                 /* VACGPU_TVDLF / VACGPU_TVDLF1             */
+  int typefull;                 /* VACGPU_TVDLF / _TVDLF1 / _TVDMU / _TVDMU1 */
   int typelimiter[VACGPU_MAXNW];/* VACGPU_LIM_* per variable                */
   int typelimited;              /* VACGPU_LIMITED_*                         */
   int dimsplit;                 /* 1 = dimensional splitting                */
@@ -136,6 +153,10 @@ typedef struct vacgpu_params {
   /* resistive MHD, eqpar[1] = eqpar(eta_) > 0 (src/vacphys.mhdres.t)     */
   int compactres;               /* 1: Laplacian form, 0: curl form          */
   double dtdiffpar;             /* diffusion dt limit dtdiffpar*dx^2/eta    */
+  /* Roe dissipation of 'tvdmu'/'tvdmu1' (src/vactvd.t:86-206)             */
+  int typeentropy[VACGPU_MAXNW];   /* VACGPU_ENTROPY_* per wave il          */
+  double entropycoef[VACGPU_MAXNW];/* 'yee' lower limit of |a| per wave     */
+  int divbwave;                 /* MHD: keep the div B wave (par/DEFAULT:47) */
 } vacgpu_params;
 
 typedef struct vacgpu_handle vacgpu_handle;

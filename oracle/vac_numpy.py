@@ -14,8 +14,17 @@ import numpy as np
 
 from vac_gb300 import abi
 
-HALF, ONE, TWO, ZERO = 0.5, 1.0, 2.0, 0.0
+HALF, ONE, TWO, ZERO, QUARTER = 0.5, 1.0, 2.0, 0.0, 0.25
 SMALLDOUBLE, BIGDOUBLE = 1.0e-99, 1.0e99
+
+
+def _fmax(a, b):
+    """Fortran MAX(a,b) as the select a>b ? a : b (the C oracle's fmax2)."""
+    return np.where(a > b, a, b)
+
+
+def _fmin(a, b):
+    return np.where(a < b, a, b)
 
 
 class Box:
@@ -54,6 +63,7 @@ class NumpyVac:
         self.smallrho = p.smallrho
         self.fixB = {}
         self.initialized = False
+        self.nstep = 1 if p.typefull in (abi.TVDLF1, abi.TVDMU1) else 2
         self.courantpar = p.courantpar
         self.dtpar = p.dtpar
         if self.dtpar > 0 and p.slowsteps != 1:
@@ -262,7 +272,13 @@ class NumpyVac:
 
     # ------------------------------------------------------- grid helpers
     def addflux(self, qdt, ixO, iw, idim, fR, ixR, fL, ixL, wnew):
+        """src/vacgrid.t:596-741 (slab); qdt<0 adds a dissipative flux."""
         self.setnoflux(iw, idim, ixO, fR, ixR, fL, ixL)
+        if qdt < ZERO:
+            wnew[(iw,) + ixO.sl()] = (wnew[(iw,) + ixO.sl()]
+                                      + (fR[ixR.sl()] - fL[ixL.sl()])
+                                      / self.dvolume[ixO.sl()])
+            return
         wnew[(iw,) + ixO.sl()] = (wnew[(iw,) + ixO.sl()]
                                   - qdt / self.dx[(idim,) + ixO.sl()]
                                   * (fR[ixR.sl()] - fL[ixL.sl()]))
@@ -510,6 +526,356 @@ class NumpyVac:
                 face.lo[idim] = face.hi[idim] = ixe
                 fL[face.sl()] = ZERO
 
+
+    # --------------------------------------------------------- Roe solver
+    def roe_dirs(self, idim):
+        """idir, jdir of src/vacphys.mhdroe.t:97 (0-based)."""
+        nd = self.ndir
+        i1 = idim + 1
+        d1 = i1 + 1 - nd * (i1 // nd)
+        j1 = d1 + 1 - nd * (d1 // nd)
+        return d1 - 1, j1 - 1
+
+    def roe_average(self, wL, wR, ixC, idim):
+        """Roe state at the faces ixC: src/vacphys.mhdroe.t:4-127 (MHD,
+        arithmetic means), src/vacphys.hdroe.t:4-45 (HD, sqrt(rho) weights).
+        Returns a dict of face arrays."""
+        sl = ixC.sl()
+        g, nd, e, b0 = self.gamma, self.ndir, self.e_, self.b0
+        rL, rR = wL[(0,) + sl], wR[(0,) + sl]
+        R = {}
+        if self.mhd:
+            rho = HALF * (rL + rR)
+            v = {c: HALF * (wL[(c,) + sl] / rL + wR[(c,) + sl] / rR)
+                 for c in range(1, nd + 1)}
+            B = {c: HALF * (wL[(b0 + c,) + sl] + wR[(b0 + c,) + sl])
+                 for c in range(1, nd + 1)}
+            pL = self.getpthermal(wL, ixC)
+            pR = self.getpthermal(wR, ixC)
+            p = HALF * (pL + pR)
+            if self.p.useprimitive:
+                dp = pR - pL
+            else:
+                s1 = s2 = s3 = None
+                for c in range(1, nd + 1):
+                    t1 = v[c] * (wR[(c,) + sl] - wL[(c,) + sl])
+                    s1 = t1 if c == 1 else s1 + t1
+                    s2 = v[c] * v[c] if c == 1 else s2 + v[c] * v[c]
+                    bR, bL = wR[(b0 + c,) + sl], wL[(b0 + c,) + sl]
+                    s3 = bR * bR - bL * bL if c == 1 else s3 + bR * bR - bL * bL
+                dp = (g - 1) * (wR[(e,) + sl] - wL[(e,) + sl] - s1
+                                + HALF * s2 * (rR - rL) - HALF * s3)
+            R["rhodv"] = (wR[(1 + idim,) + sl] - wL[(1 + idim,) + sl]
+                          - v[1 + idim] * (rR - rL))
+            cs2 = g * p / rho
+            bb = B[1] * B[1]
+            for c in range(2, nd + 1):
+                bb = bb + B[c] * B[c]
+            cf = bb / rho + cs2
+            bi = B[1 + idim]
+            cs = _fmax(ZERO, HALF * (cf - np.sqrt(cf * cf - 4.0 * cs2 * (bi * bi) / rho)))
+            cf = cf - cs
+            af = (cs2 - cs) / (cf - cs)
+            af = _fmin(ONE, _fmax(af, ZERO))
+            R["as"] = np.sqrt(ONE - af)
+            R["af"] = np.sqrt(af)
+            R["cf"] = np.sqrt(cf)
+            R["cs"] = np.sqrt(cs)
+            R["cs2"], R["dp"], R["v"] = cs2, dp, v
+            R["sr"] = np.sqrt(rho)
+            B[1 + idim] = np.where(np.abs(bi) < SMALLDOUBLE, SMALLDOUBLE, bi)
+            idir, jdir = self.roe_dirs(idim)
+            if nd == 2:
+                B[1 + idir] = np.where(B[1 + idir] >= ZERO, ONE, -ONE)
+            else:
+                bI, bJ = B[1 + idir], B[1 + jdir]
+                t = np.sqrt(bI * bI + bJ * bJ)
+                big = t > SMALLDOUBLE
+                B[1 + idir] = np.where(big, bI / t, np.sqrt(HALF))
+                B[1 + jdir] = np.where(big, bJ / t, np.sqrt(HALF))
+            R["B"] = B
+        else:
+            t = np.sqrt(rL)
+            t2 = np.sqrt(rR)
+            R["rho"] = t * t2
+            t = t / t2
+            R["v"] = {c: (wL[(c,) + sl] / rL * t + wR[(c,) + sl] / rR) / (1 + t)
+                      for c in range(1, nd + 1)}
+            hL = (self.getpthermal(wL, ixC) + wL[(e,) + sl]) / rL
+            hR = (self.getpthermal(wR, ixC) + wR[(e,) + sl]) / rR
+            R["h"] = (hL * t + hR) / (1 + t)
+        return R
+
+    def roe_wave(self, R, wL, wR, ixC, il, idim):
+        """Eigenvalue a, jump L(il)*dw and the entropy-fix bound smalla of
+        wave il: src/vacphys.mhdroe.t:130-281, src/vacphys.hdroe.t:48-141,
+        entropyfix src/vactvd.t:422-451."""
+        sl = ixC.sl()
+        g, nd, b0 = self.gamma, self.ndir, self.b0
+        rL, rR = wL[(0,) + sl], wR[(0,) + sl]
+        v = R["v"]
+        vi = v[1 + idim]
+        te = self.p.typeentropy[il]
+        lr = te in (abi.ENTROPY_HARTEN, abi.ENTROPY_POWELL, abi.ENTROPY_RATIO)
+        aL = aR = smalla = None
+        if self.mhd:
+            idir, jdir = self.roe_dirs(idim)
+            B, sr = R["B"], R["sr"]
+            bi, bI, bJ = B[1 + idim], B[1 + idir], B[1 + jdir]
+            dvI = wR[(1 + idir,) + sl] / rR - wL[(1 + idir,) + sl] / rL
+            dvJ = wR[(1 + jdir,) + sl] / rR - wL[(1 + jdir,) + sl] / rL
+            dbI = wR[(b0 + 1 + idir,) + sl] - wL[(b0 + 1 + idir,) + sl]
+            dbJ = wR[(b0 + 1 + jdir,) + sl] - wL[(b0 + 1 + jdir,) + sl]
+            cf, cs, af, as_, cs2 = R["cf"], R["cs"], R["af"], R["as"], R["cs2"]
+            dp, rhodv = R["dp"], R["rhodv"]
+            if il == 0:
+                bdv = bI * dvI
+                if nd == 3:
+                    bdv = bdv + bJ * dvJ
+                R["bdv"] = bdv * np.copysign(sr * sr, bi)
+                bdb = bI * dbI
+                if nd == 3:
+                    bdb = bdb + bJ * dbJ
+                R["bdb"] = bdb * np.sqrt(cs2) * sr
+            if il == 6:
+                R["bdv"] = (bJ * dvI - bI * dvJ) * HALF * (sr * sr)
+                R["bdb"] = (bJ * dbI - bI * dbJ) * HALF * np.copysign(sr, bi)
+            bdv, bdb = R["bdv"], R["bdb"]
+            if il == 0:
+                a = vi + cf
+                jump = HALF / cs2 * (af * (+cf * rhodv + dp) + as_ * (-cs * bdv + bdb))
+            elif il == 1:
+                a = vi - cf
+                jump = HALF / cs2 * (af * (-cf * rhodv + dp) + as_ * (+cs * bdv + bdb))
+            elif il == 2:
+                a = vi + cs
+                jump = HALF / cs2 * (as_ * (+cs * rhodv + dp) + af * (+cf * bdv - bdb))
+            elif il == 3:
+                a = vi - cs
+                jump = HALF / cs2 * (as_ * (-cs * rhodv + dp) + af * (-cf * bdv - bdb))
+            elif il == 4:
+                a = vi
+                jump = rR - rL - dp / cs2
+            elif il == 5:
+                if self.p.divbwave:
+                    a = vi
+                    jump = wR[(b0 + 1 + idim,) + sl] - wL[(b0 + 1 + idim,) + sl]
+                else:
+                    a = np.zeros_like(vi)
+                    jump = np.zeros_like(vi)
+            elif il == 6:
+                a = vi + np.abs(bi) / sr
+                jump = +bdv - bdb
+            else:
+                a = vi - np.abs(bi) / sr
+                jump = -bdv - bdb
+            if lr:
+                aL = wL[(1 + idim,) + sl] / rL
+                aR = wR[(1 + idim,) + sl] / rR
+                bLi = wL[(b0 + 1 + idim,) + sl]
+                bRi = wR[(b0 + 1 + idim,) + sl]
+                if il == 0:
+                    c2L = g * self.getpthermal(wL, ixC) / rL
+                    c2R = g * self.getpthermal(wR, ixC) / rR
+                    ccL = c2L + self.sq_sum(wL, b0, sl) / rL
+                    ccR = c2R + self.sq_sum(wR, b0, sl) / rR
+                    R["ccL"], R["ccR"] = ccL, ccR
+                    R["dL"] = np.sqrt(ccL * ccL - 4 * c2L * (bLi * bLi) / rL)
+                    R["dR"] = np.sqrt(ccR * ccR - 4 * c2R * (bRi * bRi) / rR)
+                if il in (0, 1, 2, 3):
+                    sg = ONE if il in (0, 2) else -ONE
+                    dsg = ONE if il in (0, 1) else -ONE
+                    ccL, ccR, dL, dR = R["ccL"], R["ccR"], R["dL"], R["dR"]
+                    qL = np.sqrt(HALF * (ccL + dL)) if dsg > 0 else np.sqrt(HALF * (ccL - dL))
+                    qR = np.sqrt(HALF * (ccR + dR)) if dsg > 0 else np.sqrt(HALF * (ccR - dR))
+                    aL = aL + qL if sg > 0 else aL - qL
+                    aR = aR + qR if sg > 0 else aR - qR
+                elif il in (6, 7):
+                    if il == 6:
+                        R["caL"] = np.abs(bLi) / np.sqrt(rL)
+                        R["caR"] = np.abs(bRi) / np.sqrt(rR)
+                    aL = aL + R["caL"] if il == 6 else aL - R["caL"]
+                    aR = aR + R["caR"] if il == 6 else aR - R["caR"]
+        else:
+            rho = R["rho"]
+            if il == 0:
+                vv = v[1] * v[1]
+                for c in range(2, nd + 1):
+                    vv = vv + v[c] * v[c]
+                c2 = (g - 1) * (R["h"] - HALF * vv)
+                c2 = _fmax(g * self.smallp / rho, c2)
+                pL = self.getpthermal(wL, ixC)
+                pR = self.getpthermal(wR, ixC)
+                R["dpc"] = (pR - pL) / c2
+                R["c"] = np.sqrt(c2)
+                R["dvc"] = (wR[(1 + idim,) + sl] / rR - wL[(1 + idim,) + sl] / rL) / R["c"]
+            c, dpc, dvc = R["c"], R["dpc"], R["dvc"]
+            if il == 0:
+                a = vi + c
+                jump = HALF * (dpc + rho * dvc)
+            elif il == 1:
+                a = vi - c
+                jump = HALF * (dpc - rho * dvc)
+            elif il == 2:
+                a = vi
+                jump = -dpc + rR - rL
+            else:
+                idir = il - 3
+                if idir >= idim:
+                    idir += 1
+                a = vi
+                jump = rho * (wR[(1 + idir,) + sl] / rR - wL[(1 + idir,) + sl] / rL)
+            if te in (abi.ENTROPY_HARTEN, abi.ENTROPY_POWELL):
+                uL = wL[(1 + idim,) + sl] / rL
+                uR = wR[(1 + idim,) + sl] / rR
+                if il in (0, 1):
+                    sL = np.sqrt(g * self.getpthermal(wL, ixC) / rL)
+                    sR = np.sqrt(g * self.getpthermal(wR, ixC) / rR)
+                    aL = uL + sL if il == 0 else uL - sL
+                    aR = uR + sR if il == 0 else uR - sR
+                else:
+                    aL, aR = uL, uR
+        if te == abi.ENTROPY_YEE:
+            smalla = np.full_like(a, self.p.entropycoef[il])
+        elif te == abi.ENTROPY_HARTEN:
+            smalla = _fmax(_fmax(ZERO, a - aL), aR - a)
+        elif te == abi.ENTROPY_POWELL:
+            smalla = _fmax(ZERO, TWO * (aR - aL))
+        elif te == abi.ENTROPY_RATIO:
+            a = np.where((aL < ZERO) & (aR > ZERO), a - 2 * aR * aL / (aR - aL), a)
+        return a, jump, smalla
+
+    def roe_rtimes(self, R, q, iw, il, idim):
+        """R(iw,il)*q: src/vacphys.mhdroe.t:284-449, src/vacphys.hdroe.t:144-215."""
+        g, nd, e, b0 = self.gamma, self.ndir, self.e_, self.b0
+        v = R["v"]
+        vi = v[1 + idim]
+        z = np.zeros_like(q)
+        if self.mhd:
+            idir, jdir = self.roe_dirs(idim)
+            B, sr = R["B"], R["sr"]
+            bi, bI, bJ = B[1 + idim], B[1 + idir], B[1 + jdir]
+            cf, cs, af, as_, cs2 = R["cf"], R["cs"], R["af"], R["as"], R["cs2"]
+            sgn = np.copysign(ONE, bi)
+            if iw == 0:
+                return [q * af, q * af, q * as_, q * as_, q, z, z, z][il]
+            if iw == e:
+                vv = v[1] * v[1]
+                for c in range(2, nd + 1):
+                    vv = vv + v[c] * v[c]
+                v2a2 = HALF * vv + (2 - g) / (g - 1) * cs2
+                if il < 6:
+                    bv = bI * v[1 + idir]
+                    if nd == 3:
+                        bv = bv + bJ * v[1 + jdir]
+                    bv = bv * sgn
+                else:
+                    bv = bJ * v[1 + idir] - bI * v[1 + jdir]
+                if il == 0:
+                    return q * (-as_ * cs * bv + af * (v2a2 + cf * (cf + vi)))
+                if il == 1:
+                    return q * (+as_ * cs * bv + af * (v2a2 + cf * (cf - vi)))
+                if il == 2:
+                    return q * (+af * cf * bv + as_ * (v2a2 + cs * (cs + vi)))
+                if il == 3:
+                    return q * (-af * cf * bv + as_ * (v2a2 + cs * (cs - vi)))
+                if il == 4:
+                    return q * HALF * vv
+                if il == 5:
+                    return q * bi if self.p.divbwave else z
+                return +q * bv if il == 6 else -q * bv
+            if iw <= nd:
+                vw = v[iw]
+                if iw == 1 + idim:
+                    return [q * af * (vw + cf), q * af * (vw - cf), q * as_ * (vw + cs),
+                            q * as_ * (vw - cs), q * vw, z, z, z][il]
+                bw = B[iw]
+                isI = iw == 1 + idir
+                if il == 0:
+                    return q * (af * vw - as_ * cs * bw * sgn)
+                if il == 1:
+                    return q * (af * vw + as_ * cs * bw * sgn)
+                if il == 2:
+                    return q * (as_ * vw + af * cf * bw * sgn)
+                if il == 3:
+                    return q * (as_ * vw - af * cf * bw * sgn)
+                if il == 4:
+                    return q * vw
+                if il == 5:
+                    return z
+                if il == 6:
+                    return +q * bJ if isI else -q * bI
+                return -q * bJ if isI else +q * bI
+            k = iw - b0
+            if k == 1 + idim:
+                return q if (il == 5 and self.p.divbwave) else z
+            bw = B[k]
+            if il in (0, 1):
+                return +q * as_ * np.sqrt(cs2) * bw / sr
+            if il in (2, 3):
+                return -q * af * np.sqrt(cs2) * bw / sr
+            if il in (4, 5):
+                return z
+            ss = np.copysign(sr, bi)
+            if k == 1 + idir:
+                return -q * bJ / ss
+            return +q * bI / ss
+        c, h = R["c"], R["h"]
+        shear = il >= 3
+        idir = -1
+        if shear:
+            idir = il - 3
+            if idir >= idim:
+                idir += 1
+        if iw == 0:
+            return z if shear else q
+        if iw == e:
+            if il == 0:
+                return q * (h + vi * c)
+            if il == 1:
+                return q * (h - vi * c)
+            if il == 2:
+                vv = v[1] * v[1]
+                for k in range(2, nd + 1):
+                    vv = vv + v[k] * v[k]
+                return q * HALF * vv
+            return q * v[1 + idir]
+        if iw == 1 + idim:
+            return [q * (vi + c), q * (vi - c), q * vi][il] if il < 3 else z
+        if shear:
+            return q if iw == 1 + idir else z
+        return q * v[iw]
+
+    def tvdlimit2(self, qdt, ixC, ixO, idim, wL, wR, wnew):
+        """src/vactvd.t:86-206 with getphi's TVD-MUSCL branch (:227-243)."""
+        sl = ixC.sl()
+        hxO = ixO.shifted(idim, -1)
+        R = self.roe_average(wL, wR, ixC, idim)
+        norm_dx = self.dx[(idim,) + sl] + self.dx[(idim,) + ixC.sl(idim, 1)]
+        for il in range(self.nw):
+            a, jump, smalla = self.roe_wave(R, wL, wR, ixC, il, idim)
+            te = self.p.typeentropy[il]
+            a = a * qdt * TWO / norm_dx
+            if te in (abi.ENTROPY_HARTEN, abi.ENTROPY_POWELL):
+                smalla = smalla * qdt * TWO / norm_dx
+            if il in (0, 1) and self.courantpar > ZERO and self.istep == self.nstep:
+                cm = np.abs(a).max()
+                if cm > ONE:
+                    self.nerror[2] += 1
+                if cm > SMALLDOUBLE:
+                    self.dtcourant[idim] = min(self.dtcourant[idim],
+                                               qdt * self.courantpar / cm)
+            if te in (abi.ENTROPY_NUL, abi.ENTROPY_RATIO):
+                phi = np.abs(a) * jump
+            else:
+                phi = np.where(np.abs(a) >= smalla, np.abs(a) * jump,
+                               HALF * (smalla + a * a / smalla) * jump)
+            for iw in range(self.nw):
+                F = np.zeros(self.nG)
+                F[sl] = self.roe_rtimes(R, phi, iw, il, idim) * QUARTER * (
+                    self.dvolume[ixC.sl(idim, 1)] + self.dvolume[sl])
+                self.addflux(-ONE, ixO, iw, idim, F, ixO, F, hxO, wnew)
+
     # ------------------------------------------------------------ schemes
     def hancock(self, qdt, ixO, d0, d1, wCT, wnew):
         for idim in range(d0, d1 + 1):
@@ -544,24 +910,26 @@ class NumpyVac:
             wRC = np.zeros_like(wCT)
             wRC[(slice(None),) + ixC.sl()] = wCT[(slice(None),) + ixC.sl(idim, 1)]
             wLC[(slice(None),) + ixC.sl()] = wCT[(slice(None),) + ixC.sl()]
-            if self.p.typefull != abi.TVDLF1:
+            tf = self.p.typefull
+            lf = tf in (abi.TVDLF, abi.TVDLF1)
+            if tf not in (abi.TVDLF1, abi.TVDMU1):
                 base = {abi.LIMITED_PREVIOUS: self.wold,
                         abi.LIMITED_PREDICTOR: wCT}.get(self.p.typelimited, wnew)
                 self.upwindLR(ixC, ixC, idim, base, wLC, wRC)
             A = (slice(None),) + ixC.sl()
-            wLC[A] = HALF * (wLC[A] + wRC[A])
-            cmax = np.zeros(self.nG)
-            cmax[ixC.sl()] = self.getcmax(wLC, ixC, idim, {})
-            nstep = 1 if self.p.typefull == abi.TVDLF1 else 2
-            if self.courantpar > ZERO and self.istep == nstep:
-                q = cmax[ixC.sl()] * TWO / (self.dx[(idim,) + ixC.sl()]
-                                            + self.dx[(idim,) + ixC.sl(idim, 1)])
-                cm = q.max()
-                if qdt * cm > ONE:
-                    self.nerror[2] += 1
-                if cm > SMALLDOUBLE:
-                    self.dtcourant[idim] = min(self.dtcourant[idim], self.courantpar / cm)
-            wLC[A] = 2 * wLC[A] - wRC[A]
+            if lf:
+                wLC[A] = HALF * (wLC[A] + wRC[A])
+                cmax = np.zeros(self.nG)
+                cmax[ixC.sl()] = self.getcmax(wLC, ixC, idim, {})
+                if self.courantpar > ZERO and self.istep == self.nstep:
+                    q = cmax[ixC.sl()] * TWO / (self.dx[(idim,) + ixC.sl()]
+                                                + self.dx[(idim,) + ixC.sl(idim, 1)])
+                    cm = q.max()
+                    if qdt * cm > ONE:
+                        self.nerror[2] += 1
+                    if cm > SMALLDOUBLE:
+                        self.dtcourant[idim] = min(self.dtcourant[idim], self.courantpar / cm)
+                wLC[A] = 2 * wLC[A] - wRC[A]
             vL = wLC[(1 + idim,) + ixC.sl()] / wLC[(0,) + ixC.sl()]
             vR = wRC[(1 + idim,) + ixC.sl()] / wRC[(0,) + ixC.sl()]
             for iw in range(self.nw):
@@ -571,17 +939,21 @@ class NumpyVac:
                     fL = fL + vL * wLC[(iw,) + ixC.sl()]
                     fR = fR + vR * wRC[(iw,) + ixC.sl()]
                 fL = HALF * (fL + fR)
-                fR = -cmax[ixC.sl()] * HALF * (wRC[(iw,) + ixC.sl()] - wLC[(iw,) + ixC.sl()])
-                fL = fL + fR
+                if lf:
+                    fR = -cmax[ixC.sl()] * HALF * (wRC[(iw,) + ixC.sl()] - wLC[(iw,) + ixC.sl()])
+                    fL = fL + fR
                 F = np.zeros(self.nG)
                 F[ixC.sl()] = fL
                 self.addflux(qdt, ixO, iw, idim, F, ixO, F, hxO, wnew)
+            if not lf:
+                with np.errstate(all="ignore"):
+                    self.tvdlimit2(qdt, ixC, ixO, idim, wLC, wRC, wnew)
         if self.p.sourceunsplit:
             self.addsource2(qdt * (d1 - d0 + ONE) / self.ndim, ixO, wCT, wnew)
 
     def advect(self, d0, d1):
         w1 = self.w.copy()
-        if self.p.typefull == abi.TVDLF1:  # typepred1='nul': onestep
+        if self.p.typefull in (abi.TVDLF1, abi.TVDMU1):  # typepred1='nul': onestep
             self.istep = 1
             self.tvdmusclf(self.dt, self.ixM, d0, d1, w1, self.w)
             self.getboundary(self.w)

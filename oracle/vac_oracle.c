@@ -53,6 +53,8 @@ typedef struct vo_state {
   double *wLC, *wRC, *fLC, *fRC, *vLC, *vRC, *cmaxC, *ldw, *dwC, *tmp,
       *tmp2, *divb, *csound2, *cfast2, *pp;
   double* cur[3];    /* current density components (resistive MHD) */
+  double* wroe;      /* Roe average (tvdmu) */
+  double* roe[22];   /* tvdlimit2 / Roe solver work arrays (ROE_* below) */
   double dtcourant[3];
   double dt, t, dtold, dtpar, courantpar, dtgrav;
   int it, itmin;
@@ -460,7 +462,8 @@ static void setnoflux(vo_state* s, int iw, int idim, box ixO, double* fR,
 
 /* addflux, src/vacgrid.t:596-741, Cartesian slab branch (:669-678), after
  * setnoflux (:639-640):
- * wnew(ix) -= qdt/dx(ix,idim)*(fRC(ixR)-fLC(ixL)) */
+ * wnew(ix) -= qdt/dx(ix,idim)*(fRC(ixR)-fLC(ixL)); for qdt<0 (dissipative
+ * flux, :707-717) wnew(ix) += (fRC(ixR)-fLC(ixL))/dvolume(ix) */
 static void addflux(vo_state* s, double qdt, box ixO, int iw, int idim,
                     double* fR, box ixR, double* fL, box ixL, double* wnew) {
   setnoflux(s, iw, idim, ixO, fR, ixR, fL, ixL);
@@ -469,6 +472,11 @@ static void addflux(vo_state* s, double qdt, box ixO, int iw, int idim,
   long oL = IDX(s, ixL.lo[0], ixL.lo[1], ixL.lo[2]) -
             IDX(s, ixO.lo[0], ixO.lo[1], ixO.lo[2]);
   double* wn = W(wnew, iw);
+  if (qdt < ZERO) {
+    const double* dv = s->dvolume;
+    FORBOX(ixO, ix) { wn[ix] = wn[ix] + (fR[ix + oR] - fL[ix + oL]) / dv[ix]; }
+    return;
+  }
   const double* dx = W(s->dx, idim);
   FORBOX(ixO, ix) { wn[ix] = wn[ix] - qdt / dx[ix] * (fR[ix + oR] - fL[ix + oL]); }
 }
@@ -850,6 +858,671 @@ static void getboundary(vo_state* s, double* w) {
   }
 }
 
+
+/* ------------------------------------------------------------ Roe solver */
+/* Work arrays of tvdlimit2 and the Roe solvers (allocated for tvdmu). */
+enum {
+  ROE_CF, ROE_CS, ROE_AF, ROE_AS, ROE_CS2, ROE_DP, ROE_RHODV, ROE_BDV,
+  ROE_BDB, ROE_AL, ROE_AR, ROE_CS2L, ROE_CS2R, ROE_CC2L, ROE_CC2R, ROE_A,
+  ROE_SMALLA, ROE_JUMP, ROE_PHI, ROE_RPHI, ROE_T1, ROE_T2, NROE
+};
+#define QUARTER 0.25
+
+/* Fortran SIGN(a,b): |a| with the sign of b */
+static double fsign(double a, double b) { return copysign(fabs(a), b); }
+
+/* idir, jdir of the MHD Roe solver (idir=idim+1-ndir*(idim/ndir), 1-based,
+ * src/vacphys.mhdroe.t:97,145-146), returned 0-based */
+static void roe_dirs(const vo_state* s, int idim, int* idir, int* jdir) {
+  const int nd = s->ndir;
+  const int i1 = idim + 1;
+  const int d1 = i1 + 1 - nd * (i1 / nd);
+  const int j1 = d1 + 1 - nd * (d1 / nd);
+  *idir = d1 - 1;
+  *jdir = j1 - 1;
+}
+
+/* average, src/vacphys.mhdroe.t:4-127: arithmetic means of rho, v, B, p;
+ * dp, rho*dv_idim, the sound, fast and slow speeds and their weights; then
+ * rho -> sqrt(rho), B_idir,B_jdir -> beta_idir,beta_jdir. */
+static void average_mhd(vo_state* s, const double* wL, const double* wR,
+                        box b, int idim, double* wroe) {
+  double** R = s->roe;
+  const double gamma = s->p.eqpar[0];
+  const int nd = s->ndir;
+  const double *rL = W(wL, s->rho_), *rR = W(wR, s->rho_);
+  double* rr = W(wroe, s->rho_);
+  FORBOX(b, ix) rr[ix] = HALF * (rL[ix] + rR[ix]);
+  for (int c = 1; c <= nd; c++) {
+    const double *mL = W(wL, s->m0_ + c), *mR = W(wR, s->m0_ + c);
+    const double *bL = W(wL, s->b0_ + c), *bR = W(wR, s->b0_ + c);
+    double *vr = W(wroe, s->m0_ + c), *br = W(wroe, s->b0_ + c);
+    FORBOX(b, ix) vr[ix] = HALF * (mL[ix] / rL[ix] + mR[ix] / rR[ix]);
+    FORBOX(b, ix) br[ix] = HALF * (bL[ix] + bR[ix]);
+  }
+  double *pL = R[ROE_AF], *pR = R[ROE_AS];
+  getpthermal(s, 1, wL, b, pL);
+  getpthermal(s, 1, wR, b, pR);
+  double* pr = W(wroe, s->e_);
+  FORBOX(b, ix) pr[ix] = HALF * (pL[ix] + pR[ix]);
+  double* dp = R[ROE_DP];
+  if (s->p.useprimitive) {
+    FORBOX(b, ix) dp[ix] = pR[ix] - pL[ix];
+  } else {
+    const double *eL = W(wL, s->e_), *eR = W(wR, s->e_);
+    FORBOX(b, ix) {
+      double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      for (int c = 1; c <= nd; c++) {
+        const double v = W(wroe, s->m0_ + c)[ix];
+        const double dm = W(wR, s->m0_ + c)[ix] - W(wL, s->m0_ + c)[ix];
+        const double bR = W(wR, s->b0_ + c)[ix], bL = W(wL, s->b0_ + c)[ix];
+        s1 = (c == 1) ? v * dm : s1 + v * dm;
+        s2 = (c == 1) ? v * v : s2 + v * v;
+        s3 = (c == 1) ? bR * bR - bL * bL : s3 + bR * bR - bL * bL;
+      }
+      dp[ix] = (gamma - 1) * (eR[ix] - eL[ix] - s1 +
+                              HALF * s2 * (rR[ix] - rL[ix]) - HALF * s3);
+    }
+  }
+  {
+    const double *mL = W(wL, s->m0_ + idim + 1), *mR = W(wR, s->m0_ + idim + 1);
+    const double* vr = W(wroe, s->m0_ + idim + 1);
+    double* rhodv = R[ROE_RHODV];
+    FORBOX(b, ix) rhodv[ix] = mR[ix] - mL[ix] - vr[ix] * (rR[ix] - rL[ix]);
+  }
+  double *cs2 = R[ROE_CS2], *cf = R[ROE_CF], *cs = R[ROE_CS];
+  double *af = R[ROE_AF], *as = R[ROE_AS];
+  FORBOX(b, ix) cs2[ix] = gamma * pr[ix] / rr[ix];
+  FORBOX(b, ix) {
+    double bb = 0.0;
+    for (int c = 1; c <= nd; c++) {
+      const double bc = W(wroe, s->b0_ + c)[ix];
+      bb = (c == 1) ? bc * bc : bb + bc * bc;
+    }
+    cf[ix] = bb / rr[ix] + cs2[ix];
+  }
+  const double* bi = W(wroe, s->b0_ + idim + 1);
+  FORBOX(b, ix) {
+    cs[ix] = fmax2(ZERO, HALF * (cf[ix] - sqrt(cf[ix] * cf[ix] -
+                                               4.0 * cs2[ix] *
+                                                   (bi[ix] * bi[ix]) /
+                                                   rr[ix])));
+  }
+  FORBOX(b, ix) cf[ix] = cf[ix] - cs[ix];
+  FORBOX(b, ix) af[ix] = (cs2[ix] - cs[ix]) / (cf[ix] - cs[ix]);
+  FORBOX(b, ix) af[ix] = fmin2(ONE, fmax2(af[ix], ZERO));
+  FORBOX(b, ix) as[ix] = sqrt(ONE - af[ix]);
+  FORBOX(b, ix) af[ix] = sqrt(af[ix]);
+  FORBOX(b, ix) cf[ix] = sqrt(cf[ix]);
+  FORBOX(b, ix) cs[ix] = sqrt(cs[ix]);
+  FORBOX(b, ix) rr[ix] = sqrt(rr[ix]);
+  double* bw = W(wroe, s->b0_ + idim + 1);
+  FORBOX(b, ix) if (fabs(bw[ix]) < SMALLDOUBLE) bw[ix] = SMALLDOUBLE;
+  int idir, jdir;
+  roe_dirs(s, idim, &idir, &jdir);
+  double* bI = W(wroe, s->b0_ + idir + 1);
+  if (nd == 2) {
+    FORBOX(b, ix) bI[ix] = bI[ix] >= ZERO ? ONE : -ONE;
+  } else {
+    double* bJ = W(wroe, s->b0_ + jdir + 1);
+    double* t = R[ROE_T1];
+    FORBOX(b, ix) t[ix] = sqrt(bI[ix] * bI[ix] + bJ[ix] * bJ[ix]);
+    FORBOX(b, ix) {
+      if (t[ix] > SMALLDOUBLE) {
+        bI[ix] = bI[ix] / t[ix];
+        bJ[ix] = bJ[ix] / t[ix];
+      } else {
+        bI[ix] = sqrt(HALF);
+        bJ[ix] = sqrt(HALF);
+      }
+    }
+  }
+}
+
+/* average, src/vacphys.hdroe.t:4-45: sqrt(rho) weighted Roe average;
+ * rho -> sqrt(rhoL*rhoR), m -> v, e -> enthalpy h. */
+static void average_hd(vo_state* s, const double* wL, const double* wR, box b,
+                       double* wroe) {
+  double** R = s->roe;
+  double *t = R[ROE_T1], *t2 = R[ROE_T2];
+  const double *rL = W(wL, s->rho_), *rR = W(wR, s->rho_);
+  double* rr = W(wroe, s->rho_);
+  FORBOX(b, ix) t[ix] = sqrt(rL[ix]);
+  FORBOX(b, ix) t2[ix] = sqrt(rR[ix]);
+  FORBOX(b, ix) rr[ix] = t[ix] * t2[ix];
+  FORBOX(b, ix) t[ix] = t[ix] / t2[ix];
+  for (int c = 1; c <= s->ndir; c++) {
+    const double *mL = W(wL, s->m0_ + c), *mR = W(wR, s->m0_ + c);
+    double* vr = W(wroe, s->m0_ + c);
+    FORBOX(b, ix) vr[ix] = (mL[ix] / rL[ix] * t[ix] + mR[ix] / rR[ix]) / (1 + t[ix]);
+  }
+  double* h = W(wroe, s->e_);
+  getpthermal(s, 1, wL, b, t2);
+  FORBOX(b, ix) h[ix] = (t2[ix] + W(wL, s->e_)[ix]) / rL[ix];
+  getpthermal(s, 1, wR, b, t2);
+  FORBOX(b, ix) t2[ix] = (t2[ix] + W(wR, s->e_)[ix]) / rR[ix];
+  FORBOX(b, ix) h[ix] = (h[ix] * t[ix] + t2[ix]) / (1 + t[ix]);
+}
+
+/* entropyfix, src/vactvd.t:422-451 */
+static void entropyfix(vo_state* s, box b, int il, const double* aL,
+                       const double* aR, double* a, double* smalla) {
+  switch (s->p.typeentropy[il]) {
+    case VACGPU_ENTROPY_HARTEN:
+      FORBOX(b, ix) smalla[ix] = fmax2(fmax2(ZERO, a[ix] - aL[ix]), aR[ix] - a[ix]);
+      break;
+    case VACGPU_ENTROPY_POWELL:
+      FORBOX(b, ix) smalla[ix] = fmax2(ZERO, TWO * (aR[ix] - aL[ix]));
+      break;
+    case VACGPU_ENTROPY_RATIO:
+      FORBOX(b, ix) {
+        if (aL[ix] < ZERO && aR[ix] > ZERO)
+          a[ix] = a[ix] - 2 * aR[ix] * aL[ix] / (aR[ix] - aL[ix]);
+      }
+      break;
+    default:
+      break;
+  }
+}
+
+/* geteigenjump, src/vacphys.mhdroe.t:130-281: eigenvalue a, jump L*dw and
+ * the entropy-fix bound of wave il (0-based: fastRW, fastLW, slowRW, slowLW,
+ * entroW, diverW, alfvRW, alfvLW). */
+static void geteigenjump_mhd(vo_state* s, const double* wL, const double* wR,
+                             const double* wroe, box b, int il, int idim) {
+  double** R = s->roe;
+  const int nd = s->ndir;
+  int idir, jdir;
+  roe_dirs(s, idim, &idir, &jdir);
+  const double *rL = W(wL, s->rho_), *rR = W(wR, s->rho_);
+  const double* sr = W(wroe, s->rho_);
+  const double* bi = W(wroe, s->b0_ + idim + 1);
+  const double* bI = W(wroe, s->b0_ + idir + 1);
+  const double* bJ = W(wroe, s->b0_ + jdir + 1);
+  const double *mLI = W(wL, s->m0_ + idir + 1), *mRI = W(wR, s->m0_ + idir + 1);
+  const double *mLJ = W(wL, s->m0_ + jdir + 1), *mRJ = W(wR, s->m0_ + jdir + 1);
+  const double *bLI = W(wL, s->b0_ + idir + 1), *bRI = W(wR, s->b0_ + idir + 1);
+  const double *bLJ = W(wL, s->b0_ + jdir + 1), *bRJ = W(wR, s->b0_ + jdir + 1);
+  double *bdv = R[ROE_BDV], *bdb = R[ROE_BDB];
+  const double *cf = R[ROE_CF], *cs = R[ROE_CS], *af = R[ROE_AF],
+               *as = R[ROE_AS], *cs2 = R[ROE_CS2], *dp = R[ROE_DP],
+               *rhodv = R[ROE_RHODV];
+  if (il == 0) {
+    FORBOX(b, ix) bdv[ix] = bI[ix] * (mRI[ix] / rR[ix] - mLI[ix] / rL[ix]);
+    if (nd == 3)
+      FORBOX(b, ix) bdv[ix] = bdv[ix] + bJ[ix] * (mRJ[ix] / rR[ix] - mLJ[ix] / rL[ix]);
+    FORBOX(b, ix) bdv[ix] = bdv[ix] * fsign(sr[ix] * sr[ix], bi[ix]);
+    FORBOX(b, ix) bdb[ix] = bI[ix] * (bRI[ix] - bLI[ix]);
+    if (nd == 3) FORBOX(b, ix) bdb[ix] = bdb[ix] + bJ[ix] * (bRJ[ix] - bLJ[ix]);
+    FORBOX(b, ix) bdb[ix] = bdb[ix] * sqrt(cs2[ix]) * sr[ix];
+  }
+  if (il == 6) {
+    FORBOX(b, ix) {
+      bdv[ix] = bJ[ix] * (mRI[ix] / rR[ix] - mLI[ix] / rL[ix]) -
+                bI[ix] * (mRJ[ix] / rR[ix] - mLJ[ix] / rL[ix]);
+    }
+    FORBOX(b, ix) bdb[ix] = bJ[ix] * (bRI[ix] - bLI[ix]) - bI[ix] * (bRJ[ix] - bLJ[ix]);
+    FORBOX(b, ix) bdv[ix] = bdv[ix] * HALF * (sr[ix] * sr[ix]);
+    FORBOX(b, ix) bdb[ix] = bdb[ix] * HALF * fsign(sr[ix], bi[ix]);
+  }
+  const double* v = W(wroe, s->m0_ + idim + 1);
+  double *a = R[ROE_A], *jump = R[ROE_JUMP];
+  switch (il) {
+    case 0:
+      FORBOX(b, ix) a[ix] = v[ix] + cf[ix];
+      FORBOX(b, ix) {
+        jump[ix] = HALF / cs2[ix] *
+                   (af[ix] * (+cf[ix] * rhodv[ix] + dp[ix]) +
+                    as[ix] * (-cs[ix] * bdv[ix] + bdb[ix]));
+      }
+      break;
+    case 1:
+      FORBOX(b, ix) a[ix] = v[ix] - cf[ix];
+      FORBOX(b, ix) {
+        jump[ix] = HALF / cs2[ix] *
+                   (af[ix] * (-cf[ix] * rhodv[ix] + dp[ix]) +
+                    as[ix] * (+cs[ix] * bdv[ix] + bdb[ix]));
+      }
+      break;
+    case 2:
+      FORBOX(b, ix) a[ix] = v[ix] + cs[ix];
+      FORBOX(b, ix) {
+        jump[ix] = HALF / cs2[ix] *
+                   (as[ix] * (+cs[ix] * rhodv[ix] + dp[ix]) +
+                    af[ix] * (+cf[ix] * bdv[ix] - bdb[ix]));
+      }
+      break;
+    case 3:
+      FORBOX(b, ix) a[ix] = v[ix] - cs[ix];
+      FORBOX(b, ix) {
+        jump[ix] = HALF / cs2[ix] *
+                   (as[ix] * (-cs[ix] * rhodv[ix] + dp[ix]) +
+                    af[ix] * (-cf[ix] * bdv[ix] - bdb[ix]));
+      }
+      break;
+    case 4:
+      FORBOX(b, ix) a[ix] = v[ix];
+      FORBOX(b, ix) jump[ix] = rR[ix] - rL[ix] - dp[ix] / cs2[ix];
+      break;
+    case 5:
+      if (s->p.divbwave) {
+        const double *bLi = W(wL, s->b0_ + idim + 1), *bRi = W(wR, s->b0_ + idim + 1);
+        FORBOX(b, ix) a[ix] = v[ix];
+        FORBOX(b, ix) jump[ix] = bRi[ix] - bLi[ix];
+      } else {
+        FORBOX(b, ix) a[ix] = ZERO;
+        FORBOX(b, ix) jump[ix] = ZERO;
+      }
+      break;
+    case 6:
+      FORBOX(b, ix) a[ix] = v[ix] + fabs(bi[ix]) / sr[ix];
+      FORBOX(b, ix) jump[ix] = +bdv[ix] - bdb[ix];
+      break;
+    case 7:
+      FORBOX(b, ix) a[ix] = v[ix] - fabs(bi[ix]) / sr[ix];
+      FORBOX(b, ix) jump[ix] = -bdv[ix] - bdb[ix];
+      break;
+  }
+  const int te = s->p.typeentropy[il];
+  double *aL = R[ROE_AL], *aR = R[ROE_AR], *smalla = R[ROE_SMALLA];
+  if (te == VACGPU_ENTROPY_YEE) {
+    const double c = s->p.entropycoef[il];
+    FORBOX(b, ix) smalla[ix] = c;
+  } else if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL ||
+             te == VACGPU_ENTROPY_RATIO) {
+    const double *mLi = W(wL, s->m0_ + idim + 1), *mRi = W(wR, s->m0_ + idim + 1);
+    const double *bLi = W(wL, s->b0_ + idim + 1), *bRi = W(wR, s->b0_ + idim + 1);
+    double *cs2L = R[ROE_CS2L], *cs2R = R[ROE_CS2R];
+    double *ccL = R[ROE_CC2L], *ccR = R[ROE_CC2R];
+    FORBOX(b, ix) aL[ix] = mLi[ix] / rL[ix];
+    FORBOX(b, ix) aR[ix] = mRi[ix] / rR[ix];
+    switch (il) {
+      case 0:
+        getcsound2(s, wL, b, cs2L);
+        getcsound2(s, wR, b, cs2R);
+        FORBOX(b, ix) {
+          double bb = 0.0;
+          for (int c = 1; c <= nd; c++) {
+            const double bc = W(wL, s->b0_ + c)[ix];
+            bb = (c == 1) ? bc * bc : bb + bc * bc;
+          }
+          ccL[ix] = cs2L[ix] + bb / rL[ix];
+        }
+        FORBOX(b, ix) {
+          double bb = 0.0;
+          for (int c = 1; c <= nd; c++) {
+            const double bc = W(wR, s->b0_ + c)[ix];
+            bb = (c == 1) ? bc * bc : bb + bc * bc;
+          }
+          ccR[ix] = cs2R[ix] + bb / rR[ix];
+        }
+        FORBOX(b, ix) {
+          cs2L[ix] = sqrt(ccL[ix] * ccL[ix] -
+                          4 * cs2L[ix] * (bLi[ix] * bLi[ix]) / rL[ix]);
+        }
+        FORBOX(b, ix) {
+          cs2R[ix] = sqrt(ccR[ix] * ccR[ix] -
+                          4 * cs2R[ix] * (bRi[ix] * bRi[ix]) / rR[ix]);
+        }
+        FORBOX(b, ix) aL[ix] = aL[ix] + sqrt(HALF * (ccL[ix] + cs2L[ix]));
+        FORBOX(b, ix) aR[ix] = aR[ix] + sqrt(HALF * (ccR[ix] + cs2R[ix]));
+        break;
+      case 1:
+        FORBOX(b, ix) aL[ix] = aL[ix] - sqrt(HALF * (ccL[ix] + cs2L[ix]));
+        FORBOX(b, ix) aR[ix] = aR[ix] - sqrt(HALF * (ccR[ix] + cs2R[ix]));
+        break;
+      case 2:
+        FORBOX(b, ix) aL[ix] = aL[ix] + sqrt(HALF * (ccL[ix] - cs2L[ix]));
+        FORBOX(b, ix) aR[ix] = aR[ix] + sqrt(HALF * (ccR[ix] - cs2R[ix]));
+        break;
+      case 3:
+        FORBOX(b, ix) aL[ix] = aL[ix] - sqrt(HALF * (ccL[ix] - cs2L[ix]));
+        FORBOX(b, ix) aR[ix] = aR[ix] - sqrt(HALF * (ccR[ix] - cs2R[ix]));
+        break;
+      case 6:
+        FORBOX(b, ix) ccL[ix] = fabs(bLi[ix]) / sqrt(rL[ix]);
+        FORBOX(b, ix) ccR[ix] = fabs(bRi[ix]) / sqrt(rR[ix]);
+        FORBOX(b, ix) aL[ix] = aL[ix] + ccL[ix];
+        FORBOX(b, ix) aR[ix] = aR[ix] + ccR[ix];
+        break;
+      case 7:
+        FORBOX(b, ix) aL[ix] = aL[ix] - ccL[ix];
+        FORBOX(b, ix) aR[ix] = aR[ix] - ccR[ix];
+        break;
+      default:
+        break;
+    }
+  }
+  entropyfix(s, b, il, aL, aR, a, smalla);
+}
+
+/* geteigenjump, src/vacphys.hdroe.t:48-141 (0-based il: soundRW, soundLW,
+ * entropW, then the shear waves) */
+static void geteigenjump_hd(vo_state* s, const double* wL, const double* wR,
+                            const double* wroe, box b, int il, int idim) {
+  double** R = s->roe;
+  const double gamma = s->p.eqpar[0];
+  const double *rL = W(wL, s->rho_), *rR = W(wR, s->rho_);
+  const double* rr = W(wroe, s->rho_);
+  const double* v = W(wroe, s->m0_ + idim + 1);
+  const double *mLi = W(wL, s->m0_ + idim + 1), *mRi = W(wR, s->m0_ + idim + 1);
+  double *c = R[ROE_CS], *dpc = R[ROE_DP], *dvc = R[ROE_RHODV];
+  double *t = R[ROE_T1], *t2 = R[ROE_T2];
+  if (il == 0) {
+    const double* h = W(wroe, s->e_);
+    FORBOX(b, ix) {
+      double vv = 0.0;
+      for (int k = 1; k <= s->ndir; k++) {
+        const double vk = W(wroe, s->m0_ + k)[ix];
+        vv = (k == 1) ? vk * vk : vv + vk * vk;
+      }
+      c[ix] = (gamma - 1) * (h[ix] - HALF * vv);
+    }
+    FORBOX(b, ix) c[ix] = fmax2(gamma * s->smallp / rr[ix], c[ix]);
+    getpthermal(s, 1, wL, b, t);
+    getpthermal(s, 1, wR, b, t2);
+    FORBOX(b, ix) dpc[ix] = (t2[ix] - t[ix]) / c[ix];
+    FORBOX(b, ix) c[ix] = sqrt(c[ix]);
+    FORBOX(b, ix) dvc[ix] = (mRi[ix] / rR[ix] - mLi[ix] / rL[ix]) / c[ix];
+  }
+  double *a = R[ROE_A], *jump = R[ROE_JUMP];
+  int idir = -1;
+  switch (il) {
+    case 0:
+      FORBOX(b, ix) a[ix] = v[ix] + c[ix];
+      FORBOX(b, ix) jump[ix] = HALF * (dpc[ix] + rr[ix] * dvc[ix]);
+      break;
+    case 1:
+      FORBOX(b, ix) a[ix] = v[ix] - c[ix];
+      FORBOX(b, ix) jump[ix] = HALF * (dpc[ix] - rr[ix] * dvc[ix]);
+      break;
+    case 2:
+      FORBOX(b, ix) a[ix] = v[ix];
+      FORBOX(b, ix) jump[ix] = -dpc[ix] + rR[ix] - rL[ix];
+      break;
+    default: {
+      idir = il - 3;                /* 0-based il-shearW0_-1 */
+      if (idir >= idim) idir++;
+      const double *mLd = W(wL, s->m0_ + idir + 1), *mRd = W(wR, s->m0_ + idir + 1);
+      FORBOX(b, ix) a[ix] = v[ix];
+      FORBOX(b, ix) jump[ix] = rr[ix] * (mRd[ix] / rR[ix] - mLd[ix] / rL[ix]);
+    }
+  }
+  const int te = s->p.typeentropy[il];
+  double *aL = R[ROE_AL], *aR = R[ROE_AR], *smalla = R[ROE_SMALLA];
+  if (te == VACGPU_ENTROPY_YEE) {
+    const double cy = s->p.entropycoef[il];
+    FORBOX(b, ix) smalla[ix] = cy;
+  } else if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL) {
+    if (il == 0 || il == 1) {
+      const double sg = il == 0 ? ONE : -ONE;
+      getpthermal(s, 1, wL, b, aL);
+      FORBOX(b, ix) aL[ix] = mLi[ix] / rL[ix] + sg * sqrt(gamma * aL[ix] / rL[ix]);
+      getpthermal(s, 1, wR, b, aR);
+      FORBOX(b, ix) aR[ix] = mRi[ix] / rR[ix] + sg * sqrt(gamma * aR[ix] / rR[ix]);
+    } else {
+      FORBOX(b, ix) aL[ix] = mLi[ix] / rL[ix];
+      FORBOX(b, ix) aR[ix] = mRi[ix] / rR[ix];
+    }
+  }
+  entropyfix(s, b, il, aL, aR, a, smalla);
+}
+
+/* rtimes, src/vacphys.mhdroe.t:284-449: rq = R(iw,il)*q at the Roe state */
+static void rtimes_mhd(vo_state* s, const double* q, const double* wroe,
+                       box b, int iw, int il, int idim, double* rq) {
+  double** R = s->roe;
+  const double gamma = s->p.eqpar[0];
+  const int nd = s->ndir;
+  int idir, jdir;
+  roe_dirs(s, idim, &idir, &jdir);
+  const double *cf = R[ROE_CF], *cs = R[ROE_CS], *af = R[ROE_AF],
+               *as = R[ROE_AS], *cs2 = R[ROE_CS2];
+  const double* sr = W(wroe, s->rho_);
+  const double* bi = W(wroe, s->b0_ + idim + 1);
+  const double* bI = W(wroe, s->b0_ + idir + 1);
+  const double* bJ = W(wroe, s->b0_ + jdir + 1);
+  const double* v = W(wroe, s->m0_ + idim + 1);
+  const double* vI = W(wroe, s->m0_ + idir + 1);
+  const double* vJ = W(wroe, s->m0_ + jdir + 1);
+  if (iw == s->rho_) {
+    switch (il) {
+      case 0: case 1: FORBOX(b, ix) rq[ix] = q[ix] * af[ix]; break;
+      case 2: case 3: FORBOX(b, ix) rq[ix] = q[ix] * as[ix]; break;
+      case 4: FORBOX(b, ix) rq[ix] = q[ix]; break;
+      default: FORBOX(b, ix) rq[ix] = ZERO; break;
+    }
+  } else if (iw == s->e_) {
+    FORBOX(b, ix) {
+      double vv = 0.0;
+      for (int c = 1; c <= nd; c++) {
+        const double vc = W(wroe, s->m0_ + c)[ix];
+        vv = (c == 1) ? vc * vc : vv + vc * vc;
+      }
+      /* v2a2 and bv of the fast/slow waves (:310-327), bv of the Alfven
+       * waves (:328-332) */
+      const double v2a2 = HALF * vv + (2 - gamma) / (gamma - 1) * cs2[ix];
+      double bv;
+      if (il < 6) {
+        bv = bI[ix] * vI[ix];
+        if (nd == 3) bv = bv + bJ[ix] * vJ[ix];
+        bv = bv * fsign(ONE, bi[ix]);
+      } else {
+        bv = bJ[ix] * vI[ix] - bI[ix] * vJ[ix];
+      }
+      switch (il) {
+        case 0:
+          rq[ix] = q[ix] * (-as[ix] * cs[ix] * bv +
+                            af[ix] * (v2a2 + cf[ix] * (cf[ix] + v[ix])));
+          break;
+        case 1:
+          rq[ix] = q[ix] * (+as[ix] * cs[ix] * bv +
+                            af[ix] * (v2a2 + cf[ix] * (cf[ix] - v[ix])));
+          break;
+        case 2:
+          rq[ix] = q[ix] * (+af[ix] * cf[ix] * bv +
+                            as[ix] * (v2a2 + cs[ix] * (cs[ix] + v[ix])));
+          break;
+        case 3:
+          rq[ix] = q[ix] * (-af[ix] * cf[ix] * bv +
+                            as[ix] * (v2a2 + cs[ix] * (cs[ix] - v[ix])));
+          break;
+        case 4:
+          rq[ix] = q[ix] * HALF * vv;
+          break;
+        case 5:
+          rq[ix] = s->p.divbwave ? q[ix] * bi[ix] : ZERO;
+          break;
+        case 6:
+          rq[ix] = +q[ix] * bv;
+          break;
+        default:
+          rq[ix] = -q[ix] * bv;
+          break;
+      }
+    }
+  } else if (iw <= s->m0_ + nd) {
+    const double* vw = W(wroe, iw);
+    if (iw == s->m0_ + idim + 1) {
+      switch (il) {
+        case 0: FORBOX(b, ix) rq[ix] = q[ix] * af[ix] * (vw[ix] + cf[ix]); break;
+        case 1: FORBOX(b, ix) rq[ix] = q[ix] * af[ix] * (vw[ix] - cf[ix]); break;
+        case 2: FORBOX(b, ix) rq[ix] = q[ix] * as[ix] * (vw[ix] + cs[ix]); break;
+        case 3: FORBOX(b, ix) rq[ix] = q[ix] * as[ix] * (vw[ix] - cs[ix]); break;
+        case 4: FORBOX(b, ix) rq[ix] = q[ix] * vw[ix]; break;
+        default: FORBOX(b, ix) rq[ix] = ZERO; break;
+      }
+    } else {
+      const double* bw = W(wroe, s->b0_ - s->m0_ + iw);
+      const int isI = iw == s->m0_ + idir + 1;
+      switch (il) {
+        case 0:
+          FORBOX(b, ix) rq[ix] = q[ix] * (af[ix] * vw[ix] - as[ix] * cs[ix] * bw[ix] * fsign(ONE, bi[ix]));
+          break;
+        case 1:
+          FORBOX(b, ix) rq[ix] = q[ix] * (af[ix] * vw[ix] + as[ix] * cs[ix] * bw[ix] * fsign(ONE, bi[ix]));
+          break;
+        case 2:
+          FORBOX(b, ix) rq[ix] = q[ix] * (as[ix] * vw[ix] + af[ix] * cf[ix] * bw[ix] * fsign(ONE, bi[ix]));
+          break;
+        case 3:
+          FORBOX(b, ix) rq[ix] = q[ix] * (as[ix] * vw[ix] - af[ix] * cf[ix] * bw[ix] * fsign(ONE, bi[ix]));
+          break;
+        case 4:
+          FORBOX(b, ix) rq[ix] = q[ix] * vw[ix];
+          break;
+        case 5:
+          FORBOX(b, ix) rq[ix] = ZERO;
+          break;
+        case 6:
+          if (isI) FORBOX(b, ix) rq[ix] = +q[ix] * bJ[ix];
+          else FORBOX(b, ix) rq[ix] = -q[ix] * bI[ix];
+          break;
+        default:
+          if (isI) FORBOX(b, ix) rq[ix] = -q[ix] * bJ[ix];
+          else FORBOX(b, ix) rq[ix] = +q[ix] * bI[ix];
+          break;
+      }
+    }
+  } else {
+    if (iw == s->b0_ + idim + 1) {
+      if (il == 5 && s->p.divbwave) FORBOX(b, ix) rq[ix] = q[ix];
+      else FORBOX(b, ix) rq[ix] = ZERO;
+    } else {
+      const double* bw = W(wroe, iw);
+      const int isI = iw == s->b0_ + idir + 1;
+      switch (il) {
+        case 0: case 1:
+          FORBOX(b, ix) rq[ix] = +q[ix] * as[ix] * sqrt(cs2[ix]) * bw[ix] / sr[ix];
+          break;
+        case 2: case 3:
+          FORBOX(b, ix) rq[ix] = -q[ix] * af[ix] * sqrt(cs2[ix]) * bw[ix] / sr[ix];
+          break;
+        case 4: case 5:
+          FORBOX(b, ix) rq[ix] = ZERO;
+          break;
+        default:
+          if (isI) FORBOX(b, ix) rq[ix] = -q[ix] * bJ[ix] / fsign(sr[ix], bi[ix]);
+          else FORBOX(b, ix) rq[ix] = +q[ix] * bI[ix] / fsign(sr[ix], bi[ix]);
+          break;
+      }
+    }
+  }
+}
+
+/* rtimes, src/vacphys.hdroe.t:144-215 */
+static void rtimes_hd(vo_state* s, const double* q, const double* wroe, box b,
+                      int iw, int il, int idim, double* rq) {
+  const double* c = s->roe[ROE_CS];
+  const int shear = il >= 3;
+  int idir = -1;
+  if (shear) {
+    idir = il - 3;
+    if (idir >= idim) idir++;
+  }
+  const double* h = W(wroe, s->e_);
+  const double* v = W(wroe, s->m0_ + idim + 1);
+  if (iw == s->rho_) {
+    if (shear) FORBOX(b, ix) rq[ix] = ZERO;
+    else FORBOX(b, ix) rq[ix] = q[ix];
+  } else if (iw == s->e_) {
+    switch (il) {
+      case 0: FORBOX(b, ix) rq[ix] = q[ix] * (h[ix] + v[ix] * c[ix]); break;
+      case 1: FORBOX(b, ix) rq[ix] = q[ix] * (h[ix] - v[ix] * c[ix]); break;
+      case 2:
+        FORBOX(b, ix) {
+          double vv = 0.0;
+          for (int k = 1; k <= s->ndir; k++) {
+            const double vk = W(wroe, s->m0_ + k)[ix];
+            vv = (k == 1) ? vk * vk : vv + vk * vk;
+          }
+          rq[ix] = q[ix] * HALF * vv;
+        }
+        break;
+      default: {
+        const double* vd = W(wroe, s->m0_ + idir + 1);
+        FORBOX(b, ix) rq[ix] = q[ix] * vd[ix];
+      }
+    }
+  } else if (iw == s->m0_ + idim + 1) {
+    switch (il) {
+      case 0: FORBOX(b, ix) rq[ix] = q[ix] * (v[ix] + c[ix]); break;
+      case 1: FORBOX(b, ix) rq[ix] = q[ix] * (v[ix] - c[ix]); break;
+      case 2: FORBOX(b, ix) rq[ix] = q[ix] * v[ix]; break;
+      default: FORBOX(b, ix) rq[ix] = ZERO; break;
+    }
+  } else {
+    if (shear) {
+      if (iw == s->m0_ + idir + 1) FORBOX(b, ix) rq[ix] = q[ix];
+      else FORBOX(b, ix) rq[ix] = ZERO;
+    } else {
+      const double* vw = W(wroe, iw);
+      FORBOX(b, ix) rq[ix] = q[ix] * vw[ix];
+    }
+  }
+}
+
+/* tvdlimit2, src/vactvd.t:86-206, with getphi's TVD-MUSCL branch
+ * (src/vactvd.t:227-243): for each characteristic wave il, the dissipative
+ * flux R(iw,il)*phi(il)*(dvolume(i)+dvolume(j))/4 enters wnew through
+ * addflux(-1) (wnew += (F(ix)-F(ix-1))/dvolume). */
+static void tvdlimit2(vo_state* s, double qdt, box ixC, box ixO, int idim,
+                      const double* wL, const double* wR, double* wnew) {
+  double** R = s->roe;
+  box hxO = shift(ixO, idim, -1);
+  const long sh = s->st[idim];
+  if (s->mhd)
+    average_mhd(s, wL, wR, ixC, idim, s->wroe);
+  else
+    average_hd(s, wL, wR, ixC, s->wroe);
+  const double* dx = W(s->dx, idim);
+  const double* dv = s->dvolume;
+  for (int il = 0; il < s->nw; il++) {
+    if (s->mhd)
+      geteigenjump_mhd(s, wL, wR, s->wroe, ixC, il, idim);
+    else
+      geteigenjump_hd(s, wL, wR, s->wroe, ixC, il, idim);
+    double *a = R[ROE_A], *smalla = R[ROE_SMALLA], *jump = R[ROE_JUMP];
+    double *phi = R[ROE_PHI], *rphi = R[ROE_RPHI];
+    const int te = s->p.typeentropy[il];
+    FORBOX(ixC, ix) a[ix] = a[ix] * qdt * TWO / (dx[ix] + dx[ix + sh]);
+    if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL)
+      FORBOX(ixC, ix) smalla[ix] = smalla[ix] * qdt * TWO / (dx[ix] + dx[ix + sh]);
+    if ((il == 0 || il == 1) && s->courantpar > ZERO && s->istep == s->nstep) {
+      double courantmax = 0.0;
+      int first = 1;
+      FORBOX_SEQ(ixC, ix) {
+        const double q = fabs(a[ix]);
+        if (first || q > courantmax) courantmax = q;
+        first = 0;
+      }
+      if (courantmax > ONE) s->nerror[2]++;
+      if (courantmax > SMALLDOUBLE) {
+        const double c = qdt * s->courantpar / courantmax;
+        if (c < s->dtcourant[idim]) s->dtcourant[idim] = c;
+      }
+    }
+    if (te == VACGPU_ENTROPY_NUL || te == VACGPU_ENTROPY_RATIO) {
+      FORBOX(ixC, ix) phi[ix] = fabs(a[ix]) * jump[ix];
+    } else {
+      FORBOX(ixC, ix) {
+        if (fabs(a[ix]) >= smalla[ix])
+          phi[ix] = fabs(a[ix]) * jump[ix];
+        else
+          phi[ix] = HALF * (smalla[ix] + a[ix] * a[ix] / smalla[ix]) * jump[ix];
+      }
+    }
+    for (int iw = 0; iw < s->nw; iw++) {
+      if (s->mhd)
+        rtimes_mhd(s, phi, s->wroe, ixC, iw, il, idim, rphi);
+      else
+        rtimes_hd(s, phi, s->wroe, ixC, iw, il, idim, rphi);
+      FORBOX(ixC, ix) rphi[ix] = rphi[ix] * QUARTER * (dv[ix + sh] + dv[ix]);
+      addflux(s, -ONE, ixO, iw, idim, rphi, ixO, rphi, hxO, wnew);
+    }
+  }
+}
+
 /* ---------------------------------------------------------------- schemes */
 
 /* hancock, src/vactvdlf.t:5-89 */
@@ -884,10 +1557,13 @@ static void hancock(vo_state* s, double qdt, box ixO, int idimmin,
     addsource2(s, qdt * (idimmax - idimmin + ONE) / s->ndim, ixO, wCT, wnew);
 }
 
-/* tvdmusclf with method='tvdlf'/'tvdlf1', addfluxok=.true.,
- * src/vactvdlf.t:92-299 */
+/* tvdmusclf, addfluxok=.true., src/vactvdlf.t:92-299: method 'tvdlf' /
+ * 'tvdlf1' (Lax-Friedrichs dissipation with the mean-state cmax) or 'tvdmu' /
+ * 'tvdmu1' (central flux, then tvdlimit2's Roe dissipation) */
 static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
                       int idimmax, double* wCT, double* wnew) {
+  const int tf = s->p.typefull;
+  const int lf = tf == VACGPU_TVDLF || tf == VACGPU_TVDLF1;
   for (int idim = idimmin; idim <= idimmax; idim++) {
     box hxO = shift(ixO, idim, -1);
     box ixC = ixO;
@@ -900,7 +1576,7 @@ static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
       FORBOX(ixC, ix) r[ix] = c[ix + sh];
       FORBOX(ixC, ix) l[ix] = c[ix];
     }
-    if (s->p.typefull != VACGPU_TVDLF1) {
+    if (tf != VACGPU_TVDLF1 && tf != VACGPU_TVDMU1) {
       double* base;
       switch (s->p.typelimited) {
         case VACGPU_LIMITED_PREVIOUS: base = s->wold; break;
@@ -909,33 +1585,35 @@ static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
       }
       upwindLR(s, ixC, ixC, idim, base, s->wLC, s->wRC);
     }
-    /* mean state in wLC, cmax, CFL, wLC regained (src/vactvdlf.t:168-206) */
-    for (int iw = 0; iw < s->nw; iw++) {
-      double* l = W(s->wLC, iw);
-      const double* r = W(s->wRC, iw);
-      FORBOX(ixC, ix) l[ix] = HALF * (l[ix] + r[ix]);
-    }
-    int new_cmax = 1;
-    getcmax(s, &new_cmax, s->wLC, ixC, idim, s->cmaxC);
-    if (s->courantpar > ZERO && s->istep == s->nstep) {
-      const double* dx = W(s->dx, idim);
-      double courantmax = 0.0;
-      int first = 1;
-      FORBOX_SEQ(ixC, ix) {
-        double q = s->cmaxC[ix] * TWO / (dx[ix] + dx[ix + sh]);
-        if (first || q > courantmax) courantmax = q;
-        first = 0;
+    if (lf) {
+      /* mean state in wLC, cmax, CFL, wLC regained (src/vactvdlf.t:168-206) */
+      for (int iw = 0; iw < s->nw; iw++) {
+        double* l = W(s->wLC, iw);
+        const double* r = W(s->wRC, iw);
+        FORBOX(ixC, ix) l[ix] = HALF * (l[ix] + r[ix]);
       }
-      if (qdt * courantmax > ONE) s->nerror[2]++;
-      if (courantmax > SMALLDOUBLE) {
-        double c = s->courantpar / courantmax;
-        if (c < s->dtcourant[idim]) s->dtcourant[idim] = c;
+      int new_cmax = 1;
+      getcmax(s, &new_cmax, s->wLC, ixC, idim, s->cmaxC);
+      if (s->courantpar > ZERO && s->istep == s->nstep) {
+        const double* dx = W(s->dx, idim);
+        double courantmax = 0.0;
+        int first = 1;
+        FORBOX_SEQ(ixC, ix) {
+          double q = s->cmaxC[ix] * TWO / (dx[ix] + dx[ix + sh]);
+          if (first || q > courantmax) courantmax = q;
+          first = 0;
+        }
+        if (qdt * courantmax > ONE) s->nerror[2]++;
+        if (courantmax > SMALLDOUBLE) {
+          double c = s->courantpar / courantmax;
+          if (c < s->dtcourant[idim]) s->dtcourant[idim] = c;
+        }
       }
-    }
-    for (int iw = 0; iw < s->nw; iw++) {
-      double* l = W(s->wLC, iw);
-      const double* r = W(s->wRC, iw);
-      FORBOX(ixC, ix) l[ix] = 2 * l[ix] - r[ix];
+      for (int iw = 0; iw < s->nw; iw++) {
+        double* l = W(s->wLC, iw);
+        const double* r = W(s->wRC, iw);
+        FORBOX(ixC, ix) l[ix] = 2 * l[ix] - r[ix];
+      }
     }
     getv(s, s->wLC, ixC, idim, s->vLC);
     getv(s, s->wRC, ixC, idim, s->vRC);
@@ -949,10 +1627,13 @@ static void tvdmusclf(vo_state* s, double qdt, box ixO, int idimmin,
         FORBOX(ixC, ix) s->fRC[ix] = s->fRC[ix] + s->vRC[ix] * r[ix];
       }
       FORBOX(ixC, ix) s->fLC[ix] = HALF * (s->fLC[ix] + s->fRC[ix]);
-      FORBOX(ixC, ix) s->fRC[ix] = -s->cmaxC[ix] * HALF * (r[ix] - l[ix]);
-      FORBOX(ixC, ix) s->fLC[ix] = s->fLC[ix] + s->fRC[ix];
+      if (lf) {
+        FORBOX(ixC, ix) s->fRC[ix] = -s->cmaxC[ix] * HALF * (r[ix] - l[ix]);
+        FORBOX(ixC, ix) s->fLC[ix] = s->fLC[ix] + s->fRC[ix];
+      }
       addflux(s, qdt, ixO, iw, idim, s->fLC, ixO, s->fLC, hxO, wnew);
     }
+    if (!lf) tvdlimit2(s, qdt, ixC, ixO, idim, s->wLC, s->wRC, wnew);
   }
   if (s->p.sourceunsplit)
     addsource2(s, qdt * (idimmax - idimmin + ONE) / s->ndim, ixO, wCT, wnew);
@@ -969,13 +1650,14 @@ static void advect1(vo_state* s, int pred, double qdt, int idimmin,
   getboundary(s, w);
 }
 
-/* advect, src/vac.t:363-486.  'tvdlf' has the default predictor 'hancock'
- * (twostep); 'tvdlf1' has typepred1='nul', which turns twostep into onestep
- * (src/vacio.t:286-299,511): one tvdlf1 substep with wCT = a copy of w. */
+/* advect, src/vac.t:363-486.  'tvdlf' and 'tvdmu' have the default
+ * predictor 'hancock' (twostep); 'tvdlf1' and 'tvdmu1' have typepred1='nul',
+ * which turns twostep into onestep (src/vacio.t:286-299,511): one substep
+ * with wCT = a copy of w. */
 static void advect(vo_state* s, int idimmin, int idimmax) {
   memcpy(s->w1, s->w, sizeof(double) * s->N * s->nw);
   s->istep = 0;
-  if (s->p.typefull == VACGPU_TVDLF1) {
+  if (s->p.typefull == VACGPU_TVDLF1 || s->p.typefull == VACGPU_TVDMU1) {
     advect1(s, 0, s->dt, idimmin, idimmax, s->w1, s->w);
     return;
   }
@@ -1076,6 +1758,37 @@ static void getdt_special(vo_state* s) {
 
 static char errbuf[256];
 
+/* Configurations the Roe solvers define: the MHD solver dies for ndir=1
+ * (src/vacphys.mhdroe.t:25); the left/right speeds of the MHD entropy fixes
+ * of the fastLW/slow waves and of alfvLW are saved by the fastRW and alfvRW
+ * calls (src/vacphys.mhdroe.t:245-276), so those waves' fix needs the
+ * fastRW's (alfvRW's); the HD 'ratio' fix reads speeds the HD solver never
+ * sets (src/vacphys.hdroe.t:110-134). */
+static const char* roe_check(const vacgpu_params* p, int nw) {
+  const int mhd = p->physics == VACGPU_PHYS_MHD;
+  if (mhd && p->ndir < 2) return "MHD Roe solver needs ndir>=2";
+  for (int il = 0; il < nw; il++) {
+    const int te = p->typeentropy[il];
+    if (te < VACGPU_ENTROPY_NUL || te > VACGPU_ENTROPY_YEE)
+      return "unknown typeentropy";
+    if (!mhd && te == VACGPU_ENTROPY_RATIO)
+      return "typeentropy='ratio' is undefined for the HD Roe solver";
+  }
+  if (mhd) {
+#define USES_LR(il)                                      \
+  (p->typeentropy[il] == VACGPU_ENTROPY_HARTEN ||        \
+   p->typeentropy[il] == VACGPU_ENTROPY_POWELL ||        \
+   p->typeentropy[il] == VACGPU_ENTROPY_RATIO)
+    for (int il = 1; il < 4; il++)
+      if (USES_LR(il) && !USES_LR(0))
+        return "MHD entropy fix of a fast/slow wave needs the fastRW fix";
+    if (nw == 8 && USES_LR(7) && !USES_LR(6))
+      return "MHD entropy fix of alfvLW needs the alfvRW fix";
+#undef USES_LR
+  }
+  return NULL;
+}
+
 const char* vo_last_error(void) { return errbuf; }
 
 vo_state* vo_create(const vacgpu_params* p) {
@@ -1084,6 +1797,10 @@ vo_state* vo_create(const vacgpu_params* p) {
   if (p->dixB != 2) ERR("dixB must be 2");
   int nw = p->physics == VACGPU_PHYS_MHD ? 2 + 2 * p->ndir : 2 + p->ndir;
   if (p->nw != nw) ERR("nw does not match physics and ndir");
+  if (p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1) {
+    const char* why = roe_check(p, nw);
+    if (why) ERR(why);
+  }
   vo_state* s = (vo_state*)calloc(1, sizeof(vo_state));
   s->p = *p;
   s->ndim = p->ndim;
@@ -1124,7 +1841,12 @@ vo_state* vo_create(const vacgpu_params* p) {
   s->smallrho = p->smallrho;
   s->courantpar = p->courantpar;
   s->dtpar = p->dtpar;
-  s->nstep = p->typefull == VACGPU_TVDLF1 ? 1 : 2;  /* onestep / twostep */
+  /* onestep / twostep */
+  s->nstep = (p->typefull == VACGPU_TVDLF1 || p->typefull == VACGPU_TVDMU1) ? 1 : 2;
+  if (p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1) {
+    s->wroe = calloc(N * nw, sizeof(double));
+    for (int i = 0; i < NROE; i++) s->roe[i] = calloc(N, sizeof(double));
+  }
   /* startup, src/vac.t:160-220 */
   for (int d = 0; d < 3; d++) s->dtcourant[d] = BIGDOUBLE;
   if (s->dtpar > ZERO && p->slowsteps != 1) s->courantpar = -ONE;
@@ -1140,6 +1862,8 @@ void vo_destroy(vo_state* s) {
   for (unsigned i = 0; i < sizeof(a) / sizeof(a[0]); i++) free(a[i]);
   for (int iB = 0; iB < VACGPU_MAXB; iB++) free(s->fixB[iB]);
   for (int c = 0; c < 3; c++) free(s->cur[c]);
+  free(s->wroe);
+  for (int i = 0; i < NROE; i++) free(s->roe[i]);
   free(s);
 }
 

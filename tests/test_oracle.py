@@ -1,5 +1,6 @@
 """The FP64 CPU oracle: the C restatement against the independent NumPy
-restatement (bit for bit), the committed golden fixtures, and the
+restatement (bit for bit), the reference's own Roe-solver check (R*L*dw=dw,
+src/roetest.t), the exact solution of Sod's shock tube, and the
 reference-independent properties of the scheme (conservation, free-stream
 preservation, symmetry)."""
 import numpy as np
@@ -100,7 +101,59 @@ RES_CASES = [
      resistive(1.0)),
 ]
 
-CASES = CASES + SMALLFIX_CASES + BC_CASES + RES_CASES + [
+def tvdmu(typefull=abi.TVDMU, entropy=None, **kw):
+    """Tweak: TVD-MUSCL with the Roe solver, optional typeentropy for all
+    waves and other parameter settings."""
+    def tweak(p):
+        p.typefull = typefull
+        if entropy is not None:
+            for il in range(p.nw):
+                p.typeentropy[il] = entropy
+        for k, v in kw.items():
+            setattr(p, k, v)
+    return tweak
+
+
+E = abi
+ROE_CASES = [
+    ("sod-tvdmu", lambda: inistate.sod_1d(48), "minmod", "cont", 12, tvdmu()),
+    ("hd-riemann-tvdmu", lambda: inistate.riemann_2d(20, 3), "minmod", "cont", 6, tvdmu()),
+    ("ot-tvdmu", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5, tvdmu()),
+    ("rm3-tvdmu", lambda: inistate.random_modes(8, seed=1), "minmod", "periodic", 3, tvdmu()),
+    ("rm23-tvdmu", lambda: inistate.random_modes(12, seed=2, ndim=2, ndir=3), "minmod",
+     "periodic", 4, tvdmu()),
+    ("ot-tvdmu1", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     tvdmu(E.TVDMU1)),
+    ("hd-tvdmu1", lambda: inistate.riemann_2d(16, 5), "minmod", "cont", 5, tvdmu(E.TVDMU1)),
+    ("hd-tvdmu-harten", lambda: inistate.riemann_2d(16, 3), "minmod", "cont", 5,
+     tvdmu(entropy=E.ENTROPY_HARTEN)),
+    ("hd-tvdmu-powell", lambda: inistate.riemann_2d(16, 6), "superbee", "cont", 5,
+     tvdmu(entropy=E.ENTROPY_POWELL)),
+    ("hd-tvdmu-yee", lambda: inistate.riemann_2d(16, 3), "minmod", "cont", 5,
+     tvdmu(entropy=E.ENTROPY_YEE)),
+    ("rm23-tvdmu-harten", lambda: inistate.random_modes(12, seed=2, ndim=2, ndir=3), "minmod",
+     "periodic", 4, tvdmu(entropy=E.ENTROPY_HARTEN)),
+    ("rm3-tvdmu-powell", lambda: inistate.random_modes(8, seed=1), "woodward", "periodic", 3,
+     tvdmu(entropy=E.ENTROPY_POWELL)),
+    ("ot-tvdmu-ratio", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     tvdmu(entropy=E.ENTROPY_RATIO)),
+    ("rm3-tvdmu-yee", lambda: inistate.random_modes(8, seed=1), "minmod", "periodic", 3,
+     tvdmu(entropy=E.ENTROPY_YEE)),
+    ("ot-tvdmu-nodivbwave", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     tvdmu(divbwave=0)),
+    ("ot-tvdmu-useprimitive", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     tvdmu(useprimitive=1)),
+    ("ot-tvdmu-unsplit", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     tvdmu(dimsplit=0, typelimited=E.LIMITED_PREVIOUS)),
+    ("ot-tvdmu-symm0", lambda: inistate.orszag_tang(16), "woodward", "cont", 4,
+     lambda p: (tvdmu()(p), bcs({"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM},
+                                {"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM},
+                                B.BC_PERIODIC, B.BC_PERIODIC)(p))),
+    ("rm3-tvdmu-resistive", lambda: inistate.random_modes(8, seed=7), "minmod", "periodic", 3,
+     lambda p: (tvdmu()(p), resistive(0.002)(p))),
+]
+
+CASES = CASES + SMALLFIX_CASES + BC_CASES + RES_CASES + ROE_CASES + [
     # reconstruction in primitive variables (useprimitive=T)
     ("ot-useprimitive", lambda: inistate.orszag_tang(16), "woodward", "periodic", 5,
      lambda p: setattr(p, "useprimitive", 1)),
@@ -183,3 +236,100 @@ def test_smallfix_counts_and_floors():
     gm1 = p.eqpar[0] - 1
     pth = gm1 * (w[3] - 0.5 * (w[1] ** 2 + w[2] ** 2) / w[0])
     assert pth.min() >= 0.3 * (1 - 1e-12)
+
+
+ROE_IDENTITY = [(False, 1, 1), (False, 2, 2), (False, 2, 3), (False, 3, 3),
+                (True, 2, 2), (True, 2, 3), (True, 3, 3)]
+
+
+@pytest.mark.parametrize("mhd,ndim,ndir", ROE_IDENTITY,
+                         ids=["%s%d%d" % ("mhd" if m else "hd", a, b)
+                              for m, a, b in ROE_IDENTITY])
+def test_roe_solver_identity(mhd, ndim, ndir):
+    """src/roetest.t:2-60: for random left/right states, summing
+    R(iw,il)*(L*dw)(il) over the waves returns wR-wL in every direction."""
+    rng = np.random.default_rng(11 + 7 * ndim + ndir + (100 if mhd else 0))
+    phys = abi.PHYS_MHD if mhd else abi.PHYS_HD
+    nx = [48] + [1] * (ndim - 1)
+    p = abi.default_params(ndim, ndir, phys, nx)
+    p.typefull = abi.TVDMU
+    p.smallp = 1e-10
+    nw = p.nw
+    x = np.stack(np.meshgrid(*[np.linspace(0, 1, k) for k in nx], indexing="ij"))
+
+    def state():
+        rho, pr = rng.uniform(0.2, 2.0, nx), rng.uniform(0.1, 2.0, nx)
+        v = [rng.uniform(-1, 1, nx) for _ in range(ndir)]
+        if mhd:
+            b = [rng.uniform(-1.5, 1.5, nx) for _ in range(ndir)]
+            return inistate.conserve_mhd(rho, v, pr, b, p.eqpar[0])
+        return inistate.conserve_hd(rho, v, pr, p.eqpar[0])
+
+    wl, wr = state(), state()
+    nv = NumpyVac(p, x, wl.reshape(nw, -1))
+    b = nv.ixM
+    WL = nv.w.copy()
+    WR = nv.w.copy()
+    WR[(slice(None),) + b.sl()] = wr.reshape(WR[(slice(None),) + b.sl()].shape)
+    with np.errstate(all="ignore"):
+        for idim in range(ndim):
+            R = nv.roe_average(WL, WR, b, idim)
+            acc = [0.0] * nw
+            for il in range(nw):
+                _, jump, _ = nv.roe_wave(R, WL, WR, b, il, idim)
+                for iw in range(nw):
+                    acc[iw] = acc[iw] + nv.roe_rtimes(R, jump, iw, il, idim)
+            for iw in range(nw):
+                d = WR[(iw,) + b.sl()] - WL[(iw,) + b.sl()]
+                assert np.abs(acc[iw] - d).max() <= 1e-12 * max(1.0, np.abs(d).max())
+
+
+def _sod_exact_rho(x, t, g=1.4):
+    """Exact density of Sod's problem (rho,p,u)=(1,1,0)|(0.125,0.1,0) at
+    x0=0.5: star pressure 0.30313 and velocity 0.92745 and shock speed
+    1.75216 from E. F. Toro, Riemann Solvers and Numerical Methods for Fluid
+    Dynamics, test 1 of section 4.3.3."""
+    ps, us, sh = 0.30313, 0.92745, 1.75216
+    rl, pl, rr, pr = 1.0, 1.0, 0.125, 0.1
+    cl = np.sqrt(g * pl / rl)
+    rsl = rl * (ps / pl) ** (1 / g)
+    q = (g - 1) / (g + 1)
+    rsr = rr * (ps / pr + q) / (q * ps / pr + 1)
+    head, tail = -cl, us - cl * (ps / pl) ** ((g - 1) / (2 * g))
+    xi = (x - 0.5) / t
+    fan = rl * (2 / (g + 1) - (g - 1) / ((g + 1) * cl) * xi) ** (2 / (g - 1))
+    return np.select([xi < head, xi < tail, xi < us, xi < sh], [rl, fan, rsl, rsr], rr)
+
+
+def test_sod_shock_tube_tvdmu_converges_to_exact_solution():
+    """TVD-MUSCL with the Roe dissipation on Sod's problem to t=0.2: the L1
+    density error halves with the resolution and stays below TVDLF's."""
+    err = {}
+    for tf in (abi.TVDMU, abi.TVDLF):
+        for n in (100, 200):
+            s = inistate.sod_1d(n)
+            p = inistate.params_for(s, bc="cont")
+            p.typefull = tf
+            p.tmax, p.tmaxexact = 0.2, 1
+            o = Oracle(p, s.x, s.w)
+            o.step(100000)
+            assert abs(o.t - 0.2) < 1e-12
+            err[tf, n] = np.abs(o.state()[0] - _sod_exact_rho(s.x[0], o.t)).mean()
+    assert err[abi.TVDMU, 200] < 0.005
+    assert err[abi.TVDMU, 200] < 0.6 * err[abi.TVDMU, 100]
+    assert err[abi.TVDMU, 200] < err[abi.TVDLF, 200]
+
+
+def test_roe_entropy_fix_combinations_refused():
+    s = inistate.riemann_2d(8, 1)
+    p = inistate.params_for(s, bc="cont")
+    p.typefull = abi.TVDMU
+    p.typeentropy[0] = abi.ENTROPY_RATIO
+    with pytest.raises(RuntimeError, match="ratio"):
+        Oracle(p, s.x, s.w)
+    s = inistate.orszag_tang(8)
+    p = inistate.params_for(s)
+    p.typefull = abi.TVDMU
+    p.typeentropy[2] = abi.ENTROPY_HARTEN
+    with pytest.raises(RuntimeError, match="fastRW"):
+        Oracle(p, s.x, s.w)

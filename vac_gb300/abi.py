@@ -14,7 +14,8 @@ MAXSRCPAR = 8
 PHYS_HD, PHYS_MHD = 0, 1
 LIM_MINMOD, LIM_WOODWARD, LIM_SUPERBEE, LIM_VANLEER, LIM_ALBADA = range(5)
 BC_CONT, BC_PERIODIC, BC_SYMM, BC_ASYMM, BC_FIXED, BC_FIXED1, BC_CONT1, BC_GRAD1, BC_SYMM0 = range(9)
-TVDLF, TVDLF1 = 0, 1
+TVDLF, TVDLF1, TVDMU, TVDMU1 = 0, 1, 2, 3
+ENTROPY_NUL, ENTROPY_HARTEN, ENTROPY_POWELL, ENTROPY_RATIO, ENTROPY_YEE = range(5)
 LIMITED_ORIGINAL, LIMITED_PREVIOUS, LIMITED_PREDICTOR = range(3)
 SPLIT_XYYX, SPLIT_XY = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -23,6 +24,11 @@ SRC_NONE, SRC_GRAVITY = 0, 1
 LIMITER_NAMES = {"minmod": LIM_MINMOD, "woodward": LIM_WOODWARD,
                  "superbee": LIM_SUPERBEE, "vanleer": LIM_VANLEER,
                  "albada": LIM_ALBADA}
+TYPEFULL_NAMES = {"tvdlf": TVDLF, "tvdlf1": TVDLF1, "tvdmu": TVDMU,
+                  "tvdmu1": TVDMU1}
+ENTROPY_NAMES = {"nul": ENTROPY_NUL, "harten": ENTROPY_HARTEN,
+                 "powell": ENTROPY_POWELL, "ratio": ENTROPY_RATIO,
+                 "yee": ENTROPY_YEE}
 BC_NAMES = {"cont": BC_CONT, "periodic": BC_PERIODIC, "symm": BC_SYMM,
             "asymm": BC_ASYMM, "fixed": BC_FIXED, "fixed1": BC_FIXED1,
             "cont1": BC_CONT1, "grad1": BC_GRAD1, "symm0": BC_SYMM0}
@@ -63,6 +69,9 @@ class VacParams(C.Structure):
         ("useprimitive", C.c_int),
         ("compactres", C.c_int),
         ("dtdiffpar", C.c_double),
+        ("typeentropy", C.c_int * MAXNW),
+        ("entropycoef", C.c_double * MAXNW),
+        ("divbwave", C.c_int),
     ]
 
 
@@ -109,7 +118,26 @@ def default_params(ndim, ndir, physics, nx, gamma=5.0 / 3.0):
     p.useprimitive = 0
     p.compactres = 0
     p.dtdiffpar = 0.5
+    for il in range(MAXNW):
+        p.typeentropy[il] = ENTROPY_NUL
+        p.entropycoef[il] = default_entropycoef(physics, il)
+    p.divbwave = 1
     return p
+
+
+def default_entropycoef(physics, il):
+    """physini's entropycoef of wave il (0-based): the default-real
+    literals 0.2 and 0.4 of src/vacphys.mhd0.t:18-28 and
+    src/vacphys.t.hd:21-29, i.e. single precision widened to double."""
+    f02 = float(C.c_float(0.2).value)
+    f04 = float(C.c_float(0.4).value)
+    if physics == PHYS_MHD:
+        if il < 4:        # fastRW, fastLW, slowRW, slowLW
+            return f02
+        if il in (6, 7):  # alfvRW, alfvLW
+            return f04
+        return -1.0
+    return f02 if il < 2 else -1.0  # soundRW, soundLW
 
 
 def set_all_bc(p, bc):

@@ -684,6 +684,20 @@ void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
   p->vacuumrho = -1.0;
   p->compactres = 0;
   p->dtdiffpar = 0.5;
+  // physini's entropycoef: the default-real literals 0.2 and 0.4
+  // (src/vacphys.mhd0.t:18-28, src/vacphys.t.hd:21-29), widened to double
+  for (int il = 0; il < VACGPU_MAXNW; il++) {
+    p->typeentropy[il] = VACGPU_ENTROPY_NUL;
+    double c = -1.0;
+    if (physics == VACGPU_PHYS_MHD) {
+      if (il < 4) c = (double)0.2f;
+      if (il == 6 || il == 7) c = (double)0.4f;
+    } else if (il < 2) {
+      c = (double)0.2f;
+    }
+    p->entropycoef[il] = c;
+  }
+  p->divbwave = 1;
 }
 
 int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {

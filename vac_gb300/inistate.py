@@ -13,6 +13,7 @@ the synthetic workloads this engine is measured on:
 * ``riemann_2d``     2-D gamma-law HD two-state problem split along a
                      random line (outflow boundaries)
 * ``blast_3d``       3-D MHD blast wave in a uniform oblique field
+* ``sod_1d``         1-D gamma-law HD shock tube (Sod's states)
 """
 import numpy as np
 
@@ -50,16 +51,27 @@ def conserve_hd(rho, v, p, gamma):
 
 
 MHD_NAMES = {2: "rho m1 m2 e b1 b2", 3: "rho m1 m2 m3 e b1 b2 b3"}
-HD_NAMES = {2: "rho m1 m2 e", 3: "rho m1 m2 m3 e"}
+HD_NAMES = {1: "rho m1 e", 2: "rho m1 m2 e", 3: "rho m1 m2 m3 e"}
 
 
-def _snap(x, w, gamma, mhd, ndim, header):
-    names = (MHD_NAMES if mhd else HD_NAMES)[ndim]
+def _snap(x, w, gamma, mhd, ndim, header, ndir=None):
+    """A snapshot whose header ends in VAC's physics tag _mhdDC / _hdDC
+    (D = ndim, C = ndir)."""
+    ndir = ndim if ndir is None else ndir
+    names = (MHD_NAMES if mhd else HD_NAMES)[ndir]
     eq = np.array([gamma, 0.0]) if mhd else np.array([gamma])
-    return Snapshot(header + ("_mhd%d%d" % (ndim, ndim) if mhd else
-                              "_hd%d%d" % (ndim, ndim)),
+    return Snapshot(header + ("_mhd%d%d" % (ndim, ndir) if mhd else
+                              "_hd%d%d" % (ndim, ndir)),
                     0, 0.0, ndim, eq, names + " gamma" + (" eta" if mhd else ""),
                     x, w, tuple(w.shape[1:]))
+
+
+def snap_ndir(snap):
+    """ndir from the physics tag at the end of the header (ndim if none)."""
+    tag = snap.header.rstrip()[-2:]
+    if tag.isdigit() and int(tag[0]) == snap.ndim:
+        return int(tag[1])
+    return snap.ndim
 
 
 def orszag_tang(n=200, gamma=5.0 / 3.0):
@@ -100,11 +112,13 @@ def _phase_fields(x, ks, phis):
 
 
 def random_modes(n=256, seed=0, gamma=5.0 / 3.0, ndim=3, nmodes=8,
-                 rho_amp=0.2, v_rms=0.3, b_rms=0.1, p0=0.05):
+                 rho_amp=0.2, v_rms=0.3, b_rms=0.1, p0=0.05, ndir=None):
     """rho=1+sum a_k cos(2pi k.x+phi_k) with sum|a_k|=rho_amp; v from random
     vector modes scaled to rms v_rms; B=(1,0,0)+sum a_k (e_k x k)cos(..)
     (divergence free) scaled to rms b_rms; uniform p=p0.  Unit periodic box;
-    0<|k|<=4 (k_z=0 in 2-D)."""
+    0<|k|<=4 (k_z=0 in 2-D).  ndir=3 with ndim=2 keeps the z components
+    of v and B (2.5-D)."""
+    ndir = ndim if ndir is None else ndir
     rng = np.random.default_rng(seed)
     nx = (n,) * ndim
     x = domain_grid(nx, (0.0,) * ndim, (1.0,) * ndim)
@@ -119,12 +133,12 @@ def random_modes(n=256, seed=0, gamma=5.0 / 3.0, ndim=3, nmodes=8,
     # velocity: random directions per mode
     ks = _modes(rng, nmodes, ndim)
     dirs = rng.normal(size=(nmodes, 3))
-    if ndim == 2:
+    if ndir == 2:
         dirs[:, 2] = 0.0
     cs = _phase_fields(x, ks, rng.uniform(0, 2 * np.pi, nmodes))
-    v = [np.zeros(shape) for _ in range(ndim)]
+    v = [np.zeros(shape) for _ in range(ndir)]
     for dvec, c in zip(dirs, cs):
-        for d in range(ndim):
+        for d in range(ndir):
             v[d] += dvec[d] * c
     vr = np.sqrt(np.mean(sum(vc * vc for vc in v)))
     v = [vc * (v_rms / vr) for vc in v]
@@ -132,17 +146,18 @@ def random_modes(n=256, seed=0, gamma=5.0 / 3.0, ndim=3, nmodes=8,
     ks = _modes(rng, nmodes, ndim)
     es = rng.normal(size=(nmodes, 3))
     cs = _phase_fields(x, ks, rng.uniform(0, 2 * np.pi, nmodes))
-    bp = [np.zeros(shape) for _ in range(ndim)]
+    bp = [np.zeros(shape) for _ in range(ndir)]
     for k, e, c in zip(ks, es, cs):
         pol = np.cross(e, k)
-        for d in range(ndim):
+        for d in range(ndir):
             bp[d] += pol[d] * c
     br = np.sqrt(np.mean(sum(bc * bc for bc in bp)))
     b = [bc * (b_rms / br) for bc in bp]
     b[0] = b[0] + 1.0
     p = np.full(shape, p0)
     w = conserve_mhd(rho, v, p, b, gamma)
-    return _snap(x, w, gamma, True, ndim, "random-mode MHD seed=%d" % seed)
+    return _snap(x, w, gamma, True, ndim, "random-mode MHD seed=%d" % seed,
+                 ndir=ndir)
 
 
 def riemann_2d(side, seed, gamma=1.4):
@@ -183,6 +198,17 @@ def blast_3d(n=512, gamma=5.0 / 3.0, r0=0.1, pin=10.0, pout=0.1):
     return _snap(x, w, gamma, True, 3, "MHD blast 3D")
 
 
+def sod_1d(n=100, gamma=1.4):
+    """Sod's shock tube on [0,1]: (rho,p)=(1,1) left of x=0.5, (0.125,0.1)
+    right, at rest."""
+    x = domain_grid((n,), (0.0,), (1.0,))
+    left = x[0] < 0.5
+    rho = np.where(left, 1.0, 0.125)
+    p = np.where(left, 1.0, 0.1)
+    w = conserve_hd(rho, [np.zeros_like(rho)], p, gamma)
+    return _snap(x, w, gamma, False, 1, "Sod shock tube")
+
+
 def params_for(snap, limiter="minmod", bc="periodic", precision=abi.PREC_FP64):
     """vacgpu_params for a snapshot with the path's par settings
     (typefull=nw*'tvdlf', twostep, dimsplit xyyx, divbfix, sourceunsplit,
@@ -190,7 +216,7 @@ def params_for(snap, limiter="minmod", bc="periodic", precision=abi.PREC_FP64):
     mhd = "mhd" in snap.header
     ndim = snap.ndim
     nx = snap.w.shape[1:]
-    p = abi.default_params(ndim, ndim, abi.PHYS_MHD if mhd else abi.PHYS_HD,
+    p = abi.default_params(ndim, snap_ndir(snap), abi.PHYS_MHD if mhd else abi.PHYS_HD,
                            list(nx), gamma=float(snap.eqpar[0]))
     abi.set_all_limiters(p, abi.LIMITER_NAMES[limiter])
     abi.set_all_bc(p, abi.BC_NAMES[bc])
