@@ -131,7 +131,81 @@ RES_CASES = [
     ("ot-resistive-dtdiff", lambda: inistate.orszag_tang(24), "minmod", "periodic", 6,
      _resistive(1.0), None),
 ]
-FP64_CASES = FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES + RES_CASES
+def _tvdmu(typefull=abi.TVDMU, entropy=None, **kw):
+    """TVD-MUSCL with the Roe dissipation, optionally one typeentropy for
+    every wave and other parameter settings."""
+    def tweak(p):
+        p.typefull = typefull
+        if entropy is not None:
+            for il in range(p.nw):
+                p.typeentropy[il] = entropy
+        for k, v in kw.items():
+            setattr(p, k, v)
+    return tweak
+
+
+def _hd_from_mhd(snap):
+    """The gas part of an MHD snapshot as an HD one (e minus B^2/2)."""
+    from vac_gb300.vacfile import Snapshot
+    ndir = inistate.snap_ndir(snap)
+    w = snap.w
+    bb = sum(w[ndir + 2 + c] ** 2 for c in range(ndir))
+    hd = np.concatenate([w[:ndir + 1], (w[ndir + 1] - 0.5 * bb)[None]])
+    head = snap.header.replace("_mhd", "_hd")
+    return Snapshot(head, 0, 0.0, snap.ndim, snap.eqpar[:1], "", snap.x, hd, snap.nx)
+
+
+E = abi
+# TVD-MUSCL ('tvdmu', 'tvdmu1') with the Roe solvers: HD 1-D/2-D/2.5-D/3-D,
+# MHD 2-D/2.5-D/3-D, every entropy fix, without the div B wave, with
+# useprimitive, unsplit, symm0 walls and resistivity
+ROE_CASES = [
+    ("sod-tvdmu", lambda: inistate.sod_1d(200), "minmod", "cont", 60, _tvdmu(), None),
+    ("hd-riemann-tvdmu", lambda: inistate.riemann_2d(40, 3), "minmod", "cont", 12, _tvdmu(),
+     None),
+    ("hd25-tvdmu", lambda: _hd_from_mhd(inistate.random_modes(20, seed=4, ndim=2, ndir=3,
+                                                             p0=0.5)),
+     "woodward", "periodic", 8, _tvdmu(), None),
+    ("hd3-tvdmu", lambda: _hd_from_mhd(inistate.random_modes(12, seed=5, p0=0.5)), "minmod",
+     "periodic", 4, _tvdmu(), None),
+    ("ot-tvdmu", lambda: inistate.orszag_tang(32), "woodward", "periodic", 10, _tvdmu(), None),
+    ("rm3-tvdmu", lambda: inistate.random_modes(12, seed=1), "minmod", "periodic", 4, _tvdmu(),
+     None),
+    ("rm25-tvdmu", lambda: inistate.random_modes(24, seed=2, ndim=2, ndir=3), "minmod",
+     "periodic", 8, _tvdmu(), None),
+    ("ot-tvdmu1", lambda: inistate.orszag_tang(32), "minmod", "periodic", 8, _tvdmu(E.TVDMU1),
+     None),
+    ("hd-tvdmu1", lambda: inistate.riemann_2d(32, 5), "minmod", "cont", 8, _tvdmu(E.TVDMU1),
+     None),
+    ("hd-tvdmu-harten", lambda: inistate.riemann_2d(32, 3), "minmod", "cont", 8,
+     _tvdmu(entropy=E.ENTROPY_HARTEN), None),
+    ("hd-tvdmu-powell", lambda: inistate.riemann_2d(32, 6), "superbee", "cont", 8,
+     _tvdmu(entropy=E.ENTROPY_POWELL), None),
+    ("hd-tvdmu-yee", lambda: inistate.riemann_2d(32, 3), "minmod", "cont", 8,
+     _tvdmu(entropy=E.ENTROPY_YEE), None),
+    ("rm25-tvdmu-harten", lambda: inistate.random_modes(20, seed=2, ndim=2, ndir=3), "minmod",
+     "periodic", 6, _tvdmu(entropy=E.ENTROPY_HARTEN), None),
+    ("rm3-tvdmu-powell", lambda: inistate.random_modes(12, seed=1), "woodward", "periodic", 4,
+     _tvdmu(entropy=E.ENTROPY_POWELL), None),
+    ("ot-tvdmu-ratio", lambda: inistate.orszag_tang(32), "minmod", "periodic", 8,
+     _tvdmu(entropy=E.ENTROPY_RATIO), None),
+    ("rm3-tvdmu-yee", lambda: inistate.random_modes(12, seed=1), "minmod", "periodic", 4,
+     _tvdmu(entropy=E.ENTROPY_YEE), None),
+    ("ot-tvdmu-nodivbwave", lambda: inistate.orszag_tang(32), "minmod", "periodic", 8,
+     _tvdmu(divbwave=0), None),
+    ("ot-tvdmu-useprimitive", lambda: inistate.orszag_tang(32), "minmod", "periodic", 8,
+     _tvdmu(useprimitive=1), None),
+    ("ot-tvdmu-unsplit", lambda: inistate.orszag_tang(32), "minmod", "periodic", 8,
+     _tvdmu(dimsplit=0, typelimited=E.LIMITED_PREVIOUS), None),
+    ("ot-tvdmu-symm0", lambda: inistate.orszag_tang(32), "woodward", "cont", 8,
+     lambda p: (_tvdmu()(p), _bcs({"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM},
+                                  {"*": B.BC_SYMM0, 1: B.BC_ASYMM, 4: B.BC_ASYMM},
+                                  B.BC_PERIODIC, B.BC_PERIODIC)(p)), None),
+    ("rm3-tvdmu-resistive", lambda: inistate.random_modes(12, seed=7), "minmod", "periodic", 4,
+     lambda p: (_tvdmu()(p), _resistive(0.002)(p)), None),
+]
+FP64_CASES = (FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES + RES_CASES +
+              ROE_CASES)
 
 
 def _ragged():
@@ -256,4 +330,24 @@ def test_mixed_resistive_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, 
     a, b = e.state(), o.state()
     for iw in range(a.shape[0]):
         rel = np.abs(a[iw] - b[iw]).sum() / np.abs(b[iw]).sum()
+        assert rel <= MIXED_REL_L1, (iw, rel)
+
+
+ROE_MIXED = [c for c in ROE_CASES if c[0] in (
+    "sod-tvdmu", "hd-riemann-tvdmu", "ot-tvdmu", "rm3-tvdmu", "rm25-tvdmu", "ot-tvdmu1",
+    "hd-tvdmu-harten", "rm3-tvdmu-powell")]
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak,src", ROE_MIXED,
+                         ids=[c[0] for c in ROE_MIXED])
+def test_mixed_tvdmu_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src):
+    """The Roe corrector in FP32 (double-float pressure recovery) against
+    the FP64 oracle."""
+    o, e = run_both(mk(), lim, bc, n, tweak, precision=abi.PREC_MIXED)
+    a, b = e.state(), o.state()
+    for iw in range(a.shape[0]):
+        den = np.abs(b[iw]).sum()
+        if den == 0:
+            continue
+        rel = np.abs(a[iw] - b[iw]).sum() / den
         assert rel <= MIXED_REL_L1, (iw, rel)

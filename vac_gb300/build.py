@@ -24,7 +24,9 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra flags)
 UNITS = [
     ("sweep_fp64.cu", ["-fmad=false"]),
+    ("roe_fp64.cu", ["-fmad=false"]),
     ("control.cu", ["-fmad=false"]),
+    ("roe_mixed.cu", ["--use_fast_math"]),
     ("sweep_mixed.cu", ["--use_fast_math"]),
     ("vacgpu.cu", []),
     ("noalloc.cu", []),

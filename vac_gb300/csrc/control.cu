@@ -51,6 +51,7 @@ __device__ void dt_begin_dev(Ctrl* c, int ndim) {
   const int i = threadIdx.x;
   for (int d = 0; d < 3; d++) {
     c->face_cmax[d][i] = 0ULL;
+    c->face_cmax2[d][i] = 0ULL;
     c->cell_cmax[d][i] = 0ULL;
   }
   c->pmin[i] = ~0ULL;
@@ -152,15 +153,34 @@ __device__ void dt_end_dev(Ctrl* c, const DtEndArgs& p) {
 }
 
 // After the last sweep: fold the correctors' CFL maxima into dtcourant
-// (src/vactvdlf.t:184-201), count Courant violations, it+1, t+dt.
+// (src/vactvdlf.t:184-201; 'tvdmu': the fast waves' normalised
+// eigenvalues, src/vactvd.t:144-160), count Courant violations, it+1, t+dt.
 // toggle: the number of buffer swaps of one step (batched grids).
 __device__ void step_end_dev(Ctrl* c, int ndim, int toggle) {
   if (c->done) return;
-  unsigned long long km[3] = {0, 0, 0};
+  unsigned long long km[3] = {0, 0, 0}, km2[3] = {0, 0, 0};
   if (c->courantpar > 0.0)
-    for (int d = 0; d < ndim; d++) km[d] = fold_max(c->face_cmax[d]);
+    for (int d = 0; d < ndim; d++) {
+      km[d] = fold_max(c->face_cmax[d]);
+      if (c->roe) km2[d] = fold_max(c->face_cmax2[d]);
+    }
   if (threadIdx.x != 0) return;
   for (int d = 0; d < ndim; d++) {
+    if (c->roe) {
+      // courantmax = max|a*dt*2/(dx+dx)| per wave; dtcourant =
+      // min(dtcourant, dt*courantpar/courantmax)
+      const unsigned long long ks[2] = {km[d], km2[d]};
+      for (int k = 0; k < 2; k++) {
+        if (!ks[k]) continue;
+        double cm = dkey_inv(ks[k]);
+        if (cm > 1.0) c->nerror[2]++;
+        if (cm > SMALL) {
+          double q = c->dt * c->courantpar / cm;
+          if (q < c->dtcourant[d]) c->dtcourant[d] = q;
+        }
+      }
+      continue;
+    }
     if (!km[d]) continue;
     double cm = dkey_inv(km[d]);
     if (c->dt * cm > 1.0) c->nerror[2]++;

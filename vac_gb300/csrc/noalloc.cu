@@ -76,6 +76,9 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
         "predictor");
   if (!(p->smallp >= 0.0))
     return vacgpu_internal_fail("vacgpu_sweep_noalloc needs smallp >= 0");
+  if (p->typefull != VACGPU_TVDLF && p->typefull != VACGPU_TVDLF1)
+    return vacgpu_internal_fail(
+        "vacgpu_sweep_noalloc runs the tvdlf and tvdlf1 correctors");
   if (p->smallfix || p->useprimitive ||
       (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] != 0.0))
     return vacgpu_internal_fail(

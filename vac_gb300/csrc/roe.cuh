@@ -1,0 +1,668 @@
+// roe.cuh - the TVD-MUSCL corrector of methods 'tvdmu' and 'tvdmu1'
+// (tvdmusclf, src/vactvdlf.t:92-299, with tvdlimit2 and getphi,
+// src/vactvd.t:86-243): the central flux of the upwindLR face states plus
+// Roe's characteristic dissipation, from the eight-wave MHD Roe solver
+// (src/vacphys.mhdroe.t) or the gamma-law HD one (src/vacphys.hdroe.t).
+//
+// One thread per mesh cell evaluates the Roe decomposition of both faces
+// of the cell in the sweep direction (the same per-face values the
+// neighbouring cells compute, bit for bit), then applies the updates in the
+// reference's order: the central fluxes of all variables (addflux with
+// qdt), then wave by wave the dissipative fluxes R(iw,il)*phi(il) scaled by
+// (dvolume(i)+dvolume(j))/4 (addflux with qdt=-1: += (F(i)-F(i-1))/dvolume).
+// The Roe decomposition runs in IEEE double on both paths; the FP64 instance
+// (roe_fp64.cu, built without FMA contraction) keeps every array statement's
+// operation order and is bit-identical to the CPU restatement, the mixed
+// instance (roe_mixed.cu) forms its FP32 face states and central fluxes as
+// the TVDLF corrector does and adds the double dissipation to FP32 sums.
+#pragma once
+#include "sweep.cuh"
+
+namespace vacgpu {
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+struct RoeSweep {
+  typedef Sweep<PH, NDIM, NDIR, MHD> S;
+  typedef typename PH::T T;
+  typedef typename PH::R R;
+  typedef Lay<NDIR, MHD> L;
+  // the Roe decomposition runs in double on both paths: its jumps and the
+  // conservative dp cancel, which FP32 cannot carry to the mixed path's
+  // tolerance; the face states and central fluxes stay in R
+  typedef double Q;
+  static constexpr int NW = L::NW;
+  static constexpr int E = L::E;
+  static constexpr int B0 = L::B0;
+
+  // Roe state of one face after average and geteigenjump (the saved
+  // quantities of src/vacphys.mhdroe.t:18-19,150-153 and
+  // src/vacphys.hdroe.t:63-65) and the limiter function of every wave.
+  struct Face {
+    Q v[NDIR];   // MHD: mean velocity; HD: Roe-averaged velocity
+    Q b[NDIR];   // MHD: B_idim (|B_idim| >= smalldouble), beta_idir, beta_jdir
+    Q sr;        // MHD: sqrt(mean rho); HD: sqrt(rhoL)*sqrt(rhoR)
+    Q cf, cs, af, as, cs2;  // MHD: fast/slow speeds, weights, sound^2
+                            // HD: cs = sound speed c
+    Q h;         // HD: Roe-averaged enthalpy
+    Q dp, rhodv; // MHD: pR-pL (conservative form), rho*dv_idim
+                 // HD: (pR-pL)/c^2, (vR-vL)_idim/c
+    Q phi[NW];   // getphi's TVD-MUSCL phi = |a*dt/dx|*jump (entropy fixed)
+  };
+
+  // Fortran SIGN(a,b), MAX and MIN as the oracle's selects
+  static __device__ __forceinline__ Q fsign(Q a, Q b) {
+    return copysign(fabs(a), b);
+  }
+  static __device__ __forceinline__ Q rmax(Q a, Q b) { return a > b ? a : b; }
+  static __device__ __forceinline__ Q rmin(Q a, Q b) { return a < b ? a : b; }
+  // smalldouble of the reference
+  static __device__ __forceinline__ Q tiny() { return 1.0e-99; }
+
+  // idir = idim+1-ndir*(idim/ndir) and jdir likewise, 1-based
+  // (src/vacphys.mhdroe.t:97,145-146); 0-based here
+  static __device__ __forceinline__ int dir_i(int d) {
+    const int i1 = d + 1;
+    return i1 + 1 - NDIR * (i1 / NDIR) - 1;
+  }
+  static __device__ __forceinline__ int dir_j(int d) {
+    const int d1 = dir_i(d) + 1;
+    return d1 + 1 - NDIR * (d1 / NDIR) - 1;
+  }
+
+  // getpthermal(.true.): p clipped at smallp
+  static __device__ __forceinline__ Q pth(const SweepArgs& a, const Q* u,
+                                          Q smallp) {
+    Q p = pthermal_raw<NDIR, MHD>(u, a.ph);
+    return p >= smallp ? p : smallp;
+  }
+
+  // Eigenvalue a and jump L*dw of wave il with its entropy fix
+  // (geteigenjump, src/vacphys.mhdroe.t:130-281 and
+  // src/vacphys.hdroe.t:48-141; entropyfix, src/vactvd.t:422-451), then
+  // phi of getphi's TVD-MUSCL branch (src/vactvd.t:227-243).  dxs =
+  // dx(i)+dx(j); am receives |a*dt*2/dxs| of the two fast waves.
+  template <int il>
+  static __device__ __forceinline__ void wave(const SweepArgs& a, const Q* wL,
+                                              const Q* wR, int d, Q smallp,
+                                              Q qdt, Q dxs, const Q* bd,
+                                              Face& f, Q* am) {
+    const Q g = Q(a.ph.gamma);
+    const Q rL = wL[0], rR = wR[0];
+    const Q v = f.v[d];
+    Q aa, jump;
+    if (MHD) {
+      // bd = {bdv, bdb} of the fast/slow waves, then of the Alfven waves
+      const Q bdv = il < 6 ? bd[0] : bd[2];
+      const Q bdb = il < 6 ? bd[1] : bd[3];
+      switch (il) {
+        case 0:
+          aa = v + f.cf;
+          jump = Q(0.5) / f.cs2 *
+                 (f.af * (+f.cf * f.rhodv + f.dp) + f.as * (-f.cs * bdv + bdb));
+          break;
+        case 1:
+          aa = v - f.cf;
+          jump = Q(0.5) / f.cs2 *
+                 (f.af * (-f.cf * f.rhodv + f.dp) + f.as * (+f.cs * bdv + bdb));
+          break;
+        case 2:
+          aa = v + f.cs;
+          jump = Q(0.5) / f.cs2 *
+                 (f.as * (+f.cs * f.rhodv + f.dp) + f.af * (+f.cf * bdv - bdb));
+          break;
+        case 3:
+          aa = v - f.cs;
+          jump = Q(0.5) / f.cs2 *
+                 (f.as * (-f.cs * f.rhodv + f.dp) + f.af * (-f.cf * bdv - bdb));
+          break;
+        case 4:
+          aa = v;
+          jump = rR - rL - f.dp / f.cs2;
+          break;
+        case 5:
+          if (a.ph.divbwave) {
+            aa = v;
+            jump = wR[B0 + 1 + d] - wL[B0 + 1 + d];
+          } else {
+            aa = Q(0);
+            jump = Q(0);
+          }
+          break;
+        case 6:
+          aa = v + fabs(f.b[d]) / f.sr;
+          jump = +bdv - bdb;
+          break;
+        default:
+          aa = v - fabs(f.b[d]) / f.sr;
+          jump = -bdv - bdb;
+          break;
+      }
+    } else {
+      switch (il) {
+        case 0:
+          aa = v + f.cs;
+          jump = Q(0.5) * (f.dp + f.sr * f.rhodv);
+          break;
+        case 1:
+          aa = v - f.cs;
+          jump = Q(0.5) * (f.dp - f.sr * f.rhodv);
+          break;
+        case 2:
+          aa = v;
+          jump = -f.dp + rR - rL;
+          break;
+        default: {
+          int idir = il - 3;
+          if (idir >= d) idir++;
+          aa = v;
+          jump = f.sr * (wR[1 + idir] / rR - wL[1 + idir] / rL);
+        }
+      }
+    }
+    // entropy fix: left and right eigenvalues, smalla or a modified a
+    const int te = a.ph.typeentropy[il];
+    Q smalla = Q(0);
+    if (te == VACGPU_ENTROPY_YEE) {
+      smalla = Q(a.ph.entropycoef[il]);
+    } else if (te != VACGPU_ENTROPY_NUL) {
+      Q aL = wL[1 + d] / rL, aR = wR[1 + d] / rR;
+      if (MHD) {
+        const Q bLi = wL[B0 + 1 + d], bRi = wR[B0 + 1 + d];
+        if (il < 4) {
+          const Q c2L = g * pth(a, wL, smallp) / rL;
+          const Q c2R = g * pth(a, wR, smallp) / rR;
+          Q bbL = wL[B0 + 1] * wL[B0 + 1], bbR = wR[B0 + 1] * wR[B0 + 1];
+#pragma unroll
+          for (int c = 2; c <= NDIR; c++) {
+            bbL = bbL + wL[B0 + c] * wL[B0 + c];
+            bbR = bbR + wR[B0 + c] * wR[B0 + c];
+          }
+          const Q ccL = c2L + bbL / rL, ccR = c2R + bbR / rR;
+          const Q dL = sqrt(ccL * ccL - Q(4) * c2L * (bLi * bLi) / rL);
+          const Q dR = sqrt(ccR * ccR - Q(4) * c2R * (bRi * bRi) / rR);
+          if (il == 0) {
+            aL = aL + sqrt(Q(0.5) * (ccL + dL));
+            aR = aR + sqrt(Q(0.5) * (ccR + dR));
+          } else if (il == 1) {
+            aL = aL - sqrt(Q(0.5) * (ccL + dL));
+            aR = aR - sqrt(Q(0.5) * (ccR + dR));
+          } else if (il == 2) {
+            aL = aL + sqrt(Q(0.5) * (ccL - dL));
+            aR = aR + sqrt(Q(0.5) * (ccR - dR));
+          } else {
+            aL = aL - sqrt(Q(0.5) * (ccL - dL));
+            aR = aR - sqrt(Q(0.5) * (ccR - dR));
+          }
+        } else if (il >= 6) {
+          const Q caL = fabs(bLi) / sqrt(rL), caR = fabs(bRi) / sqrt(rR);
+          if (il == 6) {
+            aL = aL + caL;
+            aR = aR + caR;
+          } else {
+            aL = aL - caL;
+            aR = aR - caR;
+          }
+        }
+      } else if (il < 2) {
+        const Q sg = il == 0 ? Q(1) : Q(-1);
+        aL = wL[1 + d] / rL + sg * sqrt(g * pth(a, wL, smallp) / rL);
+        aR = wR[1 + d] / rR + sg * sqrt(g * pth(a, wR, smallp) / rR);
+      }
+      if (te == VACGPU_ENTROPY_HARTEN)
+        smalla = rmax(rmax(Q(0), aa - aL), aR - aa);
+      else if (te == VACGPU_ENTROPY_POWELL)
+        smalla = rmax(Q(0), Q(2) * (aR - aL));
+      else if (aL < Q(0) && aR > Q(0))  // 'ratio'
+        aa = aa - Q(2) * aR * aL / (aR - aL);
+    }
+    // normalisation by dt*2/(dx(i)+dx(j)) (src/vactvd.t:131-140)
+    const Q adt = aa * qdt * Q(2) / dxs;
+    if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL)
+      smalla = smalla * qdt * Q(2) / dxs;
+    if (il < 2) am[il] = fabs(adt);
+    if (te == VACGPU_ENTROPY_NUL || te == VACGPU_ENTROPY_RATIO ||
+        fabs(adt) >= smalla)
+      f.phi[il] = fabs(adt) * jump;
+    else
+      f.phi[il] = Q(0.5) * (smalla + adt * adt / smalla) * jump;
+  }
+
+  // average (src/vacphys.mhdroe.t:4-127, src/vacphys.hdroe.t:4-45) and the
+  // waves of tvdlimit2's il loop.
+  static __device__ __forceinline__ void decompose(const SweepArgs& a,
+                                                   const Q* wL, const Q* wR,
+                                                   int d, Q smallp, Q qdt,
+                                                   Q dxs, Face& f, Q* am) {
+    const Q g = Q(a.ph.gamma);
+    const Q rL = wL[0], rR = wR[0];
+    Q bd[4] = {Q(0), Q(0), Q(0), Q(0)};
+    if (MHD) {
+      const Q rho = Q(0.5) * (rL + rR);
+      Q B[NDIR];
+#pragma unroll
+      for (int c = 0; c < NDIR; c++) {
+        f.v[c] = Q(0.5) * (wL[1 + c] / rL + wR[1 + c] / rR);
+        B[c] = Q(0.5) * (wL[B0 + 1 + c] + wR[B0 + 1 + c]);
+      }
+      const Q pL = pth(a, wL, smallp), pR = pth(a, wR, smallp);
+      const Q p = Q(0.5) * (pL + pR);
+      if (a.ph.roe_dpprim) {
+        f.dp = pR - pL;
+      } else {
+        // (g-1)*(de - v.dm + v^2/2 drho - d(B^2)/2), conservative form
+        Q s1, s2, s3;
+#pragma unroll
+        for (int c = 0; c < NDIR; c++) {
+          const Q t1 = f.v[c] * (wR[1 + c] - wL[1 + c]);
+          const Q bR = wR[B0 + 1 + c], bL = wL[B0 + 1 + c];
+          if (c == 0) {
+            s1 = t1;
+            s2 = f.v[c] * f.v[c];
+            s3 = bR * bR - bL * bL;
+          } else {
+            s1 = s1 + t1;
+            s2 = s2 + f.v[c] * f.v[c];
+            s3 = s3 + bR * bR - bL * bL;
+          }
+        }
+        f.dp = Q(a.ph.gm1) * (wR[E] - wL[E] - s1 + Q(0.5) * s2 * (rR - rL) -
+                              Q(0.5) * s3);
+      }
+      f.rhodv = wR[1 + d] - wL[1 + d] - f.v[d] * (rR - rL);
+      f.cs2 = g * p / rho;
+      Q bb = B[0] * B[0];
+#pragma unroll
+      for (int c = 1; c < NDIR; c++) bb = bb + B[c] * B[c];
+      Q cf = bb / rho + f.cs2;
+      const Q bi = B[d];
+      Q cs = rmax(Q(0), Q(0.5) * (cf - sqrt(cf * cf - Q(4) * f.cs2 * (bi * bi) /
+                                                          rho)));
+      cf = cf - cs;
+      Q af = (f.cs2 - cs) / (cf - cs);
+      af = rmin(Q(1), rmax(af, Q(0)));
+      f.as = sqrt(Q(1) - af);
+      f.af = sqrt(af);
+      f.cf = sqrt(cf);
+      f.cs = sqrt(cs);
+      f.sr = sqrt(rho);
+      if (fabs(B[d]) < tiny()) B[d] = tiny();
+      const int I = dir_i(d), J = dir_j(d);
+      if (NDIR == 2) {
+        B[I] = B[I] >= Q(0) ? Q(1) : Q(-1);
+      } else {
+        const Q t = sqrt(B[I] * B[I] + B[J] * B[J]);
+        if (t > tiny()) {
+          B[I] = B[I] / t;
+          B[J] = B[J] / t;
+        } else {
+          B[I] = sqrt(Q(0.5));
+          B[J] = sqrt(Q(0.5));
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NDIR; c++) f.b[c] = B[c];
+      // bdv, bdb of the fast/slow waves (src/vacphys.mhdroe.t:155-170) and
+      // of the Alfven waves (:172-184)
+      const Q dvI = wR[1 + I] / rR - wL[1 + I] / rL;
+      const Q dbI = wR[B0 + 1 + I] - wL[B0 + 1 + I];
+      Q bdv = f.b[I] * dvI;
+      Q bdb = f.b[I] * dbI;
+      if (NDIR == 3) {
+        const Q dvJ = wR[1 + J] / rR - wL[1 + J] / rL;
+        const Q dbJ = wR[B0 + 1 + J] - wL[B0 + 1 + J];
+        bdv = bdv + f.b[J] * dvJ;
+        bdb = bdb + f.b[J] * dbJ;
+        Q av = f.b[J] * dvI - f.b[I] * dvJ;
+        Q ab = f.b[J] * dbI - f.b[I] * dbJ;
+        bd[2] = av * Q(0.5) * (f.sr * f.sr);
+        bd[3] = ab * Q(0.5) * fsign(f.sr, f.b[d]);
+      }
+      bd[0] = bdv * fsign(f.sr * f.sr, f.b[d]);
+      bd[1] = bdb * sqrt(f.cs2) * f.sr;
+    } else {
+      const Q t0 = sqrt(rL), t2 = sqrt(rR);
+      f.sr = t0 * t2;
+      const Q t = t0 / t2;
+#pragma unroll
+      for (int c = 0; c < NDIR; c++)
+        f.v[c] = (wL[1 + c] / rL * t + wR[1 + c] / rR) / (Q(1) + t);
+      const Q pL = pth(a, wL, smallp), pR = pth(a, wR, smallp);
+      const Q hL = (pL + wL[E]) / rL;
+      const Q hR = (pR + wR[E]) / rR;
+      f.h = (hL * t + hR) / (Q(1) + t);
+      Q vv = f.v[0] * f.v[0];
+#pragma unroll
+      for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
+      Q c2 = Q(a.ph.gm1) * (f.h - Q(0.5) * vv);
+      c2 = rmax(g * smallp / f.sr, c2);
+      f.dp = (pR - pL) / c2;
+      f.cs = sqrt(c2);
+      f.rhodv = (wR[1 + d] / rR - wL[1 + d] / rL) / f.cs;
+    }
+    wave<0>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    wave<1>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    wave<2>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    if (NW > 3) wave<(NW > 3 ? 3 : 0)>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    if (NW > 4) wave<(NW > 4 ? 4 : 0)>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    if (NW > 5) wave<(NW > 5 ? 5 : 0)>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    if (NW > 6) wave<(NW > 6 ? 6 : 0)>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+    if (NW > 7) wave<(NW > 7 ? 7 : 0)>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
+  }
+
+  // Q(iw,il)*q at the Roe state (rtimes, src/vacphys.mhdroe.t:284-449 and
+  // src/vacphys.hdroe.t:144-215)
+  template <int iw, int il>
+  static __device__ __forceinline__ Q rtimes(const SweepArgs& a, const Face& f,
+                                             Q q, int d) {
+    const Q v = f.v[d];
+    if (MHD) {
+      const int I = dir_i(d), J = dir_j(d);
+      if (iw == 0) {
+        if (il <= 1) return q * f.af;
+        if (il <= 3) return q * f.as;
+        if (il == 4) return q;
+        return Q(0);
+      }
+      if (iw == E) {
+        Q vv = f.v[0] * f.v[0];
+#pragma unroll
+        for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
+        const Q g = Q(a.ph.gamma);
+        const Q v2a2 = Q(0.5) * vv + (Q(2) - g) / Q(a.ph.gm1) * f.cs2;
+        Q bv;
+        if (il < 6) {
+          bv = f.b[I] * f.v[I];
+          if (NDIR == 3) bv = bv + f.b[J] * f.v[J];
+          bv = bv * fsign(Q(1), f.b[d]);
+        } else {
+          bv = f.b[J] * f.v[I] - f.b[I] * f.v[J];
+        }
+        switch (il) {
+          case 0:
+            return q * (-f.as * f.cs * bv + f.af * (v2a2 + f.cf * (f.cf + v)));
+          case 1:
+            return q * (+f.as * f.cs * bv + f.af * (v2a2 + f.cf * (f.cf - v)));
+          case 2:
+            return q * (+f.af * f.cf * bv + f.as * (v2a2 + f.cs * (f.cs + v)));
+          case 3:
+            return q * (-f.af * f.cf * bv + f.as * (v2a2 + f.cs * (f.cs - v)));
+          case 4:
+            return q * Q(0.5) * vv;
+          case 5:
+            return a.ph.divbwave ? q * f.b[d] : Q(0);
+          case 6:
+            return +q * bv;
+          default:
+            return -q * bv;
+        }
+      }
+      if (iw <= NDIR) {
+        const int c = iw - 1;
+        const Q vw = f.v[c];
+        if (c == d) {
+          switch (il) {
+            case 0: return q * f.af * (vw + f.cf);
+            case 1: return q * f.af * (vw - f.cf);
+            case 2: return q * f.as * (vw + f.cs);
+            case 3: return q * f.as * (vw - f.cs);
+            case 4: return q * vw;
+            default: return Q(0);
+          }
+        }
+        const Q bw = f.b[c];
+        const Q sg = fsign(Q(1), f.b[d]);
+        switch (il) {
+          case 0: return q * (f.af * vw - f.as * f.cs * bw * sg);
+          case 1: return q * (f.af * vw + f.as * f.cs * bw * sg);
+          case 2: return q * (f.as * vw + f.af * f.cf * bw * sg);
+          case 3: return q * (f.as * vw - f.af * f.cf * bw * sg);
+          case 4: return q * vw;
+          case 5: return Q(0);
+          case 6: return c == I ? +q * f.b[J] : -q * f.b[I];
+          default: return c == I ? -q * f.b[J] : +q * f.b[I];
+        }
+      }
+      const int c = iw - B0 - 1;
+      if (c == d) return (il == 5 && a.ph.divbwave) ? q : Q(0);
+      const Q bw = f.b[c];
+      switch (il) {
+        case 0:
+        case 1:
+          return +q * f.as * sqrt(f.cs2) * bw / f.sr;
+        case 2:
+        case 3:
+          return -q * f.af * sqrt(f.cs2) * bw / f.sr;
+        case 4:
+        case 5:
+          return Q(0);
+        default:
+          if (c == I) return -q * f.b[J] / fsign(f.sr, f.b[d]);
+          return +q * f.b[I] / fsign(f.sr, f.b[d]);
+      }
+    } else {
+      const bool shear = il >= 3;
+      int idir = il - 3;
+      if (idir >= d) idir++;
+      if (iw == 0) return shear ? Q(0) : q;
+      if (iw == E) {
+        switch (il) {
+          case 0: return q * (f.h + v * f.cs);
+          case 1: return q * (f.h - v * f.cs);
+          case 2: {
+            Q vv = f.v[0] * f.v[0];
+#pragma unroll
+            for (int k = 1; k < NDIR; k++) vv = vv + f.v[k] * f.v[k];
+            return q * Q(0.5) * vv;
+          }
+          default: return q * f.v[idir];
+        }
+      }
+      const int c = iw - 1;
+      if (c == d) {
+        if (il == 0) return q * (v + f.cs);
+        if (il == 1) return q * (v - f.cs);
+        if (il == 2) return q * v;
+        return Q(0);
+      }
+      if (shear) return c == idir ? q : Q(0);
+      return q * f.v[c];
+    }
+  }
+
+  // One face in direction d between cell o (G index ci) and o+s: the
+  // central flux of the face states and the Roe decomposition.
+  static __device__ __forceinline__ void face(const SweepArgs& a,
+                                              const T* __restrict__ w1,
+                                              const T* __restrict__ base,
+                                              long long o, long long s, int d,
+                                              int ci, R smallp, Q qsmallp,
+                                              Q qdt, bool limit, R* F, Face& f,
+                                              Q* am) {
+    R wL[NW], wR[NW];
+    S::face_states(a, w1, base, o, s, smallp, limit, wL, wR);
+    R fL[NW], fR[NW];
+    PH::template flux<NDIR, MHD>(wL, d, a.ph, smallp, fL);
+    PH::template flux<NDIR, MHD>(wR, d, a.ph, smallp, fR);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) F[iw] = R(0.5) * (fL[iw] + fR[iw]);
+    Q qL[NW], qR[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      qL[iw] = Q(wL[iw]);
+      qR[iw] = Q(wR[iw]);
+    }
+    const Q dxs = a.a.dx[d][ci] + a.a.dx[d][ci + 1];
+    decompose(a, qL, qR, d, qsmallp, qdt, dxs, f, am);
+  }
+
+  // dvolume(ix) = dx_1*dx_2*dx_3 (gridsetup1, src/vacgrid.t:573-576)
+  static __device__ __forceinline__ Q dvol(const SweepArgs& a, const int* c) {
+    Q v = a.a.dx[0][c[0]];
+    if (NDIM > 1) v = v * a.a.dx[1][c[1]];
+    if (NDIM > 2) v = v * a.a.dx[2][c[2]];
+    return v;
+  }
+
+  // wave il's dissipative fluxes of every variable into acc
+  template <int il, int iw>
+  static __device__ __forceinline__ void dissipate_var(
+      const SweepArgs& a, const Face& fm, const Face& fp, int d, Q vm, Q vp,
+      Q dv0, int nofm, int nofp, R* acc) {
+    Q rp = rtimes<iw, il>(a, fp, fp.phi[il], d) * Q(0.25) * vp;
+    Q rm = rtimes<iw, il>(a, fm, fm.phi[il], d) * Q(0.25) * vm;
+    if ((nofp >> iw) & 1) rp = Q(0);
+    if ((nofm >> iw) & 1) rm = Q(0);
+    acc[iw] = acc[iw] + R((rp - rm) / dv0);
+  }
+  template <int il>
+  static __device__ __forceinline__ void dissipate(const SweepArgs& a,
+                                                   const Face& fm,
+                                                   const Face& fp, int d,
+                                                   Q vm, Q vp, Q dv0, int nofm,
+                                                   int nofp, R* acc) {
+    dissipate_var<il, 0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate_var<il, 1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate_var<il, 2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 3) dissipate_var<il, (NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 4) dissipate_var<il, (NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 5) dissipate_var<il, (NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 6) dissipate_var<il, (NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 7) dissipate_var<il, (NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+  }
+
+  // The corrector of one sweep (dimensions d0..d1) plus the CFL maxima of
+  // the fast waves (last substep).
+  template <int NT>
+  static __device__ void correct(const SweepArgs& a, const T* __restrict__ w,
+                                 const T* __restrict__ w1,
+                                 const T* __restrict__ base,
+                                 T* __restrict__ wout) {
+    __shared__ unsigned long long shk[NT / 32];
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = n < a.g.ncell;
+    unsigned long long key[3][2] = {{0ULL, 0ULL}, {0ULL, 0ULL}, {0ULL, 0ULL}};
+    if (active) {
+      int c[3];
+      cell_coords(a.g, n, c);
+      const long long off = gidx(a.g, c[0], c[1], c[2]);
+      const long long st[3] = {1, a.g.P, a.g.plane};
+      const long long vs = a.g.vs;
+      const double qdt = ctrl->dt;
+      const R smallp = R(ctrl->smallp);
+      const bool limit = a.ph.typefull != VACGPU_TVDMU1;
+      R acc[NW];
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
+      if (a.ph.useprim && limit) {
+        // the limiter base (the state) leaves upwindLR round-tripped
+        S::to_prim(a, smallp, acc);
+        S::to_cons(a, acc);
+      }
+      const Q qsmallp = ctrl->smallp;
+      const Q dv0 = dvol(a, c);
+      for (int d = a.d0; d <= a.d1; d++) {
+        Face fm, fp;
+        R Fm[NW], Fp[NW];
+        Q amm[2], amp[2];
+        face(a, w1, base, off - st[d], st[d], d, c[d] - 1, smallp, qsmallp,
+             qdt, limit, Fm, fm, amm);
+        face(a, w1, base, off, st[d], d, c[d], smallp, qsmallp, qdt, limit, Fp,
+             fp, amp);
+        if (a.ph.courantpar > 0.0) {
+#pragma unroll
+          for (int k = 0; k < 2; k++) {
+            const unsigned long long km = dkey((double)amm[k]);
+            const unsigned long long kp = dkey((double)amp[k]);
+            key[d][k] = km > kp ? km : kp;
+          }
+        }
+        // 'symm0' faces: no flux of those variables through the mesh edge
+        // (setnoflux in addflux, also for the dissipative flux)
+        const int nofp = c[d] == a.g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
+        const int nofm = c[d] == 2 ? a.ph.noflux[d][0] : 0;
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++) {
+          if ((nofp >> iw) & 1) Fp[iw] = R(0);
+          if ((nofm >> iw) & 1) Fm[iw] = R(0);
+        }
+        const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++)
+          acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
+        int cn[3] = {c[0], c[1], c[2]};
+        cn[d] = c[d] - 1;
+        const Q dvm = dvol(a, cn);
+        cn[d] = c[d] + 1;
+        const Q dvp = dvol(a, cn);
+        const Q vm = dv0 + dvm;  // dvolume(j)+dvolume(i) of the lower face
+        const Q vp = dvp + dv0;  // and of the upper face
+        dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+      }
+      if (a.ph.sourceunsplit) {
+        R wc[NW];
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
+        S::add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off,
+                       st, c, acc);
+      }
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
+    }
+    if (a.ph.courantpar > 0.0) {
+      for (int d = a.d0; d <= a.d1; d++) {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          unsigned long long kk = block_max_key<NT>(key[d][k], shk);
+          if (threadIdx.x == 0 && kk) {
+            unsigned long long* slot =
+                k == 0 ? &ctrl->face_cmax[d][blockIdx.x % NSLOT]
+                       : &ctrl->face_cmax2[d][blockIdx.x % NSLOT];
+            atomic_max_key(slot, kk);
+          }
+        }
+      }
+    }
+  }
+};
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
+    k_correct_roe(SweepArgs a, const typename PH::T* __restrict__ w,
+                  const typename PH::T* __restrict__ w1,
+                  const typename PH::T* __restrict__ base,
+                  typename PH::T* __restrict__ wout) {
+  RoeSweep<PH, NDIM, NDIR, MHD>::template correct<128>(a, w, w1, base, wout);
+}
+
+// (ndim, ndir, physics) instances; the MHD Roe solver needs ndir >= 2
+// (src/vacphys.mhdroe.t:25)
+template <class PH>
+void launch_correct_roe(const SweepArgs& a, const typename PH::T* w,
+                        const typename PH::T* w1, const typename PH::T* base,
+                        typename PH::T* wout, cudaStream_t st) {
+  const unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) \
+  k_correct_roe<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1, base, wout)
+  if (a.mhd) {
+    if (a.g.ndim == 2 && a.ndir == 2) KC(2, 2, true);
+    else if (a.g.ndim == 2 && a.ndir == 3) KC(2, 3, true);
+    else if (a.g.ndim == 3 && a.ndir == 3) KC(3, 3, true);
+  } else {
+    if (a.g.ndim == 1 && a.ndir == 1) KC(1, 1, false);
+    else if (a.g.ndim == 2 && a.ndir == 2) KC(2, 2, false);
+    else if (a.g.ndim == 2 && a.ndir == 3) KC(2, 3, false);
+    else if (a.g.ndim == 3 && a.ndir == 3) KC(3, 3, false);
+  }
+#undef KC
+}
+
+}  // namespace vacgpu

@@ -341,22 +341,20 @@ struct Sweep {
     for (int iw = 0; iw < NW; iw++) w1[off + iw * vs] = T(acc[iw]);
   }
 
-  // TVDLF numerical flux at the face between cell `o` and `o+st` in
-  // direction d (src/vactvdlf.t:140-259); returns the face cmax.
-  static __device__ __forceinline__ R face_flux(const SweepArgs& a,
-                                                const T* __restrict__ w1,
-                                                const T* __restrict__ base,
-                                                long long o, long long s,
-                                                int d, R smallp, R* F) {
+  // Face states of upwindLR (src/vactvdlf.t:302-367) at the face between
+  // cell `o` and `o+s`: wL = wCT(o)+ldw/2, wR = wCT(o+s)-ldw/2 with the
+  // limited slopes of `base` (in primitive variables with useprimitive,
+  // src/vactvdlf.t:325-362); the first order methods take wCT unlimited.
+  static __device__ __forceinline__ void face_states(
+      const SweepArgs& a, const T* __restrict__ w1, const T* __restrict__ base,
+      long long o, long long s, R smallp, bool limit, R* wL, R* wR) {
     const long long vs = a.g.vs;
-    R wL[NW], wR[NW];
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) {
       wL[iw] = R(w1[o + iw * vs]);
       wR[iw] = R(w1[o + iw * vs + s]);
     }
-    if (a.ph.typefull != VACGPU_TVDLF1 && a.ph.useprim) {
-      // useprimitive: primitive face states and base (src/vactvdlf.t:325-362)
+    if (limit && a.ph.useprim) {
       R bm[NW], b0[NW], b1[NW], b2[NW];
       load(base, o - s, vs, bm);
       load(base, o, vs, b0);
@@ -377,7 +375,7 @@ struct Sweep {
       }
       to_cons(a, wL);
       to_cons(a, wR);
-    } else if (a.ph.typefull != VACGPU_TVDLF1) {
+    } else if (limit) {
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) {
         const T* b = base + o + iw * vs;
@@ -388,6 +386,18 @@ struct Sweep {
         wL[iw] = wL[iw] + R(0.5) * ldL;
       }
     }
+  }
+
+  // TVDLF numerical flux at the face between cell `o` and `o+st` in
+  // direction d (src/vactvdlf.t:140-259); returns the face cmax.
+  static __device__ __forceinline__ R face_flux(const SweepArgs& a,
+                                                const T* __restrict__ w1,
+                                                const T* __restrict__ base,
+                                                long long o, long long s,
+                                                int d, R smallp, R* F) {
+    R wL[NW], wR[NW];
+    face_states(a, w1, base, o, s, smallp, a.ph.typefull != VACGPU_TVDLF1, wL,
+                wR);
     R mean[NW];
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) mean[iw] = R(0.5) * (wL[iw] + wR[iw]);

@@ -330,13 +330,20 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
     wc = base = (const T*)h->wold;
   }
-  if (h->p.typefull == VACGPU_TVDLF1) {
+  const bool roe = h->p.typefull == VACGPU_TVDMU || h->p.typefull == VACGPU_TVDMU1;
+  if (h->p.typefull == VACGPU_TVDLF1 || h->p.typefull == VACGPU_TVDMU1) {
     // typepred1='nul': onestep, the corrector alone with wCT = w
     // (src/vacio.t:286-299,511); no limiter, so the base is unused
     kbegin(h, VACGPU_K_CORRECT);
-    if (sizeof(T) == 8)
+    if (sizeof(T) == 8 && roe)
+      launch_correct_roe_fp64(a, (const double*)w, (const double*)w,
+                              (const double*)w, (double*)wout, h->st);
+    else if (sizeof(T) == 8)
       launch_correct_fp64(a, (const double*)w, (const double*)w,
                           (const double*)w, (double*)wout, h->st);
+    else if (roe)
+      launch_correct_roe_mixed(a, (const float*)w, (const float*)w,
+                               (const float*)w, (float*)wout, h->st);
     else
       launch_correct_mixed(a, (const float*)w, (const float*)w,
                            (const float*)w, (float*)wout, h->st);
@@ -361,8 +368,12 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     fill_ghosts(h, a, w1, 1);
     kend(h);
     kbegin(h, VACGPU_K_CORRECT);
-    launch_correct_fp64(a, (const double*)wc, (const double*)w1,
-                        (const double*)base, (double*)wout, h->st);
+    if (roe)
+      launch_correct_roe_fp64(a, (const double*)wc, (const double*)w1,
+                              (const double*)base, (double*)wout, h->st);
+    else
+      launch_correct_fp64(a, (const double*)wc, (const double*)w1,
+                          (const double*)base, (double*)wout, h->st);
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)wout, h->st);
@@ -389,7 +400,10 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   fill_ghosts(h, a, fw1, 1);                            \
   kend(h);                                              \
   kbegin(h, VACGPU_K_CORRECT);                          \
-  launch_correct_##SUF(a, fwc, fw1, fb, fo, h->st);     \
+  if (roe)                                              \
+    launch_correct_roe_mixed(a, fwc, fw1, fb, fo, h->st); \
+  else                                                  \
+    launch_correct_##SUF(a, fwc, fw1, fb, fo, h->st);   \
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fo, h->st); \
@@ -562,17 +576,44 @@ int check_params(const vacgpu_params* p) {
   if (!(p->eqpar[0] > 0.0)) return fail("eqpar(gamma_) must be positive");
   if (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] < 0.0)
     return fail("eqpar(eta_)<0 needs the user's specialeta, not on this path");
-  if (p->typefull != VACGPU_TVDLF && p->typefull != VACGPU_TVDLF1)
-    return fail("typefull must be tvdlf or tvdlf1");
+  if (p->typefull < VACGPU_TVDLF || p->typefull > VACGPU_TVDMU1)
+    return fail("typefull must be tvdlf, tvdlf1, tvdmu or tvdmu1");
+  const bool roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
+  if (roe) {
+    // the configurations the Roe solvers define (src/vacphys.mhdroe.t:25,
+    // :245-276; src/vacphys.hdroe.t:110-134)
+    const bool mhd = p->physics == VACGPU_PHYS_MHD;
+    if (mhd && p->ndir < 2) return fail("MHD Roe solver needs ndir>=2");
+    for (int il = 0; il < nw; il++) {
+      const int te = p->typeentropy[il];
+      if (te < VACGPU_ENTROPY_NUL || te > VACGPU_ENTROPY_YEE)
+        return fail("unknown typeentropy");
+      if (!mhd && te == VACGPU_ENTROPY_RATIO)
+        return fail("typeentropy='ratio' is undefined for the HD Roe solver");
+    }
+    if (mhd) {
+      auto lr = [&](int il) {
+        const int te = p->typeentropy[il];
+        return te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL ||
+               te == VACGPU_ENTROPY_RATIO;
+      };
+      for (int il = 1; il < 4; il++)
+        if (lr(il) && !lr(0))
+          return fail("MHD entropy fix of a fast/slow wave needs the fastRW fix");
+      if (nw == 8 && lr(7) && !lr(6))
+        return fail("MHD entropy fix of alfvLW needs the alfvRW fix");
+    }
+  }
+  const bool first_order =
+      p->typefull == VACGPU_TVDLF1 || p->typefull == VACGPU_TVDMU1;
   for (int iw = 0; iw < nw; iw++)
     if (p->typelimiter[iw] < 0 || p->typelimiter[iw] > VACGPU_LIM_ALBADA)
       return fail("unknown typelimiter");
   if (p->typelimited < 0 || p->typelimited > VACGPU_LIMITED_PREDICTOR)
     return fail("unknown typelimited");
-  if (!p->dimsplit && p->typelimited == VACGPU_LIMITED_ORIGINAL &&
-      p->typefull != VACGPU_TVDLF1)
+  if (!p->dimsplit && p->typelimited == VACGPU_LIMITED_ORIGINAL && !first_order)
     return fail("Error in TVDMUSCLF: Unsplit dim. and original is limited");
-  if (p->useprimitive && p->typefull == VACGPU_TVDLF) {
+  if (p->useprimitive && !first_order) {
     if (!p->dimsplit || p->typelimited != VACGPU_LIMITED_ORIGINAL)
       return fail("useprimitive=T is supported with dimsplit and typelimited='original'");
     if (p->smallp < 0.0 && !(p->dtpar <= 0.0 && p->courantpar > 0.0))
@@ -711,6 +752,12 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   h->pmode = 0;
   if (pm && !strcmp(pm, "f64")) h->pmode = 1;
   if (pm && !strcmp(pm, "f32")) h->pmode = 2;
+  if (h->pmode && p->precision == VACGPU_PREC_MIXED &&
+      (p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1)) {
+    delete h;
+    return fail("the Roe corrector's mixed path has the double-float "
+                "pressure recovery only (VACGPU_MIXED_PRESSURE unset)");
+  }
   DevGrid& g = h->g;
   g.ndim = p->ndim;
   g.ncell = 1;
@@ -744,7 +791,15 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.smallfix = p->smallfix;
   ph.vacuumrho = p->vacuumrho;
   ph.smallrhocoeff = p->smallrhocoeff;
-  ph.useprim = p->useprimitive && p->typefull == VACGPU_TVDLF;
+  const bool first_order =
+      p->typefull == VACGPU_TVDLF1 || p->typefull == VACGPU_TVDMU1;
+  ph.useprim = p->useprimitive && !first_order;
+  for (int il = 0; il < VACGPU_MAXNW; il++) {
+    ph.typeentropy[il] = p->typeentropy[il];
+    ph.entropycoef[il] = p->entropycoef[il];
+  }
+  ph.divbwave = p->divbwave;
+  ph.roe_dpprim = p->useprimitive;
   ph.eta = p->physics == VACGPU_PHYS_MHD ? p->eqpar[1] : 0.0;
   ph.compactres = p->compactres;
   ph.src_id = VACGPU_SRC_NONE;
@@ -758,7 +813,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   // wold: the step-start copy ('previous') or useprimitive's round-tripped
   // limiter base
   if (e == cudaSuccess && ((p->typelimited == VACGPU_LIMITED_PREVIOUS && p->dimsplit) ||
-                           (p->useprimitive && p->typefull == VACGPU_TVDLF)))
+                           ph.useprim))
     e = cudaMalloc(&h->wold, bytes);
   for (int d = 0; d < 3 && e == cudaSuccess; d++) {
     e = cudaMalloc(&h->dx[d], sizeof(double) * g.nG[d]);
@@ -825,6 +880,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   }
   Ctrl c;
   memset(&c, 0, sizeof(c));
+  c.roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
   c.dtpar = p->dtpar;
   c.courantpar = courantpar;
   c.smallp = p->smallp;

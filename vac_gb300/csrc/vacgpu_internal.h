@@ -49,7 +49,7 @@ struct DevPhys {
   double courantpar;  // <=0: no CFL evaluation (dtpar set)
   int lim[VACGPU_MAXNW];
   int typeB[VACGPU_MAXB][VACGPU_MAXNW];
-  int typefull;       // VACGPU_TVDLF / VACGPU_TVDLF1
+  int typefull;       // VACGPU_TVDLF / _TVDLF1 / _TVDMU / _TVDMU1
   int divbfix;
   int sourceunsplit;
   int smallfix;          // keeppositive before each ghost fill
@@ -69,6 +69,11 @@ struct DevPhys {
   // some face is 'fixed', 'fixed1', 'cont1' or 'grad1': ghost cells are
   // filled face by face in getboundary's order (k_ghost_face)
   int genbc;
+  // Roe dissipation of 'tvdmu'/'tvdmu1' (src/vactvd.t:86-243)
+  int typeentropy[VACGPU_MAXNW];
+  double entropycoef[VACGPU_MAXNW];
+  int divbwave;
+  int roe_dpprim;     // useprimitive: the MHD average takes dp = pR - pL
 };
 
 enum { GMAP_MIXED = -1, GMAP_PERIODIC = 0, GMAP_CONT = 1, GMAP_MIRROR = 2 };
@@ -134,6 +139,10 @@ struct Ctrl {
   int kp_r, kp_p;     // this keeppositive call found small rho / p
   // grid-level reductions (ordered-integer keys, atomicMax/atomicMin)
   unsigned long long face_cmax[3][NSLOT];  // corrector max cmax*2/(dx+dx)
+  // 'tvdmu': max |a|*dt*2/(dx+dx) of the fastRW (face_cmax) and fastLW
+  // (face_cmax2) waves of tvdlimit2 (src/vactvd.t:144-160)
+  unsigned long long face_cmax2[3][NSLOT];
+  int roe;
   unsigned long long cell_cmax[3][NSLOT];  // getdt_courant max cmax/dx
   unsigned long long pmin[NSLOT], pmax[NSLOT];
   unsigned long long rmin[NSLOT];          // keeppositive_rho min(rho)
@@ -202,6 +211,15 @@ VACGPU_DECLARE_LAUNCHERS(fp64, double)
 VACGPU_DECLARE_LAUNCHERS(mixed, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf64, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf32, float)
+
+// TVD-MUSCL corrector ('tvdmu'/'tvdmu1') with the Roe dissipation
+// (roe_fp64.cu, roe_mixed.cu); same arguments as launch_correct_*.
+void launch_correct_roe_fp64(const SweepArgs& s, const double* w,
+                             const double* w1, const double* base,
+                             double* wout, cudaStream_t st);
+void launch_correct_roe_mixed(const SweepArgs& s, const float* w,
+                              const float* w1, const float* base, float* wout,
+                              cudaStream_t st);
 
 // Fused single-kernel sweep of the mixed path (sweep_fused.cu): returns
 // false when no fused instance exists for the configuration.  `tmap` is the

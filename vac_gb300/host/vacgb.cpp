@@ -401,7 +401,30 @@ int main(int argc, char** argv) {
     if (t != "nul") tf1 = t;
   if (tf1 == "tvdlf") p.typefull = VACGPU_TVDLF;
   else if (tf1 == "tvdlf1") p.typefull = VACGPU_TVDLF1;
-  else die("Error in Advect1: " + tf1 + " is not on this path (tvdlf, tvdlf1)");
+  else if (tf1 == "tvdmu") p.typefull = VACGPU_TVDMU;
+  else if (tf1 == "tvdmu1") p.typefull = VACGPU_TVDMU1;
+  else die("Error in Advect1: " + tf1 +
+           " is not on this path (tvdlf, tvdlf1, tvdmu, tvdmu1)");
+  // typeentropy, entropycoef (per characteristic wave) and divbwave of the
+  // Roe dissipation (src/vacio.t:35,80; par/DEFAULT:47)
+  const char* entnames[] = {"nul", "harten", "powell", "ratio", "yee"};
+  for (auto* a : find_all("typeentropy")) {
+    size_t o = a->idx.empty() ? 0 : a->idx[0] - 1;
+    for (size_t k = 0; k < a->vals.size() && o + k < (size_t)nw; k++) {
+      std::string t = lower(to_str(a->vals[k]));
+      int e = -1;
+      for (int m = 0; m < 5; m++)
+        if (t == entnames[m]) e = m;
+      if (e < 0) die("No such type of entropy fix:" + t);
+      p.typeentropy[o + k] = e;
+    }
+  }
+  for (auto* a : find_all("entropycoef")) {
+    size_t o = a->idx.empty() ? 0 : a->idx[0] - 1;
+    for (size_t k = 0; k < a->vals.size() && o + k < (size_t)nw; k++)
+      p.entropycoef[o + k] = to_double(a->vals[k]);
+  }
+  p.divbwave = getb("divbwave", true);
   const char* limnames[] = {"minmod", "woodward", "superbee", "vanleer", "albada"};
   for (int iw = 0; iw < nw; iw++) {
     int l = -1;
@@ -509,7 +532,12 @@ int main(int argc, char** argv) {
       for (int iw = 0; iw < nw; iw++) std::printf("%s%d", iw ? ", " : "", p.typeB[ib][iw]);
       std::printf("]");
     }
-    std::printf("], \"ditsave\": [%d, %d], \"dtsave\": [%.17g, %.17g], \"itsave1\": [%d, %d],"
+    std::printf("], \"typeentropy\": [");
+    for (int il = 0; il < nw; il++) std::printf("%s%d", il ? ", " : "", p.typeentropy[il]);
+    std::printf("], \"entropycoef\": [");
+    for (int il = 0; il < nw; il++) std::printf("%s%.17g", il ? ", " : "", p.entropycoef[il]);
+    std::printf("], \"divbwave\": %d", p.divbwave);
+    std::printf(", \"ditsave\": [%d, %d], \"dtsave\": [%.17g, %.17g], \"itsave1\": [%d, %d],"
                 " \"tsave2\": [%.17g, %.17g], \"filenames\": [\"%s\", \"%s\"]}\n",
                 ditsave[0], ditsave[1], dtsave[0], dtsave[1], itsave[0][0], itsave[0][1],
                 tsave[1][0], tsave[1][1], fnames[0].c_str(), fnames[1].c_str());
