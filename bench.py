@@ -260,6 +260,48 @@ def run_blast(args):
     return out
 
 
+def run_tvdmu(args):
+    """The TVD-MUSCL/Roe corrector ('tvdmu', src/vactvd.t:86-243) on the
+    3-D random-mode MHD state at --tvdmu-side^3, woodward, periodic: mixed
+    and FP64 timed over --tvdmu-steps steps each, the Roe kernel's share of
+    the step, and the mixed-vs-FP64 relative L1 after those steps."""
+    import torch
+    from vac_gb300 import abi, inistate
+    from vac_gb300.engine import Engine
+    n = args.tvdmu_side
+    snap = inistate.random_modes(n, seed=0)
+    ncell = n ** 3
+    k = args.tvdmu_steps
+    stream = torch.cuda.Stream()
+    out = {"workload": "3D ideal MHD random modes %d^3 periodic, woodward, typefull='tvdmu' "
+                       "(Roe, 8 waves), %d steps timed per precision" % (n, k)}
+    res = {}
+    for name, prec in (("mixed", abi.PREC_MIXED), ("fp64", abi.PREC_FP64)):
+        p = make_params(snap, prec)
+        p.typefull = abi.TVDMU
+        e = Engine(p, snap.x, snap.w)
+        e.set_stream(stream.cuda_stream)
+        e.step(3)
+        e.upload(snap.w)
+        el = _timed_steps(e, k, stream)
+        e.timing(True)
+        e.step(1)
+        kst = e.kernel_stats()
+        e.timing(False)
+        tot = sum(v[1] for v in kst.values())
+        share = {kk: round(v[1] / tot, 4) for kk, v in kst.items() if v[0]}
+        res[name] = e.state()
+        e.close()
+        out[name] = {"steps": k, "ms_per_step": el / k * 1e3, "value": ncell * k / el,
+                     "unit": UNIT, "kernel_share": share}
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    wm, w64 = res["mixed"], res["fp64"]
+    out["rel_l1_mixed_vs_fp64"] = [
+        float(np.abs(wm[i] - w64[i]).sum() / max(np.abs(w64[i]).sum(), 1e-300))
+        for i in range(w64.shape[0])]
+    return out
+
+
 def run_served(args, capacity):
     """Config 4: a Poisson stream of 2-D (128^2..2048^2) and 3-D (64^3..256^3)
     random-mode MHD solves, 20..500 steps each, mixed precision, admitted
@@ -354,6 +396,9 @@ def main():
     ap.add_argument("--blast-side", type=int, default=512,
                     help="config 5 cells per side (0: skip)")
     ap.add_argument("--blast-steps", type=int, default=20)
+    ap.add_argument("--tvdmu-side", type=int, default=128,
+                    help="cells per side of the tvdmu/Roe case (0: skip)")
+    ap.add_argument("--tvdmu-steps", type=int, default=10)
     ap.add_argument("--side", type=int, default=N,
                     help="cells per side of the cube (smaller cases for profiling)")
     args = ap.parse_args()
@@ -465,11 +510,13 @@ def main():
                 "rel_l1_mixed_vs_fp64": rel_l1, "rel_linf_mixed_vs_fp64": linf}
         e64.close()
 
-    batched = served = plain = blast = None
+    batched = served = plain = blast = tvdmu = None
     if rank == 0 and not args.no_plain:
         plain = run_plain(args)
     if rank == 0 and args.blast_side > 0:
         blast = run_blast(args)
+    if rank == 0 and args.tvdmu_side > 0:
+        tvdmu = run_tvdmu(args)
     if rank == 0 and not args.no_batched:
         batched = run_batched(args)
     if rank == 0 and args.served > 0:
@@ -503,6 +550,7 @@ def main():
                              "alg_bytes_per_launch": alg_bytes,
                              "kernel_share": shares},
                 "fp64": fp64, "plain_fp64_config1": plain, "blast_config5": blast,
+                "tvdmu_roe": tvdmu,
                 "batched": batched, "served": served,
                 "cpu_baseline": cpu, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)

@@ -105,3 +105,45 @@ def test_par_parsing_smallfix(vacgb, tmp_path):
                                    capture_output=True, text=True, input=PAR,
                                    check=True).stdout)
     assert (d0["smallfix"], d0["smallrho"], d0["vacuumrho"]) == (0, -1.0, -1.0)
+
+
+def test_par_parsing_tvdmu(vacgb, tmp_path):
+    """typefull='tvdmu' with per-wave typeentropy/entropycoef and divbwave
+    (&methodlist, src/vacio.t:35,80); physini's default entropycoef are the
+    single precision literals 0.2 and 0.4 (src/vacphys.mhd0.t:18-28)."""
+    _setup(tmp_path)
+    par = PAR.replace("typefull=   6*'tvdlf'", "typefull=   6*'tvdmu'\n"
+                      "        typeentropy=4*'harten',2*'nul'\n"
+                      "        typeentropy(6)='powell'\n"
+                      "        entropycoef(5)=0.3D0\n        divbwave=F")
+    d = json.loads(subprocess.run([vacgb, "--dump-params"], cwd=tmp_path,
+                                  capture_output=True, text=True, input=par,
+                                  check=True).stdout)
+    assert d["typefull"] == abi.TVDMU and d["divbwave"] == 0
+    assert d["typeentropy"] == [abi.ENTROPY_HARTEN] * 4 + [abi.ENTROPY_NUL, abi.ENTROPY_POWELL]
+    f02 = float(np.float32(0.2))
+    assert d["entropycoef"] == [f02] * 4 + [0.3, -1.0]
+    d0 = json.loads(subprocess.run([vacgb, "--dump-params"], cwd=tmp_path,
+                                   capture_output=True, text=True, input=PAR,
+                                   check=True).stdout)
+    assert d0["typeentropy"] == [0] * 6 and d0["divbwave"] == 1
+    assert d0["entropycoef"] == [abi.default_entropycoef(abi.PHYS_MHD, il) for il in range(6)]
+
+
+@pytest.mark.gpu
+def test_run_tvdmu_writes_vac_outputs(vacgb, tmp_path):
+    """The host program on the TVD-MUSCL/Roe path: .out snapshots bit-equal
+    to the oracle."""
+    s = _setup(tmp_path)
+    par = PAR.replace("typefull=   6*'tvdlf'", "typefull=   6*'tvdmu'")
+    r = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True, input=par)
+    assert r.returncode == 0, r.stdout + r.stderr
+    p = inistate.params_for(s, limiter="woodward")
+    p.typelimiter[1] = abi.LIM_MINMOD
+    p.typefull = abi.TVDMU
+    o = Oracle(p, s.x, s.w)
+    for snap, it in ((1, 10), (2, 20)):
+        got = vacfile.read(str(tmp_path / "ot.out"), snapshot=snap)
+        o.step(it - o.it)
+        assert got.it == it and got.t == o.t
+        assert np.array_equal(got.w.view(np.uint64), o.state().view(np.uint64))

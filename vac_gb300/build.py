@@ -26,7 +26,7 @@ UNITS = [
     ("sweep_fp64.cu", ["-fmad=false"]),
     ("roe_fp64.cu", ["-fmad=false"]),
     ("control.cu", ["-fmad=false"]),
-    ("roe_mixed.cu", ["--use_fast_math"]),
+    ("roe_mixed.cu", []),
     ("sweep_mixed.cu", ["--use_fast_math"]),
     ("vacgpu.cu", []),
     ("noalloc.cu", []),

@@ -10,11 +10,12 @@
 // reference's order: the central fluxes of all variables (addflux with
 // qdt), then wave by wave the dissipative fluxes R(iw,il)*phi(il) scaled by
 // (dvolume(i)+dvolume(j))/4 (addflux with qdt=-1: += (F(i)-F(i-1))/dvolume).
-// The Roe decomposition runs in IEEE double on both paths; the FP64 instance
-// (roe_fp64.cu, built without FMA contraction) keeps every array statement's
-// operation order and is bit-identical to the CPU restatement, the mixed
-// instance (roe_mixed.cu) forms its FP32 face states and central fluxes as
-// the TVDLF corrector does and adds the double dissipation to FP32 sums.
+// The FP64 instance (roe_fp64.cu, built without FMA contraction) keeps every
+// array statement's operation order and is bit-identical to the CPU
+// restatement.  The mixed instance (roe_mixed.cu, IEEE FP32 division and
+// square root) runs the solver in FP32 with the conservative pressure jump
+// dp in double and the thermal pressures from the double-float recovery of
+// physics_mixed.cuh.
 #pragma once
 #include "sweep.cuh"
 
@@ -26,10 +27,14 @@ struct RoeSweep {
   typedef typename PH::T T;
   typedef typename PH::R R;
   typedef Lay<NDIR, MHD> L;
-  // the Roe decomposition runs in double on both paths: its jumps and the
-  // conservative dp cancel, which FP32 cannot carry to the mixed path's
-  // tolerance; the face states and central fluxes stay in R
-  typedef double Q;
+  // The Roe average and the entropy-fix speeds run in D (double), the
+  // waves' jumps, the right eigenvectors and the dissipative sums in Q
+  // (= R): the slow speed and the fast/slow weights af, as cancel at low
+  // beta and near the MHD degeneracies, where their square roots amplify
+  // the rounding of their arguments, so the mixed path forms them (and the
+  // conservative dp, which cancels to the pressure jump) in double.
+  typedef double D;
+  typedef R Q;
   static constexpr int NW = L::NW;
   static constexpr int E = L::E;
   static constexpr int B0 = L::B0;
@@ -38,25 +43,26 @@ struct RoeSweep {
   // quantities of src/vacphys.mhdroe.t:18-19,150-153 and
   // src/vacphys.hdroe.t:63-65) and the limiter function of every wave.
   struct Face {
-    Q v[NDIR];   // MHD: mean velocity; HD: Roe-averaged velocity
-    Q b[NDIR];   // MHD: B_idim (|B_idim| >= smalldouble), beta_idir, beta_jdir
-    Q sr;        // MHD: sqrt(mean rho); HD: sqrt(rhoL)*sqrt(rhoR)
-    Q cf, cs, af, as, cs2;  // MHD: fast/slow speeds, weights, sound^2
+    D v[NDIR];   // MHD: mean velocity; HD: Roe-averaged velocity
+    D b[NDIR];   // MHD: B_idim (|B_idim| >= smalldouble), beta_idir, beta_jdir
+    D sr;        // MHD: sqrt(mean rho); HD: sqrt(rhoL)*sqrt(rhoR)
+    D cf, cs, af, as, cs2;  // MHD: fast/slow speeds, weights, sound^2
                             // HD: cs = sound speed c
-    Q h;         // HD: Roe-averaged enthalpy
-    Q dp, rhodv; // MHD: pR-pL (conservative form), rho*dv_idim
+    D h;         // HD: Roe-averaged enthalpy
+    D dp, rhodv; // MHD: pR-pL (conservative form), rho*dv_idim
                  // HD: (pR-pL)/c^2, (vR-vL)_idim/c
-    Q phi[NW];   // getphi's TVD-MUSCL phi = |a*dt/dx|*jump (entropy fixed)
+    D phi[NW];   // getphi's TVD-MUSCL phi = |a*dt/dx|*jump (entropy fixed)
   };
 
   // Fortran SIGN(a,b), MAX and MIN as the oracle's selects
-  static __device__ __forceinline__ Q fsign(Q a, Q b) {
+  static __device__ __forceinline__ D fsign(D a, D b) {
     return copysign(fabs(a), b);
   }
-  static __device__ __forceinline__ Q rmax(Q a, Q b) { return a > b ? a : b; }
-  static __device__ __forceinline__ Q rmin(Q a, Q b) { return a < b ? a : b; }
-  // smalldouble of the reference
-  static __device__ __forceinline__ Q tiny() { return 1.0e-99; }
+  static __device__ __forceinline__ D rmax(D a, D b) { return a > b ? a : b; }
+  static __device__ __forceinline__ D rmin(D a, D b) { return a < b ? a : b; }
+  // smalldouble of the reference (1e-99), a normal number in FP32 for the
+  // mixed instance
+  static __device__ __forceinline__ D tiny() { return 1.0e-99; }
 
   // idir = idim+1-ndir*(idim/ndir) and jdir likewise, 1-based
   // (src/vacphys.mhdroe.t:97,145-146); 0-based here
@@ -69,26 +75,27 @@ struct RoeSweep {
     return d1 + 1 - NDIR * (d1 / NDIR) - 1;
   }
 
-  // getpthermal(.true.): p clipped at smallp
-  static __device__ __forceinline__ Q pth(const SweepArgs& a, const Q* u,
-                                          Q smallp) {
-    Q p = pthermal_raw<NDIR, MHD>(u, a.ph);
+  // getpthermal(.true.): p clipped at smallp, in double
+  static __device__ __forceinline__ double pthd(const SweepArgs& a,
+                                                const D* u, double smallp) {
+    const double p = pthermal_raw<NDIR, MHD>(u, a.ph);
     return p >= smallp ? p : smallp;
   }
-
   // Eigenvalue a and jump L*dw of wave il with its entropy fix
   // (geteigenjump, src/vacphys.mhdroe.t:130-281 and
   // src/vacphys.hdroe.t:48-141; entropyfix, src/vactvd.t:422-451), then
   // phi of getphi's TVD-MUSCL branch (src/vactvd.t:227-243).  dxs =
   // dx(i)+dx(j); am receives |a*dt*2/dxs| of the two fast waves.
   template <int il>
-  static __device__ __forceinline__ void wave(const SweepArgs& a, const Q* wL,
-                                              const Q* wR, int d, Q smallp,
-                                              Q qdt, Q dxs, const Q* bd,
-                                              Face& f, Q* am) {
-    const Q g = Q(a.ph.gamma);
-    const Q rL = wL[0], rR = wR[0];
-    const Q v = f.v[d];
+  static __device__ __forceinline__ void wave(const SweepArgs& a, const D* wL,
+                                              const D* wR, int d, double smallp,
+                                              D qdt, D dxs, const D* bd,
+                                              Face& f, D* am) {
+    // the jumps and eigenvalues in Q from the double Roe state
+    const Q rL = Q(wL[0]), rR = Q(wR[0]);
+    const Q v = Q(f.v[d]);
+    const Q cf = Q(f.cf), cs = Q(f.cs), af = Q(f.af), as = Q(f.as);
+    const Q cs2 = Q(f.cs2), rhodv = Q(f.rhodv), dp = Q(f.dp), sr = Q(f.sr);
     Q aa, jump;
     if (MHD) {
       // bd = {bdv, bdb} of the fast/slow waves, then of the Alfven waves
@@ -96,105 +103,110 @@ struct RoeSweep {
       const Q bdb = il < 6 ? bd[1] : bd[3];
       switch (il) {
         case 0:
-          aa = v + f.cf;
-          jump = Q(0.5) / f.cs2 *
-                 (f.af * (+f.cf * f.rhodv + f.dp) + f.as * (-f.cs * bdv + bdb));
+          aa = v + cf;
+          jump = Q(0.5) / cs2 *
+                 (af * (+cf * rhodv + dp) + as * (-cs * bdv + bdb));
           break;
         case 1:
-          aa = v - f.cf;
-          jump = Q(0.5) / f.cs2 *
-                 (f.af * (-f.cf * f.rhodv + f.dp) + f.as * (+f.cs * bdv + bdb));
+          aa = v - cf;
+          jump = Q(0.5) / cs2 *
+                 (af * (-cf * rhodv + dp) + as * (+cs * bdv + bdb));
           break;
         case 2:
-          aa = v + f.cs;
-          jump = Q(0.5) / f.cs2 *
-                 (f.as * (+f.cs * f.rhodv + f.dp) + f.af * (+f.cf * bdv - bdb));
+          aa = v + cs;
+          jump = Q(0.5) / cs2 *
+                 (as * (+cs * rhodv + dp) + af * (+cf * bdv - bdb));
           break;
         case 3:
-          aa = v - f.cs;
-          jump = Q(0.5) / f.cs2 *
-                 (f.as * (-f.cs * f.rhodv + f.dp) + f.af * (-f.cf * bdv - bdb));
+          aa = v - cs;
+          jump = Q(0.5) / cs2 *
+                 (as * (-cs * rhodv + dp) + af * (-cf * bdv - bdb));
           break;
         case 4:
           aa = v;
-          jump = rR - rL - f.dp / f.cs2;
+          jump = rR - rL - dp / cs2;
           break;
         case 5:
           if (a.ph.divbwave) {
             aa = v;
-            jump = wR[B0 + 1 + d] - wL[B0 + 1 + d];
+            jump = Q(wR[B0 + 1 + d]) - Q(wL[B0 + 1 + d]);
           } else {
             aa = Q(0);
             jump = Q(0);
           }
           break;
         case 6:
-          aa = v + fabs(f.b[d]) / f.sr;
+          aa = v + Q(fabs(f.b[d])) / sr;
           jump = +bdv - bdb;
           break;
         default:
-          aa = v - fabs(f.b[d]) / f.sr;
+          aa = v - Q(fabs(f.b[d])) / sr;
           jump = -bdv - bdb;
           break;
       }
     } else {
       switch (il) {
         case 0:
-          aa = v + f.cs;
-          jump = Q(0.5) * (f.dp + f.sr * f.rhodv);
+          aa = v + cs;
+          jump = Q(0.5) * (dp + sr * rhodv);
           break;
         case 1:
-          aa = v - f.cs;
-          jump = Q(0.5) * (f.dp - f.sr * f.rhodv);
+          aa = v - cs;
+          jump = Q(0.5) * (dp - sr * rhodv);
           break;
         case 2:
           aa = v;
-          jump = -f.dp + rR - rL;
+          jump = -dp + rR - rL;
           break;
         default: {
           int idir = il - 3;
           if (idir >= d) idir++;
           aa = v;
-          jump = f.sr * (wR[1 + idir] / rR - wL[1 + idir] / rL);
+          jump = sr * (Q(wR[1 + idir]) / rR - Q(wL[1 + idir]) / rL);
         }
       }
     }
-    // entropy fix: left and right eigenvalues, smalla or a modified a
+    // entropy fix: left and right eigenvalues, smalla or a modified a, in
+    // double (the slow speeds of the left and right states cancel as the
+    // averaged one does)
     const int te = a.ph.typeentropy[il];
     Q smalla = Q(0);
     if (te == VACGPU_ENTROPY_YEE) {
       smalla = Q(a.ph.entropycoef[il]);
     } else if (te != VACGPU_ENTROPY_NUL) {
-      Q aL = wL[1 + d] / rL, aR = wR[1 + d] / rR;
+      const double g = a.ph.gamma;
+      const double dL = wL[0], dR = wR[0];
+      double aL = (double)wL[1 + d] / dL, aR = (double)wR[1 + d] / dR;
       if (MHD) {
-        const Q bLi = wL[B0 + 1 + d], bRi = wR[B0 + 1 + d];
+        const double bLi = wL[B0 + 1 + d], bRi = wR[B0 + 1 + d];
         if (il < 4) {
-          const Q c2L = g * pth(a, wL, smallp) / rL;
-          const Q c2R = g * pth(a, wR, smallp) / rR;
-          Q bbL = wL[B0 + 1] * wL[B0 + 1], bbR = wR[B0 + 1] * wR[B0 + 1];
+          const double c2L = g * pthd(a, wL, smallp) / dL;
+          const double c2R = g * pthd(a, wR, smallp) / dR;
+          double bbL = (double)wL[B0 + 1] * (double)wL[B0 + 1];
+          double bbR = (double)wR[B0 + 1] * (double)wR[B0 + 1];
 #pragma unroll
           for (int c = 2; c <= NDIR; c++) {
-            bbL = bbL + wL[B0 + c] * wL[B0 + c];
-            bbR = bbR + wR[B0 + c] * wR[B0 + c];
+            bbL = bbL + (double)wL[B0 + c] * (double)wL[B0 + c];
+            bbR = bbR + (double)wR[B0 + c] * (double)wR[B0 + c];
           }
-          const Q ccL = c2L + bbL / rL, ccR = c2R + bbR / rR;
-          const Q dL = sqrt(ccL * ccL - Q(4) * c2L * (bLi * bLi) / rL);
-          const Q dR = sqrt(ccR * ccR - Q(4) * c2R * (bRi * bRi) / rR);
+          const double ccL = c2L + bbL / dL, ccR = c2R + bbR / dR;
+          const double qL = sqrt(ccL * ccL - 4.0 * c2L * (bLi * bLi) / dL);
+          const double qR = sqrt(ccR * ccR - 4.0 * c2R * (bRi * bRi) / dR);
           if (il == 0) {
-            aL = aL + sqrt(Q(0.5) * (ccL + dL));
-            aR = aR + sqrt(Q(0.5) * (ccR + dR));
+            aL = aL + sqrt(0.5 * (ccL + qL));
+            aR = aR + sqrt(0.5 * (ccR + qR));
           } else if (il == 1) {
-            aL = aL - sqrt(Q(0.5) * (ccL + dL));
-            aR = aR - sqrt(Q(0.5) * (ccR + dR));
+            aL = aL - sqrt(0.5 * (ccL + qL));
+            aR = aR - sqrt(0.5 * (ccR + qR));
           } else if (il == 2) {
-            aL = aL + sqrt(Q(0.5) * (ccL - dL));
-            aR = aR + sqrt(Q(0.5) * (ccR - dR));
+            aL = aL + sqrt(0.5 * (ccL - qL));
+            aR = aR + sqrt(0.5 * (ccR - qR));
           } else {
-            aL = aL - sqrt(Q(0.5) * (ccL - dL));
-            aR = aR - sqrt(Q(0.5) * (ccR - dR));
+            aL = aL - sqrt(0.5 * (ccL - qL));
+            aR = aR - sqrt(0.5 * (ccR - qR));
           }
         } else if (il >= 6) {
-          const Q caL = fabs(bLi) / sqrt(rL), caR = fabs(bRi) / sqrt(rR);
+          const double caL = fabs(bLi) / sqrt(dL), caR = fabs(bRi) / sqrt(dR);
           if (il == 6) {
             aL = aL + caL;
             aR = aR + caR;
@@ -204,21 +216,25 @@ struct RoeSweep {
           }
         }
       } else if (il < 2) {
-        const Q sg = il == 0 ? Q(1) : Q(-1);
-        aL = wL[1 + d] / rL + sg * sqrt(g * pth(a, wL, smallp) / rL);
-        aR = wR[1 + d] / rR + sg * sqrt(g * pth(a, wR, smallp) / rR);
+        const double sg = il == 0 ? 1.0 : -1.0;
+        aL = (double)wL[1 + d] / dL + sg * sqrt(g * pthd(a, wL, smallp) / dL);
+        aR = (double)wR[1 + d] / dR + sg * sqrt(g * pthd(a, wR, smallp) / dR);
       }
-      if (te == VACGPU_ENTROPY_HARTEN)
-        smalla = rmax(rmax(Q(0), aa - aL), aR - aa);
-      else if (te == VACGPU_ENTROPY_POWELL)
-        smalla = rmax(Q(0), Q(2) * (aR - aL));
-      else if (aL < Q(0) && aR > Q(0))  // 'ratio'
-        aa = aa - Q(2) * aR * aL / (aR - aL);
+      const double ad = aa;
+      if (te == VACGPU_ENTROPY_HARTEN) {
+        const double m = 0.0 > ad - aL ? 0.0 : ad - aL;
+        smalla = Q(m > aR - ad ? m : aR - ad);
+      } else if (te == VACGPU_ENTROPY_POWELL) {
+        const double q = 2.0 * (aR - aL);
+        smalla = Q(0.0 > q ? 0.0 : q);
+      } else if (aL < 0.0 && aR > 0.0) {  // 'ratio'
+        aa = Q(ad - 2.0 * aR * aL / (aR - aL));
+      }
     }
     // normalisation by dt*2/(dx(i)+dx(j)) (src/vactvd.t:131-140)
-    const Q adt = aa * qdt * Q(2) / dxs;
+    const Q adt = aa * Q(qdt) * Q(2) / Q(dxs);
     if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL)
-      smalla = smalla * qdt * Q(2) / dxs;
+      smalla = smalla * Q(qdt) * Q(2) / Q(dxs);
     if (il < 2) am[il] = fabs(adt);
     if (te == VACGPU_ENTROPY_NUL || te == VACGPU_ENTROPY_RATIO ||
         fabs(adt) >= smalla)
@@ -230,114 +246,130 @@ struct RoeSweep {
   // average (src/vacphys.mhdroe.t:4-127, src/vacphys.hdroe.t:4-45) and the
   // waves of tvdlimit2's il loop.
   static __device__ __forceinline__ void decompose(const SweepArgs& a,
-                                                   const Q* wL, const Q* wR,
-                                                   int d, Q smallp, Q qdt,
-                                                   Q dxs, Face& f, Q* am) {
-    const Q g = Q(a.ph.gamma);
-    const Q rL = wL[0], rR = wR[0];
-    Q bd[4] = {Q(0), Q(0), Q(0), Q(0)};
+                                                   const D* wL, const D* wR,
+                                                   int d, double smallp, D qdt,
+                                                   D dxs, Face& f, D* am) {
+    // The averages are formed in double (on the mixed path too): the slow
+    // speed and the fast/slow weights af, as cancel at low beta and near
+    // the MHD degeneracies, where their square roots amplify the rounding;
+    // the waves and eigenvectors then run in D.
+    const D rL = wL[0], rR = wR[0];
+    const double dL = rL, dR = rR;
+    D bd[4] = {D(0), D(0), D(0), D(0)};
     if (MHD) {
-      const Q rho = Q(0.5) * (rL + rR);
-      Q B[NDIR];
+      const double rho = 0.5 * (dL + dR);
+      double B[NDIR];
 #pragma unroll
       for (int c = 0; c < NDIR; c++) {
-        f.v[c] = Q(0.5) * (wL[1 + c] / rL + wR[1 + c] / rR);
-        B[c] = Q(0.5) * (wL[B0 + 1 + c] + wR[B0 + 1 + c]);
+        f.v[c] = D(0.5) * (wL[1 + c] / rL + wR[1 + c] / rR);
+        B[c] = 0.5 * ((double)wL[B0 + 1 + c] + (double)wR[B0 + 1 + c]);
       }
-      const Q pL = pth(a, wL, smallp), pR = pth(a, wR, smallp);
-      const Q p = Q(0.5) * (pL + pR);
+      const double pL = pthd(a, wL, smallp), pR = pthd(a, wR, smallp);
+      const double p = 0.5 * (pL + pR);
       if (a.ph.roe_dpprim) {
-        f.dp = pR - pL;
+        f.dp = D(pR - pL);
       } else {
         // (g-1)*(de - v.dm + v^2/2 drho - d(B^2)/2), conservative form
-        Q s1, s2, s3;
+        double s1, s2, s3;
 #pragma unroll
         for (int c = 0; c < NDIR; c++) {
-          const Q t1 = f.v[c] * (wR[1 + c] - wL[1 + c]);
-          const Q bR = wR[B0 + 1 + c], bL = wL[B0 + 1 + c];
+          const double vc = f.v[c];
+          const double t1 = vc * ((double)wR[1 + c] - (double)wL[1 + c]);
+          const double bR = wR[B0 + 1 + c], bL = wL[B0 + 1 + c];
           if (c == 0) {
             s1 = t1;
-            s2 = f.v[c] * f.v[c];
+            s2 = vc * vc;
             s3 = bR * bR - bL * bL;
           } else {
             s1 = s1 + t1;
-            s2 = s2 + f.v[c] * f.v[c];
+            s2 = s2 + vc * vc;
             s3 = s3 + bR * bR - bL * bL;
           }
         }
-        f.dp = Q(a.ph.gm1) * (wR[E] - wL[E] - s1 + Q(0.5) * s2 * (rR - rL) -
-                              Q(0.5) * s3);
+        f.dp = D(a.ph.gm1 * ((double)wR[E] - (double)wL[E] - s1 +
+                             0.5 * s2 * (dR - dL) - 0.5 * s3));
       }
-      f.rhodv = wR[1 + d] - wL[1 + d] - f.v[d] * (rR - rL);
-      f.cs2 = g * p / rho;
-      Q bb = B[0] * B[0];
+      f.rhodv = D((double)wR[1 + d] - (double)wL[1 + d] -
+                  (double)f.v[d] * (dR - dL));
+      const double cs2 = a.ph.gamma * p / rho;
+      double bb = B[0] * B[0];
 #pragma unroll
       for (int c = 1; c < NDIR; c++) bb = bb + B[c] * B[c];
-      Q cf = bb / rho + f.cs2;
-      const Q bi = B[d];
-      Q cs = rmax(Q(0), Q(0.5) * (cf - sqrt(cf * cf - Q(4) * f.cs2 * (bi * bi) /
-                                                          rho)));
+      double cf = bb / rho + cs2;
+      const double bi = B[d];
+      const double q = 0.5 * (cf - sqrt(cf * cf - 4.0 * cs2 * (bi * bi) / rho));
+      double cs = 0.0 > q ? 0.0 : q;
       cf = cf - cs;
-      Q af = (f.cs2 - cs) / (cf - cs);
-      af = rmin(Q(1), rmax(af, Q(0)));
-      f.as = sqrt(Q(1) - af);
-      f.af = sqrt(af);
-      f.cf = sqrt(cf);
-      f.cs = sqrt(cs);
-      f.sr = sqrt(rho);
-      if (fabs(B[d]) < tiny()) B[d] = tiny();
+      double af = (cs2 - cs) / (cf - cs);
+      af = af > 0.0 ? af : 0.0;
+      af = 1.0 < af ? 1.0 : af;
+      f.as = D(sqrt(1.0 - af));
+      f.af = D(sqrt(af));
+      f.cf = D(sqrt(cf));
+      f.cs = D(sqrt(cs));
+      f.cs2 = D(cs2);
+      f.sr = D(sqrt(rho));
       const int I = dir_i(d), J = dir_j(d);
       if (NDIR == 2) {
-        B[I] = B[I] >= Q(0) ? Q(1) : Q(-1);
+        B[I] = B[I] >= 0.0 ? 1.0 : -1.0;
       } else {
-        const Q t = sqrt(B[I] * B[I] + B[J] * B[J]);
-        if (t > tiny()) {
+        const double t = sqrt(B[I] * B[I] + B[J] * B[J]);
+        if (t > 1.0e-99) {
           B[I] = B[I] / t;
           B[J] = B[J] / t;
         } else {
-          B[I] = sqrt(Q(0.5));
-          B[J] = sqrt(Q(0.5));
+          B[I] = sqrt(0.5);
+          B[J] = sqrt(0.5);
         }
       }
 #pragma unroll
-      for (int c = 0; c < NDIR; c++) f.b[c] = B[c];
+      for (int c = 0; c < NDIR; c++) f.b[c] = D(B[c]);
+      // avoid sgn(b_idim)==0
+      if (fabs(f.b[d]) < tiny()) f.b[d] = tiny();
       // bdv, bdb of the fast/slow waves (src/vacphys.mhdroe.t:155-170) and
       // of the Alfven waves (:172-184)
-      const Q dvI = wR[1 + I] / rR - wL[1 + I] / rL;
-      const Q dbI = wR[B0 + 1 + I] - wL[B0 + 1 + I];
-      Q bdv = f.b[I] * dvI;
-      Q bdb = f.b[I] * dbI;
+      const D dvI = wR[1 + I] / rR - wL[1 + I] / rL;
+      const D dbI = wR[B0 + 1 + I] - wL[B0 + 1 + I];
+      D bdv = f.b[I] * dvI;
+      D bdb = f.b[I] * dbI;
       if (NDIR == 3) {
-        const Q dvJ = wR[1 + J] / rR - wL[1 + J] / rL;
-        const Q dbJ = wR[B0 + 1 + J] - wL[B0 + 1 + J];
+        const D dvJ = wR[1 + J] / rR - wL[1 + J] / rL;
+        const D dbJ = wR[B0 + 1 + J] - wL[B0 + 1 + J];
         bdv = bdv + f.b[J] * dvJ;
         bdb = bdb + f.b[J] * dbJ;
-        Q av = f.b[J] * dvI - f.b[I] * dvJ;
-        Q ab = f.b[J] * dbI - f.b[I] * dbJ;
-        bd[2] = av * Q(0.5) * (f.sr * f.sr);
-        bd[3] = ab * Q(0.5) * fsign(f.sr, f.b[d]);
+        D av = f.b[J] * dvI - f.b[I] * dvJ;
+        D ab = f.b[J] * dbI - f.b[I] * dbJ;
+        bd[2] = av * D(0.5) * (f.sr * f.sr);
+        bd[3] = ab * D(0.5) * fsign(f.sr, f.b[d]);
       }
       bd[0] = bdv * fsign(f.sr * f.sr, f.b[d]);
       bd[1] = bdb * sqrt(f.cs2) * f.sr;
     } else {
-      const Q t0 = sqrt(rL), t2 = sqrt(rR);
-      f.sr = t0 * t2;
-      const Q t = t0 / t2;
+      const double t0 = sqrt(dL), t2 = sqrt(dR);
+      const double sr = t0 * t2;
+      f.sr = D(sr);
+      const double t = t0 / t2;
+      double v[NDIR];
 #pragma unroll
-      for (int c = 0; c < NDIR; c++)
-        f.v[c] = (wL[1 + c] / rL * t + wR[1 + c] / rR) / (Q(1) + t);
-      const Q pL = pth(a, wL, smallp), pR = pth(a, wR, smallp);
-      const Q hL = (pL + wL[E]) / rL;
-      const Q hR = (pR + wR[E]) / rR;
-      f.h = (hL * t + hR) / (Q(1) + t);
-      Q vv = f.v[0] * f.v[0];
+      for (int c = 0; c < NDIR; c++) {
+        v[c] = ((double)wL[1 + c] / dL * t + (double)wR[1 + c] / dR) / (1.0 + t);
+        f.v[c] = D(v[c]);
+      }
+      const double pL = pthd(a, wL, smallp), pR = pthd(a, wR, smallp);
+      const double hL = (pL + (double)wL[E]) / dL;
+      const double hR = (pR + (double)wR[E]) / dR;
+      const double h = (hL * t + hR) / (1.0 + t);
+      f.h = D(h);
+      double vv = v[0] * v[0];
 #pragma unroll
-      for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
-      Q c2 = Q(a.ph.gm1) * (f.h - Q(0.5) * vv);
-      c2 = rmax(g * smallp / f.sr, c2);
-      f.dp = (pR - pL) / c2;
-      f.cs = sqrt(c2);
-      f.rhodv = (wR[1 + d] / rR - wL[1 + d] / rL) / f.cs;
+      for (int c = 1; c < NDIR; c++) vv = vv + v[c] * v[c];
+      double c2 = a.ph.gm1 * (h - 0.5 * vv);
+      const double c2min = a.ph.gamma * smallp / sr;
+      c2 = c2min > c2 ? c2min : c2;
+      f.dp = D((pR - pL) / c2);
+      const double c = sqrt(c2);
+      f.cs = D(c);
+      f.rhodv = D(((double)wR[1 + d] / dR - (double)wL[1 + d] / dL) / c);
     }
     wave<0>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
     wave<1>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
@@ -349,11 +381,26 @@ struct RoeSweep {
     if (NW > 7) wave<(NW > 7 ? 7 : 0)>(a, wL, wR, d, smallp, qdt, dxs, bd, f, am);
   }
 
-  // Q(iw,il)*q at the Roe state (rtimes, src/vacphys.mhdroe.t:284-449 and
+  // R(iw,il)*q at the Roe state (rtimes, src/vacphys.mhdroe.t:284-449 and
   // src/vacphys.hdroe.t:144-215)
   template <int iw, int il>
-  static __device__ __forceinline__ Q rtimes(const SweepArgs& a, const Face& f,
+  static __device__ __forceinline__ Q rtimes(const SweepArgs& a, const Face& f0,
                                              Q q, int d) {
+    struct {
+      Q v[NDIR], b[NDIR], sr, cf, cs, af, as, cs2, h;
+    } f;
+#pragma unroll
+    for (int c = 0; c < NDIR; c++) {
+      f.v[c] = Q(f0.v[c]);
+      f.b[c] = Q(f0.b[c]);
+    }
+    f.sr = Q(f0.sr);
+    f.cf = Q(f0.cf);
+    f.cs = Q(f0.cs);
+    f.af = Q(f0.af);
+    f.as = Q(f0.as);
+    f.cs2 = Q(f0.cs2);
+    f.h = Q(f0.h);
     const Q v = f.v[d];
     if (MHD) {
       const int I = dir_i(d), J = dir_j(d);
@@ -373,7 +420,7 @@ struct RoeSweep {
         if (il < 6) {
           bv = f.b[I] * f.v[I];
           if (NDIR == 3) bv = bv + f.b[J] * f.v[J];
-          bv = bv * fsign(Q(1), f.b[d]);
+          bv = bv * Q(fsign(1.0, f.b[d]));
         } else {
           bv = f.b[J] * f.v[I] - f.b[I] * f.v[J];
         }
@@ -410,7 +457,7 @@ struct RoeSweep {
           }
         }
         const Q bw = f.b[c];
-        const Q sg = fsign(Q(1), f.b[d]);
+        const Q sg = Q(fsign(1.0, f.b[d]));
         switch (il) {
           case 0: return q * (f.af * vw - f.as * f.cs * bw * sg);
           case 1: return q * (f.af * vw + f.as * f.cs * bw * sg);
@@ -436,8 +483,8 @@ struct RoeSweep {
         case 5:
           return Q(0);
         default:
-          if (c == I) return -q * f.b[J] / fsign(f.sr, f.b[d]);
-          return +q * f.b[I] / fsign(f.sr, f.b[d]);
+          if (c == I) return -q * f.b[J] / Q(fsign(f.sr, f.b[d]));
+          return +q * f.b[I] / Q(fsign(f.sr, f.b[d]));
       }
     } else {
       const bool shear = il >= 3;
@@ -475,9 +522,9 @@ struct RoeSweep {
                                               const T* __restrict__ w1,
                                               const T* __restrict__ base,
                                               long long o, long long s, int d,
-                                              int ci, R smallp, Q qsmallp,
-                                              Q qdt, bool limit, R* F, Face& f,
-                                              Q* am) {
+                                              int ci, R smallp, double qsmallp,
+                                              D qdt, bool limit, R* F, Face& f,
+                                              D* am) {
     R wL[NW], wR[NW];
     S::face_states(a, w1, base, o, s, smallp, limit, wL, wR);
     R fL[NW], fR[NW];
@@ -485,22 +532,22 @@ struct RoeSweep {
     PH::template flux<NDIR, MHD>(wR, d, a.ph, smallp, fR);
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) F[iw] = R(0.5) * (fL[iw] + fR[iw]);
-    Q qL[NW], qR[NW];
+    D qL[NW], qR[NW];
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) {
-      qL[iw] = Q(wL[iw]);
-      qR[iw] = Q(wR[iw]);
+      qL[iw] = D(wL[iw]);
+      qR[iw] = D(wR[iw]);
     }
-    const Q dxs = a.a.dx[d][ci] + a.a.dx[d][ci + 1];
+    const D dxs = a.a.dx[d][ci] + a.a.dx[d][ci + 1];
     decompose(a, qL, qR, d, qsmallp, qdt, dxs, f, am);
   }
 
   // dvolume(ix) = dx_1*dx_2*dx_3 (gridsetup1, src/vacgrid.t:573-576)
   static __device__ __forceinline__ Q dvol(const SweepArgs& a, const int* c) {
-    Q v = a.a.dx[0][c[0]];
+    double v = a.a.dx[0][c[0]];
     if (NDIM > 1) v = v * a.a.dx[1][c[1]];
     if (NDIM > 2) v = v * a.a.dx[2][c[2]];
-    return v;
+    return Q(v);
   }
 
   // wave il's dissipative fluxes of every variable into acc
@@ -508,8 +555,8 @@ struct RoeSweep {
   static __device__ __forceinline__ void dissipate_var(
       const SweepArgs& a, const Face& fm, const Face& fp, int d, Q vm, Q vp,
       Q dv0, int nofm, int nofp, R* acc) {
-    Q rp = rtimes<iw, il>(a, fp, fp.phi[il], d) * Q(0.25) * vp;
-    Q rm = rtimes<iw, il>(a, fm, fm.phi[il], d) * Q(0.25) * vm;
+    Q rp = rtimes<iw, il>(a, fp, Q(fp.phi[il]), d) * Q(0.25) * vp;
+    Q rm = rtimes<iw, il>(a, fm, Q(fm.phi[il]), d) * Q(0.25) * vm;
     if ((nofp >> iw) & 1) rp = Q(0);
     if ((nofm >> iw) & 1) rm = Q(0);
     acc[iw] = acc[iw] + R((rp - rm) / dv0);
@@ -560,16 +607,16 @@ struct RoeSweep {
         S::to_prim(a, smallp, acc);
         S::to_cons(a, acc);
       }
-      const Q qsmallp = ctrl->smallp;
+      const double qsmallp = ctrl->smallp;
       const Q dv0 = dvol(a, c);
       for (int d = a.d0; d <= a.d1; d++) {
         Face fm, fp;
         R Fm[NW], Fp[NW];
-        Q amm[2], amp[2];
+        D amm[2], amp[2];
         face(a, w1, base, off - st[d], st[d], d, c[d] - 1, smallp, qsmallp,
              qdt, limit, Fm, fm, amm);
-        face(a, w1, base, off, st[d], d, c[d], smallp, qsmallp, qdt, limit, Fp,
-             fp, amp);
+        face(a, w1, base, off, st[d], d, c[d], smallp, qsmallp, qdt, limit,
+             Fp, fp, amp);
         if (a.ph.courantpar > 0.0) {
 #pragma unroll
           for (int k = 0; k < 2; k++) {
