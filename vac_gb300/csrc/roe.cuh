@@ -243,6 +243,120 @@ struct RoeSweep {
       f.phi[il] = Q(0.5) * (smalla + adt * adt / smalla) * jump;
   }
 
+  // The mixed instance's MHD average: FP32 with cancellation-free forms of
+  // the reference's speeds and weights (its af^2=(cs2-cs^2)/(cf^2-cs^2)
+  // and the slow speed cancel at low beta), the conservative dp in double.
+  // With a2=gamma p/rho, ca2=B_idim^2/rho, bt2=B_perp^2/rho, b2=ca2+bt2:
+  // cf^2-cs^2 = sqrt((a2-b2)^2+4 a2 bt2), cs^2 = a2 ca2/cf^2, and
+  // a2-cs^2, cf^2-a2 are formed as a sum of positive terms or from the
+  // identity (x+y)(x-y) = 4 a2 bt2; af^2 = 0 where the speeds coincide,
+  // as the reference's clipping of 0/0 gives.
+  static __device__ __forceinline__ void average_mhd_f32(const SweepArgs& a,
+                                                         const D* wLd,
+                                                         const D* wRd, int d,
+                                                         double smallp,
+                                                         Face& f, D* bd) {
+    float wL[NW], wR[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      wL[iw] = float(wLd[iw]);
+      wR[iw] = float(wRd[iw]);
+    }
+    const float rL = wL[0], rR = wR[0];
+    const float irL = 1.0f / rL, irR = 1.0f / rR;
+    const float rho = 0.5f * (rL + rR);
+    float v[NDIR], B[NDIR];
+#pragma unroll
+    for (int c = 0; c < NDIR; c++) {
+      v[c] = 0.5f * (wL[1 + c] * irL + wR[1 + c] * irR);
+      B[c] = 0.5f * (wL[B0 + 1 + c] + wR[B0 + 1 + c]);
+      f.v[c] = v[c];
+    }
+    double pL = PH::template pthermal_raw<NDIR, MHD>(wL, a.ph);
+    double pR = PH::template pthermal_raw<NDIR, MHD>(wR, a.ph);
+    pL = pL >= smallp ? pL : smallp;
+    pR = pR >= smallp ? pR : smallp;
+    if (a.ph.roe_dpprim) {
+      f.dp = pR - pL;
+    } else {
+      double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+#pragma unroll
+      for (int c = 0; c < NDIR; c++) {
+        const double vc = v[c];
+        s1 = s1 + vc * ((double)wR[1 + c] - (double)wL[1 + c]);
+        s2 = s2 + vc * vc;
+        const double bR = wR[B0 + 1 + c], bL = wL[B0 + 1 + c];
+        s3 = s3 + (bR - bL) * (bR + bL);
+      }
+      f.dp = a.ph.gm1 * ((double)wR[E] - (double)wL[E] - s1 +
+                         0.5 * s2 * ((double)rR - (double)rL) - 0.5 * s3);
+    }
+    f.rhodv = (wR[1 + d] - wL[1 + d]) - v[d] * (rR - rL);
+    const float irho = 1.0f / rho;
+    const float p = float(0.5 * (pL + pR));
+    const float a2 = a.ph.gammaf * p * irho;
+    const float ca2 = B[d] * B[d] * irho;
+    float bt2 = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NDIR; c++)
+      if (c != d) bt2 = fmaf(B[c], B[c], bt2);
+    bt2 = bt2 * irho;
+    const float b2 = ca2 + bt2;
+    const float dd = a2 - b2;
+    const float x4 = 4.0f * a2 * bt2;
+    const float Dr = sqrtf(fmaf(dd, dd, x4));
+    const float cf2 = 0.5f * (a2 + b2 + Dr);
+    const float cs2s = cf2 > 0.0f ? a2 * ca2 / cf2 : 0.0f;
+    const float na = dd >= 0.0f ? 0.5f * (dd + Dr) : x4 / (2.0f * (Dr - dd));
+    const float ns = dd <= 0.0f ? 0.5f * (Dr - dd) : x4 / (2.0f * (Dr + dd));
+    float af2 = Dr > 0.0f ? na / Dr : 0.0f;
+    float as2 = Dr > 0.0f ? ns / Dr : 1.0f;
+    af2 = fminf(1.0f, fmaxf(af2, 0.0f));
+    as2 = fminf(1.0f, fmaxf(as2, 0.0f));
+    f.cs2 = a2;
+    f.cf = sqrtf(cf2);
+    f.cs = sqrtf(cs2s);
+    f.af = sqrtf(af2);
+    f.as = sqrtf(as2);
+    const float sr = sqrtf(rho);
+    f.sr = sr;
+    const int I = dir_i(d), J = dir_j(d);
+    float bI = B[I], bJ = NDIR == 3 ? B[J] : 0.0f;
+    if (NDIR == 2) {
+      bI = bI >= 0.0f ? 1.0f : -1.0f;
+    } else {
+      const float t = sqrtf(bI * bI + bJ * bJ);
+      if (t > 1.0e-30f) {
+        bI = bI / t;
+        bJ = bJ / t;
+      } else {
+        bI = 0.70710678f;
+        bJ = 0.70710678f;
+      }
+    }
+    float bi = B[d];
+    if (fabsf(bi) < 1.0e-30f) bi = 1.0e-30f;
+#pragma unroll
+    for (int c = 0; c < NDIR; c++) f.b[c] = B[c];
+    f.b[d] = bi;
+    f.b[I] = bI;
+    if (NDIR == 3) f.b[J] = bJ;
+    // bdv, bdb of the fast/slow and the Alfven waves
+    const float dvI = wR[1 + I] * irR - wL[1 + I] * irL;
+    const float dbI = wR[B0 + 1 + I] - wL[B0 + 1 + I];
+    float bdv = bI * dvI, bdb = bI * dbI;
+    if (NDIR == 3) {
+      const float dvJ = wR[1 + J] * irR - wL[1 + J] * irL;
+      const float dbJ = wR[B0 + 1 + J] - wL[B0 + 1 + J];
+      bdv = fmaf(bJ, dvJ, bdv);
+      bdb = fmaf(bJ, dbJ, bdb);
+      bd[2] = (bJ * dvI - bI * dvJ) * 0.5f * rho;
+      bd[3] = (bJ * dbI - bI * dbJ) * 0.5f * copysignf(sr, bi);
+    }
+    bd[0] = bdv * copysignf(rho, bi);
+    bd[1] = bdb * sqrtf(a2) * sr;
+  }
+
   // average (src/vacphys.mhdroe.t:4-127, src/vacphys.hdroe.t:4-45) and the
   // waves of tvdlimit2's il loop.
   static __device__ __forceinline__ void decompose(const SweepArgs& a,
@@ -256,7 +370,9 @@ struct RoeSweep {
     const D rL = wL[0], rR = wR[0];
     const double dL = rL, dR = rR;
     D bd[4] = {D(0), D(0), D(0), D(0)};
-    if (MHD) {
+    if constexpr (MHD && sizeof(R) == 4) {
+      average_mhd_f32(a, wL, wR, d, smallp, f, bd);
+    } else if (MHD) {
       const double rho = 0.5 * (dL + dR);
       double B[NDIR];
 #pragma unroll
@@ -577,6 +693,60 @@ struct RoeSweep {
     if (NW > 7) dissipate_var<il, (NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
   }
 
+  // The corrector of one direction d (a compile-time constant, so that the
+  // face states and Roe quantities stay in registers): both faces, the
+  // central fluxes, then wave by wave the dissipative fluxes.
+  template <int d>
+  static __device__ __forceinline__ void direction(
+      const SweepArgs& a, const T* __restrict__ w1, const T* __restrict__ base,
+      long long off, const long long* st, const int* c, R smallp,
+      double qsmallp, double qdt, bool limit, Q dv0, R* acc,
+      unsigned long long* key) {
+    Face fm, fp;
+    R Fm[NW], Fp[NW];
+    D amm[2], amp[2];
+    face(a, w1, base, off - st[d], st[d], d, c[d] - 1, smallp, qsmallp,
+         qdt, limit, Fm, fm, amm);
+    face(a, w1, base, off, st[d], d, c[d], smallp, qsmallp, qdt, limit,
+         Fp, fp, amp);
+    if (a.ph.courantpar > 0.0) {
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const unsigned long long km = dkey((double)amm[k]);
+        const unsigned long long kp = dkey((double)amp[k]);
+        key[k] = km > kp ? km : kp;
+      }
+    }
+    // 'symm0' faces: no flux of those variables through the mesh edge
+    // (setnoflux in addflux, also for the dissipative flux)
+    const int nofp = c[d] == a.g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
+    const int nofm = c[d] == 2 ? a.ph.noflux[d][0] : 0;
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      if ((nofp >> iw) & 1) Fp[iw] = R(0);
+      if ((nofm >> iw) & 1) Fm[iw] = R(0);
+    }
+    const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++)
+      acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
+    int cn[3] = {c[0], c[1], c[2]};
+    cn[d] = c[d] - 1;
+    const Q dvm = dvol(a, cn);
+    cn[d] = c[d] + 1;
+    const Q dvp = dvol(a, cn);
+    const Q vm = dv0 + dvm;  // dvolume(j)+dvolume(i) of the lower face
+    const Q vp = dvp + dv0;  // and of the upper face
+    dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+  }
+
   // The corrector of one sweep (dimensions d0..d1) plus the CFL maxima of
   // the fast waves (last substep).
   template <int NT>
@@ -610,49 +780,15 @@ struct RoeSweep {
       const double qsmallp = ctrl->smallp;
       const Q dv0 = dvol(a, c);
       for (int d = a.d0; d <= a.d1; d++) {
-        Face fm, fp;
-        R Fm[NW], Fp[NW];
-        D amm[2], amp[2];
-        face(a, w1, base, off - st[d], st[d], d, c[d] - 1, smallp, qsmallp,
-             qdt, limit, Fm, fm, amm);
-        face(a, w1, base, off, st[d], d, c[d], smallp, qsmallp, qdt, limit,
-             Fp, fp, amp);
-        if (a.ph.courantpar > 0.0) {
-#pragma unroll
-          for (int k = 0; k < 2; k++) {
-            const unsigned long long km = dkey((double)amm[k]);
-            const unsigned long long kp = dkey((double)amp[k]);
-            key[d][k] = km > kp ? km : kp;
-          }
-        }
-        // 'symm0' faces: no flux of those variables through the mesh edge
-        // (setnoflux in addflux, also for the dissipative flux)
-        const int nofp = c[d] == a.g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
-        const int nofm = c[d] == 2 ? a.ph.noflux[d][0] : 0;
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++) {
-          if ((nofp >> iw) & 1) Fp[iw] = R(0);
-          if ((nofm >> iw) & 1) Fm[iw] = R(0);
-        }
-        const R cq = PH::qdx(qdt, a.a, d, c[d]);
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++)
-          acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
-        int cn[3] = {c[0], c[1], c[2]};
-        cn[d] = c[d] - 1;
-        const Q dvm = dvol(a, cn);
-        cn[d] = c[d] + 1;
-        const Q dvp = dvol(a, cn);
-        const Q vm = dv0 + dvm;  // dvolume(j)+dvolume(i) of the lower face
-        const Q vp = dvp + dv0;  // and of the upper face
-        dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-        if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+        if (d == 0)
+          direction<0>(a, w1, base, off, st, c, smallp, qsmallp, qdt, limit,
+                       dv0, acc, key[0]);
+        else if (NDIM > 1 && d == 1)
+          direction<(NDIM > 1 ? 1 : 0)>(a, w1, base, off, st, c, smallp,
+                                        qsmallp, qdt, limit, dv0, acc, key[1]);
+        else if (NDIM > 2)
+          direction<(NDIM > 2 ? 2 : 0)>(a, w1, base, off, st, c, smallp,
+                                        qsmallp, qdt, limit, dv0, acc, key[2]);
       }
       if (a.ph.sourceunsplit) {
         R wc[NW];
@@ -665,7 +801,9 @@ struct RoeSweep {
       for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
     }
     if (a.ph.courantpar > 0.0) {
-      for (int d = a.d0; d <= a.d1; d++) {
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        if (d < a.d0 || d > a.d1) continue;
 #pragma unroll
         for (int k = 0; k < 2; k++) {
           unsigned long long kk = block_max_key<NT>(key[d][k], shk);
