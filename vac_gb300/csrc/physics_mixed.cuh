@@ -203,6 +203,15 @@ struct PHMixed {
     return sqrtf(cs2) + fabsf(u[1 + d] * rinv);
   }
 
+  // thermal pressure (unclipped) with the path's recovery, as FP32
+  template <int NDIR, bool MHD>
+  static __device__ __forceinline__ float pthermal_f(const float* u,
+                                                     const DevPhys& k) {
+    float hbb;
+    return pressure_mixed<NDIR, MHD ? NDIR : 0, PM>(u, 1.0f / u[0], k.gm1f,
+                                                    &hbb);
+  }
+
   template <int NDIR, bool MHD>
   static __device__ __forceinline__ double pthermal_raw(const float* u,
                                                         const DevPhys& k) {

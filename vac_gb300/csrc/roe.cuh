@@ -43,15 +43,15 @@ struct RoeSweep {
   // quantities of src/vacphys.mhdroe.t:18-19,150-153 and
   // src/vacphys.hdroe.t:63-65) and the limiter function of every wave.
   struct Face {
-    D v[NDIR];   // MHD: mean velocity; HD: Roe-averaged velocity
-    D b[NDIR];   // MHD: B_idim (|B_idim| >= smalldouble), beta_idir, beta_jdir
-    D sr;        // MHD: sqrt(mean rho); HD: sqrt(rhoL)*sqrt(rhoR)
-    D cf, cs, af, as, cs2;  // MHD: fast/slow speeds, weights, sound^2
+    R v[NDIR];   // MHD: mean velocity; HD: Roe-averaged velocity
+    R b[NDIR];   // MHD: B_idim (|B_idim| >= smalldouble), beta_idir, beta_jdir
+    R sr;        // MHD: sqrt(mean rho); HD: sqrt(rhoL)*sqrt(rhoR)
+    R cf, cs, af, as, cs2;  // MHD: fast/slow speeds, weights, sound^2
                             // HD: cs = sound speed c
-    D h;         // HD: Roe-averaged enthalpy
-    D dp, rhodv; // MHD: pR-pL (conservative form), rho*dv_idim
+    R h;         // HD: Roe-averaged enthalpy
+    R dp, rhodv; // MHD: pR-pL (conservative form), rho*dv_idim
                  // HD: (pR-pL)/c^2, (vR-vL)_idim/c
-    D phi[NW];   // getphi's TVD-MUSCL phi = |a*dt/dx|*jump (entropy fixed)
+    R phi[NW];   // getphi's TVD-MUSCL phi = |a*dt/dx|*jump (entropy fixed)
   };
 
   // Fortran SIGN(a,b), MAX and MIN as the oracle's selects
@@ -77,8 +77,8 @@ struct RoeSweep {
 
   // getpthermal(.true.): p clipped at smallp, in double
   static __device__ __forceinline__ double pthd(const SweepArgs& a,
-                                                const D* u, double smallp) {
-    const double p = pthermal_raw<NDIR, MHD>(u, a.ph);
+                                                const R* u, double smallp) {
+    const double p = PH::template pthermal_raw<NDIR, MHD>(u, a.ph);
     return p >= smallp ? p : smallp;
   }
   // Eigenvalue a and jump L*dw of wave il with its entropy fix
@@ -87,9 +87,9 @@ struct RoeSweep {
   // phi of getphi's TVD-MUSCL branch (src/vactvd.t:227-243).  dxs =
   // dx(i)+dx(j); am receives |a*dt*2/dxs| of the two fast waves.
   template <int il>
-  static __device__ __forceinline__ void wave(const SweepArgs& a, const D* wL,
-                                              const D* wR, int d, double smallp,
-                                              D qdt, D dxs, const D* bd,
+  static __device__ __forceinline__ void wave(const SweepArgs& a, const R* wL,
+                                              const R* wR, int d, double smallp,
+                                              D qdt, D dxs, const R* bd,
                                               Face& f, D* am) {
     // the jumps and eigenvalues in Q from the double Roe state
     const Q rL = Q(wL[0]), rR = Q(wR[0]);
@@ -245,23 +245,18 @@ struct RoeSweep {
 
   // The mixed instance's MHD average: FP32 with cancellation-free forms of
   // the reference's speeds and weights (its af^2=(cs2-cs^2)/(cf^2-cs^2)
-  // and the slow speed cancel at low beta), the conservative dp in double.
+  // and the slow speed cancel at low beta), the pressures from the
+  // double-float recovery.
   // With a2=gamma p/rho, ca2=B_idim^2/rho, bt2=B_perp^2/rho, b2=ca2+bt2:
   // cf^2-cs^2 = sqrt((a2-b2)^2+4 a2 bt2), cs^2 = a2 ca2/cf^2, and
   // a2-cs^2, cf^2-a2 are formed as a sum of positive terms or from the
   // identity (x+y)(x-y) = 4 a2 bt2; af^2 = 0 where the speeds coincide,
   // as the reference's clipping of 0/0 gives.
   static __device__ __forceinline__ void average_mhd_f32(const SweepArgs& a,
-                                                         const D* wLd,
-                                                         const D* wRd, int d,
+                                                         const R* wL,
+                                                         const R* wR, int d,
                                                          double smallp,
-                                                         Face& f, D* bd) {
-    float wL[NW], wR[NW];
-#pragma unroll
-    for (int iw = 0; iw < NW; iw++) {
-      wL[iw] = float(wLd[iw]);
-      wR[iw] = float(wRd[iw]);
-    }
+                                                         Face& f, R* bd) {
     const float rL = wL[0], rR = wR[0];
     const float irL = 1.0f / rL, irR = 1.0f / rR;
     const float rho = 0.5f * (rL + rR);
@@ -272,28 +267,30 @@ struct RoeSweep {
       B[c] = 0.5f * (wL[B0 + 1 + c] + wR[B0 + 1 + c]);
       f.v[c] = v[c];
     }
-    double pL = PH::template pthermal_raw<NDIR, MHD>(wL, a.ph);
-    double pR = PH::template pthermal_raw<NDIR, MHD>(wR, a.ph);
-    pL = pL >= smallp ? pL : smallp;
-    pR = pR >= smallp ? pR : smallp;
+    const float sp = float(smallp);
+    float pL = PH::template pthermal_f<NDIR, MHD>(wL, a.ph);
+    float pR = PH::template pthermal_f<NDIR, MHD>(wR, a.ph);
+    pL = pL >= sp ? pL : sp;
+    pR = pR >= sp ? pR : sp;
     if (a.ph.roe_dpprim) {
       f.dp = pR - pL;
     } else {
-      double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      // (g-1)*(de - v.dm + v^2/2 drho - d(B^2)/2) with d(B^2) as a sum of
+      // (bR-bL)(bR+bL): the differences of nearby FP32 values are exact
+      float s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
 #pragma unroll
       for (int c = 0; c < NDIR; c++) {
-        const double vc = v[c];
-        s1 = s1 + vc * ((double)wR[1 + c] - (double)wL[1 + c]);
-        s2 = s2 + vc * vc;
-        const double bR = wR[B0 + 1 + c], bL = wL[B0 + 1 + c];
-        s3 = s3 + (bR - bL) * (bR + bL);
+        s1 = fmaf(v[c], wR[1 + c] - wL[1 + c], s1);
+        s2 = fmaf(v[c], v[c], s2);
+        const float bR = wR[B0 + 1 + c], bL = wL[B0 + 1 + c];
+        s3 = fmaf(bR - bL, bR + bL, s3);
       }
-      f.dp = a.ph.gm1 * ((double)wR[E] - (double)wL[E] - s1 +
-                         0.5 * s2 * ((double)rR - (double)rL) - 0.5 * s3);
+      f.dp = a.ph.gm1f * ((wR[E] - wL[E]) - s1 + 0.5f * s2 * (rR - rL) -
+                          0.5f * s3);
     }
     f.rhodv = (wR[1 + d] - wL[1 + d]) - v[d] * (rR - rL);
     const float irho = 1.0f / rho;
-    const float p = float(0.5 * (pL + pR));
+    const float p = 0.5f * (pL + pR);
     const float a2 = a.ph.gammaf * p * irho;
     const float ca2 = B[d] * B[d] * irho;
     float bt2 = 0.0f;
@@ -360,7 +357,7 @@ struct RoeSweep {
   // average (src/vacphys.mhdroe.t:4-127, src/vacphys.hdroe.t:4-45) and the
   // waves of tvdlimit2's il loop.
   static __device__ __forceinline__ void decompose(const SweepArgs& a,
-                                                   const D* wL, const D* wR,
+                                                   const R* wL, const R* wR,
                                                    int d, double smallp, D qdt,
                                                    D dxs, Face& f, D* am) {
     // The averages are formed in double (on the mixed path too): the slow
@@ -369,7 +366,7 @@ struct RoeSweep {
     // the waves and eigenvectors then run in D.
     const D rL = wL[0], rR = wR[0];
     const double dL = rL, dR = rR;
-    D bd[4] = {D(0), D(0), D(0), D(0)};
+    R bd[4] = {R(0), R(0), R(0), R(0)};
     if constexpr (MHD && sizeof(R) == 4) {
       average_mhd_f32(a, wL, wR, d, smallp, f, bd);
     } else if (MHD) {
@@ -648,14 +645,8 @@ struct RoeSweep {
     PH::template flux<NDIR, MHD>(wR, d, a.ph, smallp, fR);
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) F[iw] = R(0.5) * (fL[iw] + fR[iw]);
-    D qL[NW], qR[NW];
-#pragma unroll
-    for (int iw = 0; iw < NW; iw++) {
-      qL[iw] = D(wL[iw]);
-      qR[iw] = D(wR[iw]);
-    }
     const D dxs = a.a.dx[d][ci] + a.a.dx[d][ci + 1];
-    decompose(a, qL, qR, d, qsmallp, qdt, dxs, f, am);
+    decompose(a, wL, wR, d, qsmallp, qdt, dxs, f, am);
   }
 
   // dvolume(ix) = dx_1*dx_2*dx_3 (gridsetup1, src/vacgrid.t:573-576)
