@@ -62,7 +62,8 @@ enum {
   VACGPU_BC_FIXED1 = 5,
   VACGPU_BC_CONT1 = 6,
   VACGPU_BC_GRAD1 = 7,
-  VACGPU_BC_SYMM0 = 8
+  VACGPU_BC_SYMM0 = 8,
+  VACGPU_BC_SPECIAL = 9  /* user routine specialbound: vacgpu_register_bound */
 };
 
 /* typefull1 (src/vactvdlf.t:92-299): second order 'tvdlf' or 'tvdlf1'
@@ -205,6 +206,45 @@ int vacgpu_sums(vacgpu_handle* h, double* wmean);
 /* Error counters nerror(1:4) (src/vacdef.t:54-55): toosmallp, toosmallr,
  * couranterr, poissonerr. */
 int vacgpu_error_counts(vacgpu_handle* h, int* nerror);
+
+/* specialbound (src/vacgrid.t:355-371; user routine
+ * src/vacnul.specialbound.t:2-13): the ghost values of the variables whose
+ * typeB is 'special'.  One region iB (0-based, 2*(idim-1)+upper) as the
+ * hook sees it: its cells, the layout of the device state and the device
+ * pointers the hook may read.  Element (gx,gy,gz) of variable iw is at
+ * w[offset0 + gx*stride[0] + gy*stride[1] + gz*stride[2] + iw*var_stride]
+ * (ghost-box coordinates, mesh cells 2..nx+1 in a used dimension). */
+typedef struct vacgpu_region {
+  int iB;                  /* region, 2*(idim-1)+upper                     */
+  unsigned iw_mask;        /* bit iw set: variable iw is 'special' here    */
+  int lo[3], hi[3];        /* the region's cells (inclusive)               */
+  int nx[3];               /* mesh cells per dimension (1 if unused)       */
+  int nG[3];               /* ghost-box extents                            */
+  long long offset0;       /* element offset of ghost cell (0,0,0)         */
+  long long stride[3];     /* element strides of the three dimensions      */
+  long long var_stride;    /* element stride between variables             */
+  int elem;                /* 8: double state (FP64), 4: float (mixed)     */
+  const double* qt;        /* device: getboundary's time qt of this fill   */
+                           /* (t; t+dt/2 after the predictor, t+dt after   */
+                           /* the corrector, src/vac.t:567)                */
+  const double* x[3];      /* device: cell centres along each dimension,   */
+                           /* nG[d] values over the ghost box              */
+} vacgpu_region;
+
+/* The hook is called on the host while the engine issues a ghost fill --
+ * also while it captures a CUDA graph -- once per region that has
+ * 'special' variables, after the region's other variables are filled and
+ * before the next region (getboundary's order).  It enqueues device work
+ * on `stream` (a cudaStream_t) that writes the region's cells of the
+ * variables in iw_mask, must not synchronise, and returns 0 (non-zero
+ * fails the call that issued the fill). */
+typedef int (*vacgpu_bound_fn)(void* user, void* w, const vacgpu_region* r,
+                               void* stream);
+
+/* Install the specialbound hook of the handle (NULL removes it).  A grid
+ * with 'special' faces refuses to run without one ("Special boundary is
+ * not defined", src/vacnul.specialbound.t:12). */
+int vacgpu_register_bound(vacgpu_handle* h, vacgpu_bound_fn fn, void* user);
 
 /* Install a device source hook (specialsource + getdt_special,
  * src/vacnul.specialsource.t:9-71); VACGPU_SRC_NONE removes it. */

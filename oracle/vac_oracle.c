@@ -69,6 +69,11 @@ typedef struct vo_state {
   int istep, nstep;
   int src_id;
   double src_par[VACGPU_MAXSRCPAR];
+  /* specialbound hook: fills variable iw of region iB (box lo..hi) */
+  void (*bound_fn)(void* user, double* w, const int* lo, const int* hi,
+                   const long* st, long N, const double* x, int iw, int iB,
+                   double qt);
+  void* bound_user;
 } vo_state;
 
 /* ------------------------------------------------------------------ boxes */
@@ -769,8 +774,10 @@ static box region(vo_state* s, int iB) {
 /* getboundary, src/vacgrid.t:195-413 with the default regions of boundsetup
  * (src/vacgrid.t:53-69) and periodic pairing (:121-135); keeppositive first
  * when smallfix (:213).  Regions are filled in iB order, each over the full
- * extent of the other dimensions. */
-static void getboundary(vo_state* s, double* w) {
+ * extent of the other dimensions; a region's 'special' variables go to the
+ * specialbound hook after its other variables (:355-371), with the fill's
+ * time qt. */
+static void getboundary(vo_state* s, double* w, double qt) {
   if (s->p.smallfix) keeppositive(s, w);
   for (int iB = 0; iB < 2 * s->ndim; iB++) {
     const int idim = iB / 2, upper = iB % 2;
@@ -784,7 +791,9 @@ static void getboundary(vo_state* s, double* w) {
       int type = s->p.typeB[iB][iw];
       const int fixedtype = type == VACGPU_BC_FIXED || type == VACGPU_BC_FIXED1 ||
                             type == VACGPU_BC_GRAD1;
-      if (fixedtype && s->initialized) {
+      if (type == VACGPU_BC_SPECIAL) {
+        continue;
+      } else if (fixedtype && s->initialized) {
         /* restore the stored values, grad1 on top of the current edge */
         const double* fb = W(s->fixB[iB], iw);
         for (int k = r.lo[idim]; k <= r.hi[idim]; k++) {
@@ -828,6 +837,10 @@ static void getboundary(vo_state* s, double* w) {
         if (type == VACGPU_BC_ASYMM) FORBOX(r, ix) a[ix] = -a[ix];
       }
     }
+    for (int iw = 0; iw < s->nw; iw++)
+      if (s->p.typeB[iB][iw] == VACGPU_BC_SPECIAL && s->bound_fn)
+        s->bound_fn(s->bound_user, w, r.lo, r.hi, s->st, s->N,
+                    W(s->x, idim), iw, iB, qt);
   }
   if (!s->initialized) {
     /* fixed boundaries store their values, grad1 its differences */
@@ -1647,7 +1660,7 @@ static void advect1(vo_state* s, int pred, double qdt, int idimmin,
     hancock(s, qdt, s->ixM, idimmin, idimmax, wCT, w);
   else
     tvdmusclf(s, qdt, s->ixM, idimmin, idimmax, wCT, w);
-  getboundary(s, w);
+  getboundary(s, w, s->t + qdt);  /* qt+qdt, src/vac.t:567 */
 }
 
 /* advect, src/vac.t:363-486.  'tvdlf' and 'tvdmu' have the default
@@ -1960,7 +1973,7 @@ void vo_set_state(vo_state* s, const double* wmesh, int it, double t) {
   s->itmin = it;
   s->t = t;
   s->initialized = 0;  /* a new run: fixed boundaries store again */
-  getboundary(s, s->w);
+  getboundary(s, s->w, s->t);
 }
 
 void vo_get_state(vo_state* s, double* wmesh) {
@@ -1971,6 +1984,15 @@ void vo_get_state(vo_state* s, double* wmesh) {
 /* full ixG state (test access to ghosts) */
 void vo_get_state_full(vo_state* s, double* wfull) {
   memcpy(wfull, s->w, sizeof(double) * s->N * s->nw);
+}
+
+void vo_register_bound(vo_state* s,
+                       void (*fn)(void*, double*, const int*, const int*,
+                                  const long*, long, const double*, int, int,
+                                  double),
+                       void* user) {
+  s->bound_fn = fn;
+  s->bound_user = user;
 }
 
 void vo_register_source(vo_state* s, int id, const double* par, int npar) {

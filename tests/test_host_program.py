@@ -147,3 +147,32 @@ def test_run_tvdmu_writes_vac_outputs(vacgb, tmp_path):
         o.step(it - o.it)
         assert got.it == it and got.t == o.t
         assert np.array_equal(got.w.view(np.uint64), o.state().view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_run_special_bound_hook(vacgb, tmp_path):
+    """typeB='special' through the host program: the specialbound hook
+    comes from VACGB_SPECIALBOUND=lib.so:symbol; results equal the oracle
+    with the host twin of the hook."""
+    from tests.test_special_bound import _device_hook, _host_hook
+    s = _setup(tmp_path)
+    par = PAR.replace("typeB=6*'periodic',6*'periodic',", "typeB=6*'special',6*'cont',")
+    Ld, _ = _device_hook()
+    env = dict(os.environ, VACGB_SPECIALBOUND=Ld._name + ":inflow_bound")
+    r = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True, input=par,
+                       env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    Lh, hfn = _host_hook()
+    p = inistate.params_for(s, limiter="woodward")
+    p.typelimiter[1] = abi.LIM_MINMOD
+    for iw in range(p.nw):
+        p.typeB[0][iw] = abi.BC_SPECIAL
+        p.typeB[1][iw] = abi.BC_CONT
+    o = Oracle(p, s.x, s.w, bound=(hfn, None))
+    got = vacfile.read(str(tmp_path / "ot.out"), snapshot=2)
+    o.step(20)
+    assert got.it == 20 and got.t == o.t
+    assert np.array_equal(got.w.view(np.uint64), o.state().view(np.uint64))
+    r2 = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True, input=par,
+                        env={k: v for k, v in os.environ.items() if k != "VACGB_SPECIALBOUND"})
+    assert r2.returncode != 0 and "Special boundary is not defined" in r2.stdout + r2.stderr

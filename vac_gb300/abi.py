@@ -13,7 +13,8 @@ MAXSRCPAR = 8
 
 PHYS_HD, PHYS_MHD = 0, 1
 LIM_MINMOD, LIM_WOODWARD, LIM_SUPERBEE, LIM_VANLEER, LIM_ALBADA = range(5)
-BC_CONT, BC_PERIODIC, BC_SYMM, BC_ASYMM, BC_FIXED, BC_FIXED1, BC_CONT1, BC_GRAD1, BC_SYMM0 = range(9)
+(BC_CONT, BC_PERIODIC, BC_SYMM, BC_ASYMM, BC_FIXED, BC_FIXED1, BC_CONT1, BC_GRAD1,
+ BC_SYMM0, BC_SPECIAL) = range(10)
 TVDLF, TVDLF1, TVDMU, TVDMU1 = 0, 1, 2, 3
 ENTROPY_NUL, ENTROPY_HARTEN, ENTROPY_POWELL, ENTROPY_RATIO, ENTROPY_YEE = range(5)
 LIMITED_ORIGINAL, LIMITED_PREVIOUS, LIMITED_PREDICTOR = range(3)
@@ -31,7 +32,8 @@ ENTROPY_NAMES = {"nul": ENTROPY_NUL, "harten": ENTROPY_HARTEN,
                  "yee": ENTROPY_YEE}
 BC_NAMES = {"cont": BC_CONT, "periodic": BC_PERIODIC, "symm": BC_SYMM,
             "asymm": BC_ASYMM, "fixed": BC_FIXED, "fixed1": BC_FIXED1,
-            "cont1": BC_CONT1, "grad1": BC_GRAD1, "symm0": BC_SYMM0}
+            "cont1": BC_CONT1, "grad1": BC_GRAD1, "symm0": BC_SYMM0,
+            "special": BC_SPECIAL}
 
 
 class VacParams(C.Structure):

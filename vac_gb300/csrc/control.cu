@@ -196,6 +196,11 @@ __device__ void step_end_dev(Ctrl* c, int ndim, int toggle) {
 }
 
 __global__ void k_dt_begin(Ctrl* c, int ndim) { dt_begin_dev(c, ndim); }
+// getboundary's qt: t (before the loop), qt+qdt = t+dt/2 after the
+// predictor and t+dt after the corrector (src/vac.t:54,567)
+__global__ void k_set_qt(Ctrl* c, int mode) {
+  c->qt = mode == 0 ? c->t : mode == 1 ? c->t + c->dt / 2 : c->t + c->dt;
+}
 __global__ void k_smallp(Ctrl* c, int mhd, double coeff) {
   smallp_dev(c, mhd, coeff);
 }
@@ -284,6 +289,10 @@ void launch_kp_smallrho(Ctrl* c, double coeff, cudaStream_t st) {
   k_kp_smallrho<<<1, NSLOT, 0, st>>>(c, coeff);
 }
 void launch_kp_end(Ctrl* c, cudaStream_t st) { k_kp_end<<<1, 1, 0, st>>>(c); }
+void launch_set_qt(Ctrl* c, int mode, cudaStream_t st) {
+  k_set_qt<<<1, 1, 0, st>>>(c, mode);
+}
+
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st) {
   DtEndArgs a;
   a.ndim = p.ndim;

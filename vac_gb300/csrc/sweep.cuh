@@ -793,6 +793,7 @@ __global__ void k_ghost_face(T* __restrict__ w, DevGrid g, DevPhys ph,
 #pragma unroll
   for (int iw = 0; iw < NW; iw++) {
     const int t = ph.typeB[iB][iw];
+    if (t == VACGPU_BC_SPECIAL) continue;  // the specialbound hook's
     const long long vo = (long long)iw * g.vs;
     const bool fixedtype = t == VACGPU_BC_FIXED || t == VACGPU_BC_FIXED1 ||
                            t == VACGPU_BC_GRAD1;
@@ -985,20 +986,23 @@ struct Launch {
   // getboundary face by face (grids with fixed/extrapolating faces)
   static void ghost_faces(const SweepArgs& a, T* w, T* fixb, int restore,
                           cudaStream_t st) {
+    for (int iB = 0; iB < 2 * a.g.ndim; iB++) ghost_face(a, w, fixb, restore, iB, st);
+  }
+  // region iB alone (its stored values follow those of the regions before)
+  static void ghost_face(const SweepArgs& a, T* w, T* fixb, int restore, int iB,
+                         cudaStream_t st) {
     const int nw = a.mhd ? 2 + 2 * a.ndir : 2 + a.ndir;
     long long off = 0;
-    for (int iB = 0; iB < 2 * a.g.ndim; iB++) {
-      const long long tot = fix_face_elems(a.g, iB, 1);
-      const unsigned nb = grid_for(tot, 128);
-      T* fb = fixb + off;
-      switch (nw) {
-        case 3: k_ghost_face<T, 3><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
-        case 4: k_ghost_face<T, 4><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
-        case 5: k_ghost_face<T, 5><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
-        case 6: k_ghost_face<T, 6><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
-        case 8: k_ghost_face<T, 8><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
-      }
-      off += fix_face_elems(a.g, iB, nw);
+    for (int j = 0; j < iB; j++) off += fix_face_elems(a.g, j, nw);
+    const long long tot = fix_face_elems(a.g, iB, 1);
+    const unsigned nb = grid_for(tot, 128);
+    T* fb = fixb + off;
+    switch (nw) {
+      case 3: k_ghost_face<T, 3><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+      case 4: k_ghost_face<T, 4><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+      case 5: k_ghost_face<T, 5><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+      case 6: k_ghost_face<T, 6><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
+      case 8: k_ghost_face<T, 8><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
     }
   }
   static void fix_store(const SweepArgs& a, const T* w, T* fixb, cudaStream_t st) {
@@ -1083,6 +1087,10 @@ struct Launch {
   void launch_ghost_faces_##SUF(const SweepArgs& s, PH::T* w, PH::T* fixb,    \
                                 int restore, cudaStream_t st) {              \
     Launch<PH>::ghost_faces(s, w, fixb, restore, st);                        \
+  }                                                                          \
+  void launch_ghost_face_##SUF(const SweepArgs& s, PH::T* w, PH::T* fixb,     \
+                               int restore, int iB, cudaStream_t st) {       \
+    Launch<PH>::ghost_face(s, w, fixb, restore, iB, st);                     \
   }                                                                          \
   void launch_fix_store_##SUF(const SweepArgs& s, const PH::T* w,            \
                               PH::T* fixb, cudaStream_t st) {                \

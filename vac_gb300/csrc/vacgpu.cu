@@ -142,6 +142,12 @@ struct vacgpu_handle {
   void* buf[3];      // two state buffers (ping-pong) + predictor output
   void* wold;        // step-start copy for typelimited='previous' when split
   void* fixb;        // stored ghost values of fixed/fixed1/grad1 faces
+  vacgpu_bound_fn bound_fn;  // specialbound hook
+  void* bound_user;
+  bool hook_failed;  // the hook returned non-zero while a fill was issued
+  bool any_special;
+  unsigned special[VACGPU_MAXB];  // per region: bit iw 'special'
+  double* xg[3];     // cell centres over the ghost box (specialbound hooks)
   int cur;           // which of buf[0], buf[1] holds the state
   double* dx[3];
   float* dxf[3];
@@ -273,7 +279,54 @@ bool make_tmap(vacgpu_handle* h, void* base, int rows, bool yz, CUtensorMap* m) 
 // getboundary's ghost fill of w: composed index maps, or face by face
 // (restore: reuse the stored values of fixed/fixed1/grad1 faces) when the
 // grid has fixed or extrapolating faces.
-void fill_ghosts(vacgpu_handle* h, const SweepArgs& a, void* w, int restore) {
+// getboundary's region loop with the specialbound hook: each region's
+// standard types, then the hook for its 'special' variables, region by
+// region (src/vacgrid.t:228-372).  qtmode: the fill's qt (launch_set_qt).
+int special_fill(vacgpu_handle* h, const SweepArgs& a, void* w, int restore,
+                 int qtmode) {
+  const DevGrid& g = h->g;
+  launch_set_qt(h->ctrl, qtmode, h->st);
+  for (int iB = 0; iB < 2 * g.ndim; iB++) {
+    if (h->elem == 8)
+      launch_ghost_face_fp64(a, (double*)w, (double*)h->fixb, restore, iB, h->st);
+    else
+      launch_ghost_face_mixed(a, (float*)w, (float*)h->fixb, restore, iB, h->st);
+    if (!h->special[iB]) continue;
+    vacgpu_region r;
+    memset(&r, 0, sizeof(r));
+    r.iB = iB;
+    r.iw_mask = h->special[iB];
+    const int idim = iB / 2, upper = iB % 2;
+    for (int d = 0; d < 3; d++) {
+      r.lo[d] = 0;
+      r.hi[d] = g.nG[d] - 1;
+      r.nx[d] = g.nx[d];
+      r.nG[d] = g.nG[d];
+      r.x[d] = h->xg[d];
+    }
+    r.lo[idim] = upper ? g.nx[idim] + 2 : 0;
+    r.hi[idim] = upper ? g.nx[idim] + 3 : 1;
+    r.offset0 = g.xpad;
+    r.stride[0] = 1;
+    r.stride[1] = g.P;
+    r.stride[2] = g.plane;
+    r.var_stride = g.vs;
+    r.elem = (int)h->elem;
+    r.qt = &h->ctrl->qt;
+    if (h->bound_fn(h->bound_user, w, &r, (void*)h->st)) {
+      h->hook_failed = true;
+      return fail("the specialbound hook failed for region " + std::to_string(iB + 1));
+    }
+  }
+  return 0;
+}
+
+void fill_ghosts(vacgpu_handle* h, const SweepArgs& a, void* w, int restore,
+                 int qtmode) {
+  if (h->bound_fn && h->ph.genbc) {
+    special_fill(h, a, w, restore, qtmode);
+    return;
+  }
   if (h->ph.genbc) {
     if (h->elem == 8)
       launch_ghost_faces_fp64(a, (double*)w, (double*)h->fixb, restore, h->st);
@@ -357,7 +410,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
       kend(h);
     }
     kbegin(h, VACGPU_K_GHOST);
-    fill_ghosts(h, a, wout, 1);
+    fill_ghosts(h, a, wout, 1, 2);
     kend(h);
   } else if (sizeof(T) == 8) {
     kbegin(h, VACGPU_K_PREDICT);
@@ -365,7 +418,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)w1, h->st);
-    fill_ghosts(h, a, w1, 1);
+    fill_ghosts(h, a, w1, 1, 1);
     kend(h);
     kbegin(h, VACGPU_K_CORRECT);
     if (roe)
@@ -377,7 +430,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kend(h);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)wout, h->st);
-    fill_ghosts(h, a, wout, 1);
+    fill_ghosts(h, a, wout, 1, 2);
     kend(h);
   } else if (h->fused && h->pmode == 0 && d0 == d1) {
     kbegin(h, VACGPU_K_SWEEP);
@@ -397,7 +450,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fw1, h->st); \
-  fill_ghosts(h, a, fw1, 1);                            \
+  fill_ghosts(h, a, fw1, 1, 1);                         \
   kend(h);                                              \
   kbegin(h, VACGPU_K_CORRECT);                          \
   if (roe)                                              \
@@ -407,7 +460,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   kend(h);                                              \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fo, h->st); \
-  fill_ghosts(h, a, fo, 1);                             \
+  fill_ghosts(h, a, fo, 1, 2);                          \
   kend(h);
     switch (h->pmode) {
       case 1: MIXED_SWEEP(mixedf64) break;
@@ -514,6 +567,16 @@ int tune_nzc(vacgpu_handle* h) {
   h->nzc = nbest;
   CK(cudaGetLastError());
   return 0;
+}
+
+// Captured graphs hold the launch arguments and hooks of their capture.
+void drop_graphs(vacgpu_handle* h) {
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      if (h->gexec[i][j]) {
+        cudaGraphExecDestroy(h->gexec[i][j]);
+        h->gexec[i][j] = nullptr;
+      }
 }
 
 int issue_steps(vacgpu_handle* h, int k, int it_base) {
@@ -625,7 +688,7 @@ int check_params(const vacgpu_params* p) {
   for (int d = 0; d < p->ndim; d++)
     for (int iw = 0; iw < nw; iw++) {
       int lo = p->typeB[2 * d][iw], hi = p->typeB[2 * d + 1][iw];
-      if (lo < 0 || lo > VACGPU_BC_SYMM0 || hi < 0 || hi > VACGPU_BC_SYMM0)
+      if (lo < 0 || lo > VACGPU_BC_SPECIAL || hi < 0 || hi > VACGPU_BC_SPECIAL)
         return fail("unsupported boundary type");
       if ((lo == VACGPU_BC_PERIODIC) != (hi == VACGPU_BC_PERIODIC))
         return fail("Error in BoundSetup: No periodic pair");
@@ -804,6 +867,10 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.compactres = p->compactres;
   ph.src_id = VACGPU_SRC_NONE;
   set_gmaps(ph, p->ndim, p->nw);
+  for (int iB = 0; iB < 2 * p->ndim; iB++)
+    for (int iw = 0; iw < p->nw; iw++)
+      if (p->typeB[iB][iw] == VACGPU_BC_SPECIAL) h->special[iB] |= 1u << iw;
+  for (int iB = 0; iB < VACGPU_MAXB; iB++) h->any_special |= h->special[iB] != 0;
   size_t bytes = h->elem * (size_t)g.vs * h->nw;
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 3 && e == cudaSuccess; i++) {
@@ -816,7 +883,9 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
                            ph.useprim))
     e = cudaMalloc(&h->wold, bytes);
   for (int d = 0; d < 3 && e == cudaSuccess; d++) {
-    e = cudaMalloc(&h->dx[d], sizeof(double) * g.nG[d]);
+    e = cudaMalloc(&h->xg[d], sizeof(double) * g.nG[d]);
+    if (e == cudaSuccess) e = cudaMemset(h->xg[d], 0, sizeof(double) * g.nG[d]);
+    if (e == cudaSuccess) e = cudaMalloc(&h->dx[d], sizeof(double) * g.nG[d]);
     if (e == cudaSuccess) e = cudaMalloc(&h->dxf[d], sizeof(float) * g.nG[d]);
   }
   if (e == cudaSuccess)
@@ -929,6 +998,9 @@ int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
       int c = std::abs(ixe - ix);
       q[ix] = (1 + c) * q[ixe] - c * q[ixf];
     }
+    // cell centres over the ghost box (q covers one more cell each side)
+    CK(cudaMemcpy(h->xg[d], q.data() + 1, sizeof(double) * (N + 4),
+                  cudaMemcpyHostToDevice));
     h->hdx[d].assign(N + 4, 0.0);
     std::vector<float> f(N + 4);
     for (int i = 0; i < N + 4; i++) {
@@ -980,8 +1052,14 @@ int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
   return 0;
 }
 
+static const char* NO_SPECIAL =
+    "Special boundary is not defined (typeB 'special' needs a hook: "
+    "vacgpu_register_bound)";
+
 int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   if (!h) return fail("null handle");
+  if (h->any_special && !h->bound_fn) return fail(NO_SPECIAL);
+  h->hook_failed = false;
   const DevGrid& g = h->g;
   long long n = g.ncell * h->nw;
   // it, t, itmin (startup, src/vac.t:176) and the dt state of a fresh run
@@ -1015,18 +1093,19 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   if (h->elem == 8) {
     k_scatter<double><<<nb, 256, 0, h->st>>>(h->stage, (double*)h->buf[0], g, h->nw);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)h->buf[0], h->st);
-    fill_ghosts(h, a, h->buf[0], 0);
+    fill_ghosts(h, a, h->buf[0], 0, 0);
     if (h->ph.genbc)
       launch_fix_store_fp64(a, (const double*)h->buf[0], (double*)h->fixb, h->st);
   } else {
     k_scatter<float><<<nb, 256, 0, h->st>>>(h->stage, (float*)h->buf[0], g, h->nw);
     if (h->p.smallfix) launch_keeppositive_mixed(a, (float*)h->buf[0], h->st);
-    fill_ghosts(h, a, h->buf[0], 0);
+    fill_ghosts(h, a, h->buf[0], 0, 0);
     if (h->ph.genbc)
       launch_fix_store_mixed(a, (const float*)h->buf[0], (float*)h->fixb, h->st);
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->st));
+  if (h->hook_failed) return fail("the specialbound hook failed");
   h->cur = 0;
   h->it_host = it;
   h->have_state = true;
@@ -1055,6 +1134,7 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   if (!h->have_grid || !h->have_state)
     return fail("vacgpu_step before vacgpu_set_grid/vacgpu_upload");
   if (maxsteps < 0) return fail("maxsteps must be >= 0");
+  if (h->any_special && !h->bound_fn) return fail(NO_SPECIAL);
   if (h->tuning && maxsteps > 0 && !h->timing && tune_nzc(h)) return 1;
   const int nsw = h->p.dimsplit ? h->p.ndim : 1;
   const int start_cur = h->cur;
@@ -1069,6 +1149,12 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
     if (issue_steps(h, k, h->it_host + issued)) return 1;
     issued += k;
     CK(cudaGetLastError());
+    if (h->hook_failed) {
+      h->hook_failed = false;
+      drop_graphs(h);
+      CK(cudaStreamSynchronize(h->st));
+      return fail("the specialbound hook failed");
+    }
     int done = 0;
     CK(cudaMemcpyAsync(&done, &h->ctrl->done, sizeof(int),
                        cudaMemcpyDeviceToHost, h->st));
@@ -1117,9 +1203,20 @@ int vacgpu_error_counts(vacgpu_handle* h, int* nerror) {
   return 0;
 }
 
+int vacgpu_register_bound(vacgpu_handle* h, vacgpu_bound_fn fn, void* user) {
+  if (!h) return fail("null handle");
+  if (h->st) CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);
+  h->bound_fn = fn;
+  h->bound_user = user;
+  return 0;
+}
+
 int vacgpu_register_source(vacgpu_handle* h, int source_id,
                            const double* params, int nparams) {
   if (!h) return fail("null handle");
+  if (h->st) CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);
   if (source_id != VACGPU_SRC_NONE && source_id != VACGPU_SRC_GRAVITY)
     return fail("unknown source id");
   if (nparams < 0 || nparams > VACGPU_MAXSRCPAR) return fail("bad nparams");
@@ -1159,6 +1256,7 @@ void vacgpu_destroy(vacgpu_handle* h) {
   cudaFree(h->wold);
   cudaFree(h->fixb);
   for (int d = 0; d < 3; d++) {
+    cudaFree(h->xg[d]);
     cudaFree(h->dx[d]);
     cudaFree(h->dxf[d]);
     cudaFree(h->idxf[d]);

@@ -66,8 +66,8 @@ struct DevPhys {
   int asym[3][2];
   // bit iw set: 'symm0' face, zero flux of iw through it (setnoflux)
   int noflux[3][2];
-  // some face is 'fixed', 'fixed1', 'cont1' or 'grad1': ghost cells are
-  // filled face by face in getboundary's order (k_ghost_face)
+  // some face is 'fixed', 'fixed1', 'cont1', 'grad1' or 'special': ghost
+  // cells are filled face by face in getboundary's order (k_ghost_face)
   int genbc;
   // Roe dissipation of 'tvdmu'/'tvdmu1' (src/vactvd.t:86-243)
   int typeentropy[VACGPU_MAXNW];
@@ -88,7 +88,8 @@ inline void set_gmaps(DevPhys& ph, int ndim, int nw) {
       for (int v = 0; v < nw && d < ndim; v++) {
         int t = ph.typeB[2 * d + s][v];
         const bool gen = t == VACGPU_BC_FIXED || t == VACGPU_BC_FIXED1 ||
-                         t == VACGPU_BC_CONT1 || t == VACGPU_BC_GRAD1;
+                         t == VACGPU_BC_CONT1 || t == VACGPU_BC_GRAD1 ||
+                         t == VACGPU_BC_SPECIAL;
         int mv = gen ? GMAP_MIXED
                  : t == VACGPU_BC_PERIODIC ? GMAP_PERIODIC
                  : t == VACGPU_BC_CONT     ? GMAP_CONT
@@ -123,6 +124,7 @@ struct Ctrl {
   double smallp;
   double dtgrav;
   double dtdiff;      // resistive diffusion dt limit (BIG without resistivity)
+  double qt;          // time of the current ghost fill (specialbound hooks)
   double tstop;
   double dtcourant[3];
   int it, itmin;
@@ -205,6 +207,8 @@ struct SweepArgs {
                               cudaStream_t st);                              \
   void launch_ghost_faces_##SUF(const SweepArgs& s, T* w, T* fixb,            \
                                 int restore, cudaStream_t st);               \
+  void launch_ghost_face_##SUF(const SweepArgs& s, T* w, T* fixb,             \
+                               int restore, int iB, cudaStream_t st);        \
   void launch_fix_store_##SUF(const SweepArgs& s, const T* w, T* fixb,        \
                               cudaStream_t st);
 VACGPU_DECLARE_LAUNCHERS(fp64, double)
@@ -241,6 +245,8 @@ void launch_kp_begin(Ctrl* c, int rho_floor, cudaStream_t st);
 void launch_kp_smallrho(Ctrl* c, double coeff, cudaStream_t st);
 void launch_kp_end(Ctrl* c, cudaStream_t st);
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st);
+// qt of a ghost fill: mode 0 t, 1 t+dt/2, 2 t+dt (src/vac.t:54,567)
+void launch_set_qt(Ctrl* c, int mode, cudaStream_t st);
 void launch_step_end(Ctrl* c, int ndim, cudaStream_t st);
 // Batched control: which = 0 dt_begin, 1 smallp, 2 dt_end, 3 step_end
 // (toggle = buffer swaps per step), 4 call_begin; one block per grid.

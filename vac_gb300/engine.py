@@ -55,6 +55,7 @@ def lib():
         L.vacgpu_sums.argtypes = [vp, dp]
         L.vacgpu_error_counts.argtypes = [vp, ip]
         L.vacgpu_register_source.argtypes = [vp, C.c_int, dp, C.c_int]
+        L.vacgpu_register_bound.argtypes = [vp, vp, vp]
         L.vacgpu_destroy.argtypes = [vp]
         L.vacgpu_destroy.restype = None
         L.vacgpu_last_error.argtypes = [C.c_char_p, C.c_int]
@@ -110,12 +111,18 @@ class Engine:
     coordinates, ``w``: (nw, n1, ...) conservative state, both indexed like
     VAC's x(ix^D,idim) and w(ix^D,iw)."""
 
-    def __init__(self, params, x, w, it=0, t=0.0):
+    def __init__(self, params, x, w, it=0, t=0.0, bound=None):
+        """bound: (function pointer, user pointer) of a vacgpu_bound_fn
+        specialbound hook, installed before the first ghost fill."""
         L = lib()
         self.p = params
         h = C.c_void_p()
         _ck(L.vacgpu_create(C.byref(params), C.byref(h)), "vacgpu_create")
         self.h = h
+        if bound:
+            _ck(L.vacgpu_register_bound(self.h, C.c_void_p(bound[0]),
+                                        C.c_void_p(bound[1])),
+                "vacgpu_register_bound")
         self.nw = params.nw
         self.nx = tuple(params.nx[d] for d in range(params.ndim))
         xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)

@@ -12,6 +12,10 @@
 // to the log filename(1) (savefilelog_default, src/vacio.t:1050-1105) at
 // every save event; between save events the engine advances without host
 // round trips.  Errors print the message and stop, as die() does.
+//
+// typeB='special' faces call the user's specialbound, which this program
+// loads as a device hook (vacgpu_bound_fn) from a shared library named by
+// VACGB_SPECIALBOUND=library.so:symbol.
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -24,6 +28,8 @@
 #include <sstream>
 #include <string>
 #include <vector>
+
+#include <dlfcn.h>
 
 #include "../../include/vacgpu.h"
 
@@ -468,7 +474,7 @@ int main(int argc, char** argv) {
   p.dtmin = getd("dtmin", 1e-99);
   // boundlist: typeB(iw,iB) in column order (iw fastest), default 'cont'
   const char* bcnames[] = {"cont", "periodic", "symm", "asymm", "fixed",
-                           "fixed1", "cont1", "grad1", "symm0"};
+                           "fixed1", "cont1", "grad1", "symm0", "special"};
   for (auto* a : find_all("typeb")) {
     size_t o = 0;
     if (a->idx.size() == 2) o = (a->idx[1] - 1) * nw + (a->idx[0] - 1);
@@ -479,7 +485,7 @@ int main(int argc, char** argv) {
       if (ib >= 2 * ini.ndim) break;
       std::string t = lower(to_str(a->vals[k]));
       int b = -1;
-      for (int m = 0; m < 9; m++)
+      for (int m = 0; m < 10; m++)
         if (t == bcnames[m]) b = m;
       if (b < 0) die("Error in GetBoundary: boundary type " + t + " is not on this path");
       p.typeB[ib][iw] = b;
@@ -553,6 +559,22 @@ int main(int argc, char** argv) {
     }
   };
   chk(vacgpu_create(&p, &h));
+  bool special = false;
+  for (int ib = 0; ib < 2 * p.ndim; ib++)
+    for (int iw = 0; iw < nw; iw++) special |= p.typeB[ib][iw] == VACGPU_BC_SPECIAL;
+  if (special) {
+    // the user's specialbound as a device hook: VACGB_SPECIALBOUND=lib.so:symbol
+    const char* spec = std::getenv("VACGB_SPECIALBOUND");
+    if (!spec) die("Special boundary is not defined (set VACGB_SPECIALBOUND=lib.so:symbol)");
+    std::string sp(spec);
+    size_t colon = sp.rfind(':');
+    if (colon == std::string::npos) die("VACGB_SPECIALBOUND must be library.so:symbol");
+    void* lib = dlopen(sp.substr(0, colon).c_str(), RTLD_NOW | RTLD_LOCAL);
+    if (!lib) die(std::string("VACGB_SPECIALBOUND: ") + dlerror());
+    void* fn = dlsym(lib, sp.substr(colon + 1).c_str());
+    if (!fn) die("VACGB_SPECIALBOUND: no symbol " + sp.substr(colon + 1));
+    chk(vacgpu_register_bound(h, (vacgpu_bound_fn)fn, nullptr));
+  }
   chk(vacgpu_set_grid(h, ini.x.data()));
   chk(vacgpu_upload(h, ini.w.data(), ini.it, ini.t));
   std::printf("Start Advance  %10.3f sec\n", cputime());
