@@ -13,9 +13,10 @@
 // The FP64 instance (roe_fp64.cu, built without FMA contraction) keeps every
 // array statement's operation order and is bit-identical to the CPU
 // restatement.  The mixed instance (roe_mixed.cu, IEEE FP32 division and
-// square root) runs the solver in FP32 with the conservative pressure jump
-// dp in double and the thermal pressures from the double-float recovery of
-// physics_mixed.cuh.
+// square root) runs the solver in FP32 with cancellation-free forms of the
+// MHD average (average_mhd_f32), the thermal pressures from the
+// double-float recovery of physics_mixed.cuh, and the HD average and the
+// entropy-fix speeds in double.
 #pragma once
 #include "sweep.cuh"
 
@@ -27,14 +28,9 @@ struct RoeSweep {
   typedef typename PH::T T;
   typedef typename PH::R R;
   typedef Lay<NDIR, MHD> L;
-  // The Roe average and the entropy-fix speeds run in D (double), the
-  // waves' jumps, the right eigenvectors and the dissipative sums in Q
-  // (= R): the slow speed and the fast/slow weights af, as cancel at low
-  // beta and near the MHD degeneracies, where their square roots amplify
-  // the rounding of their arguments, so the mixed path forms them (and the
-  // conservative dp, which cancels to the pressure jump) in double.
+  // R: the path's arithmetic (double on the FP64 path, float on the mixed
+  // one); D: double, for the HD average and the entropy-fix speeds
   typedef double D;
-  typedef R Q;
   static constexpr int NW = L::NW;
   static constexpr int E = L::E;
   static constexpr int B0 = L::B0;
@@ -60,8 +56,7 @@ struct RoeSweep {
   }
   static __device__ __forceinline__ D rmax(D a, D b) { return a > b ? a : b; }
   static __device__ __forceinline__ D rmin(D a, D b) { return a < b ? a : b; }
-  // smalldouble of the reference (1e-99), a normal number in FP32 for the
-  // mixed instance
+  // smalldouble of the reference
   static __device__ __forceinline__ D tiny() { return 1.0e-99; }
 
   // idir = idim+1-ndir*(idim/ndir) and jdir likewise, 1-based
@@ -91,35 +86,34 @@ struct RoeSweep {
                                               const R* wR, int d, double smallp,
                                               D qdt, D dxs, const R* bd,
                                               Face& f, D* am) {
-    // the jumps and eigenvalues in Q from the double Roe state
-    const Q rL = Q(wL[0]), rR = Q(wR[0]);
-    const Q v = Q(f.v[d]);
-    const Q cf = Q(f.cf), cs = Q(f.cs), af = Q(f.af), as = Q(f.as);
-    const Q cs2 = Q(f.cs2), rhodv = Q(f.rhodv), dp = Q(f.dp), sr = Q(f.sr);
-    Q aa, jump;
+    const R rL = wL[0], rR = wR[0];
+    const R v = f.v[d];
+    const R cf = f.cf, cs = f.cs, af = f.af, as = f.as;
+    const R cs2 = f.cs2, rhodv = f.rhodv, dp = f.dp, sr = f.sr;
+    R aa, jump;
     if (MHD) {
       // bd = {bdv, bdb} of the fast/slow waves, then of the Alfven waves
-      const Q bdv = il < 6 ? bd[0] : bd[2];
-      const Q bdb = il < 6 ? bd[1] : bd[3];
+      const R bdv = il < 6 ? bd[0] : bd[2];
+      const R bdb = il < 6 ? bd[1] : bd[3];
       switch (il) {
         case 0:
           aa = v + cf;
-          jump = Q(0.5) / cs2 *
+          jump = R(0.5) / cs2 *
                  (af * (+cf * rhodv + dp) + as * (-cs * bdv + bdb));
           break;
         case 1:
           aa = v - cf;
-          jump = Q(0.5) / cs2 *
+          jump = R(0.5) / cs2 *
                  (af * (-cf * rhodv + dp) + as * (+cs * bdv + bdb));
           break;
         case 2:
           aa = v + cs;
-          jump = Q(0.5) / cs2 *
+          jump = R(0.5) / cs2 *
                  (as * (+cs * rhodv + dp) + af * (+cf * bdv - bdb));
           break;
         case 3:
           aa = v - cs;
-          jump = Q(0.5) / cs2 *
+          jump = R(0.5) / cs2 *
                  (as * (-cs * rhodv + dp) + af * (-cf * bdv - bdb));
           break;
         case 4:
@@ -129,18 +123,18 @@ struct RoeSweep {
         case 5:
           if (a.ph.divbwave) {
             aa = v;
-            jump = Q(wR[B0 + 1 + d]) - Q(wL[B0 + 1 + d]);
+            jump = R(wR[B0 + 1 + d]) - R(wL[B0 + 1 + d]);
           } else {
-            aa = Q(0);
-            jump = Q(0);
+            aa = R(0);
+            jump = R(0);
           }
           break;
         case 6:
-          aa = v + Q(fabs(f.b[d])) / sr;
+          aa = v + R(fabs(f.b[d])) / sr;
           jump = +bdv - bdb;
           break;
         default:
-          aa = v - Q(fabs(f.b[d])) / sr;
+          aa = v - R(fabs(f.b[d])) / sr;
           jump = -bdv - bdb;
           break;
       }
@@ -148,11 +142,11 @@ struct RoeSweep {
       switch (il) {
         case 0:
           aa = v + cs;
-          jump = Q(0.5) * (dp + sr * rhodv);
+          jump = R(0.5) * (dp + sr * rhodv);
           break;
         case 1:
           aa = v - cs;
-          jump = Q(0.5) * (dp - sr * rhodv);
+          jump = R(0.5) * (dp - sr * rhodv);
           break;
         case 2:
           aa = v;
@@ -162,7 +156,7 @@ struct RoeSweep {
           int idir = il - 3;
           if (idir >= d) idir++;
           aa = v;
-          jump = sr * (Q(wR[1 + idir]) / rR - Q(wL[1 + idir]) / rL);
+          jump = sr * (R(wR[1 + idir]) / rR - R(wL[1 + idir]) / rL);
         }
       }
     }
@@ -170,9 +164,9 @@ struct RoeSweep {
     // double (the slow speeds of the left and right states cancel as the
     // averaged one does)
     const int te = a.ph.typeentropy[il];
-    Q smalla = Q(0);
+    R smalla = R(0);
     if (te == VACGPU_ENTROPY_YEE) {
-      smalla = Q(a.ph.entropycoef[il]);
+      smalla = R(a.ph.entropycoef[il]);
     } else if (te != VACGPU_ENTROPY_NUL) {
       const double g = a.ph.gamma;
       const double dL = wL[0], dR = wR[0];
@@ -223,24 +217,24 @@ struct RoeSweep {
       const double ad = aa;
       if (te == VACGPU_ENTROPY_HARTEN) {
         const double m = 0.0 > ad - aL ? 0.0 : ad - aL;
-        smalla = Q(m > aR - ad ? m : aR - ad);
+        smalla = R(m > aR - ad ? m : aR - ad);
       } else if (te == VACGPU_ENTROPY_POWELL) {
         const double q = 2.0 * (aR - aL);
-        smalla = Q(0.0 > q ? 0.0 : q);
+        smalla = R(0.0 > q ? 0.0 : q);
       } else if (aL < 0.0 && aR > 0.0) {  // 'ratio'
-        aa = Q(ad - 2.0 * aR * aL / (aR - aL));
+        aa = R(ad - 2.0 * aR * aL / (aR - aL));
       }
     }
     // normalisation by dt*2/(dx(i)+dx(j)) (src/vactvd.t:131-140)
-    const Q adt = aa * Q(qdt) * Q(2) / Q(dxs);
+    const R adt = aa * R(qdt) * R(2) / R(dxs);
     if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL)
-      smalla = smalla * Q(qdt) * Q(2) / Q(dxs);
+      smalla = smalla * R(qdt) * R(2) / R(dxs);
     if (il < 2) am[il] = fabs(adt);
     if (te == VACGPU_ENTROPY_NUL || te == VACGPU_ENTROPY_RATIO ||
         fabs(adt) >= smalla)
       f.phi[il] = fabs(adt) * jump;
     else
-      f.phi[il] = Q(0.5) * (smalla + adt * adt / smalla) * jump;
+      f.phi[il] = R(0.5) * (smalla + adt * adt / smalla) * jump;
   }
 
   // The mixed instance's MHD average: FP32 with cancellation-free forms of
@@ -360,16 +354,15 @@ struct RoeSweep {
                                                    const R* wL, const R* wR,
                                                    int d, double smallp, D qdt,
                                                    D dxs, Face& f, D* am) {
-    // The averages are formed in double (on the mixed path too): the slow
-    // speed and the fast/slow weights af, as cancel at low beta and near
-    // the MHD degeneracies, where their square roots amplify the rounding;
-    // the waves and eigenvectors then run in D.
+    // FP64 path: the reference's statements in double.  Mixed path: the
+    // MHD average in FP32 with cancellation-free forms (average_mhd_f32),
+    // the HD average in double.
     const D rL = wL[0], rR = wR[0];
     const double dL = rL, dR = rR;
     R bd[4] = {R(0), R(0), R(0), R(0)};
     if constexpr (MHD && sizeof(R) == 4) {
       average_mhd_f32(a, wL, wR, d, smallp, f, bd);
-    } else if (MHD) {
+    } else if constexpr (MHD) {
       const double rho = 0.5 * (dL + dR);
       double B[NDIR];
 #pragma unroll
@@ -497,43 +490,28 @@ struct RoeSweep {
   // R(iw,il)*q at the Roe state (rtimes, src/vacphys.mhdroe.t:284-449 and
   // src/vacphys.hdroe.t:144-215)
   template <int iw, int il>
-  static __device__ __forceinline__ Q rtimes(const SweepArgs& a, const Face& f0,
-                                             Q q, int d) {
-    struct {
-      Q v[NDIR], b[NDIR], sr, cf, cs, af, as, cs2, h;
-    } f;
-#pragma unroll
-    for (int c = 0; c < NDIR; c++) {
-      f.v[c] = Q(f0.v[c]);
-      f.b[c] = Q(f0.b[c]);
-    }
-    f.sr = Q(f0.sr);
-    f.cf = Q(f0.cf);
-    f.cs = Q(f0.cs);
-    f.af = Q(f0.af);
-    f.as = Q(f0.as);
-    f.cs2 = Q(f0.cs2);
-    f.h = Q(f0.h);
-    const Q v = f.v[d];
+  static __device__ __forceinline__ R rtimes(const SweepArgs& a, const Face& f,
+                                             R q, int d) {
+    const R v = f.v[d];
     if (MHD) {
       const int I = dir_i(d), J = dir_j(d);
       if (iw == 0) {
         if (il <= 1) return q * f.af;
         if (il <= 3) return q * f.as;
         if (il == 4) return q;
-        return Q(0);
+        return R(0);
       }
       if (iw == E) {
-        Q vv = f.v[0] * f.v[0];
+        R vv = f.v[0] * f.v[0];
 #pragma unroll
         for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
-        const Q g = Q(a.ph.gamma);
-        const Q v2a2 = Q(0.5) * vv + (Q(2) - g) / Q(a.ph.gm1) * f.cs2;
-        Q bv;
+        const R g = R(a.ph.gamma);
+        const R v2a2 = R(0.5) * vv + (R(2) - g) / R(a.ph.gm1) * f.cs2;
+        R bv;
         if (il < 6) {
           bv = f.b[I] * f.v[I];
           if (NDIR == 3) bv = bv + f.b[J] * f.v[J];
-          bv = bv * Q(fsign(1.0, f.b[d]));
+          bv = bv * R(fsign(1.0, f.b[d]));
         } else {
           bv = f.b[J] * f.v[I] - f.b[I] * f.v[J];
         }
@@ -547,9 +525,9 @@ struct RoeSweep {
           case 3:
             return q * (-f.af * f.cf * bv + f.as * (v2a2 + f.cs * (f.cs - v)));
           case 4:
-            return q * Q(0.5) * vv;
+            return q * R(0.5) * vv;
           case 5:
-            return a.ph.divbwave ? q * f.b[d] : Q(0);
+            return a.ph.divbwave ? q * f.b[d] : R(0);
           case 6:
             return +q * bv;
           default:
@@ -558,7 +536,7 @@ struct RoeSweep {
       }
       if (iw <= NDIR) {
         const int c = iw - 1;
-        const Q vw = f.v[c];
+        const R vw = f.v[c];
         if (c == d) {
           switch (il) {
             case 0: return q * f.af * (vw + f.cf);
@@ -566,25 +544,25 @@ struct RoeSweep {
             case 2: return q * f.as * (vw + f.cs);
             case 3: return q * f.as * (vw - f.cs);
             case 4: return q * vw;
-            default: return Q(0);
+            default: return R(0);
           }
         }
-        const Q bw = f.b[c];
-        const Q sg = Q(fsign(1.0, f.b[d]));
+        const R bw = f.b[c];
+        const R sg = R(fsign(1.0, f.b[d]));
         switch (il) {
           case 0: return q * (f.af * vw - f.as * f.cs * bw * sg);
           case 1: return q * (f.af * vw + f.as * f.cs * bw * sg);
           case 2: return q * (f.as * vw + f.af * f.cf * bw * sg);
           case 3: return q * (f.as * vw - f.af * f.cf * bw * sg);
           case 4: return q * vw;
-          case 5: return Q(0);
+          case 5: return R(0);
           case 6: return c == I ? +q * f.b[J] : -q * f.b[I];
           default: return c == I ? -q * f.b[J] : +q * f.b[I];
         }
       }
       const int c = iw - B0 - 1;
-      if (c == d) return (il == 5 && a.ph.divbwave) ? q : Q(0);
-      const Q bw = f.b[c];
+      if (c == d) return (il == 5 && a.ph.divbwave) ? q : R(0);
+      const R bw = f.b[c];
       switch (il) {
         case 0:
         case 1:
@@ -594,25 +572,25 @@ struct RoeSweep {
           return -q * f.af * sqrt(f.cs2) * bw / f.sr;
         case 4:
         case 5:
-          return Q(0);
+          return R(0);
         default:
-          if (c == I) return -q * f.b[J] / Q(fsign(f.sr, f.b[d]));
-          return +q * f.b[I] / Q(fsign(f.sr, f.b[d]));
+          if (c == I) return -q * f.b[J] / R(fsign(f.sr, f.b[d]));
+          return +q * f.b[I] / R(fsign(f.sr, f.b[d]));
       }
     } else {
       const bool shear = il >= 3;
       int idir = il - 3;
       if (idir >= d) idir++;
-      if (iw == 0) return shear ? Q(0) : q;
+      if (iw == 0) return shear ? R(0) : q;
       if (iw == E) {
         switch (il) {
           case 0: return q * (f.h + v * f.cs);
           case 1: return q * (f.h - v * f.cs);
           case 2: {
-            Q vv = f.v[0] * f.v[0];
+            R vv = f.v[0] * f.v[0];
 #pragma unroll
             for (int k = 1; k < NDIR; k++) vv = vv + f.v[k] * f.v[k];
-            return q * Q(0.5) * vv;
+            return q * R(0.5) * vv;
           }
           default: return q * f.v[idir];
         }
@@ -622,9 +600,9 @@ struct RoeSweep {
         if (il == 0) return q * (v + f.cs);
         if (il == 1) return q * (v - f.cs);
         if (il == 2) return q * v;
-        return Q(0);
+        return R(0);
       }
-      if (shear) return c == idir ? q : Q(0);
+      if (shear) return c == idir ? q : R(0);
       return q * f.v[c];
     }
   }
@@ -650,29 +628,29 @@ struct RoeSweep {
   }
 
   // dvolume(ix) = dx_1*dx_2*dx_3 (gridsetup1, src/vacgrid.t:573-576)
-  static __device__ __forceinline__ Q dvol(const SweepArgs& a, const int* c) {
+  static __device__ __forceinline__ R dvol(const SweepArgs& a, const int* c) {
     double v = a.a.dx[0][c[0]];
     if (NDIM > 1) v = v * a.a.dx[1][c[1]];
     if (NDIM > 2) v = v * a.a.dx[2][c[2]];
-    return Q(v);
+    return R(v);
   }
 
   // wave il's dissipative fluxes of every variable into acc
   template <int il, int iw>
   static __device__ __forceinline__ void dissipate_var(
-      const SweepArgs& a, const Face& fm, const Face& fp, int d, Q vm, Q vp,
-      Q dv0, int nofm, int nofp, R* acc) {
-    Q rp = rtimes<iw, il>(a, fp, Q(fp.phi[il]), d) * Q(0.25) * vp;
-    Q rm = rtimes<iw, il>(a, fm, Q(fm.phi[il]), d) * Q(0.25) * vm;
-    if ((nofp >> iw) & 1) rp = Q(0);
-    if ((nofm >> iw) & 1) rm = Q(0);
+      const SweepArgs& a, const Face& fm, const Face& fp, int d, R vm, R vp,
+      R dv0, int nofm, int nofp, R* acc) {
+    R rp = rtimes<iw, il>(a, fp, R(fp.phi[il]), d) * R(0.25) * vp;
+    R rm = rtimes<iw, il>(a, fm, R(fm.phi[il]), d) * R(0.25) * vm;
+    if ((nofp >> iw) & 1) rp = R(0);
+    if ((nofm >> iw) & 1) rm = R(0);
     acc[iw] = acc[iw] + R((rp - rm) / dv0);
   }
   template <int il>
   static __device__ __forceinline__ void dissipate(const SweepArgs& a,
                                                    const Face& fm,
                                                    const Face& fp, int d,
-                                                   Q vm, Q vp, Q dv0, int nofm,
+                                                   R vm, R vp, R dv0, int nofm,
                                                    int nofp, R* acc) {
     dissipate_var<il, 0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
     dissipate_var<il, 1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
@@ -691,7 +669,7 @@ struct RoeSweep {
   static __device__ __forceinline__ void direction(
       const SweepArgs& a, const T* __restrict__ w1, const T* __restrict__ base,
       long long off, const long long* st, const int* c, R smallp,
-      double qsmallp, double qdt, bool limit, Q dv0, R* acc,
+      double qsmallp, double qdt, bool limit, R dv0, R* acc,
       unsigned long long* key) {
     Face fm, fp;
     R Fm[NW], Fp[NW];
@@ -723,11 +701,11 @@ struct RoeSweep {
       acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
     int cn[3] = {c[0], c[1], c[2]};
     cn[d] = c[d] - 1;
-    const Q dvm = dvol(a, cn);
+    const R dvm = dvol(a, cn);
     cn[d] = c[d] + 1;
-    const Q dvp = dvol(a, cn);
-    const Q vm = dv0 + dvm;  // dvolume(j)+dvolume(i) of the lower face
-    const Q vp = dvp + dv0;  // and of the upper face
+    const R dvp = dvol(a, cn);
+    const R vm = dv0 + dvm;  // dvolume(j)+dvolume(i) of the lower face
+    const R vp = dvp + dv0;  // and of the upper face
     dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
     dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
     dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
@@ -769,7 +747,7 @@ struct RoeSweep {
         S::to_cons(a, acc);
       }
       const double qsmallp = ctrl->smallp;
-      const Q dv0 = dvol(a, c);
+      const R dv0 = dvol(a, c);
       for (int d = a.d0; d <= a.d1; d++) {
         if (d == 0)
           direction<0>(a, w1, base, off, st, c, smallp, qsmallp, qdt, limit,
