@@ -151,7 +151,8 @@ typedef struct vacgpu_params {
   double vacuumrho;             /* >=0: rho<smallrho becomes vacuum         */
   int useprimitive;             /* limit primitive variables (upwindLR,     */
                                 /* src/vactvdlf.t:325-362)                  */
-  /* resistive MHD, eqpar[1] = eqpar(eta_) > 0 (src/vacphys.mhdres.t)     */
+  /* resistive MHD, eqpar[1] = eqpar(eta_): > 0 constant eta, < 0 the     */
+  /* specialeta hook's field (src/vacphys.mhdres.t)                        */
   int compactres;               /* 1: Laplacian form, 0: curl form          */
   double dtdiffpar;             /* diffusion dt limit dtdiffpar*dx^2/eta    */
   /* Roe dissipation of 'tvdmu'/'tvdmu1' (src/vactvd.t:86-206)             */
@@ -245,6 +246,31 @@ typedef int (*vacgpu_bound_fn)(void* user, void* w, const vacgpu_region* r,
  * with 'special' faces refuses to run without one ("Special boundary is
  * not defined", src/vacnul.specialbound.t:12). */
 int vacgpu_register_bound(vacgpu_handle* h, vacgpu_bound_fn fn, void* user);
+
+/* specialeta (src/vacphys.mhdres.t:26-30,127-129,271-273; eqpar(eta_) < 0):
+ * the user's resistivity field.  The engine calls the hook on the host while
+ * it issues a step (also under CUDA-graph capture) before each resistive
+ * source evaluation -- the predictor's, from the state, and the
+ * corrector's, from the predictor output -- and before the first step's dt
+ * choice (getdt_res); the hook enqueues device work on `stream` that writes
+ * eta, and gradeta for the compact form, on the cells of `box` (the mesh
+ * and one layer around it in each used dimension).  Arrays share the
+ * state's cell indexing (box.offset0, box.stride); box.qt points at the
+ * time-loop t, box.iB is -1. */
+typedef struct vacgpu_eta_args {
+  vacgpu_region box;
+  const void* w;            /* device: the state the source is evaluated on */
+  const double* current[3]; /* device: J_1..J_3 on box (from idirmin on)    */
+  int idirmin;              /* first J component set: 7-2*ndir              */
+  double* eta;              /* device, out: eta on box                      */
+  double* gradeta[3];       /* device, out (compactres, else NULL): d eta/dx_j */
+} vacgpu_eta_args;
+typedef int (*vacgpu_eta_fn)(void* user, const vacgpu_eta_args* e,
+                             void* stream);
+
+/* Install the specialeta hook (NULL removes it); a grid with
+ * eqpar(eta_) < 0 refuses to run without one. */
+int vacgpu_register_eta(vacgpu_handle* h, vacgpu_eta_fn fn, void* user);
 
 /* Install a device source hook (specialsource + getdt_special,
  * src/vacnul.specialsource.t:9-71); VACGPU_SRC_NONE removes it. */

@@ -74,6 +74,15 @@ typedef struct vo_state {
                    const long* st, long N, const double* x, int iw, int iB,
                    double qt);
   void* bound_user;
+  /* specialeta hook (eqpar(eta_) < 0): eta, and gradeta for the compact
+   * form, on box lo..hi from w and the current J (components idirmin..3) */
+  void (*eta_fn)(void* user, const double* w, const double* const* cur,
+                 double* eta, double* const* gradeta, const int* lo,
+                 const int* hi, const long* st, long N,
+                 const double* const* x, int idirmin, double t);
+  void* eta_user;
+  double* eta;        /* eta(ixG^T) of the common block */
+  double* gradeta[3];
 } vo_state;
 
 /* ------------------------------------------------------------------ boxes */
@@ -584,9 +593,22 @@ static int getcurrent(vo_state* s, const double* w, box ix) {
   return idirmin;
 }
 
-/* addsource_res2, src/vacphys.mhdres.t:236-315 (curl form, compactres=F),
- * constant eta = eqpar(eta_) > 0:  B_i -= eps_ijk d_j (eta J_k) qdt,
- * e += eps_ijk d_i (B_j eta J_k qdt) */
+/* specialeta (src/vacphys.mhdres.t:26-30,127-129,271-273): the user's
+ * eta(ix) -- and gradeta for the compact form -- on box ix from w and the
+ * current of getcurrent, at the time-loop t */
+static void special_eta(vo_state* s, const double* w, box ix, int idirmin) {
+  if (!s->eta_fn) return;
+  const double* cur[3] = {s->cur[0], s->cur[1], s->cur[2]};
+  const double* x[3] = {W(s->x, 0), W(s->x, s->ndim > 1 ? 1 : 0),
+                        W(s->x, s->ndim > 2 ? 2 : 0)};
+  double* g[3] = {s->gradeta[0], s->gradeta[1], s->gradeta[2]};
+  s->eta_fn(s->eta_user, w, cur, s->eta, g, ix.lo, ix.hi, s->st, s->N, x,
+            idirmin, s->t);
+}
+
+/* addsource_res2, src/vacphys.mhdres.t:236-315 (curl form, compactres=F):
+ * B_i -= eps_ijk d_j (eta J_k) qdt, e += eps_ijk d_i (B_j eta J_k qdt);
+ * eta = eqpar(eta_) > 0 or the specialeta field */
 static void addsource_res2(vo_state* s, double qdt, box ixO, const double* w,
                            double* wnew) {
   box ix = ixO;
@@ -596,6 +618,9 @@ static void addsource_res2(vo_state* s, double qdt, box ixO, const double* w,
   }
   const int idirmin = getcurrent(s, w, ix);
   const double eta = s->p.eqpar[1];
+  const int field = eta < ZERO;
+  if (field) special_eta(s, w, ix, idirmin);
+  const double* ef = s->eta;
   for (int iw = 0; iw < s->nw; iw++) {
     double* wn = W(wnew, iw);
     if (iw > s->b0_ && iw <= s->b0_ + s->ndir) {
@@ -605,7 +630,10 @@ static void addsource_res2(vo_state* s, double qdt, box ixO, const double* w,
           const int l = lvc(idir, jdir, kdir);
           if (!l) continue;
           const double* c = s->cur[kdir - 1];
-          FORBOX(ix, i) s->tmp[i] = c[i] * eta * qdt;
+          if (field)
+            FORBOX(ix, i) s->tmp[i] = c[i] * ef[i] * qdt;
+          else
+            FORBOX(ix, i) s->tmp[i] = c[i] * eta * qdt;
           gradient(s, s->tmp, ixO, jdir - 1, s->tmp2);
           if (l == 1)
             FORBOX(ixO, i) wn[i] = wn[i] - s->tmp2[i];
@@ -620,7 +648,10 @@ static void addsource_res2(vo_state* s, double qdt, box ixO, const double* w,
             if (!l) continue;
             const double* c = s->cur[kdir - 1];
             const double* bj = W(w, s->b0_ + jdir);
-            FORBOX(ix, i) s->tmp[i] = bj[i] * c[i] * eta * qdt;
+            if (field)
+              FORBOX(ix, i) s->tmp[i] = bj[i] * c[i] * ef[i] * qdt;
+            else
+              FORBOX(ix, i) s->tmp[i] = bj[i] * c[i] * eta * qdt;
             gradient(s, s->tmp, ixO, idir - 1, s->tmp2);
             if (l == 1)
               FORBOX(ixO, i) wn[i] = wn[i] + s->tmp2[i];
@@ -631,13 +662,17 @@ static void addsource_res2(vo_state* s, double qdt, box ixO, const double* w,
   }
 }
 
-/* addsource_res1, src/vacphys.mhdres.t:96-233 (compact form, compactres=T),
- * constant eta > 0: B_i += qdt eta lap(B_i), e += qdt eta lap(B_i) B_i for
- * each i, then e += qdt eta J^2 */
+/* addsource_res1, src/vacphys.mhdres.t:96-233 (compact form, compactres=T):
+ * B_i += qdt (eta lap(B_i) - [grad(eta) x J]_i), e += the same times B_i for
+ * each i, then e += qdt eta J^2 (the gradeta terms for the specialeta
+ * field only) */
 static void addsource_res1(vo_state* s, double qdt, box ixO, const double* w,
                            double* wnew) {
   const int idirmin = getcurrent(s, w, ixO);
   const double eta = s->p.eqpar[1];
+  const int field = eta < ZERO;
+  if (field) special_eta(s, w, ixO, idirmin);
+  const double* ef = s->eta;
   double* tmp = s->tmp;
   for (int idir = 1; idir <= s->ndir; idir++) {
     FORBOX(ixO, i) tmp[i] = ZERO;
@@ -647,7 +682,22 @@ static void addsource_res1(vo_state* s, double qdt, box ixO, const double* w,
       const double* dx = W(s->dx, idim);
       FORBOX(ixO, i) tmp[i] = tmp[i] + (q[i + sh] - 2 * q[i] + q[i - sh]) / (dx[i] * dx[i]);
     }
-    FORBOX(ixO, i) tmp[i] = tmp[i] * eta;
+    if (field) {
+      FORBOX(ixO, i) tmp[i] = tmp[i] * ef[i];
+      for (int jdir = 1; jdir <= s->ndim; jdir++)
+        for (int kdir = idirmin; kdir <= 3; kdir++) {
+          const int l = lvc(idir, jdir, kdir);
+          if (!l) continue;
+          const double* ge = s->gradeta[jdir - 1];
+          const double* c = s->cur[kdir - 1];
+          if (l == 1)
+            FORBOX(ixO, i) tmp[i] = tmp[i] - ge[i] * c[i];
+          else
+            FORBOX(ixO, i) tmp[i] = tmp[i] + ge[i] * c[i];
+        }
+    } else {
+      FORBOX(ixO, i) tmp[i] = tmp[i] * eta;
+    }
     for (int iw = 0; iw < s->nw; iw++) {
       double* wn = W(wnew, iw);
       if (iw == s->b0_ + idir)
@@ -660,7 +710,7 @@ static void addsource_res1(vo_state* s, double qdt, box ixO, const double* w,
   FORBOX(ixO, i) {
     double jj = ZERO;
     for (int idir = idirmin; idir <= 3; idir++) jj = jj + s->cur[idir - 1][i] * s->cur[idir - 1][i];
-    e[i] = e[i] + qdt * eta * jj;
+    e[i] = e[i] + qdt * (field ? ef[i] : eta) * jj;
   }
 }
 
@@ -1719,19 +1769,43 @@ static void getdt_courant(vo_state* s) {
   }
 }
 
-/* getdt_res, src/vacphys.mhdres.t:5-45 (eqpar(eta_) > 0): the diffusion
- * limit dtdiffpar*min(dx)^2/eta, called from getdt (src/vacphys.mhd0.t:83-103) */
+/* getdt_res, src/vacphys.mhdres.t:5-45: the diffusion limit, called from
+ * getdt (src/vacphys.mhd0.t:83-103) on ixM: dtdiffpar*min(dx)^2/eta for
+ * eqpar(eta_) > 0; for the specialeta field min over idim of
+ * dtdiffpar/(smalldouble+max(eta/dx^2)), eta set from w at it==itmin and
+ * otherwise the one of the last resistive source */
 static void getdt_res(vo_state* s) {
-  double m = ZERO;
-  int first = 1;
-  for (int d = 0; d < s->ndim; d++) {
-    const double* dx = W(s->dx, d);
-    FORBOX_SEQ(s->ixM, i) {
-      if (first || dx[i] < m) m = dx[i];
-      first = 0;
+  double dtdiff;
+  if (s->p.eqpar[1] > ZERO) {
+    double m = ZERO;
+    int first = 1;
+    for (int d = 0; d < s->ndim; d++) {
+      const double* dx = W(s->dx, d);
+      FORBOX_SEQ(s->ixM, i) {
+        if (first || dx[i] < m) m = dx[i];
+        first = 0;
+      }
+    }
+    dtdiff = s->p.dtdiffpar * (m * m) / s->p.eqpar[1];
+  } else {
+    if (s->it == s->itmin) {
+      const int idirmin = getcurrent(s, s->w, s->ixM);
+      special_eta(s, s->w, s->ixM, idirmin);
+    }
+    dtdiff = BIGDOUBLE;
+    for (int d = 0; d < s->ndim; d++) {
+      const double* dx = W(s->dx, d);
+      double m = ZERO;
+      int first = 1;
+      FORBOX_SEQ(s->ixM, i) {
+        const double q = s->eta[i] / (dx[i] * dx[i]);
+        if (first || q > m) m = q;
+        first = 0;
+      }
+      const double c = s->p.dtdiffpar / (SMALLDOUBLE + m);
+      if (c < dtdiff) dtdiff = c;
     }
   }
-  const double dtdiff = s->p.dtdiffpar * (m * m) / s->p.eqpar[1];
   if (dtdiff < s->dt) s->dt = dtdiff;
 }
 
@@ -1850,6 +1924,10 @@ vo_state* vo_create(const vacgpu_params* p) {
   for (unsigned i = 0; i < sizeof(t1) / sizeof(t1[0]); i++)
     *t1[i] = calloc(N, sizeof(double));
   for (int c = 0; c < 3; c++) s->cur[c] = calloc(N, sizeof(double));
+  if (s->mhd && p->eqpar[1] < ZERO) {
+    s->eta = calloc(N, sizeof(double));
+    for (int c = 0; c < 3; c++) s->gradeta[c] = calloc(N, sizeof(double));
+  }
   s->smallp = p->smallp;
   s->smallrho = p->smallrho;
   s->courantpar = p->courantpar;
@@ -1876,6 +1954,8 @@ void vo_destroy(vo_state* s) {
   for (int iB = 0; iB < VACGPU_MAXB; iB++) free(s->fixB[iB]);
   for (int c = 0; c < 3; c++) free(s->cur[c]);
   free(s->wroe);
+  free(s->eta);
+  for (int c = 0; c < 3; c++) free(s->gradeta[c]);
   for (int i = 0; i < NROE; i++) free(s->roe[i]);
   free(s);
 }
@@ -1993,6 +2073,16 @@ void vo_register_bound(vo_state* s,
                        void* user) {
   s->bound_fn = fn;
   s->bound_user = user;
+}
+
+void vo_register_eta(vo_state* s,
+                     void (*fn)(void*, const double*, const double* const*,
+                                double*, double* const*, const int*,
+                                const int*, const long*, long,
+                                const double* const*, int, double),
+                     void* user) {
+  s->eta_fn = fn;
+  s->eta_user = user;
 }
 
 void vo_register_source(vo_state* s, int id, const double* par, int npar) {

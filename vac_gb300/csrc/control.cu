@@ -85,6 +85,8 @@ __device__ void smallp_dev(Ctrl* c, int mhd, double coeff) {
 struct DtEndArgs {
   int ndim, itmax, slowsteps, dtcantgrow, tmaxexact;
   double tmax, dtmin;
+  int etafield;       // specialeta: dtdiff from the field's max eta/dx^2
+  double dtdiffpar;
 };
 
 __device__ void dt_end_dev(Ctrl* c, const DtEndArgs& p) {
@@ -121,7 +123,17 @@ __device__ void dt_end_dev(Ctrl* c, const DtEndArgs& p) {
     }
     // getdt: the resistive diffusion limit (getdt_res,
     // src/vacphys.mhdres.t:5-45), fixed by the grid
-    if (c->dtdiff < dt) dt = c->dtdiff;
+    if (p.etafield) {
+      // min over idim of dtdiffpar/(smalldouble+max(eta/dx^2))
+      double dtdiff = BIG;
+      for (int d = 0; d < p.ndim; d++) {
+        const double q = p.dtdiffpar / (SMALL + dkey_inv(c->etak[d]));
+        if (q < dtdiff) dtdiff = q;
+      }
+      if (dtdiff < dt) dt = dtdiff;
+    } else if (c->dtdiff < dt) {
+      dt = c->dtdiff;
+    }
     // getdt_special (uniform gravity: dtgrav fixed at the first step)
     if (c->dtgrav < dt) dt = c->dtgrav;
     if (p.dtcantgrow && c->it > c->itmin && c->dtold < dt) dt = c->dtold;
@@ -289,12 +301,53 @@ void launch_kp_smallrho(Ctrl* c, double coeff, cudaStream_t st) {
   k_kp_smallrho<<<1, NSLOT, 0, st>>>(c, coeff);
 }
 void launch_kp_end(Ctrl* c, cudaStream_t st) { k_kp_end<<<1, 1, 0, st>>>(c); }
+// Ctrl::etak = max over the mesh of eta/dx_d^2 (getdt_res,
+// src/vacphys.mhdres.t:31-35); first_only: only at it==itmin
+__global__ void k_eta_reset(Ctrl* c, int first_only) {
+  if (c->done || (first_only && c->it != c->itmin)) return;
+  for (int d = 0; d < 3; d++) c->etak[d] = 0ULL;
+}
+__global__ void k_eta_max(SweepArgs a, int first_only) {
+  Ctrl* c = a.ctrl;
+  if (c->done || (first_only && c->it != c->itmin)) return;
+  const DevGrid& g = a.g;
+  unsigned long long key[3] = {0ULL, 0ULL, 0ULL};
+  for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+       n < g.ncell; n += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(n % g.nx[0]);
+    const long long r = n / g.nx[0];
+    const int iy = (int)(r % g.nx[1]), iz = (int)(r / g.nx[1]);
+    const int cc[3] = {ix + g.gh[0], iy + g.gh[1], iz + g.gh[2]};
+    const double e = a.etaf[gidx(g, cc[0], cc[1], cc[2])];
+    for (int d = 0; d < g.ndim; d++) {
+      const double dx = a.a.dx[d][cc[d]];
+      const unsigned long long k = dkey(e / (dx * dx));
+      if (k > key[d]) key[d] = k;
+    }
+  }
+  for (int d = 0; d < g.ndim; d++) {
+    unsigned long long k = key[d];
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o);
+      k = v > k ? v : k;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&c->etak[d], k);
+  }
+}
+
+void launch_eta_max(const SweepArgs& a, int first_only, cudaStream_t st) {
+  k_eta_reset<<<1, 1, 0, st>>>(a.ctrl, first_only);
+  k_eta_max<<<2 * 152, 256, 0, st>>>(a, first_only);
+}
+
 void launch_set_qt(Ctrl* c, int mode, cudaStream_t st) {
   k_set_qt<<<1, 1, 0, st>>>(c, mode);
 }
 
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st) {
   DtEndArgs a;
+  a.etafield = p.physics == VACGPU_PHYS_MHD && p.eqpar[1] < 0.0;
+  a.dtdiffpar = p.dtdiffpar;
   a.ndim = p.ndim;
   a.itmax = p.itmax;
   a.slowsteps = p.slowsteps;
@@ -310,6 +363,8 @@ void launch_step_end(Ctrl* c, int ndim, cudaStream_t st) {
 
 static DtEndArgs dt_end_args(const vacgpu_params& p) {
   DtEndArgs a;
+  a.etafield = p.physics == VACGPU_PHYS_MHD && p.eqpar[1] < 0.0;
+  a.dtdiffpar = p.dtdiffpar;
   a.ndim = p.ndim;
   a.itmax = p.itmax;
   a.slowsteps = p.slowsteps;

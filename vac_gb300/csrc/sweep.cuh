@@ -87,13 +87,16 @@ struct Sweep {
     return j;
   }
 
-  // resistive terms of addsource for constant eta = eqpar(eta_) > 0:
-  // addsource_res2 (curl form, src/vacphys.mhdres.t:236-315) or
-  // addsource_res1 (compactres, :96-233), in the reference's term order
+  // resistive terms of addsource: addsource_res2 (curl form,
+  // src/vacphys.mhdres.t:236-315) or addsource_res1 (compactres, :96-233),
+  // in the reference's term order; eta = eqpar(eta_) > 0 or, with a
+  // specialeta field, eta (and gradeta) of the cell and its neighbours
   static __device__ __forceinline__ void add_resistive(
       const SweepArgs& a, double qdt, const R* wc, const T* __restrict__ wct,
       const long long* st, const int* c, R* acc) {
-    const R eta = R(a.ph.eta), q = PH::qdiv(qdt);
+    const double* ef = a.etaf;
+    const long long off = ef ? gidx(a.g, c[0], c[1], c[2]) : 0;
+    const R eta = ef ? R(ef[off]) : R(a.ph.eta), q = PH::qdiv(qdt);
     const long long vs = a.g.vs;
     if (!a.ph.compactres) {
       // B_i -= eps_ijk d_j (eta J_k qdt)
@@ -109,8 +112,9 @@ struct Sweep {
             cp[jd - 1]++;
             cm[jd - 1]--;
             const long long s = st[jd - 1];
-            const R tp = current(a, wct, s, st, cp, kd) * eta * q;
-            const R tm = current(a, wct, -s, st, cm, kd) * eta * q;
+            const R ep = ef ? R(ef[off + s]) : eta, em = ef ? R(ef[off - s]) : eta;
+            const R tp = current(a, wct, s, st, cp, kd) * ep * q;
+            const R tm = current(a, wct, -s, st, cm, kd) * em * q;
             const R g = R(0.5) * (tp - tm) / PH::dx(a.a, jd - 1, c[jd - 1]);
             acc[L::B0 + idir] = l == 1 ? acc[L::B0 + idir] - g : acc[L::B0 + idir] + g;
           }
@@ -127,14 +131,16 @@ struct Sweep {
             cp[idir - 1]++;
             cm[idir - 1]--;
             const long long s = st[idir - 1];
+            const R ep = ef ? R(ef[off + s]) : eta, em = ef ? R(ef[off - s]) : eta;
             const T* bj = wct + (long long)(L::B0 + jd) * vs;
-            const R tp = R(bj[s]) * current(a, wct, s, st, cp, kd) * eta * q;
-            const R tm = R(bj[-s]) * current(a, wct, -s, st, cm, kd) * eta * q;
+            const R tp = R(bj[s]) * current(a, wct, s, st, cp, kd) * ep * q;
+            const R tm = R(bj[-s]) * current(a, wct, -s, st, cm, kd) * em * q;
             const R g = R(0.5) * (tp - tm) / PH::dx(a.a, idir - 1, c[idir - 1]);
             acc[L::E] = l == 1 ? acc[L::E] + g : acc[L::E] - g;
           }
     } else {
-      // B_i += qdt eta lap(B_i), e += qdt eta lap(B_i) B_i, then e += qdt eta J^2
+      // B_i += qdt (eta lap(B_i) - [grad(eta) x J]_i), e += the same B_i,
+      // then e += qdt eta J^2
 #pragma unroll
       for (int idir = 1; idir <= NDIR; idir++) {
         const T* qb = wct + (long long)(L::B0 + idir) * vs;
@@ -145,6 +151,18 @@ struct Sweep {
           t = t + (R(qb[st[d]]) - R(2) * R(qb[0]) + R(qb[-st[d]])) / (dx * dx);
         }
         t = t * eta;
+        if (ef) {
+#pragma unroll
+          for (int jd = 1; jd <= NDIM; jd++)
+#pragma unroll
+            for (int kd = IDM0; kd <= 3; kd++) {
+              const int l = lvc(idir, jd, kd);
+              if (!l) continue;
+              const R ge = R(a.gradetaf[jd - 1][off]);
+              const R jk = current(a, wct, 0, st, c, kd);
+              t = l == 1 ? t - ge * jk : t + ge * jk;
+            }
+        }
         acc[L::B0 + idir] = acc[L::B0 + idir] + q * t;
         acc[L::E] = acc[L::E] + q * t * wc[L::B0 + idir];
       }
@@ -156,6 +174,29 @@ struct Sweep {
       }
       acc[L::E] = acc[L::E] + q * eta * jj;
     }
+  }
+
+  // getcurrent (src/vacphys.mhdres.t:48-93) into double fields over the
+  // mesh and one layer around it, for the specialeta hook
+  static __device__ void current_field(const SweepArgs& a, const T* __restrict__ w,
+                                       double* const* cur) {
+    const DevGrid& g = a.g;
+    int ext[3], lo[3];
+    for (int d = 0; d < 3; d++) {
+      lo[d] = d < g.ndim ? 1 : 0;
+      ext[d] = d < g.ndim ? g.nx[d] + 2 : 1;
+    }
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= (long long)ext[0] * ext[1] * ext[2]) return;
+    int c[3];
+    c[0] = lo[0] + (int)(n % ext[0]);
+    c[1] = lo[1] + (int)((n / ext[0]) % ext[1]);
+    c[2] = lo[2] + (int)(n / ((long long)ext[0] * ext[1]));
+    const long long off = gidx(g, c[0], c[1], c[2]);
+    const long long st[3] = {1, g.P, g.plane};
+#pragma unroll
+    for (int k = IDM0; k <= 3; k++)
+      cur[k - 1][off] = double(current(a, w + off, 0, st, c, k));
   }
 
   // addsource2 (src/vac.t:575-605): specialsource (uniform gravity,
@@ -866,6 +907,14 @@ inline long long ghost_count(const DevGrid& g) {
 
 template <class PH, int NDIM, int NDIR, bool MHD>
 __global__ void __launch_bounds__(128)
+    k_current_field(SweepArgs a, const typename PH::T* __restrict__ w,
+                    double* c0, double* c1, double* c2) {
+  double* cur[3] = {c0, c1, c2};
+  if (MHD) Sweep<PH, NDIM, NDIR, MHD>::current_field(a, w, cur);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
     k_predict(SweepArgs a, const typename PH::T* __restrict__ w,
               typename PH::T* __restrict__ w1) {
   Sweep<PH, NDIM, NDIR, MHD>::predict(a, w, w1);
@@ -1005,6 +1054,16 @@ struct Launch {
       case 8: k_ghost_face<T, 8><<<nb, 128, 0, st>>>(w, a.g, a.ph, a.ctrl, iB, fb, restore); break;
     }
   }
+  static void current_field(const SweepArgs& a, const T* w, double* const* cur,
+                            cudaStream_t st) {
+    long long n = 1;
+    for (int d = 0; d < 3; d++) n *= d < a.g.ndim ? a.g.nx[d] + 2 : 1;
+    const unsigned nb = grid_for(n, 128);
+#define KC(D, C, M) \
+  k_current_field<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, cur[0], cur[1], cur[2])
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
   static void fix_store(const SweepArgs& a, const T* w, T* fixb, cudaStream_t st) {
     const int nw = a.mhd ? 2 + 2 * a.ndir : 2 + a.ndir;
     long long off = 0;
@@ -1095,6 +1154,10 @@ struct Launch {
   void launch_fix_store_##SUF(const SweepArgs& s, const PH::T* w,            \
                               PH::T* fixb, cudaStream_t st) {                \
     Launch<PH>::fix_store(s, w, fixb, st);                                   \
+  }                                                                          \
+  void launch_current_field_##SUF(const SweepArgs& s, const PH::T* w,        \
+                                  double* const* cur, cudaStream_t st) {     \
+    Launch<PH>::current_field(s, w, cur, st);                                \
   }
 
 }  // namespace vacgpu

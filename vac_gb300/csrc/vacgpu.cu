@@ -144,7 +144,12 @@ struct vacgpu_handle {
   void* fixb;        // stored ghost values of fixed/fixed1/grad1 faces
   vacgpu_bound_fn bound_fn;  // specialbound hook
   void* bound_user;
-  bool hook_failed;  // the hook returned non-zero while a fill was issued
+  bool hook_failed;  // a hook returned non-zero while a step was issued
+  vacgpu_eta_fn eta_fn;  // specialeta hook (eqpar(eta_) < 0)
+  void* eta_user;
+  double* etaf;      // its eta field, gradeta (compactres) and the current
+  double* gradetaf[3];
+  double* curf[3];
   bool any_special;
   unsigned special[VACGPU_MAXB];  // per region: bit iw 'special'
   double* xg[3];     // cell centres over the ghost box (specialbound hooks)
@@ -348,12 +353,53 @@ SweepArgs make_args(vacgpu_handle* h, int d0, int d1) {
     a.a.dxf[d] = h->dxf[d];
   }
   a.ctrl = h->ctrl;
+  a.etaf = h->etaf;
+  for (int d = 0; d < 3; d++) a.gradetaf[d] = h->gradetaf[d];
   a.ndir = h->p.ndir;
   a.mhd = h->p.physics == VACGPU_PHYS_MHD;
   a.d0 = d0;
   a.d1 = d1;
   a.typelimited = h->p.typelimited;
   return a;
+}
+
+// specialeta before a resistive source evaluation on w (the source's wCT):
+// the current field, the hook, and the eta/dx^2 maxima of getdt_res
+// (first_only: the step-start call, which counts at it==itmin only).
+void eta_hook(vacgpu_handle* h, const SweepArgs& a, const void* w, int first_only) {
+  if (!h->etaf || !h->eta_fn) return;
+  const DevGrid& g = h->g;
+  kbegin(h, VACGPU_K_DT);
+  if (h->elem == 8)
+    launch_current_field_fp64(a, (const double*)w, h->curf, h->st);
+  else
+    launch_current_field_mixed(a, (const float*)w, h->curf, h->st);
+  vacgpu_eta_args e;
+  memset(&e, 0, sizeof(e));
+  vacgpu_region& r = e.box;
+  r.iB = -1;
+  for (int d = 0; d < 3; d++) {
+    r.lo[d] = d < g.ndim ? 1 : 0;
+    r.hi[d] = d < g.ndim ? g.nx[d] + 2 : 0;
+    r.nx[d] = g.nx[d];
+    r.nG[d] = g.nG[d];
+    r.x[d] = h->xg[d];
+  }
+  r.offset0 = g.xpad;
+  r.stride[0] = 1;
+  r.stride[1] = g.P;
+  r.stride[2] = g.plane;
+  r.var_stride = g.vs;
+  r.elem = (int)h->elem;
+  r.qt = &h->ctrl->t;
+  e.w = w;
+  for (int k = 0; k < 3; k++) e.current[k] = h->curf[k];
+  e.idirmin = 7 - 2 * h->p.ndir;
+  e.eta = h->etaf;
+  for (int k = 0; k < 3; k++) e.gradeta[k] = h->gradetaf[k];
+  if (h->eta_fn(h->eta_user, &e, (void*)h->st)) h->hook_failed = true;
+  launch_eta_max(a, first_only, h->st);
+  kend(h);
 }
 
 template <typename T>
@@ -387,6 +433,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   if (h->p.typefull == VACGPU_TVDLF1 || h->p.typefull == VACGPU_TVDMU1) {
     // typepred1='nul': onestep, the corrector alone with wCT = w
     // (src/vacio.t:286-299,511); no limiter, so the base is unused
+    if (h->p.sourceunsplit) eta_hook(h, a, w, 0);
     kbegin(h, VACGPU_K_CORRECT);
     if (sizeof(T) == 8 && roe)
       launch_correct_roe_fp64(a, (const double*)w, (const double*)w,
@@ -413,6 +460,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     fill_ghosts(h, a, wout, 1, 2);
     kend(h);
   } else if (sizeof(T) == 8) {
+    if (h->p.sourceunsplit) eta_hook(h, a, w, 0);
     kbegin(h, VACGPU_K_PREDICT);
     launch_predict_fp64(a, (const double*)w, (double*)w1, h->st);
     kend(h);
@@ -420,6 +468,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)w1, h->st);
     fill_ghosts(h, a, w1, 1, 1);
     kend(h);
+    if (h->p.sourceunsplit) eta_hook(h, a, w1, 0);
     kbegin(h, VACGPU_K_CORRECT);
     if (roe)
       launch_correct_roe_fp64(a, (const double*)wc, (const double*)w1,
@@ -445,6 +494,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     float* fo = (float*)wout;
     const float* fb = (const float*)base;
 #define MIXED_SWEEP(SUF)                                \
+  if (h->p.sourceunsplit) eta_hook(h, a, fw, 0);        \
   kbegin(h, VACGPU_K_PREDICT);                          \
   launch_predict_##SUF(a, fw, fw1, h->st);              \
   kend(h);                                              \
@@ -452,6 +502,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fw1, h->st); \
   fill_ghosts(h, a, fw1, 1, 1);                         \
   kend(h);                                              \
+  if (h->p.sourceunsplit) eta_hook(h, a, fw1, 0);       \
   kbegin(h, VACGPU_K_CORRECT);                          \
   if (roe)                                              \
     launch_correct_roe_mixed(a, fwc, fw1, fb, fo, h->st); \
@@ -501,6 +552,8 @@ void run_step(vacgpu_handle* h, int parity_odd) {
     launch_cell_cmax_mixed(a, (const float*)w, h->st);
     kend(h);
   }
+  // getdt_res with the specialeta field: eta from the state at it==itmin
+  eta_hook(h, a, w, 1);
   kbegin(h, VACGPU_K_CONTROL);
   launch_dt_end(h->ctrl, p, h->st);
   kend(h);
@@ -637,8 +690,8 @@ int check_params(const vacgpu_params* p) {
   for (int d = 0; d < p->ndim; d++)
     if (p->nx[d] < 2) return fail("nx must be >= 2 in every dimension");
   if (!(p->eqpar[0] > 0.0)) return fail("eqpar(gamma_) must be positive");
-  if (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] < 0.0)
-    return fail("eqpar(eta_)<0 needs the user's specialeta, not on this path");
+  if (p->physics == VACGPU_PHYS_MHD && p->eqpar[1] < 0.0 && p->useprimitive)
+    return fail("eqpar(eta_)<0 (specialeta) with useprimitive=T is not supported");
   if (p->typefull < VACGPU_TVDLF || p->typefull > VACGPU_TVDMU1)
     return fail("typefull must be tvdlf, tvdlf1, tvdmu or tvdmu1");
   const bool roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
@@ -888,6 +941,20 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     if (e == cudaSuccess) e = cudaMalloc(&h->dx[d], sizeof(double) * g.nG[d]);
     if (e == cudaSuccess) e = cudaMalloc(&h->dxf[d], sizeof(float) * g.nG[d]);
   }
+  if (e == cudaSuccess && p->physics == VACGPU_PHYS_MHD && p->eqpar[1] < 0.0) {
+    // specialeta: the field, gradeta for the compact form, the current
+    const size_t fb = sizeof(double) * g.vs;
+    e = cudaMalloc(&h->etaf, fb);
+    if (e == cudaSuccess) e = cudaMemset(h->etaf, 0, fb);
+    for (int k = 0; k < 3 && e == cudaSuccess; k++) {
+      e = cudaMalloc(&h->curf[k], fb);
+      if (e == cudaSuccess) e = cudaMemset(h->curf[k], 0, fb);
+      if (e == cudaSuccess && p->compactres) {
+        e = cudaMalloc(&h->gradetaf[k], fb);
+        if (e == cudaSuccess) e = cudaMemset(h->gradetaf[k], 0, fb);
+      }
+    }
+  }
   if (e == cudaSuccess)
     e = cudaMalloc(&h->stage, sizeof(double) * g.ncell * h->nw);
   if (e == cudaSuccess && ph.genbc) {
@@ -1038,9 +1105,10 @@ int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
       }
   h->volume = vol;
   // getdt_res (src/vacphys.mhdres.t:5-45): dtdiffpar*min(dx)^2/eta, a
-  // constant of the grid
+  // constant of the grid for a constant eta (the specialeta field's limit
+  // is formed on the device)
   h->dtdiff = BIGD;
-  if (h->ph.eta != 0.0) {
+  if (h->ph.eta > 0.0) {
     double m = h->hdx[0][2];
     for (int d = 0; d < nd; d++)
       for (int i = 0; i < g.nx[d]; i++)
@@ -1052,6 +1120,8 @@ int vacgpu_set_grid(vacgpu_handle* h, const double* x) {
   return 0;
 }
 
+static const char* NO_ETA =
+    "eqpar(eta_)<0 needs the user's specialeta (vacgpu_register_eta)";
 static const char* NO_SPECIAL =
     "Special boundary is not defined (typeB 'special' needs a hook: "
     "vacgpu_register_bound)";
@@ -1059,6 +1129,7 @@ static const char* NO_SPECIAL =
 int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   if (!h) return fail("null handle");
   if (h->any_special && !h->bound_fn) return fail(NO_SPECIAL);
+  if (h->etaf && !h->eta_fn) return fail(NO_ETA);
   h->hook_failed = false;
   const DevGrid& g = h->g;
   long long n = g.ncell * h->nw;
@@ -1135,6 +1206,7 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
     return fail("vacgpu_step before vacgpu_set_grid/vacgpu_upload");
   if (maxsteps < 0) return fail("maxsteps must be >= 0");
   if (h->any_special && !h->bound_fn) return fail(NO_SPECIAL);
+  if (h->etaf && !h->eta_fn) return fail(NO_ETA);
   if (h->tuning && maxsteps > 0 && !h->timing && tune_nzc(h)) return 1;
   const int nsw = h->p.dimsplit ? h->p.ndim : 1;
   const int start_cur = h->cur;
@@ -1153,7 +1225,7 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
       h->hook_failed = false;
       drop_graphs(h);
       CK(cudaStreamSynchronize(h->st));
-      return fail("the specialbound hook failed");
+      return fail("a user hook (specialbound or specialeta) failed");
     }
     int done = 0;
     CK(cudaMemcpyAsync(&done, &h->ctrl->done, sizeof(int),
@@ -1200,6 +1272,15 @@ int vacgpu_error_counts(vacgpu_handle* h, int* nerror) {
   CK(cudaMemcpyAsync(&c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   for (int i = 0; i < 4; i++) nerror[i] = c.nerror[i];
+  return 0;
+}
+
+int vacgpu_register_eta(vacgpu_handle* h, vacgpu_eta_fn fn, void* user) {
+  if (!h) return fail("null handle");
+  if (h->st) CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);
+  h->eta_fn = fn;
+  h->eta_user = user;
   return 0;
 }
 
@@ -1255,6 +1336,11 @@ void vacgpu_destroy(vacgpu_handle* h) {
   for (int i = 0; i < 3; i++) cudaFree(h->buf[i]);
   cudaFree(h->wold);
   cudaFree(h->fixb);
+  cudaFree(h->etaf);
+  for (int k = 0; k < 3; k++) {
+    cudaFree(h->curf[k]);
+    cudaFree(h->gradetaf[k]);
+  }
   for (int d = 0; d < 3; d++) {
     cudaFree(h->xg[d]);
     cudaFree(h->dx[d]);

@@ -125,6 +125,9 @@ struct Ctrl {
   double dtgrav;
   double dtdiff;      // resistive diffusion dt limit (BIG without resistivity)
   double qt;          // time of the current ghost fill (specialbound hooks)
+  // specialeta: max over the mesh of eta/dx_d^2 (ordered keys), of the
+  // last field the hook produced (the first step's: from the state)
+  unsigned long long etak[3];
   double tstop;
   double dtcourant[3];
   int it, itmin;
@@ -187,6 +190,10 @@ struct SweepArgs {
   DevPhys ph;
   DevArrays a;
   Ctrl* ctrl;
+  // specialeta field (eqpar(eta_) < 0): eta and, for the compact form,
+  // gradeta in the state's cell indexing; nullptr for a constant eta
+  const double* etaf;
+  const double* gradetaf[3];
   int ndir, mhd;
   int d0, d1;           // sweep dimensions (d0==d1 when split)
   int typelimited;
@@ -210,7 +217,9 @@ struct SweepArgs {
   void launch_ghost_face_##SUF(const SweepArgs& s, T* w, T* fixb,             \
                                int restore, int iB, cudaStream_t st);        \
   void launch_fix_store_##SUF(const SweepArgs& s, const T* w, T* fixb,        \
-                              cudaStream_t st);
+                              cudaStream_t st);                              \
+  void launch_current_field_##SUF(const SweepArgs& s, const T* w,            \
+                                  double* const* cur, cudaStream_t st);
 VACGPU_DECLARE_LAUNCHERS(fp64, double)
 VACGPU_DECLARE_LAUNCHERS(mixed, float)
 VACGPU_DECLARE_LAUNCHERS(mixedf64, float)
@@ -247,6 +256,8 @@ void launch_kp_end(Ctrl* c, cudaStream_t st);
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st);
 // qt of a ghost fill: mode 0 t, 1 t+dt/2, 2 t+dt (src/vac.t:54,567)
 void launch_set_qt(Ctrl* c, int mode, cudaStream_t st);
+// specialeta: Ctrl::etak from the field (first_only: at it==itmin only)
+void launch_eta_max(const SweepArgs& a, int first_only, cudaStream_t st);
 void launch_step_end(Ctrl* c, int ndim, cudaStream_t st);
 // Batched control: which = 0 dt_begin, 1 smallp, 2 dt_end, 3 step_end
 // (toggle = buffer swaps per step), 4 call_begin; one block per grid.

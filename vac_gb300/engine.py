@@ -56,6 +56,7 @@ def lib():
         L.vacgpu_error_counts.argtypes = [vp, ip]
         L.vacgpu_register_source.argtypes = [vp, C.c_int, dp, C.c_int]
         L.vacgpu_register_bound.argtypes = [vp, vp, vp]
+        L.vacgpu_register_eta.argtypes = [vp, vp, vp]
         L.vacgpu_destroy.argtypes = [vp]
         L.vacgpu_destroy.restype = None
         L.vacgpu_last_error.argtypes = [C.c_char_p, C.c_int]
@@ -111,9 +112,10 @@ class Engine:
     coordinates, ``w``: (nw, n1, ...) conservative state, both indexed like
     VAC's x(ix^D,idim) and w(ix^D,iw)."""
 
-    def __init__(self, params, x, w, it=0, t=0.0, bound=None):
+    def __init__(self, params, x, w, it=0, t=0.0, bound=None, eta=None):
         """bound: (function pointer, user pointer) of a vacgpu_bound_fn
-        specialbound hook, installed before the first ghost fill."""
+        specialbound hook, installed before the first ghost fill; eta:
+        likewise a vacgpu_eta_fn specialeta hook."""
         L = lib()
         self.p = params
         h = C.c_void_p()
@@ -123,6 +125,9 @@ class Engine:
             _ck(L.vacgpu_register_bound(self.h, C.c_void_p(bound[0]),
                                         C.c_void_p(bound[1])),
                 "vacgpu_register_bound")
+        if eta:
+            _ck(L.vacgpu_register_eta(self.h, C.c_void_p(eta[0]), C.c_void_p(eta[1])),
+                "vacgpu_register_eta")
         self.nw = params.nw
         self.nx = tuple(params.nx[d] for d in range(params.ndim))
         xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)
