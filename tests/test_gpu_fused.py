@@ -102,3 +102,53 @@ def test_z_chunk_tuning_is_invisible(monkeypatch):
     pinned.step(4)
     assert (tuned.it, tuned.t) == (pinned.it, pinned.t)
     assert np.array_equal(tuned.state().view(np.uint64), pinned.state().view(np.uint64))
+
+
+def test_full_size_conservation_and_symmetry():
+    """The benchmark's workload at its full size (256^3 random-mode MHD,
+    woodward, periodic, mixed, fused sweeps): without the Powell source the
+    flux form conserves mass, momentum, energy and B (volume sums, FP64,
+    relative to their scale); and a state mirrored in x evolves into the
+    mirror image (m_x and B_x change sign) to FP32 rounding."""
+    n = 256
+    s = inistate.random_modes(n, seed=0)
+    p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
+    p.divbfix = 0
+    e = Engine(p, s.x, s.w)
+    m0 = e.sums()
+    e.step(6)
+    m1 = e.sums()
+    scale = np.abs(s.w).reshape(s.w.shape[0], -1).mean(axis=1)
+    assert np.all(np.abs(m1 - m0) <= 2e-7 * np.maximum(scale, 1e-3)), (m1 - m0) / scale
+    a = e.state()
+    e.close()
+    # mirror x -> -x about the box centre: cell i <-> n-1-i
+    w = s.w[:, ::-1].copy()
+    w[1] = -w[1]
+    w[5] = -w[5]
+    em = Engine(p, s.x, w)
+    em.step(6)
+    b = em.state()[:, ::-1]
+    em.close()
+    b[1] = -b[1]
+    b[5] = -b[5]
+    rel = [float(np.abs(a[i] - b[i]).sum() / np.abs(a[i]).sum()) for i in range(a.shape[0])]
+    assert max(rel) <= 1e-5, rel
+
+
+def test_full_size_uniform_state_is_preserved_exactly():
+    """A uniform state at 256^3 stays bit for bit uniform: identical face
+    fluxes cancel exactly and div B is zero."""
+    n = 256
+    s = inistate.random_modes(n, seed=0)
+    w = s.w.copy()
+    for iw in range(w.shape[0]):
+        w[iw] = w[iw].mean()
+    p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
+    e = Engine(p, s.x, w)
+    e.step(4)
+    out = e.state()
+    e.close()
+    for iw in range(w.shape[0]):
+        assert np.all(out[iw] == out[iw].flat[0])
+        assert abs(out[iw].flat[0] - np.float32(w[iw].flat[0])) <= 1e-7 * abs(w[iw].flat[0]) + 1e-30
