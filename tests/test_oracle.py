@@ -333,3 +333,26 @@ def test_roe_entropy_fix_combinations_refused():
     p.typeentropy[2] = abi.ENTROPY_HARTEN
     with pytest.raises(RuntimeError, match="fastRW"):
         Oracle(p, s.x, s.w)
+
+
+@pytest.mark.parametrize("typefull", [abi.TVDLF, abi.TVDMU], ids=["tvdlf", "tvdmu"])
+def test_smooth_wave_converges_at_second_order(typefull):
+    """A density wave advected once across the periodic unit interval
+    (rho = 1 + 0.2 sin 2 pi x, v = 1, p = 1): the woodward-limited schemes
+    converge at second order in L1 (the limiter clips only at the
+    extrema)."""
+    errs = []
+    for n in (64, 128, 256):
+        x = inistate.domain_grid((n,), (0.0,), (1.0,))
+        rho = 1.0 + 0.2 * np.sin(2 * np.pi * x[0])
+        w = inistate.conserve_hd(rho, [np.ones_like(rho)], np.ones_like(rho), 1.4)
+        s = inistate._snap(x, w, 1.4, False, 1, "smooth density wave")
+        p = inistate.params_for(s, limiter="woodward", bc="periodic")
+        p.typefull = typefull
+        p.tmax, p.tmaxexact = 1.0, 1
+        o = Oracle(p, s.x, s.w)
+        o.step(10 ** 7)
+        assert abs(o.t - 1.0) < 1e-12
+        errs.append(np.abs(o.state()[0] - rho).mean())
+    orders = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(orders) >= 1.8, (errs, orders)
