@@ -15,6 +15,9 @@ using namespace vacgpu;
 // Scratch shared by every call on a device: the predictor state (8 FP64
 // variables x VACGPU_NOALLOC_MAX_GCELLS cells = 16 MiB) and one Ctrl block.
 static __device__ __align__(256) double g_na_w1[VACGPU_NOALLOC_MAX_GCELLS * VACGPU_MAXNW];
+// the corrector's face fluxes: at most (nx_d+1)*prod(nx_other) <= the
+// ghost-box cells per variable
+static __device__ __align__(256) double g_na_faces[VACGPU_NOALLOC_MAX_GCELLS * VACGPU_MAXNW];
 static __device__ __align__(256) Ctrl g_na_ctrl;
 
 namespace {
@@ -22,6 +25,7 @@ namespace {
 constexpr int MAXDEV = 64;
 struct NaAddr {
   double* w1;
+  double* faces;
   Ctrl* ctrl;
 };
 NaAddr g_addr[MAXDEV];
@@ -108,13 +112,16 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
       // set-up once per device, with that device current
       void* pw = nullptr;
       void* pc = nullptr;
+      void* pf = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&pw, g_na_w1);
       if (e == cudaSuccess) e = cudaGetSymbolAddress(&pc, g_na_ctrl);
+      if (e == cudaSuccess) e = cudaGetSymbolAddress(&pf, g_na_faces);
       if (e != cudaSuccess)
         return vacgpu_internal_fail(
             (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e))
                 .c_str());
       g_addr[dev].w1 = (double*)pw;
+      g_addr[dev].faces = (double*)pf;
       g_addr[dev].ctrl = (Ctrl*)pc;
       g_ready[dev] = true;
     }
@@ -162,6 +169,8 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
   s.mhd = p->physics == VACGPU_PHYS_MHD;
   s.d0 = s.d1 = idim;
   s.typelimited = p->typelimited;
+  s.faces = a.faces;
+  s.face_stride = (long long)p->nw * face_count(g, idim);
 
   cudaStream_t st = (cudaStream_t)stream;
   k_na_begin<<<1, NSLOT, 0, st>>>(a.ctrl, dt, p->smallp);

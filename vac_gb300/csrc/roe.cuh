@@ -4,12 +4,12 @@
 // Roe's characteristic dissipation, from the eight-wave MHD Roe solver
 // (src/vacphys.mhdroe.t) or the gamma-law HD one (src/vacphys.hdroe.t).
 //
-// One thread per mesh cell evaluates the Roe decomposition of both faces
-// of the cell in the sweep direction (the same per-face values the
-// neighbouring cells compute, bit for bit), then applies the updates in the
-// reference's order: the central fluxes of all variables (addflux with
-// qdt), then wave by wave the dissipative fluxes R(iw,il)*phi(il) scaled by
-// (dvolume(i)+dvolume(j))/4 (addflux with qdt=-1: += (F(i)-F(i-1))/dvolume).
+// A face pass evaluates each face once (one thread per face): the face
+// states, the central flux and the Roe decomposition, storing the central
+// flux and the dissipative fluxes R(iw,il)*phi(il)*(dvolume(i)+dvolume(j))/4
+// of every wave; a cell pass then applies them in the reference's order: the
+// central fluxes of all variables (addflux with qdt), then wave by wave the
+// dissipative ones (addflux with qdt=-1: += (F(i)-F(i-1))/dvolume).
 // The FP64 instance (roe_fp64.cu, built without FMA contraction) keeps every
 // array statement's operation order and is bit-identical to the CPU
 // restatement.  The mixed instance (roe_mixed.cu, IEEE FP32 division and
@@ -635,166 +635,183 @@ struct RoeSweep {
     return R(v);
   }
 
-  // wave il's dissipative fluxes of every variable into acc
-  template <int il, int iw>
-  static __device__ __forceinline__ void dissipate_var(
-      const SweepArgs& a, const Face& fm, const Face& fp, int d, R vm, R vp,
-      R dv0, int nofm, int nofp, R* acc) {
-    R rp = rtimes<iw, il>(a, fp, R(fp.phi[il]), d) * R(0.25) * vp;
-    R rm = rtimes<iw, il>(a, fm, R(fm.phi[il]), d) * R(0.25) * vm;
-    if ((nofp >> iw) & 1) rp = R(0);
-    if ((nofm >> iw) & 1) rm = R(0);
-    acc[iw] = acc[iw] + R((rp - rm) / dv0);
-  }
-  template <int il>
-  static __device__ __forceinline__ void dissipate(const SweepArgs& a,
-                                                   const Face& fm,
-                                                   const Face& fp, int d,
-                                                   R vm, R vp, R dv0, int nofm,
-                                                   int nofp, R* acc) {
-    dissipate_var<il, 0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate_var<il, 1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate_var<il, 2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 3) dissipate_var<il, (NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 4) dissipate_var<il, (NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 5) dissipate_var<il, (NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 6) dissipate_var<il, (NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 7) dissipate_var<il, (NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-  }
-
-  // The corrector of one direction d (a compile-time constant, so that the
-  // face states and Roe quantities stay in registers): both faces, the
-  // central fluxes, then wave by wave the dissipative fluxes.
-  template <int d>
-  static __device__ __forceinline__ void direction(
-      const SweepArgs& a, const T* __restrict__ w1, const T* __restrict__ base,
-      long long off, const long long* st, const int* c, R smallp,
-      double qsmallp, double qdt, bool limit, R dv0, R* acc,
-      unsigned long long* key) {
-    Face fm, fp;
-    R Fm[NW], Fp[NW];
-    D amm[2], amp[2];
-    face(a, w1, base, off - st[d], st[d], d, c[d] - 1, smallp, qsmallp,
-         qdt, limit, Fm, fm, amm);
-    face(a, w1, base, off, st[d], d, c[d], smallp, qsmallp, qdt, limit,
-         Fp, fp, amp);
-    if (a.ph.courantpar > 0.0) {
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        const unsigned long long km = dkey((double)amm[k]);
-        const unsigned long long kp = dkey((double)amp[k]);
-        key[k] = km > kp ? km : kp;
-      }
-    }
-    // 'symm0' faces: no flux of those variables through the mesh edge
-    // (setnoflux in addflux, also for the dissipative flux)
-    const int nofp = c[d] == a.g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
-    const int nofm = c[d] == 2 ? a.ph.noflux[d][0] : 0;
-#pragma unroll
-    for (int iw = 0; iw < NW; iw++) {
-      if ((nofp >> iw) & 1) Fp[iw] = R(0);
-      if ((nofm >> iw) & 1) Fm[iw] = R(0);
-    }
-    const R cq = PH::qdx(qdt, a.a, d, c[d]);
-#pragma unroll
-    for (int iw = 0; iw < NW; iw++)
-      acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
-    int cn[3] = {c[0], c[1], c[2]};
-    cn[d] = c[d] - 1;
-    const R dvm = dvol(a, cn);
-    cn[d] = c[d] + 1;
-    const R dvp = dvol(a, cn);
-    const R vm = dv0 + dvm;  // dvolume(j)+dvolume(i) of the lower face
-    const R vp = dvp + dv0;  // and of the upper face
-    dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-  }
-
-  // The corrector of one sweep (dimensions d0..d1) plus the CFL maxima of
-  // the fast waves (last substep).
-  template <int NT>
-  static __device__ void correct(const SweepArgs& a, const T* __restrict__ w,
-                                 const T* __restrict__ w1,
-                                 const T* __restrict__ base,
-                                 T* __restrict__ wout) {
+  // Face pass of direction d (a compile-time constant, so that the face
+  // state and the Roe quantities stay in registers): once per face, the
+  // central flux and, wave by wave, the dissipative fluxes
+  // R(iw,il)*phi(il)*(dvolume(i)+dvolume(j))/4, with setnoflux applied to
+  // both ('symm0' mesh faces), into buf[k*nf+f] (k = iw for the central
+  // flux, NW+il*NW+iw for the dissipative ones); plus the CFL maxima of
+  // the two fast waves.
+  template <int NT, int d>
+  static __device__ void face_pass(const SweepArgs& a, const T* __restrict__ w1,
+                                   const T* __restrict__ base,
+                                   R* __restrict__ buf) {
     __shared__ unsigned long long shk[NT / 32];
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) return;
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = n < a.g.ncell;
-    unsigned long long key[3][2] = {{0ULL, 0ULL}, {0ULL, 0ULL}, {0ULL, 0ULL}};
-    if (active) {
-      int c[3];
-      cell_coords(a.g, n, c);
-      const long long off = gidx(a.g, c[0], c[1], c[2]);
-      const long long st[3] = {1, a.g.P, a.g.plane};
-      const long long vs = a.g.vs;
-      const double qdt = ctrl->dt;
-      const R smallp = R(ctrl->smallp);
+    const DevGrid& g = a.g;
+    const long long nf = face_count(g, d);
+    const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long key[2] = {0ULL, 0ULL};
+    if (f < nf) {
+      int cl[3];
+      face_left_cell(g, d, f, cl);
+      const long long st[3] = {1, g.P, g.plane};
+      const long long o = gidx(g, cl[0], cl[1], cl[2]);
       const bool limit = a.ph.typefull != VACGPU_TVDMU1;
-      R acc[NW];
-#pragma unroll
-      for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
-      if (a.ph.useprim && limit) {
-        // the limiter base (the state) leaves upwindLR round-tripped
-        S::to_prim(a, smallp, acc);
-        S::to_cons(a, acc);
+      Face fs;
+      R F[NW];
+      D am[2];
+      face(a, w1, base, o, st[d], d, cl[d], R(ctrl->smallp), ctrl->smallp,
+           ctrl->dt, limit, F, fs, am);
+      if (a.ph.courantpar > 0.0) {
+        key[0] = dkey((double)am[0]);
+        key[1] = dkey((double)am[1]);
       }
-      const double qsmallp = ctrl->smallp;
-      const R dv0 = dvol(a, c);
-      for (int d = a.d0; d <= a.d1; d++) {
-        if (d == 0)
-          direction<0>(a, w1, base, off, st, c, smallp, qsmallp, qdt, limit,
-                       dv0, acc, key[0]);
-        else if (NDIM > 1 && d == 1)
-          direction<(NDIM > 1 ? 1 : 0)>(a, w1, base, off, st, c, smallp,
-                                        qsmallp, qdt, limit, dv0, acc, key[1]);
-        else if (NDIM > 2)
-          direction<(NDIM > 2 ? 2 : 0)>(a, w1, base, off, st, c, smallp,
-                                        qsmallp, qdt, limit, dv0, acc, key[2]);
-      }
-      if (a.ph.sourceunsplit) {
-        R wc[NW];
+      const int nof = cl[d] == 1 ? a.ph.noflux[d][0]
+                      : cl[d] == g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
 #pragma unroll
-        for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
-        S::add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off,
-                       st, c, acc);
-      }
-#pragma unroll
-      for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
+      for (int iw = 0; iw < NW; iw++)
+        buf[iw * nf + f] = ((nof >> iw) & 1) ? R(0) : F[iw];
+      // dvolume(j)+dvolume(i): the right and the left cell of the face
+      int cr[3] = {cl[0], cl[1], cl[2]};
+      cr[d] = cl[d] + 1;
+      const R vf = dvol(a, cr) + dvol(a, cl);
+      store_waves<0>(a, fs, d, vf, nof, nf, f, buf);
+      store_waves<1>(a, fs, d, vf, nof, nf, f, buf);
+      store_waves<2>(a, fs, d, vf, nof, nf, f, buf);
+      if (NW > 3) store_waves<(NW > 3 ? 3 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+      if (NW > 4) store_waves<(NW > 4 ? 4 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+      if (NW > 5) store_waves<(NW > 5 ? 5 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+      if (NW > 6) store_waves<(NW > 6 ? 6 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+      if (NW > 7) store_waves<(NW > 7 ? 7 : 0)>(a, fs, d, vf, nof, nf, f, buf);
     }
     if (a.ph.courantpar > 0.0) {
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        if (d < a.d0 || d > a.d1) continue;
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-          unsigned long long kk = block_max_key<NT>(key[d][k], shk);
-          if (threadIdx.x == 0 && kk) {
-            unsigned long long* slot =
-                k == 0 ? &ctrl->face_cmax[d][blockIdx.x % NSLOT]
-                       : &ctrl->face_cmax2[d][blockIdx.x % NSLOT];
-            atomic_max_key(slot, kk);
-          }
+      for (int k = 0; k < 2; k++) {
+        const unsigned long long kk = block_max_key<NT>(key[k], shk);
+        if (threadIdx.x == 0 && kk) {
+          unsigned long long* slot = k == 0 ? &ctrl->face_cmax[d][blockIdx.x % NSLOT]
+                                            : &ctrl->face_cmax2[d][blockIdx.x % NSLOT];
+          atomic_max_key(slot, kk);
         }
       }
     }
   }
+  // wave il's dissipative flux of variable iw at one face
+  template <int il, int iw>
+  static __device__ __forceinline__ void store_wave_var(const SweepArgs& a,
+                                                        const Face& fs, int d,
+                                                        R vf, int nof,
+                                                        long long nf,
+                                                        long long f, R* buf) {
+    R r = rtimes<iw, il>(a, fs, fs.phi[il], d) * R(0.25) * vf;
+    if ((nof >> iw) & 1) r = R(0);
+    buf[(long long)(NW + il * NW + iw) * nf + f] = r;
+  }
+  template <int il>
+  static __device__ __forceinline__ void store_waves(const SweepArgs& a,
+                                                     const Face& fs, int d,
+                                                     R vf, int nof, long long nf,
+                                                     long long f, R* buf) {
+    store_wave_var<il, 0>(a, fs, d, vf, nof, nf, f, buf);
+    store_wave_var<il, 1>(a, fs, d, vf, nof, nf, f, buf);
+    store_wave_var<il, 2>(a, fs, d, vf, nof, nf, f, buf);
+    if (NW > 3) store_wave_var<il, (NW > 3 ? 3 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+    if (NW > 4) store_wave_var<il, (NW > 4 ? 4 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+    if (NW > 5) store_wave_var<il, (NW > 5 ? 5 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+    if (NW > 6) store_wave_var<il, (NW > 6 ? 6 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+    if (NW > 7) store_wave_var<il, (NW > 7 ? 7 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+  }
+
+  // Cell pass: per direction the central fluxes of all variables
+  // (addflux with qdt), then wave by wave the dissipative fluxes (addflux
+  // with qdt=-1: += (F(i+1/2)-F(i-1/2))/dvolume), then the sources.
+  static __device__ void correct(const SweepArgs& a, const T* __restrict__ w,
+                                 const T* __restrict__ w1,
+                                 T* __restrict__ wout) {
+    const Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    const long long st[3] = {1, a.g.P, a.g.plane};
+    const long long vs = a.g.vs;
+    const double qdt = ctrl->dt;
+    const R smallp = R(ctrl->smallp);
+    R acc[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
+    if (a.ph.useprim && a.ph.typefull != VACGPU_TVDMU1) {
+      // the limiter base (the state) leaves upwindLR round-tripped
+      S::to_prim(a, smallp, acc);
+      S::to_cons(a, acc);
+    }
+    const R dv0 = dvol(a, c);
+    for (int d = a.d0; d <= a.d1; d++) {
+      const R* buf = (const R*)a.faces + (long long)(d - a.d0) * a.face_stride;
+      const long long nf = face_count(a.g, d);
+      int cm[3] = {c[0], c[1], c[2]};
+      cm[d] = c[d] - 1;
+      const long long fm = face_index(a.g, d, cm), fp = face_index(a.g, d, c);
+      const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++)
+        acc[iw] = acc[iw] - cq * (buf[iw * nf + fp] - buf[iw * nf + fm]);
+#pragma unroll
+      for (int il = 0; il < NW; il++)
+#pragma unroll
+        for (int iw = 0; iw < NW; iw++) {
+          const R* r = buf + (long long)(NW + il * NW + iw) * nf;
+          acc[iw] = acc[iw] + (r[fp] - r[fm]) / dv0;
+        }
+    }
+    if (a.ph.sourceunsplit) {
+      R wc[NW];
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
+      S::add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off, st,
+                     c, acc);
+    }
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
+  }
 };
+
+template <class PH, int NDIM, int NDIR, bool MHD, int D>
+__global__ void __launch_bounds__(128)
+    k_roe_face(SweepArgs a, const typename PH::T* __restrict__ w1,
+               const typename PH::T* __restrict__ base,
+               typename PH::R* __restrict__ buf) {
+  RoeSweep<PH, NDIM, NDIR, MHD>::template face_pass<128, D>(a, w1, base, buf);
+}
 
 template <class PH, int NDIM, int NDIR, bool MHD>
 __global__ void __launch_bounds__(128)
     k_correct_roe(SweepArgs a, const typename PH::T* __restrict__ w,
                   const typename PH::T* __restrict__ w1,
-                  const typename PH::T* __restrict__ base,
                   typename PH::T* __restrict__ wout) {
-  RoeSweep<PH, NDIM, NDIR, MHD>::template correct<128>(a, w, w1, base, wout);
+  RoeSweep<PH, NDIM, NDIR, MHD>::correct(a, w, w1, wout);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+void launch_roe_instance(const SweepArgs& a, const typename PH::T* w,
+                         const typename PH::T* w1, const typename PH::T* base,
+                         typename PH::T* wout, cudaStream_t st) {
+  for (int d = a.d0; d <= a.d1; d++) {
+    typename PH::R* buf =
+        (typename PH::R*)a.faces + (long long)(d - a.d0) * a.face_stride;
+    const unsigned nbf = grid_for(face_count(a.g, d), 128);
+    if (d == 0)
+      k_roe_face<PH, NDIM, NDIR, MHD, 0><<<nbf, 128, 0, st>>>(a, w1, base, buf);
+    else if (NDIM > 1 && d == 1)
+      k_roe_face<PH, NDIM, NDIR, MHD, (NDIM > 1 ? 1 : 0)><<<nbf, 128, 0, st>>>(a, w1, base, buf);
+    else if (NDIM > 2)
+      k_roe_face<PH, NDIM, NDIR, MHD, (NDIM > 2 ? 2 : 0)><<<nbf, 128, 0, st>>>(a, w1, base, buf);
+  }
+  k_correct_roe<PH, NDIM, NDIR, MHD><<<grid_for(a.g.ncell, 128), 128, 0, st>>>(a, w, w1, wout);
 }
 
 // (ndim, ndir, physics) instances; the MHD Roe solver needs ndir >= 2
@@ -803,9 +820,7 @@ template <class PH>
 void launch_correct_roe(const SweepArgs& a, const typename PH::T* w,
                         const typename PH::T* w1, const typename PH::T* base,
                         typename PH::T* wout, cudaStream_t st) {
-  const unsigned nb = grid_for(a.g.ncell, 128);
-#define KC(D, C, M) \
-  k_correct_roe<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1, base, wout)
+#define KC(D, C, M) launch_roe_instance<PH, D, C, M>(a, w, w1, base, wout, st)
   if (a.mhd) {
     if (a.g.ndim == 2 && a.ndir == 2) KC(2, 2, true);
     else if (a.g.ndim == 2 && a.ndir == 3) KC(2, 3, true);

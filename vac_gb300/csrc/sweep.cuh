@@ -457,77 +457,87 @@ struct Sweep {
     return cmax;
   }
 
-  // TVDLF corrector (src/vactvdlf.t:92-299) plus the CFL maximum of the last
-  // substep (src/vactvdlf.t:184-201).
+  // TVDLF corrector (src/vactvdlf.t:92-299), face pass: the numerical flux
+  // of every face of direction d, once per face, with setnoflux applied
+  // ('symm0' mesh faces carry no flux of their variables), into
+  // F[iw*nf+f]; plus the CFL maximum of the last substep
+  // (src/vactvdlf.t:184-201).
   template <int NT>
-  static __device__ void correct(const SweepArgs& a, const T* __restrict__ w,
-                                 const T* __restrict__ w1,
-                                 const T* __restrict__ base,
-                                 T* __restrict__ wout) {
+  static __device__ void face_pass(const SweepArgs& a, const T* __restrict__ w1,
+                                   const T* __restrict__ base, int d,
+                                   R* __restrict__ F) {
     __shared__ unsigned long long shk[NT / 32];
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) return;
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = n < a.g.ncell;
-    unsigned long long key[3] = {0ULL, 0ULL, 0ULL};
-    if (active) {
-      int c[3];
-      cell_coords(a.g, n, c);
-      const long long off = gidx(a.g, c[0], c[1], c[2]);
-      const long long st[3] = {1, a.g.P, a.g.plane};
-      const long long vs = a.g.vs;
-      const double qdt = ctrl->dt;
-      const R smallp = R(ctrl->smallp);
-      R acc[NW];
+    const DevGrid& g = a.g;
+    const long long nf = face_count(g, d);
+    const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long key = 0ULL;
+    if (f < nf) {
+      int cl[3];
+      face_left_cell(g, d, f, cl);
+      const long long st[3] = {1, g.P, g.plane};
+      const long long o = gidx(g, cl[0], cl[1], cl[2]);
+      R Ff[NW];
+      const R cm = face_flux(a, w1, base, o, st[d], d, R(ctrl->smallp), Ff);
+      if (a.ph.courantpar > 0.0) key = dkey(PH::cfl(cm, a.a, d, cl[d]));
+      const int nof = cl[d] == 1 ? a.ph.noflux[d][0]
+                      : cl[d] == g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
 #pragma unroll
-      for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
-      if (a.ph.useprim && a.ph.typefull != VACGPU_TVDLF1) {
-        // the limiter base (the state) leaves upwindLR round-tripped
-        to_prim(a, smallp, acc);
-        to_cons(a, acc);
-      }
-      for (int d = a.d0; d <= a.d1; d++) {
-        R Fm[NW], Fp[NW];
-        R cm = face_flux(a, w1, base, off - st[d], st[d], d, smallp, Fm);
-        R cp = face_flux(a, w1, base, off, st[d], d, smallp, Fp);
-        if (a.ph.courantpar > 0.0) {
-          double qm = PH::cfl(cm, a.a, d, c[d] - 1);
-          double qp = PH::cfl(cp, a.a, d, c[d]);
-          unsigned long long km = dkey(qm), kp = dkey(qp);
-          key[d] = km > kp ? km : kp;
-        }
-        if (c[d] == a.g.nx[d] + 1 && a.ph.noflux[d][1]) {  // 'symm0'
-#pragma unroll
-          for (int iw = 0; iw < NW; iw++)
-            if ((a.ph.noflux[d][1] >> iw) & 1) Fp[iw] = R(0);
-        }
-        if (c[d] == 2 && a.ph.noflux[d][0]) {
-#pragma unroll
-          for (int iw = 0; iw < NW; iw++)
-            if ((a.ph.noflux[d][0] >> iw) & 1) Fm[iw] = R(0);
-        }
-        const R cq = PH::qdx(qdt, a.a, d, c[d]);
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++)
-          acc[iw] = acc[iw] - cq * (Fp[iw] - Fm[iw]);
-      }
-      if (a.ph.sourceunsplit) {
-        R wc[NW];
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
-        add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off, st,
-                    c, acc);
-      }
-#pragma unroll
-      for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
+      for (int iw = 0; iw < NW; iw++)
+        F[iw * nf + f] = ((nof >> iw) & 1) ? R(0) : Ff[iw];
     }
     if (a.ph.courantpar > 0.0) {
-      for (int d = a.d0; d <= a.d1; d++) {
-        unsigned long long k = block_max_key<NT>(key[d], shk);
-        if (threadIdx.x == 0 && k)
-          atomic_max_key(&ctrl->face_cmax[d][blockIdx.x % NSLOT], k);
-      }
+      const unsigned long long k = block_max_key<NT>(key, shk);
+      if (threadIdx.x == 0 && k)
+        atomic_max_key(&ctrl->face_cmax[d][blockIdx.x % NSLOT], k);
     }
+  }
+
+  // TVDLF corrector, cell pass: wnew = w - dt/dx (F(i+1/2) - F(i-1/2)) per
+  // direction, then the unsplit sources (src/vactvdlf.t:250-296).
+  static __device__ void correct(const SweepArgs& a, const T* __restrict__ w,
+                                 const T* __restrict__ w1,
+                                 T* __restrict__ wout) {
+    const Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    const long long st[3] = {1, a.g.P, a.g.plane};
+    const long long vs = a.g.vs;
+    const double qdt = ctrl->dt;
+    const R smallp = R(ctrl->smallp);
+    R acc[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) acc[iw] = R(w[off + iw * vs]);
+    if (a.ph.useprim && a.ph.typefull != VACGPU_TVDLF1) {
+      // the limiter base (the state) leaves upwindLR round-tripped
+      to_prim(a, smallp, acc);
+      to_cons(a, acc);
+    }
+    for (int d = a.d0; d <= a.d1; d++) {
+      const R* F = (const R*)a.faces + (long long)(d - a.d0) * a.face_stride;
+      const long long nf = face_count(a.g, d);
+      int cm[3] = {c[0], c[1], c[2]};
+      cm[d] = c[d] - 1;
+      const long long fm = face_index(a.g, d, cm), fp = face_index(a.g, d, c);
+      const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++)
+        acc[iw] = acc[iw] - cq * (F[iw * nf + fp] - F[iw * nf + fm]);
+    }
+    if (a.ph.sourceunsplit) {
+      R wc[NW];
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
+      add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off, st, c,
+                  acc);
+    }
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
   }
 
   // getpthermal's one-time smallp: min/max of the unclipped pressure on the
@@ -922,11 +932,18 @@ __global__ void __launch_bounds__(128)
 
 template <class PH, int NDIM, int NDIR, bool MHD>
 __global__ void __launch_bounds__(128)
+    k_face(SweepArgs a, const typename PH::T* __restrict__ w1,
+           const typename PH::T* __restrict__ base, int d,
+           typename PH::R* __restrict__ F) {
+  Sweep<PH, NDIM, NDIR, MHD>::template face_pass<128>(a, w1, base, d, F);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
     k_correct(SweepArgs a, const typename PH::T* __restrict__ w,
               const typename PH::T* __restrict__ w1,
-              const typename PH::T* __restrict__ base,
               typename PH::T* __restrict__ wout) {
-  Sweep<PH, NDIM, NDIR, MHD>::template correct<128>(a, w, w1, base, wout);
+  Sweep<PH, NDIM, NDIR, MHD>::correct(a, w, w1, wout);
 }
 
 template <class PH, int NDIM, int NDIR, bool MHD>
@@ -998,11 +1015,19 @@ struct Launch {
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }
+  // face pass per direction into the face buffer, then the cell pass
   static void correct(const SweepArgs& a, const T* w, const T* w1,
                       const T* base, T* wout, cudaStream_t st) {
-    unsigned nb = grid_for(a.g.ncell, 128);
+    for (int d = a.d0; d <= a.d1; d++) {
+      typename PH::R* F = (typename PH::R*)a.faces + (long long)(d - a.d0) * a.face_stride;
+      const unsigned nbf = grid_for(face_count(a.g, d), 128);
 #define KC(D, C, M) \
-  k_correct<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1, base, wout)
+  k_face<PH, D, C, M><<<nbf, 128, 0, st>>>(a, w1, base, d, F)
+      VACGPU_DISPATCH(a, KC);
+#undef KC
+    }
+    const unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) k_correct<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1, wout)
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }

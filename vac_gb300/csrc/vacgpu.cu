@@ -150,6 +150,8 @@ struct vacgpu_handle {
   double* etaf;      // its eta field, gradeta (compactres) and the current
   double* gradetaf[3];
   double* curf[3];
+  void* faces;       // the split correctors' face buffer
+  long long face_stride;
   bool any_special;
   unsigned special[VACGPU_MAXB];  // per region: bit iw 'special'
   double* xg[3];     // cell centres over the ghost box (specialbound hooks)
@@ -355,6 +357,8 @@ SweepArgs make_args(vacgpu_handle* h, int d0, int d1) {
   a.ctrl = h->ctrl;
   a.etaf = h->etaf;
   for (int d = 0; d < 3; d++) a.gradetaf[d] = h->gradetaf[d];
+  a.faces = h->faces;
+  a.face_stride = h->face_stride;
   a.ndir = h->p.ndir;
   a.mhd = h->p.physics == VACGPU_PHYS_MHD;
   a.d0 = d0;
@@ -802,6 +806,19 @@ size_t vacgpu_internal_device_bytes(const vacgpu_params* p) {
   const long long P = ((align - 2 + nG[0] + align - 1) / align) * align;
   const size_t vs = (size_t)P * nG[1] * nG[2];
   size_t b = 3 * elem * vs * p->nw + 8 * (size_t)ncell * p->nw;
+  {
+    // the split correctors' face buffer (the fused mixed sweep needs none;
+    // counted regardless)
+    const bool roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
+    long long mf = 0;
+    for (int d = 0; d < p->ndim; d++) {
+      long long f = 1;
+      for (int k = 0; k < 3; k++) f *= (k < p->ndim ? p->nx[k] : 1) + (k == d ? 1 : 0);
+      if (f > mf) mf = f;
+    }
+    b += elem * (size_t)mf * (roe ? p->nw * (p->nw + 1) : p->nw) *
+         (p->dimsplit ? 1 : p->ndim);
+  }
   b += 8 * ((ncell + 255) / 256) * p->nw + sizeof(Ctrl) + 64 * 1024;
   return b;
 }
@@ -1012,6 +1029,21 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
     if (!ok) {
       vacgpu_destroy(h);
       return fail("TMA descriptor set-up failed");
+    }
+  }
+  if (h->elem == 8 || !h->fused || h->pmode != 0) {
+    // split corrector: per sweep direction the faces' fluxes (and, for the
+    // Roe dissipation, R(iw,il)*phi(il) of every wave)
+    const bool roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
+    const long long K = roe ? (long long)h->nw * (h->nw + 1) : h->nw;
+    long long mf = 0;
+    for (int d = 0; d < p->ndim; d++)
+      if (face_count(g, d) > mf) mf = face_count(g, d);
+    h->face_stride = K * mf;
+    const int nsw = p->dimsplit ? 1 : p->ndim;
+    if (cudaMalloc(&h->faces, h->elem * (size_t)h->face_stride * nsw) != cudaSuccess) {
+      vacgpu_destroy(h);
+      return fail("device allocation of the corrector's face buffer failed");
     }
   }
   Ctrl c;
@@ -1336,6 +1368,7 @@ void vacgpu_destroy(vacgpu_handle* h) {
   for (int i = 0; i < 3; i++) cudaFree(h->buf[i]);
   cudaFree(h->wold);
   cudaFree(h->fixb);
+  cudaFree(h->faces);
   cudaFree(h->etaf);
   for (int k = 0; k < 3; k++) {
     cudaFree(h->curf[k]);

@@ -153,6 +153,35 @@ struct Ctrl {
   unsigned long long rmin[NSLOT];          // keeppositive_rho min(rho)
 };
 
+// Faces of direction d: the nx_d+1 faces of each mesh line; the face with
+// left cell (ghost-box coordinates) cl has index ((i2*e1)+i1)*e0+i0 with
+// i_d = cl_d-1, i_k = cl_k-gh_k otherwise, e_d = nx_d+1, e_k = nx_k.
+__host__ __device__ inline long long face_count(const DevGrid& g, int d) {
+  long long n = 1;
+  for (int k = 0; k < 3; k++) n *= g.nx[k] + (k == d ? 1 : 0);
+  return n;
+}
+__host__ __device__ inline long long face_index(const DevGrid& g, int d,
+                                                const int* cl) {
+  long long idx = 0;
+  for (int k = 2; k >= 0; k--) {
+    const int e = g.nx[k] + (k == d ? 1 : 0);
+    const int i = k == d ? cl[k] - 1 : cl[k] - g.gh[k];
+    idx = idx * e + i;
+  }
+  return idx;
+}
+// Left cell of face f of direction d.
+__host__ __device__ inline void face_left_cell(const DevGrid& g, int d,
+                                               long long f, int* cl) {
+  for (int k = 0; k < 3; k++) {
+    const int e = g.nx[k] + (k == d ? 1 : 0);
+    const int i = (int)(f % e);
+    f /= e;
+    cl[k] = k == d ? i + 1 : i + g.gh[k];
+  }
+}
+
 // Order-preserving map of a double onto unsigned 64-bit integers.
 __host__ __device__ inline unsigned long long dkey(double v) {
   long long b;
@@ -194,6 +223,12 @@ struct SweepArgs {
   // gradeta in the state's cell indexing; nullptr for a constant eta
   const double* etaf;
   const double* gradetaf[3];
+  // corrector face buffer (the path's arithmetic type): per sweep
+  // direction d0..d1 a block of face_stride elements holding, for every
+  // face of the direction, its numerical flux (and the Roe dissipative
+  // fluxes) variable-major
+  void* faces;
+  long long face_stride;
   int ndir, mhd;
   int d0, d1;           // sweep dimensions (d0==d1 when split)
   int typelimited;
