@@ -673,18 +673,25 @@ struct RoeSweep {
 #pragma unroll
       for (int iw = 0; iw < NW; iw++)
         buf[iw * nf + f] = ((nof >> iw) & 1) ? R(0) : F[iw];
-      // dvolume(j)+dvolume(i): the right and the left cell of the face
-      int cr[3] = {cl[0], cl[1], cl[2]};
-      cr[d] = cl[d] + 1;
-      const R vf = dvol(a, cr) + dvol(a, cl);
-      store_waves<0>(a, fs, d, vf, nof, nf, f, buf);
-      store_waves<1>(a, fs, d, vf, nof, nf, f, buf);
-      store_waves<2>(a, fs, d, vf, nof, nf, f, buf);
-      if (NW > 3) store_waves<(NW > 3 ? 3 : 0)>(a, fs, d, vf, nof, nf, f, buf);
-      if (NW > 4) store_waves<(NW > 4 ? 4 : 0)>(a, fs, d, vf, nof, nf, f, buf);
-      if (NW > 5) store_waves<(NW > 5 ? 5 : 0)>(a, fs, d, vf, nof, nf, f, buf);
-      if (NW > 6) store_waves<(NW > 6 ? 6 : 0)>(a, fs, d, vf, nof, nf, f, buf);
-      if (NW > 7) store_waves<(NW > 7 ? 7 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+      if constexpr (sizeof(R) == 4) {
+        // mixed path: the limiter functions and the Roe state the right
+        // eigenvectors need; the cell pass forms R(iw,il)*phi(il)
+        store_face(fs, nf, f, buf);
+      } else {
+        // FP64 path: the dissipative fluxes themselves (their right
+        // eigenvectors take double divisions the cell pass need not repeat)
+        int cr[3] = {cl[0], cl[1], cl[2]};
+        cr[d] = cl[d] + 1;
+        const R vf = dvol(a, cr) + dvol(a, cl);  // dvolume(j)+dvolume(i)
+        store_waves<0>(a, fs, d, vf, nof, nf, f, buf);
+        store_waves<1>(a, fs, d, vf, nof, nf, f, buf);
+        store_waves<2>(a, fs, d, vf, nof, nf, f, buf);
+        if (NW > 3) store_waves<(NW > 3 ? 3 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+        if (NW > 4) store_waves<(NW > 4 ? 4 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+        if (NW > 5) store_waves<(NW > 5 ? 5 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+        if (NW > 6) store_waves<(NW > 6 ? 6 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+        if (NW > 7) store_waves<(NW > 7 ? 7 : 0)>(a, fs, d, vf, nof, nf, f, buf);
+      }
     }
     if (a.ph.courantpar > 0.0) {
 #pragma unroll
@@ -724,6 +731,110 @@ struct RoeSweep {
     if (NW > 7) store_wave_var<il, (NW > 7 ? 7 : 0)>(a, fs, d, vf, nof, nf, f, buf);
   }
 
+  // The mixed path's face record after the central flux: phi of every wave
+  // and the Roe state of rtimes (MHD: v, b, sr, cf, cs, af, as, cs2; HD:
+  // v, h, cs), at buf[(NW+k)*nf+f].
+  static constexpr int NFF = MHD ? 2 * NDIR + 6 : NDIR + 2;
+  static __device__ __forceinline__ void store_face(const Face& fs, long long nf,
+                                                    long long f, R* buf) {
+    R* b = buf + (long long)NW * nf + f;
+    int k = 0;
+#pragma unroll
+    for (int il = 0; il < NW; il++) b[(k++) * nf] = fs.phi[il];
+#pragma unroll
+    for (int c = 0; c < NDIR; c++) b[(k++) * nf] = fs.v[c];
+    if (MHD) {
+#pragma unroll
+      for (int c = 0; c < NDIR; c++) b[(k++) * nf] = fs.b[c];
+      b[(k++) * nf] = fs.sr;
+      b[(k++) * nf] = fs.cf;
+      b[(k++) * nf] = fs.cs;
+      b[(k++) * nf] = fs.af;
+      b[(k++) * nf] = fs.as;
+      b[(k++) * nf] = fs.cs2;
+    } else {
+      b[(k++) * nf] = fs.h;
+      b[(k++) * nf] = fs.cs;
+    }
+  }
+  static __device__ __forceinline__ void load_face(const R* buf, long long nf,
+                                                   long long f, Face& fs) {
+    const R* b = buf + (long long)NW * nf + f;
+    int k = 0;
+#pragma unroll
+    for (int il = 0; il < NW; il++) fs.phi[il] = b[(k++) * nf];
+#pragma unroll
+    for (int c = 0; c < NDIR; c++) fs.v[c] = b[(k++) * nf];
+    if (MHD) {
+#pragma unroll
+      for (int c = 0; c < NDIR; c++) fs.b[c] = b[(k++) * nf];
+      fs.sr = b[(k++) * nf];
+      fs.cf = b[(k++) * nf];
+      fs.cs = b[(k++) * nf];
+      fs.af = b[(k++) * nf];
+      fs.as = b[(k++) * nf];
+      fs.cs2 = b[(k++) * nf];
+    } else {
+      fs.h = b[(k++) * nf];
+      fs.cs = b[(k++) * nf];
+    }
+  }
+  // wave il's dissipative fluxes of every variable from the two faces' records
+  template <int il, int iw>
+  static __device__ __forceinline__ void dissipate_var(
+      const SweepArgs& a, const Face& fm, const Face& fp, int d, R vm, R vp,
+      R dv0, int nofm, int nofp, R* acc) {
+    R rp = rtimes<iw, il>(a, fp, fp.phi[il], d) * R(0.25) * vp;
+    R rm = rtimes<iw, il>(a, fm, fm.phi[il], d) * R(0.25) * vm;
+    if ((nofp >> iw) & 1) rp = R(0);
+    if ((nofm >> iw) & 1) rm = R(0);
+    acc[iw] = acc[iw] + (rp - rm) / dv0;
+  }
+  template <int il>
+  static __device__ __forceinline__ void dissipate(const SweepArgs& a,
+                                                   const Face& fm,
+                                                   const Face& fp, int d,
+                                                   R vm, R vp, R dv0, int nofm,
+                                                   int nofp, R* acc) {
+    dissipate_var<il, 0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate_var<il, 1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate_var<il, 2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 3) dissipate_var<il, (NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 4) dissipate_var<il, (NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 5) dissipate_var<il, (NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 6) dissipate_var<il, (NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 7) dissipate_var<il, (NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+  }
+  // one direction of the mixed path's cell pass (compile-time d keeps the
+  // two face records in registers)
+  template <int d>
+  static __device__ __forceinline__ void dissipate_dir(const SweepArgs& a,
+                                                       const R* buf,
+                                                       long long nf,
+                                                       long long fm_i,
+                                                       long long fp_i,
+                                                       const int* c, R dv0,
+                                                       R* acc) {
+    Face fm, fp;
+    load_face(buf, nf, fm_i, fm);
+    load_face(buf, nf, fp_i, fp);
+    int cn[3] = {c[0], c[1], c[2]};
+    cn[d] = c[d] - 1;
+    const R vm = dv0 + dvol(a, cn);  // dvolume(j)+dvolume(i), lower face
+    cn[d] = c[d] + 1;
+    const R vp = dvol(a, cn) + dv0;  // and upper face
+    const int nofp = c[d] == a.g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
+    const int nofm = c[d] == 2 ? a.ph.noflux[d][0] : 0;
+    dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+  }
+
   // Cell pass: per direction the central fluxes of all variables
   // (addflux with qdt), then wave by wave the dissipative fluxes (addflux
   // with qdt=-1: += (F(i+1/2)-F(i-1/2))/dvolume), then the sources.
@@ -760,13 +871,22 @@ struct RoeSweep {
 #pragma unroll
       for (int iw = 0; iw < NW; iw++)
         acc[iw] = acc[iw] - cq * (buf[iw * nf + fp] - buf[iw * nf + fm]);
+      if constexpr (sizeof(R) == 4) {
+        if (d == 0)
+          dissipate_dir<0>(a, buf, nf, fm, fp, c, dv0, acc);
+        else if (NDIM > 1 && d == 1)
+          dissipate_dir<(NDIM > 1 ? 1 : 0)>(a, buf, nf, fm, fp, c, dv0, acc);
+        else if (NDIM > 2)
+          dissipate_dir<(NDIM > 2 ? 2 : 0)>(a, buf, nf, fm, fp, c, dv0, acc);
+      } else {
 #pragma unroll
-      for (int il = 0; il < NW; il++)
+        for (int il = 0; il < NW; il++)
 #pragma unroll
-        for (int iw = 0; iw < NW; iw++) {
-          const R* r = buf + (long long)(NW + il * NW + iw) * nf;
-          acc[iw] = acc[iw] + (r[fp] - r[fm]) / dv0;
-        }
+          for (int iw = 0; iw < NW; iw++) {
+            const R* r = buf + (long long)(NW + il * NW + iw) * nf;
+            acc[iw] = acc[iw] + (r[fp] - r[fm]) / dv0;
+          }
+      }
     }
     if (a.ph.sourceunsplit) {
       R wc[NW];
