@@ -373,8 +373,9 @@ void vacgpu_server_destroy(vacgpu_server* s);
 
 /* Largest grid vacgpu_sweep_noalloc accepts, in cells including the ghost
  * layers (prod over the used dimensions of nx+4): 262144 cells, e.g. 508^2
- * in 2-D or 60^3 in 3-D.  Its scratch is a fixed 16 MiB FP64 device array
- * (8 variables) that every GPU which loads the library holds until exit. */
+ * in 2-D or 60^3 in 3-D.  Its scratch is two fixed 16 MiB FP64 device
+ * arrays (8 variables: the predictor state and the corrector's face fluxes)
+ * that every GPU which loads the library holds until exit. */
 #define VACGPU_NOALLOC_MAX_GCELLS 262144
 
 /* One dimensional sweep of the split twostep scheme in FP64 -- the Hancock
