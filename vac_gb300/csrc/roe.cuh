@@ -84,7 +84,7 @@ struct RoeSweep {
   template <int il>
   static __device__ __forceinline__ void wave(const SweepArgs& a, const R* wL,
                                               const R* wR, int d, double smallp,
-                                              D qdt, D dxs, const R* bd,
+                                              D qdt, R dxs, const R* bd,
                                               Face& f, D* am) {
     const R rL = wL[0], rR = wR[0];
     const R v = f.v[d];
@@ -226,9 +226,9 @@ struct RoeSweep {
       }
     }
     // normalisation by dt*2/(dx(i)+dx(j)) (src/vactvd.t:131-140)
-    const R adt = aa * R(qdt) * R(2) / R(dxs);
+    const R adt = aa * R(qdt) * R(2) / dxs;
     if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL)
-      smalla = smalla * R(qdt) * R(2) / R(dxs);
+      smalla = smalla * R(qdt) * R(2) / dxs;
     if (il < 2) am[il] = fabs(adt);
     if (te == VACGPU_ENTROPY_NUL || te == VACGPU_ENTROPY_RATIO ||
         fabs(adt) >= smalla)
@@ -353,7 +353,7 @@ struct RoeSweep {
   static __device__ __forceinline__ void decompose(const SweepArgs& a,
                                                    const R* wL, const R* wR,
                                                    int d, double smallp, D qdt,
-                                                   D dxs, Face& f, D* am) {
+                                                   R dxs, Face& f, D* am) {
     // FP64 path: the reference's statements in double.  Mixed path: the
     // MHD average in FP32 with cancellation-free forms (average_mhd_f32),
     // the HD average in double.
@@ -623,16 +623,16 @@ struct RoeSweep {
     PH::template flux<NDIR, MHD>(wR, d, a.ph, smallp, fR);
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) F[iw] = R(0.5) * (fL[iw] + fR[iw]);
-    const D dxs = a.a.dx[d][ci] + a.a.dx[d][ci + 1];
+    const R dxs = PH::dx(a.a, d, ci) + PH::dx(a.a, d, ci + 1);
     decompose(a, wL, wR, d, qsmallp, qdt, dxs, f, am);
   }
 
   // dvolume(ix) = dx_1*dx_2*dx_3 (gridsetup1, src/vacgrid.t:573-576)
   static __device__ __forceinline__ R dvol(const SweepArgs& a, const int* c) {
-    double v = a.a.dx[0][c[0]];
-    if (NDIM > 1) v = v * a.a.dx[1][c[1]];
-    if (NDIM > 2) v = v * a.a.dx[2][c[2]];
-    return R(v);
+    R v = PH::dx(a.a, 0, c[0]);
+    if (NDIM > 1) v = v * PH::dx(a.a, 1, c[1]);
+    if (NDIM > 2) v = v * PH::dx(a.a, 2, c[2]);
+    return v;
   }
 
   // Face pass of direction d (a compile-time constant, so that the face
