@@ -113,7 +113,7 @@ void finish(vacgpu_server* s, Req* r, bool ok, const std::string& err) {
   s->cv.notify_all();
 }
 
-bool admit_one(vacgpu_server* s, Req* r) {
+bool admit_one(Req* r) {
   char buf[512];
   if (vacgpu_create(&r->p, &r->h) || vacgpu_set_grid(r->h, r->x.data()) ||
       vacgpu_upload(r->h, r->w.data(), 0, 0.0)) {
@@ -152,7 +152,7 @@ void worker_loop(vacgpu_server* s) {
       }
     }
     for (Req* r : admit) {
-      if (!admit_one(s, r)) {
+      if (!admit_one(r)) {
         finish(s, r, false, r->err);
         continue;
       }
