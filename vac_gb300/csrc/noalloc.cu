@@ -149,6 +149,7 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
   ph.gm1 = p->eqpar[0] - 1.0;
   ph.gammaf = (float)ph.gamma;
   ph.gm1f = (float)ph.gm1;
+  ph.c2gf = (2.0f - ph.gammaf) / ph.gm1f;
   ph.pt3 = 0.5 * (p->eqpar[0] - 1.0);
   ph.smallpcoeff = p->smallpcoeff;
   ph.courantpar = courantmax ? 1.0 : -1.0;

@@ -48,6 +48,10 @@ struct RoeSweep {
     R dp, rhodv; // MHD: pR-pL (conservative form), rho*dv_idim
                  // HD: (pR-pL)/c^2, (vR-vL)_idim/c
     R phi[NW];   // getphi's TVD-MUSCL phi = |a*dt/dx|*jump (entropy fixed)
+    // mixed cell pass only (prep_face): SIGN(1,B_idim), sqrt(cs2)/sr,
+    // 1/SIGN(sr,B_idim), v^2 and v^2/2+(2-gamma)/(gamma-1)*cs2, formed once
+    // per face instead of in each of rtimes' products
+    R sgn, csr, isrs, vv, v2a2;
   };
 
   // Fortran SIGN(a,b), MAX and MIN as the oracle's selects
@@ -502,16 +506,25 @@ struct RoeSweep {
         return R(0);
       }
       if (iw == E) {
-        R vv = f.v[0] * f.v[0];
+        R vv, v2a2;
+        if constexpr (sizeof(R) == 4) {
+          vv = f.vv;
+          v2a2 = f.v2a2;
+        } else {
+          vv = f.v[0] * f.v[0];
 #pragma unroll
-        for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
-        const R g = R(a.ph.gamma);
-        const R v2a2 = R(0.5) * vv + (R(2) - g) / R(a.ph.gm1) * f.cs2;
+          for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
+          const R g = R(a.ph.gamma);
+          v2a2 = R(0.5) * vv + (R(2) - g) / R(a.ph.gm1) * f.cs2;
+        }
         R bv;
         if (il < 6) {
           bv = f.b[I] * f.v[I];
           if (NDIR == 3) bv = bv + f.b[J] * f.v[J];
-          bv = bv * R(fsign(1.0, f.b[d]));
+          if constexpr (sizeof(R) == 4)
+            bv = bv * f.sgn;
+          else
+            bv = bv * R(fsign(1.0, f.b[d]));
         } else {
           bv = f.b[J] * f.v[I] - f.b[I] * f.v[J];
         }
@@ -548,7 +561,11 @@ struct RoeSweep {
           }
         }
         const R bw = f.b[c];
-        const R sg = R(fsign(1.0, f.b[d]));
+        R sg;
+        if constexpr (sizeof(R) == 4)
+          sg = f.sgn;
+        else
+          sg = R(fsign(1.0, f.b[d]));
         switch (il) {
           case 0: return q * (f.af * vw - f.as * f.cs * bw * sg);
           case 1: return q * (f.af * vw + f.as * f.cs * bw * sg);
@@ -563,6 +580,22 @@ struct RoeSweep {
       const int c = iw - B0 - 1;
       if (c == d) return (il == 5 && a.ph.divbwave) ? q : R(0);
       const R bw = f.b[c];
+      if constexpr (sizeof(R) == 4) {
+        switch (il) {
+          case 0:
+          case 1:
+            return +q * f.as * (f.csr * bw);
+          case 2:
+          case 3:
+            return -q * f.af * (f.csr * bw);
+          case 4:
+          case 5:
+            return R(0);
+          default:
+            if (c == I) return -q * f.b[J] * f.isrs;
+            return +q * f.b[I] * f.isrs;
+        }
+      }
       switch (il) {
         case 0:
         case 1:
@@ -780,30 +813,47 @@ struct RoeSweep {
     }
   }
   // wave il's dissipative fluxes of every variable from the two faces' records
+  // (the mixed path: the face's scale 0.25*(dvolume_i+dvolume_j)/dvolume
+  // multiplies instead of one division per wave and variable)
   template <int il, int iw>
   static __device__ __forceinline__ void dissipate_var(
-      const SweepArgs& a, const Face& fm, const Face& fp, int d, R vm, R vp,
-      R dv0, int nofm, int nofp, R* acc) {
-    R rp = rtimes<iw, il>(a, fp, fp.phi[il], d) * R(0.25) * vp;
-    R rm = rtimes<iw, il>(a, fm, fm.phi[il], d) * R(0.25) * vm;
+      const SweepArgs& a, const Face& fm, const Face& fp, int d, R sm, R sp,
+      int nofm, int nofp, R* acc) {
+    R rp = rtimes<iw, il>(a, fp, fp.phi[il], d) * sp;
+    R rm = rtimes<iw, il>(a, fm, fm.phi[il], d) * sm;
     if ((nofp >> iw) & 1) rp = R(0);
     if ((nofm >> iw) & 1) rm = R(0);
-    acc[iw] = acc[iw] + (rp - rm) / dv0;
+    acc[iw] = acc[iw] + (rp - rm);
   }
   template <int il>
   static __device__ __forceinline__ void dissipate(const SweepArgs& a,
                                                    const Face& fm,
                                                    const Face& fp, int d,
-                                                   R vm, R vp, R dv0, int nofm,
+                                                   R sm, R sp, int nofm,
                                                    int nofp, R* acc) {
-    dissipate_var<il, 0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate_var<il, 1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate_var<il, 2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 3) dissipate_var<il, (NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 4) dissipate_var<il, (NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 5) dissipate_var<il, (NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 6) dissipate_var<il, (NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 7) dissipate_var<il, (NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate_var<il, 0>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    dissipate_var<il, 1>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    dissipate_var<il, 2>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 3) dissipate_var<il, (NW > 3 ? 3 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 4) dissipate_var<il, (NW > 4 ? 4 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 5) dissipate_var<il, (NW > 5 ? 5 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 6) dissipate_var<il, (NW > 6 ? 6 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 7) dissipate_var<il, (NW > 7 ? 7 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+  }
+  // the per-face constants of rtimes on the mixed path
+  static __device__ __forceinline__ void prep_face(const SweepArgs& a, int d,
+                                                   Face& f) {
+    R vv = f.v[0] * f.v[0];
+#pragma unroll
+    for (int c = 1; c < NDIR; c++) vv = vv + f.v[c] * f.v[c];
+    f.vv = vv;
+    if (MHD) {
+      f.sgn = copysignf(1.0f, f.b[d]);
+      const R isr = R(1) / f.sr;
+      f.isrs = f.sgn * isr;
+      f.csr = sqrtf(f.cs2) * isr;
+      f.v2a2 = R(0.5) * vv + a.ph.c2gf * f.cs2;
+    }
   }
   // one direction of the mixed path's cell pass (compile-time d keeps the
   // two face records in registers)
@@ -818,21 +868,25 @@ struct RoeSweep {
     Face fm, fp;
     load_face(buf, nf, fm_i, fm);
     load_face(buf, nf, fp_i, fp);
+    prep_face(a, d, fm);
+    prep_face(a, d, fp);
     int cn[3] = {c[0], c[1], c[2]};
     cn[d] = c[d] - 1;
     const R vm = dv0 + dvol(a, cn);  // dvolume(j)+dvolume(i), lower face
     cn[d] = c[d] + 1;
     const R vp = dvol(a, cn) + dv0;  // and upper face
+    const R q = R(0.25) / dv0;
+    const R sm = vm * q, sp = vp * q;
     const int nofp = c[d] == a.g.nx[d] + 1 ? a.ph.noflux[d][1] : 0;
     const int nofm = c[d] == 2 ? a.ph.noflux[d][0] : 0;
-    dissipate<0>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate<1>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    dissipate<2>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
-    if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, vm, vp, dv0, nofm, nofp, acc);
+    dissipate<0>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    dissipate<1>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    dissipate<2>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 3) dissipate<(NW > 3 ? 3 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 4) dissipate<(NW > 4 ? 4 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 5) dissipate<(NW > 5 ? 5 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 6) dissipate<(NW > 6 ? 6 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
+    if (NW > 7) dissipate<(NW > 7 ? 7 : 0)>(a, fm, fp, d, sm, sp, nofm, nofp, acc);
   }
 
   // Cell pass: per direction the central fluxes of all variables
@@ -908,8 +962,9 @@ __global__ void __launch_bounds__(128)
   RoeSweep<PH, NDIM, NDIR, MHD>::template face_pass<128, D>(a, w1, base, buf);
 }
 
+// (the mixed cell pass is held to 128 registers: 4 CTAs per SM)
 template <class PH, int NDIM, int NDIR, bool MHD>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(typename PH::R) == 4 ? 4 : 1)
     k_correct_roe(SweepArgs a, const typename PH::T* __restrict__ w,
                   const typename PH::T* __restrict__ w1,
                   typename PH::T* __restrict__ wout) {

@@ -911,6 +911,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   ph.gm1 = p->eqpar[0] - 1.0;
   ph.gammaf = (float)ph.gamma;
   ph.gm1f = (float)ph.gm1;
+  ph.c2gf = (2.0f - ph.gammaf) / ph.gm1f;
   ph.pt3 = 0.5 * (p->eqpar[0] - 1.0);
   ph.smallpcoeff = p->smallpcoeff;
   double courantpar = p->courantpar;

@@ -45,6 +45,7 @@ __host__ __device__ inline long long gidx(const DevGrid& g, int gx, int gy,
 struct DevPhys {
   double gamma, pt1, gm1, pt3;
   float gammaf, gm1f;  // the same, rounded once for the FP32 physics
+  float c2gf;           // (2-gammaf)/gm1f, the FP32 Roe eigenvectors' constant
   double smallpcoeff;
   double courantpar;  // <=0: no CFL evaluation (dtpar set)
   int lim[VACGPU_MAXNW];
