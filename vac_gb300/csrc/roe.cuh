@@ -229,8 +229,13 @@ struct RoeSweep {
         aa = R(ad - 2.0 * aR * aL / (aR - aL));
       }
     }
-    // normalisation by dt*2/(dx(i)+dx(j)) (src/vactvd.t:131-140)
-    const R adt = aa * R(qdt) * R(2) / dxs;
+    // normalisation by dt*2/(dx(i)+dx(j)) (src/vactvd.t:131-140); the
+    // mixed path multiplies by the face's dt*2/(dx(i)+dx(j)) formed once
+    R adt;
+    if constexpr (sizeof(R) == 4)
+      adt = aa * (R(qdt) * R(2) / dxs);
+    else
+      adt = aa * R(qdt) * R(2) / dxs;
     if (te == VACGPU_ENTROPY_HARTEN || te == VACGPU_ENTROPY_POWELL)
       smalla = smalla * R(qdt) * R(2) / dxs;
     if (il < 2) am[il] = fabs(adt);
@@ -304,8 +309,9 @@ struct RoeSweep {
     const float cs2s = cf2 > 0.0f ? a2 * ca2 / cf2 : 0.0f;
     const float na = dd >= 0.0f ? 0.5f * (dd + Dr) : x4 / (2.0f * (Dr - dd));
     const float ns = dd <= 0.0f ? 0.5f * (Dr - dd) : x4 / (2.0f * (Dr + dd));
-    float af2 = Dr > 0.0f ? na / Dr : 0.0f;
-    float as2 = Dr > 0.0f ? ns / Dr : 1.0f;
+    const float iDr = Dr > 0.0f ? 1.0f / Dr : 0.0f;
+    float af2 = Dr > 0.0f ? na * iDr : 0.0f;
+    float as2 = Dr > 0.0f ? ns * iDr : 1.0f;
     af2 = fminf(1.0f, fmaxf(af2, 0.0f));
     as2 = fminf(1.0f, fmaxf(as2, 0.0f));
     f.cs2 = a2;
@@ -322,8 +328,9 @@ struct RoeSweep {
     } else {
       const float t = sqrtf(bI * bI + bJ * bJ);
       if (t > 1.0e-30f) {
-        bI = bI / t;
-        bJ = bJ / t;
+        const float it = 1.0f / t;
+        bI = bI * it;
+        bJ = bJ * it;
       } else {
         bI = 0.70710678f;
         bJ = 0.70710678f;

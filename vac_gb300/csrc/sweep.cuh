@@ -294,6 +294,59 @@ struct Sweep {
     for (int iw = 0; iw < NW; iw++) out[off + iw * a.g.vs] = T(u[iw]);
   }
 
+  // One direction of the predictor, the direction a compile-time constant
+  // (a runtime one puts the face states in a stack frame)
+  template <int d>
+  static __device__ __forceinline__ void predict_dir(
+      const SweepArgs& a, const T* __restrict__ w, long long off,
+      const long long* st, const int* c, double qdt, R smallp, const R* u,
+      const R* pc, R* acc) {
+    const long long vs = a.g.vs;
+    R uL[NW], uR[NW];
+    if (a.ph.useprim) {
+      R pm[NW], pp[NW];
+      load(w, off - st[d], vs, pm);
+      load(w, off + st[d], vs, pp);
+      to_prim(a, smallp, pm);
+      to_prim(a, smallp, pp);
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) {
+        R l = PH::limiter(a.ph.lim[iw], pp[iw] - pc[iw], pc[iw] - pm[iw]);
+        uR[iw] = pc[iw] - R(0.5) * l;
+        uL[iw] = pc[iw] + R(0.5) * l;
+      }
+      to_cons(a, uR);
+      to_cons(a, uL);
+    } else {
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++) {
+        R wm = R(w[off + iw * vs - st[d]]);
+        R wp = R(w[off + iw * vs + st[d]]);
+        R l = PH::limiter(a.ph.lim[iw], wp - u[iw], u[iw] - wm);
+        uR[iw] = u[iw] - R(0.5) * l;
+        uL[iw] = u[iw] + R(0.5) * l;
+      }
+    }
+    R fL[NW], fR[NW];
+    PH::template flux<NDIR, MHD>(uR, d, a.ph, smallp, fR);
+    PH::template flux<NDIR, MHD>(uL, d, a.ph, smallp, fL);
+    // 'symm0' faces (setnoflux, src/vacgrid.t:416-454): no flux through
+    // the mesh edge
+    if (c[d] == a.g.nx[d] + 1 && a.ph.noflux[d][1]) {
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++)
+        if ((a.ph.noflux[d][1] >> iw) & 1) fL[iw] = R(0);
+    }
+    if (c[d] == 2 && a.ph.noflux[d][0]) {
+#pragma unroll
+      for (int iw = 0; iw < NW; iw++)
+        if ((a.ph.noflux[d][0] >> iw) & 1) fR[iw] = R(0);
+    }
+    const R cq = PH::qdx(qdt, a.a, d, c[d]);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) acc[iw] = acc[iw] - cq * (fL[iw] - fR[iw]);
+  }
+
   // Hancock predictor (src/vactvdlf.t:5-89): w1 = w - dt/2/dx*(F(w+ldw/2)
   // - F(w-ldw/2)) + dt/2*(nsweepdims/ndim)*S(w), on the mesh.  With
   // useprimitive the slopes and face states are formed in primitive
@@ -324,49 +377,14 @@ struct Sweep {
       to_prim(a, smallp, pc);
     }
     for (int d = a.d0; d <= a.d1; d++) {
-      R uL[NW], uR[NW];
-      if (a.ph.useprim) {
-        R pm[NW], pp[NW];
-        load(w, off - st[d], vs, pm);
-        load(w, off + st[d], vs, pp);
-        to_prim(a, smallp, pm);
-        to_prim(a, smallp, pp);
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++) {
-          R l = PH::limiter(a.ph.lim[iw], pp[iw] - pc[iw], pc[iw] - pm[iw]);
-          uR[iw] = pc[iw] - R(0.5) * l;
-          uL[iw] = pc[iw] + R(0.5) * l;
-        }
-        to_cons(a, uR);
-        to_cons(a, uL);
-      } else {
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++) {
-          R wm = R(w[off + iw * vs - st[d]]);
-          R wp = R(w[off + iw * vs + st[d]]);
-          R l = PH::limiter(a.ph.lim[iw], wp - u[iw], u[iw] - wm);
-          uR[iw] = u[iw] - R(0.5) * l;
-          uL[iw] = u[iw] + R(0.5) * l;
-        }
-      }
-      R fL[NW], fR[NW];
-      PH::template flux<NDIR, MHD>(uR, d, a.ph, smallp, fR);
-      PH::template flux<NDIR, MHD>(uL, d, a.ph, smallp, fL);
-      // 'symm0' faces (setnoflux, src/vacgrid.t:416-454): no flux through
-      // the mesh edge
-      if (c[d] == a.g.nx[d] + 1 && a.ph.noflux[d][1]) {
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++)
-          if ((a.ph.noflux[d][1] >> iw) & 1) fL[iw] = R(0);
-      }
-      if (c[d] == 2 && a.ph.noflux[d][0]) {
-#pragma unroll
-        for (int iw = 0; iw < NW; iw++)
-          if ((a.ph.noflux[d][0] >> iw) & 1) fR[iw] = R(0);
-      }
-      const R cq = PH::qdx(qdt, a.a, d, c[d]);
-#pragma unroll
-      for (int iw = 0; iw < NW; iw++) acc[iw] = acc[iw] - cq * (fL[iw] - fR[iw]);
+      if (d == 0)
+        predict_dir<0>(a, w, off, st, c, qdt, smallp, u, pc, acc);
+      else if (NDIM > 1 && d == 1)
+        predict_dir<(NDIM > 1 ? 1 : 0)>(a, w, off, st, c, qdt, smallp, u, pc,
+                                        acc);
+      else if (NDIM > 2)
+        predict_dir<(NDIM > 2 ? 2 : 0)>(a, w, off, st, c, qdt, smallp, u, pc,
+                                        acc);
     }
     if (a.ph.sourceunsplit) {
       // the round-tripped state (useprimitive) leaves rho and B unchanged
@@ -462,10 +480,13 @@ struct Sweep {
   // ('symm0' mesh faces carry no flux of their variables), into
   // F[iw*nf+f]; plus the CFL maximum of the last substep
   // (src/vactvdlf.t:184-201).
+  // (inlined into k_face, whose direction is a compile-time constant: a
+  // runtime one puts the face states in a stack frame)
   template <int NT>
-  static __device__ void face_pass(const SweepArgs& a, const T* __restrict__ w1,
-                                   const T* __restrict__ base, int d,
-                                   R* __restrict__ F) {
+  static __device__ __forceinline__ void face_pass(const SweepArgs& a,
+                                                   const T* __restrict__ w1,
+                                                   const T* __restrict__ base,
+                                                   int d, R* __restrict__ F) {
     __shared__ unsigned long long shk[NT / 32];
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) return;
@@ -923,19 +944,34 @@ __global__ void __launch_bounds__(128)
   if (MHD) Sweep<PH, NDIM, NDIR, MHD>::current_field(a, w, cur);
 }
 
+// (register bounds: 96 for the FP32 state, 128 for FP64 -- the
+// predictor waits on its stencil loads and wants the resident warps)
 template <class PH, int NDIM, int NDIR, bool MHD>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(typename PH::R) == 4 ? 5 : 4)
     k_predict(SweepArgs a, const typename PH::T* __restrict__ w,
               typename PH::T* __restrict__ w1) {
   Sweep<PH, NDIM, NDIR, MHD>::predict(a, w, w1);
 }
 
-template <class PH, int NDIM, int NDIR, bool MHD>
+template <class PH, int NDIM, int NDIR, bool MHD, int D>
 __global__ void __launch_bounds__(128)
     k_face(SweepArgs a, const typename PH::T* __restrict__ w1,
-           const typename PH::T* __restrict__ base, int d,
+           const typename PH::T* __restrict__ base,
            typename PH::R* __restrict__ F) {
-  Sweep<PH, NDIM, NDIR, MHD>::template face_pass<128>(a, w1, base, d, F);
+  Sweep<PH, NDIM, NDIR, MHD>::template face_pass<128>(a, w1, base, D, F);
+}
+
+// the face pass of direction d
+template <class PH, int NDIM, int NDIR, bool MHD>
+void launch_face_dir(const SweepArgs& a, const typename PH::T* w1,
+                     const typename PH::T* base, int d, typename PH::R* F,
+                     unsigned nb, cudaStream_t st) {
+  if (d == 0)
+    k_face<PH, NDIM, NDIR, MHD, 0><<<nb, 128, 0, st>>>(a, w1, base, F);
+  else if (NDIM > 1 && d == 1)
+    k_face<PH, NDIM, NDIR, MHD, (NDIM > 1 ? 1 : 0)><<<nb, 128, 0, st>>>(a, w1, base, F);
+  else if (NDIM > 2)
+    k_face<PH, NDIM, NDIR, MHD, (NDIM > 2 ? 2 : 0)><<<nb, 128, 0, st>>>(a, w1, base, F);
 }
 
 template <class PH, int NDIM, int NDIR, bool MHD>
@@ -1021,8 +1057,7 @@ struct Launch {
     for (int d = a.d0; d <= a.d1; d++) {
       typename PH::R* F = (typename PH::R*)a.faces + (long long)(d - a.d0) * a.face_stride;
       const unsigned nbf = grid_for(face_count(a.g, d), 128);
-#define KC(D, C, M) \
-  k_face<PH, D, C, M><<<nbf, 128, 0, st>>>(a, w1, base, d, F)
+#define KC(D, C, M) launch_face_dir<PH, D, C, M>(a, w1, base, d, F, nbf, st)
       VACGPU_DISPATCH(a, KC);
 #undef KC
     }
