@@ -140,12 +140,23 @@ struct PHMixed {
   static __device__ __forceinline__ void flux(const float* u, int d,
                                               const DevPhys& k, float smallp,
                                               float* f) {
+    float p, rinv;
+    flux_p<NDIR, MHD>(u, d, k, smallp, f, p, rinv);
+  }
+  // the same, also returning the unclipped thermal pressure and 1/rho
+  template <int NDIR, bool MHD>
+  static __device__ __forceinline__ void flux_p(const float* u, int d,
+                                                const DevPhys& k, float smallp,
+                                                float* f, float& p_raw,
+                                                float& rinv_out) {
     const int E = NDIR + 1;
     const float rinv = 1.0f / u[0];
     const float v = u[1 + d] * rinv;
     float hbb;
     float p = pressure_mixed<NDIR, MHD ? NDIR : 0, PM>(u, rinv, k.gm1f,
                                                        &hbb);
+    p_raw = p;
+    rinv_out = rinv;
     if (MHD) {
       const float pt = p + hbb;
       const float bi = u[E + 1 + d];
@@ -201,6 +212,52 @@ struct PHMixed {
       return sqrtf(0.5f * (cf2 + sqrtf(disc))) + fabsf(u[1 + d] * rinv);
     }
     return sqrtf(cs2) + fabsf(u[1 + d] * rinv);
+  }
+
+  // getcmax at the mean M of two states L, R whose unclipped thermal
+  // pressures pL, pR and inverse densities riL, riR are known.  With
+  // K = m^2/(2 rho) and B^2/2 the mean's pressure is, exactly,
+  //   p(M) = (pL+pR)/2 + (g-1) (rhoL rhoR |vL-vR|^2 / (4 (rhoL+rhoR))
+  //                             + |BL-BR|^2 / 8),
+  // where rhoL rhoR |vL-vR|^2 = |rhoR mL - rhoL mR|^2 / (rhoL rhoR).  Both
+  // corrections are non-negative, so p(M) keeps the accuracy of pL and pR
+  // without a recovery of its own.  M is (L+R)/2 up to rounding.
+  template <int NDIR, bool MHD>
+  static __device__ __forceinline__ float cmax_mean(
+      const float* L, const float* R, const float* M, float pL, float pR,
+      float riL, float riR, int d, const DevPhys& k, float smallp) {
+    const int E = NDIR + 1;
+    const float rinv = 1.0f / M[0];
+    float kk = 0.0f;
+#pragma unroll
+    for (int c = 1; c <= NDIR; c++) {
+      const float t = fmaf(R[0], L[c], -(L[0] * R[c]));
+      kk = fmaf(t, t, kk);
+    }
+    // 1/(4 (rhoL+rhoR)) = rinv/8 with rhoL+rhoR = 2 rho_M
+    float corr = kk * (riL * riR) * (0.125f * rinv);
+    float bb = 0.0f;
+    if (MHD) {
+      float db = 0.0f;
+#pragma unroll
+      for (int c = 1; c <= NDIR; c++) {
+        const float t = L[E + c] - R[E + c];
+        db = fmaf(t, t, db);
+        bb = fmaf(M[E + c], M[E + c], bb);
+      }
+      corr = fmaf(0.125f, db, corr);
+    }
+    float p = fmaf(k.gm1f, corr, 0.5f * (pL + pR));
+    p = p >= smallp ? p : smallp;
+    const float cs2 = k.gammaf * p * rinv;
+    if (MHD) {
+      const float cf2 = bb * rinv + cs2;
+      const float bi = M[E + 1 + d];
+      float disc = cf2 * cf2 - 4.0f * cs2 * (bi * bi) * rinv;
+      disc = disc > 0.0f ? disc : 0.0f;
+      return sqrtf(0.5f * (cf2 + sqrtf(disc))) + fabsf(M[1 + d] * rinv);
+    }
+    return sqrtf(cs2) + fabsf(M[1 + d] * rinv);
   }
 
   // thermal pressure (unclipped) with the path's recovery, as FP32

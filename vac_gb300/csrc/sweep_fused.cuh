@@ -358,12 +358,22 @@ struct Fused {
       R[v] = wr[v] - 0.5f * ldr[v];
       M[v] = 0.5f * (L[v] + R[v]);
     }
-    const float cmax = PH::template cmax<NDIR, MHD>(M, D, a.ph, smallp);
 #pragma unroll
     for (int v = 0; v < NW; v++) L[v] = 2.0f * M[v] - R[v];
     float fL[NW], fR[NW];
-    PHF::template flux<NDIR, MHD>(L, D, a.ph, smallp, fL);
-    PHF::template flux<NDIR, MHD>(R, D, a.ph, smallp, fR);
+    float cmax;
+    if constexpr (PM == PMF) {
+      // the mean's pressure from the two recovered face-state pressures
+      float pL, pR, riL, riR;
+      PHF::template flux_p<NDIR, MHD>(L, D, a.ph, smallp, fL, pL, riL);
+      PHF::template flux_p<NDIR, MHD>(R, D, a.ph, smallp, fR, pR, riR);
+      cmax = PH::template cmax_mean<NDIR, MHD>(L, R, M, pL, pR, riL, riR, D,
+                                                a.ph, smallp);
+    } else {
+      cmax = PH::template cmax<NDIR, MHD>(M, D, a.ph, smallp);
+      PHF::template flux<NDIR, MHD>(L, D, a.ph, smallp, fL);
+      PHF::template flux<NDIR, MHD>(R, D, a.ph, smallp, fR);
+    }
 #pragma unroll
     for (int v = 0; v < NW; v++)
       F[v] = 0.5f * (fL[v] + fR[v]) - cmax * 0.5f * (R[v] - L[v]);
