@@ -953,7 +953,7 @@ struct RoeSweep {
       R wc[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
-      S::add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off, st,
+      S::add_sources(a, S::src_qdt(a, qdt), wc, w1 + off, st,
                      c, acc);
     }
 #pragma unroll

@@ -199,6 +199,19 @@ struct Sweep {
       cur[k - 1][off] = double(current(a, w + off, 0, st, c, k));
   }
 
+  // qdt*(idimmax-idimmin+1)/ndim of the unsplit source call
+  // (src/vactvdlf.t:85,292):
+  // the reference's double expression on the FP64 path; formed in FP32 on
+  // the mixed one, whose sources take it rounded to FP32 anyway (GB300's
+  // FP64 pipe would spend a double division per cell on it)
+  static __device__ __forceinline__ double src_qdt(const SweepArgs& a,
+                                                   double qdt) {
+    if constexpr (sizeof(R) == 4)
+      return (double)((float)qdt * (float)((a.d1 - a.d0) + 1) / (float)NDIM);
+    else
+      return qdt * ((a.d1 - a.d0) + 1.0) / NDIM;
+  }
+
   // addsource2 (src/vac.t:575-605): specialsource (uniform gravity,
   // vacusr.gravity.t:24-75) then addsource (resistive terms, then the
   // Powell divB source, src/vacphys.mhd0.t:208-280).  wc = wCT at the
@@ -393,7 +406,7 @@ struct Sweep {
 #pragma unroll
         for (int iw = 0; iw < NW; iw++) u[iw] = pc[iw];
       }
-      add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, u, w + off, st, c,
+      add_sources(a, src_qdt(a, qdt), u, w + off, st, c,
                   acc);
     }
 #pragma unroll
@@ -554,7 +567,7 @@ struct Sweep {
       R wc[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
-      add_sources(a, qdt * ((a.d1 - a.d0) + 1.0) / NDIM, wc, w1 + off, st, c,
+      add_sources(a, src_qdt(a, qdt), wc, w1 + off, st, c,
                   acc);
     }
 #pragma unroll
