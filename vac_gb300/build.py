@@ -6,8 +6,9 @@ time-loop control are built with ``-fmad=false`` and host code with
 ``-ffp-contract=off`` so no multiply-add is contracted where the reference's
 FP64 operation order is reproduced.  The FP32-state (mixed) units are built
 with ``--use_fast_math``: FP32 subnormals flush to zero and FP32 division
-and square root are the approximate forms; the FP64 arithmetic they contain
-is unaffected.
+and square root are the approximate forms; the double arithmetic they
+contain keeps IEEE division and square root (and, as in any default build,
+may contract multiply-adds).
 """
 import os
 import shutil
