@@ -50,6 +50,11 @@ FP64_CASES = [
     ("hd-gravity", lambda: inistate.riemann_2d(32, 5), "woodward", "cont", 10, None,
      (abi.SRC_GRAVITY, [0.0, -0.5])),
     ("ot-ragged", lambda: _ragged(), "minmod", "periodic", 10, None, None),
+    # non-uniform grids: dx, face widths and dvolume vary per cell
+    ("ot-stretched", lambda: inistate.stretched(inistate.orszag_tang(32)), "woodward",
+     "periodic", 10, None, None),
+    ("rm3-stretched", lambda: inistate.stretched(inistate.random_modes(12, seed=3)),
+     "minmod", "periodic", 4, None, None),
 ]
 
 
@@ -203,6 +208,20 @@ ROE_CASES = [
                                   B.BC_PERIODIC, B.BC_PERIODIC)(p)), None),
     ("rm3-tvdmu-resistive", lambda: inistate.random_modes(12, seed=7), "minmod", "periodic", 4,
      lambda p: (_tvdmu()(p), _resistive(0.002)(p)), None),
+    ("ot-tvdmu-stretched", lambda: inistate.stretched(inistate.orszag_tang(32)), "woodward",
+     "periodic", 8, _tvdmu(), None),
+    ("hd3-tvdmu-stretched",
+     lambda: inistate.stretched(_hd_from_mhd(inistate.random_modes(12, seed=5, p0=0.5))),
+     "minmod", "periodic", 4, _tvdmu(), None),
+    ("hd-tvdmu-gravity", lambda: inistate.riemann_2d(32, 5), "woodward", "cont", 8, _tvdmu(),
+     (abi.SRC_GRAVITY, [0.0, -0.5])),
+    ("ot-tvdmu-fixed-bcs", lambda: inistate.orszag_tang(24), "minmod", "cont", 6,
+     lambda p: (_tvdmu()(p), _bcs(B.BC_FIXED, B.BC_CONT1, B.BC_GRAD1, B.BC_FIXED1)(p)),
+     None),
+    ("hd-tvdmu-smallfix", lambda: inistate.riemann_2d(32, 3), "minmod", "cont", 8,
+     lambda p: (_tvdmu()(p), _smallfix(smallp=0.3, smallrho=0.3)(p)), None),
+    ("rm3-tvdmu-xy", lambda: inistate.random_modes(12, seed=2), "minmod", "periodic", 4,
+     _tvdmu(typedimsplit=abi.SPLIT_XY), None),
 ]
 FP64_CASES = (FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES + RES_CASES +
               ROE_CASES)
@@ -256,6 +275,8 @@ MIXED_CASES = [
     ("ot", lambda: inistate.orszag_tang(64), "minmod", "periodic", 50),
     ("rm3", lambda: inistate.random_modes(32, seed=3), "woodward", "periodic", 20),
     ("hd", lambda: inistate.riemann_2d(64, 7), "minmod", "cont", 30),
+    ("rm3-stretched", lambda: inistate.stretched(inistate.random_modes(32, seed=3)),
+     "woodward", "periodic", 20),
 ]
 
 
@@ -353,6 +374,8 @@ ROE_MIXED = [
      "periodic", 20, _tvdmu(entropy=E.ENTROPY_HARTEN), None),
     ("rm3-tvdmu-powell", lambda: inistate.random_modes(32, seed=1, p0=0.5), "woodward",
      "periodic", 20, _tvdmu(entropy=E.ENTROPY_POWELL), None),
+    ("ot-tvdmu-stretched", lambda: inistate.stretched(inistate.orszag_tang(64)), "minmod",
+     "periodic", 50, _tvdmu(), None),
 ]
 
 

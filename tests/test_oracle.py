@@ -161,6 +161,13 @@ CASES = CASES + SMALLFIX_CASES + BC_CASES + RES_CASES + ROE_CASES + [
      lambda p: setattr(p, "useprimitive", 1)),
     ("rm3-useprimitive-smallfix", lambda: inistate.random_modes(8, seed=4), "minmod",
      "periodic", 3, lambda p: (setattr(p, "useprimitive", 1), smallfix(smallp=0.049)(p))),
+    # non-uniform grids (dx, face widths and dvolume vary per cell)
+    ("ot-stretched", lambda: inistate.stretched(inistate.orszag_tang(16)), "woodward",
+     "periodic", 4, None),
+    ("sod-stretched-tvdmu", lambda: inistate.stretched(inistate.sod_1d(64)), "minmod", "cont",
+     10, tvdmu()),
+    ("rm3-stretched-tvdmu", lambda: inistate.stretched(inistate.random_modes(8, seed=3)),
+     "minmod", "periodic", 3, tvdmu()),
 ]
 
 

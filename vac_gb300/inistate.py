@@ -198,6 +198,24 @@ def blast_3d(n=512, gamma=5.0 / 3.0, r0=0.1, pin=10.0, pout=0.1):
     return _snap(x, w, gamma, True, 3, "MHD blast 3D")
 
 
+def stretched(snap, amp=0.15):
+    """The snapshot's state on a smoothly non-uniform grid: along each axis
+    the cell centres move as x -> x + amp L/(2 pi) sin(2 pi (x - x0)/L) over
+    the box [x0, x0+L) (monotonic for amp < 1), so that dx, the face widths
+    and dvolume vary from cell to cell (gridsetup1 derives them from the
+    centres, src/vacgrid.t:457-593)."""
+    x = np.array(snap.x, dtype=np.float64, copy=True)
+    for d in range(snap.ndim):
+        c = x[d]
+        n = c.shape[d]
+        lo, hi = c.min(), c.max()
+        length = (hi - lo) * n / (n - 1)
+        x0 = lo - 0.5 * length / n
+        x[d] = c + amp * length / (2.0 * np.pi) * np.sin(2.0 * np.pi * (c - x0) / length)
+    return Snapshot(snap.header, snap.it, snap.t, snap.ndim, snap.eqpar,
+                    snap.varnames, x, snap.w, snap.nx)
+
+
 def sod_1d(n=100, gamma=1.4):
     """Sod's shock tube on [0,1]: (rho,p)=(1,1) left of x=0.5, (0.125,0.1)
     right, at rest."""
