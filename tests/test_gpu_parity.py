@@ -50,6 +50,11 @@ FP64_CASES = [
     ("hd-gravity", lambda: inistate.riemann_2d(32, 5), "woodward", "cont", 10, None,
      (abi.SRC_GRAVITY, [0.0, -0.5])),
     ("ot-ragged", lambda: _ragged(), "minmod", "periodic", 10, None, None),
+    # limiter bases: wold ('previous', split sweeps) and the predictor output
+    ("ot-limited-previous", lambda: inistate.orszag_tang(24), "minmod", "periodic", 8,
+     lambda p: setattr(p, "typelimited", abi.LIMITED_PREVIOUS), None),
+    ("ot-limited-predictor", lambda: inistate.orszag_tang(24), "woodward", "periodic", 8,
+     lambda p: setattr(p, "typelimited", abi.LIMITED_PREDICTOR), None),
     # non-uniform grids: dx, face widths and dvolume vary per cell
     ("ot-stretched", lambda: inistate.stretched(inistate.orszag_tang(32)), "woodward",
      "periodic", 10, None, None),
@@ -222,6 +227,10 @@ ROE_CASES = [
      lambda p: (_tvdmu()(p), _smallfix(smallp=0.3, smallrho=0.3)(p)), None),
     ("rm3-tvdmu-xy", lambda: inistate.random_modes(12, seed=2), "minmod", "periodic", 4,
      _tvdmu(typedimsplit=abi.SPLIT_XY), None),
+    ("rm3-tvdmu-limited-predictor", lambda: inistate.random_modes(12, seed=2), "minmod",
+     "periodic", 4, _tvdmu(typelimited=abi.LIMITED_PREDICTOR), None),
+    ("ot-tvdmu-limited-previous", lambda: inistate.orszag_tang(32), "woodward", "periodic", 8,
+     _tvdmu(typelimited=abi.LIMITED_PREVIOUS), None),
 ]
 FP64_CASES = (FP64_CASES + SMALLFIX_CASES + PRIMITIVE_CASES + BC_CASES + RES_CASES +
               ROE_CASES)

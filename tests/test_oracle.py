@@ -161,6 +161,13 @@ CASES = CASES + SMALLFIX_CASES + BC_CASES + RES_CASES + ROE_CASES + [
      lambda p: setattr(p, "useprimitive", 1)),
     ("rm3-useprimitive-smallfix", lambda: inistate.random_modes(8, seed=4), "minmod",
      "periodic", 3, lambda p: (setattr(p, "useprimitive", 1), smallfix(smallp=0.049)(p))),
+    # limiter bases: wold ('previous', split sweeps) and the predictor output
+    ("ot-limited-previous", lambda: inistate.orszag_tang(16), "minmod", "periodic", 4,
+     lambda p: setattr(p, "typelimited", abi.LIMITED_PREVIOUS)),
+    ("ot-limited-predictor", lambda: inistate.orszag_tang(16), "woodward", "periodic", 4,
+     lambda p: setattr(p, "typelimited", abi.LIMITED_PREDICTOR)),
+    ("rm3-tvdmu-limited-predictor", lambda: inistate.random_modes(8, seed=2), "minmod",
+     "periodic", 3, lambda p: (tvdmu()(p), setattr(p, "typelimited", abi.LIMITED_PREDICTOR))),
     # non-uniform grids (dx, face widths and dvolume vary per cell)
     ("ot-stretched", lambda: inistate.stretched(inistate.orszag_tang(16)), "woodward",
      "periodic", 4, None),
