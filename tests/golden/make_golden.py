@@ -5,7 +5,9 @@ For each case this writes ``<name>.ini`` (the seeded initial state, what
 VAC's ``readfileini`` reads, src/vacio.t:534-755) and ``<name>.out`` (the
 FP64 CPU oracle's state after ``nsteps`` steps, ``it`` and ``t`` in its
 header, as ``savefileout_bin`` writes it, src/vacio.t:1008-1047), and
-records the par settings and a SHA-256 of every output in ``cases.json``.
+records the par settings and a SHA-256 of every output in ``cases.json``;
+``<name>.par`` is the same case as a VAC par file, so that the Fortran
+build of the reference (or the drop-in host program) runs it unchanged.
 
 The fixtures freeze the oracle's results: the tests replay each ``.ini``
 through the C oracle, the NumPy restatement and the FP64 GPU path and
@@ -87,6 +89,51 @@ def params(snap, case):
     return p
 
 
+LIMITER = {v: k for k, v in abi.LIMITER_NAMES.items()}
+TYPEFULL = {v: k for k, v in abi.TYPEFULL_NAMES.items()}
+ENTROPY = {v: k for k, v in abi.ENTROPY_NAMES.items()}
+LIMITED = {abi.LIMITED_ORIGINAL: "original", abi.LIMITED_PREVIOUS: "previous",
+           abi.LIMITED_PREDICTOR: "predictor"}
+
+
+def par_file(name, snap, case):
+    """A VAC par file (namelists read by src/vacio.t:25-118) that runs the
+    case from ``<name>.ini``: ``vac < <name>.par`` with the Fortran build
+    or ``vacgb < <name>.par`` writes ``<name>.run.out`` whose last snapshot
+    is the case's ``.out``."""
+    p = params(snap, case)
+    nw, nb = p.nw, 2 * p.ndim
+    tf = lambda b: "T" if b else "F"
+    lines = [" &testlist /",
+             " &filelist",
+             "        filenameini='%s.ini'" % name,
+             "        filename='%s.log','%s.run.out'" % (name, name),
+             " /",
+             " &savelist",
+             "        ditsave=%d,%d" % (case["nsteps"], case["nsteps"]),
+             " /",
+             " &stoplist",
+             "        itmax=%d" % case["nsteps"],
+             " /",
+             " &methodlist",
+             "        typefull=%d*'%s'" % (nw, TYPEFULL[p.typefull]),
+             "        typelimiter=%d*'%s'" % (nw, LIMITER[p.typelimiter[0]]),
+             "        typelimited='%s'" % LIMITED[p.typelimited],
+             "        dimsplit=%s" % tf(p.dimsplit)]
+    if p.typefull in (abi.TVDMU, abi.TVDMU1) and "typeentropy" in case["settings"]:
+        lines.append("        typeentropy=%d*'%s'" % (nw, ENTROPY[p.typeentropy[0]]))
+        lines.append("        entropycoef=%d*%r" % (nw, p.entropycoef[0]))
+    lines += [" /",
+              " &boundlist",
+              "        typeB=%d*'%s'" % (nw * nb, case["bc"]),
+              " /",
+              " &paramlist",
+              "        courantpar=%r" % p.courantpar,
+              "        dtpar=%r" % p.dtpar,
+              " /"]
+    return "\n".join(lines) + "\n"
+
+
 def sha(path):
     with open(path, "rb") as f:
         return hashlib.sha256(f.read()).hexdigest()
@@ -97,6 +144,9 @@ def main():
     for name, mk, lim, bc, nsteps, settings in CASES:
         s = mk()
         case = {"limiter": lim, "bc": bc, "nsteps": nsteps, "settings": settings}
+        if "eqpar" in settings:
+            # eqpar travels in the .ini header, as in VAC's own files
+            s.eqpar = np.asarray(settings["eqpar"], dtype=np.float64)
         ini = os.path.join(HERE, name + ".ini")
         vacfile.write(ini, s)
         s0 = vacfile.read(ini)
@@ -106,6 +156,8 @@ def main():
                        o.state(), s0.nx)
         outp = os.path.join(HERE, name + ".out")
         vacfile.write(outp, out)
+        with open(os.path.join(HERE, name + ".par"), "w") as f:
+            f.write(par_file(name, s0, case))
         case.update(it=int(o.it), t=float(o.t).hex(), nerror=list(map(int, o.nerror())),
                     sha256_ini=sha(ini), sha256_out=sha(outp))
         index[name] = case

@@ -91,3 +91,30 @@ def test_gpu_fp64_reproduces_fixture(gpu_lib, name):
     e.step(case["nsteps"])
     check(e, case, out)
     assert e.nerror() == case["nerror"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_par_file_states_the_case(name):
+    """Each case's VAC par file, read by the drop-in host program's namelist
+    parser (``vacgb --dump-params``, no GPU), gives the case's parameters."""
+    import subprocess
+    from vac_gb300 import abi, build
+    build.build()
+    case, ini, _ = load(name)
+    with open(os.path.join(GOLDEN, name + ".par")) as f:
+        par = f.read()
+    d = json.loads(subprocess.run([build.VACGB, "--dump-params"], cwd=GOLDEN, input=par,
+                                  capture_output=True, text=True, check=True).stdout)
+    p = params(ini, case)
+    nw = p.nw
+    for k in ("ndim", "ndir", "physics", "nw", "typefull", "typelimited", "dimsplit",
+              "typedimsplit", "divbfix", "courantpar", "dtpar", "useprimitive", "smallfix"):
+        assert d[k] == getattr(p, k), k
+    assert d["nx"][:p.ndim] == list(p.nx)[:p.ndim]
+    assert d["gamma"] == p.eqpar[0] and d["itmax"] == case["nsteps"]
+    assert d["typelimiter"] == list(p.typelimiter)[:nw]
+    assert d["typeB"] == [list(p.typeB[ib])[:nw] for ib in range(2 * p.ndim)]
+    if p.typefull in (abi.TVDMU, abi.TVDMU1):
+        assert d["typeentropy"] == list(p.typeentropy)[:nw]
+        assert d["entropycoef"] == list(p.entropycoef)[:nw]
+    assert d["filenames"] == [name + ".log", name + ".run.out"]
