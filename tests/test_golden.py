@@ -118,3 +118,24 @@ def test_par_file_states_the_case(name):
         assert d["typeentropy"] == list(p.typeentropy)[:nw]
         assert d["entropycoef"] == list(p.entropycoef)[:nw]
     assert d["filenames"] == [name + ".log", name + ".run.out"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_host_program_runs_par_file(gpu_lib, name, tmp_path):
+    """The drop-in host program run the way VAC is run (``vacgb < <case>.par``
+    beside ``<case>.ini``) writes a ``.run.out`` whose last snapshot is the
+    fixture, bit for bit."""
+    import shutil
+    import subprocess
+    from vac_gb300 import build
+    case, _, out = load(name)
+    for ext in ("ini", "par"):
+        shutil.copy(os.path.join(GOLDEN, name + "." + ext), tmp_path)
+    with open(tmp_path / (name + ".par")) as f:
+        r = subprocess.run([build.VACGB], cwd=tmp_path, input=f.read(),
+                           capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = vacfile.read(str(tmp_path / (name + ".run.out")))
+    assert got.it == out.it and got.t == out.t
+    assert np.array_equal(bits(got.w), bits(out.w))
