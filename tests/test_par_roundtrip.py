@@ -1,0 +1,126 @@
+"""The drop-in host program's namelist reader on seeded random VAC par
+files: repeat counts (n*'x'), subscripted assignments (typeB(iw,iB)=...,
+with or without blanks inside the subscript, on their own line or after
+other values), Fortran logicals (T, .false., .TRUE.) and reals with D
+exponents, trailing comments.  ``vacgb --dump-params`` (no GPU) must give
+back the parameters the file states (src/vacio.t:25-118 reads the same
+namelists)."""
+import json
+import subprocess
+
+import numpy as np
+import pytest
+
+from vac_gb300 import abi, inistate, vacfile
+
+BCS = ["cont", "periodic", "symm", "asymm", "fixed", "fixed1", "cont1", "grad1", "symm0"]
+LIMS = ["minmod", "woodward", "superbee", "vanleer", "albada"]
+SCHEMES = ["tvdlf", "tvdlf1", "tvdmu", "tvdmu1"]
+ENTS = ["nul", "harten", "powell", "ratio", "yee"]
+REALS = [("0.8", 0.8), ("8.D-1", 0.8), ("8.0d-1", 0.8), ("0.75E0", 0.75), (".6", 0.6),
+         ("5d-1", 0.5), ("0.45D0", 0.45)]
+TRUE = ["T", ".true.", ".TRUE.", ".t."]
+FALSE = ["F", ".false.", ".FALSE.", ".f."]
+
+INIS = [("ot", lambda: inistate.orszag_tang(8)),
+        ("rm3", lambda: inistate.random_modes(6, seed=1)),
+        ("hd2", lambda: inistate.riemann_2d(8, 1)),
+        ("sod", lambda: inistate.sod_1d(16))]
+
+
+@pytest.fixture(scope="module")
+def setup(tmp_path_factory):
+    from vac_gb300 import build
+    build.build()
+    d = tmp_path_factory.mktemp("par")
+    nws = {}
+    for name, mk in INIS:
+        s = mk()
+        vacfile.write(str(d / (name + ".ini")), s)
+        nws[name] = (s.w.shape[0], s.ndim)
+    return build.VACGB, d, nws
+
+
+def runs(vals):
+    """n*'x' run-length form of a list of names."""
+    out, k = [], 0
+    while k < len(vals):
+        m = k
+        while m < len(vals) and vals[m] == vals[k]:
+            m += 1
+        out.append("%d*'%s'" % (m - k, vals[k]) if m - k > 1 else "'%s'" % vals[k])
+        k = m
+    return out
+
+
+def sub(rng, *idx):
+    sep = [",", ", ", " , "][rng.integers(3)]
+    pad = ["", " "][rng.integers(2)]
+    return "(" + pad + sep.join(str(i) for i in idx) + pad + ")"
+
+
+def make_par(rng, ini, nw, ndim):
+    """A random par file and the parameters it states."""
+    exp = {}
+    lim = [LIMS[rng.integers(5)] for _ in range(nw)]
+    over = {int(rng.integers(nw)): LIMS[rng.integers(5)] for _ in range(rng.integers(3))}
+    scheme = SCHEMES[rng.integers(4)]
+    split = bool(rng.integers(2))
+    nb = 2 * ndim
+    tb = [[BCS[rng.integers(len(BCS))] for _ in range(nw)] for _ in range(nb)]
+    bover = {}
+    for _ in range(rng.integers(4)):
+        bover[(int(rng.integers(nw)), int(rng.integers(nb)))] = BCS[rng.integers(len(BCS))]
+    cr, cval = REALS[rng.integers(len(REALS))]
+    L = [" &testlist /", " &filelist", "    filenameini='%s.ini'   ! initial state" % ini, " /",
+         " &methodlist",
+         "    typefull= %d*'%s'" % (nw, scheme),
+         "    typelimiter= " + ", ".join(runs(lim))]
+    for iw, l in over.items():
+        L.append("    typelimiter%s = '%s'" % (sub(rng, iw + 1), l))
+        lim[iw] = l
+    L.append("    dimsplit=%s" % (TRUE if split else FALSE)[rng.integers(4)])
+    tl = ["original", "previous", "predictor", None][rng.integers(4)]
+    if tl:
+        L.append("    typelimited='%s'" % tl)
+    ent = None
+    if scheme.startswith("tvdmu"):
+        ent = [ENTS[rng.integers(5)] for _ in range(nw)]
+        L.append("    typeentropy=" + ",".join(runs(ent)) + "  ! per wave")
+    L.append(" /")
+    flat = [tb[ib][iw] for ib in range(nb) for iw in range(nw)]
+    items = runs(flat)
+    bl = " &boundlist typeB= " + ", ".join(items)
+    for (iw, ib), b in bover.items():
+        bl += [" ", ", ", "\n    "][rng.integers(3)] + "typeB%s='%s'" % (sub(rng, iw + 1, ib + 1), b)
+        tb[ib][iw] = b
+    L += [bl, " /", " &paramlist courantpar=%s, dtpar=-1d0 /" % cr,
+          " &stoplist itmax=%d /" % rng.integers(1, 500)]
+    exp.update(typelimiter=[LIMS.index(l) for l in lim], typefull=SCHEMES.index(scheme),
+               dimsplit=int(split), typeB=[[BCS.index(b) for b in row] for row in tb],
+               courantpar=cval)
+    if not split:
+        exp["typelimited"] = (abi.LIMITED_PREDICTOR if tl == "predictor"
+                              else abi.LIMITED_PREVIOUS)
+    elif tl:
+        exp["typelimited"] = ["original", "previous", "predictor"].index(tl)
+    else:
+        exp["typelimited"] = abi.LIMITED_ORIGINAL
+    if ent:
+        exp["typeentropy"] = [ENTS.index(e) for e in ent]
+    return "\n".join(L) + "\n", exp
+
+
+@pytest.mark.parametrize("k", range(40))
+def test_random_par_files_read_back(setup, k):
+    vacgb, d, nws = setup
+    rng = np.random.default_rng(700 + k)
+    ini = INIS[k % len(INIS)][0]
+    nw, ndim = nws[ini]
+    par, exp = make_par(rng, ini, nw, ndim)
+    r = subprocess.run([vacgb, "--dump-params"], cwd=d, input=par, capture_output=True,
+                       text=True)
+    assert r.returncode == 0, par + r.stderr
+    got = json.loads(r.stdout)
+    for key, val in exp.items():
+        assert got[key] == val, (key, par)

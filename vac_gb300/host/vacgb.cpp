@@ -93,11 +93,18 @@ void parse_namelists(const std::string& text, Namelists& nl) {
     if (i >= n) return "";
     if (text[i] == '\'' || text[i] == '"') return read_quoted();
     std::string s;
-    while (i < n && !std::isspace((unsigned char)text[i]) && text[i] != ',' &&
+    int depth = 0;  // a subscript list "name(iw,iB)" keeps its commas
+    while (i < n && (depth > 0 || (!std::isspace((unsigned char)text[i]) && text[i] != ',')) &&
            text[i] != '/' && text[i] != '=' && text[i] != '!') {
       if (text[i] == '*' && !s.empty()) {  // repeat count
         s += text[i++];
         if (i < n && (text[i] == '\'' || text[i] == '"')) return s + read_quoted();
+        continue;
+      }
+      if (text[i] == '(') depth++;
+      if (text[i] == ')' && depth > 0) depth--;
+      if (std::isspace((unsigned char)text[i])) {
+        i++;
         continue;
       }
       s += text[i++];
@@ -128,7 +135,14 @@ void parse_namelists(const std::string& text, Namelists& nl) {
         break;
       }
       std::string key;
-      while (i < n && text[i] != '=' && !std::isspace((unsigned char)text[i])) key += text[i++];
+      int kdepth = 0;  // blanks inside "name(iw, iB)" belong to the key
+      while (i < n && text[i] != '=' &&
+             (kdepth > 0 || !std::isspace((unsigned char)text[i]))) {
+        if (text[i] == '(') kdepth++;
+        if (text[i] == ')' && kdepth > 0) kdepth--;
+        if (!std::isspace((unsigned char)text[i])) key += text[i];
+        i++;
+      }
       skip_ws();
       if (i >= n || text[i] != '=') die("Error in namelist " + grp + ": expected = after " + key);
       i++;
