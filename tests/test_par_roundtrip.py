@@ -124,3 +124,42 @@ def test_random_par_files_read_back(setup, k):
     got = json.loads(r.stdout)
     for key, val in exp.items():
         assert got[key] == val, (key, par)
+
+
+ARRAYS = """ &filelist filenameini='ot.ini'
+   filename(2)='b.out'
+   filename(1)='a.log' /
+ &savelist ditsave(1)=10
+   ditsave(2)=20
+   dtsave(2)=0.5d0, itsave(2,1)=7 /
+ &methodlist typefull=6*'tvdmu' typefull(2)='tvdmu'
+   eqpar(1)=1.4d0
+   eqpar(2)=0.01
+   typeentropy=3*'harten' typeentropy(4)='yee', entropycoef(2)=0.3 /
+"""
+
+
+def test_array_assignments_accumulate(setup):
+    """Several assignments to elements of one array all take effect, in
+    file order (filename, eqpar, typefull, dtsave, ditsave, itsave,
+    typeentropy, entropycoef)."""
+    vacgb, d, _ = setup
+    got = json.loads(subprocess.run([vacgb, "--dump-params"], cwd=d, input=ARRAYS,
+                                    capture_output=True, text=True, check=True).stdout)
+    assert got["filenames"] == ["a.log", "b.out"]
+    assert got["ditsave"] == [10, 20] and got["dtsave"] == [1e99, 0.5]
+    assert got["itsave1"] == [10000000, 7]
+    assert got["eqpar"] == [1.4, 0.01] and got["typefull"] == abi.TVDMU
+    assert got["typeentropy"] == [abi.ENTROPY_HARTEN] * 3 + [abi.ENTROPY_YEE, 0, 0]
+    assert got["entropycoef"][1] == 0.3
+
+
+@pytest.mark.parametrize("bad", ["typeB(7,1)='cont'", "typeB(0,1)='cont'",
+                                 "typelimiter(0)='minmod'"])
+def test_subscript_out_of_range_is_an_error(setup, bad):
+    vacgb, d, _ = setup
+    grp = "boundlist" if bad.startswith("typeB") else "methodlist"
+    par = " &filelist filenameini='ot.ini' /\n &%s %s /\n" % (grp, bad)
+    r = subprocess.run([vacgb, "--dump-params"], cwd=d, input=par, capture_output=True,
+                       text=True)
+    assert r.returncode != 0 and "subscript out of range" in (r.stdout + r.stderr)

@@ -341,6 +341,17 @@ int main(int argc, char** argv) {
     auto v = find_all(name);
     return v.empty() ? nullptr : v.back();
   };
+  // every assignment of a 1-D array, in file order: "name = v1, v2, ..."
+  // fills from element 1, "name(i) = ..." from element i; elements beyond
+  // the array are ignored
+  auto fill1 = [&](const std::string& name, size_t size, auto setter) {
+    for (auto* a : find_all(name)) {
+      if (!a->idx.empty() && a->idx[0] < 1)
+        die("Error in namelist: subscript out of range for " + name);
+      size_t o = a->idx.empty() ? 0 : (size_t)(a->idx[0] - 1);
+      for (size_t k = 0; k < a->vals.size() && o + k < size; k++) setter(o + k, a->vals[k]);
+    }
+  };
   auto getd = [&](const std::string& name, double def) {
     auto a = last(name);
     return a && !a->vals.empty() ? to_double(a->vals[0]) : def;
@@ -362,8 +373,7 @@ int main(int argc, char** argv) {
   std::string fini = gets("filenameini", "");
   if (fini.empty()) die("Error in ReadParameters: filenameini is not set");
   std::vector<std::string> fnames(2, "");
-  if (auto a = last("filename"))
-    for (size_t k = 0; k < a->vals.size() && k < 2; k++) fnames[k] = to_str(a->vals[k]);
+  fill1("filename", 2, [&](size_t k, const std::string& v) { fnames[k] = to_str(v); });
   std::string typeini = lower(gets("typefileini", "auto"));
   int snapini = geti("snapshotini", 0);
   if (getb("fullgridini", false) || getb("fullgridout", false))
@@ -403,19 +413,13 @@ int main(int argc, char** argv) {
   vacgpu_default_params(&p, ini.ndim, ndir, physics, ini.nx.data());
   p.precision = prec_opt == "mixed" ? VACGPU_PREC_MIXED : VACGPU_PREC_FP64;
   for (size_t k = 0; k < ini.eqpar.size() && k < VACGPU_MAXEQPAR; k++) p.eqpar[k] = ini.eqpar[k];
-  if (auto a = last("eqpar"))
-    for (size_t k = 0; k < a->vals.size() && k < VACGPU_MAXEQPAR; k++)
-      p.eqpar[(a->idx.empty() ? 1 : a->idx[0]) - 1 + k] = to_double(a->vals[k]);
+  fill1("eqpar", VACGPU_MAXEQPAR,
+        [&](size_t k, const std::string& v) { p.eqpar[k] = to_double(v); });
 
   // methodlist (readparameters' harmonisation, src/vacio.t:216-364)
   std::vector<std::string> typefull(nw, "tvdlf"), typelim(nw, "minmod");
-  if (auto a = last("typefull"))
-    for (size_t k = 0; k < a->vals.size() && (int)k < nw; k++) typefull[k] = lower(to_str(a->vals[k]));
-  for (auto* a : find_all("typelimiter")) {
-    size_t o = a->idx.empty() ? 0 : a->idx[0] - 1;
-    for (size_t k = 0; k < a->vals.size() && o + k < (size_t)nw; k++)
-      typelim[o + k] = lower(to_str(a->vals[k]));
-  }
+  fill1("typefull", nw, [&](size_t k, const std::string& v) { typefull[k] = lower(to_str(v)); });
+  fill1("typelimiter", nw, [&](size_t k, const std::string& v) { typelim[k] = lower(to_str(v)); });
   std::string tf1 = "nul";
   for (auto& t : typefull)
     if (t != "nul") tf1 = t;
@@ -428,22 +432,15 @@ int main(int argc, char** argv) {
   // typeentropy, entropycoef (per characteristic wave) and divbwave of the
   // Roe dissipation (src/vacio.t:35,80; par/DEFAULT:47)
   const char* entnames[] = {"nul", "harten", "powell", "ratio", "yee"};
-  for (auto* a : find_all("typeentropy")) {
-    size_t o = a->idx.empty() ? 0 : a->idx[0] - 1;
-    for (size_t k = 0; k < a->vals.size() && o + k < (size_t)nw; k++) {
-      std::string t = lower(to_str(a->vals[k]));
-      int e = -1;
-      for (int m = 0; m < 5; m++)
-        if (t == entnames[m]) e = m;
-      if (e < 0) die("No such type of entropy fix:" + t);
-      p.typeentropy[o + k] = e;
-    }
-  }
-  for (auto* a : find_all("entropycoef")) {
-    size_t o = a->idx.empty() ? 0 : a->idx[0] - 1;
-    for (size_t k = 0; k < a->vals.size() && o + k < (size_t)nw; k++)
-      p.entropycoef[o + k] = to_double(a->vals[k]);
-  }
+  fill1("typeentropy", nw, [&](size_t k, const std::string& v) {
+    std::string t = lower(to_str(v));
+    int e = -1;
+    for (int m = 0; m < 5; m++)
+      if (t == entnames[m]) e = m;
+    if (e < 0) die("No such type of entropy fix:" + t);
+    p.typeentropy[k] = e;
+  });
+  fill1("entropycoef", nw, [&](size_t k, const std::string& v) { p.entropycoef[k] = to_double(v); });
   p.divbwave = getb("divbwave", true);
   const char* limnames[] = {"minmod", "woodward", "superbee", "vanleer", "albada"};
   for (int iw = 0; iw < nw; iw++) {
@@ -491,6 +488,9 @@ int main(int argc, char** argv) {
                            "fixed1", "cont1", "grad1", "symm0", "special"};
   for (auto* a : find_all("typeb")) {
     size_t o = 0;
+    for (size_t m = 0; m < a->idx.size(); m++)
+      if (a->idx[m] < 1 || (m == 0 && a->idx.size() == 2 && a->idx[0] > nw))
+        die("Error in namelist: subscript out of range for typeB");
     if (a->idx.size() == 2) o = (a->idx[1] - 1) * nw + (a->idx[0] - 1);
     else if (a->idx.size() == 1) o = a->idx[0] - 1;
     for (size_t k = 0; k < a->vals.size(); k++) {
@@ -519,6 +519,9 @@ int main(int argc, char** argv) {
   auto fill2 = [&](const char* nm, auto setter) {
     for (auto* a : find_all(nm)) {
       size_t o = 0;
+      for (size_t m = 0; m < a->idx.size(); m++)
+        if (a->idx[m] < 1 || (m == 0 && a->idx.size() == 2 && a->idx[0] > NSAVE))
+          die(std::string("Error in namelist: subscript out of range for ") + nm);
       if (a->idx.size() == 2) o = (a->idx[1] - 1) * NSAVE + (a->idx[0] - 1);
       else if (a->idx.size() == 1) o = a->idx[0] - 1;
       for (size_t k = 0; k < a->vals.size(); k++) setter(o + k, a->vals[k]);
@@ -530,10 +533,8 @@ int main(int argc, char** argv) {
   fill2("itsave", [&](size_t q, const std::string& v) {
     if (q < 2 * NSAVE) itsave[q / NSAVE][q % NSAVE] = (int)to_double(v);
   });
-  if (auto a = last("dtsave"))
-    for (size_t k = 0; k < a->vals.size() && k < 2; k++) dtsave[(a->idx.empty() ? 1 : a->idx[0]) - 1 + k] = to_double(a->vals[k]);
-  if (auto a = last("ditsave"))
-    for (size_t k = 0; k < a->vals.size() && k < 2; k++) ditsave[(a->idx.empty() ? 1 : a->idx[0]) - 1 + k] = (int)to_double(a->vals[k]);
+  fill1("dtsave", 2, [&](size_t k, const std::string& v) { dtsave[k] = to_double(v); });
+  fill1("ditsave", 2, [&](size_t k, const std::string& v) { ditsave[k] = (int)to_double(v); });
 
   if (dump) {
     std::printf("{\"ndim\": %d, \"ndir\": %d, \"physics\": %d, \"nw\": %d, \"nx\": [%d, %d, %d],"
@@ -556,7 +557,8 @@ int main(int argc, char** argv) {
     for (int il = 0; il < nw; il++) std::printf("%s%d", il ? ", " : "", p.typeentropy[il]);
     std::printf("], \"entropycoef\": [");
     for (int il = 0; il < nw; il++) std::printf("%s%.17g", il ? ", " : "", p.entropycoef[il]);
-    std::printf("], \"divbwave\": %d", p.divbwave);
+    std::printf("], \"divbwave\": %d, \"eqpar\": [%.17g, %.17g]", p.divbwave, p.eqpar[0],
+                p.eqpar[1]);
     std::printf(", \"ditsave\": [%d, %d], \"dtsave\": [%.17g, %.17g], \"itsave1\": [%d, %d],"
                 " \"tsave2\": [%.17g, %.17g], \"filenames\": [\"%s\", \"%s\"]}\n",
                 ditsave[0], ditsave[1], dtsave[0], dtsave[1], itsave[0][0], itsave[0][1],
