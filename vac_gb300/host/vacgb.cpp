@@ -507,12 +507,13 @@ int main(int argc, char** argv) {
   }
   // savelist: tsave(isave,ifile), itsave(isave,ifile), dtsave(ifile), ditsave(ifile)
   const int NSAVE = 100;
-  double tsave[2][NSAVE];
-  int itsave[2][NSAVE];
+  // one sentinel past the last save slot, where the save counters stop
+  double tsave[2][NSAVE + 1];
+  int itsave[2][NSAVE + 1];
   double dtsave[2] = {1e99, 1e99};
   int ditsave[2] = {10000000, 10000000};
   for (int f = 0; f < 2; f++)
-    for (int k = 0; k < NSAVE; k++) {
+    for (int k = 0; k <= NSAVE; k++) {
       tsave[f][k] = 1e99;
       itsave[f][k] = 10000000;
     }
@@ -651,11 +652,11 @@ int main(int argc, char** argv) {
     bool ok = false;
     if (t >= tsave[f][isavet[f]]) {
       ok = true;
-      isavet[f]++;
+      if (isavet[f] < NSAVE) isavet[f]++;
     }
     if (it == itsave[f][isaveit[f]]) {
       ok = true;
-      isaveit[f]++;
+      if (isaveit[f] < NSAVE) isaveit[f]++;
     }
     if (it == itsavelast[f] + ditsave[f]) ok = true;
     if (t >= tsavelast[f] + dtsave[f]) ok = true;
