@@ -163,3 +163,25 @@ def test_subscript_out_of_range_is_an_error(setup, bad):
     r = subprocess.run([vacgb, "--dump-params"], cwd=d, input=par, capture_output=True,
                        text=True)
     assert r.returncode != 0 and "subscript out of range" in (r.stdout + r.stderr)
+
+
+@pytest.mark.parametrize("cut,msg", [(-8, "Error in ReadFileIni"), (200, "Error in ReadFileIni"),
+                                     ("eqpar", "wrong size of the eqpar")])
+def test_damaged_ini_is_an_error(setup, tmp_path, cut, msg):
+    """A truncated binary .ini, or one whose records disagree with its
+    header, stops the program with a message instead of being read."""
+    vacgb, d, _ = setup
+    raw = (d / "ot.ini").read_bytes()
+    if cut == "eqpar":
+        s = vacfile.read(str(d / "ot.ini"))
+        vacfile.write(str(tmp_path / "bad.ini"), s)
+        raw = bytearray((tmp_path / "bad.ini").read_bytes())
+        # neqpar in the it,t,ndim,neqpar,nw record (after the 79-byte header record)
+        raw[4 + 79 + 4 + 4 + 16:4 + 79 + 4 + 4 + 20] = (3).to_bytes(4, "little")
+        raw = bytes(raw)
+    else:
+        raw = raw[:cut]
+    (tmp_path / "bad.ini").write_bytes(raw)
+    r = subprocess.run([vacgb, "--dump-params"], cwd=tmp_path, capture_output=True, text=True,
+                       input=" &filelist filenameini='bad.ini' /\n")
+    assert r.returncode != 0 and msg in (r.stdout + r.stderr), r.stdout + r.stderr

@@ -220,6 +220,7 @@ struct Snap {
 bool read_rec(std::ifstream& f, std::vector<char>& buf) {
   int32_t n1, n2;
   if (!f.read((char*)&n1, 4)) return false;
+  if (n1 < 0) die("Error in ReadFileIni: corrupt record");
   buf.resize(n1);
   if (!f.read(buf.data(), n1) || !f.read((char*)&n2, 4) || n1 != n2)
     die("Error in ReadFileIni: corrupt record");
@@ -232,29 +233,40 @@ Snap read_ini_binary(const std::string& fn, int snapshot) {
   Snap last;
   int count = 0;
   std::vector<char> b;
+  // the next record of the snapshot, at least `min` bytes (exactly, if exact)
+  auto rec = [&](size_t min, bool exact, const char* what) {
+    if (!read_rec(f, b)) die(std::string("Error in ReadFileIni: ") + fn + " ends before the " + what);
+    if (b.size() < min || (exact && b.size() != min))
+      die(std::string("Error in ReadFileIni: wrong size of the ") + what + " record in " + fn);
+  };
   while (read_rec(f, b)) {
     Snap s;
     s.head = std::string(b.begin(), b.end());
-    read_rec(f, b);
+    rec(24, false, "it,t,ndim,neqpar,nw");
     std::memcpy(&s.it, b.data(), 4);
     std::memcpy(&s.t, b.data() + 4, 8);
     std::memcpy(&s.ndim, b.data() + 12, 4);
     std::memcpy(&s.neqpar, b.data() + 16, 4);
     std::memcpy(&s.nw, b.data() + 20, 4);
     if (s.ndim < 0) die("Error: input file contains general grid");
-    read_rec(f, b);
+    if (s.ndim < 1 || s.ndim > 3 || s.nw < 1 || s.neqpar < 0)
+      die("Error in ReadFileIni: bad ndim, nw or neqpar in " + fn);
+    rec(4 * (size_t)s.ndim, false, "nx");
     s.nx.resize(s.ndim);
     std::memcpy(s.nx.data(), b.data(), 4 * s.ndim);
-    read_rec(f, b);
+    for (int v : s.nx)
+      if (v < 1) die("Error in ReadFileIni: bad grid size in " + fn);
+    rec(8 * (size_t)s.neqpar, true, "eqpar");
     s.eqpar.resize(b.size() / 8);
     std::memcpy(s.eqpar.data(), b.data(), b.size());
-    read_rec(f, b);
+    rec(0, false, "varnames");
     s.varnames = std::string(b.begin(), b.end());
-    read_rec(f, b);
+    const size_t bytes = 8 * (size_t)s.ncell();
+    rec(bytes * s.ndim, true, "x");
     s.x.resize(b.size() / 8);
     std::memcpy(s.x.data(), b.data(), b.size());
     for (int iw = 0; iw < s.nw; iw++) {
-      read_rec(f, b);
+      rec(bytes, true, "w");
       size_t o = s.w.size();
       s.w.resize(o + b.size() / 8);
       std::memcpy(s.w.data() + o, b.data(), b.size());
@@ -272,8 +284,12 @@ Snap read_ini_ascii(const std::string& fn) {
   Snap s;
   std::getline(f, s.head);
   f >> s.it >> s.t >> s.ndim >> s.neqpar >> s.nw;
+  if (!f || s.ndim < 1 || s.ndim > 3 || s.nw < 1 || s.neqpar < 0)
+    die("Error in ReadFileIni: bad header line in " + fn);
   s.nx.resize(s.ndim);
   for (auto& v : s.nx) f >> v;
+  for (int v : s.nx)
+    if (!f || v < 1) die("Error in ReadFileIni: bad grid size in " + fn);
   s.eqpar.resize(s.neqpar);
   for (auto& v : s.eqpar) f >> v;
   std::string line;
@@ -286,6 +302,7 @@ Snap read_ini_ascii(const std::string& fn) {
     for (int d = 0; d < s.ndim; d++) f >> s.x[d * n + c];
     for (int iw = 0; iw < s.nw; iw++) f >> s.w[iw * n + c];
   }
+  if (!f) die("Error in ReadFileIni: " + fn + " ends before its last cell");
   return s;
 }
 
