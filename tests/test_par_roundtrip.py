@@ -185,3 +185,23 @@ def test_damaged_ini_is_an_error(setup, tmp_path, cut, msg):
     r = subprocess.run([vacgb, "--dump-params"], cwd=tmp_path, capture_output=True, text=True,
                        input=" &filelist filenameini='bad.ini' /\n")
     assert r.returncode != 0 and msg in (r.stdout + r.stderr), r.stdout + r.stderr
+
+
+def test_ascii_ini_header_is_read(setup, tmp_path):
+    """An ASCII .ini (typefileini='auto' detects it, src/vacio.t:534-570)
+    gives the same grid and equation parameters as the binary one."""
+    vacgb, d, _ = setup
+    s = vacfile.read(str(d / "rm3.ini"))
+    vacfile.write_ascii(str(tmp_path / "a.ini"), s)
+    # this host writes binary .out files only; with an ASCII .ini VAC's
+    # typefileout would default to ASCII
+    par = " &filelist filenameini='%s' typefileout='binary' /\n"
+    out = []
+    for path in (str(tmp_path / "a.ini"), str(d / "rm3.ini")):
+        out.append(json.loads(subprocess.run([vacgb, "--dump-params"], cwd=tmp_path,
+                                             input=par % path, capture_output=True, text=True,
+                                             check=True).stdout))
+    for key in ("ndim", "ndir", "physics", "nw", "nx"):
+        assert out[0][key] == out[1][key], key
+    # the ASCII file keeps 6 significant digits
+    assert abs(out[0]["gamma"] - out[1]["gamma"]) <= 1e-5 * out[1]["gamma"]
