@@ -99,8 +99,16 @@ enum { VACGPU_SPLIT_XYYX = 0, VACGPU_SPLIT_XY = 1 };
 /* Arithmetic of the device state.
  * FP64: every operation in IEEE double, in the reference's operation order
  *       (no FMA contraction), bit-compatible with the FP64 oracle.
- * MIXED: state and fluxes in FP32; the thermal/total pressure recovery
- *       p=(g-1)(e-m^2/2rho-B^2/2), the conservation sums and t+=dt in FP64. */
+ * MIXED: state, fluxes and wave speeds in FP32.  The thermal-pressure
+ *       recovery p=(g-1)(e-m^2/2rho-B^2/2), where low-beta cells cancel, is
+ *       evaluated by default in double-float arithmetic on the FP32 pipes
+ *       (exact FMA products and compensated sums, 44+ significant bits;
+ *       the result is within a few FP32 ulps of p itself, however much
+ *       e and m^2/2rho+B^2/2 cancel), not on the FP64 pipe; the environment
+ *       variable VACGPU_MIXED_PRESSURE=f64 selects native IEEE double
+ *       instead (split kernels, slower on GB300's narrow FP64 pipe).  The
+ *       conservation sums, dt and t+=dt are native FP64.  Tolerance of the
+ *       state against the FP64 path: relative L1 <= 1e-5 per variable. */
 enum { VACGPU_PREC_FP64 = 0, VACGPU_PREC_MIXED = 1 };
 
 /* device source hooks standing in for specialsource/getdt_special

@@ -155,7 +155,11 @@ def test_array_assignments_accumulate(setup):
 
 
 @pytest.mark.parametrize("bad", ["typeB(7,1)='cont'", "typeB(0,1)='cont'",
-                                 "typelimiter(0)='minmod'"])
+                                 "typeB(1,5)='cont'", "typeB(25)='cont'",
+                                 "typeB(1,1,1)='cont'", "typelimiter(0)='minmod'",
+                                 "typelimiter(7)='minmod'", "typelimiter(1,1)='minmod'",
+                                 "eqpar(5)=1.0", "dtsave(3)=1.0", "ditsave(3)=5",
+                                 "tsave(1,3)=1.0", "itsave(101,1)=5", "tsave(201)=1.0"])
 def test_subscript_out_of_range_is_an_error(setup, bad):
     vacgb, d, _ = setup
     grp = "boundlist" if bad.startswith("typeB") else "methodlist"
@@ -166,7 +170,8 @@ def test_subscript_out_of_range_is_an_error(setup, bad):
 
 
 @pytest.mark.parametrize("cut,msg", [(-8, "Error in ReadFileIni"), (200, "Error in ReadFileIni"),
-                                     ("eqpar", "wrong size of the eqpar")])
+                                     ("eqpar", "wrong size of the eqpar"),
+                                     ("ndir", "ndir outside"), ("nw", "Incompatible number")])
 def test_damaged_ini_is_an_error(setup, tmp_path, cut, msg):
     """A truncated binary .ini, or one whose records disagree with its
     header, stops the program with a message instead of being read."""
@@ -179,6 +184,16 @@ def test_damaged_ini_is_an_error(setup, tmp_path, cut, msg):
         # neqpar in the it,t,ndim,neqpar,nw record (after the 79-byte header record)
         raw[4 + 79 + 4 + 4 + 16:4 + 79 + 4 + 4 + 20] = (3).to_bytes(4, "little")
         raw = bytes(raw)
+    elif cut in ("ndir", "nw"):
+        # a header whose ndir digit asks for 9 vector components, with a
+        # file that holds the 20 variables they would need; or an honest
+        # 2-D header over 20 variables
+        import numpy as np
+        s = vacfile.read(str(d / "ot.ini"))
+        s.w = np.concatenate([s.w] * 4)[:20].copy()
+        s.header = "damaged_mhd29" if cut == "ndir" else "damaged_mhd22"
+        vacfile.write(str(tmp_path / "bad.ini"), s)
+        raw = (tmp_path / "bad.ini").read_bytes()
     else:
         raw = raw[:cut]
     (tmp_path / "bad.ini").write_bytes(raw)

@@ -89,11 +89,16 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
         "vacgpu_sweep_noalloc supports neither smallfix, useprimitive nor "
         "resistivity");
   const double* dxs[3] = {dx0, dx1, dx2};
+  // cells with ghosts, checked against the limit after every factor so that
+  // no product can wrap (each factor is at most the limit + 4)
   long long gcells = 1;
-  for (int d = 0; d < p->ndim; d++) {
+  for (int d = 0; d < p->ndim && gcells <= VACGPU_NOALLOC_MAX_GCELLS; d++) {
     if (p->nx[d] < 2) return vacgpu_internal_fail("nx must be >= 2");
     if (!dxs[d]) return vacgpu_internal_fail("dx of a used dimension is NULL");
-    gcells *= p->nx[d] + 4;
+    const long long f = p->nx[d] > VACGPU_NOALLOC_MAX_GCELLS
+                            ? (long long)VACGPU_NOALLOC_MAX_GCELLS + 1
+                            : (long long)p->nx[d] + 4;
+    gcells *= f;
   }
   if (gcells > VACGPU_NOALLOC_MAX_GCELLS)
     return vacgpu_internal_fail(

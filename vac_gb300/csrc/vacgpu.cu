@@ -145,6 +145,10 @@ struct vacgpu_handle {
   vacgpu_bound_fn bound_fn;  // specialbound hook
   void* bound_user;
   bool hook_failed;  // a hook returned non-zero while a step was issued
+  // A bounded device wait of the fused sweep gave up (Ctrl::fault): some
+  // tiles of that sweep were not written, so the state is invalid.  Steps
+  // are refused until vacgpu_upload gives the handle a new state.
+  bool faulted;
   vacgpu_eta_fn eta_fn;  // specialeta hook (eqpar(eta_) < 0)
   void* eta_user;
   double* etaf;      // its eta field, gradeta (compactres) and the current
@@ -1164,6 +1168,7 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   if (h->any_special && !h->bound_fn) return fail(NO_SPECIAL);
   if (h->etaf && !h->eta_fn) return fail(NO_ETA);
   h->hook_failed = false;
+  h->faulted = false;
   const DevGrid& g = h->g;
   long long n = g.ncell * h->nw;
   // it, t, itmin (startup, src/vac.t:176) and the dt state of a fresh run
@@ -1238,6 +1243,8 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   if (!h->have_grid || !h->have_state)
     return fail("vacgpu_step before vacgpu_set_grid/vacgpu_upload");
   if (maxsteps < 0) return fail("maxsteps must be >= 0");
+  if (h->faulted)
+    return fail("the state is invalid after a timed-out device wait; upload a state first");
   if (h->any_special && !h->bound_fn) return fail(NO_SPECIAL);
   if (h->etaf && !h->eta_fn) return fail(NO_ETA);
   if (h->tuning && maxsteps > 0 && !h->timing && tune_nzc(h)) return 1;
@@ -1271,7 +1278,10 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
   CK(cudaStreamSynchronize(h->st));
   // every executed step swapped the buffers nsw times; skipped ones none
   h->cur = start_cur ^ ((c.steps * nsw) & 1);
-  if (c.fault) return fail("a device wait timed out (TMA copy never completed)");
+  if (c.fault) {
+    h->faulted = true;
+    return fail("a device wait timed out (TMA copy never completed); the state is invalid");
+  }
   h->it_host = c.it;
   if (t) *t = c.t;
   if (it) *it = c.it;

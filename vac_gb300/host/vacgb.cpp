@@ -284,7 +284,10 @@ Snap read_ini_ascii(const std::string& fn) {
   Snap s;
   std::getline(f, s.head);
   f >> s.it >> s.t >> s.ndim >> s.neqpar >> s.nw;
-  if (!f || s.ndim < 1 || s.ndim > 3 || s.nw < 1 || s.neqpar < 0)
+  // neqpar: the physics' own parameters plus the user's (nspecialpar); a
+  // header asking for more than 1024 is damaged
+  if (!f || s.ndim < 1 || s.ndim > 3 || s.nw < 1 || s.nw > VACGPU_MAXNW || s.neqpar < 0 ||
+      s.neqpar > 1024)
     die("Error in ReadFileIni: bad header line in " + fn);
   s.nx.resize(s.ndim);
   for (auto& v : s.nx) f >> v;
@@ -292,6 +295,7 @@ Snap read_ini_ascii(const std::string& fn) {
     if (!f || v < 1) die("Error in ReadFileIni: bad grid size in " + fn);
   s.eqpar.resize(s.neqpar);
   for (auto& v : s.eqpar) f >> v;
+  if (!f) die("Error in ReadFileIni: bad equation parameters in " + fn);
   std::string line;
   std::getline(f, line);
   std::getline(f, s.varnames);
@@ -359,11 +363,12 @@ int main(int argc, char** argv) {
     return v.empty() ? nullptr : v.back();
   };
   // every assignment of a 1-D array, in file order: "name = v1, v2, ..."
-  // fills from element 1, "name(i) = ..." from element i; elements beyond
-  // the array are ignored
+  // fills from element 1, "name(i) = ..." from element i; values past the
+  // last element are ignored; a subscript outside 1..size, or more than one
+  // subscript, stops the program
   auto fill1 = [&](const std::string& name, size_t size, auto setter) {
     for (auto* a : find_all(name)) {
-      if (!a->idx.empty() && a->idx[0] < 1)
+      if (a->idx.size() > 1 || (!a->idx.empty() && (a->idx[0] < 1 || (size_t)a->idx[0] > size)))
         die("Error in namelist: subscript out of range for " + name);
       size_t o = a->idx.empty() ? 0 : (size_t)(a->idx[0] - 1);
       for (size_t k = 0; k < a->vals.size() && o + k < size; k++) setter(o + k, a->vals[k]);
@@ -422,9 +427,12 @@ int main(int argc, char** argv) {
     if (p != std::string::npos && p + 1 < suf.size()) ndir = suf[p + 1] - '0';
   }
   if (phys.empty()) die("physics unknown: give --physics=mhd or --physics=hd");
+  // the header's ndir digit: a vector has ndim..3 components
+  if (ndir < ini.ndim || ndir > 3)
+    die("Error in ReadFileIni: header " + ini.head + " gives ndir outside ndim..3");
   const int physics = phys == "mhd" ? VACGPU_PHYS_MHD : VACGPU_PHYS_HD;
   const int nw = physics == VACGPU_PHYS_MHD ? 2 + 2 * ndir : 2 + ndir;
-  if (ini.nw != nw) die("Incompatible number of variables in " + fini);
+  if (ini.nw != nw || nw > VACGPU_MAXNW) die("Incompatible number of variables in " + fini);
 
   vacgpu_params p;
   vacgpu_default_params(&p, ini.ndim, ndir, physics, ini.nx.data());
@@ -505,9 +513,15 @@ int main(int argc, char** argv) {
                            "fixed1", "cont1", "grad1", "symm0", "special"};
   for (auto* a : find_all("typeb")) {
     size_t o = 0;
-    for (size_t m = 0; m < a->idx.size(); m++)
-      if (a->idx[m] < 1 || (m == 0 && a->idx.size() == 2 && a->idx[0] > nw))
-        die("Error in namelist: subscript out of range for typeB");
+    // typeB(iw,iB): iw in 1..nw, iB in 1..2*ndim; typeB(q) in 1..nw*2*ndim
+    const size_t nb = (size_t)nw * 2 * ini.ndim;
+    bool bad = a->idx.size() > 2;
+    for (size_t m = 0; m < a->idx.size(); m++) bad = bad || a->idx[m] < 1;
+    if (a->idx.size() == 2)
+      bad = bad || a->idx[0] > nw || a->idx[1] > 2 * ini.ndim;
+    else if (a->idx.size() == 1)
+      bad = bad || (size_t)a->idx[0] > nb;
+    if (bad) die("Error in namelist: subscript out of range for typeB");
     if (a->idx.size() == 2) o = (a->idx[1] - 1) * nw + (a->idx[0] - 1);
     else if (a->idx.size() == 1) o = a->idx[0] - 1;
     for (size_t k = 0; k < a->vals.size(); k++) {
@@ -537,9 +551,14 @@ int main(int argc, char** argv) {
   auto fill2 = [&](const char* nm, auto setter) {
     for (auto* a : find_all(nm)) {
       size_t o = 0;
-      for (size_t m = 0; m < a->idx.size(); m++)
-        if (a->idx[m] < 1 || (m == 0 && a->idx.size() == 2 && a->idx[0] > NSAVE))
-          die(std::string("Error in namelist: subscript out of range for ") + nm);
+      // name(isave,ifile): isave in 1..NSAVE, ifile in 1..2; name(q) in 1..2*NSAVE
+      bool bad = a->idx.size() > 2;
+      for (size_t m = 0; m < a->idx.size(); m++) bad = bad || a->idx[m] < 1;
+      if (a->idx.size() == 2)
+        bad = bad || a->idx[0] > NSAVE || a->idx[1] > 2;
+      else if (a->idx.size() == 1)
+        bad = bad || a->idx[0] > 2 * NSAVE;
+      if (bad) die(std::string("Error in namelist: subscript out of range for ") + nm);
       if (a->idx.size() == 2) o = (a->idx[1] - 1) * NSAVE + (a->idx[0] - 1);
       else if (a->idx.size() == 1) o = a->idx[0] - 1;
       for (size_t k = 0; k < a->vals.size(); k++) setter(o + k, a->vals[k]);
