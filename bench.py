@@ -150,6 +150,49 @@ def cpu_sample(snap, steps, threads):
     return N ** 3 * steps / dt, dt
 
 
+def cpu_serial_config1():
+    """Config 1 in full (Orszag-Tang 200^2, FP64, minmod, 200 steps) by the
+    FP64 oracle port on one core: VAC itself is serial.  Runs in a child
+    process started with OMP_NUM_THREADS=1 (the OpenMP runtime reads it
+    once per process)."""
+    from oracle.oracle import Oracle
+    from vac_gb300 import abi, inistate
+    snap = inistate.orszag_tang(200)
+    p = inistate.params_for(snap, limiter="minmod", bc="periodic", precision=abi.PREC_FP64)
+    o = Oracle(p, snap.x, snap.w)
+    t0 = time.perf_counter()
+    o.step(200)
+    el = time.perf_counter() - t0
+    return {"value": 200 * 200 * 200 / el, "seconds": el}
+
+
+def cpu_serial_subprocess():
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-serial-only"],
+                       capture_output=True, text=True, env=env, timeout=600)
+    if r.returncode != 0:
+        return {"unavailable": r.stderr.strip().splitlines()[-1] if r.stderr else "failed"}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return {"value": d["value"], "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "config 1 in full: Orszag-Tang 200^2, FP64, minmod, 200 steps, "
+                      "FP64 oracle port on 1 core, %.1f s (VAC is serial)" % d["seconds"]}
+
+
+def sweep_traffic(ncell):
+    """DRAM bytes (read + write) of one fused-sweep launch at the bench's
+    256^3 size, from the committed ncu record of that launch
+    (profiles/k_sweep_pair_mhd_256.md, mean of the x, y and z sweeps);
+    (None, reason) if the record is absent."""
+    f = os.path.join(ROOT, "profiles", "k_sweep_pair_mhd_256.md")
+    if os.path.exists(f):
+        for ln in open(f):
+            if ln.startswith("dram_bytes_per_launch_256="):
+                v = float(ln.split("=")[1])
+                return v * ncell / 256 ** 3, ("ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                                              "of 256^3 launches, profiles/k_sweep_pair_mhd_256.md")
+    return None, "no committed 256^3 ncu record"
+
+
 def run_batched(args):
     """Config 3: 64 2-D gamma=1.4 Riemann problems, sides log-uniform in
     [64, 1024], outflow, minmod, mixed precision; all grids advance 50 steps
@@ -173,6 +216,98 @@ def run_batched(args):
             "value": cells * 50 / el, "unit": UNIT,
             "tuned": {"persistent_ctas": ctas, "order": ["round-robin", "grid-major"][order],
                       "trial_ms": ms}}
+
+
+def _errors(wm, w64):
+    """Per variable: relative L1 sum|a-b|/sum|b| and relative Linf
+    max|a-b|/max|b| of the mixed state against the FP64 state."""
+    l1, linf = [], []
+    for i in range(w64.shape[0]):
+        d = np.abs(wm[i] - w64[i])
+        l1.append(float(d.sum() / max(np.abs(w64[i]).sum(), 1e-300)))
+        linf.append(float(d.max() / max(np.abs(w64[i]).max(), 1e-300)))
+    return l1, linf
+
+
+def _physical(w, gamma, mhd):
+    """Minimum density and thermal pressure of an FP64 state."""
+    nd = w.shape[0] - 2 if not mhd else (w.shape[0] - 2) // 2
+    rho = w[0]
+    m2 = sum(w[1 + c] ** 2 for c in range(nd))
+    b2 = sum(w[2 + nd + c] ** 2 for c in range(nd)) if mhd else 0.0
+    p = (gamma - 1.0) * (w[1 + nd] - 0.5 * m2 / rho - 0.5 * b2)
+    return {"min_rho": float(rho.min()), "min_p": float(p.min())}
+
+
+def _fresh_timed(params, snap, k, stream, warm):
+    """A new engine on the seeded state: `warm` untimed steps (graph capture,
+    z-chunk tuning), the state uploaded again (it=0, t=0), then k steps timed
+    with CUDA events on its stream.  Returns (seconds, state after k steps)."""
+    from vac_gb300.engine import Engine
+    e = Engine(params, snap.x, snap.w)
+    e.set_stream(stream.cuda_stream)
+    if warm:
+        e.step(warm)
+        e.upload(snap.w)
+    el = _timed_steps(e, k, stream)
+    w = e.state()
+    e.close()
+    return el, w
+
+
+def fp64_flops_per_cell_update():
+    """FP64 operations per cell-update of the plain path (config 2's 3-D
+    MHD step), from the committed ncu record of its FP64 instruction
+    counts (profiles/fp64_step_mhd_128.md); None if absent."""
+    f = os.path.join(ROOT, "profiles", "fp64_step_mhd_128.md")
+    if os.path.exists(f):
+        for ln in open(f):
+            if ln.startswith("fp64_flops_per_cell_update="):
+                return float(ln.split("=")[1])
+    return None
+
+
+def run_fp64_c2(args, snap, stream, mixed_value):
+    """Config 2 in plain FP64, and the mixed path's error against it: both
+    precisions advance exactly --acc-steps (the config's 100) steps from the
+    same seeded state; the FP64 run is timed over those steps.  The FP64
+    path's own roofline: FP64 FLOP/s against the FP64 pipe's measured
+    throughput, and its HBM fraction."""
+    from vac_gb300 import abi
+    from vac_gb300.engine import measure_fp64_peak
+    k = args.acc_steps
+    ncell = N ** 3
+    el64, w64 = _fresh_timed(make_params(snap, abi.PREC_FP64), snap, k, stream, 1)
+    _, wm = _fresh_timed(make_params(snap, abi.PREC_MIXED), snap, k, stream, 3)
+    l1, linf = _errors(wm, w64)
+    v64 = ncell * k / el64
+    peak = measure_fp64_peak(stream.cuda_stream)
+    fpc = fp64_flops_per_cell_update()
+    hbm = _hbm_peak()
+    roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak / 1e12,
+            "peak_source": "measured: vacgpu_measure_fp64_peak (DFMA chains on every SM, "
+                           "CUDA events)",
+            "flops_per_cell_update": fpc,
+            "flops_source": "ncu FP64 instruction counts of one step "
+                            "(profiles/fp64_step_mhd_128.md)",
+            "hbm_frac": 2 * 3 * NW * 8 * v64 / (hbm * 1e9),
+            "hbm_alg_bytes_per_cell_update": 2 * 3 * NW * 8}
+    if fpc:
+        roof["achieved"] = fpc * v64 / 1e12
+        roof["frac"] = fpc * v64 / peak
+    return {"value": v64, "unit": UNIT, "ms_per_step": el64 / k * 1e3, "steps": k,
+            "mixed_over_fp64": mixed_value / v64,
+            "steps_compared": k, "rel_l1_mixed_vs_fp64": l1, "rel_linf_mixed_vs_fp64": linf,
+            "max_rel_l1": max(l1),
+            "fp64_state_after_steps": _physical(w64, float(snap.eqpar[0]), True),
+            "roofline": roof}
+
+
+def _hbm_peak():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except Exception:
+        return 6800.0
 
 
 def _timed_steps(eng, k, stream):
@@ -222,41 +357,33 @@ def run_plain(args):
 
 def run_blast(args):
     """Config 5: 3-D ideal MHD blast on 512^3 cells, outflow ('cont'),
-    woodward, B=(1,1,0)/sqrt2, p from 10 to 0.1 across r=0.1: mixed
-    precision timed over --blast-steps steps (the fused sweep), FP64 over 2
-    steps, and the mixed-vs-FP64 relative L1 after those 2 steps from the
-    same initial state."""
-    import torch
+    woodward, B=(1,1,0)/sqrt2, p from 10 to 0.1 across r=0.1.  Mixed and
+    FP64 each advance --blast-steps (the config's 100) steps from the same
+    initial state, timed over those steps; the mixed state's relative L1
+    and Linf per variable against the FP64 state after them."""
     from vac_gb300 import abi, inistate
-    from vac_gb300.engine import Engine
+    import torch
     n = args.blast_side
+    k = args.blast_steps
     snap = inistate.blast_3d(n)
     ncell = n ** 3
     stream = torch.cuda.Stream()
-    out = {"workload": "3D ideal MHD blast %d^3, cont, woodward, mixed %d steps timed, "
-                       "FP64 2 steps timed" % (n, args.blast_steps)}
     pm = inistate.params_for(snap, limiter="woodward", bc="cont", precision=abi.PREC_MIXED)
-    em = Engine(pm, snap.x, snap.w)
-    em.set_stream(stream.cuda_stream)
-    em.step(2)
-    wm2 = em.state()
-    em.step(3)
-    el = _timed_steps(em, args.blast_steps, stream)
-    em.close()
-    out["mixed"] = {"steps": args.blast_steps, "ms_per_step": el / args.blast_steps * 1e3,
-                    "value": ncell * args.blast_steps / el, "unit": UNIT}
     p64 = inistate.params_for(snap, limiter="woodward", bc="cont", precision=abi.PREC_FP64)
-    e64 = Engine(p64, snap.x, snap.w)
-    e64.set_stream(stream.cuda_stream)
-    el64 = _timed_steps(e64, 2, stream)
-    w64 = e64.state()
-    e64.close()
-    out["fp64"] = {"steps": 2, "ms_per_step": el64 / 2 * 1e3, "value": ncell * 2 / el64,
-                   "unit": UNIT}
+    elm, wm = _fresh_timed(pm, snap, k, stream, 3)
+    el64, w64 = _fresh_timed(p64, snap, k, stream, 1)
+    l1, linf = _errors(wm, w64)
+    del wm
+    out = {"workload": "3D ideal MHD blast %d^3, cont, woodward, %d steps per precision "
+                       "from the same initial state" % (n, k),
+           "mixed": {"steps": k, "ms_per_step": elm / k * 1e3, "value": ncell * k / elm,
+                     "unit": UNIT},
+           "fp64": {"steps": k, "ms_per_step": el64 / k * 1e3, "value": ncell * k / el64,
+                    "unit": UNIT},
+           "steps_compared": k, "rel_l1_mixed_vs_fp64": l1, "rel_linf_mixed_vs_fp64": linf,
+           "max_rel_l1": max(l1),
+           "fp64_state_after_steps": _physical(w64, float(snap.eqpar[0]), True)}
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
-    out["rel_l1_mixed_vs_fp64_after_2_steps"] = [
-        float(np.abs(wm2[i] - w64[i]).sum() / max(np.abs(w64[i]).sum(), 1e-300))
-        for i in range(w64.shape[0])]
     return out
 
 
@@ -295,62 +422,156 @@ def run_tvdmu(args):
         out[name] = {"steps": k, "ms_per_step": el / k * 1e3, "value": ncell * k / el,
                      "unit": UNIT, "kernel_share": share}
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
-    wm, w64 = res["mixed"], res["fp64"]
-    out["rel_l1_mixed_vs_fp64"] = [
-        float(np.abs(wm[i] - w64[i]).sum() / max(np.abs(w64[i]).sum(), 1e-300))
-        for i in range(w64.shape[0])]
+    out["rel_l1_mixed_vs_fp64"], out["rel_linf_mixed_vs_fp64"] = _errors(res["mixed"],
+                                                                         res["fp64"])
     return out
 
 
-def run_served(args, capacity):
-    """Config 4: a Poisson stream of 2-D (128^2..2048^2) and 3-D (64^3..256^3)
-    random-mode MHD solves, 20..500 steps each, mixed precision, admitted
-    against a 150 GB HBM budget; p50/p99 time to solution."""
-    import threading
-    from vac_gb300 import abi, inistate
-    from vac_gb300.engine import Server
+def random_modes_dev(n, seed, ndim, device):
+    """vac_gb300.inistate.random_modes (p0=0.05, beta ~ 0.1, 8 modes per
+    field) with the fields evaluated by torch on `device`: the same seeded
+    draws in the same order, the same formulas; the result differs from the
+    NumPy evaluation by rounding only.  Returns (x, w) as NumPy arrays in
+    the (ndim|nw, *nx) layout of a snapshot.  The served stream's requests
+    are drawn with it (a NumPy evaluation of a 256^3 state takes tens of
+    seconds of host time)."""
+    import torch
+    from vac_gb300 import inistate
+    rng = np.random.default_rng(seed)
+    nmodes, gamma = 8, 5.0 / 3.0
+    nx = (n,) * ndim
+    x = inistate.domain_grid(nx, (0.0,) * ndim, (1.0,) * ndim)
+    xd = [torch.as_tensor(x[d], device=device) for d in range(ndim)]
+
+    def phase_fields(ks, phis):
+        out = []
+        for k, ph in zip(ks, phis):
+            z = torch.full(nx, complex(np.cos(ph), np.sin(ph)), dtype=torch.complex128,
+                           device=device)
+            for d in range(ndim):
+                z = z * torch.exp(2j * np.pi * float(k[d]) * xd[d])
+            out.append(z.real)
+        return out
+
+    ks = inistate._modes(rng, nmodes, ndim)
+    a = rng.uniform(0.5, 1.0, nmodes)
+    a *= 0.2 / a.sum()
+    cs = phase_fields(ks, rng.uniform(0, 2 * np.pi, nmodes))
+    rho = torch.ones(nx, dtype=torch.float64, device=device)
+    for ak, c in zip(a, cs):
+        rho += float(ak) * c
+    ks = inistate._modes(rng, nmodes, ndim)
+    dirs = rng.normal(size=(nmodes, 3))
+    if ndim == 2:
+        dirs[:, 2] = 0.0
+    cs = phase_fields(ks, rng.uniform(0, 2 * np.pi, nmodes))
+    v = [torch.zeros(nx, dtype=torch.float64, device=device) for _ in range(ndim)]
+    for dvec, c in zip(dirs, cs):
+        for d in range(ndim):
+            v[d] += float(dvec[d]) * c
+    vr = torch.sqrt(torch.mean(sum(vc * vc for vc in v)))
+    v = [vc * (0.3 / vr) for vc in v]
+    ks = inistate._modes(rng, nmodes, ndim)
+    es = rng.normal(size=(nmodes, 3))
+    cs = phase_fields(ks, rng.uniform(0, 2 * np.pi, nmodes))
+    bp = [torch.zeros(nx, dtype=torch.float64, device=device) for _ in range(ndim)]
+    for k, e, c in zip(ks, es, cs):
+        pol = np.cross(e, k)
+        for d in range(ndim):
+            bp[d] += float(pol[d]) * c
+    br = torch.sqrt(torch.mean(sum(bc * bc for bc in bp)))
+    b = [bc * (0.1 / br) for bc in bp]
+    b[0] = b[0] + 1.0
+    v2 = sum(vc * vc for vc in v)
+    b2 = sum(bc * bc for bc in b)
+    e = 0.05 / (gamma - 1) + 0.5 * rho * v2 + 0.5 * b2
+    w = torch.stack([rho] + [rho * vc for vc in v] + [e] + b)
+    return x, w.cpu().numpy()
+
+
+def _served_requests(args):
+    """The request stream of config 4 (seeded): kind, side, step count."""
     rng = np.random.default_rng(7)
     reqs = []
     for i in range(args.served):
         if rng.uniform() < 0.5:
-            n = int(round(np.exp(rng.uniform(np.log(128), np.log(2048)))))
-            s = inistate.random_modes(n, seed=100 + i, ndim=2)
+            n, nd = int(round(np.exp(rng.uniform(np.log(128), np.log(2048))))), 2
         else:
-            n = int(round(np.exp(rng.uniform(np.log(64), np.log(256)))))
-            s = inistate.random_modes(n, seed=100 + i, ndim=3)
-        steps = int(rng.integers(20, 501))
-        p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
-        reqs.append((p, s.x, s.w, steps, int(np.prod(s.w.shape[1:]))))
-    work = [r[4] * r[3] for r in reqs]
-    rate = 0.9 * capacity / np.mean(work)  # offered load ~0.9 of capacity
+            n, nd = int(round(np.exp(rng.uniform(np.log(64), np.log(256))))), 3
+        reqs.append((nd, n, int(rng.integers(20, 501)), 100 + i))
+    return reqs
+
+
+def run_served_rate(args, reqs, rate, arrivals_seed):
+    """One served run: the requests arrive as a Poisson stream of the given
+    mean rate; each is drawn on the device, copied to the host and submitted
+    at its arrival time (the server copies it back on admission).  Per
+    request: time to solution, its queue part (submission to admission) and
+    its service part (admission to result)."""
+    import threading
+    from vac_gb300 import abi, inistate
+    from vac_gb300.engine import Server
+    rng = np.random.default_rng(arrivals_seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
     srv = Server(hbm_budget_bytes=150e9, max_active=8, steps_per_chunk=16)
     ids = [None] * len(reqs)
+    late = [0.0] * len(reqs)
     t0 = time.perf_counter()
 
     def feed():
-        for i, r in enumerate(reqs):
+        for i, (nd, n, steps, seed) in enumerate(reqs):
+            x, w = random_modes_dev(n, seed, nd, "cuda")
+            snap = inistate._snap(x, w, 5.0 / 3.0, True, nd, "served")
+            p = inistate.params_for(snap, limiter="woodward", precision=abi.PREC_MIXED)
             dt = arrivals[i] - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            ids[i] = srv.submit(r[0], r[1], r[2], r[3])
+            late[i] = max(0.0, -dt)
+            ids[i] = srv.submit(p, x, w, steps)
 
     th = threading.Thread(target=feed)
     th.start()
     th.join()
-    tts = []
+    tts, qs, svs = [], [], []
     for rid in ids:
-        res = srv.result(rid, wait=600.0, fetch=False)
+        res = srv.result(rid, wait=1200.0, fetch=False)
         tts.append(res[3])
+        q, sv = srv.timing(rid)
+        qs.append(q)
+        svs.append(sv)
     st = srv.stats()
     srv.close()
-    return {"workload": "Poisson stream of %d MHD solves: 2D 128^2-2048^2 / 3D 64^3-256^3, "
-                        "20-500 steps, random modes, mixed, 150 GB budget" % len(reqs),
-            "requests": len(reqs), "offered_rate_per_s": rate,
-            "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+
+    def pct(a):
+        return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)),
+                "mean": float(np.mean(a))}
+    return {"offered_rate_per_s": rate, "requests": len(reqs),
+            "time_to_solution_s": pct(tts), "queue_s": pct(qs), "service_s": pct(svs),
             "value": st["cell_updates"] / st["span_s"] if st["span_s"] > 0 else None,
             "unit": UNIT, "peak_concurrent": st["peak_active"],
-            "cell_updates": st["cell_updates"], "span_s": st["span_s"]}
+            "cell_updates": st["cell_updates"], "span_s": st["span_s"],
+            "max_submit_lag_s": float(max(late))}
+
+
+def run_served(args, capacity):
+    """Config 4: a Poisson stream of 2-D (128^2..2048^2) and 3-D
+    (64^3..256^3) random-mode MHD solves, 20..500 steps each, mixed
+    precision, admitted against a 150 GB HBM budget, at offered loads of
+    --served-loads times the single-grid capacity (cell-updates/s of the
+    256^3 bench divided by the stream's mean work per request); per load
+    p50/p99 of the time to solution, split into queue and service time,
+    and the aggregate cell-updates/s."""
+    reqs = _served_requests(args)
+    work = np.mean([(n ** nd) * steps for nd, n, steps, _ in reqs])
+    loads = [float(v) for v in args.served_loads.split(",")]
+    runs = []
+    for i, ld in enumerate(loads):
+        runs.append(dict(run_served_rate(args, reqs, ld * capacity / work, 11 + i), load=ld))
+    return {"workload": "Poisson stream of %d MHD solves per load: 2D 128^2-2048^2 / "
+                        "3D 64^3-256^3, 20-500 steps, random modes, mixed, 150 GB budget, "
+                        "8 slots" % len(reqs),
+            "loads": runs, "mean_cell_updates_per_request": float(work),
+            "capacity_cell_updates_per_s": capacity}
 
 
 def run_reference(args, ws, rank):
@@ -390,12 +611,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--served", type=int, default=12, help="requests in the served stream (0: skip)")
+    ap.add_argument("--served", type=int, default=200,
+                    help="requests per offered load in the served stream (0: skip)")
+    ap.add_argument("--served-loads", default="0.5,0.9,1.2",
+                    help="offered loads of the served stream, in units of the capacity")
+    ap.add_argument("--acc-steps", type=int, default=100,
+                    help="steps of config 2's mixed-vs-FP64 accuracy run")
+    ap.add_argument("--no-serial", action="store_true",
+                    help="skip the 1-core CPU baseline (config 1 in full)")
+    ap.add_argument("--cpu-serial-only", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip config 1")
     ap.add_argument("--blast-side", type=int, default=512,
                     help="config 5 cells per side (0: skip)")
-    ap.add_argument("--blast-steps", type=int, default=20)
+    ap.add_argument("--blast-steps", type=int, default=100)
     ap.add_argument("--tvdmu-side", type=int, default=128,
                     help="cells per side of the tvdmu/Roe case (0: skip)")
     ap.add_argument("--tvdmu-steps", type=int, default=10)
@@ -403,6 +632,9 @@ def main():
                     help="cells per side of the cube (smaller cases for profiling)")
     args = ap.parse_args()
     N = args.side
+    if args.cpu_serial_only:
+        print(json.dumps(cpu_serial_config1()), flush=True)
+        return
     ws, rank, lrank = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -454,12 +686,7 @@ def main():
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / avg_s / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic_%s.txt" % dom)
-    if os.path.exists(tf):
-        for ln in open(tf):
-            if ln.startswith("bytes_per_cell="):
-                traffic = float(ln.split("=")[1]) * ncell
+    traffic, traffic_src = sweep_traffic(ncell)
     shares = {k: round(v[1] / sum(x[1] for x in kst.values()), 4) for k, v in kst.items() if v[0]}
 
     # ---- end to end through the C ABI with host buffers
@@ -484,31 +711,10 @@ def main():
     e2e_value, e2e_el = whole_job(ws, ncell * K, time.perf_counter() - t0)
     eng2.close()
 
-    # ---- plain FP64 run of the same steps and the mixed-vs-FP64 error
+    # ---- plain FP64 run and the mixed-vs-FP64 error after the config's steps
     fp64 = None
-    if not args.no_fp64:
-        wm = eng.state()  # mixed state after W + 2K steps
-        e64 = Engine(make_params(snap, abi.PREC_FP64), snap.x, snap.w)
-        e64.set_stream(stream.cuda_stream)
-        e64.step(W)
-        torch.cuda.synchronize()
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        e64.step(K)
-        a1.record(stream)
-        torch.cuda.synchronize()
-        el64 = a0.elapsed_time(a1) / 1e3
-        e64.step(K)
-        w64 = e64.state()
-        rel_l1 = [float(np.abs(wm[i] - w64[i]).sum() / max(np.abs(w64[i]).sum(), 1e-300))
-                  for i in range(NW)]
-        linf = [float(np.abs(wm[i] - w64[i]).max() / max(np.abs(w64[i]).max(), 1e-300))
-                for i in range(NW)]
-        fp64 = {"value": ncell * K / el64, "unit": UNIT, "ms_per_step": el64 / K * 1e3,
-                "mixed_over_fp64": (ncell * K / el) / (ncell * K / el64),
-                "steps_compared": W + 2 * K,
-                "rel_l1_mixed_vs_fp64": rel_l1, "rel_linf_mixed_vs_fp64": linf}
-        e64.close()
+    if not args.no_fp64 and rank == 0:
+        fp64 = run_fp64_c2(args, snap, stream, value / ws)
 
     batched = served = plain = blast = tvdmu = None
     if rank == 0 and not args.no_plain:
@@ -522,7 +728,9 @@ def main():
     if rank == 0 and args.served > 0:
         served = run_served(args, value / ws)
 
-    cpu = None
+    cpu = serial = None
+    if rank == 0 and ws == 1 and not args.no_serial:
+        serial = cpu_serial_subprocess()
     if rank == 0 and ws == 1 and args.cpu_steps > 0:
         threads = os.cpu_count() or 1
         v, t = cpu_sample(snap, args.cpu_steps, threads)
@@ -546,13 +754,15 @@ def main():
                 "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
                              "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                              "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
-                             "traffic": traffic, "avg_launch_ms": avg_s * 1e3,
+                             "traffic": traffic, "traffic_source": traffic_src,
+                             "avg_launch_ms": avg_s * 1e3,
                              "alg_bytes_per_launch": alg_bytes,
                              "kernel_share": shares},
                 "fp64": fp64, "plain_fp64_config1": plain, "blast_config5": blast,
                 "tvdmu_roe": tvdmu,
                 "batched": batched, "served": served,
-                "cpu_baseline": cpu, "clocks": clk.summary()}
+                "cpu_baseline": cpu, "cpu_baseline_serial": serial,
+                "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
     eng.close()
     if ws > 1:

@@ -285,6 +285,55 @@ int vacgpu_register_eta(vacgpu_handle* h, vacgpu_eta_fn fn, void* user);
 int vacgpu_register_source(vacgpu_handle* h, int source_id,
                            const double* params, int nparams);
 
+/* specialsource (src/vac.t:575-605 calls it from addsource2; user routine
+ * src/vacnul.specialsource.t:9-47): the user's source terms
+ * w = w + qdt*S(wCT), added on the mesh cells of box before the physics
+ * sources (resistivity, Powell's div B terms) of the same call.  The engine
+ * calls the hook on the host while it issues a step (also while it captures
+ * a CUDA graph) once per advect1 call: after the Hancock predictor (wCT = the
+ * state, w = the predictor output, qtC = t) and after the corrector
+ * (wCT = the predictor output, w = the new state, qtC = t+dt/2); onestep
+ * schemes ('tvdlf1', 'tvdmu1') call it once with wCT = the state.  dt lives
+ * on the device, so qdt, qtC and qt are device pointers the hook's kernels
+ * read: *qdt = qdt*(idimmax-idimmin+1)/ndim of the call (src/vactvdlf.t:85,
+ * 292), *box.qt = qt = t.  The hook enqueues device work on `stream` that
+ * updates w on the cells of box (the arrays use box's indexing), must not
+ * synchronise, and returns 0 (non-zero fails the call that issued it). */
+typedef struct vacgpu_source_args {
+  vacgpu_region box;       /* the mesh; box.qt: device pointer to qt        */
+  const double* qdt;       /* device: the source's time step                */
+  const double* qtC;       /* device: time of wCT                           */
+  const void* wCT;         /* device: the time-centred state                */
+  void* w;                 /* device, in/out: the state the source updates  */
+} vacgpu_source_args;
+typedef int (*vacgpu_source_fn)(void* user, const vacgpu_source_args* s,
+                                void* stream);
+
+/* getdt_special (src/vac.t:66; user routine
+ * src/vacnul.specialsource.t:50-71): the user's time-step limit.  Called
+ * like the source hook, once per step before the step's dt is chosen
+ * (unless dtpar > 0, when the step uses dtpar and the limit is not read);
+ * it enqueues device work that stores its limit dt_mine in *dt (which the
+ * engine sets to 1e99 before the call), and the step takes
+ * dt = min(dt, dt_mine) after the CFL and resistive limits, as the
+ * reference's "dt=min(dt,dt_mine)".  w: the state at the start of the
+ * step on box (the mesh). */
+typedef struct vacgpu_dtspecial_args {
+  vacgpu_region box;
+  const void* w;           /* device: the state                             */
+  double* dt;              /* device, out: the user's dt limit              */
+} vacgpu_dtspecial_args;
+typedef int (*vacgpu_dtspecial_fn)(void* user, const vacgpu_dtspecial_args* a,
+                                   void* stream);
+
+/* Install the user's specialsource and getdt_special hooks (either may be
+ * NULL; both NULL removes them).  They replace a built-in source of
+ * vacgpu_register_source.  A grid with a source hook runs the split
+ * predictor/corrector kernels (the hook reads the predictor output from
+ * device memory). */
+int vacgpu_register_source_fn(vacgpu_handle* h, vacgpu_source_fn src,
+                              vacgpu_dtspecial_fn dt, void* user);
+
 /* Run the handle's work on the caller's CUDA stream (a cudaStream_t passed
  * as void*; NULL returns to the handle's own stream).  No counterpart in the
  * reference (VAC has no device); it lets a host order the engine's kernels
@@ -371,6 +420,12 @@ int vacgpu_server_submit(vacgpu_server* s, const vacgpu_params* p,
  * waiting up to wait_s seconds; other nonzero: the solve failed. */
 int vacgpu_server_result(vacgpu_server* s, long long id, double wait_s,
                          double* w, double* t, int* it, double* tts);
+/* The time-to-solution of a finished solve split in two: queue_s from
+ * submission to admission (waiting for a slot or for device memory),
+ * service_s from admission (device allocation, upload, steps, download)
+ * to the result.  0: finished; 1: not finished yet; other: error. */
+int vacgpu_server_timing(vacgpu_server* s, long long id, double* queue_s,
+                         double* service_s);
 /* Queue length, running solves, finished solves, the largest number of
  * solves that ran at once, cell updates of finished solves and the time
  * from the first submission to the last completion. */
@@ -437,6 +492,13 @@ int vacgpu_last_error(char* buf, int len);
 
 /* Library version string. */
 const char* vacgpu_version(void);
+
+/* Diagnostic (no counterpart in the reference): the FP64 throughput of this
+ * GPU's FP64 pipe, measured by timing a kernel of independent FP64
+ * fused multiply-add chains on every SM with CUDA events on the given
+ * stream (NULL: legacy default stream).  *flops_per_s receives 2 x DFMA/s.
+ * The denominator of the plain FP64 path's FP64-pipe roofline. */
+int vacgpu_measure_fp64_peak(double* flops_per_s, void* stream);
 
 #ifdef __cplusplus
 }

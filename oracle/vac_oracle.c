@@ -81,6 +81,16 @@ typedef struct vo_state {
                  const int* hi, const long* st, long N,
                  const double* const* x, int idirmin, double t);
   void* eta_user;
+  /* specialsource hook (src/vacnul.specialsource.t:9-47): w += qdt*S(wCT)
+   * on box lo..hi, wCT at time qtC, w at qt; and getdt_special
+   * (src/vacnul.specialsource.t:50-71): the user's dt limit from w */
+  void (*src_fn)(void* user, double qdt, double qtC, const double* wCT,
+                 double qt, double* w, const int* lo, const int* hi,
+                 const long* st, long N, const double* const* x);
+  double (*dtsp_fn)(void* user, const double* w, const int* lo, const int* hi,
+                    const long* st, long N, const double* const* x);
+  void* src_user;
+  double qtc;         /* qtC of the advect1 call in progress */
   double* eta;        /* eta(ixG^T) of the common block */
   double* gradeta[3];
 } vo_state;
@@ -718,7 +728,13 @@ static void addsource_res1(vo_state* s, double qdt, box ixO, const double* w,
  * terms, src/vacphys.mhd0.t:223-230, then Powell) */
 static void addsource2(vo_state* s, double qdt, box ixO, const double* wCT,
                        double* w) {
-  if (s->src_id == VACGPU_SRC_GRAVITY) addsource_grav(s, qdt, ixO, wCT, w);
+  if (s->src_fn) {
+    const double* x[3] = {W(s->x, 0), W(s->x, s->ndim > 1 ? 1 : 0),
+                          W(s->x, s->ndim > 2 ? 2 : 0)};
+    s->src_fn(s->src_user, qdt, s->qtc, wCT, s->t, w, ixO.lo, ixO.hi, s->st, s->N, x);
+  } else if (s->src_id == VACGPU_SRC_GRAVITY) {
+    addsource_grav(s, qdt, ixO, wCT, w);
+  }
   if (s->mhd && fabs(s->p.eqpar[1]) > SMALLDOUBLE) {
     if (s->p.compactres)
       addsource_res1(s, qdt, ixO, wCT, w);
@@ -1720,11 +1736,15 @@ static void advect1(vo_state* s, int pred, double qdt, int idimmin,
 static void advect(vo_state* s, int idimmin, int idimmax) {
   memcpy(s->w1, s->w, sizeof(double) * s->N * s->nw);
   s->istep = 0;
+  /* qtC of each advect1 call (src/vac.t:407,426-427) */
   if (s->p.typefull == VACGPU_TVDLF1 || s->p.typefull == VACGPU_TVDMU1) {
+    s->qtc = s->t;
     advect1(s, 0, s->dt, idimmin, idimmax, s->w1, s->w);
     return;
   }
+  s->qtc = s->t;
   advect1(s, 1, s->dt / 2, idimmin, idimmax, s->w, s->w1);
+  s->qtc = s->t + s->dt / 2;
   advect1(s, 0, s->dt, idimmin, idimmax, s->w1, s->w);
 }
 
@@ -1809,8 +1829,16 @@ static void getdt_res(vo_state* s) {
   if (dtdiff < s->dt) s->dt = dtdiff;
 }
 
-/* getdt_grav, vacusr.gravity.t (dt limit of the gravity hook) */
+/* getdt_special: the user hook's dt=min(dt,dt_mine), or getdt_grav,
+ * vacusr.gravity.t (dt limit of the gravity hook) */
 static void getdt_special(vo_state* s) {
+  if (s->dtsp_fn) {
+    const double* x[3] = {W(s->x, 0), W(s->x, s->ndim > 1 ? 1 : 0),
+                          W(s->x, s->ndim > 2 ? 2 : 0)};
+    double d = s->dtsp_fn(s->src_user, s->w, s->ixM.lo, s->ixM.hi, s->st, s->N, x);
+    if (d < s->dt) s->dt = d;
+    return;
+  }
   if (s->src_id != VACGPU_SRC_GRAVITY) return;
   if (s->it == s->itmin) {
     s->dtgrav = BIGDOUBLE;
@@ -2083,6 +2111,21 @@ void vo_register_eta(vo_state* s,
                      void* user) {
   s->eta_fn = fn;
   s->eta_user = user;
+}
+
+/* the user's specialsource and getdt_special (either may be NULL); they
+ * replace a built-in source */
+void vo_register_source_fn(
+    vo_state* s,
+    void (*src)(void*, double, double, const double*, double, double*, const int*,
+                const int*, const long*, long, const double* const*),
+    double (*dtsp)(void*, const double*, const int*, const int*, const long*, long,
+                   const double* const*),
+    void* user) {
+  s->src_fn = src;
+  s->dtsp_fn = dtsp;
+  s->src_user = user;
+  if (src || dtsp) s->src_id = VACGPU_SRC_NONE;
 }
 
 void vo_register_source(vo_state* s, int id, const double* par, int npar) {

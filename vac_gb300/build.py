@@ -35,8 +35,10 @@ UNITS = [
     ("vacgpu.cu", []),
     ("noalloc.cu", []),
     ("sweep_fused.cu", ["--use_fast_math"]),
+    ("sweep_pair.cu", ["--use_fast_math"]),
     ("batch.cu", ["--use_fast_math"]),
     ("server.cu", []),
+    ("diag.cu", []),
 ]
 
 

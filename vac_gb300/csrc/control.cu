@@ -134,8 +134,10 @@ __device__ void dt_end_dev(Ctrl* c, const DtEndArgs& p) {
     } else if (c->dtdiff < dt) {
       dt = c->dtdiff;
     }
-    // getdt_special (uniform gravity: dtgrav fixed at the first step)
+    // getdt_special (uniform gravity: dtgrav fixed at the first step; the
+    // user's hook: its limit of this step)
     if (c->dtgrav < dt) dt = c->dtgrav;
+    if (c->dtspecial < dt) dt = c->dtspecial;
     if (p.dtcantgrow && c->it > c->itmin && c->dtold < dt) dt = c->dtold;
     c->dtold = dt;
   }
@@ -241,6 +243,22 @@ __global__ void kb_call_begin(Ctrl* const* cs, int maxsteps, double tstop) {
     c->tstop = tstop;
   }
 }
+
+// the arguments of a specialsource hook call, in the reference's double
+// arithmetic: qdt*(idimmax-idimmin+1)/ndim with qdt = dt/2 (predictor) or
+// dt, and qtC = t or t+dt/2 (src/vac.t:407,426-427, src/vactvdlf.t:85,292)
+__global__ void k_src_args(Ctrl* c, int pred, int half, int nsweep, int ndim) {
+  if (c->done) return;
+  const double qdt = pred ? c->dt / 2 : c->dt;
+  c->src_qdt = qdt * (double)nsweep / ndim;
+  c->src_qtc = half ? c->t + c->dt / 2 : c->t;
+}
+__global__ void k_dtspecial_begin(Ctrl* c) { c->dtspecial = BIG; }
+
+void launch_src_args(Ctrl* c, int pred, int half, int nsweep, int ndim, cudaStream_t st) {
+  k_src_args<<<1, 1, 0, st>>>(c, pred, half, nsweep, ndim);
+}
+void launch_dtspecial_begin(Ctrl* c, cudaStream_t st) { k_dtspecial_begin<<<1, 1, 0, st>>>(c); }
 
 void launch_dt_begin(Ctrl* c, int ndim, cudaStream_t st) {
   k_dt_begin<<<1, NSLOT, 0, st>>>(c, ndim);

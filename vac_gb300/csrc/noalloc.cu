@@ -180,10 +180,16 @@ extern "C" int vacgpu_sweep_noalloc(const vacgpu_params* p, const double* w,
 
   cudaStream_t st = (cudaStream_t)stream;
   k_na_begin<<<1, NSLOT, 0, st>>>(a.ctrl, dt, p->smallp);
-  launch_predict_fp64(s, w, a.w1, st);
-  launch_ghost_fp64(s, a.w1, st);
-  const double* base = p->typelimited == VACGPU_LIMITED_PREDICTOR ? a.w1 : w;
-  launch_correct_fp64(s, w, a.w1, base, wout, st);
+  if (p->typefull == VACGPU_TVDLF1) {
+    // onestep (typepred1='nul'): the corrector alone with wCT = w and no
+    // limiter (src/vacio.t:286-299,511)
+    launch_correct_fp64(s, w, w, w, wout, st);
+  } else {
+    launch_predict_fp64(s, w, a.w1, st);
+    launch_ghost_fp64(s, a.w1, st);
+    const double* base = p->typelimited == VACGPU_LIMITED_PREDICTOR ? a.w1 : w;
+    launch_correct_fp64(s, w, a.w1, base, wout, st);
+  }
   launch_ghost_fp64(s, wout, st);
   if (courantmax) k_na_end<<<1, NSLOT, 0, st>>>(a.ctrl, idim, courantmax);
   cudaError_t e = cudaGetLastError();

@@ -949,7 +949,7 @@ struct RoeSweep {
           }
       }
     }
-    if (a.ph.sourceunsplit) {
+    if (a.ph.sourceunsplit && !a.ph.src_hook) {
       R wc[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);

@@ -44,6 +44,7 @@ struct Req {
   std::vector<double> x, w;
   int nsteps;
   double t_submit;
+  double t_admit = 0.0;  // device work (allocation, upload) begins
   size_t bytes;
   vacgpu_handle* h = nullptr;
   cudaEvent_t ev = nullptr;
@@ -115,6 +116,7 @@ void finish(vacgpu_server* s, Req* r, bool ok, const std::string& err) {
 
 bool admit_one(Req* r) {
   char buf[512];
+  r->t_admit = now_s();
   if (vacgpu_create(&r->p, &r->h) || vacgpu_set_grid(r->h, r->x.data()) ||
       vacgpu_upload(r->h, r->w.data(), 0, 0.0)) {
     vacgpu_last_error(buf, sizeof buf);
@@ -265,6 +267,19 @@ int vacgpu_server_result(vacgpu_server* s, long long id, double wait_s,
   if (t) *t = r->t_sim;
   if (it) *it = r->it;
   if (tts) *tts = r->t_done - r->t_submit;
+  return 0;
+}
+
+int vacgpu_server_timing(vacgpu_server* s, long long id, double* queue_s,
+                         double* service_s) {
+  if (!s) return vacgpu_internal_fail("null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto f = s->all.find(id);
+  if (f == s->all.end()) return vacgpu_internal_fail("unknown request id");
+  Req* r = f->second;
+  if (r->state < 2) return 1;
+  if (queue_s) *queue_s = r->t_admit - r->t_submit;
+  if (service_s) *service_s = r->t_done - r->t_admit;
   return 0;
 }
 

@@ -399,7 +399,7 @@ struct Sweep {
         predict_dir<(NDIM > 2 ? 2 : 0)>(a, w, off, st, c, qdt, smallp, u, pc,
                                         acc);
     }
-    if (a.ph.sourceunsplit) {
+    if (a.ph.sourceunsplit && !a.ph.src_hook) {
       // the round-tripped state (useprimitive) leaves rho and B unchanged
       if (a.ph.useprim) {
         to_cons(a, pc);
@@ -563,7 +563,7 @@ struct Sweep {
       for (int iw = 0; iw < NW; iw++)
         acc[iw] = acc[iw] - cq * (F[iw * nf + fp] - F[iw * nf + fm]);
     }
-    if (a.ph.sourceunsplit) {
+    if (a.ph.sourceunsplit && !a.ph.src_hook) {
       R wc[NW];
 #pragma unroll
       for (int iw = 0; iw < NW; iw++) wc[iw] = R(w1[off + iw * vs]);
@@ -572,6 +572,33 @@ struct Sweep {
     }
 #pragma unroll
     for (int iw = 0; iw < NW; iw++) wout[off + iw * vs] = T(acc[iw]);
+  }
+
+  // addsource (src/vac.t:575-605 after specialsource) as a pass of its own
+  // when the user's specialsource hook runs between the flux update and
+  // it: w += addsource(wCT) on the mesh, with the operations the predictor
+  // (pred) or corrector kernel performs in place otherwise.
+  static __device__ void source_pass(const SweepArgs& a, const T* __restrict__ wct,
+                                     T* __restrict__ w, int pred) {
+    const Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) return;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.g.ncell) return;
+    int c[3];
+    cell_coords(a.g, n, c);
+    const long long off = gidx(a.g, c[0], c[1], c[2]);
+    const long long st[3] = {1, a.g.P, a.g.plane};
+    const long long vs = a.g.vs;
+    const double qdt = pred ? ctrl->dt / 2 : ctrl->dt;
+    R acc[NW], wc[NW];
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) {
+      acc[iw] = R(w[off + iw * vs]);
+      wc[iw] = R(wct[off + iw * vs]);
+    }
+    add_sources(a, src_qdt(a, qdt), wc, wct + off, st, c, acc);
+#pragma unroll
+    for (int iw = 0; iw < NW; iw++) w[off + iw * vs] = T(acc[iw]);
   }
 
   // getpthermal's one-time smallp: min/max of the unclipped pressure on the
@@ -989,6 +1016,13 @@ void launch_face_dir(const SweepArgs& a, const typename PH::T* w1,
 
 template <class PH, int NDIM, int NDIR, bool MHD>
 __global__ void __launch_bounds__(128)
+    k_source_pass(SweepArgs a, const typename PH::T* __restrict__ wct,
+                  typename PH::T* __restrict__ w, int pred) {
+  Sweep<PH, NDIM, NDIR, MHD>::source_pass(a, wct, w, pred);
+}
+
+template <class PH, int NDIM, int NDIR, bool MHD>
+__global__ void __launch_bounds__(128)
     k_correct(SweepArgs a, const typename PH::T* __restrict__ w,
               const typename PH::T* __restrict__ w1,
               typename PH::T* __restrict__ wout) {
@@ -1076,6 +1110,13 @@ struct Launch {
     }
     const unsigned nb = grid_for(a.g.ncell, 128);
 #define KC(D, C, M) k_correct<PH, D, C, M><<<nb, 128, 0, st>>>(a, w, w1, wout)
+    VACGPU_DISPATCH(a, KC);
+#undef KC
+  }
+  static void source_pass(const SweepArgs& a, const T* wct, T* w, int pred,
+                          cudaStream_t st) {
+    const unsigned nb = grid_for(a.g.ncell, 128);
+#define KC(D, C, M) k_source_pass<PH, D, C, M><<<nb, 128, 0, st>>>(a, wct, w, pred)
     VACGPU_DISPATCH(a, KC);
 #undef KC
   }
@@ -1199,6 +1240,10 @@ struct Launch {
   }                                                                          \
   void launch_ghost_##SUF(const SweepArgs& s, PH::T* w, cudaStream_t st) {   \
     Launch<PH>::ghost(s, w, st);                                             \
+  }                                                                          \
+  void launch_source_pass_##SUF(const SweepArgs& s, const PH::T* wct,        \
+                                PH::T* w, int pred, cudaStream_t st) {       \
+    Launch<PH>::source_pass(s, wct, w, pred, st);                            \
   }                                                                          \
   void launch_pminmax_##SUF(const SweepArgs& s, const PH::T* w,              \
                             cudaStream_t st) {                               \

@@ -151,6 +151,9 @@ struct vacgpu_handle {
   bool faulted;
   vacgpu_eta_fn eta_fn;  // specialeta hook (eqpar(eta_) < 0)
   void* eta_user;
+  vacgpu_source_fn src_fn;       // the user's specialsource
+  vacgpu_dtspecial_fn dtsp_fn;   // the user's getdt_special
+  void* src_user;
   double* etaf;      // its eta field, gradeta (compactres) and the current
   double* gradetaf[3];
   double* curf[3];
@@ -410,6 +413,58 @@ void eta_hook(vacgpu_handle* h, const SweepArgs& a, const void* w, int first_onl
   kend(h);
 }
 
+// the mesh of the state as a hook region
+static void mesh_region(const vacgpu_handle* h, vacgpu_region& r) {
+  const DevGrid& g = h->g;
+  memset(&r, 0, sizeof(r));
+  r.iB = -1;
+  for (int d = 0; d < 3; d++) {
+    r.lo[d] = d < g.ndim ? 2 : 0;
+    r.hi[d] = d < g.ndim ? g.nx[d] + 1 : 0;
+    r.nx[d] = g.nx[d];
+    r.nG[d] = g.nG[d];
+    r.x[d] = h->xg[d];
+  }
+  r.offset0 = g.xpad;
+  r.stride[0] = 1;
+  r.stride[1] = g.P;
+  r.stride[2] = g.plane;
+  r.var_stride = g.vs;
+  r.elem = (int)h->elem;
+  r.qt = &h->ctrl->t;
+}
+
+// addsource2 with the user's specialsource (src/vac.t:575-605): the hook,
+// then addsource as a pass of its own (the predictor and corrector kernels
+// leave it out while a hook is installed).  pred: after the Hancock
+// predictor (qdt = dt/2); half: qtC = t+dt/2 (the corrector of twostep).
+template <typename T>
+void source_hook(vacgpu_handle* h, const SweepArgs& a, int pred, int half, const T* wct,
+                 T* w) {
+  if (!h->src_fn || !h->p.sourceunsplit) return;
+  kbegin(h, VACGPU_K_CONTROL);
+  launch_src_args(h->ctrl, pred, half, a.d1 - a.d0 + 1, h->p.ndim, h->st);
+  kend(h);
+  vacgpu_source_args s;
+  memset(&s, 0, sizeof(s));
+  mesh_region(h, s.box);
+  s.qdt = &h->ctrl->src_qdt;
+  s.qtC = &h->ctrl->src_qtc;
+  s.wCT = wct;
+  s.w = w;
+  if (h->src_fn(h->src_user, &s, (void*)h->st)) h->hook_failed = true;
+  kbegin(h, pred ? VACGPU_K_PREDICT : VACGPU_K_CORRECT);
+  if (sizeof(T) == 8)
+    launch_source_pass_fp64(a, (const double*)wct, (double*)w, pred, h->st);
+  else if (h->pmode == 1)
+    launch_source_pass_mixedf64(a, (const float*)wct, (float*)w, pred, h->st);
+  else if (h->pmode == 2)
+    launch_source_pass_mixedf32(a, (const float*)wct, (float*)w, pred, h->st);
+  else
+    launch_source_pass_mixed(a, (const float*)wct, (float*)w, pred, h->st);
+  kend(h);
+}
+
 template <typename T>
 void run_sweep(vacgpu_handle* h, int d0, int d1) {
   SweepArgs a = make_args(h, d0, d1);
@@ -456,6 +511,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
       launch_correct_mixed(a, (const float*)w, (const float*)w,
                            (const float*)w, (float*)wout, h->st);
     kend(h);
+    source_hook<T>(h, a, 0, 0, w, wout);
     if (h->p.smallfix) {
       kbegin(h, VACGPU_K_GHOST);
       if (sizeof(T) == 8)
@@ -472,6 +528,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
     kbegin(h, VACGPU_K_PREDICT);
     launch_predict_fp64(a, (const double*)w, (double*)w1, h->st);
     kend(h);
+    source_hook<T>(h, a, 1, 0, w, w1);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)w1, h->st);
     fill_ghosts(h, a, w1, 1, 1);
@@ -485,11 +542,12 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
       launch_correct_fp64(a, (const double*)wc, (const double*)w1,
                           (const double*)base, (double*)wout, h->st);
     kend(h);
+    source_hook<T>(h, a, 0, 1, (const T*)w1, wout);
     kbegin(h, VACGPU_K_GHOST);
     if (h->p.smallfix) launch_keeppositive_fp64(a, (double*)wout, h->st);
     fill_ghosts(h, a, wout, 1, 2);
     kend(h);
-  } else if (h->fused && h->pmode == 0 && d0 == d1) {
+  } else if (h->fused && h->pmode == 0 && d0 == d1 && !h->src_fn) {
     kbegin(h, VACGPU_K_SWEEP);
     // the fused sweep also writes the ghost cells of its output
     launch_sweep_fused(a, &h->tmap[h->cur][d0 == 1], (float*)wout, h->idxf, h->nzc,
@@ -506,6 +564,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   kbegin(h, VACGPU_K_PREDICT);                          \
   launch_predict_##SUF(a, fw, fw1, h->st);              \
   kend(h);                                              \
+  source_hook<T>(h, a, 1, 0, w, w1);                    \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fw1, h->st); \
   fill_ghosts(h, a, fw1, 1, 1);                         \
@@ -517,6 +576,7 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   else                                                  \
     launch_correct_##SUF(a, fwc, fw1, fb, fo, h->st);   \
   kend(h);                                              \
+  source_hook<T>(h, a, 0, 1, (const T*)w1, wout);       \
   kbegin(h, VACGPU_K_GHOST);                            \
   if (h->p.smallfix) launch_keeppositive_##SUF(a, fo, h->st); \
   fill_ghosts(h, a, fo, 1, 2);                          \
@@ -562,6 +622,18 @@ void run_step(vacgpu_handle* h, int parity_odd) {
   }
   // getdt_res with the specialeta field: eta from the state at it==itmin
   eta_hook(h, a, w, 1);
+  // getdt_special: the user's limit of this step from the state
+  if (h->dtsp_fn) {
+    kbegin(h, VACGPU_K_CONTROL);
+    launch_dtspecial_begin(h->ctrl, h->st);
+    kend(h);
+    vacgpu_dtspecial_args d;
+    memset(&d, 0, sizeof(d));
+    mesh_region(h, d.box);
+    d.w = w;
+    d.dt = &h->ctrl->dtspecial;
+    if (h->dtsp_fn(h->src_user, &d, (void*)h->st)) h->hook_failed = true;
+  }
   kbegin(h, VACGPU_K_CONTROL);
   launch_dt_end(h->ctrl, p, h->st);
   kend(h);
@@ -829,6 +901,23 @@ size_t vacgpu_internal_device_bytes(const vacgpu_params* p) {
 
 extern "C" {
 
+// split corrector: per sweep direction the faces' fluxes (and, for the Roe
+// dissipation, R(iw,il)*phi(il) of every wave)
+static int alloc_faces(vacgpu_handle* h) {
+  const vacgpu_params* p = &h->p;
+  const DevGrid& g = h->g;
+  const bool roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
+  const long long K = roe ? (long long)h->nw * (h->nw + 1) : h->nw;
+  long long mf = 0;
+  for (int d = 0; d < p->ndim; d++)
+    if (face_count(g, d) > mf) mf = face_count(g, d);
+  h->face_stride = K * mf;
+  const int nsw = p->dimsplit ? 1 : p->ndim;
+  if (cudaMalloc(&h->faces, h->elem * (size_t)h->face_stride * nsw) != cudaSuccess)
+    return fail("device allocation of the corrector's face buffer failed");
+  return 0;
+}
+
 void vacgpu_default_params(vacgpu_params* p, int ndim, int ndir, int physics,
                            const int* nx) {
   memset(p, 0, sizeof(*p));
@@ -1036,20 +1125,9 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
       return fail("TMA descriptor set-up failed");
     }
   }
-  if (h->elem == 8 || !h->fused || h->pmode != 0) {
-    // split corrector: per sweep direction the faces' fluxes (and, for the
-    // Roe dissipation, R(iw,il)*phi(il) of every wave)
-    const bool roe = p->typefull == VACGPU_TVDMU || p->typefull == VACGPU_TVDMU1;
-    const long long K = roe ? (long long)h->nw * (h->nw + 1) : h->nw;
-    long long mf = 0;
-    for (int d = 0; d < p->ndim; d++)
-      if (face_count(g, d) > mf) mf = face_count(g, d);
-    h->face_stride = K * mf;
-    const int nsw = p->dimsplit ? 1 : p->ndim;
-    if (cudaMalloc(&h->faces, h->elem * (size_t)h->face_stride * nsw) != cudaSuccess) {
-      vacgpu_destroy(h);
-      return fail("device allocation of the corrector's face buffer failed");
-    }
+  if ((h->elem == 8 || !h->fused || h->pmode != 0) && alloc_faces(h)) {
+    vacgpu_destroy(h);
+    return 1;
   }
   Ctrl c;
   memset(&c, 0, sizeof(c));
@@ -1058,6 +1136,7 @@ int vacgpu_create(const vacgpu_params* p, vacgpu_handle** out) {
   c.courantpar = courantpar;
   c.smallp = p->smallp;
   c.dtgrav = BIGD;
+  c.dtspecial = BIGD;
   c.dtdiff = BIGD;
   for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
   c.tstop = 1e300;
@@ -1189,6 +1268,7 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t) {
   for (int d = 0; d < 3; d++) c.dtcourant[d] = BIGD;
   for (int i = 0; i < 4; i++) c.nerror[i] = 0;
   c.dtgrav = h->dtgrav > 0 ? h->dtgrav : BIGD;
+  c.dtspecial = BIGD;
   c.dtdiff = h->have_grid ? h->dtdiff : BIGD;
   c.cur = 0;
   c.fault = 0;
@@ -1265,7 +1345,7 @@ int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
       h->hook_failed = false;
       drop_graphs(h);
       CK(cudaStreamSynchronize(h->st));
-      return fail("a user hook (specialbound or specialeta) failed");
+      return fail("a user hook (specialbound, specialeta, specialsource or getdt_special) failed");
     }
     int done = 0;
     CK(cudaMemcpyAsync(&done, &h->ctrl->done, sizeof(int),
@@ -1369,6 +1449,29 @@ int vacgpu_register_source(vacgpu_handle* h, int source_id,
   }
   double v = h->dtgrav;
   CK(cudaMemcpy(&h->ctrl->dtgrav, &v, sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int vacgpu_register_source_fn(vacgpu_handle* h, vacgpu_source_fn src,
+                              vacgpu_dtspecial_fn dt, void* user) {
+  if (!h) return fail("null handle");
+  if (src && h->ph.useprim)
+    return fail("a specialsource hook with useprimitive is not supported");
+  if (h->st) CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);
+  if (src && !h->faces && alloc_faces(h)) return 1;
+  h->src_fn = src;
+  h->dtsp_fn = dt;
+  h->src_user = user;
+  h->ph.src_hook = src != nullptr;
+  if (src) h->tuning = false;  // the split kernels run; no z chunk to tune
+  if (src || dt) {
+    // the hooks replace a built-in source
+    h->ph.src_id = VACGPU_SRC_NONE;
+    h->dtgrav = BIGD;
+    double v = BIGD;
+    CK(cudaMemcpy(&h->ctrl->dtgrav, &v, sizeof(double), cudaMemcpyHostToDevice));
+  }
   return 0;
 }
 

@@ -59,6 +59,9 @@ struct DevPhys {
   double eta;            // resistivity eqpar(eta_) (0: ideal MHD)
   int compactres;        // resistive source in the Laplacian form
   int src_id;
+  // a user specialsource hook runs between the flux update and addsource:
+  // the predictor/corrector kernels leave the sources to k_add_sources
+  int src_hook;
   double src_par[VACGPU_MAXSRCPAR];
   // Boundary index map per face [dim][lo/hi] when every variable shares it:
   // GMAP_PERIODIC, GMAP_CONT or GMAP_MIRROR ('symm' and 'asymm'); GMAP_MIXED
@@ -124,6 +127,8 @@ struct Ctrl {
   double t, dt, dtold, dtpar, courantpar;
   double smallp;
   double dtgrav;
+  double dtspecial;   // the user's getdt_special limit of this step (BIG: none)
+  double src_qdt, src_qtc;  // qdt and qtC of the source call being issued
   double dtdiff;      // resistive diffusion dt limit (BIG without resistivity)
   double qt;          // time of the current ghost fill (specialbound hooks)
   // specialeta: max over the mesh of eta/dx_d^2 (ordered keys), of the
@@ -242,6 +247,8 @@ struct SweepArgs {
   void launch_correct_##SUF(const SweepArgs& s, const T* w, const T* w1,     \
                             const T* base, T* wout, cudaStream_t st);        \
   void launch_ghost_##SUF(const SweepArgs& s, T* w, cudaStream_t st);        \
+  void launch_source_pass_##SUF(const SweepArgs& s, const T* wct, T* w,     \
+                                int pred, cudaStream_t st);                  \
   void launch_pminmax_##SUF(const SweepArgs& s, const T* w, cudaStream_t st); \
   void launch_cell_cmax_##SUF(const SweepArgs& s, const T* w,                \
                               cudaStream_t st);                              \
@@ -290,6 +297,11 @@ void launch_kp_begin(Ctrl* c, int rho_floor, cudaStream_t st);
 void launch_kp_smallrho(Ctrl* c, double coeff, cudaStream_t st);
 void launch_kp_end(Ctrl* c, cudaStream_t st);
 void launch_dt_end(Ctrl* c, const vacgpu_params& p, cudaStream_t st);
+// the user source hook's call arguments: qdt = (pred ? dt/2 : dt) *
+// (d1-d0+1)/ndim, qtC = t (+dt/2 for the corrector, pred = 0, half = 1)
+void launch_src_args(Ctrl* c, int pred, int half, int nsweep, int ndim, cudaStream_t st);
+// getdt_special: Ctrl::dtspecial = BIG before the user's dt hook
+void launch_dtspecial_begin(Ctrl* c, cudaStream_t st);
 // qt of a ghost fill: mode 0 t, 1 t+dt/2, 2 t+dt (src/vac.t:54,567)
 void launch_set_qt(Ctrl* c, int mode, cudaStream_t st);
 // specialeta: Ctrl::etak from the field (first_only: at it==itmin only)

@@ -24,8 +24,8 @@ SYMBOLS = [
     "vacgpu_batch_create", "vacgpu_batch_set_grid", "vacgpu_batch_upload",
     "vacgpu_batch_download", "vacgpu_batch_step", "vacgpu_batch_status",
     "vacgpu_batch_tune", "vacgpu_batch_destroy", "vacgpu_server_create",
-    "vacgpu_server_submit", "vacgpu_server_result", "vacgpu_server_stats",
-    "vacgpu_server_destroy",
+    "vacgpu_server_submit", "vacgpu_server_result", "vacgpu_server_timing",
+    "vacgpu_server_stats", "vacgpu_server_destroy", "vacgpu_measure_fp64_peak",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
@@ -79,7 +79,9 @@ def lib():
         L.vacgpu_server_submit.argtypes = [vp, C.POINTER(abi.VacParams), dp, dp, C.c_int,
                                            C.POINTER(C.c_longlong)]
         L.vacgpu_server_result.argtypes = [vp, C.c_longlong, C.c_double, dp, dp, ip, dp]
+        L.vacgpu_server_timing.argtypes = [vp, C.c_longlong, dp, dp]
         L.vacgpu_server_stats.argtypes = [vp, ip, ip, ip, ip, dp, dp]
+        L.vacgpu_measure_fp64_peak.argtypes = [dp, vp]
         L.vacgpu_server_destroy.argtypes = [vp]
         L.vacgpu_server_destroy.restype = None
         _lib = L
@@ -264,6 +266,13 @@ class Batch:
             pass
 
 
+def measure_fp64_peak(stream_ptr=None):
+    """FP64-pipe throughput of the current GPU, FLOP/s (2 x DFMA/s)."""
+    v = C.c_double()
+    _ck(lib().vacgpu_measure_fp64_peak(C.byref(v), stream_ptr), "vacgpu_measure_fp64_peak")
+    return v.value
+
+
 class Server:
     """Continuous-batching solve server (vacgpu_server_*)."""
 
@@ -298,6 +307,15 @@ class Server:
         if fetch:
             st = np.stack([out[k * n:(k + 1) * n].reshape(nx, order="F") for k in range(nw)])
         return st, t.value, it.value, tts.value
+
+    def timing(self, rid):
+        """(queue seconds, service seconds) of a finished solve, else None."""
+        q, sv = C.c_double(), C.c_double()
+        rc = lib().vacgpu_server_timing(self.h, rid, C.byref(q), C.byref(sv))
+        if rc == 1:
+            return None
+        _ck(rc, "vacgpu_server_timing")
+        return q.value, sv.value
 
     def stats(self):
         q, a, d, pk = C.c_int(), C.c_int(), C.c_int(), C.c_int()
