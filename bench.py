@@ -574,6 +574,53 @@ def run_served(args, capacity):
             "capacity_cell_updates_per_s": capacity}
 
 
+def run_snapshots(args, snap, hin):
+    """Save events every --snap-every steps on the 256^3 mixed run, 40 steps:
+    the state leaves the device synchronously (vacgpu_download, then the
+    next steps) or as an asynchronous snapshot (vacgpu_snapshot_begin; a
+    second host thread waits for it and copies it out while the next steps
+    run, as the vacgb host program's writer thread does).  Wall-clock time
+    of each against the same steps without saves; host buffers pinned."""
+    import threading as th
+    import torch
+    from vac_gb300 import abi
+    from vac_gb300.engine import Engine
+    k, n = args.snap_every, 40
+    out = torch.empty_like(hin).pin_memory()
+    res = {}
+    for mode in ("none", "sync", "async"):
+        e = Engine(make_params(snap, abi.PREC_MIXED), snap.x, snap.w)
+        e.step(3)
+        e.upload(snap.w)
+        if mode == "async":  # first use of the slot allocates its buffers
+            e.snapshot_begin(0)
+            e.snapshot_wait(0, out.data_ptr())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        writer = None
+        for _ in range(n // k):
+            e.step(k)
+            if mode == "sync":
+                e.download_flat(out.data_ptr())
+            elif mode == "async":
+                if writer:
+                    writer.join()
+                e.snapshot_begin(0)
+                writer = th.Thread(target=e.snapshot_wait, args=(0, out.data_ptr()))
+                writer.start()
+        if writer:
+            writer.join()
+        torch.cuda.synchronize()
+        res[mode] = time.perf_counter() - t0
+        e.close()
+    return {"workload": "3D MHD random modes %d^3 mixed, %d steps, a save event every %d "
+                        "steps (%d MB FP64 state per save)" % (N, n, k, hin.numel() * 8 // 10**6),
+            "seconds_no_saves": res["none"], "seconds_sync_saves": res["sync"],
+            "seconds_async_saves": res["async"],
+            "save_cost_sync_ms": (res["sync"] - res["none"]) / (n // k) * 1e3,
+            "save_cost_async_ms": (res["async"] - res["none"]) / (n // k) * 1e3}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -628,8 +675,15 @@ def main():
     ap.add_argument("--tvdmu-side", type=int, default=128,
                     help="cells per side of the tvdmu/Roe case (0: skip)")
     ap.add_argument("--tvdmu-steps", type=int, default=10)
+    ap.add_argument("--snap-every", type=int, default=4,
+                    help="steps between save events of the snapshot run (0: skip)")
     ap.add_argument("--side", type=int, default=N,
                     help="cells per side of the cube (smaller cases for profiling)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="precision of the timed 256^3 run (the headline is mixed)")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu "
+                         "--profile-from-start off)")
     args = ap.parse_args()
     N = args.side
     if args.cpu_serial_only:
@@ -649,8 +703,10 @@ def main():
     ncell = N ** 3
     K, W = args.steps, max(args.warmup, 3)
 
+    prec = abi.PREC_MIXED if args.precision == "mixed" else abi.PREC_FP64
+    elem = 4 if args.precision == "mixed" else 8
     stream = torch.cuda.Stream()
-    eng = Engine(make_params(snap, abi.PREC_MIXED), snap.x, snap.w)
+    eng = Engine(make_params(snap, prec), snap.x, snap.w)
     eng.set_stream(stream.cuda_stream)
     eng.step(W)
     # ---- device-resident timed region: K steps, CUDA events on the stream
@@ -660,10 +716,14 @@ def main():
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(lrank) as clk:
+        if args.profile_range:
+            torch.cuda.profiler.start()
         ev0.record(stream)
         eng.step(K)
         ev1.record(stream)
         torch.cuda.synchronize()
+        if args.profile_range:
+            torch.cuda.profiler.stop()
     el = ev0.elapsed_time(ev1) / 1e3
     barrier(ws)
     value, el = whole_job(ws, ncell * K, el)
@@ -678,7 +738,7 @@ def main():
     dom = max((k for k in kst if kst[k][0]), key=lambda k: kst[k][1])
     n_l, ms_l = kst[dom]
     avg_s = ms_l / n_l / 1e3
-    alg_bytes = 2 * NW * 4 * ncell  # one read + one write of the state per sweep
+    alg_bytes = 2 * NW * elem * ncell  # one read + one write of the state per sweep
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -692,7 +752,7 @@ def main():
     # ---- end to end through the C ABI with host buffers
     hin = torch.from_numpy(np.concatenate([snap.w[i].ravel(order="F") for i in range(NW)])).pin_memory()
     hout = torch.empty_like(hin).pin_memory()
-    eng2 = Engine(make_params(snap, abi.PREC_MIXED), snap.x, snap.w)
+    eng2 = Engine(make_params(snap, prec), snap.x, snap.w)
     eng2.set_stream(stream.cuda_stream)
     eng2.step(W)
     # warm-up of the transfer path too: the first DMA over freshly pinned
@@ -716,7 +776,9 @@ def main():
     if not args.no_fp64 and rank == 0:
         fp64 = run_fp64_c2(args, snap, stream, value / ws)
 
-    batched = served = plain = blast = tvdmu = None
+    batched = served = plain = blast = tvdmu = snaps = None
+    if rank == 0 and args.snap_every > 0:
+        snaps = run_snapshots(args, snap, hin)
     if rank == 0 and not args.no_plain:
         plain = run_plain(args)
     if rank == 0 and args.blast_side > 0:
@@ -742,8 +804,9 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": K, "warmup": W, "ms_per_step": el / K * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 (FP64 pressure recovery via double-float, FP64 sums and t)",
-                "data": "synthetic", "config": workload_config("mixed"),
+                "dtype": "f32 (FP64 pressure recovery via double-float, FP64 sums and t)"
+                         if elem == 4 else "f64",
+                "data": "synthetic", "config": workload_config(args.precision),
                 "parallelism": "replicas" if ws > 1 else "single",
                 "e2e": {"value": e2e_value, "unit": UNIT,
                         "h2d_bytes_per_step": hin.numel() * 8 / K,
@@ -759,7 +822,7 @@ def main():
                              "alg_bytes_per_launch": alg_bytes,
                              "kernel_share": shares},
                 "fp64": fp64, "plain_fp64_config1": plain, "blast_config5": blast,
-                "tvdmu_roe": tvdmu,
+                "tvdmu_roe": tvdmu, "snapshots": snaps,
                 "batched": batched, "served": served,
                 "cpu_baseline": cpu, "cpu_baseline_serial": serial,
                 "clocks": clk.summary()}

@@ -197,6 +197,25 @@ int vacgpu_upload(vacgpu_handle* h, const double* w, int it, double t);
  * src/vacio.t:1008-1047). */
 int vacgpu_download(vacgpu_handle* h, double* w);
 
+/* Asynchronous snapshots for VAC's save events (timetosave,
+ * src/vac.t:56-58,631-661, which calls savefileout_bin,
+ * src/vacio.t:1008-1047, and stops the run while it writes).
+ * vacgpu_snapshot_begin enqueues a copy of the current state -- the state
+ * after every step issued so far -- into snapshot slot `slot` (0 or 1) and
+ * returns at once: the copy leaves the device on a copy stream of its own
+ * while later vacgpu_step calls run.  vacgpu_snapshot_wait(h, slot, w)
+ * waits for that copy and writes the snapshot to w in vacgpu_download's
+ * layout, w(ixM^S,1:nw) (NULL w only releases the slot).  A slot holds one
+ * snapshot: a second begin on a pending slot is an error, as is a wait on
+ * an empty one.  The caller keeps it and t of the snapshot (vacgpu_step
+ * returns them).  The first begin of a slot allocates its device and
+ * page-locked host buffers (8 bytes per mesh cell and variable each).
+ * vacgpu_snapshot_wait may run on another host thread while this thread
+ * calls vacgpu_step on the handle; no other call on the handle may run
+ * concurrently with it. */
+int vacgpu_snapshot_begin(vacgpu_handle* h, int slot);
+int vacgpu_snapshot_wait(vacgpu_handle* h, int slot, double* w);
+
 /* Advance: repeat the body of the time loop (src/vac.t:59-106) at most
  * maxsteps times.  Before each step the dt is chosen exactly as VAC does
  * (dtpar / getdt_courant / getdt_special / dtcantgrow / slowsteps /
@@ -305,6 +324,7 @@ typedef struct vacgpu_source_args {
   const double* qtC;       /* device: time of wCT                           */
   const void* wCT;         /* device: the time-centred state                */
   void* w;                 /* device, in/out: the state the source updates  */
+  int nw, ndir;            /* variables: rho, m_1..m_ndir, e[, b_1..b_ndir] */
 } vacgpu_source_args;
 typedef int (*vacgpu_source_fn)(void* user, const vacgpu_source_args* s,
                                 void* stream);

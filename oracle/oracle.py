@@ -61,6 +61,7 @@ def lib():
         L.vo_register_source.argtypes = [vp, C.c_int, dp, C.c_int]
         L.vo_register_bound.argtypes = [vp, vp, vp]
         L.vo_register_eta.argtypes = [vp, vp, vp]
+        L.vo_register_source_fn.argtypes = [vp, vp, vp, vp]
         L.vo_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -76,10 +77,12 @@ class Oracle:
     ``w``: (nw, *nx) likewise.  Arrays are passed as VAC column-major
     blocks: x[d] is stored with ix1 fastest."""
 
-    def __init__(self, params, x, w, it=0, t=0.0, bound=None, eta=None):
+    def __init__(self, params, x, w, it=0, t=0.0, bound=None, eta=None, source=None):
         """bound: (function pointer, user pointer) of a specialbound hook
         with vo_register_bound's signature, installed before the first
-        ghost fill; eta: likewise a specialeta hook (vo_register_eta)."""
+        ghost fill; eta: likewise a specialeta hook (vo_register_eta);
+        source: (specialsource, getdt_special, user) of
+        vo_register_source_fn (either function pointer may be None)."""
         L = lib()
         self.p = params
         self.h = L.vo_create(C.byref(params))
@@ -89,6 +92,8 @@ class Oracle:
             L.vo_register_bound(self.h, bound[0], bound[1])
         if eta:
             L.vo_register_eta(self.h, eta[0], eta[1])
+        if source:
+            L.vo_register_source_fn(self.h, source[0], source[1], source[2])
         self.nx = tuple(params.nx[d] for d in range(params.ndim))
         self.nw = params.nw
         xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)

@@ -176,3 +176,55 @@ def test_run_special_bound_hook(vacgb, tmp_path):
     r2 = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True, input=par,
                         env={k: v for k, v in os.environ.items() if k != "VACGB_SPECIALBOUND"})
     assert r2.returncode != 0 and "Special boundary is not defined" in r2.stdout + r2.stderr
+
+
+@pytest.mark.gpu
+def test_run_special_source_hook(vacgb, tmp_path):
+    """The user's specialsource and getdt_special through the host program
+    (VACGB_SPECIALSOURCE=lib.so:source:getdt); results equal the oracle with
+    the host twins of the hooks."""
+    from tests.test_special_source import _device_hook, _host_hook
+    s = _setup(tmp_path)
+    Ld, _, _ = _device_hook()
+    env = dict(os.environ, VACGB_SPECIALSOURCE=Ld._name + ":src_dev:dt_dev")
+    r = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True, input=PAR,
+                       env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    Lh, hs, hd = _host_hook()
+    p = inistate.params_for(s, limiter="woodward")
+    p.typelimiter[1] = abi.LIM_MINMOD
+    o = Oracle(p, s.x, s.w, source=(hs, hd, 1 + p.ndir))
+    for snap, it in ((1, 10), (2, 20)):
+        got = vacfile.read(str(tmp_path / "ot.out"), snapshot=snap)
+        o.step(it - o.it)
+        assert got.it == it and got.t == o.t
+        assert np.array_equal(got.w.view(np.uint64), o.state().view(np.uint64))
+    bad = dict(os.environ, VACGB_SPECIALSOURCE=Ld._name + ":no_such_symbol")
+    r2 = subprocess.run([vacgb], cwd=tmp_path, capture_output=True, text=True, input=PAR,
+                        env=bad)
+    assert r2.returncode != 0 and "no symbol no_such_symbol" in r2.stdout + r2.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_async_saves_match_synchronous_saves(vacgb, tmp_path, precision):
+    """Snapshots written by the writer thread while the run continues give
+    the same .out and .log files, byte for byte, as a download and write
+    before the run continues (VACGB_SYNC_SAVE=1); a snapshot every step."""
+    par = PAR.replace("ditsave=5,10", "ditsave=1,1").replace("itmax=20", "itmax=12")
+    outs = {}
+    for mode in ("async", "sync"):
+        d = tmp_path / mode
+        d.mkdir()
+        _setup(d)
+        env = dict(os.environ)
+        env.pop("VACGB_SYNC_SAVE", None)
+        if mode == "sync":
+            env["VACGB_SYNC_SAVE"] = "1"
+        r = subprocess.run([vacgb, "--precision=" + precision], cwd=d, capture_output=True,
+                           text=True, input=par, env=env)
+        assert r.returncode == 0, r.stdout + r.stderr
+        outs[mode] = ((d / "ot.out").read_bytes(), (d / "ot.log").read_bytes())
+    assert outs["async"] == outs["sync"]
+    last = vacfile.read(str(tmp_path / "async" / "ot.out"))  # the last snapshot
+    assert last.it == 12

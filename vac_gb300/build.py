@@ -83,7 +83,7 @@ def build(verbose=False):
     os.makedirs(BINDIR, exist_ok=True)
     if not os.path.exists(VACGB) or os.path.getmtime(VACGB) < max(
             os.path.getmtime(src), os.path.getmtime(LIB)):
-        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", src, "-o", VACGB,
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", src, "-o", VACGB,
                "-L" + LIBDIR, "-lvacgpu", "-ldl", "-Wl,-rpath,$ORIGIN/../lib"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "batch_items.cuh"
 #include "physics_mixed.cuh"
 #include "sweep.cuh"
 #include "sweep_fused.cuh"
@@ -47,16 +48,6 @@ int vacgpu_internal_view(vacgpu_handle* h, HandleView* v);
 int vacgpu_internal_set_cur(vacgpu_handle* h, int cur);
 
 namespace {
-
-struct BItem {
-  int inst, bx, by, bz;
-};
-
-struct BInst {
-  FusedArgs fa;        // wout chosen per sweep from buf[] and Ctrl::cur
-  SweepArgs sa;        // first-step passes
-  float* buf[2];
-};
 
 typedef PHMixed<PREC_FF> PHB;
 
@@ -126,6 +117,8 @@ struct vacgpu_batch {
   // launch shape (autotuned): persistent CTAs (0: one per work item) and
   // work-list order
   int ctas, order;
+  bool pair;     // 3-D grids on the two-cells-per-thread sweep
+  bool pairgen;  // ... in its general form
   bool tuned;
   double tune_ms[8];
   int it0;
@@ -180,6 +173,12 @@ void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
 
 void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas, int order) {
   const vacgpu_params& p = b->p0;
+  if (b->pair) {
+    launch_batch_pair(b->d_items[D][order], b->nitems[D], b->d_insts, b->d_maps, sweep, D,
+                      p.physics == VACGPU_PHYS_MHD, p.typelimiter[0], b->pairgen, ctas,
+                      b->st);
+    return;
+  }
   int l0 = p.typelimiter[0];
   bool uni = p.typefull != VACGPU_TVDLF1;
   for (int v = 1; v < b->nw; v++) uni = uni && p.typelimiter[v] == l0;
@@ -263,6 +262,14 @@ int prepare(vacgpu_batch* b) {
       memcpy(&maps[4 * i + k], v.tmap[k / 2][k % 2], sizeof(CUtensorMap));
     ctrls[i] = v.ctrl;
   }
+  // the pair sweep when it applies to every grid: the single-grid path
+  // runs it on each of them, so the batch gives the same bits
+  b->pair = b->p0.ndim == 3;
+  b->pairgen = false;
+  for (int i = 0; i < n && b->pair; i++) {
+    b->pair = pair_applies(ins[i].fa, b->p0.physics == VACGPU_PHYS_MHD);
+    b->pairgen = b->pairgen || pair_general(ins[i].fa, b->p0.physics == VACGPU_PHYS_MHD);
+  }
   BCK(cudaMalloc(&b->d_insts, sizeof(BInst) * n));
   BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 4 * n));
   BCK(cudaMalloc(&b->d_ctrls, sizeof(Ctrl*) * n));
@@ -278,10 +285,13 @@ int prepare(vacgpu_batch* b) {
     const int tx = kind == 0 ? TileCfg<0>::TX : TileCfg<1>::TX;
     const int ty = kind == 1 ? TileCfg<1>::TY : TileCfg<0>::TY;
     const int ar = kind == 2 && D == 1 ? 2 : 1, am = kind == 2 ? D : 2;
+    // the pair sweep's x tiles start one column left of the mesh: nx + 1
+    // columns of faces
+    const int xext = b->pair && D == 0 ? 1 : 0;
     std::vector<std::vector<BItem>> per(n);
     for (int i = 0; i < n; i++) {
       const DevGrid& g = ins[i].fa.g;
-      const int nbx = (g.nx[0] + tx - 1) / tx, nby = (g.nx[ar] + ty - 1) / ty;
+      const int nbx = (g.nx[0] + xext + tx - 1) / tx, nby = (g.nx[ar] + ty - 1) / ty;
       const int nbz = g.ndim == 3 ? (g.nx[am] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
       for (int z = 0; z < nbz; z++)
         for (int y = 0; y < nby; y++)

@@ -1,0 +1,39 @@
+// batch_items.cuh - the work list of a batch of grids: what a persistent
+// sweep kernel reads per work item (batch.cu builds the lists; the fused
+// and pair sweep units hold the kernels that walk them).
+#pragma once
+#include "sweep_fused.cuh"
+
+namespace vacgpu {
+
+// one work item: a tile (bx, by) and z chunk bz of grid inst
+struct BItem {
+  int inst, bx, by, bz;
+};
+
+// one grid of the batch
+struct BInst {
+  FusedArgs fa;        // wout chosen per sweep from buf[] and Ctrl::cur
+  SweepArgs sa;        // first-step passes
+  float* buf[2];
+};
+
+// The launch of the pair sweep over a batch work list (sweep_pair.cu):
+// `ctas` persistent CTAs (0: one per item) walk items[0..nitems); sweep:
+// index of the sweep within the step (its parity picks the source buffer);
+// gen: the general form (some grid has pair_general).  False if the pair
+// kernel has no instance for (D, mhd, lim).
+bool launch_batch_pair(const BItem* items, int nitems, const BInst* insts,
+                       const CUtensorMap* maps, int sweep, int D, bool mhd, int lim,
+                       bool gen, int ctas, cudaStream_t st);
+
+// The grid needs the general form of the pair sweep: gravity, a
+// non-periodic face, split sources, no Powell terms for MHD, or no CFL
+// maximum.
+bool pair_general(const FusedArgs& a, bool mhd);
+
+// The pair sweep applies to a grid (3-D, one limiter for every variable,
+// minmod or woodward, even row offsets); also false when VACGPU_PAIR=0.
+bool pair_applies(const FusedArgs& a, bool mhd);
+
+}  // namespace vacgpu

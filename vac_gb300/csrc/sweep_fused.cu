@@ -11,14 +11,6 @@ int fused_smem_bytes(int nw, int k) { return fused_smem_floats(nw, k) * 4; }
 bool launch_sweep_pair(const FusedArgs& a, int D, bool mhd, const void* tmap, int nzc,
                        cudaStream_t st);
 
-static bool pair_enabled() {
-  static const bool on = [] {
-    const char* e = getenv("VACGPU_PAIR");
-    return !(e && atoi(e) == 0);
-  }();
-  return on;
-}
-
 template <int NDIM, int D, bool MHD, int LIMC, int PMF>
 static void launch_pmf(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
                        cudaStream_t st) {
@@ -105,7 +97,7 @@ bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
   a.zchunks = grid.z;
   // 3-D grids: the two-cells-per-thread kernel (packed FP32) where it
   // applies; VACGPU_PAIR=0 keeps the one-cell kernel
-  if (nd == 3 && pair_enabled() && launch_sweep_pair(a, s.d0, s.mhd, tmap, nzc, st))
+  if (nd == 3 && launch_sweep_pair(a, s.d0, s.mhd, tmap, nzc, st))
     return true;
   const CUtensorMap* map = (const CUtensorMap*)tmap;
   const int D = s.d0;

@@ -51,63 +51,57 @@ __host__ __device__ constexpr int pair_smem_floats(int nw) {
 
 struct PairK {  // per-launch constants, splatted
   f2 gm1, gamma, half, mhalf, quarter, eighth;
+  f2 mone;  // -1: x * mone negates x in one packed multiply (exact, -0 for +0)
   float smallp;
 };
 
-// Dekker/Knuth error-free sums of non-negative terms.  TS=0: Fast2Sum on
-// the lane-wise ordered pair (two min/max on the ALU pipe, three FP32
-// operations); TS=1: Knuth's branch-free TwoSum (six FP32 operations).
-template <int TS>
+// Dekker's error-free sum of non-negative terms: Fast2Sum on the
+// lane-wise ordered pair (two min/max, three FP32 operations; measured a
+// little faster than Knuth's branch-free six-operation TwoSum here).
 __device__ __forceinline__ void p_tsum(f2 a, f2 b, f2& s, f2& e) {
-  if (TS == 0) {
-    const f2 hi = vmax(a, b), lo = vmin(a, b);
-    s = hi + lo;
-    e = lo - (s - hi);
-  } else {
-    s = a + b;
-    const f2 bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-  }
+  const f2 hi = vmax(a, b), lo = vmin(a, b);
+  s = hi + lo;
+  e = lo - (s - hi);
 }
 
 // a*a = h + l exactly (FMA TwoProduct)
-__device__ __forceinline__ void p_tsq(f2 a, f2& h, f2& l) {
+__device__ __forceinline__ void p_tsq(f2 a, f2& h, f2& l, const PairK& k) {
   h = a * a;
-  l = ffma(a, a, fneg(h));
+  l = ffma(a, a, h * k.mone);
 }
 
 // Thermal pressure (unclipped) of a 3-D state in double-float arithmetic;
 // hbb receives B^2/2 (MHD).  The same steps as pressure_mixed<.., PREC_FF>.
-template <bool MHD, int TS>
+template <bool MHD>
 __device__ __forceinline__ f2 p_pressure(const f2* u, f2 rinv, const PairK& k,
                                          f2& hbb) {
   f2 mh, ml;
-  p_tsq(u[1], mh, ml);
+  p_tsq(u[1], mh, ml, k);
 #pragma unroll
   for (int c = 2; c <= 3; c++) {
     f2 ph, pl, t;
-    p_tsq(u[c], ph, pl);
-    p_tsum<TS>(mh, ph, mh, t);
+    p_tsq(u[c], ph, pl, k);
+    p_tsum(mh, ph, mh, t);
     ml = ml + (pl + t);
   }
   // mm/rho: FP32 quotient, exact FMA remainder, corrected low part
   const f2 qh = mh * rinv;
-  const f2 rem = ffma(qh, fneg(u[0]), mh);
+  const f2 rem = ffma(qh, u[0] * k.mone, mh);
   const f2 ql = (rem + ml) * rinv;
   f2 sh = qh, sl = ql;
   if (MHD) {
     f2 bh, bl;
-    p_tsq(u[5], bh, bl);
+    p_tsq(u[5], bh, bl, k);
 #pragma unroll
     for (int c = 6; c <= 7; c++) {
       f2 ph, pl, t;
-      p_tsq(u[c], ph, pl);
-      p_tsum<TS>(bh, ph, bh, t);
+      p_tsq(u[c], ph, pl, k);
+      p_tsum(bh, ph, bh, t);
       bl = bl + (pl + t);
     }
     hbb = k.half * (bh + bl);
     f2 t;
-    p_tsum<TS>(qh, bh, sh, t);
+    p_tsum(qh, bh, sh, t);
     sl = ql + bl + t;
   }
   f2 d = ffma(k.mhalf, sh, u[4]);
@@ -118,17 +112,17 @@ __device__ __forceinline__ f2 p_pressure(const f2* u, f2 rinv, const PairK& k,
 // getflux + transport along DD (src/vacphys.mhd0.t:149-205,
 // src/vacphys.t.hd:49-75) of a 3-D state; p: unclipped thermal pressure,
 // rinv: 1/rho.  f[rho] is m_DD itself (v rho up to a rounding).
-template <int DD, bool MHD, int TS>
+template <int DD, bool MHD>
 __device__ __forceinline__ void p_flux(const f2* u, const PairK& k, f2* f,
                                        f2& p, f2& rinv) {
   rinv = vrcp(u[0]);
   const f2 v = u[1 + DD] * rinv;
   f2 hbb;
-  p = p_pressure<MHD, TS>(u, rinv, k, hbb);
+  p = p_pressure<MHD>(u, rinv, k, hbb);
   f[0] = u[1 + DD];
   if (MHD) {
     const f2 pt = p + hbb;
-    const f2 nbi = fneg(u[5 + DD]);
+    const f2 nbi = u[5 + DD] * k.mone;
 #pragma unroll
     for (int c = 1; c <= 3; c++) {
       const f2 fk = c == DD + 1 ? ffma(u[4 + c], nbi, pt) : u[4 + c] * nbi;
@@ -166,7 +160,7 @@ __device__ __forceinline__ f2 p_cmax_mean(const f2* L, const f2* R,
   f2 kk;
 #pragma unroll
   for (int c = 1; c <= 3; c++) {
-    const f2 t = ffma(R[0], L[c], fneg(L[0] * R[c]));
+    const f2 t = ffma(R[0], L[c], (L[0] * R[c]) * k.mone);
     kk = c == 1 ? t * t : ffma(t, t, kk);
   }
   f2 corr = kk * (riL * riR) * (k.eighth * rinv);
@@ -196,29 +190,35 @@ __device__ __forceinline__ f2 p_cmax_mean(const f2* L, const f2* R,
   return vsqrt(cs2) + va;
 }
 
-// dwlimiter2 (src/vacgrid.t:938-996) of a = dw(i+1/2), b = dw(i-1/2):
-// minmod s max(0, min(|a|, s b)); woodward 2 s max(0, min(|a|, s b,
-// s (a+b)/4)), s = sign(1, a).  The sign products are sign-bit flips.
+// Half the limited slope, dwlimiter2 (src/vacgrid.t:938-996) of
+// a = dw(i+1/2), b = dw(i-1/2) times 1/2: minmod s max(0, min(|a|, s b))/2;
+// woodward s max(0, min(|a|, s b, s (a+b)/4)), s = sign(1, a).  s is
+// formed by bit operations (+-1 or +-1/2 with a's sign) and applied by
+// exact multiplications, so the result equals 0.5 * the limiter's value
+// bit for bit (powers of two scale without rounding).
 template <int LIMC>
-__device__ __forceinline__ f2 p_lim(f2 a, f2 b, const PairK& k) {
+__device__ __forceinline__ f2 p_hlim(f2 a, f2 b, const PairK& k) {
   float al, ah, bl, bh;
   if (LIMC == LIMC_WOODWARD) {
-    const f2 c = (a + b) * k.quarter;
-    const f2 sb = vxorsign(b, a), sc = vxorsign(c, a);
+    f2 s;
+    s.v = (a.v & 0x8000000080000000ull) | 0x3f8000003f800000ull;  // +-1
+    const f2 sb = b * s, sc = (a + b) * (s * k.quarter);
     float sbl, sbh, scl, sch;
     f2u(a, al, ah);
     f2u(sb, sbl, sbh);
     f2u(sc, scl, sch);
     const f2 r = f2m(fmaxf(0.0f, fminf(fminf(fabsf(al), sbl), scl)),
                      fmaxf(0.0f, fminf(fminf(fabsf(ah), sbh), sch)));
-    return vxorsign(r + r, a);
+    return r * s;
   }
   const f2 sb = vxorsign(b, a);
+  f2 sh;
+  sh.v = (a.v & 0x8000000080000000ull) | 0x3f0000003f000000ull;  // +-1/2
   float sbl, sbh;
   f2u(a, al, ah);
   f2u(sb, sbl, sbh);
   const f2 r = f2m(fmaxf(0.0f, fminf(fabsf(al), sbl)), fmaxf(0.0f, fminf(fabsf(ah), sbh)));
-  return vxorsign(r, a);
+  return r * sh;
 }
 
 // ------------------------------------------------------------ the kernel
@@ -259,8 +259,12 @@ __device__ __forceinline__ void pair_ghost_images(const FusedArgs& a,
   }
 }
 
-// One split sweep along D of a 3-D grid, two cells per thread.
-template <int D, bool MHD, int LIMC, int TS>
+// One split sweep along D of a 3-D grid, two cells per thread.  GEN:
+// the general form (gravity, non-periodic faces, sources or the CFL
+// maximum switched off); false: the common case -- every face periodic,
+// unsplit sources with Powell's terms for MHD, no gravity, CFL maximum --
+// with those decisions fixed at compile time.
+template <int D, bool MHD, int LIMC, bool GEN>
 struct PairSweep {
   static constexpr int K = D == 0 ? 0 : 2;        // in-plane / marching
   static constexpr int AM = D == 0 ? 2 : D;        // marching axis
@@ -285,33 +289,34 @@ struct PairSweep {
   // B_k at the cells, their upper and lower neighbours along D.  Every
   // operation is the one the full predictor does for B_k (p_flux, sources),
   // so a cell's value is the same bits whichever of the two computes it.
-  static __device__ __forceinline__ f2 bflux(const f2* x) {
+  // nqdivb: -qs * div B.
+  static __device__ __forceinline__ f2 bflux(const f2* x, const PairK& k) {
     const f2 ri = vrcp(x[0]);
     const f2 v = x[1] * ri;
-    return ffma(v, x[4], (x[2] * ri) * fneg(x[3]));
+    return ffma(v, x[4], (x[2] * ri) * (x[3] * k.mone));
   }
   static __device__ __forceinline__ f2 predict_b(const f2* c, const f2* pp,
-                                                 const f2* mm, f2 cq, f2 qdivb,
+                                                 const f2* mm, f2 cq, f2 nqdivb,
                                                  bool powell, const PairK& k) {
     f2 uL[5], uR[5];
 #pragma unroll
     for (int i = 0; i < 5; i++) {
-      const f2 hl = k.half * p_lim<LIMC>(pp[i] - c[i], c[i] - mm[i], k);
+      const f2 hl = p_hlim<LIMC>(pp[i] - c[i], c[i] - mm[i], k);
       uR[i] = c[i] - hl;
       uL[i] = c[i] + hl;
     }
-    const f2 fR = bflux(uR), fL = bflux(uL);
-    f2 out = ffma(fneg(cq), fL - fR, c[4]);
-    if (powell) out = ffma(c[2], vrcp(c[0]) * fneg(qdivb), out);
+    const f2 fR = bflux(uR, k), fL = bflux(uL, k);
+    f2 out = ffma(cq, fR - fL, c[4]);
+    if (powell) out = ffma(c[2], vrcp(c[0]) * nqdivb, out);
     return out;
   }
 
   // addsource2 with wCT = wc: gravity (specialsource), then Powell's terms
-  // (addsource) for qdivb = qs * div B.
+  // (addsource) for nq = -qs * div B.
   static __device__ __forceinline__ void sources(const FusedArgs& a, f2 qs,
-                                                 const f2* wc, f2 qdivb, bool powell,
+                                                 const f2* wc, f2 nq, bool powell,
                                                  f2* acc) {
-    if (a.ph.src_id == VACGPU_SRC_GRAVITY) {
+    if (GEN && a.ph.src_id == VACGPU_SRC_GRAVITY) {
 #pragma unroll
       for (int d = 1; d <= 3; d++)
         if (a.gravf[d - 1] != 0.0f) acc[d] = ffma(qs * f2s(a.gravf[d - 1]), wc[0], acc[d]);
@@ -320,7 +325,6 @@ struct PairSweep {
         if (a.gravf[d - 1] != 0.0f) acc[4] = ffma(qs * f2s(a.gravf[d - 1]), wc[d], acc[4]);
     }
     if (MHD && powell) {
-      const f2 nq = fneg(qdivb);
       const f2 t = vrcp(wc[0]) * nq;
       f2 mb = wc[1] * wc[5];
       mb = ffma(wc[2], wc[6], mb);
@@ -339,8 +343,8 @@ struct PairSweep {
   static __device__ __forceinline__ f2 face(const f2* L, const f2* R,
                                             const PairK& k, f2* G) {
     f2 fL[NW], fR[NW], pL, pR, riL, riR;
-    p_flux<D, MHD, TS>(L, k, fL, pL, riL);
-    p_flux<D, MHD, TS>(R, k, fR, pR, riR);
+    p_flux<D, MHD>(L, k, fL, pL, riL);
+    p_flux<D, MHD>(R, k, fR, pR, riR);
     f2 M[NW];
     M[0] = k.half * (L[0] + R[0]);
     M[1 + D] = k.half * (L[1 + D] + R[1 + D]);
@@ -348,23 +352,20 @@ struct PairSweep {
 #pragma unroll
       for (int c = 5; c <= 7; c++) M[c] = k.half * (L[c] + R[c]);
     const f2 cm = p_cmax_mean<D, MHD>(L, R, M, pL, pR, riL, riR, k);
-    const f2 ncm = fneg(cm);
 #pragma unroll
-    for (int v = 0; v < NW; v++) G[v] = ffma(ncm, R[v] - L[v], fL[v] + fR[v]);
+    for (int v = 0; v < NW; v++) G[v] = ffma(cm, L[v] - R[v], fL[v] + fR[v]);
     return cm;
   }
 
   // the new state of a pair of cells to HBM (lane-masked), with the ghost
-  // images of cells within two cells of a mesh face
+  // images of cells within two cells of a mesh face; off: element offset of
+  // the first cell, ghost-range coordinates gx (x), gr (row axis), gm
+  // (marching axis); nearxr: the pair is within two cells of an x or
+  // row-axis face
   static __device__ __forceinline__ void store(const FusedArgs& a, const f2* acc,
-                                               int ix0, int iy, int iz, bool ok0,
-                                               bool ok1) {
+                                               long long off, int gx, int gr, int gm,
+                                               bool nearxr, bool ok0, bool ok1) {
     const DevGrid& g = a.g;
-    int gc[3];
-    gc[0] = ix0 + 2;
-    gc[AR] = iy + 2;
-    gc[AM] = iz + 2;
-    const long long off = gidx(g, gc[0], gc[1], gc[2]);
     if (ok0 && ok1) {
 #pragma unroll
       for (int v = 0; v < NW; v++) st2(a.wout + off + v * g.vs, acc[v]);
@@ -377,9 +378,11 @@ struct PairSweep {
         if (ok1) a.wout[off + 1 + v * g.vs] = hi;
       }
     }
-    bool nb = gc[1] < 4 || gc[1] >= g.nx[1] || gc[2] < 4 || gc[2] >= g.nx[2] ||
-              gc[0] < 4 || gc[0] + 1 >= g.nx[0];
-    if (!nb) return;
+    if (!(nearxr || gm < 4 || gm >= g.nx[AM])) return;
+    int gc[3];
+    gc[0] = gx;
+    gc[AR] = gr;
+    gc[AM] = gm;
 #pragma unroll 1
     for (int h = 0; h < 2; h++) {
       if (!(h ? ok1 : ok0)) continue;
@@ -419,9 +422,9 @@ struct PairSweep {
     const double dtd = ctrl->dt;
     const float qdt = (float)dtd;
     const f2 qdt2 = f2s((float)(dtd / 2));
-    const f2 qs1h = f2s((float)(dtd / 2 / 3) * 0.5f);  // predictor source x 1/2
+    const f2 nqs1h = f2s(-((float)(dtd / 2 / 3) * 0.5f));  // -predictor source x 1/2
     const f2 qs2 = f2s((float)(dtd / 3));               // corrector source
-    const f2 qs2h = f2s((float)(dtd / 3) * 0.5f);
+    const f2 nqs2h = f2s(-((float)(dtd / 3) * 0.5f));
     const f2 qs1 = f2s((float)(dtd / 2 / 3));
     PairK k;
     k.gm1 = f2s(a.ph.gm1f);
@@ -430,9 +433,11 @@ struct PairSweep {
     k.mhalf = f2s(-0.5f);
     k.quarter = f2s(0.25f);
     k.eighth = f2s(0.125f);
+    k.mone = f2s(-1.0f);
     k.smallp = (float)ctrl->smallp;
-    const bool powell = MHD && a.ph.divbfix && a.ph.sourceunsplit;
-    const bool srcs = a.ph.sourceunsplit;
+    const bool powell = MHD && (!GEN || (a.ph.divbfix && a.ph.sourceunsplit));
+    const bool srcs = !GEN || a.ph.sourceunsplit;
+    const bool cfl = !GEN || a.cfl;
     const int cstart = x0 + g.xpad - 2;
     const int sh = cstart & 3;
     const int colx = cstart - sh;
@@ -472,9 +477,19 @@ struct PairSweep {
       cflx = f2m(2.0f / (a.dxf[0][gx0] + a.dxf[0][gx1]),
                  2.0f / (a.dxf[0][gx1] + a.dxf[0][min(ix0 + 4, g.nG[0] - 1)]));
     // ghost fixes of the predictor at non-periodic faces
-    const bool fix_x = a.periodic_mask[0] != all && (x0 <= 0 || x0 + TX + 1 >= nX);
-    const bool fix_r = a.periodic_mask[AR] != all && (y0 == 0 || y0 + TY >= nR);
-    const bool fix_m = a.periodic_mask[AM] != all;
+    const bool fix_x = GEN && a.periodic_mask[0] != all && (x0 <= 0 || x0 + TX + 1 >= nX);
+    const bool fix_r = GEN && a.periodic_mask[AR] != all && (y0 == 0 || y0 + TY >= nR);
+    const bool fix_m = GEN && a.periodic_mask[AM] != all;
+    // the pair's output offset at marching-axis ghost index 0, the stride
+    // along that axis, and whether it lies within two cells of an x or
+    // row-axis face (ghost images)
+    int gco[3];
+    gco[0] = ix0 + 2;
+    gco[AR] = iy + 2;
+    gco[AM] = 0;
+    const long long obase = gidx(g, gco[0], gco[1], gco[2]);
+    const long long sam = AM == 2 ? g.plane : g.P;
+    const bool nearxr = gco[AR] < 4 || gco[AR] >= g.nx[AR] || gco[0] < 4 || gco[0] + 1 >= g.nx[0];
 
     f2 qmax = f2s(0.0f);
     if (tid == 0) {
@@ -494,7 +509,13 @@ struct PairSweep {
     for (int v = 0; v < NW; v++) u0[v] = w1p[v] = hlp[v] = Gp[v] = f2s(0.0f);
 
     const int pfirst = z0 - 1, plast = z1;
+    // 1/dx and dx along the marching axis at planes j-1 and j, and the
+    // next plane's, loaded one plane ahead of use (ghost-range indices
+    // j+1 .. j+3 stay below nG = nM + 4)
+    float idzp = a.idxf[AM][pfirst + 1], dxzp = a.dxf[AM][pfirst + 1];
+    float idzc = a.idxf[AM][pfirst + 2], dxzc = a.dxf[AM][pfirst + 2];
     for (int j = pfirst; j <= plast; j++) {
+      const float idzn = a.idxf[AM][j + 3], dxzn = a.dxf[AM][j + 3];
       bool ok = true;
       if (j == pfirst) ok = wait_plane(j - 1) && wait_plane(j);
       ok = ok && wait_plane(j + 1);
@@ -506,8 +527,7 @@ struct PairSweep {
       const float* pm = slot(j - 1);
       const float* p0 = slot(j);
       const float* pp = slot(j + 1);
-      const int gz = j + 2;  // ghost-range index of plane j along AM
-      const f2 idxz = f2s(a.idxf[AM][gz]);
+      const f2 idxz = f2s(idzc);
       const bool edge = j == z0 - 1 || j == z1;
       const bool ring = powell && !edge;  // planes updated later need the ring
 
@@ -525,19 +545,18 @@ struct PairSweep {
         f2 uL[NW], uR[NW];
 #pragma unroll
         for (int v = 0; v < NW; v++) {
-          const f2 l = p_lim<LIMC>(up[v] - u0[v], u0[v] - um[v], k);
-          hl_[v] = k.half * l;
+          hl_[v] = p_hlim<LIMC>(up[v] - u0[v], u0[v] - um[v], k);
           uR[v] = u0[v] - hl_[v];
           uL[v] = u0[v] + hl_[v];
         }
         f2 fL[NW], fR[NW], pt_, ri_;
-        p_flux<D, MHD, TS>(uR, k, fR, pt_, ri_);
-        p_flux<D, MHD, TS>(uL, k, fL, pt_, ri_);
+        p_flux<D, MHD>(uR, k, fR, pt_, ri_);
+        p_flux<D, MHD>(uL, k, fL, pt_, ri_);
         const f2 cq = qdt2 * idxz;
 #pragma unroll
-        for (int v = 0; v < NW; v++) w1[v] = ffma(fneg(cq), fL[v] - fR[v], u0[v]);
+        for (int v = 0; v < NW; v++) w1[v] = ffma(cq, fR[v] - fL[v], u0[v]);
         if (srcs) {
-          f2 qdivb = f2s(0.0f);
+          f2 nqdivb = f2s(0.0f);
           if (powell) {
             const float* bxr = p0 + 5 * BPL + br * FB_X + bc;
             const float* byr = p0 + (5 + AR) * BPL + br * FB_X + bc;
@@ -547,9 +566,9 @@ struct PairSweep {
             const f2 dby = ld2(byr + FB_X) - ld2(byr - FB_X);
             const f2 dbz = up[5 + AM] - um[5 + AM];
             const f2 divb = ffma(dbz, idxz, ffma(dby, idxy, dbx * idxx));
-            qdivb = qs1h * divb;
+            nqdivb = nqs1h * divb;
           }
-          sources(a, qs1, u0, qdivb, powell, w1);
+          sources(a, qs1, u0, nqdivb, powell, w1);
         }
         // marching-axis ghost planes: w1(-1) from w1(0), w1(n) from w1(n-1)
         if (fix_m && j == 0) {
@@ -615,7 +634,7 @@ struct PairSweep {
             const f2 ix_ = f2m(a.idxf[0][gxl], a.idxf[0][gxh]);
             const f2 iy_ = f2s(a.idxf[AR][min(max(y0 + rl + 2, 0), g.nG[AR] - 1)]);
             const f2 divb = ffma(dbz, idxz, ffma(dby, iy_, dbx * ix_));
-            const f2 o = predict_b(c, cp, cm_, qdt2 * idxz, qs1h * divb, true, k);
+            const f2 o = predict_b(c, cp, cm_, qdt2 * idxz, nqs1h * divb, true, k);
             if (wq == 0) {
               st2(wb(sm, j, 1, rl, lx0), o);
             } else {
@@ -645,7 +664,7 @@ struct PairSweep {
             const f2 dby = ld2(byr + FB_X) - ld2(byr - FB_X);
             const f2 dbz = ld2(pp + (5 + AM) * BPL + o0) - ld2(pm + (5 + AM) * BPL + o0);
             const f2 divb = ffma(dbz, idxz, ffma(dby, idxy, dbx * idxx));
-            bz = predict_b(c, cp, cm_, qdt2 * idxx, qs1h * divb, true, k);
+            bz = predict_b(c, cp, cm_, qdt2 * idxx, nqs1h * divb, true, k);
           }
         } else {
           f2 u[NW], hlv[NW], dbx = f2s(0.0f);
@@ -660,7 +679,7 @@ struct PairSweep {
             const f2 dp = f2m(d1, rgt - ch), dm = f2m(cl - lft, d1);
             if (v == 5) dbx = f2m(r[1] - lft, rgt - cl);
             u[v] = c;
-            hlv[v] = k.half * p_lim<LIMC>(dp, dm, k);
+            hlv[v] = p_hlim<LIMC>(dp, dm, k);
           }
           f2 uL[NW], uR[NW];
 #pragma unroll
@@ -669,21 +688,21 @@ struct PairSweep {
             uL[v] = u[v] + hlv[v];
           }
           f2 fL[NW], fR[NW], pt_, ri_;
-          p_flux<D, MHD, TS>(uR, k, fR, pt_, ri_);
-          p_flux<D, MHD, TS>(uL, k, fL, pt_, ri_);
+          p_flux<D, MHD>(uR, k, fR, pt_, ri_);
+          p_flux<D, MHD>(uL, k, fL, pt_, ri_);
           const f2 cq = qdt2 * idxx;
 #pragma unroll
-          for (int v = 0; v < NW; v++) w1[v] = ffma(fneg(cq), fL[v] - fR[v], u[v]);
+          for (int v = 0; v < NW; v++) w1[v] = ffma(cq, fR[v] - fL[v], u[v]);
           if (srcs) {
-            f2 qdivb = f2s(0.0f);
+            f2 nqdivb = f2s(0.0f);
             if (powell) {
               const float* byr = p0 + (5 + AR) * BPL + o0;
               const f2 dby = ld2(byr + FB_X) - ld2(byr - FB_X);
               const f2 dbz = ld2(pp + (5 + AM) * BPL + o0) - ld2(pm + (5 + AM) * BPL + o0);
               const f2 divb = ffma(dbz, idxz, ffma(dby, idxy, dbx * idxx));
-              qdivb = qs1h * divb;
+              nqdivb = nqs1h * divb;
             }
-            sources(a, qs1, u, qdivb, powell, w1);
+            sources(a, qs1, u, nqdivb, powell, w1);
           }
           // x-face ghost cells of the region: w1(-1) from w1(0), w1(n) from
           // w1(n-1) (the pair's first cell has an even index)
@@ -727,7 +746,7 @@ struct PairSweep {
               const f2 dbz = ld2(pp + (5 + AM) * BPL + ob) - ld2(pm + (5 + AM) * BPL + ob);
               const f2 iy_ = f2s(a.idxf[AR][min(max(y0 + rl + 2, 0), g.nG[AR] - 1)]);
               const f2 divb = ffma(dbz, idxz, ffma(dby, iy_, dbx2 * idxx));
-              st2(wb(sm, j, 1, rl, lx0), predict_b(c, cp, cm_, qdt2 * idxx, qs1h * divb, true, k));
+              st2(wb(sm, j, 1, rl, lx0), predict_b(c, cp, cm_, qdt2 * idxx, nqs1h * divb, true, k));
             }
           }
         }
@@ -747,10 +766,12 @@ struct PairSweep {
                    gfix(oh, sh2, 5 + AM, a.periodic_mask[AM], a.asymm_hi[AM]));
         }
       }
-      __syncthreads();  // barrier B: w1b of plane j complete
       // getboundary of the ring/tile predictor values at non-periodic x and
-      // row faces (read at the next iteration's update)
+      // row faces (read at the next iteration's update).  The transverse B
+      // of plane j in w1b is otherwise read only at the next iteration,
+      // after its barrier A, so this barrier is needed only here.
       if (ring && (fix_r || (K == 2 && fix_x))) {
+        __syncthreads();  // barrier B: w1b of plane j complete
         for (int c = tid; c < 36 * 10; c += PT_NT) {
           const int lx = c % 36 - WBO, lyy = c / 36 - 1;
           const int ixc = x0 + lx, iyc = y0 + lyy;
@@ -788,8 +809,8 @@ struct PairSweep {
             R[v] = w1[v] - hl_[v];
           }
           const f2 cm = face(L, R, k, G);
-          if (a.cfl) {
-            const float cf = 2.0f / (a.dxf[AM][gz - 1] + a.dxf[AM][gz]);
+          if (cfl) {
+            const float cf = 2.0f / (dxzp + dxzc);
             float cl, ch, ql, qh;
             f2u(cm * f2s(cf), cl, ch);
             f2u(qmax, ql, qh);
@@ -809,7 +830,7 @@ struct PairSweep {
           R[v] = f2m(rh, nb);
         }
         const f2 cm = face(L, R, k, G);
-        if (a.cfl) {
+        if (cfl) {
           // faces (-1|0) .. (n-1|n) of mesh rows inside the chunk
           float cl, ch, ql, qh;
           f2u(cm * cflx, cl, ch);
@@ -842,16 +863,15 @@ struct PairSweep {
       if (jo >= z0 && jo < z1 && (ok0 || ok1)) {
         const float* pu = pm;  // state plane j-1
         f2 acc[NW];
-        const f2 idxo = K == 2 ? f2s(a.idxf[AM][gz - 1]) : idxx;
-        const f2 cqh = f2s(0.5f * qdt) * idxo;
-        const f2 ncq = fneg(cqh);
+        const f2 idxo = K == 2 ? f2s(idzp) : idxx;
+        const f2 ncq = f2s(-0.5f * qdt) * idxo;
 #pragma unroll
         for (int v = 0; v < NW; v++) {
           const f2 w = ld2(pu + v * BPL + br * FB_X + bc);
           acc[v] = K == 2 ? ffma(ncq, G[v] - Gp[v], w) : ffma(ncq, Gp[v], w);
         }
         if (srcs) {
-          f2 qdivb = f2s(0.0f);
+          f2 nqdivb = f2s(0.0f);
           if (powell) {
             f2 dbx;
             if (K == 2) {
@@ -863,14 +883,19 @@ struct PairSweep {
             }
             const f2 dby = ld2(wb(sm, jo, 1, ly + 1, lx0)) - ld2(wb(sm, jo, 1, ly - 1, lx0));
             const f2 dbz = bz - bzm2;
-            const f2 divb = ffma(dbz, f2s(a.idxf[AM][gz - 1]), ffma(dby, idxy, dbx * idxx));
-            qdivb = qs2h * divb;
+            const f2 divb = ffma(dbz, f2s(idzp), ffma(dby, idxy, dbx * idxx));
+            nqdivb = nqs2h * divb;
           }
-          sources(a, qs2, w1p, qdivb, powell, acc);
+          sources(a, qs2, w1p, nqdivb, powell, acc);
         }
-        store(a, acc, ix0, iy, jo, ok0, ok1);
+        store(a, acc, obase + (long long)(jo + 2) * sam, gco[0], gco[AR], jo + 2, nearxr, ok0,
+              ok1);
       }
       // ---------------- carry to the next plane
+      idzp = idzc;
+      idzc = idzn;
+      dxzp = dxzc;
+      dxzc = dxzn;
       if (K == 0 && !edge) dbxp = dbxc;
       bzm2 = bzm1;
       bzm1 = bz;
@@ -894,7 +919,7 @@ struct PairSweep {
 #pragma unroll
       for (int s2 = 0; s2 < FWRING; s2++) uses[s2] += (np - s2 + FWRING - 1) / FWRING;
     }
-    if (a.cfl) {
+    if (cfl) {
       float q = fmaxf(f2lo(qmax), f2hi(qmax));
       {
         const float l = f2lo(qmax), h = f2hi(qmax);
@@ -917,7 +942,7 @@ struct PairSweep {
   }
 };
 
-template <int D, bool MHD, int LIMC, int TS>
+template <int D, bool MHD, int LIMC, bool GEN>
 __global__ void __launch_bounds__(PT_NT, 3)
     k_sweep_pair(const __grid_constant__ CUtensorMap map, FusedArgs a) {
   extern __shared__ __align__(128) float dsm[];
@@ -925,7 +950,7 @@ __global__ void __launch_bounds__(PT_NT, 3)
   init_bars(bars);
   int uses[FWRING] = {0, 0, 0, 0};
   const unsigned slotid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  PairSweep<D, MHD, LIMC, TS>::run(&map, a, dsm, blockIdx.x, blockIdx.y, blockIdx.z, bars,
+  PairSweep<D, MHD, LIMC, GEN>::run(&map, a, dsm, blockIdx.x, blockIdx.y, blockIdx.z, bars,
                                    uses, slotid);
 }
 

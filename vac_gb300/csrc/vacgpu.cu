@@ -206,6 +206,17 @@ struct vacgpu_handle {
   bool tuning;
   int tncand;
   int tcand[6];
+  // asynchronous snapshots (vacgpu_snapshot_begin/wait): per slot the
+  // mesh-ordered FP64 copy on the device, its page-locked host copy, and
+  // the events that order the gather (on st) and the download (on cst)
+  struct Snap {
+    double* dev;
+    double* host;
+    cudaEvent_t gathered, copied;
+    bool pending;
+  };
+  Snap snap[2];
+  cudaStream_t cst;  // copy stream of the snapshot downloads
 };
 
 namespace {
@@ -452,6 +463,8 @@ void source_hook(vacgpu_handle* h, const SweepArgs& a, int pred, int half, const
   s.qtC = &h->ctrl->src_qtc;
   s.wCT = wct;
   s.w = w;
+  s.nw = h->nw;
+  s.ndir = h->p.ndir;
   if (h->src_fn(h->src_user, &s, (void*)h->st)) h->hook_failed = true;
   kbegin(h, pred ? VACGPU_K_PREDICT : VACGPU_K_CORRECT);
   if (sizeof(T) == 8)
@@ -1317,6 +1330,50 @@ int vacgpu_download(vacgpu_handle* h, double* w) {
   return 0;
 }
 
+int vacgpu_snapshot_begin(vacgpu_handle* h, int slot) {
+  if (!h) return fail("null handle");
+  if (slot < 0 || slot > 1) return fail("snapshot slot must be 0 or 1");
+  if (!h->have_state) return fail("vacgpu_snapshot_begin before vacgpu_upload");
+  vacgpu_handle::Snap& sn = h->snap[slot];
+  if (sn.pending)
+    return fail("snapshot slot " + std::to_string(slot) +
+                " is still in flight (call vacgpu_snapshot_wait first)");
+  const DevGrid& g = h->g;
+  const long long n = g.ncell * h->nw;
+  if (!h->cst) CK(cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking));
+  if (!sn.dev) {
+    CK(cudaMalloc(&sn.dev, sizeof(double) * n));
+    CK(cudaMallocHost(&sn.host, sizeof(double) * n));
+    CK(cudaEventCreateWithFlags(&sn.gathered, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&sn.copied, cudaEventDisableTiming));
+  }
+  // the gather follows the steps issued so far on the handle's stream; the
+  // download waits for it on the copy stream, so later steps overlap it
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  if (h->elem == 8)
+    k_gather<double><<<nb, 256, 0, h->st>>>((const double*)h->buf[h->cur], sn.dev, g, h->nw);
+  else
+    k_gather<float><<<nb, 256, 0, h->st>>>((const float*)h->buf[h->cur], sn.dev, g, h->nw);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(sn.gathered, h->st));
+  CK(cudaStreamWaitEvent(h->cst, sn.gathered, 0));
+  CK(cudaMemcpyAsync(sn.host, sn.dev, sizeof(double) * n, cudaMemcpyDeviceToHost, h->cst));
+  CK(cudaEventRecord(sn.copied, h->cst));
+  sn.pending = true;
+  return 0;
+}
+
+int vacgpu_snapshot_wait(vacgpu_handle* h, int slot, double* w) {
+  if (!h) return fail("null handle");
+  if (slot < 0 || slot > 1) return fail("snapshot slot must be 0 or 1");
+  vacgpu_handle::Snap& sn = h->snap[slot];
+  if (!sn.pending) return fail("no snapshot in flight in slot " + std::to_string(slot));
+  CK(cudaEventSynchronize(sn.copied));
+  if (w) memcpy(w, sn.host, sizeof(double) * h->g.ncell * h->nw);
+  sn.pending = false;
+  return 0;
+}
+
 int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
                 int* it, double* dt, int* finished) {
   if (!h) return fail("null handle");
@@ -1479,6 +1536,16 @@ void vacgpu_destroy(vacgpu_handle* h) {
   if (!h) return;
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->own_st) cudaStreamSynchronize(h->own_st);
+  if (h->cst) {
+    cudaStreamSynchronize(h->cst);
+    cudaStreamDestroy(h->cst);
+  }
+  for (auto& sn : h->snap) {
+    cudaFree(sn.dev);
+    cudaFreeHost(sn.host);
+    if (sn.gathered) cudaEventDestroy(sn.gathered);
+    if (sn.copied) cudaEventDestroy(sn.copied);
+  }
   for (int i = 0; i < 3; i++) cudaFree(h->buf[i]);
   cudaFree(h->wold);
   cudaFree(h->fixb);

@@ -26,6 +26,7 @@ SYMBOLS = [
     "vacgpu_batch_tune", "vacgpu_batch_destroy", "vacgpu_server_create",
     "vacgpu_server_submit", "vacgpu_server_result", "vacgpu_server_timing",
     "vacgpu_server_stats", "vacgpu_server_destroy", "vacgpu_measure_fp64_peak",
+    "vacgpu_register_source_fn", "vacgpu_snapshot_begin", "vacgpu_snapshot_wait",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
@@ -57,6 +58,9 @@ def lib():
         L.vacgpu_register_source.argtypes = [vp, C.c_int, dp, C.c_int]
         L.vacgpu_register_bound.argtypes = [vp, vp, vp]
         L.vacgpu_register_eta.argtypes = [vp, vp, vp]
+        L.vacgpu_register_source_fn.argtypes = [vp, vp, vp, vp]
+        L.vacgpu_snapshot_begin.argtypes = [vp, C.c_int]
+        L.vacgpu_snapshot_wait.argtypes = [vp, C.c_int, vp]
         L.vacgpu_destroy.argtypes = [vp]
         L.vacgpu_destroy.restype = None
         L.vacgpu_last_error.argtypes = [C.c_char_p, C.c_int]
@@ -114,10 +118,12 @@ class Engine:
     coordinates, ``w``: (nw, n1, ...) conservative state, both indexed like
     VAC's x(ix^D,idim) and w(ix^D,iw)."""
 
-    def __init__(self, params, x, w, it=0, t=0.0, bound=None, eta=None):
+    def __init__(self, params, x, w, it=0, t=0.0, bound=None, eta=None, source=None):
         """bound: (function pointer, user pointer) of a vacgpu_bound_fn
         specialbound hook, installed before the first ghost fill; eta:
-        likewise a vacgpu_eta_fn specialeta hook."""
+        likewise a vacgpu_eta_fn specialeta hook; source: (specialsource
+        function pointer or None, getdt_special function pointer or None,
+        user pointer) of vacgpu_register_source_fn."""
         L = lib()
         self.p = params
         h = C.c_void_p()
@@ -130,6 +136,10 @@ class Engine:
         if eta:
             _ck(L.vacgpu_register_eta(self.h, C.c_void_p(eta[0]), C.c_void_p(eta[1])),
                 "vacgpu_register_eta")
+        if source:
+            _ck(L.vacgpu_register_source_fn(self.h, C.c_void_p(source[0]),
+                                            C.c_void_p(source[1]), C.c_void_p(source[2])),
+                "vacgpu_register_source_fn")
         self.nw = params.nw
         self.nx = tuple(params.nx[d] for d in range(params.ndim))
         xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)
@@ -168,6 +178,24 @@ class Engine:
         n = int(np.prod(self.nx))
         out = np.empty(self.nw * n, dtype=np.float64)
         _ck(lib().vacgpu_download(self.h, _dp(out)), "vacgpu_download")
+        return np.stack([out[i * n:(i + 1) * n].reshape(self.nx, order="F")
+                         for i in range(self.nw)])
+
+    def snapshot_begin(self, slot=0):
+        """Start an asynchronous copy of the current state into `slot`."""
+        _ck(lib().vacgpu_snapshot_begin(self.h, slot), "vacgpu_snapshot_begin")
+
+    def snapshot_wait(self, slot=0, out_ptr=None):
+        """Wait for the snapshot in `slot`; return it as (nw, *nx), or write
+        it to the VAC-ordered flat FP64 host buffer at out_ptr."""
+        if out_ptr is not None:
+            _ck(lib().vacgpu_snapshot_wait(self.h, slot, C.c_void_p(out_ptr)),
+                "vacgpu_snapshot_wait")
+            return None
+        n = int(np.prod(self.nx))
+        out = np.empty(self.nw * n, dtype=np.float64)
+        _ck(lib().vacgpu_snapshot_wait(self.h, slot, C.c_void_p(out.ctypes.data)),
+            "vacgpu_snapshot_wait")
         return np.stack([out[i * n:(i + 1) * n].reshape(self.nx, order="F")
                          for i in range(self.nw)])
 

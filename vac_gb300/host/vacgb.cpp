@@ -15,8 +15,12 @@
 //
 // typeB='special' faces call the user's specialbound, which this program
 // loads as a device hook (vacgpu_bound_fn) from a shared library named by
-// VACGB_SPECIALBOUND=library.so:symbol.
+// VACGB_SPECIALBOUND=library.so:symbol.  The user's specialsource and
+// getdt_special are loaded likewise from
+// VACGB_SPECIALSOURCE=library.so:source_symbol[:getdt_symbol] (an empty
+// source symbol installs the dt limit alone).
 #include <chrono>
+#include <thread>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -628,6 +632,25 @@ int main(int argc, char** argv) {
     if (!fn) die("VACGB_SPECIALBOUND: no symbol " + sp.substr(colon + 1));
     chk(vacgpu_register_bound(h, (vacgpu_bound_fn)fn, nullptr));
   }
+  if (const char* spec = std::getenv("VACGB_SPECIALSOURCE")) {
+    // library.so:source_symbol[:getdt_symbol]
+    std::string sp(spec);
+    size_t c1 = sp.find(".so:");
+    if (c1 == std::string::npos)
+      die("VACGB_SPECIALSOURCE must be library.so:source_symbol[:getdt_symbol]");
+    c1 += 3;
+    void* lib = dlopen(sp.substr(0, c1).c_str(), RTLD_NOW | RTLD_LOCAL);
+    if (!lib) die(std::string("VACGB_SPECIALSOURCE: ") + dlerror());
+    std::string rest = sp.substr(c1 + 1);
+    size_t c2 = rest.find(':');
+    std::string ssym = rest.substr(0, c2);
+    std::string dsym = c2 == std::string::npos ? "" : rest.substr(c2 + 1);
+    void* fs = ssym.empty() ? nullptr : dlsym(lib, ssym.c_str());
+    void* fd = dsym.empty() ? nullptr : dlsym(lib, dsym.c_str());
+    if (!ssym.empty() && !fs) die("VACGB_SPECIALSOURCE: no symbol " + ssym);
+    if (!dsym.empty() && !fd) die("VACGB_SPECIALSOURCE: no symbol " + dsym);
+    chk(vacgpu_register_source_fn(h, (vacgpu_source_fn)fs, (vacgpu_dtspecial_fn)fd, nullptr));
+  }
   chk(vacgpu_set_grid(h, ini.x.data()));
   chk(vacgpu_upload(h, ini.w.data(), ini.it, ini.t));
   std::printf("Start Advance  %10.3f sec\n", cputime());
@@ -639,29 +662,61 @@ int main(int argc, char** argv) {
   std::ofstream outf, logf;
   std::vector<double> wbuf(ini.w.size());
   std::string headout = ini.head;
+  // savefileout_bin's records of one snapshot (state w taken at sit, st_)
+  auto write_out = [&](int sit, double st_, const double* w) {
+    write_rec(outf, pad79(headout).data(), 79);
+    char rec2[24];
+    int32_t ndimout = p.ndim, neq = (int32_t)ini.eqpar.size(), nww = nw;
+    std::memcpy(rec2, &sit, 4);
+    std::memcpy(rec2 + 4, &st_, 8);
+    std::memcpy(rec2 + 12, &ndimout, 4);
+    std::memcpy(rec2 + 16, &neq, 4);
+    std::memcpy(rec2 + 20, &nww, 4);
+    write_rec(outf, rec2, 24);
+    write_rec(outf, ini.nx.data(), 4 * p.ndim);
+    std::vector<double> eq(ini.eqpar.size());
+    for (size_t k = 0; k < eq.size(); k++) eq[k] = k < VACGPU_MAXEQPAR ? p.eqpar[k] : ini.eqpar[k];
+    write_rec(outf, eq.data(), (int32_t)(8 * eq.size()));
+    write_rec(outf, pad79(ini.varnames).data(), 79);
+    write_rec(outf, ini.x.data(), (int32_t)(8 * ini.x.size()));
+    const long long n = ini.ncell();
+    for (int iw = 0; iw < nw; iw++) write_rec(outf, w + iw * n, (int32_t)(8 * n));
+    outf.flush();
+  };
+  // A save event of the .out file takes a snapshot (vacgpu_snapshot_begin)
+  // and hands it to a writer thread, which waits for the copy and writes the
+  // records while the next steps run; the next event, and the end of the
+  // run, join it first, so records stay in order.  VACGB_SYNC_SAVE=1 writes
+  // each record before the run continues (vacgpu_download).
+  const bool sync_save = std::getenv("VACGB_SYNC_SAVE") && std::atoi(std::getenv("VACGB_SYNC_SAVE"));
+  std::thread writer;
+  std::string writer_err;
+  auto join_writer = [&]() {
+    if (writer.joinable()) writer.join();
+    if (!writer_err.empty()) die(writer_err);
+  };
   auto savefile = [&](int ifile) {
     if (ifile == 1) {  // savefileout_bin
       if (fnames[1].empty()) return;
+      join_writer();
       if (!outf.is_open()) outf.open(fnames[1], std::ios::binary);
-      chk(vacgpu_download(h, wbuf.data()));
-      write_rec(outf, pad79(headout).data(), 79);
-      char rec2[24];
-      int32_t ndimout = p.ndim, neq = (int32_t)ini.eqpar.size(), nww = nw;
-      std::memcpy(rec2, &it, 4);
-      std::memcpy(rec2 + 4, &t, 8);
-      std::memcpy(rec2 + 12, &ndimout, 4);
-      std::memcpy(rec2 + 16, &neq, 4);
-      std::memcpy(rec2 + 20, &nww, 4);
-      write_rec(outf, rec2, 24);
-      write_rec(outf, ini.nx.data(), 4 * p.ndim);
-      std::vector<double> eq(ini.eqpar.size());
-      for (size_t k = 0; k < eq.size(); k++) eq[k] = k < VACGPU_MAXEQPAR ? p.eqpar[k] : ini.eqpar[k];
-      write_rec(outf, eq.data(), (int32_t)(8 * eq.size()));
-      write_rec(outf, pad79(ini.varnames).data(), 79);
-      write_rec(outf, ini.x.data(), (int32_t)(8 * ini.x.size()));
-      const long long n = ini.ncell();
-      for (int iw = 0; iw < nw; iw++) write_rec(outf, wbuf.data() + iw * n, (int32_t)(8 * n));
-      outf.flush();
+      if (sync_save) {
+        chk(vacgpu_download(h, wbuf.data()));
+        write_out(it, t, wbuf.data());
+        return;
+      }
+      chk(vacgpu_snapshot_begin(h, 0));
+      const int sit = it;
+      const double st_ = t;
+      writer = std::thread([&, sit, st_]() {
+        if (vacgpu_snapshot_wait(h, 0, wbuf.data())) {
+          char buf[1024];
+          vacgpu_last_error(buf, sizeof buf);
+          writer_err = buf;
+          return;
+        }
+        write_out(sit, st_, wbuf.data());
+      });
     } else {  // savefilelog_default
       if (fnames[0].empty()) return;
       if (!logf.is_open()) {
@@ -722,6 +777,7 @@ int main(int argc, char** argv) {
   const double tfin = cputime();
   for (int f = 0; f < 2; f++)
     if (itsavelast[f] < it) savefile(f);
+  join_writer();
   std::printf("Finish Advance %10.3f sec\n", tfin);
   int nerror[4];
   chk(vacgpu_error_counts(h, nerror));
