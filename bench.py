@@ -203,7 +203,7 @@ def run_batched(args):
     grids = inistate.riemann_batch(n=64, seed=0)
     cells = sum(int(np.prod([g[0].nx[d] for d in range(2)])) for g in grids)
     b = Batch(grids)
-    ctas, order, ms = b.tune()
+    ctas, order, rows, ms = b.tune()
     b.step(50)  # capture + first replay
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -215,7 +215,7 @@ def run_batched(args):
             "grids": 64, "cells": cells, "steps": 50, "seconds": el,
             "value": cells * 50 / el, "unit": UNIT,
             "tuned": {"persistent_ctas": ctas, "order": ["round-robin", "grid-major"][order],
-                      "trial_ms": ms}}
+                      "rows_per_item": rows, "trial_ms": ms}}
 
 
 def _errors(wm, w64):
@@ -255,14 +255,16 @@ def _fresh_timed(params, snap, k, stream, warm):
     return el, w
 
 
-def fp64_flops_per_cell_update():
-    """FP64 operations per cell-update of the plain path (config 2's 3-D
-    MHD step), from the committed ncu record of its FP64 instruction
-    counts (profiles/fp64_step_mhd_128.md); None if absent."""
+def fp64_per_cell_update(key):
+    """FP64 operations (key fp64_flops_per_cell_update, DFMA = 2) or FP64
+    pipe instructions (fp64_inst_per_cell_update) per cell-update of the
+    plain path (config 2's 3-D MHD step), from the committed ncu record of
+    its FP64 instruction counts (profiles/fp64_step_mhd_128.md); None if
+    absent."""
     f = os.path.join(ROOT, "profiles", "fp64_step_mhd_128.md")
     if os.path.exists(f):
         for ln in open(f):
-            if ln.startswith("fp64_flops_per_cell_update="):
+            if ln.startswith(key + "="):
                 return float(ln.split("=")[1])
     return None
 
@@ -282,7 +284,8 @@ def run_fp64_c2(args, snap, stream, mixed_value):
     l1, linf = _errors(wm, w64)
     v64 = ncell * k / el64
     peak = measure_fp64_peak(stream.cuda_stream)
-    fpc = fp64_flops_per_cell_update()
+    fpc = fp64_per_cell_update("fp64_flops_per_cell_update")
+    ipc = fp64_per_cell_update("fp64_inst_per_cell_update")
     hbm = _hbm_peak()
     roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak / 1e12,
             "peak_source": "measured: vacgpu_measure_fp64_peak (DFMA chains on every SM, "
@@ -295,6 +298,11 @@ def run_fp64_c2(args, snap, stream, mixed_value):
     if fpc:
         roof["achieved"] = fpc * v64 / 1e12
         roof["frac"] = fpc * v64 / peak
+    if ipc:
+        # DADD and DMUL occupy the pipe like a DFMA: instruction rate against
+        # the DFMA rate (half the flop peak)
+        roof["inst_per_cell_update"] = ipc
+        roof["pipe_frac"] = ipc * v64 / (peak / 2)
     return {"value": v64, "unit": UNIT, "ms_per_step": el64 / k * 1e3, "steps": k,
             "mixed_over_fp64": mixed_value / v64,
             "steps_compared": k, "rel_l1_mixed_vs_fp64": l1, "rel_linf_mixed_vs_fp64": linf,
@@ -576,11 +584,12 @@ def run_served(args, capacity):
 
 def run_snapshots(args, snap, hin):
     """Save events every --snap-every steps on the 256^3 mixed run, 40 steps:
-    the state leaves the device synchronously (vacgpu_download, then the
-    next steps) or as an asynchronous snapshot (vacgpu_snapshot_begin; a
-    second host thread waits for it and copies it out while the next steps
-    run, as the vacgb host program's writer thread does).  Wall-clock time
-    of each against the same steps without saves; host buffers pinned."""
+    the state leaves the device synchronously (vacgpu_download into a pinned
+    buffer, then the next steps) or as an asynchronous snapshot
+    (vacgpu_snapshot_begin; a second host thread waits for it and takes it in
+    place from the library's page-locked copy, as the vacgb host program's
+    writer thread does, while the next steps run).  Wall-clock time of each
+    against the same steps without saves."""
     import threading as th
     import torch
     from vac_gb300 import abi
@@ -594,7 +603,7 @@ def run_snapshots(args, snap, hin):
         e.upload(snap.w)
         if mode == "async":  # first use of the slot allocates its buffers
             e.snapshot_begin(0)
-            e.snapshot_wait(0, out.data_ptr())
+            e.snapshot_view(0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         writer = None
@@ -606,7 +615,7 @@ def run_snapshots(args, snap, hin):
                 if writer:
                     writer.join()
                 e.snapshot_begin(0)
-                writer = th.Thread(target=e.snapshot_wait, args=(0, out.data_ptr()))
+                writer = th.Thread(target=e.snapshot_view, args=(0,))
                 writer.start()
         if writer:
             writer.join()

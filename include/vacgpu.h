@@ -205,7 +205,8 @@ int vacgpu_download(vacgpu_handle* h, double* w);
  * returns at once: the copy leaves the device on a copy stream of its own
  * while later vacgpu_step calls run.  vacgpu_snapshot_wait(h, slot, w)
  * waits for that copy and writes the snapshot to w in vacgpu_download's
- * layout, w(ixM^S,1:nw) (NULL w only releases the slot).  A slot holds one
+ * layout, w(ixM^S,1:nw) (NULL w: no copy; vacgpu_snapshot_data gives the
+ * snapshot in place).  A slot holds one
  * snapshot: a second begin on a pending slot is an error, as is a wait on
  * an empty one.  The caller keeps it and t of the snapshot (vacgpu_step
  * returns them).  The first begin of a slot allocates its device and
@@ -215,6 +216,12 @@ int vacgpu_download(vacgpu_handle* h, double* w);
  * concurrently with it. */
 int vacgpu_snapshot_begin(vacgpu_handle* h, int slot);
 int vacgpu_snapshot_wait(vacgpu_handle* h, int slot, double* w);
+/* The page-locked host copy of slot's completed snapshot in
+ * vacgpu_download's layout, valid from vacgpu_snapshot_wait until the next
+ * vacgpu_snapshot_begin on that slot or vacgpu_destroy: a host that writes
+ * the snapshot itself reads it there and saves the copy into its own array
+ * (wait with w = NULL).  NULL (and the message) if the slot holds none. */
+const double* vacgpu_snapshot_data(vacgpu_handle* h, int slot);
 
 /* Advance: repeat the body of the time loop (src/vac.t:59-106) at most
  * maxsteps times.  Before each step the dt is chosen exactly as VAC does
@@ -412,9 +419,12 @@ int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop);
 int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
                         double* dt, int* finished);
 /* Run (or report) the launch-shape autotuner: persistent CTAs, work-list
- * order (0 round-robin over grids, 1 grid-major) and the six trial times
- * in ms (ctas 152/304/one per tile x order 0/1). */
-int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, double* ms);
+ * order (0 round-robin over grids, 1 grid-major), rows per work item of the
+ * 2-D line sweep (16, 32 or 64; 0 for 3-D batches, which have one item
+ * shape) and the trial times in ms, 18 doubles: per item shape, per CTA
+ * count (two persistent counts, then one CTA per item), per order (0 where
+ * not tried). */
+int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, double* ms);
 void vacgpu_batch_destroy(vacgpu_batch* b);
 
 /* ------------------------------------------------------------- server --

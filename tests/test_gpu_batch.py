@@ -34,8 +34,8 @@ def test_batch_mhd3d_and_tuner(gpu_lib):
     grids = [(inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED), s.x, s.w)
              for s in snaps]
     b = Batch(grids)
-    ctas, order, ms = b.tune()
-    assert ctas > 0 and order in (0, 1) and all(m > 0 for m in ms)
+    ctas, order, rows, ms = b.tune()
+    assert ctas > 0 and order in (0, 1) and rows == 0 and len(ms) == 6 and all(m > 0 for m in ms)
     b.step(5)
     for i, (p, x, w) in enumerate(grids):
         e = Engine(p, x, w)
@@ -47,3 +47,27 @@ def test_batch_mhd3d_and_tuner(gpu_lib):
         for iw in range(p.nw):
             rel = np.abs(got[iw] - ref[iw]).sum() / np.abs(ref[iw]).sum()
             assert rel <= 1e-5, (i, iw, rel)
+
+
+def test_batch_mhd2d_general_and_tuned_rows(gpu_lib):
+    """2-D MHD grids of different sizes on the warp-marching line sweep, one
+    of them with reflecting walls, so the batch runs the sweep's general
+    form while the periodic grids alone run its fast form: the same bits.
+    The tuner picks rows per work item among 16, 32 and 64 (chunking does
+    not change any arithmetic)."""
+    from tests.test_gpu_fused import reflecting
+    snaps = [inistate.orszag_tang(n) for n in (40, 75, 130)]
+    grids = []
+    for i, s in enumerate(snaps):
+        p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
+        if i == 1:
+            reflecting(p, 2)
+        grids.append((p, s.x, s.w))
+    b = Batch(grids)
+    ctas, order, rows, ms = b.tune()
+    assert rows in (16, 32, 64) and len(ms) == 18 and all(m > 0 for m in ms)
+    b.step(6)
+    for i, (p, x, w) in enumerate(grids):
+        e = Engine(p, x, w)
+        e.step(6)
+        assert np.array_equal(bits(b.state(i)), bits(e.state())), i

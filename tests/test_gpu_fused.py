@@ -152,3 +152,36 @@ def test_full_size_uniform_state_is_preserved_exactly():
     for iw in range(w.shape[0]):
         assert np.all(out[iw] == out[iw].flat[0])
         assert abs(out[iw].flat[0] - np.float32(w[iw].flat[0])) <= 1e-7 * abs(w[iw].flat[0]) + 1e-30
+
+
+GRAVITY_CASES = [
+    ("hd2-gravity-cont", lambda: inistate.riemann_2d(48, 5), "woodward", "cont", 12, [0.0, -0.5]),
+    ("ot2-gravity-periodic", lambda: inistate.orszag_tang(40), "minmod", "periodic", 10,
+     [0.3, -0.2]),
+    ("rm3-gravity-periodic", lambda: inistate.random_modes(20, seed=6), "woodward", "periodic", 6,
+     [0.2, 0.0, -0.3]),
+]
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,grav", GRAVITY_CASES, ids=[c[0] for c in GRAVITY_CASES])
+def test_fused_with_gravity(gpu_lib, monkeypatch, name, mk, lim, bc, n, grav):
+    """The fused sweeps' general form (the gravity source of vacusr.gravity.t
+    in the predictor and the corrector) against the oracle and the split
+    kernels."""
+    s = mk()
+    p64 = inistate.params_for(s, limiter=lim, bc=bc)
+    pm = inistate.params_for(s, limiter=lim, bc=bc, precision=abi.PREC_MIXED)
+    o = Oracle(p64, s.x, s.w)
+    o.register_source(abi.SRC_GRAVITY, grav)
+    o.step(n)
+    ref = o.state()
+    out = {}
+    for fz in ("1", "0"):
+        monkeypatch.setenv("VACGPU_FUSED", fz)
+        e = Engine(pm, s.x, s.w)
+        e.register_source(abi.SRC_GRAVITY, grav)
+        e.step(n)
+        out[fz] = e.state()
+        assert (e.kernel_stats()["sweep"][0] > 0) == (fz == "1")
+    assert max(rel_l1(out["1"], ref)) <= MIXED_REL_L1, rel_l1(out["1"], ref)
+    assert max(rel_l1(out["1"], out["0"])) <= FUSED_VS_SPLIT, rel_l1(out["1"], out["0"])

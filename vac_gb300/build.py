@@ -36,6 +36,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("sweep_fused.cu", ["--use_fast_math"]),
     ("sweep_pair.cu", ["--use_fast_math"]),
+    ("sweep_line2.cu", ["--use_fast_math"]),
     ("batch.cu", ["--use_fast_math"]),
     ("server.cu", []),
     ("diag.cu", []),

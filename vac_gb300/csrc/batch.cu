@@ -49,6 +49,9 @@ int vacgpu_internal_set_cur(vacgpu_handle* h, int cur);
 
 namespace {
 
+// rows per work item of the 2-D line sweep (the autotuner's item shapes)
+constexpr int LINE2_SHAPES[3] = {16, 32, 64};
+
 typedef PHMixed<PREC_FF> PHB;
 
 template <int NDIM, int D, bool MHD, int LIMC>
@@ -107,10 +110,12 @@ struct vacgpu_batch {
   BInst* d_insts;
   CUtensorMap* d_maps;  // per grid: [state buffer][box: x/z, y]
   Ctrl** d_ctrls;
-  // work lists per sweep direction (tile shapes differ): order 0
-  // interleaved over grids, 1 grid-major
-  BItem* d_items[3][2];
-  int nitems[3];
+  // work lists per sweep direction (tile shapes differ), work-list order
+  // (0 interleaved over grids, 1 grid-major) and item shape (2-D line
+  // sweeps: rows per item, LINE2_SHAPES; one shape otherwise)
+  BItem* d_items[3][2][3];
+  int nitems[3][3];
+  int nshape, shape;
   cudaStream_t st;
   int nw;
   bool ready;
@@ -118,9 +123,10 @@ struct vacgpu_batch {
   // work-list order
   int ctas, order;
   bool pair;     // 3-D grids on the two-cells-per-thread sweep
-  bool pairgen;  // ... in its general form
+  bool line2;    // 2-D grids on the warp-marching sweep
+  bool pairgen;  // ... either in its general form
   bool tuned;
-  double tune_ms[8];
+  double tune_ms[18];
   int it0;
   struct G {
     int nsteps, par;
@@ -146,8 +152,8 @@ void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
                     int order) {
   constexpr int NW = MHD ? 2 + 2 * NDIM : 2 + NDIM;
   const int smem = fused_smem_floats(NW, fused_kind(NDIM, D)) * 4;
-  const int n = b->nitems[D];
-  const BItem* items = b->d_items[D][order];
+  const int n = b->nitems[D][0];
+  const BItem* items = b->d_items[D][order][0];
   if (ctas <= 0 || ctas > n) ctas = n;
 #define KB(DD, LL)                                                          \
   {                                                                         \
@@ -171,10 +177,16 @@ void launch_sweep_b(vacgpu_batch* b, int D, int LIMC, int sweep, int ctas,
 #undef KB
 }
 
-void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas, int order) {
+void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas, int order, int shape) {
   const vacgpu_params& p = b->p0;
+  if (b->line2) {
+    launch_batch_line2(b->d_items[D][order][shape], b->nitems[D][shape], b->d_insts, sweep, D,
+                       p.physics == VACGPU_PHYS_MHD, p.typelimiter[0], b->pairgen, ctas,
+                       b->st);
+    return;
+  }
   if (b->pair) {
-    launch_batch_pair(b->d_items[D][order], b->nitems[D], b->d_insts, b->d_maps, sweep, D,
+    launch_batch_pair(b->d_items[D][order][0], b->nitems[D][0], b->d_insts, b->d_maps, sweep, D,
                       p.physics == VACGPU_PHYS_MHD, p.typelimiter[0], b->pairgen, ctas,
                       b->st);
     return;
@@ -197,7 +209,7 @@ void launch_sweep_any(vacgpu_batch* b, int D, int sweep, int ctas, int order) {
 }
 
 // One step of every grid (the body of VAC's time loop, batched).
-void issue_step(vacgpu_batch* b, int parity, int ctas, int order) {
+void issue_step(vacgpu_batch* b, int parity, int ctas, int order, int shape) {
   const vacgpu_params& p = b->p0;
   const int n = b->n;
   const bool mhd = p.physics == VACGPU_PHYS_MHD;
@@ -219,7 +231,7 @@ void issue_step(vacgpu_batch* b, int parity, int ctas, int order) {
   const int nsw = p.ndim;
   for (int s = 0; s < nsw; s++) {
     const int D = (!parity || p.typedimsplit == VACGPU_SPLIT_XY) ? s : nsw - 1 - s;
-    launch_sweep_any(b, D, s, ctas, order);  // also fills the ghost cells
+    launch_sweep_any(b, D, s, ctas, order, shape);  // also fills the ghost cells
   }
   launchb_control(3, b->d_ctrls, n, p, nsw & 1, 0, 0.0, b->st);
 }
@@ -264,12 +276,17 @@ int prepare(vacgpu_batch* b) {
   }
   // the pair sweep when it applies to every grid: the single-grid path
   // runs it on each of them, so the batch gives the same bits
+  const bool mhd = b->p0.physics == VACGPU_PHYS_MHD;
   b->pair = b->p0.ndim == 3;
+  b->line2 = b->p0.ndim == 2;
   b->pairgen = false;
-  for (int i = 0; i < n && b->pair; i++) {
-    b->pair = pair_applies(ins[i].fa, b->p0.physics == VACGPU_PHYS_MHD);
-    b->pairgen = b->pairgen || pair_general(ins[i].fa, b->p0.physics == VACGPU_PHYS_MHD);
+  for (int i = 0; i < n; i++) {
+    b->pair = b->pair && pair_applies(ins[i].fa, mhd);
+    b->line2 = b->line2 && line2_applies(ins[i].fa, mhd);
+    b->pairgen = b->pairgen || pair_general(ins[i].fa, mhd);
   }
+  b->nshape = b->line2 ? 3 : 1;
+  b->shape = 0;
   BCK(cudaMalloc(&b->d_insts, sizeof(BInst) * n));
   BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 4 * n));
   BCK(cudaMalloc(&b->d_ctrls, sizeof(Ctrl*) * n));
@@ -288,9 +305,17 @@ int prepare(vacgpu_batch* b) {
     // the pair sweep's x tiles start one column left of the mesh: nx + 1
     // columns of faces
     const int xext = b->pair && D == 0 ? 1 : 0;
+    for (int sh = 0; sh < b->nshape; sh++) {
     std::vector<std::vector<BItem>> per(n);
     for (int i = 0; i < n; i++) {
       const DevGrid& g = ins[i].fa.g;
+      if (b->line2) {  // (strip, first and end row), strips fastest
+        const int ns = line2_strips(D, mhd, g.nx[0]), rows = LINE2_SHAPES[sh];
+        for (int y = 0; y < g.nx[1]; y += rows)
+          for (int x = 0; x < ns; x++)
+            per[i].push_back({i, x, 2 + y, 2 + std::min(y + rows, g.nx[1])});
+        continue;
+      }
       const int nbx = (g.nx[0] + xext + tx - 1) / tx, nby = (g.nx[ar] + ty - 1) / ty;
       const int nbz = g.ndim == 3 ? (g.nx[am] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
       for (int z = 0; z < nbz; z++)
@@ -308,12 +333,13 @@ int prepare(vacgpu_batch* b) {
     std::sort(idx.begin(), idx.end(),
               [&](int a, int c) { return per[a].size() > per[c].size(); });
     for (int i : idx) gm.insert(gm.end(), per[i].begin(), per[i].end());
-    b->nitems[D] = (int)rr.size();
+    b->nitems[D][sh] = (int)rr.size();
     for (int o = 0; o < 2; o++) {
       const std::vector<BItem>& l = o ? gm : rr;
-      BCK(cudaMalloc(&b->d_items[D][o], sizeof(BItem) * l.size()));
-      BCK(cudaMemcpy(b->d_items[D][o], l.data(), sizeof(BItem) * l.size(),
+      BCK(cudaMalloc(&b->d_items[D][o][sh], sizeof(BItem) * l.size()));
+      BCK(cudaMemcpy(b->d_items[D][o][sh], l.data(), sizeof(BItem) * l.size(),
                      cudaMemcpyHostToDevice));
+    }
     }
   }
   b->ready = true;
@@ -322,8 +348,11 @@ int prepare(vacgpu_batch* b) {
 
 // Autotuner: time one step of every candidate launch shape on the batch
 // itself (state and control blocks restored after each trial) and keep the
-// fastest.  Candidates: persistent CTAs = 1, 2 per SM (the resident limit of
-// the 103 KB kernel) or one CTA per work item, times two work-list orders.
+// fastest.  Candidates: persistent CTAs (per SM: 1 and 2 for the one-cell
+// sweep, whose 103 KB CTAs fit twice; 2 and 3 for the pair sweep; 4 and 8
+// CTAs of four warps for the 2-D line sweep) or one CTA (line sweep: one
+// warp) per work item, times two work-list orders, times the item shapes
+// (2-D line sweep: 16, 32 or 64 rows per item).
 int autotune(vacgpu_batch* b) {
   if (b->tuned) return 0;
   const int n = b->n;
@@ -356,32 +385,41 @@ int autotune(vacgpu_batch* b) {
     return 0;
   };
   if (copy(true)) return 1;
-  const int cand_ctas[3] = {152, 304, 0};  // 0: one CTA per work item
+  int sms = 152;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int per_sm[2] = {b->line2 ? 4 : b->pair ? 2 : 1, b->line2 ? 8 : b->pair ? 3 : 2};
+  const int cand_ctas[3] = {per_sm[0] * sms, per_sm[1] * sms, 0};  // 0: one per item
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int bc = 304, bo = 0, k = 0;
-  for (int c = 0; c < 3; c++)
-    for (int o = 0; o < 2; o++, k++) {
-      launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
-      issue_step(b, b->it0 & 1, cand_ctas[c], o);  // warm
-      if (copy(false)) return 1;
-      launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
-      cudaEventRecord(e0, b->st);
-      issue_step(b, b->it0 & 1, cand_ctas[c], o);
-      cudaEventRecord(e1, b->st);
-      cudaEventSynchronize(e1);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      b->tune_ms[k] = ms;
-      if (ms < best) {
-        best = ms;
-        bc = cand_ctas[c];
-        bo = o;
+  int bc = cand_ctas[1], bo = 0, bs = 0, k = 0;
+  for (int sh = 0; sh < b->nshape; sh++)
+    for (int c = 0; c < 3; c++)
+      for (int o = 0; o < 2; o++, k++) {
+        launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
+        issue_step(b, b->it0 & 1, cand_ctas[c], o, sh);  // warm
+        if (copy(false)) return 1;
+        launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
+        cudaEventRecord(e0, b->st);
+        issue_step(b, b->it0 & 1, cand_ctas[c], o, sh);
+        cudaEventRecord(e1, b->st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        b->tune_ms[k] = ms;
+        if (ms < best) {
+          best = ms;
+          bc = cand_ctas[c];
+          bo = o;
+          bs = sh;
+        }
+        if (copy(false)) return 1;
       }
-      if (copy(false)) return 1;
-    }
   BCK(cudaStreamSynchronize(b->st));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -389,6 +427,7 @@ int autotune(vacgpu_batch* b) {
   BCK(cudaGetLastError());
   b->ctas = bc;
   b->order = bo;
+  b->shape = bs;
   b->tuned = true;
   return 0;
 }
@@ -475,7 +514,7 @@ int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop) {
     BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     launchb_control(4, b->d_ctrls, b->n, b->p0, 0, nsteps, tstop, b->st);
     for (int s = 0; s < nsteps; s++)
-      issue_step(b, (par + s) & 1, b->ctas, b->order);
+      issue_step(b, (par + s) & 1, b->ctas, b->order, b->shape);
     BCK(cudaStreamEndCapture(b->st, &gr));
     BCK(cudaGraphInstantiate(&ex, gr, 0));
     cudaGraphDestroy(gr);
@@ -512,13 +551,15 @@ int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
   return 0;
 }
 
-int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, double* ms) {
+int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, double* ms) {
   if (!b) return bfail("null batch");
   if (prepare(b) || autotune(b)) return 1;
-  if (ctas) *ctas = b->ctas > 0 ? b->ctas : b->nitems[0];
+  const int ni = b->nitems[0][b->shape];
+  if (ctas) *ctas = b->ctas > 0 ? b->ctas : (b->line2 ? (ni + 3) / 4 : ni);
   if (order) *order = b->order;
+  if (rows) *rows = b->line2 ? LINE2_SHAPES[b->shape] : 0;
   if (ms)
-    for (int k = 0; k < 6; k++) ms[k] = b->tune_ms[k];
+    for (int k = 0; k < 18; k++) ms[k] = k < 6 * b->nshape ? b->tune_ms[k] : 0.0;
   return 0;
 }
 
@@ -531,7 +572,8 @@ void vacgpu_batch_destroy(vacgpu_batch* b) {
   cudaFree(b->d_maps);
   cudaFree(b->d_ctrls);
   for (int D = 0; D < 3; D++)
-    for (int o = 0; o < 2; o++) cudaFree(b->d_items[D][o]);
+    for (int o = 0; o < 2; o++)
+      for (int sh = 0; sh < 3; sh++) cudaFree(b->d_items[D][o][sh]);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }

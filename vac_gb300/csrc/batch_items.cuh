@@ -36,4 +36,19 @@ bool pair_general(const FusedArgs& a, bool mhd);
 // minmod or woodward, even row offsets); also false when VACGPU_PAIR=0.
 bool pair_applies(const FusedArgs& a, bool mhd);
 
+// Strips of the 2-D line sweep along D over nx mesh columns: 60 output
+// columns a strip (64 for the HD y sweep, which needs no halo columns).
+__host__ __device__ inline int line2_strips(int D, bool mhd, int nx) {
+  const int tw = (D == 0 || mhd) ? 60 : 64;
+  return (nx + tw - 1) / tw;
+}
+
+// The same for 2-D grids and the warp-marching sweep (sweep_line2.cu),
+// whose work items are (grid, strip bx, chunk of rows by) and whose
+// launch runs `ctas` CTAs of four warps (0: one warp per item).
+bool line2_applies(const FusedArgs& a, bool mhd);
+int line2_items(int D, bool mhd, const DevGrid& g, int* nstrips);
+bool launch_batch_line2(const BItem* items, int nitems, const BInst* insts, int sweep, int D,
+                        bool mhd, int lim, bool gen, int ctas, cudaStream_t st);
+
 }  // namespace vacgpu

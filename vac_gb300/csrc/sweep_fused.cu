@@ -10,6 +10,8 @@ int fused_smem_bytes(int nw, int k) { return fused_smem_floats(nw, k) * 4; }
 
 bool launch_sweep_pair(const FusedArgs& a, int D, bool mhd, const void* tmap, int nzc,
                        cudaStream_t st);
+bool launch_sweep_line2(const FusedArgs& a, const float* win, int D, bool mhd,
+                        cudaStream_t st);
 
 template <int NDIM, int D, bool MHD, int LIMC, int PMF>
 static void launch_pmf(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
@@ -59,7 +61,7 @@ static void launch_one(const CUtensorMap* map, const FusedArgs& a, dim3 grid,
     launch_lim<NDIM, D, MHD, LIMC_RUNTIME>(map, a, grid, st);
 }
 
-bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
+bool launch_sweep_fused(const SweepArgs& s, const void* tmap, const float* win, float* wout,
                         const float* const* idxf, int nzc, cudaStream_t st) {
   const int nd = s.g.ndim;
   if (s.d0 != s.d1 || s.ndir != nd || (nd != 2 && nd != 3)) return false;
@@ -99,6 +101,8 @@ bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
   // applies; VACGPU_PAIR=0 keeps the one-cell kernel
   if (nd == 3 && launch_sweep_pair(a, s.d0, s.mhd, tmap, nzc, st))
     return true;
+  // 2-D grids: the warp-marching two-cells-per-thread kernel where it applies
+  if (nd == 2 && launch_sweep_line2(a, win, s.d0, s.mhd, st)) return true;
   const CUtensorMap* map = (const CUtensorMap*)tmap;
   const int D = s.d0;
 #define L1(ND, DD)                                              \

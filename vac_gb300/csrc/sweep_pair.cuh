@@ -70,15 +70,18 @@ __device__ __forceinline__ void p_tsq(f2 a, f2& h, f2& l, const PairK& k) {
   l = ffma(a, a, h * k.mone);
 }
 
-// Thermal pressure (unclipped) of a 3-D state in double-float arithmetic;
-// hbb receives B^2/2 (MHD).  The same steps as pressure_mixed<.., PREC_FF>.
-template <bool MHD>
+// Variables of a state with ND vector components: rho, m_1..m_ND (u[1..ND]),
+// e (u[ND+1]), B_1..B_ND (u[ND+2..2ND+1], MHD).
+
+// Thermal pressure (unclipped) in double-float arithmetic; hbb receives
+// B^2/2 (MHD).  The same steps as pressure_mixed<.., PREC_FF>.
+template <bool MHD, int ND = 3>
 __device__ __forceinline__ f2 p_pressure(const f2* u, f2 rinv, const PairK& k,
                                          f2& hbb) {
   f2 mh, ml;
   p_tsq(u[1], mh, ml, k);
 #pragma unroll
-  for (int c = 2; c <= 3; c++) {
+  for (int c = 2; c <= ND; c++) {
     f2 ph, pl, t;
     p_tsq(u[c], ph, pl, k);
     p_tsum(mh, ph, mh, t);
@@ -91,9 +94,9 @@ __device__ __forceinline__ f2 p_pressure(const f2* u, f2 rinv, const PairK& k,
   f2 sh = qh, sl = ql;
   if (MHD) {
     f2 bh, bl;
-    p_tsq(u[5], bh, bl, k);
+    p_tsq(u[ND + 2], bh, bl, k);
 #pragma unroll
-    for (int c = 6; c <= 7; c++) {
+    for (int c = ND + 3; c <= 2 * ND + 1; c++) {
       f2 ph, pl, t;
       p_tsq(u[c], ph, pl, k);
       p_tsum(bh, ph, bh, t);
@@ -104,47 +107,48 @@ __device__ __forceinline__ f2 p_pressure(const f2* u, f2 rinv, const PairK& k,
     p_tsum(qh, bh, sh, t);
     sl = ql + bl + t;
   }
-  f2 d = ffma(k.mhalf, sh, u[4]);
+  f2 d = ffma(k.mhalf, sh, u[ND + 1]);
   d = ffma(k.mhalf, sl, d);
   return k.gm1 * d;
 }
 
 // getflux + transport along DD (src/vacphys.mhd0.t:149-205,
-// src/vacphys.t.hd:49-75) of a 3-D state; p: unclipped thermal pressure,
-// rinv: 1/rho.  f[rho] is m_DD itself (v rho up to a rounding).
-template <int DD, bool MHD>
+// src/vacphys.t.hd:49-75); p: unclipped thermal pressure, rinv: 1/rho.
+// f[rho] is m_DD itself (v rho up to a rounding).
+template <int DD, bool MHD, int ND = 3>
 __device__ __forceinline__ void p_flux(const f2* u, const PairK& k, f2* f,
                                        f2& p, f2& rinv) {
+  constexpr int E = ND + 1;  // e; B_c is u[E + c]
   rinv = vrcp(u[0]);
   const f2 v = u[1 + DD] * rinv;
   f2 hbb;
-  p = p_pressure<MHD>(u, rinv, k, hbb);
+  p = p_pressure<MHD, ND>(u, rinv, k, hbb);
   f[0] = u[1 + DD];
   if (MHD) {
     const f2 pt = p + hbb;
-    const f2 nbi = u[5 + DD] * k.mone;
+    const f2 nbi = u[E + 1 + DD] * k.mone;
 #pragma unroll
-    for (int c = 1; c <= 3; c++) {
-      const f2 fk = c == DD + 1 ? ffma(u[4 + c], nbi, pt) : u[4 + c] * nbi;
+    for (int c = 1; c <= ND; c++) {
+      const f2 fk = c == DD + 1 ? ffma(u[E + c], nbi, pt) : u[E + c] * nbi;
       f[c] = ffma(v, u[c], fk);
     }
-    f2 bm = u[5] * u[1];
-    bm = ffma(u[6], u[2], bm);
-    bm = ffma(u[7], u[3], bm);
-    const f2 t = ffma(nbi, bm, u[1 + DD] * pt);
-    f[4] = ffma(t, rinv, v * u[4]);
+    f2 bm = u[E + 1] * u[1];
 #pragma unroll
-    for (int c = 1; c <= 3; c++) {
+    for (int c = 2; c <= ND; c++) bm = ffma(u[E + c], u[c], bm);
+    const f2 t = ffma(nbi, bm, u[1 + DD] * pt);
+    f[E] = ffma(t, rinv, v * u[E]);
+#pragma unroll
+    for (int c = 1; c <= ND; c++) {
       if (c == DD + 1)
-        f[4 + c] = f2s(0.0f);
+        f[E + c] = f2s(0.0f);
       else
-        f[4 + c] = ffma(v, u[4 + c], (u[c] * rinv) * nbi);
+        f[E + c] = ffma(v, u[E + c], (u[c] * rinv) * nbi);
     }
   } else {
     const f2 pc = vclamp_lo(p, k.smallp);
 #pragma unroll
-    for (int c = 1; c <= 3; c++) f[c] = c == DD + 1 ? ffma(v, u[c], pc) : v * u[c];
-    f[4] = v * (pc + u[4]);
+    for (int c = 1; c <= ND; c++) f[c] = c == DD + 1 ? ffma(v, u[c], pc) : v * u[c];
+    f[E] = v * (pc + u[E]);
   }
 }
 
@@ -152,14 +156,15 @@ __device__ __forceinline__ void p_flux(const f2* u, const PairK& k, f2* f,
 // inverse densities riL, riR), as PHMixed::cmax_mean: the mean's pressure
 // (pL+pR)/2 + (g-1)(|rhoR mL - rhoL mR|^2/(4 rhoL rhoR (rhoL+rhoR))
 // + |BL-BR|^2/8) has no cancellation.  Only M's rho, m_DD and B are read.
-template <int DD, bool MHD>
+template <int DD, bool MHD, int ND = 3>
 __device__ __forceinline__ f2 p_cmax_mean(const f2* L, const f2* R,
                                           const f2* M, f2 pL, f2 pR, f2 riL,
                                           f2 riR, const PairK& k) {
+  constexpr int B1 = ND + 2;  // B_1
   const f2 rinv = vrcp(M[0]);
   f2 kk;
 #pragma unroll
-  for (int c = 1; c <= 3; c++) {
+  for (int c = 1; c <= ND; c++) {
     const f2 t = ffma(R[0], L[c], (L[0] * R[c]) * k.mone);
     kk = c == 1 ? t * t : ffma(t, t, kk);
   }
@@ -168,10 +173,10 @@ __device__ __forceinline__ f2 p_cmax_mean(const f2* L, const f2* R,
   if (MHD) {
     f2 db;
 #pragma unroll
-    for (int c = 5; c <= 7; c++) {
+    for (int c = B1; c < B1 + ND; c++) {
       const f2 t = L[c] - R[c];
-      db = c == 5 ? t * t : ffma(t, t, db);
-      bb = c == 5 ? M[c] * M[c] : ffma(M[c], M[c], bb);
+      db = c == B1 ? t * t : ffma(t, t, db);
+      bb = c == B1 ? M[c] * M[c] : ffma(M[c], M[c], bb);
     }
     corr = ffma(k.eighth, db, corr);
   }
@@ -181,7 +186,7 @@ __device__ __forceinline__ f2 p_cmax_mean(const f2* L, const f2* R,
   const f2 va = vabs(M[1 + DD] * rinv);
   if (MHD) {
     const f2 cf2 = ffma(bb, rinv, cs2);
-    const f2 bi = M[5 + DD];
+    const f2 bi = M[B1 + DD];
     const f2 q = cs2 * (bi * bi) * rinv;
     f2 disc = ffma(cf2, cf2, f2s(-4.0f) * q);
     disc = vmax(disc, f2s(0.0f));
@@ -225,8 +230,8 @@ __device__ __forceinline__ f2 p_hlim(f2 a, f2 b, const PairK& k) {
 
 // getboundary's ghost images of one new cell value per variable (scalar,
 // one lane): the composition of the region copies of src/vacgrid.t:195-413
-// as in Fused::ghost_images.
-template <int NW>
+// as in Fused::ghost_images (NDIM = 2: gc[2] = 0 and no z images).
+template <int NW, int NDIM = 3>
 __device__ __forceinline__ void pair_ghost_images(const FusedArgs& a,
                                                   const int* gc, long long off,
                                                   const float* acc) {
@@ -235,7 +240,7 @@ __device__ __forceinline__ void pair_ghost_images(const FusedArgs& a,
   typedef Fused<3, 0, true, PREC_FF, LIMC_MINMOD> FX;
   const int nx_ = 1 + FX::preimages(a, 0, gc[0], x1, fx, x2);
   const int ny_ = 1 + FX::preimages(a, 1, gc[1], y1, fy, y2);
-  const int nz_ = 1 + FX::preimages(a, 2, gc[2], z1, fz, z2);
+  const int nz_ = NDIM == 3 ? 1 + FX::preimages(a, 2, gc[2], z1, fz, z2) : 1;
 #pragma unroll 1
   for (int k = 0; k < nz_; k++) {
     const int pz = k == 0 ? gc[2] : (k == 1 ? z1 : z2);

@@ -214,6 +214,7 @@ struct vacgpu_handle {
     double* host;
     cudaEvent_t gathered, copied;
     bool pending;
+    bool ready;  // host holds a completed snapshot (until the next begin)
   };
   Snap snap[2];
   cudaStream_t cst;  // copy stream of the snapshot downloads
@@ -563,8 +564,8 @@ void run_sweep(vacgpu_handle* h, int d0, int d1) {
   } else if (h->fused && h->pmode == 0 && d0 == d1 && !h->src_fn) {
     kbegin(h, VACGPU_K_SWEEP);
     // the fused sweep also writes the ghost cells of its output
-    launch_sweep_fused(a, &h->tmap[h->cur][d0 == 1], (float*)wout, h->idxf, h->nzc,
-                       h->st);
+    launch_sweep_fused(a, &h->tmap[h->cur][d0 == 1], (const float*)w, (float*)wout, h->idxf,
+                       h->nzc, h->st);
     kend(h);
   } else {
     const float* fw = (const float*)w;
@@ -1347,6 +1348,7 @@ int vacgpu_snapshot_begin(vacgpu_handle* h, int slot) {
     CK(cudaEventCreateWithFlags(&sn.gathered, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&sn.copied, cudaEventDisableTiming));
   }
+  sn.ready = false;
   // the gather follows the steps issued so far on the handle's stream; the
   // download waits for it on the copy stream, so later steps overlap it
   const unsigned nb = (unsigned)((n + 255) / 256);
@@ -1371,7 +1373,21 @@ int vacgpu_snapshot_wait(vacgpu_handle* h, int slot, double* w) {
   CK(cudaEventSynchronize(sn.copied));
   if (w) memcpy(w, sn.host, sizeof(double) * h->g.ncell * h->nw);
   sn.pending = false;
+  sn.ready = true;
   return 0;
+}
+
+const double* vacgpu_snapshot_data(vacgpu_handle* h, int slot) {
+  if (!h || slot < 0 || slot > 1) {
+    fail("bad handle or snapshot slot");
+    return nullptr;
+  }
+  const vacgpu_handle::Snap& sn = h->snap[slot];
+  if (!sn.ready) {
+    fail("no completed snapshot in slot " + std::to_string(slot));
+    return nullptr;
+  }
+  return sn.host;
 }
 
 int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,

@@ -281,7 +281,8 @@ void launch_correct_roe_mixed(const SweepArgs& s, const float* w,
 // false when no fused instance exists for the configuration.  `tmap` is the
 // CUtensorMap (as bytes) of the input state buffer with the box of the sweep
 // direction (fused_box_rows).
-bool launch_sweep_fused(const SweepArgs& s, const void* tmap, float* wout,
+bool launch_sweep_fused(const SweepArgs& s, const void* tmap, const float* win,
+                        float* wout,
                         const float* const* idxf, int nzc, cudaStream_t st);
 // rows of the fused sweep's TMA box: x and z sweeps and the 3-D y sweep
 // (k=0), the 2-D y sweep (k=1)

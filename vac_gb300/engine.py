@@ -27,6 +27,7 @@ SYMBOLS = [
     "vacgpu_server_submit", "vacgpu_server_result", "vacgpu_server_timing",
     "vacgpu_server_stats", "vacgpu_server_destroy", "vacgpu_measure_fp64_peak",
     "vacgpu_register_source_fn", "vacgpu_snapshot_begin", "vacgpu_snapshot_wait",
+    "vacgpu_snapshot_data",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
@@ -61,6 +62,8 @@ def lib():
         L.vacgpu_register_source_fn.argtypes = [vp, vp, vp, vp]
         L.vacgpu_snapshot_begin.argtypes = [vp, C.c_int]
         L.vacgpu_snapshot_wait.argtypes = [vp, C.c_int, vp]
+        L.vacgpu_snapshot_data.argtypes = [vp, C.c_int]
+        L.vacgpu_snapshot_data.restype = C.POINTER(C.c_double)
         L.vacgpu_destroy.argtypes = [vp]
         L.vacgpu_destroy.restype = None
         L.vacgpu_last_error.argtypes = [C.c_char_p, C.c_int]
@@ -76,7 +79,7 @@ def lib():
         L.vacgpu_batch_download.argtypes = [vp, C.c_int, dp]
         L.vacgpu_batch_step.argtypes = [vp, C.c_int, C.c_double]
         L.vacgpu_batch_status.argtypes = [vp, C.c_int, dp, ip, dp, ip]
-        L.vacgpu_batch_tune.argtypes = [vp, ip, ip, dp]
+        L.vacgpu_batch_tune.argtypes = [vp, ip, ip, ip, dp]
         L.vacgpu_batch_destroy.argtypes = [vp]
         L.vacgpu_batch_destroy.restype = None
         L.vacgpu_server_create.argtypes = [C.c_double, C.c_int, C.c_int, C.POINTER(vp)]
@@ -199,6 +202,18 @@ class Engine:
         return np.stack([out[i * n:(i + 1) * n].reshape(self.nx, order="F")
                          for i in range(self.nw)])
 
+    def snapshot_view(self, slot=0):
+        """Wait for the snapshot in `slot` and return the library's
+        page-locked copy in place: a list of nw arrays of shape nx (views, no
+        host copy; valid until the next snapshot_begin on the slot)."""
+        _ck(lib().vacgpu_snapshot_wait(self.h, slot, None), "vacgpu_snapshot_wait")
+        ptr = lib().vacgpu_snapshot_data(self.h, slot)
+        if not ptr:
+            raise RuntimeError("vacgpu_snapshot_data: %s" % last_error())
+        n = int(np.prod(self.nx))
+        flat = np.ctypeslib.as_array(ptr, shape=(self.nw * n,))
+        return [flat[i * n:(i + 1) * n].reshape(self.nx, order="F") for i in range(self.nw)]
+
     def sums(self):
         out = np.empty(self.nw, dtype=np.float64)
         _ck(lib().vacgpu_sums(self.h, _dp(out)), "vacgpu_sums")
@@ -264,10 +279,13 @@ class Batch:
         _ck(lib().vacgpu_batch_step(self.h, nsteps, tstop), "vacgpu_batch_step")
 
     def tune(self):
-        c, o = C.c_int(), C.c_int()
-        ms = (C.c_double * 6)()
-        _ck(lib().vacgpu_batch_tune(self.h, C.byref(c), C.byref(o), ms), "vacgpu_batch_tune")
-        return c.value, o.value, list(ms)
+        """(persistent CTAs, work-list order, rows per item of the 2-D line
+        sweep or 0, trial times in ms of the candidates tried)."""
+        c, o, r = C.c_int(), C.c_int(), C.c_int()
+        ms = (C.c_double * 18)()
+        _ck(lib().vacgpu_batch_tune(self.h, C.byref(c), C.byref(o), C.byref(r), ms),
+            "vacgpu_batch_tune")
+        return c.value, o.value, r.value, [m for m in ms if m > 0]
 
     def status(self, i):
         t, it, dt, fin = C.c_double(), C.c_int(), C.c_double(), C.c_int()

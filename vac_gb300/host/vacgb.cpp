@@ -709,13 +709,16 @@ int main(int argc, char** argv) {
       const int sit = it;
       const double st_ = t;
       writer = std::thread([&, sit, st_]() {
-        if (vacgpu_snapshot_wait(h, 0, wbuf.data())) {
+        // the records go out straight from the library's page-locked copy
+        const double* snapw = nullptr;
+        if (vacgpu_snapshot_wait(h, 0, nullptr) == 0) snapw = vacgpu_snapshot_data(h, 0);
+        if (!snapw) {
           char buf[1024];
           vacgpu_last_error(buf, sizeof buf);
           writer_err = buf;
           return;
         }
-        write_out(sit, st_, wbuf.data());
+        write_out(sit, st_, snapw);
       });
     } else {  // savefilelog_default
       if (fnames[0].empty()) return;
