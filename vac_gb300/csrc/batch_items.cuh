@@ -44,10 +44,10 @@ __host__ __device__ inline int line2_strips(int D, bool mhd, int nx) {
 }
 
 // The same for 2-D grids and the warp-marching sweep (sweep_line2.cu),
-// whose work items are (grid, strip bx, chunk of rows by) and whose
-// launch runs `ctas` CTAs of four warps (0: one warp per item).
+// whose work items are (grid, strip bx, output rows by .. bz-1 as
+// ghost-range indices) and whose launch runs `ctas` CTAs of four warps (0:
+// one warp per item).
 bool line2_applies(const FusedArgs& a, bool mhd);
-int line2_items(int D, bool mhd, const DevGrid& g, int* nstrips);
 bool launch_batch_line2(const BItem* items, int nitems, const BInst* insts, int sweep, int D,
                         bool mhd, int lim, bool gen, int ctas, cudaStream_t st);
 

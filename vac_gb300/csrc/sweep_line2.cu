@@ -23,7 +23,8 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
 }
 
 // Batched grids: each warp takes items gw, gw + W, ... of the work list
-// (W warps in the launch); an item is (grid, strip, chunk of rows).
+// (W warps in the launch); an item is (grid, strip bx, output rows by ..
+// bz-1 in ghost-range indices).
 template <int D, bool MHD, int LIMC, bool GEN>
 __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
     kb_sweep_line2(const BItem* __restrict__ items, int nitems, const BInst* __restrict__ insts,
@@ -33,9 +34,8 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
     const BItem item = items[it];
     const BInst* in = insts + item.inst;
     const int src = in->fa.ctrl->cur ^ (sweep & 1);
-    const int gya = 2 + item.by * L2_ROWS, gyb = min(gya + L2_ROWS, in->fa.g.nx[1] + 2);
-    Line2<D, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], item.bx, gya, gyb,
-                                  (unsigned)it);
+    Line2<D, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], item.bx, item.by,
+                                  item.bz, (unsigned)it);
   }
 }
 
@@ -52,7 +52,8 @@ bool line2_applies(const FusedArgs& a, bool mhd) {
   return a.g.ndim == 2 && !(a.g.xpad & 1) && !(a.g.P & 1);
 }
 
-int line2_items(int D, bool mhd, const DevGrid& g, int* nstrips) {
+// single-grid work items: strips x chunks of L2_ROWS rows
+static int line2_items(int D, bool mhd, const DevGrid& g, int* nstrips) {
   *nstrips = line2_strips(D, mhd, g.nx[0]);
   return *nstrips * ((g.nx[1] + L2_ROWS - 1) / L2_ROWS);
 }
