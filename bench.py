@@ -206,9 +206,13 @@ def run_batched(args):
     ctas, order, rows, ms = b.tune()
     b.step(50)  # capture + first replay
     torch.cuda.synchronize()
+    if args.profile_range:
+        torch.cuda.profiler.start()
     t0 = time.perf_counter()
     b.step(50)
     el = time.perf_counter() - t0
+    if args.profile_range:
+        torch.cuda.profiler.stop()
     b.close()
     return {"workload": "64 grids 2D HD Riemann, sides log-uniform [64,1024] (seeded), "
                         "cont, minmod, mixed, 50 steps per grid in one graph launch",
@@ -677,6 +681,8 @@ def main():
                     help="skip the 1-core CPU baseline (config 1 in full)")
     ap.add_argument("--cpu-serial-only", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run config 3 alone and print its JSON object (profiling)")
     ap.add_argument("--no-plain", action="store_true", help="skip config 1")
     ap.add_argument("--blast-side", type=int, default=512,
                     help="config 5 cells per side (0: skip)")
@@ -701,6 +707,11 @@ def main():
     ws, rank, lrank = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.batched_only:
+        import torch
+        torch.cuda.set_device(lrank)
+        print(json.dumps(run_batched(args)), flush=True)
         return
 
     import torch

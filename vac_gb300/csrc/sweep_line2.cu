@@ -17,9 +17,12 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
     k_sweep_line2(const FusedArgs a, const float* __restrict__ win, int nstrips, int nitems) {
   const int item = blockIdx.x * (L2_NT / 32) + (threadIdx.x >> 5);
   if (item >= nitems) return;
+  constexpr int RF = line2_ring_floats(MHD ? 6 : 4);
+  __shared__ __align__(16) float ring[L2_NT / 32][RF];
   const int sx = item % nstrips, ch = item / nstrips;
   const int gya = 2 + ch * L2_ROWS, gyb = min(gya + L2_ROWS, a.g.nx[1] + 2);
-  Line2<D, MHD, LIMC, GEN>::run(a, win, a.wout, sx, gya, gyb, (unsigned)item);
+  Line2<D, MHD, LIMC, GEN>::run(a, win, a.wout, ring[threadIdx.x >> 5], sx, gya, gyb,
+                                (unsigned)item);
 }
 
 // Batched grids: each warp takes items gw, gw + W, ... of the work list
@@ -29,18 +32,22 @@ template <int D, bool MHD, int LIMC, bool GEN>
 __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
     kb_sweep_line2(const BItem* __restrict__ items, int nitems, const BInst* __restrict__ insts,
                    int sweep) {
+  constexpr int RF = line2_ring_floats(MHD ? 6 : 4);
+  __shared__ __align__(16) float ring[L2_NT / 32][RF];
   const int nwarps = gridDim.x * (L2_NT / 32);
   for (int it = blockIdx.x * (L2_NT / 32) + (threadIdx.x >> 5); it < nitems; it += nwarps) {
     const BItem item = items[it];
     const BInst* in = insts + item.inst;
     const int src = in->fa.ctrl->cur ^ (sweep & 1);
-    Line2<D, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], item.bx, item.by,
-                                  item.bz, (unsigned)it);
+    Line2<D, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1],
+                                  ring[threadIdx.x >> 5], item.bx, item.by, item.bz,
+                                  (unsigned)it);
   }
 }
 
 // The warp-marching sweep applies to a 2-D grid with one limiter for every
-// variable (minmod or woodward) and even row offsets; also false when
+// variable (minmod or woodward), even row offsets and fewer than 2^31
+// elements in the state; also false when
 // VACGPU_PAIR=0 (the one-cell kernels for every grid).
 bool line2_applies(const FusedArgs& a, bool mhd) {
   if (!pair_enabled()) return false;
@@ -49,7 +56,9 @@ bool line2_applies(const FusedArgs& a, bool mhd) {
   bool uniform = a.ph.typefull != VACGPU_TVDLF1;
   for (int v = 1; v < nw; v++) uniform = uniform && a.ph.lim[v] == l0;
   if (!uniform || (l0 != VACGPU_LIM_WOODWARD && l0 != VACGPU_LIM_MINMOD)) return false;
-  return a.g.ndim == 2 && !(a.g.xpad & 1) && !(a.g.P & 1);
+  // the kernel indexes variables with 32-bit element offsets
+  return a.g.ndim == 2 && !(a.g.xpad & 1) && !(a.g.P & 1) &&
+         a.g.vs * nw < (1LL << 31);
 }
 
 // single-grid work items: strips x chunks of L2_ROWS rows

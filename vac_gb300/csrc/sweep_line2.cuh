@@ -40,6 +40,11 @@ namespace vacgpu {
 
 constexpr int L2_NT = 128;   // threads per CTA: four independent warps
 constexpr int L2_ROWS = 32;  // rows per work item
+constexpr int L2_LOOK = 3;   // rows in flight ahead of use
+constexpr int L2_RING = L2_LOOK + 1;  // staging slots per warp
+
+// floats of one warp's row-staging ring for nw variables
+__host__ __device__ constexpr int line2_ring_floats(int nw) { return L2_RING * nw * 64; }
 
 template <int D, bool MHD, int LIMC, bool GEN>
 struct Line2 {
@@ -58,8 +63,13 @@ struct Line2 {
     const float* win;   // element (gx, gy) of variable v: win[v*vs + gy*P + gx]
     float* wout;        // the same layout
     float* wraw;        // wout without the row offset xpad (ghost images)
-    long long vs, P;
+    long long P;
+    int vs;             // variable stride (2-D states: below 2^31 / NW elements)
     int xpad;
+    const float* idy;   // 1/dy and dy over the ghost range
+    const float* dy;
+    int pmx, alx, ahx;  // x faces: periodic, 'asymm' low and high variable masks
+    int pmy, aly, ahy;  // y faces
     int c0, cl;         // first column of the pair; the column pair it loads
     int nX, nY;         // mesh cells
     int gy_hi;          // last row of the ghost range (nY + 3)
@@ -71,42 +81,77 @@ struct Line2 {
     PairK k;
   };
 
-  static __device__ __forceinline__ void load_row(const Ctx& c, int gy, f2* u) {
-    gy = min(gy, c.gy_hi);  // rows past the ghost range (prefetch) are not used
+  // Rows reach registers through a per-warp ring of L2_RING slots in
+  // shared memory, fed by cp.async 8-byte copies L2_LOOK rows ahead of use:
+  // each lane copies its own pair of every variable and later reads back
+  // exactly those bytes, so rows in flight hold no registers and need no
+  // barrier.  Rows are issued and pulled strictly in order; a pull waits
+  // until at most L2_LOOK-1 copies are outstanding (its own row has landed)
+  // and issues the next row.  The slot a copy overwrites was read one pull
+  // earlier.
+  struct Pipe {
+    unsigned sm;  // shared address of this lane's pair in slot 0, variable 0
+    int issued;   // next row to issue
+  };
+
+  static __device__ __forceinline__ void issue_row(const Ctx& c, Pipe& pp) {
+    const int gy = min(pp.issued, c.gy_hi);  // rows past the ghost range are not used
     const float* p = c.win + (long long)gy * c.P + c.cl;
+    const unsigned s = pp.sm + (unsigned)((pp.issued % L2_RING) * NW * 256);
+#pragma unroll
+    for (int v = 0; v < NW; v++)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s + v * 256),
+                   "l"(p + v * c.vs)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    pp.issued++;
+  }
+
+  static __device__ __forceinline__ void prime(const Ctx& c, Pipe& pp, int first) {
+    pp.issued = first;
+#pragma unroll
+    for (int i = 0; i < L2_LOOK; i++) issue_row(c, pp);
+  }
+
+  static __device__ __forceinline__ void pull(const Ctx& c, Pipe& pp, int gy, f2* u) {
+    asm volatile("cp.async.wait_group %0;" ::"n"(L2_LOOK - 1) : "memory");
+    const unsigned s = pp.sm + (unsigned)((gy % L2_RING) * NW * 256);
 #pragma unroll
     for (int v = 0; v < NW; v++) {
-      const float2 t = __ldg(reinterpret_cast<const float2*>(p + v * c.vs));
-      u[v] = f2m(t.x, t.y);
+      float lo, hi;
+      asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(lo), "=f"(hi) : "r"(s + v * 256));
+      u[v] = f2m(lo, hi);
     }
+    issue_row(c, pp);
+  }
+
+  static __device__ __forceinline__ void drain() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
   }
 
   // getboundary of w1 at the x faces of a strip that reaches them: the
   // first ghost column takes the adjacent mesh value (non-periodic
   // variables, negated where 'asymm')
   static __device__ __forceinline__ void fix_w1_x(const FusedArgs& a, const Ctx& c, f2* w1) {
-    const int pmk = a.periodic_mask[0];
 #pragma unroll
     for (int v = 0; v < NW; v++) {
       float lo, hi;
       f2u(w1[v], lo, hi);
       const float dn = __shfl_down_sync(FULL, lo, 1);
       const float up = __shfl_up_sync(FULL, hi, 1);
-      if (c.c0 + 1 == 1) hi = PS::gfix(hi, dn, v, pmk, a.asymm_lo[0]);
-      if (c.c0 == c.nX + 2) lo = PS::gfix(lo, up, v, pmk, a.asymm_hi[0]);
-      if (c.c0 + 1 == c.nX + 2) hi = PS::gfix(hi, lo, v, pmk, a.asymm_hi[0]);
+      if (c.c0 + 1 == 1) hi = PS::gfix(hi, dn, v, c.pmx, c.alx);
+      if (c.c0 == c.nX + 2) lo = PS::gfix(lo, up, v, c.pmx, c.ahx);
+      if (c.c0 + 1 == c.nX + 2) hi = PS::gfix(hi, lo, v, c.pmx, c.ahx);
       w1[v] = f2m(lo, hi);
     }
   }
 
   // the same along y: value `own` of the ghost row replaced from `src`
-  static __device__ __forceinline__ f2 fix_y1(const FusedArgs& a, f2 own, f2 src, int v,
-                                              int amask) {
+  static __device__ __forceinline__ f2 fix_y1(const Ctx& c, f2 own, f2 src, int v, int amask) {
     float ol, oh, sl, sh;
     f2u(own, ol, oh);
     f2u(src, sl, sh);
-    return f2m(PS::gfix(ol, sl, v, a.periodic_mask[1], amask),
-               PS::gfix(oh, sh, v, a.periodic_mask[1], amask));
+    return f2m(PS::gfix(ol, sl, v, c.pmy, amask), PS::gfix(oh, sh, v, c.pmy, amask));
   }
 
   // addsource2 with wCT = wc: gravity, then Powell's terms for
@@ -251,42 +296,50 @@ struct Line2 {
       hl[v] = p_hlim<LIMC>(dp, dm, c.k);
     }
     f2 divb = f2s(0.0f);
-    if (MHD && c.powell) divb = ffma(bu - bd, f2s(a.idxf[1][gy]), dbx * c.idxx);
+    if (MHD && c.powell) divb = ffma(bu - bd, f2s(c.idy[gy]), dbx * c.idxx);
     predict(a, c, u, hl, c.qdt2 * c.idxx, divb, w1);
     if (GEN && c.fix_x) fix_w1_x(a, c, w1);
   }
 
   // rows gya .. gyb-1 (ghost-range indices)
-  static __device__ void run_x(const FusedArgs& a, const Ctx& c, int gya, int gyb, f2& qmax) {
-    // carried: w of rows r, r+1 and the prefetched r+2; w1 and half slopes
-    // of row r; B_y of w1 at row r-1
-    f2 w0[NW], wp[NW], wn[NW], w1c[NW], hlc[NW];
+  static __device__ void run_x(const FusedArgs& a, const Ctx& c, Pipe& pp, int gya, int gyb,
+                               f2& qmax) {
+    // carried: w of rows r and r+1 (MHD); w1 and half slopes of row r; B_y
+    // of w1 at row r-1 (MHD)
+    f2 w0[NW], wp[NW], w1c[NW], hlc[NW];
     f2 by1m = f2s(0.0f);
-    {
-      f2 wm[NW];
-      load_row(c, gya - 1, wm);
-      load_row(c, gya, w0);
-      load_row(c, gya + 1, wp);
-      if (MHD) {
-        f2 wmm[NW], t1[NW], th[NW];
-        load_row(c, gya - 2, wmm);
-        predict_x(a, c, wm, wmm[BY], w0[BY], gya - 1, t1, th);
-        by1m = t1[BY];
-      }
+    if (MHD) {
+      f2 wmm[NW], wm[NW], t1[NW], th[NW];
+      prime(c, pp, gya - 2);
+      pull(c, pp, gya - 2, wmm);
+      pull(c, pp, gya - 1, wm);
+      pull(c, pp, gya, w0);
+      pull(c, pp, gya + 1, wp);
+      predict_x(a, c, wm, wmm[BY], w0[BY], gya - 1, t1, th);
+      by1m = t1[BY];
       predict_x(a, c, w0, wm[BY], wp[BY], gya, w1c, hlc);
-      load_row(c, gya + 2, wn);
+    } else {
+      prime(c, pp, gya);
+      pull(c, pp, gya, w0);
+      predict_x(a, c, w0, w0[0], w0[0], gya, w1c, hlc);
     }
     const f2 ncq = f2s(-0.5f * c.qdt) * c.idxx;
     for (int r = gya; r < gyb; r++) {
-      f2 w1n[NW], hln[NW], wnn[NW];
-      predict_x(a, c, wp, w0[BY], wn[BY], r + 1, w1n, hln);
-      load_row(c, r + 3, wnn);
+      // predictor of row r+1: its state, and B_y of w at rows r and r+2 (MHD)
+      f2 w1n[NW], hln[NW], wn[NW];
+      if (MHD) {
+        pull(c, pp, r + 2, wn);
+        predict_x(a, c, wp, w0[BY], wn[BY], r + 1, w1n, hln);
+      } else {
+        pull(c, pp, r + 1, wn);
+        predict_x(a, c, wn, wn[0], wn[0], r + 1, w1n, hln);
+      }
       // B_y of w1 at rows r-1 and r+1; ghost rows of non-periodic y faces
       // take the adjacent mesh row's
       f2 byd = by1m, byu = w1n[BY];
       if (MHD && GEN && c.fix_y) {
-        if (r == 2) byd = fix_y1(a, byd, w1c[BY], BY, a.asymm_lo[1]);
-        if (r == c.nY + 1) byu = fix_y1(a, byu, w1c[BY], BY, a.asymm_hi[1]);
+        if (r == 2) byd = fix_y1(c, byd, w1c[BY], BY, c.aly);
+        if (r == c.nY + 1) byu = fix_y1(c, byu, w1c[BY], BY, c.ahy);
       }
       // faces (c0|c0+1) and (c0+1|c0+2): the right state of the second from
       // the next lane
@@ -319,7 +372,7 @@ struct Line2 {
           f2u(w1c[BX], bl, bh);
           const float bm_ = __shfl_up_sync(FULL, bh, 1);
           const float bp_ = __shfl_down_sync(FULL, bl, 1);
-          divb = ffma(byu - byd, f2s(a.idxf[1][r]), f2m(bh - bm_, bp_ - bl) * c.idxx);
+          divb = ffma(byu - byd, f2s(c.idy[r]), f2m(bh - bm_, bp_ - bl) * c.idxx);
         }
         sources(a, c, c.qs2, w1c, c.nqs2h * divb, acc);
       }
@@ -327,9 +380,12 @@ struct Line2 {
       by1m = w1c[BY];
 #pragma unroll
       for (int v = 0; v < NW; v++) {
-        w0[v] = wp[v];
-        wp[v] = wn[v];
-        wn[v] = wnn[v];
+        if (MHD) {
+          w0[v] = wp[v];
+          wp[v] = wn[v];
+        } else {
+          w0[v] = wn[v];
+        }
         w1c[v] = w1n[v];
         hlc[v] = hln[v];
       }
@@ -340,20 +396,22 @@ struct Line2 {
 
   // output rows gya .. gyb-1: iterations r = gya-1 .. gyb predict row r,
   // form the face (r-1|r) and update row r-1
-  static __device__ void run_y(const FusedArgs& a, const Ctx& c, int gya, int gyb, f2& qmax) {
+  static __device__ void run_y(const FusedArgs& a, const Ctx& c, Pipe& pp, int gya, int gyb,
+                               f2& qmax) {
     f2 wm[NW], w0[NW], wp[NW], w1p[NW], hlp[NW], Gp[NW];
     f2 b1pp = f2s(0.0f);  // B_y of w1 at row r-2
-    load_row(c, gya - 2, wm);
-    load_row(c, gya - 1, w0);
-    load_row(c, gya, wp);
+    prime(c, pp, gya - 2);
+    pull(c, pp, gya - 2, wm);
+    pull(c, pp, gya - 1, w0);
+    pull(c, pp, gya, wp);
 #pragma unroll
     for (int v = 0; v < NW; v++) w1p[v] = hlp[v] = Gp[v] = f2s(0.0f);
-    float idp = a.idxf[1][gya - 2], dyp = a.dxf[1][gya - 2];  // row r-1
-    float idc = a.idxf[1][gya - 1], dyc = a.dxf[1][gya - 1];  // row r
+    float idp = c.idy[gya - 2], dyp = c.dy[gya - 2];  // row r-1
+    float idc = c.idy[gya - 1], dyc = c.dy[gya - 1];  // row r
     for (int r = gya - 1; r <= gyb; r++) {
       f2 wn[NW];
-      load_row(c, r + 2, wn);
-      const float idn = a.idxf[1][min(r + 1, c.gy_hi)], dyn = a.dxf[1][min(r + 1, c.gy_hi)];
+      pull(c, pp, r + 2, wn);
+      const float idn = c.idy[min(r + 1, c.gy_hi)], dyn = c.dy[min(r + 1, c.gy_hi)];
       // predictor of row r
       f2 w1[NW], hl[NW];
 #pragma unroll
@@ -373,11 +431,11 @@ struct Line2 {
       if (GEN && c.fix_y) {
         if (r == 2) {
 #pragma unroll
-          for (int v = 0; v < NW; v++) w1p[v] = fix_y1(a, w1p[v], w1[v], v, a.asymm_lo[1]);
+          for (int v = 0; v < NW; v++) w1p[v] = fix_y1(c, w1p[v], w1[v], v, c.aly);
         }
         if (r == c.nY + 2) {
 #pragma unroll
-          for (int v = 0; v < NW; v++) w1[v] = fix_y1(a, w1[v], w1p[v], v, a.asymm_hi[1]);
+          for (int v = 0; v < NW; v++) w1[v] = fix_y1(c, w1[v], w1p[v], v, c.ahy);
         }
       }
       // face (r-1|r)
@@ -425,9 +483,10 @@ struct Line2 {
   }
 
   // One work item: strip sx, output rows gya .. gyb-1; win/wout: the state
-  // buffers (without the row offset).
-  static __device__ void run(const FusedArgs& a, const float* win, float* wout, int sx,
-                             int gya, int gyb, unsigned slot) {
+  // buffers (without the row offset); ring: this warp's row-staging area of
+  // line2_ring_floats(NW) floats in shared memory.
+  static __device__ void run(const FusedArgs& a, const float* win, float* wout, float* ring,
+                             int sx, int gya, int gyb, unsigned slot) {
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) return;
     const DevGrid& g = a.g;
@@ -436,7 +495,15 @@ struct Line2 {
     c.win = win + g.xpad;
     c.wout = wout + g.xpad;
     c.wraw = wout;
-    c.vs = g.vs;
+    c.vs = (int)g.vs;
+    c.idy = a.idxf[1];
+    c.dy = a.dxf[1];
+    c.pmx = a.periodic_mask[0];
+    c.alx = a.asymm_lo[0];
+    c.ahx = a.asymm_hi[0];
+    c.pmy = a.periodic_mask[1];
+    c.aly = a.asymm_lo[1];
+    c.ahy = a.asymm_hi[1];
     c.P = g.P;
     c.xpad = g.xpad;
     c.nX = g.nx[0];
@@ -475,13 +542,16 @@ struct Line2 {
     c.srcs = !GEN || a.ph.sourceunsplit;
     c.cfl = !GEN || a.cfl;
     const int all = (1 << NW) - 1;
-    c.fix_x = GEN && a.periodic_mask[0] != all && (gxs <= 1 || gxs + 63 >= c.nX + 2);
-    c.fix_y = GEN && a.periodic_mask[1] != all;
+    c.fix_x = GEN && c.pmx != all && (gxs <= 1 || gxs + 63 >= c.nX + 2);
+    c.fix_y = GEN && c.pmy != all;
     f2 qmax = f2s(0.0f);
+    Pipe pp;
+    pp.sm = smem_u32(ring) + lane * 8;
     if (D == 0)
-      run_x(a, c, gya, gyb, qmax);
+      run_x(a, c, pp, gya, gyb, qmax);
     else
-      run_y(a, c, gya, gyb, qmax);
+      run_y(a, c, pp, gya, gyb, qmax);
+    drain();  // the ring's last copies land before the next item reuses it
     if (c.cfl) {
       float q;
       {
