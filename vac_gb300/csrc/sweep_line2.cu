@@ -28,8 +28,10 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
 // Batched grids: each warp takes items gw, gw + W, ... of the work list
 // (W warps in the launch); an item is (grid, strip bx, output rows by ..
 // bz-1 in ghost-range indices).
+// (register bound: the work-list loop of the general y sweep needs more than
+// 128 registers, so it runs three CTAs per SM rather than spill)
 template <int D, bool MHD, int LIMC, bool GEN>
-__global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4)
+__global__ void __launch_bounds__(L2_NT, MHD ? 2 : (D == 1 && GEN ? 3 : 4))
     kb_sweep_line2(const BItem* __restrict__ items, int nitems, const BInst* __restrict__ insts,
                    int sweep) {
   constexpr int RF = line2_ring_floats(MHD ? 6 : 4);

@@ -62,14 +62,13 @@ struct Line2 {
   struct Ctx {
     const float* win;   // element (gx, gy) of variable v: win[v*vs + gy*P + gx]
     float* wout;        // the same layout
-    float* wraw;        // wout without the row offset xpad (ghost images)
-    long long P;
-    int vs;             // variable stride (2-D states: below 2^31 / NW elements)
-    int xpad;
+    int P;              // row pitch and variable stride (elements; 2-D states
+    int vs;             // stay below 2^31 elements)
     const float* idy;   // 1/dy and dy over the ghost range
     const float* dy;
-    int pmx, alx, ahx;  // x faces: periodic, 'asymm' low and high variable masks
-    int pmy, aly, ahy;  // y faces
+    // boundary variable masks of the x and y faces, 8 bits each: periodic
+    // (bits 0-7), 'asymm' at the low face (8-15) and at the high face (16-23)
+    int bmx, bmy;
     int c0, cl;         // first column of the pair; the column pair it loads
     int nX, nY;         // mesh cells
     int gy_hi;          // last row of the ghost range (nY + 3)
@@ -139,9 +138,10 @@ struct Line2 {
       f2u(w1[v], lo, hi);
       const float dn = __shfl_down_sync(FULL, lo, 1);
       const float up = __shfl_up_sync(FULL, hi, 1);
-      if (c.c0 + 1 == 1) hi = PS::gfix(hi, dn, v, c.pmx, c.alx);
-      if (c.c0 == c.nX + 2) lo = PS::gfix(lo, up, v, c.pmx, c.ahx);
-      if (c.c0 + 1 == c.nX + 2) hi = PS::gfix(hi, lo, v, c.pmx, c.ahx);
+      const int pm = c.bmx & 255, al = (c.bmx >> 8) & 255, ah = c.bmx >> 16;
+      if (c.c0 + 1 == 1) hi = PS::gfix(hi, dn, v, pm, al);
+      if (c.c0 == c.nX + 2) lo = PS::gfix(lo, up, v, pm, ah);
+      if (c.c0 + 1 == c.nX + 2) hi = PS::gfix(hi, lo, v, pm, ah);
       w1[v] = f2m(lo, hi);
     }
   }
@@ -151,7 +151,7 @@ struct Line2 {
     float ol, oh, sl, sh;
     f2u(own, ol, oh);
     f2u(src, sl, sh);
-    return f2m(PS::gfix(ol, sl, v, c.pmy, amask), PS::gfix(oh, sh, v, c.pmy, amask));
+    return f2m(PS::gfix(ol, sl, v, c.bmy & 255, amask), PS::gfix(oh, sh, v, c.bmy & 255, amask));
   }
 
   // addsource2 with wCT = wc: gravity, then Powell's terms for
@@ -338,8 +338,8 @@ struct Line2 {
       // take the adjacent mesh row's
       f2 byd = by1m, byu = w1n[BY];
       if (MHD && GEN && c.fix_y) {
-        if (r == 2) byd = fix_y1(c, byd, w1c[BY], BY, c.aly);
-        if (r == c.nY + 1) byu = fix_y1(c, byu, w1c[BY], BY, c.ahy);
+        if (r == 2) byd = fix_y1(c, byd, w1c[BY], BY, (c.bmy >> 8) & 255);
+        if (r == c.nY + 1) byu = fix_y1(c, byu, w1c[BY], BY, c.bmy >> 16);
       }
       // faces (c0|c0+1) and (c0+1|c0+2): the right state of the second from
       // the next lane
@@ -431,11 +431,11 @@ struct Line2 {
       if (GEN && c.fix_y) {
         if (r == 2) {
 #pragma unroll
-          for (int v = 0; v < NW; v++) w1p[v] = fix_y1(c, w1p[v], w1[v], v, c.aly);
+          for (int v = 0; v < NW; v++) w1p[v] = fix_y1(c, w1p[v], w1[v], v, (c.bmy >> 8) & 255);
         }
         if (r == c.nY + 2) {
 #pragma unroll
-          for (int v = 0; v < NW; v++) w1[v] = fix_y1(c, w1[v], w1p[v], v, c.ahy);
+          for (int v = 0; v < NW; v++) w1[v] = fix_y1(c, w1[v], w1p[v], v, c.bmy >> 16);
         }
       }
       // face (r-1|r)
@@ -494,18 +494,12 @@ struct Line2 {
     Ctx c;
     c.win = win + g.xpad;
     c.wout = wout + g.xpad;
-    c.wraw = wout;
     c.vs = (int)g.vs;
     c.idy = a.idxf[1];
     c.dy = a.dxf[1];
-    c.pmx = a.periodic_mask[0];
-    c.alx = a.asymm_lo[0];
-    c.ahx = a.asymm_hi[0];
-    c.pmy = a.periodic_mask[1];
-    c.aly = a.asymm_lo[1];
-    c.ahy = a.asymm_hi[1];
-    c.P = g.P;
-    c.xpad = g.xpad;
+    c.bmx = a.periodic_mask[0] | a.asymm_lo[0] << 8 | a.asymm_hi[0] << 16;
+    c.bmy = a.periodic_mask[1] | a.asymm_lo[1] << 8 | a.asymm_hi[1] << 16;
+    c.P = (int)g.P;
     c.nX = g.nx[0];
     c.nY = g.nx[1];
     c.gy_hi = g.nG[1] - 1;
@@ -542,8 +536,8 @@ struct Line2 {
     c.srcs = !GEN || a.ph.sourceunsplit;
     c.cfl = !GEN || a.cfl;
     const int all = (1 << NW) - 1;
-    c.fix_x = GEN && c.pmx != all && (gxs <= 1 || gxs + 63 >= c.nX + 2);
-    c.fix_y = GEN && c.pmy != all;
+    c.fix_x = GEN && (c.bmx & 255) != all && (gxs <= 1 || gxs + 63 >= c.nX + 2);
+    c.fix_y = GEN && (c.bmy & 255) != all;
     f2 qmax = f2s(0.0f);
     Pipe pp;
     pp.sm = smem_u32(ring) + lane * 8;
