@@ -230,7 +230,11 @@ const double* vacgpu_snapshot_data(vacgpu_handle* h, int slot);
  * timetofinish (src/vac.t:608-628) holds or t >= tstop (the next save time
  * of the caller's timetosave).  dt, it and t stay on the device between
  * steps; *t, *it, *dt receive their values at return, *finished is set to 1
- * when timetofinish held. */
+ * when timetofinish held.  The fused sweeps wait for their TMA copies with
+ * a bounded wait (about 2^31 cycles); if one gives up, the tiles of that
+ * sweep were not all written, the call fails with that message, the state
+ * on the device is invalid, and every further vacgpu_step on the handle is
+ * refused until vacgpu_upload gives it a new state. */
 int vacgpu_step(vacgpu_handle* h, int maxsteps, double tstop, double* t,
                 int* it, double* dt, int* finished);
 

@@ -120,8 +120,9 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* b,
 }
 
 // Bounded wait for the phase with the given parity; false on timeout
-// (about 2^31 cycles, > 1 s).
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, int parity) {
+// (limit cycles; by default about 2^31, > 1 s).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, int parity,
+                                          long long limit = 1LL << 31) {
   const unsigned a = smem_u32(b);
   const long long t0 = clock64();
   while (true) {
@@ -134,7 +135,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, int parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > (1LL << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -751,7 +752,15 @@ struct Fused {
         ok = wait_plane(0);
       }
       if (__syncthreads_or(!ok)) {  // barrier A
-        if (tid == 0) atomicExch(&ctrl->fault, 1);
+        if (tid == 0) {
+          atomicExch(&ctrl->fault, 1);
+          // copies still in flight (3-D: planes j-1 .. j+1; 2-D: the one
+          // plane): wait for them, again with a bound, before exiting
+          for (int p = NDIM == 3 ? max(j - 1, pbase) : 0; p <= (NDIM == 3 ? j + 1 : 0); p++) {
+            const int q = p - pbase;
+            mbar_wait(&bars[q % FWRING], (uses[q % FWRING] + q / FWRING) & 1, 1LL << 28);
+          }
+        }
         return false;
       }
       if (NDIM == 3 && tid == 0 && j + 2 <= z1 + 1) issue(j + 2);

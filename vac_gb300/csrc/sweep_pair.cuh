@@ -525,7 +525,15 @@ struct PairSweep {
       if (j == pfirst) ok = wait_plane(j - 1) && wait_plane(j);
       ok = ok && wait_plane(j + 1);
       if (__syncthreads_or(!ok)) {  // barrier A
-        if (tid == 0) atomicExch(&ctrl->fault, 1);
+        if (tid == 0) {
+          atomicExch(&ctrl->fault, 1);
+          // the copies of planes j-1 .. j+1 may still be in flight: wait for
+          // them, again with a bound, so none lands after the CTA exits
+          for (int p = max(j - 1, pbase); p <= j + 1; p++) {
+            const int q = p - pbase;
+            mbar_wait(&bars[q % FWRING], (uses[q % FWRING] + q / FWRING) & 1, 1LL << 28);
+          }
+        }
         return false;
       }
       if (tid == 0 && j + 2 <= z1 + 1) issue(j + 2);
@@ -675,14 +683,13 @@ struct PairSweep {
           f2 u[NW], hlv[NW], dbx = f2s(0.0f);
 #pragma unroll
           for (int v = 0; v < NW; v++) {
+            // the pair and its neighbours shifted by one cell each way, so
+            // the slopes and B_x(x+1)-B_x(x-1) are packed differences
             const float* r = p0 + v * BPL + o0;
-            float cl, ch;
             const f2 c = ld2(r);
-            f2u(c, cl, ch);
-            const float lft = r[-1], rgt = r[2];
-            const float d1 = ch - cl;
-            const f2 dp = f2m(d1, rgt - ch), dm = f2m(cl - lft, d1);
-            if (v == 5) dbx = f2m(r[1] - lft, rgt - cl);
+            const f2 cl = f2m(r[-1], r[0]), cr = f2m(r[1], r[2]);
+            const f2 dp = cr - c, dm = c - cl;
+            if (v == 5) dbx = cr - cl;
             u[v] = c;
             hlv[v] = p_hlim<LIMC>(dp, dm, k);
           }
