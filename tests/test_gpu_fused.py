@@ -185,3 +185,35 @@ def test_fused_with_gravity(gpu_lib, monkeypatch, name, mk, lim, bc, n, grav):
         assert (e.kernel_stats()["sweep"][0] > 0) == (fz == "1")
     assert max(rel_l1(out["1"], ref)) <= MIXED_REL_L1, rel_l1(out["1"], ref)
     assert max(rel_l1(out["1"], out["0"])) <= FUSED_VS_SPLIT, rel_l1(out["1"], out["0"])
+
+
+def _ot_shape(nx, ny):
+    """Orszag-Tang's fields on an nx x ny periodic box (uneven shapes)."""
+    x = inistate.domain_grid((nx, ny), (0.0, 0.0), (2 * np.pi, 2 * np.pi))
+    X, Y = x
+    g = 5.0 / 3.0
+    rho = np.full_like(X, g * g)
+    v = [-np.sin(Y), np.sin(X)]
+    b = [-np.sin(Y), np.sin(2 * X)]
+    w = inistate.conserve_mhd(rho, v, np.full_like(X, g), b, g)
+    return inistate._snap(x, w, g, True, 2, "Orszag-Tang fields %dx%d" % (nx, ny))
+
+
+LINE2_SHAPES = [
+    ("mhd-61x33-periodic", lambda: _ot_shape(61, 33), "woodward", "periodic", 10, None),
+    ("mhd-124x9-periodic", lambda: _ot_shape(124, 9), "minmod", "periodic", 10, None),
+    ("mhd-6x70-reflect", lambda: _ot_shape(6, 70), "minmod", "symm", 8,
+     lambda p: reflecting(p, 2)),
+    ("mhd-129x65-reflect", lambda: _ot_shape(129, 65), "woodward", "symm", 6,
+     lambda p: reflecting(p, 2)),
+    ("hd-67x131-cont", lambda: _hd(67, 131), "woodward", "cont", 12, None),
+    ("hd-128x4-cont", lambda: _hd(128, 4), "minmod", "cont", 12, None),
+]
+
+
+@pytest.mark.parametrize("name,mk,lim,bc,n,tweak", LINE2_SHAPES, ids=[c[0] for c in LINE2_SHAPES])
+def test_line_sweep_shapes(gpu_lib, monkeypatch, name, mk, lim, bc, n, tweak):
+    """The 2-D line sweep on shapes that cut its 60- and 64-column strips
+    and 32-row chunks unevenly (one strip, partly filled strips, fewer rows
+    than a chunk, several chunks), against the oracle and the split kernels."""
+    test_fused_against_oracle_and_split(gpu_lib, monkeypatch, name, mk, lim, bc, n, tweak)
