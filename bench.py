@@ -203,7 +203,7 @@ def run_batched(args):
     grids = inistate.riemann_batch(n=64, seed=0)
     cells = sum(int(np.prod([g[0].nx[d] for d in range(2)])) for g in grids)
     b = Batch(grids)
-    ctas, order, rows, ms = b.tune()
+    ctas, order, rows, one, ms = b.tune()
     b.step(50)  # capture + first replay
     torch.cuda.synchronize()
     if args.profile_range:
@@ -215,11 +215,12 @@ def run_batched(args):
         torch.cuda.profiler.stop()
     b.close()
     return {"workload": "64 grids 2D HD Riemann, sides log-uniform [64,1024] (seeded), "
-                        "cont, minmod, mixed, 50 steps per grid in one graph launch",
+                        "cont, minmod, mixed, 50 steps per grid in one call (graph replay "
+                        "or one cooperative launch, as tuned)",
             "grids": 64, "cells": cells, "steps": 50, "seconds": el,
             "value": cells * 50 / el, "unit": UNIT,
             "tuned": {"persistent_ctas": ctas, "order": ["round-robin", "grid-major"][order],
-                      "rows_per_item": rows, "trial_ms": ms}}
+                      "rows_per_item": rows, "one_launch": one, "trial_ms": ms}}
 
 
 def _errors(wm, w64):
@@ -653,7 +654,7 @@ def run_reference(args, ws, rank):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": workload_config("fp64"),
+            "data": "synthetic", "config": workload_config(args.precision),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d full 256^3 steps of the FP64 oracle port "
                                        "(OpenMP, %d threads)" % (args.steps, threads)},

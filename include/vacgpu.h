@@ -416,8 +416,10 @@ int vacgpu_batch_download(vacgpu_batch* b, int i, double* w);
 /* Advance every grid by up to nsteps steps (vacgpu_step semantics per
  * grid).  The steps are captured once into a CUDA graph of batched launches
  * (persistent sweep kernels over the work list of all grids' tiles) and
- * replayed on later calls with the same nsteps.  The first call tunes the
- * launch shape (VACGPU_TUNE=0 skips tuning). */
+ * replayed on later calls with the same nsteps, or, for 2-D line-sweep
+ * batches where the tuner finds it faster, run as one cooperative launch
+ * with grid-wide barriers between the phases of each step.  The first call
+ * tunes the launch shape (VACGPU_TUNE=0 skips tuning). */
 int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop);
 /* t, it, dt and the finished flag of grid i. */
 int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
@@ -425,10 +427,13 @@ int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
 /* Run (or report) the launch-shape autotuner: persistent CTAs, work-list
  * order (0 round-robin over grids, 1 grid-major), rows per work item of the
  * 2-D line sweep (16, 32 or 64; 0 for 3-D batches, which have one item
- * shape) and the trial times in ms, 18 doubles: per item shape, per CTA
- * count (two persistent counts, then one CTA per item), per order (0 where
- * not tried). */
-int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, double* ms);
+ * shape), whether the steps run as one cooperative launch (2-D line-sweep
+ * batches only; ctas is then that launch's CTA count) and the trial times
+ * in ms of two steps, 24 doubles: per item shape, per CTA count (two
+ * persistent counts, then one CTA per item), per order; then the one-launch
+ * form per item shape and order (0 where not tried). */
+int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, int* onelaunch,
+                      double* ms);
 void vacgpu_batch_destroy(vacgpu_batch* b);
 
 /* ------------------------------------------------------------- server --

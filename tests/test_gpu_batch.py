@@ -34,8 +34,8 @@ def test_batch_mhd3d_and_tuner(gpu_lib):
     grids = [(inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED), s.x, s.w)
              for s in snaps]
     b = Batch(grids)
-    ctas, order, rows, ms = b.tune()
-    assert ctas > 0 and order in (0, 1) and rows == 0 and len(ms) == 6 and all(m > 0 for m in ms)
+    ctas, order, rows, one, ms = b.tune()
+    assert ctas > 0 and order in (0, 1) and rows == 0 and not one and len(ms) == 6
     b.step(5)
     for i, (p, x, w) in enumerate(grids):
         e = Engine(p, x, w)
@@ -64,10 +64,56 @@ def test_batch_mhd2d_general_and_tuned_rows(gpu_lib):
             reflecting(p, 2)
         grids.append((p, s.x, s.w))
     b = Batch(grids)
-    ctas, order, rows, ms = b.tune()
-    assert rows in (16, 32, 64) and len(ms) == 18 and all(m > 0 for m in ms)
+    ctas, order, rows, one, ms = b.tune()
+    assert rows in (16, 32, 64) and len(ms) == 24
     b.step(6)
     for i, (p, x, w) in enumerate(grids):
         e = Engine(p, x, w)
         e.step(6)
         assert np.array_equal(bits(b.state(i)), bits(e.state())), i
+
+
+@pytest.mark.parametrize("form", ["graph", "one_launch"])
+@pytest.mark.parametrize("case", ["hd_outflow", "mhd_periodic"])
+def test_batch_line_sweep_forms(gpu_lib, monkeypatch, form, case):
+    """Both forms of a 2-D line-sweep batch, forced through VACGPU_ONELAUNCH:
+    the graph of launches per step, and all steps of a call in one
+    cooperative launch with grid-wide barriers between the phases.  Each
+    gives the bits, t and it of the grids advanced alone, over two calls,
+    and with a tstop that the grids reach at different steps (grids that
+    are done sit out the remaining steps of the launch)."""
+    monkeypatch.setenv("VACGPU_ONELAUNCH", "1" if form == "one_launch" else "0")
+    if case == "hd_outflow":
+        grids = inistate.riemann_batch(n=5, seed=7, lo=24, hi=140)
+    else:
+        grids = []
+        for n in (36, 64, 100):
+            s = inistate.orszag_tang(n)
+            grids.append((inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED),
+                          s.x, s.w))
+    b = Batch(grids)
+    ctas, order, rows, one, ms = b.tune()
+    assert one == (form == "one_launch") and ctas > 0
+    b.step(3)
+    b.step(4)
+    for i, (p, x, w) in enumerate(grids):
+        e = Engine(p, x, w)
+        e.step(7)
+        t, it, dt, fin = b.status(i)
+        assert (it, t) == (e.it, e.t), (i, it, e.it, t, e.t)
+        assert np.array_equal(bits(b.state(i)), bits(e.state())), i
+    # a stop time that the first grid reaches after 5 steps
+    e0 = Engine(*grids[0])
+    e0.step(5)
+    tstop = e0.t
+    b2 = Batch(grids)
+    b2.step(9, tstop)
+    its = set()
+    for i, (p, x, w) in enumerate(grids):
+        e = Engine(p, x, w)
+        e.step(9, tstop)
+        t, it, dt, fin = b2.status(i)
+        its.add(it)
+        assert (it, t) == (e.it, e.t), (i, it, e.it, t, e.t)
+        assert np.array_equal(bits(b2.state(i)), bits(e.state())), i
+    assert len(its) > 1  # the grids stopped at different steps

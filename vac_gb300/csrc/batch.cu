@@ -126,7 +126,13 @@ struct vacgpu_batch {
   bool line2;    // 2-D grids on the warp-marching sweep
   bool pairgen;  // ... either in its general form
   bool tuned;
-  double tune_ms[18];
+  // 2-D line sweeps: all steps of a call in one cooperative launch
+  // (kb_steps_line2) instead of the graph of launches; chosen by the tuner
+  bool onelaunch;
+  int steps_ctas;
+  int nparts;  // blocks per grid of the first-step passes (largest grid / 8192 cells)
+  GridSync* d_gs;
+  double tune_ms[24];
   int it0;
   struct G {
     int nsteps, par;
@@ -214,7 +220,7 @@ void issue_step(vacgpu_batch* b, int parity, int ctas, int order, int shape) {
   const int n = b->n;
   const bool mhd = p.physics == VACGPU_PHYS_MHD;
   launchb_control(0, b->d_ctrls, n, p, 0, 0, 0.0, b->st);
-  dim3 pg(8, n);
+  dim3 pg(b->nparts, n);
 #define PASS(K)                                                             \
   if (p.ndim == 2) {                                                        \
     if (mhd) K<2, true><<<pg, 128, 0, b->st>>>(b->d_insts);                 \
@@ -234,6 +240,38 @@ void issue_step(vacgpu_batch* b, int parity, int ctas, int order, int shape) {
     launch_sweep_any(b, D, s, ctas, order, shape);  // also fills the ghost cells
   }
   launchb_control(3, b->d_ctrls, n, p, nsw & 1, 0, 0.0, b->st);
+}
+
+// nsteps steps of every grid of a 2-D line-sweep batch in one cooperative
+// launch (kb_steps_line2): the call's begin, then per step the dt choice,
+// the first-step passes where a grid needs them, the two sweeps and the
+// step's end, separated by grid-wide barriers.  The barrier's counters are
+// cleared before every launch, so a launch after a timed-out barrier starts
+// clean.
+int issue_steps_one(vacgpu_batch* b, int nsteps, double tstop, int par, int order, int shape) {
+  const vacgpu_params& p = b->p0;
+  Line2Steps ls;
+  for (int D = 0; D < 2; D++) {
+    ls.items[D] = b->d_items[D][order][shape];
+    ls.nitems[D] = b->nitems[D][shape];
+  }
+  ls.insts = b->d_insts;
+  ls.ctrls = b->d_ctrls;
+  ls.n = b->n;
+  ls.nsteps = nsteps;
+  ls.tstop = tstop;
+  ls.par0 = par;
+  ls.xy = p.typedimsplit == VACGPU_SPLIT_XY;
+  ls.dte = dt_end_args(p);
+  ls.smallpcoeff = p.smallpcoeff;
+  ls.nparts = b->nparts;
+  ls.gs = b->d_gs;
+  BCK(cudaMemsetAsync(b->d_gs, 0, sizeof(GridSync), b->st));
+  if (!launch_line2_steps(ls, p.physics == VACGPU_PHYS_MHD, p.typelimiter[0], b->pairgen,
+                          b->steps_ctas, b->st))
+    return bfail(std::string("cooperative launch of the batched steps failed: ") +
+                 cudaGetErrorString(cudaGetLastError()));
+  return 0;
 }
 
 int prepare(vacgpu_batch* b) {
@@ -287,9 +325,17 @@ int prepare(vacgpu_batch* b) {
   }
   b->nshape = b->line2 ? 3 : 1;
   b->shape = 0;
+  long long maxcell = 0;
+  for (int i = 0; i < n; i++) maxcell = std::max(maxcell, (long long)ins[i].sa.g.ncell);
+  b->nparts = (int)std::min(256LL, std::max(8LL, (maxcell + 8191) / 8192));
   BCK(cudaMalloc(&b->d_insts, sizeof(BInst) * n));
   BCK(cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 4 * n));
   BCK(cudaMalloc(&b->d_ctrls, sizeof(Ctrl*) * n));
+  if (b->line2) {
+    BCK(cudaMalloc(&b->d_gs, sizeof(GridSync)));
+    BCK(cudaMemset(b->d_gs, 0, sizeof(GridSync)));
+    b->steps_ctas = line2_steps_ctas(mhd, b->p0.typelimiter[0], b->pairgen);
+  }
   BCK(cudaMemcpy(b->d_insts, ins.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 4 * n, cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_ctrls, ctrls.data(), sizeof(Ctrl*) * n, cudaMemcpyHostToDevice));
@@ -346,13 +392,15 @@ int prepare(vacgpu_batch* b) {
   return 0;
 }
 
-// Autotuner: time one step of every candidate launch shape on the batch
-// itself (state and control blocks restored after each trial) and keep the
-// fastest.  Candidates: persistent CTAs (per SM: 1 and 2 for the one-cell
+// Autotuner: time two steps of every candidate launch shape on the batch
+// itself, after one untimed step (state and control blocks restored after
+// each trial), and keep the fastest.  Candidates: persistent CTAs (per SM: 1 and 2 for the one-cell
 // sweep, whose 103 KB CTAs fit twice; 2 and 3 for the pair sweep; 4 and 8
 // CTAs of four warps for the 2-D line sweep) or one CTA (line sweep: one
 // warp) per work item, times two work-list orders, times the item shapes
-// (2-D line sweep: 16, 32 or 64 rows per item).
+// (2-D line sweep: 16, 32 or 64 rows per item); for 2-D line-sweep batches
+// also the one-launch form of every item shape and order
+// (VACGPU_ONELAUNCH=0 leaves it out, =1 takes it).
 int autotune(vacgpu_batch* b) {
   if (b->tuned) return 0;
   const int n = b->n;
@@ -396,21 +444,37 @@ int autotune(vacgpu_batch* b) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  // one trial: from the saved state, one untimed step (it runs the
+  // first-step passes where a grid needs them, as only a run's first step
+  // does), then two timed steps; then the state and control blocks restored
+  const int par = b->it0 & 1;
+  auto trial = [&](int mode, int ctas, int o, int sh, float* ms) -> int {
+    if (mode == 0) {
+      launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
+      issue_step(b, par, ctas, o, sh);
+      cudaEventRecord(e0, b->st);
+      issue_step(b, par ^ 1, ctas, o, sh);
+      issue_step(b, par, ctas, o, sh);
+      cudaEventRecord(e1, b->st);
+    } else {
+      if (issue_steps_one(b, 1, 1e300, par, o, sh)) return 1;
+      cudaEventRecord(e0, b->st);
+      if (issue_steps_one(b, 2, 1e300, par ^ 1, o, sh)) return 1;
+      cudaEventRecord(e1, b->st);
+    }
+    if (copy(false)) return 1;
+    BCK(cudaEventSynchronize(e1));
+    BCK(cudaEventElapsedTime(ms, e0, e1));
+    return 0;
+  };
   float best = 1e30f;
-  int bc = cand_ctas[1], bo = 0, bs = 0, k = 0;
+  int bc = cand_ctas[1], bo = 0, bs = 0, bm = 0, k = 0;
+  for (int k = 0; k < 24; k++) b->tune_ms[k] = 0.0;
   for (int sh = 0; sh < b->nshape; sh++)
     for (int c = 0; c < 3; c++)
       for (int o = 0; o < 2; o++, k++) {
-        launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
-        issue_step(b, b->it0 & 1, cand_ctas[c], o, sh);  // warm
-        if (copy(false)) return 1;
-        launchb_control(4, b->d_ctrls, n, b->p0, 0, 1 << 30, 1e300, b->st);
-        cudaEventRecord(e0, b->st);
-        issue_step(b, b->it0 & 1, cand_ctas[c], o, sh);
-        cudaEventRecord(e1, b->st);
-        cudaEventSynchronize(e1);
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
+        if (trial(0, cand_ctas[c], o, sh, &ms)) return 1;
         b->tune_ms[k] = ms;
         if (ms < best) {
           best = ms;
@@ -418,16 +482,30 @@ int autotune(vacgpu_batch* b) {
           bo = o;
           bs = sh;
         }
-        if (copy(false)) return 1;
+      }
+  const char* ol = getenv("VACGPU_ONELAUNCH");
+  if (b->line2 && !(ol && atoi(ol) == 0))
+    for (int sh = 0; sh < b->nshape; sh++)
+      for (int o = 0; o < 2; o++) {
+        float ms = 0.f;
+        if (trial(1, 0, o, sh, &ms)) return 1;
+        b->tune_ms[18 + 2 * sh + o] = ms;
+        if (ms < best || (ol && atoi(ol) == 1 && !bm)) {
+          best = ms;
+          bo = o;
+          bs = sh;
+          bm = 1;
+        }
       }
   BCK(cudaStreamSynchronize(b->st));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(snap);
   BCK(cudaGetLastError());
-  b->ctas = bc;
+  b->ctas = bm ? b->steps_ctas : bc;
   b->order = bo;
   b->shape = bs;
+  b->onelaunch = bm;
   b->tuned = true;
   return 0;
 }
@@ -509,7 +587,9 @@ int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop) {
   cudaGraphExec_t ex = nullptr;
   for (auto& g : b->graphs)
     if (g.nsteps == nsteps && g.par == par) ex = g.ex;
-  if (!ex) {
+  if (b->onelaunch) {
+    if (issue_steps_one(b, nsteps, tstop, par, b->order, b->shape)) return 1;
+  } else if (!ex) {
     cudaGraph_t gr;
     BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     launchb_control(4, b->d_ctrls, b->n, b->p0, 0, nsteps, tstop, b->st);
@@ -520,8 +600,13 @@ int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop) {
     cudaGraphDestroy(gr);
     b->graphs.push_back({nsteps, par, ex});
   }
-  BCK(cudaGraphLaunch(ex, b->st));
+  if (!b->onelaunch) BCK(cudaGraphLaunch(ex, b->st));
   BCK(cudaStreamSynchronize(b->st));
+  if (b->onelaunch) {
+    GridSync gs;
+    BCK(cudaMemcpy(&gs, b->d_gs, sizeof(gs), cudaMemcpyDeviceToHost));
+    if (gs.fault) return bfail("a grid-wide barrier of the batched steps timed out");
+  }
   // every grid advanced the same number of steps unless it finished early
   int steps0 = -1;
   for (int i = 0; i < b->n; i++) {
@@ -551,15 +636,17 @@ int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
   return 0;
 }
 
-int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, double* ms) {
+int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, int* onelaunch,
+                      double* ms) {
   if (!b) return bfail("null batch");
   if (prepare(b) || autotune(b)) return 1;
   const int ni = b->nitems[0][b->shape];
   if (ctas) *ctas = b->ctas > 0 ? b->ctas : (b->line2 ? (ni + 3) / 4 : ni);
   if (order) *order = b->order;
   if (rows) *rows = b->line2 ? LINE2_SHAPES[b->shape] : 0;
+  if (onelaunch) *onelaunch = b->onelaunch;
   if (ms)
-    for (int k = 0; k < 18; k++) ms[k] = k < 6 * b->nshape ? b->tune_ms[k] : 0.0;
+    for (int k = 0; k < 24; k++) ms[k] = b->tune_ms[k];
   return 0;
 }
 
@@ -571,6 +658,7 @@ void vacgpu_batch_destroy(vacgpu_batch* b) {
   cudaFree(b->d_insts);
   cudaFree(b->d_maps);
   cudaFree(b->d_ctrls);
+  cudaFree(b->d_gs);
   for (int D = 0; D < 3; D++)
     for (int o = 0; o < 2; o++)
       for (int sh = 0; sh < 3; sh++) cudaFree(b->d_items[D][o][sh]);

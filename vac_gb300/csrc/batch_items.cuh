@@ -2,6 +2,7 @@
 // sweep kernel reads per work item (batch.cu builds the lists; the fused
 // and pair sweep units hold the kernels that walk them).
 #pragma once
+#include "control.cuh"
 #include "sweep_fused.cuh"
 
 namespace vacgpu {
@@ -42,6 +43,42 @@ __host__ __device__ inline int line2_strips(int D, bool mhd, int nx) {
   const int tw = (D == 0 || mhd) ? 60 : 64;
   return (nx + tw - 1) / tw;
 }
+
+// State of the grid-wide barrier of a cooperative launch, in device
+// memory: arrivals, generation (advanced by the last arrival), a fault flag
+// (a barrier wait gave up) and, per step parity, whether some grid needs
+// the first-step passes.
+struct GridSync {
+  unsigned count, gen;
+  int fault;
+  int need[2];
+};
+
+// Every step of a 2-D line-sweep batch in one cooperative launch
+// (sweep_line2.cu): per step the control of each grid (dt choice), the
+// first-step passes where a grid needs them, both sweeps over their work
+// lists and the step epilogue, separated by grid-wide barriers.
+struct Line2Steps {
+  const BItem* items[2];  // work lists of the x and y sweeps
+  int nitems[2];
+  const BInst* insts;
+  Ctrl* const* ctrls;
+  int n;                  // grids
+  int nsteps;             // steps at most (each grid stops as VAC would)
+  double tstop;
+  int par0;               // parity of it at the first step
+  int xy;                 // typedimsplit 'xy' (else 'xyyx')
+  DtEndArgs dte;
+  double smallpcoeff;
+  int nparts;             // blocks per grid of the first-step passes
+  GridSync* gs;
+};
+
+// Resident CTAs of the cooperative kernel for (mhd, lim, gen) on this
+// device, and its launch (false: no instance, or the launch was refused).
+int line2_steps_ctas(bool mhd, int lim, bool gen);
+bool launch_line2_steps(const Line2Steps& ls, bool mhd, int lim, bool gen, int ctas,
+                        cudaStream_t st);
 
 // The same for 2-D grids and the warp-marching sweep (sweep_line2.cu),
 // whose work items are (grid, strip bx, output rows by .. bz-1 as

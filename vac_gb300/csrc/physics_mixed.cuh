@@ -128,8 +128,8 @@ struct PHMixed {
       case LIM_VANLEER:
         return 2.0f * fmaxf(b * a, 0.0f) / (a + b + 1.0e-12f);
       case LIM_ALBADA:
-        return (b * (a * a + 1.0e-12f) + a * (b * b + 1.0e-12f)) /
-               (a * a + b * b + 2.0e-12f);
+        return fmaf(b, fmaf(a, a, 1.0e-12f), a * fmaf(b, b, 1.0e-12f)) /
+               (fmaf(a, a, b * b) + 2.0e-12f);
       default:
         return s * fmaxf(0.0f, fminf(fabsf(a), s * b));
     }
@@ -170,13 +170,13 @@ struct PHMixed {
       float bm = u[E + 1] * u[1];
 #pragma unroll
       for (int c = 2; c <= NDIR; c++) bm = fmaf(u[E + c], u[c], bm);
-      f[E] = (u[1 + d] * pt - bi * bm) * rinv + v * u[E];
+      f[E] = fmaf(fmaf(u[1 + d], pt, -(bi * bm)), rinv, v * u[E]);
 #pragma unroll
       for (int c = 1; c <= NDIR; c++) {
         if (c == d + 1)
           f[E + c] = 0.0f;
         else
-          f[E + c] = v * u[E + c] - u[c] * rinv * bi;
+          f[E + c] = fmaf(v, u[E + c], -(u[c] * rinv * bi));
       }
     } else {
       p = p >= smallp ? p : smallp;
@@ -193,6 +193,10 @@ struct PHMixed {
   // getcmax (src/vacphys0.t.mhd:79-116, src/vacphys0.t.hd:72-100).  The
   // discriminant cf2^2-4cs2 b_i^2/rho can round below zero in FP32; it is
   // clamped at zero here (the FP64 path keeps the reference's expression).
+  // Sums of two products are written as explicit FMAs (here and in the
+  // fluxes): left to the compiler, which product it fuses can differ from
+  // one kernel to another, and the batched and single-grid kernels must
+  // round alike.
   template <int NDIR, bool MHD>
   static __device__ __forceinline__ float cmax(const float* u, int d,
                                                const DevPhys& k,
@@ -205,9 +209,9 @@ struct PHMixed {
     p = p >= smallp ? p : smallp;
     const float cs2 = k.gammaf * p * rinv;
     if (MHD) {
-      const float cf2 = 2.0f * hbb * rinv + cs2;
+      const float cf2 = fmaf(2.0f * hbb, rinv, cs2);
       const float bi = u[E + 1 + d];
-      float disc = cf2 * cf2 - 4.0f * cs2 * (bi * bi) * rinv;
+      float disc = fmaf(cf2, cf2, -(4.0f * cs2 * (bi * bi) * rinv));
       disc = disc > 0.0f ? disc : 0.0f;
       return sqrtf(0.5f * (cf2 + sqrtf(disc))) + fabsf(u[1 + d] * rinv);
     }
@@ -251,9 +255,9 @@ struct PHMixed {
     p = p >= smallp ? p : smallp;
     const float cs2 = k.gammaf * p * rinv;
     if (MHD) {
-      const float cf2 = bb * rinv + cs2;
+      const float cf2 = fmaf(bb, rinv, cs2);
       const float bi = M[E + 1 + d];
-      float disc = cf2 * cf2 - 4.0f * cs2 * (bi * bi) * rinv;
+      float disc = fmaf(cf2, cf2, -(4.0f * cs2 * (bi * bi) * rinv));
       disc = disc > 0.0f ? disc : 0.0f;
       return sqrtf(0.5f * (cf2 + sqrtf(disc))) + fabsf(M[1 + d] * rinv);
     }

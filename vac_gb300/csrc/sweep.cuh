@@ -604,27 +604,35 @@ struct Sweep {
   // getpthermal's one-time smallp: min/max of the unclipped pressure on the
   // mesh (src/vacphys0.t.mhd:202-217).
   template <int NT>
-  static __device__ void pminmax(const SweepArgs& a, const T* __restrict__ w) {
+  // bid, nblk: this block's part of the grid's cells (default: the launch's
+  // blocks); the control fields are read through L2, as a persistent
+  // kernel needs when another SM set them earlier in the same launch
+  static __device__ void pminmax(const SweepArgs& a, const T* __restrict__ w, int bid = -1,
+                                 int nblk = 0) {
     __shared__ unsigned long long shk[NT / 32];
     Ctrl* ctrl = a.ctrl;
-    if (ctrl->done || !ctrl->need_smallp) return;
+    if (__ldcg(&ctrl->done) || !__ldcg(&ctrl->need_smallp)) return;
+    if (bid < 0) {
+      bid = blockIdx.x;
+      nblk = gridDim.x;
+    }
     unsigned long long kmin = ~0ULL, kmax = 0ULL;
-    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-         n < a.g.ncell; n += (long long)gridDim.x * blockDim.x) {
+    for (long long n = (long long)bid * blockDim.x + threadIdx.x;
+         n < a.g.ncell; n += (long long)nblk * blockDim.x) {
       int c[3];
       cell_coords(a.g, n, c);
       const long long off = gidx(a.g, c[0], c[1], c[2]);
       R u[NW];
 #pragma unroll
-      for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+      for (int iw = 0; iw < NW; iw++) u[iw] = R(__ldcg(w + off + iw * a.g.vs));
       const unsigned long long k = dkey(PH::template pthermal_raw<NDIR, MHD>(u, a.ph));
       kmin = k < kmin ? k : kmin;
       kmax = k > kmax ? k : kmax;
     }
     unsigned long long k = block_max_key<NT>(kmax, shk);
-    if (threadIdx.x == 0) atomic_max_key(&ctrl->pmax[blockIdx.x % NSLOT], k);
+    if (threadIdx.x == 0) atomic_max_key(&ctrl->pmax[bid % NSLOT], k);
     k = ~block_max_key<NT>(~kmin, shk);
-    if (threadIdx.x == 0) atomic_min_key(&ctrl->pmin[blockIdx.x % NSLOT], k);
+    if (threadIdx.x == 0) atomic_min_key(&ctrl->pmin[bid % NSLOT], k);
   }
 
   // keeppositive (smallfix), src/vacphys.t.mhd:9-53, src/vacphys.t.hd:
@@ -728,34 +736,40 @@ struct Sweep {
   // Cell-centred max(cmax/dx) of getdt_courant for the dimensions whose
   // dtcourant is unset (src/vac.t:690-711).
   template <int NT>
-  static __device__ void cell_cmax(const SweepArgs& a, const T* __restrict__ w) {
+  static __device__ void cell_cmax(const SweepArgs& a, const T* __restrict__ w, int bid = -1,
+                                   int nblk = 0) {
     __shared__ unsigned long long shk[NT / 32];
     Ctrl* ctrl = a.ctrl;
-    if (ctrl->done) return;
-    if (!(ctrl->need_cell[0] | ctrl->need_cell[1] | ctrl->need_cell[2]))
-      return;
-    const R smallp = R(ctrl->smallp);
+    if (__ldcg(&ctrl->done)) return;
+    int need[3];
+    for (int d = 0; d < 3; d++) need[d] = __ldcg(&ctrl->need_cell[d]);
+    if (!(need[0] | need[1] | need[2])) return;
+    if (bid < 0) {
+      bid = blockIdx.x;
+      nblk = gridDim.x;
+    }
+    const R smallp = R(__ldcg(&ctrl->smallp));
     unsigned long long key[3] = {0ULL, 0ULL, 0ULL};
-    for (long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-         n < a.g.ncell; n += (long long)gridDim.x * blockDim.x) {
+    for (long long n = (long long)bid * blockDim.x + threadIdx.x;
+         n < a.g.ncell; n += (long long)nblk * blockDim.x) {
       int c[3];
       cell_coords(a.g, n, c);
       const long long off = gidx(a.g, c[0], c[1], c[2]);
       R u[NW];
 #pragma unroll
-      for (int iw = 0; iw < NW; iw++) u[iw] = R(w[off + iw * a.g.vs]);
+      for (int iw = 0; iw < NW; iw++) u[iw] = R(__ldcg(w + off + iw * a.g.vs));
       for (int d = 0; d < NDIM; d++) {
-        if (!ctrl->need_cell[d]) continue;
+        if (!need[d]) continue;
         R cm = PH::template cmax<NDIR, MHD>(u, d, a.ph, smallp);
         unsigned long long k = dkey(PH::cell_ratio(cm, a.a, d, c[d]));
         key[d] = k > key[d] ? k : key[d];
       }
     }
     for (int d = 0; d < NDIM; d++) {
-      if (!ctrl->need_cell[d]) continue;
+      if (!need[d]) continue;
       unsigned long long k = block_max_key<NT>(key[d], shk);
       if (threadIdx.x == 0)
-        atomic_max_key(&ctrl->cell_cmax[d][blockIdx.x % NSLOT], k);
+        atomic_max_key(&ctrl->cell_cmax[d][bid % NSLOT], k);
     }
   }
 };

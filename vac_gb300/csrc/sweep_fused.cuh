@@ -229,10 +229,10 @@ struct Fused {
     const int bx = (E + 1) * C::BPL, by = (E + 1 + AR) * C::BPL;
     float divb = 0.5f * (p0[bx + o + 1] - p0[bx + o - 1]) * a.idxf[0][gc[0]];
     if (NDIM > 1)
-      divb += 0.5f * (p0[by + o + FB_X] - p0[by + o - FB_X]) * a.idxf[AR][gc[AR]];
+      divb = fmaf(0.5f * (p0[by + o + FB_X] - p0[by + o - FB_X]), a.idxf[AR][gc[AR]], divb);
     if (NDIM > 2) {
       const int bz = (E + 1 + AM) * C::BPL;
-      divb += 0.5f * (pp[bz + o] - pm[bz + o]) * a.idxf[AM][gc[AM]];
+      divb = fmaf(0.5f * (pp[bz + o] - pm[bz + o]), a.idxf[AM][gc[AM]], divb);
     }
     return divb;
   }
@@ -336,8 +336,8 @@ struct Fused {
       uL[i] = c + 0.5f * l;
     }
     const float riR = 1.0f / uR[0], riL = 1.0f / uL[0];
-    const float fR = uR[1] * riR * uR[4] - uR[2] * riR * uR[3];
-    const float fL = uL[1] * riL * uL[4] - uL[2] * riL * uL[3];
+    const float fR = fmaf(uR[1] * riR, uR[4], -(uR[2] * riR * uR[3]));
+    const float fL = fmaf(uL[1] * riL, uL[4], -(uL[2] * riL * uL[3]));
     float out = u[4] - qdt * a.idxf[D][gc[D]] * (fL - fR);
     if (a.ph.sourceunsplit && a.ph.divbfix)
       out = out - u[2] / u[0] * (qs * divb_w(a, pm, p0, pp, sy, sx, gc));
@@ -377,7 +377,7 @@ struct Fused {
     }
 #pragma unroll
     for (int v = 0; v < NW; v++)
-      F[v] = 0.5f * (fL[v] + fR[v]) - cmax * 0.5f * (R[v] - L[v]);
+      F[v] = fmaf(-cmax * 0.5f, R[v] - L[v], 0.5f * (fL[v] + fR[v]));
     return cmax;
   }
 
@@ -518,10 +518,10 @@ struct Fused {
         const int bxo = (E + 1) * C::RN + r, byo = (E + 1 + AR) * C::RN + r;
         float divb = 0.5f * (c0[bxo + 1] - c0[bxo - 1]) * a.idxf[0][gc[0]];
         if (NDIM > 1)
-          divb += 0.5f * (c0[byo + C::RX] - c0[byo - C::RX]) * a.idxf[AR][gc[AR]];
+          divb = fmaf(0.5f * (c0[byo + C::RX] - c0[byo - C::RX]), a.idxf[AR][gc[AR]], divb);
         if (NDIM > 2) {
           const float bzp = w1slot(sm, jo + 1)[(E + 1 + AM) * C::RN + r];
-          divb += 0.5f * (bzp - bzm) * a.idxf[AM][gc[AM]];
+          divb = fmaf(0.5f * (bzp - bzm), a.idxf[AM][gc[AM]], divb);
         }
         qdivb = qs * divb;
       }

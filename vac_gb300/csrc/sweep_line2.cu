@@ -3,6 +3,8 @@
 #include <cstdlib>
 
 #include "batch_items.cuh"
+#include "physics_mixed.cuh"
+#include "sweep.cuh"
 #include "sweep_line2.cuh"
 
 namespace vacgpu {
@@ -48,8 +50,9 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : (D == 1 && GEN ? 3 : 4))
 }
 
 // The warp-marching sweep applies to a 2-D grid with one limiter for every
-// variable (minmod or woodward), even row offsets and fewer than 2^31
-// elements in the state; also false when
+// variable (minmod or woodward), rows that start 2 elements before a
+// 16-byte boundary and fewer than 2^31 elements in the state; also false
+// when
 // VACGPU_PAIR=0 (the one-cell kernels for every grid).
 bool line2_applies(const FusedArgs& a, bool mhd) {
   if (!pair_enabled()) return false;
@@ -58,8 +61,9 @@ bool line2_applies(const FusedArgs& a, bool mhd) {
   bool uniform = a.ph.typefull != VACGPU_TVDLF1;
   for (int v = 1; v < nw; v++) uniform = uniform && a.ph.lim[v] == l0;
   if (!uniform || (l0 != VACGPU_LIM_WOODWARD && l0 != VACGPU_LIM_MINMOD)) return false;
-  // the kernel indexes variables with 32-bit element offsets
-  return a.g.ndim == 2 && !(a.g.xpad & 1) && !(a.g.P & 1) &&
+  // the kernel indexes variables with 32-bit element offsets and stages
+  // rows in 16-byte chunks from 4-column boundaries (mesh column 0 on one)
+  return a.g.ndim == 2 && (a.g.xpad + 2) % 4 == 0 && a.g.P % 4 == 0 &&
          a.g.vs * nw < (1LL << 31);
 }
 
@@ -139,5 +143,173 @@ bool launch_batch_line2(const BItem* items, int nitems, const BInst* insts, int 
 #undef KL
   return false;
 }
+
+}  // namespace vacgpu
+
+// ------------------------------------------------- one launch, many steps
+
+namespace vacgpu {
+
+// Grid-wide barrier of a cooperative launch (every CTA resident): the last
+// CTA to arrive resets the count and advances the generation; the others
+// wait for the generation to move, at most about 2^31 cycles, after which
+// the barrier reports failure and sets the fault flag.  Writes before the
+// barrier are visible after it (CTA barrier, then a device-scope fence by
+// the arriving thread, and a fence after the wait).
+__device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned* vgen = &gs->gen;
+    const unsigned g = *vgen;
+    __threadfence();
+    if (atomicAdd(&gs->count, 1u) == nb - 1) {
+      atomicExch(&gs->count, 0u);
+      __threadfence();
+      atomicAdd(&gs->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*vgen == g) {
+        if (clock64() - t0 > (1LL << 31)) {
+          atomicExch(&gs->fault, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)&gs->fault) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Every step of a batch of 2-D grids (the body of VAC's time loop for each
+// grid, as issue_step issues it with separate launches): CTA b runs the
+// control of grids b, b + gridDim.x, ...; the sweeps' warps take the work
+// items in turn.  Control fields written on one SM are read on others
+// through L2 (the control functions, Line2::run and the first-step passes
+// use ld.global.cg), and the rows of the state arrive by cp.async.cg, so no
+// stale L1 line from an earlier step is read.
+template <bool MHD, int LIMC, bool GEN>
+__global__ void __launch_bounds__(L2_NT, MHD ? 2 : 3) kb_steps_line2(const Line2Steps ls) {
+  constexpr int RF = line2_ring_floats(MHD ? 6 : 4);
+  __shared__ __align__(16) float ring[L2_NT / 32][RF];
+  typedef Sweep<PHMixed<PREC_FF>, 2, 2, MHD> SW;
+  const unsigned nb = gridDim.x;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int nwarps = nb * (L2_NT / 32), gw = blockIdx.x * (L2_NT / 32) + warp;
+  GridSync* gs = ls.gs;
+  if (tid == 0) {
+    for (int g = blockIdx.x; g < ls.n; g += nb) {  // call_begin
+      Ctrl* c = ls.ctrls[g];
+      c->done = 0;
+      c->steps = 0;
+      c->maxsteps = ls.nsteps;
+      c->tstop = ls.tstop;
+    }
+    if (blockIdx.x == 0) gs->need[0] = gs->need[1] = 0;
+  }
+  if (!grid_sync(gs, nb)) return;
+  for (int s = 0; s < ls.nsteps; s++) {
+    const int par = (ls.par0 + s) & 1;
+    if (blockIdx.x == 0 && tid == 0) gs->need[(s + 1) & 1] = 0;
+    for (int g = blockIdx.x; g < ls.n; g += nb) {
+      Ctrl* c = ls.ctrls[g];
+      dt_begin_dev(c, 2);
+      if (tid == 0 && !c->done && (c->need_smallp | c->need_cell[0] | c->need_cell[1]))
+        atomicOr(&gs->need[s & 1], 1);
+    }
+    if (!grid_sync(gs, nb)) return;
+    if (__ldcg(&gs->need[s & 1])) {
+      // the first-step passes: nparts parts of each grid's cells
+      const int np = ls.nparts;
+      for (int u = blockIdx.x; u < np * ls.n; u += nb) {
+        const BInst* in = ls.insts + u / np;
+        SW::template pminmax<L2_NT>(in->sa, in->buf[__ldcg(&in->sa.ctrl->cur)], u % np, np);
+      }
+      if (!grid_sync(gs, nb)) return;
+      for (int g = blockIdx.x; g < ls.n; g += nb) smallp_dev(ls.ctrls[g], MHD, ls.smallpcoeff);
+      if (!grid_sync(gs, nb)) return;
+      for (int u = blockIdx.x; u < np * ls.n; u += nb) {
+        const BInst* in = ls.insts + u / np;
+        SW::template cell_cmax<L2_NT>(in->sa, in->buf[__ldcg(&in->sa.ctrl->cur)], u % np, np);
+      }
+      if (!grid_sync(gs, nb)) return;
+    }
+    for (int g = blockIdx.x; g < ls.n; g += nb) dt_end_dev(ls.ctrls[g], ls.dte);
+    if (!grid_sync(gs, nb)) return;
+    for (int sw = 0; sw < 2; sw++) {
+      const int D = (!par || ls.xy) ? sw : 1 - sw;
+      const BItem* items = ls.items[D];
+      for (int it = gw; it < ls.nitems[D]; it += nwarps) {
+        const BItem item = items[it];
+        const BInst* in = ls.insts + item.inst;
+        const int src = __ldcg(&in->fa.ctrl->cur) ^ (sw & 1);
+        if (D == 0)
+          Line2<0, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], ring[warp],
+                                        item.bx, item.by, item.bz, (unsigned)it);
+        else
+          Line2<1, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], ring[warp],
+                                        item.bx, item.by, item.bz, (unsigned)it);
+      }
+      if (!grid_sync(gs, nb)) return;
+    }
+    for (int g = blockIdx.x; g < ls.n; g += nb) step_end_dev(ls.ctrls[g], 2, 0);
+    if (!grid_sync(gs, nb)) return;
+  }
+}
+
+template <bool MHD, int LIMC, bool GEN>
+static int steps_ctas() {
+  static int ctas = 0;
+  if (!ctas) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kb_steps_line2<MHD, LIMC, GEN>, L2_NT,
+                                                  0);
+    ctas = sms * per;
+  }
+  return ctas;
+}
+
+template <bool MHD, int LIMC, bool GEN>
+static bool launch_steps(const Line2Steps& ls, int ctas, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(L2_NT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kb_steps_line2<MHD, LIMC, GEN>, ls) == cudaSuccess;
+}
+
+#define L2S_DISPATCH(F, ...)                                                  \
+  if (mhd) {                                                                  \
+    if (lim == VACGPU_LIM_WOODWARD)                                           \
+      return gen ? F<true, LIMC_WOODWARD, true>(__VA_ARGS__)                  \
+                 : F<true, LIMC_WOODWARD, false>(__VA_ARGS__);                \
+    return gen ? F<true, LIMC_MINMOD, true>(__VA_ARGS__)                      \
+               : F<true, LIMC_MINMOD, false>(__VA_ARGS__);                    \
+  }                                                                           \
+  if (lim == VACGPU_LIM_WOODWARD)                                             \
+    return gen ? F<false, LIMC_WOODWARD, true>(__VA_ARGS__)                   \
+               : F<false, LIMC_WOODWARD, false>(__VA_ARGS__);                 \
+  return gen ? F<false, LIMC_MINMOD, true>(__VA_ARGS__)                       \
+             : F<false, LIMC_MINMOD, false>(__VA_ARGS__);
+
+int line2_steps_ctas(bool mhd, int lim, bool gen) { L2S_DISPATCH(steps_ctas) }
+
+bool launch_line2_steps(const Line2Steps& ls, bool mhd, int lim, bool gen, int ctas,
+                        cudaStream_t st) {
+  L2S_DISPATCH(launch_steps, ls, ctas, st)
+}
+#undef L2S_DISPATCH
 
 }  // namespace vacgpu

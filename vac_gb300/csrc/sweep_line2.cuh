@@ -43,8 +43,13 @@ constexpr int L2_ROWS = 32;  // rows per work item
 constexpr int L2_LOOK = 3;   // rows in flight ahead of use
 constexpr int L2_RING = L2_LOOK + 1;  // staging slots per warp
 
+// A staged row holds, per variable, 68 floats: the strip's 64 columns from
+// the 16-byte boundary at or below its first one (2 columns earlier when
+// the strip has halo columns).
+constexpr int L2_ROWF = 68;
+
 // floats of one warp's row-staging ring for nw variables
-__host__ __device__ constexpr int line2_ring_floats(int nw) { return L2_RING * nw * 64; }
+__host__ __device__ constexpr int line2_ring_floats(int nw) { return L2_RING * nw * L2_ROWF; }
 
 template <int D, bool MHD, int LIMC, bool GEN>
 struct Line2 {
@@ -69,7 +74,7 @@ struct Line2 {
     // boundary variable masks of the x and y faces, 8 bits each: periodic
     // (bits 0-7), 'asymm' at the low face (8-15) and at the high face (16-23)
     int bmx, bmy;
-    int c0, cl;         // first column of the pair; the column pair it loads
+    int c0;             // first column of the pair
     int nX, nY;         // mesh cells
     int gy_hi;          // last row of the ghost range (nY + 3)
     bool ok0, ok1;      // the pair's cells are outputs of this strip
@@ -77,31 +82,43 @@ struct Line2 {
     f2 idxx, cflx, qdt2, qs1, qs2, nqs1h, nqs2h;
     float qdt;
     bool powell, srcs, cfl, fix_x, fix_y;
+    int cs;             // first staged column (16-byte aligned element)
+    int cmax4;          // last 16-byte aligned column a row can be read from
     PairK k;
   };
 
   // Rows reach registers through a per-warp ring of L2_RING slots in
-  // shared memory, fed by cp.async 8-byte copies L2_LOOK rows ahead of use:
-  // each lane copies its own pair of every variable and later reads back
-  // exactly those bytes, so rows in flight hold no registers and need no
-  // barrier.  Rows are issued and pulled strictly in order; a pull waits
-  // until at most L2_LOOK-1 copies are outstanding (its own row has landed)
-  // and issues the next row.  The slot a copy overwrites was read one pull
-  // earlier.
+  // shared memory, fed by cp.async 16-byte copies (.cg: through L2 only, so
+  // a kernel that runs several steps never reads a stale L1 line) L2_LOOK
+  // rows ahead of use; rows in flight hold no registers.  The lanes copy the
+  // row's 16-byte chunks between them (chunk q: variable q / 17, columns
+  // 4 (q % 17) .. +3 of the staged row) and each reads back its own pair
+  // after a warp barrier.  Rows are issued and pulled strictly in order; a
+  // pull waits until at most L2_LOOK-1 copies are outstanding (its own row
+  // has landed) and issues the next row, whose slot every lane read one pull
+  // earlier (before this pull's warp barrier).
+  static constexpr int NCHUNK = NW * (L2_ROWF / 4);
   struct Pipe {
-    unsigned sm;  // shared address of this lane's pair in slot 0, variable 0
+    unsigned sm;  // shared address of this warp's ring
     int issued;   // next row to issue
+    int rd;       // byte offset of this lane's pair within a variable's row
   };
 
   static __device__ __forceinline__ void issue_row(const Ctx& c, Pipe& pp) {
     const int gy = min(pp.issued, c.gy_hi);  // rows past the ghost range are not used
-    const float* p = c.win + (long long)gy * c.P + c.cl;
-    const unsigned s = pp.sm + (unsigned)((pp.issued % L2_RING) * NW * 256);
+    const float* row = c.win + (long long)gy * c.P;
+    const unsigned s = pp.sm + (unsigned)((pp.issued % L2_RING) * NW * L2_ROWF * 4);
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int v = 0; v < NW; v++)
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s + v * 256),
-                   "l"(p + v * c.vs)
-                   : "memory");
+    for (int q0 = 0; q0 < NCHUNK; q0 += 32) {
+      const int q = q0 + lane;
+      if (q < NCHUNK) {
+        const int v = q / (L2_ROWF / 4), col = c.cs + 4 * (q % (L2_ROWF / 4));
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s + q * 16),
+                     "l"(row + v * c.vs + min(col, c.cmax4))
+                     : "memory");
+      }
+    }
     asm volatile("cp.async.commit_group;" ::: "memory");
     pp.issued++;
   }
@@ -114,11 +131,14 @@ struct Line2 {
 
   static __device__ __forceinline__ void pull(const Ctx& c, Pipe& pp, int gy, f2* u) {
     asm volatile("cp.async.wait_group %0;" ::"n"(L2_LOOK - 1) : "memory");
-    const unsigned s = pp.sm + (unsigned)((gy % L2_RING) * NW * 256);
+    __syncwarp();
+    const unsigned s = pp.sm + (unsigned)((gy % L2_RING) * NW * L2_ROWF * 4) + pp.rd;
 #pragma unroll
     for (int v = 0; v < NW; v++) {
       float lo, hi;
-      asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(lo), "=f"(hi) : "r"(s + v * 256));
+      asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                   : "=f"(lo), "=f"(hi)
+                   : "r"(s + v * L2_ROWF * 4));
       u[v] = f2m(lo, hi);
     }
     issue_row(c, pp);
@@ -488,7 +508,9 @@ struct Line2 {
   static __device__ void run(const FusedArgs& a, const float* win, float* wout, float* ring,
                              int sx, int gya, int gyb, unsigned slot) {
     Ctrl* ctrl = a.ctrl;
-    if (ctrl->done) return;
+    // control fields through L2: a persistent batch kernel sets them on
+    // another SM earlier in the same launch
+    if (__ldcg(&ctrl->done)) return;
     const DevGrid& g = a.g;
     const int lane = threadIdx.x & 31;
     Ctx c;
@@ -505,7 +527,8 @@ struct Line2 {
     c.gy_hi = g.nG[1] - 1;
     const int gxs = 2 - HALO + TW * sx;
     c.c0 = gxs + 2 * lane;
-    c.cl = min(c.c0, (g.nG[0] - 1) & ~1);
+    c.cs = HALO ? gxs - 2 : gxs;
+    c.cmax4 = (int)g.P - 4 - g.xpad;
     const int ob = gxs + HALO, oe = min(gxs + HALO + TW, c.nX + 2);
     c.ok0 = c.c0 >= ob && c.c0 < oe;
     c.ok1 = c.c0 + 1 >= ob && c.c0 + 1 < oe;
@@ -517,7 +540,7 @@ struct Line2 {
               gxc = min(c.c0 + 2, g.nG[0] - 1);
     c.idxx = f2m(a.idxf[0][gxa], a.idxf[0][gxb]);
     c.cflx = f2m(2.0f / (a.dxf[0][gxa] + a.dxf[0][gxb]), 2.0f / (a.dxf[0][gxb] + a.dxf[0][gxc]));
-    const double dtd = ctrl->dt;
+    const double dtd = __ldcg(&ctrl->dt);
     c.qdt = (float)dtd;
     c.qdt2 = f2s((float)(dtd / 2));
     c.nqs1h = f2s(-((float)(dtd / 2 / 2) * 0.5f));  // -predictor source x 1/2
@@ -531,7 +554,7 @@ struct Line2 {
     c.k.quarter = f2s(0.25f);
     c.k.eighth = f2s(0.125f);
     c.k.mone = f2s(-1.0f);
-    c.k.smallp = (float)ctrl->smallp;
+    c.k.smallp = (float)__ldcg(&ctrl->smallp);
     c.powell = MHD && (!GEN || (a.ph.divbfix && a.ph.sourceunsplit));
     c.srcs = !GEN || a.ph.sourceunsplit;
     c.cfl = !GEN || a.cfl;
@@ -540,7 +563,8 @@ struct Line2 {
     c.fix_y = GEN && (c.bmy & 255) != all;
     f2 qmax = f2s(0.0f);
     Pipe pp;
-    pp.sm = smem_u32(ring) + lane * 8;
+    pp.sm = smem_u32(ring);
+    pp.rd = (c.c0 - c.cs) * 4;
     if (D == 0)
       run_x(a, c, pp, gya, gyb, qmax);
     else

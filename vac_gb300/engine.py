@@ -79,7 +79,7 @@ def lib():
         L.vacgpu_batch_download.argtypes = [vp, C.c_int, dp]
         L.vacgpu_batch_step.argtypes = [vp, C.c_int, C.c_double]
         L.vacgpu_batch_status.argtypes = [vp, C.c_int, dp, ip, dp, ip]
-        L.vacgpu_batch_tune.argtypes = [vp, ip, ip, ip, dp]
+        L.vacgpu_batch_tune.argtypes = [vp, ip, ip, ip, ip, dp]
         L.vacgpu_batch_destroy.argtypes = [vp]
         L.vacgpu_batch_destroy.restype = None
         L.vacgpu_server_create.argtypes = [C.c_double, C.c_int, C.c_int, C.POINTER(vp)]
@@ -280,12 +280,13 @@ class Batch:
 
     def tune(self):
         """(persistent CTAs, work-list order, rows per item of the 2-D line
-        sweep or 0, trial times in ms of the candidates tried)."""
-        c, o, r = C.c_int(), C.c_int(), C.c_int()
-        ms = (C.c_double * 18)()
-        _ck(lib().vacgpu_batch_tune(self.h, C.byref(c), C.byref(o), C.byref(r), ms),
-            "vacgpu_batch_tune")
-        return c.value, o.value, r.value, [m for m in ms if m > 0]
+        sweep or 0, one cooperative launch for all steps (bool), trial times
+        in ms of the candidates tried)."""
+        c, o, r, one = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        ms = (C.c_double * 24)()
+        _ck(lib().vacgpu_batch_tune(self.h, C.byref(c), C.byref(o), C.byref(r),
+                                    C.byref(one), ms), "vacgpu_batch_tune")
+        return c.value, o.value, r.value, bool(one.value), [m for m in ms if m > 0]
 
     def status(self, i):
         t, it, dt, fin = C.c_double(), C.c_int(), C.c_double(), C.c_int()
