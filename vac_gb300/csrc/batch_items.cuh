@@ -46,12 +46,14 @@ __host__ __device__ inline int line2_strips(int D, bool mhd, int nx) {
 
 // State of the grid-wide barrier of a cooperative launch, in device
 // memory: arrivals, generation (advanced by the last arrival), a fault flag
-// (a barrier wait gave up) and, per step parity, whether some grid needs
-// the first-step passes.
+// (a barrier wait gave up), per step parity whether some grid needs the
+// first-step passes, and the next unclaimed work item of the first and the
+// second sweep of a step.
 struct GridSync {
   unsigned count, gen;
   int fault;
   int need[2];
+  int next[2];
 };
 
 // Every step of a 2-D line-sweep batch in one cooperative launch

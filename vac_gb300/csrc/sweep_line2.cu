@@ -188,40 +188,58 @@ __device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb) {
 // Every step of a batch of 2-D grids (the body of VAC's time loop for each
 // grid, as issue_step issues it with separate launches): CTA b runs the
 // control of grids b, b + gridDim.x, ...; the sweeps' warps take the work
-// items in turn.  Control fields written on one SM are read on others
-// through L2 (the control functions, Line2::run and the first-step passes
-// use ld.global.cg), and the rows of the state arrive by cp.async.cg, so no
-// stale L1 line from an earlier step is read.
+// items in turn.  A step takes three grid-wide barriers: the owner of a
+// grid chooses its dt right after the previous step's end (dt_begin, and
+// dt_end unless the grid needs the first-step passes, which then run
+// between barriers of their own), then the two sweeps.  Control fields
+// written on one SM are read on others through L2 (the control functions,
+// Line2::run and the first-step passes use ld.global.cg), and the rows of
+// the state arrive by cp.async.cg, so no stale L1 line from an earlier step
+// is read.
 template <bool MHD, int LIMC, bool GEN>
 __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 3) kb_steps_line2(const Line2Steps ls) {
   constexpr int RF = line2_ring_floats(MHD ? 6 : 4);
   __shared__ __align__(16) float ring[L2_NT / 32][RF];
+  __shared__ int defer;
   typedef Sweep<PHMixed<PREC_FF>, 2, 2, MHD> SW;
   const unsigned nb = gridDim.x;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int nwarps = nb * (L2_NT / 32), gw = blockIdx.x * (L2_NT / 32) + warp;
   GridSync* gs = ls.gs;
-  if (tid == 0) {
-    for (int g = blockIdx.x; g < ls.n; g += nb) {  // call_begin
-      Ctrl* c = ls.ctrls[g];
+  // the next work item of a sweep, for the whole warp
+  auto claim = [&](int* ctr) {
+    int t = 0;
+    if ((tid & 31) == 0) t = atomicAdd(ctr, 1);
+    return __shfl_sync(0xffffffffu, t, 0);
+  };
+  // the dt choice of step s for grid g: dt_begin, then dt_end unless the
+  // grid needs the first-step passes (flagged for the whole launch)
+  auto choose_dt = [&](Ctrl* c, int s) {
+    dt_begin_dev(c, 2);
+    if (tid == 0) {
+      defer = !c->done && (c->need_smallp | c->need_cell[0] | c->need_cell[1]);
+      if (defer) atomicOr(&gs->need[s & 1], 1);
+    }
+    __syncthreads();
+    if (!defer) dt_end_dev(c, ls.dte);
+    __syncthreads();
+  };
+  // (the host clears *gs, need flags included, before the launch)
+  for (int g = blockIdx.x; g < ls.n; g += nb) {  // call_begin, then step 0's dt
+    Ctrl* c = ls.ctrls[g];
+    if (tid == 0) {
       c->done = 0;
       c->steps = 0;
       c->maxsteps = ls.nsteps;
       c->tstop = ls.tstop;
     }
-    if (blockIdx.x == 0) gs->need[0] = gs->need[1] = 0;
+    __syncthreads();
+    if (ls.nsteps > 0) choose_dt(c, 0);
   }
-  if (!grid_sync(gs, nb)) return;
   for (int s = 0; s < ls.nsteps; s++) {
     const int par = (ls.par0 + s) & 1;
-    if (blockIdx.x == 0 && tid == 0) gs->need[(s + 1) & 1] = 0;
-    for (int g = blockIdx.x; g < ls.n; g += nb) {
-      Ctrl* c = ls.ctrls[g];
-      dt_begin_dev(c, 2);
-      if (tid == 0 && !c->done && (c->need_smallp | c->need_cell[0] | c->need_cell[1]))
-        atomicOr(&gs->need[s & 1], 1);
-    }
     if (!grid_sync(gs, nb)) return;
+    // every CTA read need[(s+1)&1] in step s-1, before this barrier
+    if (blockIdx.x == 0 && tid == 0) gs->need[(s + 1) & 1] = 0;
     if (__ldcg(&gs->need[s & 1])) {
       // the first-step passes: nparts parts of each grid's cells
       const int np = ls.nparts;
@@ -237,13 +255,21 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 3) kb_steps_line2(const Line2
         SW::template cell_cmax<L2_NT>(in->sa, in->buf[__ldcg(&in->sa.ctrl->cur)], u % np, np);
       }
       if (!grid_sync(gs, nb)) return;
+      for (int g = blockIdx.x; g < ls.n; g += nb) {
+        Ctrl* c = ls.ctrls[g];
+        if (!c->done && (c->need_cell[0] | c->need_cell[1])) dt_end_dev(c, ls.dte);
+      }
+      if (!grid_sync(gs, nb)) return;
     }
-    for (int g = blockIdx.x; g < ls.n; g += nb) dt_end_dev(ls.ctrls[g], ls.dte);
-    if (!grid_sync(gs, nb)) return;
     for (int sw = 0; sw < 2; sw++) {
       const int D = (!par || ls.xy) ? sw : 1 - sw;
       const BItem* items = ls.items[D];
-      for (int it = gw; it < ls.nitems[D]; it += nwarps) {
+      // items claimed one at a time (the next claim in flight while an item
+      // runs); next[sw] is cleared for the following step once every warp
+      // is past this sweep's barrier
+      int it = claim(&gs->next[sw]);
+      while (it < ls.nitems[D]) {
+        const int nx = claim(&gs->next[sw]);
         const BItem item = items[it];
         const BInst* in = ls.insts + item.inst;
         const int src = __ldcg(&in->fa.ctrl->cur) ^ (sw & 1);
@@ -253,11 +279,17 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 3) kb_steps_line2(const Line2
         else
           Line2<1, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], ring[warp],
                                         item.bx, item.by, item.bz, (unsigned)it);
+        it = nx;
       }
       if (!grid_sync(gs, nb)) return;
+      if (blockIdx.x == 0 && tid == 0) gs->next[sw] = 0;
     }
-    for (int g = blockIdx.x; g < ls.n; g += nb) step_end_dev(ls.ctrls[g], 2, 0);
-    if (!grid_sync(gs, nb)) return;
+    for (int g = blockIdx.x; g < ls.n; g += nb) {
+      Ctrl* c = ls.ctrls[g];
+      step_end_dev(c, 2, 0);
+      __syncthreads();
+      if (s + 1 < ls.nsteps) choose_dt(c, s + 1);
+    }
   }
 }
 
