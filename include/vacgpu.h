@@ -539,6 +539,15 @@ const char* vacgpu_version(void);
  * The denominator of the plain FP64 path's FP64-pipe roofline. */
 int vacgpu_measure_fp64_peak(double* flops_per_s, void* stream);
 
+/* Diagnostic (no counterpart in the reference): runs out, on purpose, the
+ * two kinds of bounded device wait the kernels use, each with a limit of
+ * about 2^22 cycles: an mbarrier phase that no copy completes (the TMA
+ * waits of the sweeps) and a grid-wide barrier that one CTA of a
+ * cooperative launch never reaches (the one-launch batched step).
+ * *mbar_timed_out and *grid_timed_out receive 1 when the wait gave up and
+ * reported it, as designed; the context stays usable.  Nothing faults. */
+int vacgpu_test_bounded_waits(int* mbar_timed_out, int* grid_timed_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,7 @@
 // sweep_line2.cu - instances and launchers of the warp-marching fused sweep
 // of 2-D grids (mixed precision), single grids and batches.
 #include <cstdlib>
+#include <string>
 
 #include "batch_items.cuh"
 #include "physics_mixed.cuh"
@@ -152,11 +153,12 @@ namespace vacgpu {
 
 // Grid-wide barrier of a cooperative launch (every CTA resident): the last
 // CTA to arrive resets the count and advances the generation; the others
-// wait for the generation to move, at most about 2^31 cycles, after which
-// the barrier reports failure and sets the fault flag.  Writes before the
-// barrier are visible after it (CTA barrier, then a device-scope fence by
-// the arriving thread, and a fence after the wait).
-__device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb) {
+// wait for the generation to move, at most `limit` cycles (about a second
+// by default), after which the barrier reports failure and sets the fault
+// flag.  Writes before the barrier are visible after it (CTA barrier, then
+// a device-scope fence by the arriving thread, and a fence after the wait).
+__device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb,
+                                          long long limit = 1LL << 31) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -171,7 +173,7 @@ __device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb) {
     } else {
       const long long t0 = clock64();
       while (*vgen == g) {
-        if (clock64() - t0 > (1LL << 31)) {
+        if (clock64() - t0 > limit) {
           atomicExch(&gs->fault, 1);
           break;
         }
@@ -344,4 +346,65 @@ bool launch_line2_steps(const Line2Steps& ls, bool mhd, int lim, bool gen, int c
 }
 #undef L2S_DISPATCH
 
+// ------------------------------------------ bounded waits, run out on purpose
+
+// An mbarrier phase that nothing completes (no arrival, no copy): the
+// bounded wait of the TMA-fed sweeps gives up after `limit` cycles.
+__global__ void k_wait_mbar_out(int* out, long long limit) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    out[0] = mbar_wait(&bar, 0, limit) ? 0 : 1;
+  }
+}
+
+// A grid-wide barrier that CTA 1 never reaches: CTA 0's wait gives up after
+// `limit` cycles and sets the fault flag.
+__global__ void k_wait_grid_out(GridSync* gs, int* out, long long limit) {
+  if (blockIdx.x != 0) return;
+  const bool ok = grid_sync(gs, gridDim.x, limit);
+  if (threadIdx.x == 0) out[1] = (!ok && gs->fault) ? 1 : 0;
+}
+
 }  // namespace vacgpu
+
+int vacgpu_internal_fail(const char* msg);
+
+extern "C" int vacgpu_test_bounded_waits(int* mbar_timed_out, int* grid_timed_out) {
+  using namespace vacgpu;
+  int* d = nullptr;
+  GridSync* gs = nullptr;
+  int h[2] = {0, 0};
+  cudaError_t e = cudaMalloc(&d, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&gs, sizeof(GridSync));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(gs, 0, sizeof(GridSync));
+  const long long limit = 1LL << 22;  // about 2 ms
+  if (e == cudaSuccess) {
+    k_wait_mbar_out<<<1, 32>>>(d, limit);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(32);
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_wait_grid_out, gs, d, limit);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(gs);
+  if (e != cudaSuccess) {
+    std::string m = std::string("bounded-wait test: ") + cudaGetErrorString(e);
+    return vacgpu_internal_fail(m.c_str());
+  }
+  if (mbar_timed_out) *mbar_timed_out = h[0];
+  if (grid_timed_out) *grid_timed_out = h[1];
+  return 0;
+}

@@ -27,7 +27,7 @@ SYMBOLS = [
     "vacgpu_server_submit", "vacgpu_server_result", "vacgpu_server_timing",
     "vacgpu_server_stats", "vacgpu_server_destroy", "vacgpu_measure_fp64_peak",
     "vacgpu_register_source_fn", "vacgpu_snapshot_begin", "vacgpu_snapshot_wait",
-    "vacgpu_snapshot_data",
+    "vacgpu_snapshot_data", "vacgpu_test_bounded_waits",
 ]
 
 K_PREDICT, K_CORRECT, K_SWEEP, K_GHOST, K_DT, K_CONTROL, K_NCLASS = range(7)
