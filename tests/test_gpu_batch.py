@@ -53,8 +53,9 @@ def test_batch_mhd2d_general_and_tuned_rows(gpu_lib):
     """2-D MHD grids of different sizes on the warp-marching line sweep, one
     of them with reflecting walls, so the batch runs the sweep's general
     form while the periodic grids alone run its fast form: the same bits.
-    The tuner picks rows per work item among 16, 32 and 64 (chunking does
-    not change any arithmetic)."""
+    The tuner picks the rows per work item: 16, or a guided list whose
+    items shrink toward its end (chunking does not change any
+    arithmetic)."""
     from tests.test_gpu_fused import reflecting
     snaps = [inistate.orszag_tang(n) for n in (40, 75, 130)]
     grids = []
@@ -65,7 +66,7 @@ def test_batch_mhd2d_general_and_tuned_rows(gpu_lib):
         grids.append((p, s.x, s.w))
     b = Batch(grids)
     ctas, order, rows, one, ms = b.tune()
-    assert rows in (16, 32, 64) and len(ms) == 24
+    assert rows in (16, -32, -16) and len(ms) == 24
     b.step(6)
     for i, (p, x, w) in enumerate(grids):
         e = Engine(p, x, w)

@@ -50,7 +50,10 @@ int vacgpu_internal_set_cur(vacgpu_handle* h, int cur);
 namespace {
 
 // rows per work item of the 2-D line sweep (the autotuner's item shapes)
-constexpr int LINE2_SHAPES[3] = {16, 32, 64};
+// (negative: a guided list of base -r: items of -r rows, then toward the
+// end of the list items of -r/2, -r/4 and -r/8 rows, two of each per grid
+// and strip, so the sweep ends on short items)
+constexpr int LINE2_SHAPES[3] = {16, -32, -16};
 
 typedef PHMixed<PREC_FF> PHB;
 
@@ -352,33 +355,56 @@ int prepare(vacgpu_batch* b) {
     // columns of faces
     const int xext = b->pair && D == 0 ? 1 : 0;
     for (int sh = 0; sh < b->nshape; sh++) {
-    std::vector<std::vector<BItem>> per(n);
+    // per grid, per level (guided lists: item size B, B/2, B/4, B/8)
+    std::vector<std::vector<BItem>> per[4];
+    for (auto& l : per) l.resize(n);
     for (int i = 0; i < n; i++) {
       const DevGrid& g = ins[i].fa.g;
       if (b->line2) {  // (strip, first and end row), strips fastest
-        const int ns = line2_strips(D, mhd, g.nx[0]), rows = LINE2_SHAPES[sh];
-        for (int y = 0; y < g.nx[1]; y += rows)
+        const int ns = line2_strips(D, mhd, g.nx[0]), r = LINE2_SHAPES[sh];
+        const int ny = g.nx[1], B = r > 0 ? r : -r;
+        // row chunks (first row, rows, level): the last rows in short chunks
+        std::vector<int> tail;  // sizes from the top row down
+        int rem = ny;
+        if (r < 0)
+          for (int lv = 3; lv >= 1; lv--)
+            for (int k = 0; k < 2 && rem > 0; k++) {
+              const int c = std::min(std::max(B >> lv, 1), rem);
+              tail.push_back(c | lv << 16);
+              rem -= c;
+            }
+        auto add = [&](int y0, int rows, int lv) {
           for (int x = 0; x < ns; x++)
-            per[i].push_back({i, x, 2 + y, 2 + std::min(y + rows, g.nx[1])});
+            per[lv][i].push_back({i, x, 2 + y0, 2 + y0 + rows});
+        };
+        for (int y = 0; y < rem; y += B) add(y, std::min(B, rem - y), 0);
+        int y = rem;
+        for (int k = (int)tail.size() - 1; k >= 0; k--) {
+          add(y, tail[k] & 0xffff, tail[k] >> 16);
+          y += tail[k] & 0xffff;
+        }
         continue;
       }
       const int nbx = (g.nx[0] + xext + tx - 1) / tx, nby = (g.nx[ar] + ty - 1) / ty;
       const int nbz = g.ndim == 3 ? (g.nx[am] + ins[i].fa.nzc - 1) / ins[i].fa.nzc : 1;
       for (int z = 0; z < nbz; z++)
         for (int y = 0; y < nby; y++)
-          for (int x = 0; x < nbx; x++) per[i].push_back({i, x, y, z});
+          for (int x = 0; x < nbx; x++) per[0][i].push_back({i, x, y, z});
     }
     std::vector<BItem> rr, gm;
-    size_t maxk = 0;
-    for (auto& v : per) maxk = std::max(maxk, v.size());
-    for (size_t k = 0; k < maxk; k++)
-      for (int i = 0; i < n; i++)
-        if (k < per[i].size()) rr.push_back(per[i][k]);
-    std::vector<int> idx(n);
-    for (int i = 0; i < n; i++) idx[i] = i;
-    std::sort(idx.begin(), idx.end(),
-              [&](int a, int c) { return per[a].size() > per[c].size(); });
-    for (int i : idx) gm.insert(gm.end(), per[i].begin(), per[i].end());
+    for (int lv = 0; lv < 4; lv++) {
+      size_t maxk = 0;
+      for (auto& v : per[lv]) maxk = std::max(maxk, v.size());
+      for (size_t k = 0; k < maxk; k++)
+        for (int i = 0; i < n; i++)
+          if (k < per[lv][i].size()) rr.push_back(per[lv][i][k]);
+      std::vector<int> idx(n);
+      for (int i = 0; i < n; i++) idx[i] = i;
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) {
+        return ins[a].fa.g.ncell > ins[c].fa.g.ncell;
+      });
+      for (int i : idx) gm.insert(gm.end(), per[lv][i].begin(), per[lv][i].end());
+    }
     b->nitems[D][sh] = (int)rr.size();
     for (int o = 0; o < 2; o++) {
       const std::vector<BItem>& l = o ? gm : rr;
