@@ -197,9 +197,10 @@ __device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb,
 // written on one SM are read on others through L2 (the control functions,
 // Line2::run and the first-step passes use ld.global.cg), and the rows of
 // the state arrive by cp.async.cg, so no stale L1 line from an earlier step
-// is read.
+// is read.  (HD: four CTAs per SM at 128 registers, with some spilling in
+// the general form, ran config 3 about 3 % faster than three CTAs without.)
 template <bool MHD, int LIMC, bool GEN>
-__global__ void __launch_bounds__(L2_NT, MHD ? 2 : 3) kb_steps_line2(const Line2Steps ls) {
+__global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4) kb_steps_line2(const Line2Steps ls) {
   constexpr int RF = line2_ring_floats(MHD ? 6 : 4);
   __shared__ __align__(16) float ring[L2_NT / 32][RF];
   __shared__ int defer;
