@@ -416,10 +416,14 @@ int vacgpu_batch_download(vacgpu_batch* b, int i, double* w);
 /* Advance every grid by up to nsteps steps (vacgpu_step semantics per
  * grid).  The steps are captured once into a CUDA graph of batched launches
  * (persistent sweep kernels over the work list of all grids' tiles) and
- * replayed on later calls with the same nsteps, or, for 2-D line-sweep
- * batches where the tuner finds it faster, run as one cooperative launch
- * with grid-wide barriers between the phases of each step.  The first call
- * tunes the launch shape (VACGPU_TUNE=0 skips tuning). */
+ * replayed on later calls with the same nsteps and tstop, or, for 2-D
+ * line-sweep batches where the tuner finds it faster, run as one
+ * cooperative launch (itself captured and replayed) with grid-wide barriers
+ * between the phases of each step.  The first call tunes the launch shape
+ * (VACGPU_TUNE=0 skips tuning).  With 'xyyx' splitting every grid starts a
+ * step with the sweep its own it selects: after a tstop that ended the
+ * grids at different parities of it, 2-D batches continue correctly (one
+ * launch, per-grid sweep order) and 3-D batches refuse the call. */
 int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop);
 /* t, it, dt and the finished flag of grid i. */
 int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,

@@ -82,7 +82,8 @@ def test_batch_line_sweep_forms(gpu_lib, monkeypatch, form, case):
     cooperative launch with grid-wide barriers between the phases.  Each
     gives the bits, t and it of the grids advanced alone, over two calls,
     and with a tstop that the grids reach at different steps (grids that
-    are done sit out the remaining steps of the launch)."""
+    are done sit out the remaining steps of the launch), and over the call
+    after it, which steps grids at different parities of it."""
     monkeypatch.setenv("VACGPU_ONELAUNCH", "1" if form == "one_launch" else "0")
     if case == "hd_outflow":
         grids = inistate.riemann_batch(n=5, seed=7, lo=24, hi=140)
@@ -103,18 +104,56 @@ def test_batch_line_sweep_forms(gpu_lib, monkeypatch, form, case):
         t, it, dt, fin = b.status(i)
         assert (it, t) == (e.it, e.t), (i, it, e.it, t, e.t)
         assert np.array_equal(bits(b.state(i)), bits(e.state())), i
-    # a stop time that the first grid reaches after 5 steps
-    e0 = Engine(*grids[0])
-    e0.step(5)
-    tstop = e0.t
+    # a stop time that the grids reach at different steps, of both parities
+    for k in (4, 5, 3, 6):
+        e0 = Engine(*grids[0])
+        e0.step(k)
+        tstop = e0.t
+        singles = [Engine(*g) for g in grids]
+        for e in singles:
+            e.step(9, tstop)
+        if len({e.it % 2 for e in singles}) > 1:
+            break
+    else:
+        pytest.fail("no stop time leaves the grids at different parities of it")
     b2 = Batch(grids)
     b2.step(9, tstop)
     its = set()
-    for i, (p, x, w) in enumerate(grids):
-        e = Engine(p, x, w)
-        e.step(9, tstop)
+    for i, e in enumerate(singles):
         t, it, dt, fin = b2.status(i)
-        its.add(it)
+        its.add(it % 2)
         assert (it, t) == (e.it, e.t), (i, it, e.it, t, e.t)
         assert np.array_equal(bits(b2.state(i)), bits(e.state())), i
-    assert len(its) > 1  # the grids stopped at different steps
+    # the grids stopped at different parities of it; the next call steps each
+    # with the sweep order of its own it ('xyyx')
+    assert its == {0, 1}
+    b2.step(5)
+    for i, e in enumerate(singles):
+        e.step(5)
+        t, it, dt, fin = b2.status(i)
+        assert (it, t) == (e.it, e.t), (i, it, e.it, t, e.t)
+        assert np.array_equal(bits(b2.state(i)), bits(e.state())), i
+
+
+def test_batch3d_refuses_mixed_parities(gpu_lib):
+    """A 3-D batch whose grids a stop time left at different parities of it
+    ('xyyx': each grid's next step starts with the sweep its own it
+    selects) refuses the next call instead of stepping some grids in the
+    wrong order."""
+    snaps = [inistate.random_modes(n, seed=i) for i, n in enumerate([12, 20, 33])]
+    grids = [(inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED), s.x, s.w)
+             for s in snaps]
+    for k in (4, 5, 3, 6):
+        e0 = Engine(*grids[0])
+        e0.step(k)
+        singles = [Engine(*g) for g in grids]
+        for e in singles:
+            e.step(9, e0.t)
+        if len({e.it % 2 for e in singles}) > 1:
+            break
+    else:
+        pytest.fail("no stop time leaves the grids at different parities of it")
+    b = Batch(grids)
+    b.step(9, e0.t)
+    with pytest.raises(RuntimeError, match="parities"):
+        b.step(2)

@@ -139,8 +139,18 @@ struct vacgpu_batch {
   int it0;
   struct G {
     int nsteps, par;
+    double tstop;
+    bool onelaunch;
     cudaGraphExec_t ex;
   };
+  bool nograph_one;  // the cooperative launch could not be captured: launch it directly
+  // 2-D line sweeps: host copies of the work lists (the phase lists of a
+  // call on grids at different parities of it are built from them) and
+  // the device buffers of those phase lists
+  std::vector<BItem> h_items[2][2][3];
+  BItem* d_plist[2];
+  int nplist[2];
+  std::vector<int> its;  // it of every grid after the last call
   std::vector<G> graphs;
 };
 
@@ -251,20 +261,21 @@ void issue_step(vacgpu_batch* b, int parity, int ctas, int order, int shape) {
 // step's end, separated by grid-wide barriers.  The barrier's counters are
 // cleared before every launch, so a launch after a timed-out barrier starts
 // clean.
-int issue_steps_one(vacgpu_batch* b, int nsteps, double tstop, int par, int order, int shape) {
+int issue_steps_lists(vacgpu_batch* b, int nsteps, double tstop, int par, int xy,
+                      const BItem* l0, int n0, const BItem* l1, int n1) {
   const vacgpu_params& p = b->p0;
   Line2Steps ls;
-  for (int D = 0; D < 2; D++) {
-    ls.items[D] = b->d_items[D][order][shape];
-    ls.nitems[D] = b->nitems[D][shape];
-  }
+  ls.items[0] = l0;
+  ls.nitems[0] = n0;
+  ls.items[1] = l1;
+  ls.nitems[1] = n1;
   ls.insts = b->d_insts;
   ls.ctrls = b->d_ctrls;
   ls.n = b->n;
   ls.nsteps = nsteps;
   ls.tstop = tstop;
   ls.par0 = par;
-  ls.xy = p.typedimsplit == VACGPU_SPLIT_XY;
+  ls.xy = xy;
   ls.dte = dt_end_args(p);
   ls.smallpcoeff = p.smallpcoeff;
   ls.nparts = b->nparts;
@@ -275,6 +286,47 @@ int issue_steps_one(vacgpu_batch* b, int nsteps, double tstop, int par, int orde
     return bfail(std::string("cooperative launch of the batched steps failed: ") +
                  cudaGetErrorString(cudaGetLastError()));
   return 0;
+}
+
+int issue_steps_one(vacgpu_batch* b, int nsteps, double tstop, int par, int order, int shape) {
+  return issue_steps_lists(b, nsteps, tstop, par, b->p0.typedimsplit == VACGPU_SPLIT_XY,
+                           b->d_items[0][order][shape], b->nitems[0][shape],
+                           b->d_items[1][order][shape], b->nitems[1][shape]);
+}
+
+// A call on 2-D grids whose it differ in parity ('xyyx' splitting: each
+// grid starts its step with the sweep its own it selects).  Phase list q
+// serves the first sweep of the launch's steps s with s%2 == q and the
+// second sweep of the others: grid g's x items where (it_g + q) is even,
+// its y items otherwise, the two lists merged by position so that the
+// short items of a guided list stay at the end.
+int issue_steps_mixed(vacgpu_batch* b, int nsteps, double tstop) {
+  const std::vector<BItem>& X = b->h_items[0][b->order][b->shape];
+  const std::vector<BItem>& Y = b->h_items[1][b->order][b->shape];
+  for (int q = 0; q < 2; q++) {
+    std::vector<BItem> P;
+    P.reserve(X.size() + Y.size());
+    size_t ix = 0, iy = 0;
+    auto takex = [&](const BItem& it) { return ((b->its[it.inst] + q) & 1) == 0; };
+    while (ix < X.size() || iy < Y.size()) {
+      const bool fromx = iy >= Y.size() ||
+                         (ix < X.size() && (double)ix * Y.size() <= (double)iy * X.size());
+      if (fromx) {
+        if (takex(X[ix])) P.push_back(X[ix]);
+        ix++;
+      } else {
+        if (!takex(Y[iy])) P.push_back(Y[iy]);
+        iy++;
+      }
+    }
+    if (!b->d_plist[q]) BCK(cudaMalloc(&b->d_plist[q], sizeof(BItem) * (X.size() + Y.size())));
+    BCK(cudaMemcpyAsync(b->d_plist[q], P.data(), sizeof(BItem) * P.size(),
+                        cudaMemcpyHostToDevice, b->st));
+    BCK(cudaStreamSynchronize(b->st));  // P leaves scope
+    b->nplist[q] = (int)P.size();
+  }
+  return issue_steps_lists(b, nsteps, tstop, 0, 0, b->d_plist[0], b->nplist[0], b->d_plist[1],
+                           b->nplist[1]);
 }
 
 int prepare(vacgpu_batch* b) {
@@ -373,9 +425,10 @@ int prepare(vacgpu_batch* b) {
               tail.push_back(c | lv << 16);
               rem -= c;
             }
+        // (the item's sweep direction in bit 30 of bx, the strip below it)
         auto add = [&](int y0, int rows, int lv) {
           for (int x = 0; x < ns; x++)
-            per[lv][i].push_back({i, x, 2 + y0, 2 + y0 + rows});
+            per[lv][i].push_back({i, x | D << 30, 2 + y0, 2 + y0 + rows});
         };
         for (int y = 0; y < rem; y += B) add(y, std::min(B, rem - y), 0);
         int y = rem;
@@ -408,6 +461,7 @@ int prepare(vacgpu_batch* b) {
     b->nitems[D][sh] = (int)rr.size();
     for (int o = 0; o < 2; o++) {
       const std::vector<BItem>& l = o ? gm : rr;
+      if (b->line2) b->h_items[D][o][sh] = l;
       BCK(cudaMalloc(&b->d_items[D][o][sh], sizeof(BItem) * l.size()));
       BCK(cudaMemcpy(b->d_items[D][o][sh], l.data(), sizeof(BItem) * l.size(),
                      cudaMemcpyHostToDevice));
@@ -588,6 +642,9 @@ int vacgpu_batch_upload(vacgpu_batch* b, int i, const double* w, int it,
   if (vacgpu_upload(b->h[i], w, it, t)) return 1;
   if (i == 0) b->it0 = it;
   if (it != b->it0) return bfail("grids of a batch start at the same it");
+  if (b->its.size() != (size_t)b->n) b->its.assign(b->n, it);
+  b->its[i] = it;
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.ex);
   b->graphs.clear();
   return 0;
 }
@@ -609,41 +666,71 @@ int vacgpu_batch_step(vacgpu_batch* b, int nsteps, double tstop) {
   const char* tz = getenv("VACGPU_TUNE");
   if (!b->tuned && !(tz && atoi(tz) == 0))
     if (autotune(b)) return 1;
-  const int par = b->it0 & 1;
+  if (b->its.size() != (size_t)b->n) b->its.assign(b->n, b->it0);
+  // 'xyyx' grids that a stop time left at different parities of it
+  bool mixed = false;
+  if (b->p0.typedimsplit != VACGPU_SPLIT_XY)
+    for (int i = 1; i < b->n; i++) mixed = mixed || ((b->its[i] ^ b->its[0]) & 1);
+  if (mixed && !b->line2)
+    return bfail("grids of a 3-D batch are at different parities of it (a stop time ended "
+                 "them at different steps); upload them again to continue");
+  const int par = b->its[0] & 1;
   cudaGraphExec_t ex = nullptr;
   for (auto& g : b->graphs)
-    if (g.nsteps == nsteps && g.par == par) ex = g.ex;
-  if (b->onelaunch) {
-    if (issue_steps_one(b, nsteps, tstop, par, b->order, b->shape)) return 1;
-  } else if (!ex) {
-    cudaGraph_t gr;
+    if (g.nsteps == nsteps && g.par == par && g.tstop == tstop && g.onelaunch == b->onelaunch)
+      ex = g.ex;
+  if (mixed) {
+    if (issue_steps_mixed(b, nsteps, tstop)) return 1;
+  } else if (!ex && !(b->onelaunch && b->nograph_one)) {
+    // the call's launches captured once and replayed (the one-launch form:
+    // the clears of its counters and the cooperative launch)
+    cudaGraph_t gr = nullptr;
     BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-    launchb_control(4, b->d_ctrls, b->n, b->p0, 0, nsteps, tstop, b->st);
-    for (int s = 0; s < nsteps; s++)
-      issue_step(b, (par + s) & 1, b->ctas, b->order, b->shape);
-    BCK(cudaStreamEndCapture(b->st, &gr));
-    BCK(cudaGraphInstantiate(&ex, gr, 0));
-    cudaGraphDestroy(gr);
-    b->graphs.push_back({nsteps, par, ex});
+    int rc = 0;
+    if (b->onelaunch) {
+      rc = issue_steps_one(b, nsteps, tstop, par, b->order, b->shape);
+    } else {
+      launchb_control(4, b->d_ctrls, b->n, b->p0, 0, nsteps, tstop, b->st);
+      for (int s = 0; s < nsteps; s++)
+        issue_step(b, (par + s) & 1, b->ctas, b->order, b->shape);
+    }
+    const cudaError_t e = cudaStreamEndCapture(b->st, &gr);
+    cudaGraphExec_t gx = nullptr;
+    if (!rc && e == cudaSuccess && cudaGraphInstantiate(&gx, gr, 0) == cudaSuccess) {
+      ex = gx;
+      b->graphs.push_back({nsteps, par, tstop, b->onelaunch, ex});
+    } else if (b->onelaunch) {
+      b->nograph_one = true;  // launched directly below
+    } else {
+      if (gr) cudaGraphDestroy(gr);
+      (void)cudaGetLastError();
+      return rc ? 1 : bfail("capture of the batched steps failed");
+    }
+    if (gr) cudaGraphDestroy(gr);
+    (void)cudaGetLastError();
   }
-  if (!b->onelaunch) BCK(cudaGraphLaunch(ex, b->st));
+  if (mixed) {
+  } else if (ex) {
+    BCK(cudaGraphLaunch(ex, b->st));
+  } else if (issue_steps_one(b, nsteps, tstop, par, b->order, b->shape)) {
+    return 1;
+  }
   BCK(cudaStreamSynchronize(b->st));
-  if (b->onelaunch) {
+  if (b->onelaunch || mixed) {
     GridSync gs;
     BCK(cudaMemcpy(&gs, b->d_gs, sizeof(gs), cudaMemcpyDeviceToHost));
     if (gs.fault) return bfail("a grid-wide barrier of the batched steps timed out");
   }
   // every grid advanced the same number of steps unless it finished early
-  int steps0 = -1;
   for (int i = 0; i < b->n; i++) {
     HandleView v;
     vacgpu_internal_view(b->h[i], &v);
     Ctrl c;
     BCK(cudaMemcpy(&c, v.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost));
     if (c.fault) return bfail("a device wait timed out (TMA copy never completed)");
-    if (i == 0) steps0 = c.steps;
+    b->its[i] = c.it;
   }
-  b->it0 += steps0;
+  b->it0 = b->its[0];
   return 0;
 }
 
@@ -685,6 +772,8 @@ void vacgpu_batch_destroy(vacgpu_batch* b) {
   cudaFree(b->d_maps);
   cudaFree(b->d_ctrls);
   cudaFree(b->d_gs);
+  cudaFree(b->d_plist[0]);
+  cudaFree(b->d_plist[1]);
   for (int D = 0; D < 3; D++)
     for (int o = 0; o < 2; o++)
       for (int sh = 0; sh < 3; sh++) cudaFree(b->d_items[D][o][sh]);

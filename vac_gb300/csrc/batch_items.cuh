@@ -7,7 +7,8 @@
 
 namespace vacgpu {
 
-// one work item: a tile (bx, by) and z chunk bz of grid inst
+// one work item: a tile (bx, by) and z chunk bz of grid inst (2-D line
+// sweeps: strip bx with the sweep direction in bit 30, rows by .. bz-1)
 struct BItem {
   int inst, bx, by, bz;
 };

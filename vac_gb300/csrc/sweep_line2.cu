@@ -45,8 +45,8 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : (D == 1 && GEN ? 3 : 4))
     const BInst* in = insts + item.inst;
     const int src = in->fa.ctrl->cur ^ (sweep & 1);
     Line2<D, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1],
-                                  ring[threadIdx.x >> 5], item.bx, item.by, item.bz,
-                                  (unsigned)it);
+                                  ring[threadIdx.x >> 5], item.bx & L2_STRIP, item.by,
+                                  item.bz, (unsigned)it);
   }
 }
 
@@ -265,23 +265,25 @@ __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4) kb_steps_line2(const Line2
       if (!grid_sync(gs, nb)) return;
     }
     for (int sw = 0; sw < 2; sw++) {
-      const int D = (!par || ls.xy) ? sw : 1 - sw;
-      const BItem* items = ls.items[D];
+      // the list of this sweep (each item carries its own direction: the
+      // lists of a call on grids at different parities of it mix both)
+      const BItem* items = ls.items[(!par || ls.xy) ? sw : 1 - sw];
+      const int nit = ls.nitems[(!par || ls.xy) ? sw : 1 - sw];
       // items claimed one at a time (the next claim in flight while an item
       // runs); next[sw] is cleared for the following step once every warp
       // is past this sweep's barrier
       int it = claim(&gs->next[sw]);
-      while (it < ls.nitems[D]) {
+      while (it < nit) {
         const int nx = claim(&gs->next[sw]);
         const BItem item = items[it];
         const BInst* in = ls.insts + item.inst;
         const int src = __ldcg(&in->fa.ctrl->cur) ^ (sw & 1);
-        if (D == 0)
+        if (!(item.bx >> 30))
           Line2<0, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], ring[warp],
-                                        item.bx, item.by, item.bz, (unsigned)it);
+                                        item.bx & L2_STRIP, item.by, item.bz, (unsigned)it);
         else
           Line2<1, MHD, LIMC, GEN>::run(in->fa, in->buf[src], in->buf[src ^ 1], ring[warp],
-                                        item.bx, item.by, item.bz, (unsigned)it);
+                                        item.bx & L2_STRIP, item.by, item.bz, (unsigned)it);
         it = nx;
       }
       if (!grid_sync(gs, nb)) return;

@@ -42,6 +42,9 @@ constexpr int L2_NT = 128;   // threads per CTA: four independent warps
 constexpr int L2_ROWS = 32;  // rows per work item
 constexpr int L2_LOOK = 3;   // rows in flight ahead of use
 constexpr int L2_RING = L2_LOOK + 1;  // staging slots per warp
+// a batched work item's strip is bx & L2_STRIP; bit 30 of bx is its sweep
+// direction
+constexpr int L2_STRIP = (1 << 30) - 1;
 
 // A staged row holds, per variable, 68 floats: the strip's 64 columns from
 // the 16-byte boundary at or below its first one (2 columns earlier when

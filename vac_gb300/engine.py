@@ -331,8 +331,12 @@ class Server:
         self.meta = {}
 
     def submit(self, params, x, w, nsteps):
-        xf = np.ascontiguousarray(pack_mesh(x), dtype=np.float64)
-        wf = np.ascontiguousarray(pack_mesh(w), dtype=np.float64)
+        """Queue a solve of nsteps steps; x, w as for Engine, or already
+        flat in the C ABI's packed layout (each component in Fortran
+        order).  Returns the request id."""
+        x, w = np.asarray(x), np.asarray(w)
+        xf = np.ascontiguousarray(x if x.ndim == 1 else pack_mesh(x), dtype=np.float64)
+        wf = np.ascontiguousarray(w if w.ndim == 1 else pack_mesh(w), dtype=np.float64)
         rid = C.c_longlong()
         _ck(lib().vacgpu_server_submit(self.h, C.byref(params), _dp(xf), _dp(wf),
                                        nsteps, C.byref(rid)), "vacgpu_server_submit")
