@@ -440,14 +440,16 @@ def run_tvdmu(args):
     return out
 
 
-def random_modes_dev(n, seed, ndim, device):
+def random_modes_dev(n, seed, ndim, device, packed=False):
     """vac_gb300.inistate.random_modes (p0=0.05, beta ~ 0.1, 8 modes per
     field) with the fields evaluated by torch on `device`: the same seeded
     draws in the same order, the same formulas; the result differs from the
     NumPy evaluation by rounding only.  Returns (x, w) as NumPy arrays in
     the (ndim|nw, *nx) layout of a snapshot.  The served stream's requests
     are drawn with it (a NumPy evaluation of a 256^3 state takes tens of
-    seconds of host time)."""
+    seconds of host time).  packed: (x, w) as flat arrays in the C ABI's
+    layout instead (each component in Fortran order, permuted on the
+    device)."""
     import torch
     from vac_gb300 import inistate
     rng = np.random.default_rng(seed)
@@ -499,6 +501,11 @@ def random_modes_dev(n, seed, ndim, device):
     b2 = sum(bc * bc for bc in b)
     e = 0.05 / (gamma - 1) + 0.5 * rho * v2 + 0.5 * b2
     w = torch.stack([rho] + [rho * vc for vc in v] + [e] + b)
+    if packed:
+        perm = (0,) + tuple(range(ndim, 0, -1))
+        xt = torch.as_tensor(np.ascontiguousarray(x), device=device)
+        return (xt.permute(*perm).contiguous().reshape(-1).cpu().numpy(),
+                w.permute(*perm).contiguous().reshape(-1).cpu().numpy())
     return x, w.cpu().numpy()
 
 
@@ -517,34 +524,57 @@ def _served_requests(args):
 
 def run_served_rate(args, reqs, rate, arrivals_seed):
     """One served run: the requests arrive as a Poisson stream of the given
-    mean rate; each is drawn on the device, copied to the host and submitted
-    at its arrival time (the server copies it back on admission).  Per
-    request: time to solution, its queue part (submission to admission) and
-    its service part (admission to result)."""
+    mean rate.  A producer thread draws them on the device, in the ABI's
+    packed layout, and hands them to the submitting thread, at most 8 GB
+    ahead; the submitting thread submits each at its arrival time (the
+    server copies it, and back to the device on admission).  Per request:
+    time to solution, its queue part (submission to admission) and its
+    service part (admission to result); max_submit_lag_s is how far the
+    latest submission fell behind its arrival time."""
+    import queue
     import threading
     from vac_gb300 import abi, inistate
     from vac_gb300.engine import Server
     rng = np.random.default_rng(arrivals_seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
-    srv = Server(hbm_budget_bytes=150e9, max_active=8, steps_per_chunk=16)
+    srv = Server(hbm_budget_bytes=150e9, max_active=args.served_slots, steps_per_chunk=16)
     ids = [None] * len(reqs)
     late = [0.0] * len(reqs)
-    t0 = time.perf_counter()
+    ready = queue.Queue()
+    cv = threading.Condition()
+    ahead = [0]  # bytes drawn and not yet submitted
+    cap = 8e9
 
-    def feed():
-        for i, (nd, n, steps, seed) in enumerate(reqs):
-            x, w = random_modes_dev(n, seed, nd, "cuda")
-            snap = inistate._snap(x, w, 5.0 / 3.0, True, nd, "served")
+    def produce():
+        for nd, n, steps, seed in reqs:
+            nw = 2 + 2 * nd
+            nbytes = 8 * (nw + nd) * n ** nd
+            with cv:
+                cv.wait_for(lambda: ahead[0] == 0 or ahead[0] + nbytes <= cap)
+                ahead[0] += nbytes
+            xf, wf = random_modes_dev(n, seed, nd, "cuda", packed=True)
+            shape = np.broadcast_to(np.float64(0.0), (nw,) + (n,) * nd)
+            snap = inistate._snap(None, shape, 5.0 / 3.0, True, nd, "served")
             p = inistate.params_for(snap, limiter="woodward", precision=abi.PREC_MIXED)
-            dt = arrivals[i] - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            late[i] = max(0.0, -dt)
-            ids[i] = srv.submit(p, x, w, steps)
+            ready.put((p, xf, wf, steps, nbytes))
 
-    th = threading.Thread(target=feed)
-    th.start()
-    th.join()
+    prod = threading.Thread(target=produce)
+    prod.start()
+    while ready.qsize() < min(16, len(reqs)) and prod.is_alive():
+        time.sleep(0.01)
+    t0 = time.perf_counter()
+    for i in range(len(reqs)):
+        p, xf, wf, steps, nbytes = ready.get()
+        dt = arrivals[i] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        late[i] = max(0.0, -dt)
+        ids[i] = srv.submit(p, xf, wf, steps)
+        del xf, wf
+        with cv:
+            ahead[0] -= nbytes
+            cv.notify_all()
+    prod.join()
     tts, qs, svs = [], [], []
     for rid in ids:
         res = srv.result(rid, wait=1200.0, fetch=False)
@@ -582,8 +612,9 @@ def run_served(args, capacity):
         runs.append(dict(run_served_rate(args, reqs, ld * capacity / work, 11 + i), load=ld))
     return {"workload": "Poisson stream of %d MHD solves per load: 2D 128^2-2048^2 / "
                         "3D 64^3-256^3, 20-500 steps, random modes, mixed, 150 GB budget, "
-                        "8 slots" % len(reqs),
-            "loads": runs, "mean_cell_updates_per_request": float(work),
+                        "%d slots" % (len(reqs), args.served_slots),
+            "loads": runs, "slots": args.served_slots,
+            "mean_cell_updates_per_request": float(work),
             "capacity_cell_updates_per_s": capacity}
 
 
@@ -674,6 +705,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--served", type=int, default=200,
                     help="requests per offered load in the served stream (0: skip)")
+    ap.add_argument("--served-slots", type=int, default=8,
+                    help="solves the served run keeps in flight at most")
     ap.add_argument("--served-loads", default="0.5,0.9,1.2",
                     help="offered loads of the served stream, in units of the capacity")
     ap.add_argument("--acc-steps", type=int, default=100,
