@@ -537,7 +537,8 @@ def run_served_rate(args, reqs, rate, arrivals_seed):
     from vac_gb300.engine import Server
     rng = np.random.default_rng(arrivals_seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
-    srv = Server(hbm_budget_bytes=150e9, max_active=args.served_slots, steps_per_chunk=16)
+    srv = Server(hbm_budget_bytes=150e9, max_active=args.served_slots,
+                 steps_per_chunk=args.served_chunk)
     ids = [None] * len(reqs)
     late = [0.0] * len(reqs)
     ready = queue.Queue()
@@ -707,6 +708,8 @@ def main():
                     help="requests per offered load in the served stream (0: skip)")
     ap.add_argument("--served-slots", type=int, default=8,
                     help="solves the served run keeps in flight at most")
+    ap.add_argument("--served-chunk", type=int, default=16,
+                    help="steps the server issues per solve at a time")
     ap.add_argument("--served-loads", default="0.5,0.9,1.2",
                     help="offered loads of the served stream, in units of the capacity")
     ap.add_argument("--acc-steps", type=int, default=100,
