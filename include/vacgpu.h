@@ -432,8 +432,11 @@ int vacgpu_batch_status(vacgpu_batch* b, int i, double* t, int* it,
  * order (0 round-robin over grids, 1 grid-major), rows per work item of the
  * 2-D line sweep (16, or -B for a guided list: items of B rows, then two
  * each of B/2, B/4 and B/8 rows per grid and strip at the end of the list,
- * B = 32 or 16; 0 for 3-D batches, which have one item shape), whether the steps run as one cooperative launch (2-D line-sweep
- * batches only; ctas is then that launch's CTA count) and the trial times
+ * B = 32 or 16; 0 for 3-D batches, which have one item shape), whether
+ * the steps run as one cooperative launch (2-D line-sweep batches only;
+ * ctas is then that launch's CTA count; 2 once a step call has captured
+ * that launch into a CUDA graph, 1 otherwise, 0 for the graph of separate
+ * launches) and the trial times
  * in ms of two steps, 24 doubles: per item shape, per CTA count (two
  * persistent counts, then one CTA per item), per order; then the one-launch
  * form per item shape and order (0 where not tried). */

@@ -95,9 +95,10 @@ def test_batch_line_sweep_forms(gpu_lib, monkeypatch, form, case):
                           s.x, s.w))
     b = Batch(grids)
     ctas, order, rows, one, ms = b.tune()
-    assert one == (form == "one_launch") and ctas > 0
+    assert bool(one) == (form == "one_launch") and ctas > 0
     b.step(3)
     b.step(4)
+    assert (b.tune()[3] in (1, 2)) == (form == "one_launch")
     for i, (p, x, w) in enumerate(grids):
         e = Engine(p, x, w)
         e.step(7)

@@ -757,7 +757,11 @@ int vacgpu_batch_tune(vacgpu_batch* b, int* ctas, int* order, int* rows, int* on
   if (ctas) *ctas = b->ctas > 0 ? b->ctas : (b->line2 ? (ni + 3) / 4 : ni);
   if (order) *order = b->order;
   if (rows) *rows = b->line2 ? LINE2_SHAPES[b->shape] : 0;
-  if (onelaunch) *onelaunch = b->onelaunch;
+  if (onelaunch) {
+    bool graphed = false;
+    for (auto& g : b->graphs) graphed = graphed || g.onelaunch;
+    *onelaunch = !b->onelaunch ? 0 : graphed ? 2 : 1;
+  }
   if (ms)
     for (int k = 0; k < 24; k++) ms[k] = b->tune_ms[k];
   return 0;

@@ -280,13 +280,14 @@ class Batch:
 
     def tune(self):
         """(persistent CTAs, work-list order, rows per item of the 2-D line
-        sweep or 0, one cooperative launch for all steps (bool), trial times
-        in ms of the candidates tried)."""
+        sweep or 0, one cooperative launch for all steps (0 no, 1 yes, 2 yes
+        and captured in a CUDA graph by a step call), trial times in ms of
+        the candidates tried)."""
         c, o, r, one = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         ms = (C.c_double * 24)()
         _ck(lib().vacgpu_batch_tune(self.h, C.byref(c), C.byref(o), C.byref(r),
                                     C.byref(one), ms), "vacgpu_batch_tune")
-        return c.value, o.value, r.value, bool(one.value), [m for m in ms if m > 0]
+        return c.value, o.value, r.value, one.value, [m for m in ms if m > 0]
 
     def status(self, i):
         t, it, dt, fin = C.c_double(), C.c_int(), C.c_double(), C.c_int()
