@@ -1,7 +1,8 @@
 """Batched grids: every grid of a batch (persistent sweep kernels over all
-grids' tiles, one CUDA graph) gives bit for bit the state, t and it of the
-same grid advanced alone by vacgpu_step in the same precision, and stays
-within the mixed tolerance of the FP64 oracle."""
+grids' tiles in one CUDA graph, or, for 2-D grids, all steps of a call in
+one cooperative launch) gives bit for bit the state, t and it of the same
+grid advanced alone by vacgpu_step in the same precision, and stays within
+the mixed tolerance of the FP64 oracle."""
 import numpy as np
 import pytest
 
