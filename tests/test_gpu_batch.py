@@ -76,7 +76,7 @@ def test_batch_mhd2d_general_and_tuned_rows(gpu_lib):
 
 
 @pytest.mark.parametrize("form", ["graph", "one_launch"])
-@pytest.mark.parametrize("case", ["hd_outflow", "mhd_periodic"])
+@pytest.mark.parametrize("case", ["hd_outflow", "mhd_periodic", "mhd_reflecting"])
 def test_batch_line_sweep_forms(gpu_lib, monkeypatch, form, case):
     """Both forms of a 2-D line-sweep batch, forced through VACGPU_ONELAUNCH:
     the graph of launches per step, and all steps of a call in one
@@ -89,11 +89,14 @@ def test_batch_line_sweep_forms(gpu_lib, monkeypatch, form, case):
     if case == "hd_outflow":
         grids = inistate.riemann_batch(n=5, seed=7, lo=24, hi=140)
     else:
+        from tests.test_gpu_fused import reflecting
         grids = []
-        for n in (36, 64, 100):
+        for k, n in enumerate((36, 64, 100)):
             s = inistate.orszag_tang(n)
-            grids.append((inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED),
-                          s.x, s.w))
+            p = inistate.params_for(s, limiter="woodward", precision=abi.PREC_MIXED)
+            if case == "mhd_reflecting" and k == 1:
+                reflecting(p, 2)  # the whole batch runs the general form
+            grids.append((p, s.x, s.w))
     b = Batch(grids)
     ctas, order, rows, one, ms = b.tune()
     assert bool(one) == (form == "one_launch") and ctas > 0
