@@ -474,13 +474,14 @@ int prepare(vacgpu_batch* b) {
 
 // Autotuner: time two steps of every candidate launch shape on the batch
 // itself, after one untimed step (state and control blocks restored after
-// each trial), and keep the fastest.  Candidates: persistent CTAs (per SM: 1 and 2 for the one-cell
-// sweep, whose 103 KB CTAs fit twice; 2 and 3 for the pair sweep; 4 and 8
-// CTAs of four warps for the 2-D line sweep) or one CTA (line sweep: one
-// warp) per work item, times two work-list orders, times the item shapes
-// (2-D line sweep: 16, 32 or 64 rows per item); for 2-D line-sweep batches
-// also the one-launch form of every item shape and order
-// (VACGPU_ONELAUNCH=0 leaves it out, =1 takes it).
+// each trial), and keep the fastest.  Candidates: persistent CTAs (per SM:
+// 1 and 2 for the one-cell sweep, whose 103 KB CTAs fit twice; 2 and 3 for
+// the pair sweep; 4 and 8 CTAs of four warps for the 2-D line sweep) or one
+// CTA (line sweep: one warp) per work item, times two work-list orders,
+// times the item shapes (2-D line sweep: LINE2_SHAPES, 16 rows per item or
+// a guided list); for 2-D line-sweep batches also the one-launch form of
+// every item shape and order (VACGPU_ONELAUNCH=0 leaves it out, =1 takes
+// it).
 int autotune(vacgpu_batch* b) {
   if (b->tuned) return 0;
   const int n = b->n;

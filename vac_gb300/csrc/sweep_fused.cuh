@@ -19,8 +19,9 @@
 // The tile shape depends on the kind so that each phase is one work item
 // per thread: the predictor is needed in full on (TX+2) x TY cells for K=0,
 // TX x (TY+2) for K=1 and TX x TY for K=2 -- 256 cells each with 30x8, 32x6
-// and 32x8 tiles -- and the in-plane faces number at most 256.  The remaining halo cells feed only the div B of the Powell source,
-// so there only the transverse B component is predicted.  With
+// and 32x8 tiles -- and the in-plane faces number at most 256.  The
+// remaining halo cells feed only the div B of the Powell source, so there
+// only the transverse B component is predicted.  With
 // typelimited='original' the corrector limits the same state w that the
 // predictor limits (src/vactvdlf.t:150-157), so the predictor's limited
 // slopes are kept in shared memory and reused by the faces.
