@@ -402,3 +402,37 @@ def test_mixed_tvdmu_within_tolerance(gpu_lib, name, mk, lim, bc, n, tweak, src)
             continue
         rel = np.abs(a[iw] - b[iw]).sum() / den
         assert rel <= MIXED_REL_L1, (iw, rel)
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED], ids=["fp64", "mixed"])
+def test_alfven_wave_one_period(gpu_lib, precision):
+    """A circularly polarized Alfven wave (2.5-D, ndir = 3; an exact ideal-MHD
+    solution) over one period at 64 cells per wavelength: FP64 bit for bit
+    with the oracle, mixed within its tolerance, and both within the scheme's
+    own distance from the exact (initial) state."""
+    from tests.test_oracle import alfven_wave
+    s = alfven_wave(64)
+    p = inistate.params_for(s, limiter="woodward", bc="periodic", precision=precision)
+    p.tmax, p.tmaxexact = 1.0, 1
+    q = inistate.params_for(s, limiter="woodward", bc="periodic")
+    q.tmax, q.tmaxexact = 1.0, 1
+    o = Oracle(q, s.x, s.w)
+    e = Engine(p, s.x, s.w)
+    o.step(10 ** 7)
+    e.step(10 ** 7)
+    ref, got = o.state(), e.state()
+    if precision == abi.PREC_FP64:
+        assert (e.it, e.t) == (o.it, o.t)
+        assert np.array_equal(bits(got), bits(ref))
+    else:
+        assert abs(e.t - 1.0) < 1e-12
+        for iw in range(p.nw):
+            if np.abs(ref[iw]).max() < 1e-3:
+                # m1, zero in the exact solution: the scheme's 1e-4 of it,
+                # within 1e-4 of the wave's amplitude 0.1
+                assert np.abs(got[iw] - ref[iw]).max() < 1e-5, iw
+                continue
+            rel = np.abs(got[iw] - ref[iw]).sum() / np.abs(ref[iw]).sum()
+            assert rel <= MIXED_REL_L1, (iw, rel)
+    for iw in (6, 7):
+        assert np.abs(got[iw] - s.w[iw]).mean() < 2e-4
