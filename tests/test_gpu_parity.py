@@ -438,3 +438,21 @@ def test_alfven_wave_one_period(gpu_lib, precision, oblique):
             assert rel <= MIXED_REL_L1, (iw, rel)
     for iw in (5, 6, 7):
         assert np.abs(got[iw] - s.w[iw]).mean() < (1e-3 if oblique else 2e-4)
+
+
+def test_fast_wave_one_period_fp64(gpu_lib):
+    """The linear fast magnetosonic wave (an eigenmode of linearised ideal
+    MHD) over one period at 64 cells per wavelength: FP64 bit for bit with
+    the oracle, and back at the initial state within the scheme's error."""
+    from tests.test_oracle import fast_wave
+    s, period = fast_wave(64)
+    p = inistate.params_for(s, limiter="woodward", bc="periodic")
+    p.tmax, p.tmaxexact = period, 1
+    o = Oracle(p, s.x, s.w)
+    e = Engine(p, s.x, s.w)
+    o.step(10 ** 7)
+    e.step(10 ** 7)
+    assert (e.it, e.t) == (o.it, o.t)
+    got = e.state()
+    assert np.array_equal(bits(got), bits(o.state()))
+    assert max(np.abs(got[iw] - s.w[iw]).mean() for iw in range(6)) < 3e-3 * 1e-6
