@@ -456,3 +456,33 @@ def test_fast_wave_one_period_fp64(gpu_lib):
     got = e.state()
     assert np.array_equal(bits(got), bits(o.state()))
     assert max(np.abs(got[iw] - s.w[iw]).mean() for iw in range(6)) < 3e-3 * 1e-6
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED], ids=["fp64", "mixed"])
+def test_alfven_wave_3d_one_period(gpu_lib, precision):
+    """The diagonal 3-D Alfven wave over one period (16^3 in FP64, bit for
+    bit with the oracle; 32^3 in mixed precision on the fused pair sweep,
+    within the mixed tolerance of the oracle), each within the scheme's
+    distance from the exact (initial) state."""
+    from tests.test_oracle import alfven_wave_3d
+    n = 16 if precision == abi.PREC_FP64 else 32
+    s = alfven_wave_3d(n)
+    p = inistate.params_for(s, limiter="woodward", bc="periodic", precision=precision)
+    p.tmax, p.tmaxexact = np.sqrt(0.5), 1
+    q = inistate.params_for(s, limiter="woodward", bc="periodic")
+    q.tmax, q.tmaxexact = np.sqrt(0.5), 1
+    o = Oracle(q, s.x, s.w)
+    e = Engine(p, s.x, s.w)
+    o.step(10 ** 7)
+    e.step(10 ** 7)
+    ref, got = o.state(), e.state()
+    if precision == abi.PREC_FP64:
+        assert (e.it, e.t) == (o.it, o.t)
+        assert np.array_equal(bits(got), bits(ref))
+    else:
+        assert abs(e.t - np.sqrt(0.5)) < 1e-12
+        for iw in range(p.nw):
+            rel = np.abs(got[iw] - ref[iw]).sum() / np.abs(ref[iw]).sum()
+            assert rel <= MIXED_REL_L1, (iw, rel)
+    for iw in (5, 6, 7):
+        assert np.abs(got[iw] - s.w[iw]).mean() < (6e-3 if n == 16 else 1.3e-3)
