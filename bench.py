@@ -41,7 +41,7 @@ NW = 8
 def workload_config(prec_name):
     mb = NW * 4 * N ** 3 / 1e6
     return {"workload": "3D ideal MHD TVDLF+woodward %d^3 periodic, random modes "
-                        "(seeded), 100-step config timed per step" % N,
+                        "(seeded), 100-step run timed per step" % N,
             "grid": [N, N, N], "nw": NW, "limiter": "woodward",
             "precision": prec_name,
             "l2": "state > L2 (%.0f MB FP32), no flush needed" % mb if mb > 129
@@ -150,8 +150,8 @@ def cpu_sample(snap, steps, threads):
     return N ** 3 * steps / dt, dt
 
 
-def cpu_serial_config1():
-    """Config 1 in full (Orszag-Tang 200^2, FP64, minmod, 200 steps) by the
+def cpu_serial_ot200():
+    """Orszag-Tang 200^2 in full (FP64, minmod, 200 steps) by the
     FP64 oracle port on one core: VAC itself is serial.  Runs in a child
     process started with OMP_NUM_THREADS=1 (the OpenMP runtime reads it
     once per process)."""
@@ -174,7 +174,7 @@ def cpu_serial_subprocess():
         return {"unavailable": r.stderr.strip().splitlines()[-1] if r.stderr else "failed"}
     d = json.loads(r.stdout.strip().splitlines()[-1])
     return {"value": d["value"], "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "config 1 in full: Orszag-Tang 200^2, FP64, minmod, 200 steps, "
+            "sample": "Orszag-Tang 200^2 in full: FP64, minmod, 200 steps, "
                       "FP64 oracle port on 1 core, %.1f s (VAC is serial)" % d["seconds"]}
 
 
@@ -194,7 +194,7 @@ def sweep_traffic(ncell):
 
 
 def run_batched(args):
-    """Config 3: 64 2-D gamma=1.4 Riemann problems, sides log-uniform in
+    """The batched workload: 64 2-D gamma=1.4 Riemann problems, sides log-uniform in
     [64, 1024], outflow, minmod, mixed precision; all grids advance 50 steps
     in one replay of a CUDA graph of batched persistent-kernel launches."""
     import torch
@@ -264,7 +264,7 @@ def _fresh_timed(params, snap, k, stream, warm):
 def fp64_per_cell_update(key):
     """FP64 operations (key fp64_flops_per_cell_update, DFMA = 2) or FP64
     pipe instructions (fp64_inst_per_cell_update) per cell-update of the
-    plain path (config 2's 3-D MHD step), from the committed ncu record of
+    plain path (the 256^3 3-D MHD step), from the committed ncu record of
     its FP64 instruction counts (profiles/fp64_step_mhd_128.md); None if
     absent."""
     f = os.path.join(ROOT, "profiles", "fp64_step_mhd_128.md")
@@ -276,8 +276,8 @@ def fp64_per_cell_update(key):
 
 
 def run_fp64_c2(args, snap, stream, mixed_value):
-    """Config 2 in plain FP64, and the mixed path's error against it: both
-    precisions advance exactly --acc-steps (the config's 100) steps from the
+    """The 256^3 3-D MHD run in plain FP64, and the mixed path's error against it: both
+    precisions advance exactly --acc-steps (the run's 100) steps from the
     same seeded state; the FP64 run is timed over those steps.  The FP64
     path's own roofline: FP64 FLOP/s against the FP64 pipe's measured
     throughput, and its HBM fraction."""
@@ -337,7 +337,7 @@ def _timed_steps(eng, k, stream):
 
 
 def run_plain(args):
-    """Config 1: the plain FP64 method, 2-D ideal MHD Orszag-Tang on
+    """The plain FP64 method, 2-D ideal MHD Orszag-Tang on
     200^2 periodic cells, minmod, 200 steps (state resident, 2 MB: an L2
     resident latency case, not a roofline case), with the FP64 oracle port
     on the host cores timed on the same run."""
@@ -370,9 +370,9 @@ def run_plain(args):
 
 
 def run_blast(args):
-    """Config 5: 3-D ideal MHD blast on 512^3 cells, outflow ('cont'),
+    """3-D ideal MHD blast on 512^3 cells, outflow ('cont'),
     woodward, B=(1,1,0)/sqrt2, p from 10 to 0.1 across r=0.1.  Mixed and
-    FP64 each advance --blast-steps (the config's 100) steps from the same
+    FP64 each advance --blast-steps (the run's 100) steps from the same
     initial state, timed over those steps; the mixed state's relative L1
     and Linf per variable against the FP64 state after them."""
     from vac_gb300 import abi, inistate
@@ -511,7 +511,7 @@ def random_modes_dev(n, seed, ndim, device, packed=False):
 
 
 def _served_requests(args):
-    """The request stream of config 4 (seeded): kind, side, step count."""
+    """The served request stream (seeded): kind, side, step count."""
     rng = np.random.default_rng(7)
     reqs = []
     for i in range(args.served):
@@ -599,7 +599,7 @@ def run_served_rate(args, reqs, rate, arrivals_seed):
 
 
 def run_served(args, capacity):
-    """Config 4: a Poisson stream of 2-D (128^2..2048^2) and 3-D
+    """The served workload: a Poisson stream of 2-D (128^2..2048^2) and 3-D
     (64^3..256^3) random-mode MHD solves, 20..500 steps each, mixed
     precision, admitted against a 150 GB HBM budget, at offered loads of
     --served-loads times the single-grid capacity (cell-updates/s of the
@@ -714,16 +714,16 @@ def main():
     ap.add_argument("--served-loads", default="0.5,0.9,1.2",
                     help="offered loads of the served stream, in units of the capacity")
     ap.add_argument("--acc-steps", type=int, default=100,
-                    help="steps of config 2's mixed-vs-FP64 accuracy run")
+                    help="steps of the 256^3 mixed-vs-FP64 accuracy run")
     ap.add_argument("--no-serial", action="store_true",
-                    help="skip the 1-core CPU baseline (config 1 in full)")
+                    help="skip the 1-core CPU baseline (Orszag-Tang 200^2 in full)")
     ap.add_argument("--cpu-serial-only", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-only", action="store_true",
-                    help="run config 3 alone and print its JSON object (profiling)")
-    ap.add_argument("--no-plain", action="store_true", help="skip config 1")
+                    help="run the batched workload alone and print its JSON object (profiling)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the Orszag-Tang 200^2 FP64 run")
     ap.add_argument("--blast-side", type=int, default=512,
-                    help="config 5 cells per side (0: skip)")
+                    help="blast run cells per side (0: skip)")
     ap.add_argument("--blast-steps", type=int, default=100)
     ap.add_argument("--tvdmu-side", type=int, default=128,
                     help="cells per side of the tvdmu/Roe case (0: skip)")
@@ -740,7 +740,7 @@ def main():
     args = ap.parse_args()
     N = args.side
     if args.cpu_serial_only:
-        print(json.dumps(cpu_serial_config1()), flush=True)
+        print(json.dumps(cpu_serial_ot200()), flush=True)
         return
     ws, rank, lrank = dist_setup()
     if args.impl == "reference":
@@ -829,7 +829,7 @@ def main():
     e2e_value, e2e_el = whole_job(ws, ncell * K, time.perf_counter() - t0)
     eng2.close()
 
-    # ---- plain FP64 run and the mixed-vs-FP64 error after the config's steps
+    # ---- plain FP64 run and the mixed-vs-FP64 error after the run's steps
     fp64 = None
     if not args.no_fp64 and rank == 0:
         fp64 = run_fp64_c2(args, snap, stream, value / ws)
@@ -879,7 +879,7 @@ def main():
                              "avg_launch_ms": avg_s * 1e3,
                              "alg_bytes_per_launch": alg_bytes,
                              "kernel_share": shares},
-                "fp64": fp64, "plain_fp64_config1": plain, "blast_config5": blast,
+                "fp64": fp64, "plain_fp64_ot200": plain, "blast_512": blast,
                 "tvdmu_roe": tvdmu, "snapshots": snaps,
                 "batched": batched, "served": served,
                 "cpu_baseline": cpu, "cpu_baseline_serial": serial,

@@ -34,7 +34,7 @@ def run_both(s, lim, bc, nsteps, tweak=None, precision=abi.PREC_FP64, src=None):
 
 
 FP64_CASES = [
-    ("ot200-config1", lambda: inistate.orszag_tang(200), "minmod", "periodic", 200, None, None),
+    ("ot200-fp64-200steps", lambda: inistate.orszag_tang(200), "minmod", "periodic", 200, None, None),
     ("ot-woodward", lambda: inistate.orszag_tang(40), "woodward", "periodic", 30, None, None),
     ("rm3-woodward", lambda: inistate.random_modes(20, seed=1), "woodward", "periodic", 8, None, None),
     ("rm3-minmod-xy", lambda: inistate.random_modes(12, seed=2), "minmod", "periodic", 5,

@@ -197,8 +197,8 @@ __device__ __forceinline__ bool grid_sync(GridSync* gs, unsigned nb,
 // written on one SM are read on others through L2 (the control functions,
 // Line2::run and the first-step passes use ld.global.cg), and the rows of
 // the state arrive by cp.async.cg, so no stale L1 line from an earlier step
-// is read.  (HD: four CTAs per SM at 128 registers, with some spilling in
-// the general form, ran config 3 about 3 % faster than three CTAs without.)
+// is read.  (HD: four CTAs per SM at 128 registers; on 64 uneven HD grids
+// that ran about 3 % faster than three CTAs per SM.)
 template <bool MHD, int LIMC, bool GEN>
 __global__ void __launch_bounds__(L2_NT, MHD ? 2 : 4) kb_steps_line2(const Line2Steps ls) {
   constexpr int RF = line2_ring_floats(MHD ? 6 : 4);
