@@ -420,7 +420,8 @@ int vacgpu_batch_download(vacgpu_batch* b, int i, double* w);
  * line-sweep batches where the tuner finds it faster, run as one
  * cooperative launch (itself captured and replayed) with grid-wide barriers
  * between the phases of each step.  The first call tunes the launch shape
- * (VACGPU_TUNE=0 skips tuning).  With 'xyyx' splitting every grid starts a
+ * (VACGPU_TUNE=0 skips tuning; VACGPU_ONELAUNCH=0 leaves the one-launch
+ * form out of the trials, =1 takes it).  With 'xyyx' splitting every grid starts a
  * step with the sweep its own it selects: after a tstop that ended the
  * grids at different parities of it, 2-D batches continue correctly (one
  * launch, per-grid sweep order) and 3-D batches refuse the call. */
